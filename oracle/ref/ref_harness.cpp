@@ -1,0 +1,430 @@
+// Harness that runs aphros's OWN hot-path code (compiled from the reference
+// sources by oracle/ref/Makefile) on inputs read from raw binary files, to
+// pin the C oracle and to make golden fixtures.  Test infrastructure only.
+//
+// Modes (all arrays raw little-endian float64, cells x-fastest, periodic;
+// face arrays hold, for each direction d, the value on the face between
+// cell c-e_d and cell c at the index of c):
+//
+// n and bs are "N" or "NX,NY,NZ"; the domain extent (longest side) is 1.
+//
+//   proj  n bs h dt rho1 rho2 tol maxiter alpha.bin vflux.bin out
+//     rho = CalcMixture formula (kernel/hydro.ipp:1818-1821),
+//     rho_f = UEmbed::InterpolateHarmonic, system = Proj::GetFlux +
+//     Proj::GetFluxSum (solver/proj.ipp:343-383) with the RHS mean removed,
+//     solve with linear::SolverConjugate ("conjugate" module), fluxes by
+//     UEmbed::Eval (proj.ipp:399-403).
+//     Writes out.expr (8N), out.p (N), out.flux (3N), out.info (text).
+//   vof   n bs h dt steps u.bin vflux.bin out
+//     Vof (scheme weymouth) StartStep/MakeIteration/FinishStep/PostStep and
+//     curvature::Heights::CalcCurvature per step, as in
+//     test/advection/main.cpp:242-256.  Writes out.u, out.n (3N AoS),
+//     out.a, out.k (after the last step) and out.sumu (text, per step).
+//   overlap in out         rows (x y z hx hy hz cx cy cz r) -> GetSphereOverlap
+//   reconst in out         rows (n0 n1 n2 u a h0 h1 h2 q dt d) ->
+//                          GetLineA(n,u,h) GetLineU(n,a,h) GetLineFlux(...)
+//   height  in out         rows of 13 -> UHeight::Good
+#include <cmath>
+#include <cstdio>
+#include <cstdlib>
+#include <fstream>
+#include <iostream>
+#include <memory>
+#include <sstream>
+#include <string>
+#include <vector>
+
+#include "distr/distrbasic.h"
+#include "linear/linear.h"
+#include "overlap/overlap.h"
+#include "parse/vof.h"
+#include "solver/approx_eb.h"
+#include "solver/curv.h"
+#include "solver/reconst.h"
+#include "solver/vof.h"
+#include "util/distr.h"
+#include "util/height.h"
+
+using M = MeshCartesian<double, 3>;
+using Scal = typename M::Scal;
+using Vect = typename M::Vect;
+using MIdx = typename M::MIdx;
+using Expr = typename M::Expr;
+using ExprFace = typename M::ExprFace;
+using UEB = UEmbed<M>;
+
+namespace {
+
+std::vector<double> ReadRaw(const std::string& path, size_t count) {
+  std::vector<double> v(count);
+  FILE* f = std::fopen(path.c_str(), "rb");
+  if (!f) {
+    std::cerr << "cannot open " << path << std::endl;
+    std::exit(2);
+  }
+  const size_t got = std::fread(v.data(), sizeof(double), count, f);
+  std::fclose(f);
+  if (got != count) {
+    std::cerr << "short read " << path << std::endl;
+    std::exit(2);
+  }
+  return v;
+}
+
+void WriteRaw(const std::string& path, const std::vector<double>& v) {
+  FILE* f = std::fopen(path.c_str(), "wb");
+  std::fwrite(v.data(), sizeof(double), v.size(), f);
+  std::fclose(f);
+}
+
+struct Global {
+  int n = 0; // unused when nx,ny,nz set
+  int nn[3] = {0, 0, 0};
+  Scal dt = 0, rho1 = 1, rho2 = 1;
+  int steps = 0;
+  std::vector<double> alpha, vflux, u;
+  std::vector<double> out_expr, out_p, out_flux, out_u, out_n, out_a, out_k;
+  std::vector<double> sumu;
+  std::string out;
+  Scal residual = 0;
+  int iter = 0;
+};
+Global g;
+
+size_t Wrap(int i, int n) {
+  return size_t(((i % n) + n) % n);
+}
+size_t GIdx(const MIdx& w) {
+  return Wrap(w[0], g.nn[0]) +
+         size_t(g.nn[0]) *
+             (Wrap(w[1], g.nn[1]) + size_t(g.nn[1]) * Wrap(w[2], g.nn[2]));
+}
+size_t NCells() {
+  return size_t(g.nn[0]) * g.nn[1] * g.nn[2];
+}
+// parses "n" or "nx,ny,nz"
+MIdx ParseSize(const char* s) {
+  int a = 0, b = 0, c = 0;
+  if (std::sscanf(s, "%d,%d,%d", &a, &b, &c) == 3) return MIdx(a, b, c);
+  a = std::atoi(s);
+  return MIdx(a, a, a);
+}
+
+// face value from the global face arrays: direction d, face of cell cp
+template <class MM>
+Scal FaceInput(const MM& m, IdxFace f, const std::vector<double>& arr) {
+  const auto p = m.GetIndexFaces().GetMIdxDir(f);
+  return arr[p.second.raw() * NCells() + GIdx(p.first)];
+}
+
+void RunProj(M& m, Vars& var) {
+  auto sem = m.GetSem(__func__);
+  struct {
+    FieldCell<Scal> fcrho;
+    FieldFace<Scal> ffdens;
+    FieldFace<Scal> ffv;
+    FieldFace<ExprFace> ffe;
+    FieldCell<Expr> fcs;
+    FieldCell<Scal> fcp;
+    Scal sum7;
+    Scal cnt;
+    std::unique_ptr<linear::Solver<M>> solver;
+    typename linear::Solver<M>::Info info;
+  } * ctx(sem);
+  auto& t = *ctx;
+  if (sem("init")) {
+    t.fcrho.Reinit(m);
+    for (auto c : m.AllCells()) {
+      const Scal a2 = g.alpha[GIdx(m.GetIndexCells().GetMIdx(c))];
+      const Scal a1 = 1 - a2;
+      t.fcrho[c] = g.rho1 * a1 + g.rho2 * a2;
+    }
+    t.ffdens = UEB::InterpolateHarmonic(t.fcrho, MapEmbed<BCond<Scal>>(), m);
+    t.ffv.Reinit(m);
+    for (auto f : m.AllFaces()) {
+      t.ffv[f] = FaceInput(m, f, g.vflux);
+    }
+    // Proj::GetFlux (proj.ipp:343-360), periodic: no boundary conditions
+    t.ffe = UEB::GradientImplicit(MapEmbed<BCond<Scal>>(), m);
+    for (auto f : m.Faces()) {
+      t.ffe[f] *= -m.GetArea(f) / t.ffdens[f] * g.dt;
+      t.ffe[f][2] += t.ffv[f];
+    }
+    // Proj::GetFluxSum (proj.ipp:367-383), zero source
+    t.fcs.Reinit(m, Expr::GetUnit(0));
+    for (auto c : m.Cells()) {
+      Expr sum(0);
+      m.LoopNci(c, [&](auto q) {
+        const auto cf = m.GetFace(c, q);
+        const ExprFace v = t.ffe[cf] * m.GetOutwardFactor(c, q);
+        m.AppendExpr(sum, v, q);
+      });
+      t.fcs[c] = sum;
+    }
+    t.sum7 = 0;
+    t.cnt = 0;
+    for (auto c : m.Cells()) {
+      t.sum7 += t.fcs[c].back();
+      t.cnt += 1;
+    }
+    m.Reduce(&t.sum7, Reduction::sum);
+    m.Reduce(&t.cnt, Reduction::sum);
+  }
+  if (sem("mean")) {
+    const Scal mean = t.sum7 / t.cnt;
+    for (auto c : m.Cells()) {
+      t.fcs[c].back() -= mean;
+      const size_t i = GIdx(m.GetIndexCells().GetMIdx(c));
+      for (size_t q = 0; q < 8; ++q) {
+        g.out_expr[8 * i + q] = t.fcs[c][q];
+      }
+    }
+    t.fcp.Reinit(m, 0);
+    auto factory = linear::ModuleLinear<M>::GetInstance("conjugate");
+    fassert(factory, "conjugate solver not found");
+    t.solver = factory->Make(var, "symm", m);
+  }
+  if (sem.Nested("solve")) {
+    t.info = t.solver->Solve(t.fcs, nullptr, t.fcp, m);
+  }
+  if (sem("fluxes")) {
+    for (auto c : m.Cells()) {
+      g.out_p[GIdx(m.GetIndexCells().GetMIdx(c))] = t.fcp[c];
+    }
+    for (auto f : m.Faces()) {
+      const auto p = m.GetIndexFaces().GetMIdxDir(f);
+      const MIdx w = p.first;
+      bool inner = true;
+      for (int d = 0; d < 3; ++d) {
+        if (w[d] < 0 || w[d] >= g.nn[d]) inner = false;
+      }
+      if (!inner) continue;
+      g.out_flux[p.second.raw() * NCells() + GIdx(w)] =
+          UEB::Eval(t.ffe[f], f, t.fcp, m);
+    }
+    if (m.IsRoot()) {
+      g.residual = t.info.residual;
+      g.iter = t.info.iter;
+    }
+  }
+  if (sem()) {
+  }
+}
+
+void RunVof(M& m, Vars& var) {
+  auto sem = m.GetSem(__func__);
+  struct {
+    FieldCell<Scal> fcu;
+    FieldEmbed<Scal> ffv;
+    FieldCell<Scal> fcsrc;
+    MapEmbed<BCondAdvection<Scal>> bc; // empty: periodic (Vof keeps a reference)
+    std::unique_ptr<Vof<M>> as;
+    Multi<FieldCell<Scal>> fck;
+    std::unique_ptr<curvature::Estimator<M>> curv;
+    GRange<size_t> layers;
+    int step = 0;
+    Scal sumu;
+  } * ctx(sem);
+  auto& t = *ctx;
+  if (sem("init")) {
+    t.fcu.Reinit(m);
+    for (auto c : m.AllCells()) {
+      t.fcu[c] = g.u[GIdx(m.GetIndexCells().GetMIdx(c))];
+    }
+    t.ffv.Reinit(m, 0);
+    for (auto f : m.AllFaces()) {
+      t.ffv[f] = FaceInput(m, f, g.vflux);
+    }
+    t.fcsrc.Reinit(m, 0.);
+    VofPar<M> par; // defaults: weymouth, clipth 1e-10, dim 3 (solver/vof.h:13-53)
+    (void)var;
+    const FieldCell<Scal> fccl(m, 0);
+    t.as.reset(new Vof<M>(
+        m, m, t.fcu, fccl, t.bc, &t.ffv, &t.fcsrc,
+        0., g.dt, par));
+    t.layers = GRange<size_t>(1);
+    t.fck.resize(t.layers);
+    t.fck.InitAll(FieldCell<Scal>(m, GetNan<Scal>()));
+    t.curv = std::make_unique<curvature::Heights<M>>();
+  }
+  sem.LoopBegin();
+  if (sem("empty")) {
+    // an empty first stage in the loop, as test/advection/main.cpp:218-220
+  }
+  if (sem("check")) {
+    if (t.step >= g.steps) {
+      sem.LoopBreak();
+    }
+  }
+  if (sem.Nested("start")) {
+    t.as->StartStep();
+  }
+  if (sem.Nested("iter")) {
+    t.as->MakeIteration();
+  }
+  if (sem.Nested("finish")) {
+    t.as->FinishStep();
+  }
+  if (sem.Nested("post")) {
+    t.as->PostStep();
+  }
+  if (sem.Nested("curv")) {
+    t.curv->CalcCurvature(t.fck, t.as->GetPlic(), m, m);
+  }
+  if (sem("stat")) {
+    t.sumu = 0;
+    auto& u = t.as->GetField();
+    for (auto c : m.Cells()) {
+      t.sumu += u[c] * m.GetVolume(c);
+    }
+    m.Reduce(&t.sumu, Reduction::sum);
+  }
+  if (sem("stat2")) {
+    if (m.IsRoot()) {
+      g.sumu.push_back(t.sumu);
+    }
+    ++t.step;
+  }
+  sem.LoopEnd();
+  if (sem("out")) {
+    auto& u = t.as->GetField();
+    auto& a = t.as->GetAlpha();
+    auto& nn = t.as->GetNormal();
+    for (auto c : m.Cells()) {
+      const size_t i = GIdx(m.GetIndexCells().GetMIdx(c));
+      g.out_u[i] = u[c];
+      g.out_a[i] = a[c];
+      g.out_k[i] = t.fck[0][c];
+      for (int d = 0; d < 3; ++d) {
+        g.out_n[3 * i + d] = nn[c][d];
+      }
+    }
+  }
+  if (sem()) {
+  }
+}
+
+std::string MeshConf(MIdx n, MIdx bs) {
+  Subdomains<MIdx> sub(n, bs, 1);
+  std::string conf = sub.GetConfig();
+  conf += "\nset string backend local";
+  conf += "\nset double extent " + std::to_string(1.0);
+  return conf;
+}
+
+int Main(int argc, const char** argv) {
+  if (argc < 2) {
+    std::cerr << "usage: ref_harness MODE ..." << std::endl;
+    return 1;
+  }
+  const std::string mode = argv[1];
+  if (mode == "proj") {
+    if (argc != 13) return 1;
+    const MIdx nsz = ParseSize(argv[2]);
+    for (int d = 0; d < 3; ++d) g.nn[d] = nsz[d];
+    const MIdx bs = ParseSize(argv[3]);
+    const double h = std::atof(argv[4]);
+    (void)h;
+    g.dt = std::atof(argv[5]);
+    g.rho1 = std::atof(argv[6]);
+    g.rho2 = std::atof(argv[7]);
+    const std::string tol = argv[8];
+    const std::string maxiter = argv[9];
+    g.alpha = ReadRaw(argv[10], NCells());
+    g.vflux = ReadRaw(argv[11], 3 * NCells());
+    g.out = argv[12];
+    g.out_expr.assign(8 * NCells(), 0);
+    g.out_p.assign(NCells(), 0);
+    g.out_flux.assign(3 * NCells(), 0);
+    std::string conf = MeshConf(nsz, bs);
+    conf += "\nset double hypre_symm_tol " + tol;
+    conf += "\nset int hypre_symm_maxiter " + maxiter;
+    conf += "\nset int linsolver_symm_maxnorm 0";
+    MpiWrapper mpi(&argc, &argv);
+    int r = RunMpiBasicString<M>(mpi, RunProj, conf);
+    return r;
+  }
+  if (mode == "vof") {
+    if (argc != 10) return 1;
+    const MIdx nsz = ParseSize(argv[2]);
+    for (int d = 0; d < 3; ++d) g.nn[d] = nsz[d];
+    const MIdx bs = ParseSize(argv[3]);
+    (void)std::atof(argv[4]);
+    g.dt = std::atof(argv[5]);
+    g.steps = std::atoi(argv[6]);
+    g.u = ReadRaw(argv[7], NCells());
+    g.vflux = ReadRaw(argv[8], 3 * NCells());
+    g.out = argv[9];
+    g.out_u.assign(NCells(), 0);
+    g.out_a.assign(NCells(), 0);
+    g.out_k.assign(NCells(), 0);
+    g.out_n.assign(3 * NCells(), 0);
+    std::string conf = MeshConf(nsz, bs);
+    conf += "\nset string vof_scheme weymouth";
+    conf += "\nset double vof_clipth 1e-10";
+    if (std::getenv("REF_VERBOSE")) conf += "\nset int verbose_stages 1";
+    MpiWrapper mpi(&argc, &argv);
+    return RunMpiBasicString<M>(mpi, RunVof, conf);
+  }
+  return 1;
+}
+
+int Table(const std::string& mode, const char* in, const char* out) {
+  std::ifstream fi(in);
+  std::ofstream fo(out);
+  fo.precision(17);
+  std::string line;
+  using R = Reconst<Scal>;
+  while (std::getline(fi, line)) {
+    std::istringstream s(line);
+    if (mode == "overlap") {
+      double v[10];
+      for (auto& x : v) s >> x;
+      fo << GetSphereOverlap(
+                Vect(v[0], v[1], v[2]), Vect(v[3], v[4], v[5]),
+                Vect(v[6], v[7], v[8]), v[9])
+         << "\n";
+    } else if (mode == "reconst") {
+      double v[11];
+      for (auto& x : v) s >> x;
+      const Vect n(v[0], v[1], v[2]);
+      const Vect h(v[5], v[6], v[7]);
+      fo << R::GetLineA(n, v[3], h) << " " << R::GetLineU(n, v[4], h) << " "
+         << R::GetLineFlux(n, v[4], h, v[8], v[9], size_t(v[10])) << "\n";
+    } else if (mode == "height") {
+      std::vector<double> uu(13);
+      for (auto& x : uu) s >> x;
+      fo << UHeight<Scal>::Good(uu) << "\n";
+    }
+  }
+  return 0;
+}
+
+} // namespace
+
+int main(int argc, const char** argv) {
+  const std::string mode = argc > 1 ? argv[1] : "";
+  if (mode == "overlap" || mode == "reconst" || mode == "height") {
+    if (argc != 4) return 1;
+    return Table(mode, argv[2], argv[3]);
+  }
+  const int r = Main(argc, argv);
+  if (r != 0) return r;
+  if (mode == "proj") {
+    WriteRaw(g.out + ".expr", g.out_expr);
+    WriteRaw(g.out + ".p", g.out_p);
+    WriteRaw(g.out + ".flux", g.out_flux);
+    std::ofstream fo(g.out + ".info");
+    fo.precision(17);
+    fo << g.residual << " " << g.iter << "\n";
+  } else if (mode == "vof") {
+    WriteRaw(g.out + ".u", g.out_u);
+    WriteRaw(g.out + ".n", g.out_n);
+    WriteRaw(g.out + ".a", g.out_a);
+    WriteRaw(g.out + ".k", g.out_k);
+    std::ofstream fo(g.out + ".sumu");
+    fo.precision(17);
+    for (auto s : g.sumu) fo << s << "\n";
+  }
+  return 0;
+}
