@@ -1,0 +1,282 @@
+"""ctypes binding of libaphgpu (include/aphgpu.h).
+
+The CUDA library is the only implementation: if it is missing or cannot be
+loaded this module raises, there is no fallback.
+"""
+import ctypes
+import os
+
+import numpy as np
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(_HERE, "_build", "libaphgpu.so")
+
+OK = 0
+ERR_ARG = 1
+ERR_CUDA = 2
+ERR_NOMEM = 3
+ERR_NOT_SYMMETRIC = 4
+ERR_STATE = 5
+ERR_UNSUPPORTED = 6
+
+K_SMOOTH32, K_SMOOTH64, K_APPLY64, K_APPLY32, K_RESTRICT32 = 0, 1, 2, 3, 4
+K_VOF_FLUX, K_VOF_UPDATE, K_RECONSTRUCT, K_HEIGHTS, K_CURVATURE = 5, 6, 7, 8, 9
+KERNEL_NAMES = {0: "KSmooth<float>", 1: "KSmooth<double>", 2: "KPcgApply<double>",
+                3: "KPcgApply<float>", 4: "KResidualRestrict<float>",
+                5: "KSweepFlux", 6: "KSweepUpdate", 7: "KReconstruct",
+                8: "KHeights", 9: "KCurvature"}
+
+SOLVER_CG = 0
+SOLVER_MGPCG = 1
+SOLVER_MIXED = 2
+
+_D = ctypes.c_double
+_I = ctypes.c_int
+_P = ctypes.c_void_p
+_PD = ctypes.POINTER(ctypes.c_double)
+
+
+class Conf(ctypes.Structure):
+    _fields_ = [
+        ("solver", _I), ("tol", _D), ("miniter", _I), ("maxiter", _I),
+        ("maxnorm", _I), ("mg_pre", _I), ("mg_post", _I),
+        ("mg_coarse_max", _I), ("inner_rtol", _D), ("inner_maxiter", _I),
+    ]
+
+
+class Info(ctypes.Structure):
+    _fields_ = [("residual", _D), ("iter", _I), ("inner_iter", _I),
+                ("converged", _I)]
+
+
+class AphgpuError(RuntimeError):
+    def __init__(self, code, msg):
+        super().__init__("aphgpu error %d: %s" % (code, msg))
+        self.code = code
+
+
+_lib = None
+
+
+def lib():
+    """Loads libaphgpu.so (raises if it has not been built)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(LIB_PATH):
+        raise ImportError(
+            "libaphgpu.so not found at %s: build it with "
+            "`python -m aphros_gb300.build`" % LIB_PATH)
+    L = ctypes.CDLL(LIB_PATH)
+    L.aphgpu_conf_default.argtypes = [ctypes.POINTER(Conf)]
+    L.aphgpu_conf_default.restype = None
+    L.aphgpu_create.argtypes = [ctypes.POINTER(_P), _I, _I, _I, _D, _I]
+    L.aphgpu_destroy.argtypes = [_P]
+    L.aphgpu_destroy.restype = None
+    L.aphgpu_last_error.argtypes = [_P]
+    L.aphgpu_last_error.restype = ctypes.c_char_p
+    L.aphgpu_device_bytes.argtypes = [_P]
+    L.aphgpu_device_bytes.restype = ctypes.c_int64
+    L.aphgpu_sync.argtypes = [_P]
+    L.aphgpu_set_system_expr.argtypes = [_P, _P]
+    L.aphgpu_get_system_expr.argtypes = [_P, _P]
+    L.aphgpu_assemble_projection.argtypes = [_P, _P, _D, _D, _P, _P, _D, _I]
+    L.aphgpu_solve.argtypes = [_P, ctypes.POINTER(Conf), _P, _P, ctypes.POINTER(Info)]
+    L.aphgpu_solve_resident.argtypes = [_P, ctypes.POINTER(Conf), _I, ctypes.POINTER(Info)]
+    L.aphgpu_get_solution.argtypes = [_P, _P]
+    L.aphgpu_residual_norms.argtypes = [_P, _PD, _PD]
+    L.aphgpu_flux_correct.argtypes = [_P, _P]
+    L.aphgpu_acceleration.argtypes = [_P, _P]
+    L.aphgpu_vof_init.argtypes = [_P, _P, _D]
+    L.aphgpu_vof_step.argtypes = [_P, _P, _D]
+    L.aphgpu_vof_get.argtypes = [_P, _P, _P, _P, _P]
+    L.aphgpu_curvature.argtypes = [_P, _P, _P]
+    L.aphgpu_surface_tension.argtypes = [_P, _D, _P]
+    L.aphgpu_set_force_resident.argtypes = [_P, _I]
+    L.aphgpu_last_timing.argtypes = [_P, _PD, ctypes.POINTER(ctypes.c_int64)]
+    L.aphgpu_mark.argtypes = [_P, _I]
+    L.aphgpu_elapsed.argtypes = [_P, _I, _I, _PD]
+    L.aphgpu_time_kernel.argtypes = [_P, _I, _I, _PD, _PD]
+    for name in ("aphgpu_create", "aphgpu_sync", "aphgpu_set_system_expr",
+                 "aphgpu_get_system_expr",
+                 "aphgpu_assemble_projection", "aphgpu_solve",
+                 "aphgpu_solve_resident", "aphgpu_get_solution",
+                 "aphgpu_residual_norms", "aphgpu_flux_correct",
+                 "aphgpu_acceleration", "aphgpu_vof_init", "aphgpu_vof_step",
+                 "aphgpu_vof_get", "aphgpu_curvature", "aphgpu_surface_tension",
+                 "aphgpu_set_force_resident", "aphgpu_last_timing",
+                 "aphgpu_mark", "aphgpu_elapsed", "aphgpu_time_kernel"):
+        getattr(L, name).restype = _I
+    _lib = L
+    return L
+
+
+def ptr(a):
+    """Pointer of a C-contiguous numpy array (or None)."""
+    if a is None:
+        return None
+    assert a.flags["C_CONTIGUOUS"], "array must be C-contiguous"
+    return a.ctypes.data_as(_P)
+
+
+def default_conf(**kw):
+    c = Conf()
+    lib().aphgpu_conf_default(ctypes.byref(c))
+    for k, v in kw.items():
+        setattr(c, k, v)
+    return c
+
+
+class Context:
+    """One periodic nx*ny*nz domain resident on one GPU (aphgpu_ctx)."""
+
+    def __init__(self, n, h, device=0):
+        if isinstance(n, int):
+            n = (n, n, n)
+        self.n = tuple(int(v) for v in n)
+        self.h = float(h)
+        self.N = self.n[0] * self.n[1] * self.n[2]
+        self._L = lib()
+        p = _P()
+        rc = self._L.aphgpu_create(ctypes.byref(p), self.n[0], self.n[1],
+                                   self.n[2], self.h, device)
+        if rc != OK:
+            raise AphgpuError(rc, "aphgpu_create failed")
+        self._p = p
+
+    def close(self):
+        if getattr(self, "_p", None):
+            self._L.aphgpu_destroy(self._p)
+            self._p = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    @property
+    def handle(self):
+        return self._p
+
+    def _check(self, rc):
+        if rc != OK:
+            msg = self._L.aphgpu_last_error(self._p)
+            raise AphgpuError(rc, msg.decode() if msg else "")
+
+    def _f64(self, a, count):
+        a = np.ascontiguousarray(a, dtype=np.float64)
+        assert a.size == count, "expected %d values, got %d" % (count, a.size)
+        return a
+
+    # ---- Poisson ----
+    def set_system_expr(self, expr8):
+        e = self._f64(expr8, 8 * self.N)
+        self._check(self._L.aphgpu_set_system_expr(self._p, ptr(e)))
+
+    def get_system_expr(self):
+        e = np.empty(8 * self.N)
+        self._check(self._L.aphgpu_get_system_expr(self._p, ptr(e)))
+        return e
+
+    def assemble_projection(self, alpha, rho1, rho2, vflux, dt, febp=None,
+                            remove_mean=True):
+        a = None if alpha is None else self._f64(alpha, self.N)
+        v = self._f64(vflux, 3 * self.N)
+        f = None if febp is None else self._f64(febp, 3 * self.N)
+        self._check(self._L.aphgpu_assemble_projection(
+            self._p, ptr(a), rho1, rho2, ptr(v), ptr(f), dt, int(remove_mean)))
+
+    def solve(self, conf, x0=None, out=True):
+        info = Info()
+        x = np.empty(self.N) if out else None
+        xi = None if x0 is None else self._f64(x0, self.N)
+        self._check(self._L.aphgpu_solve(self._p, ctypes.byref(conf), ptr(xi),
+                                         ptr(x), ctypes.byref(info)))
+        return x, info
+
+    def solve_resident(self, conf, zero_guess=True):
+        info = Info()
+        self._check(self._L.aphgpu_solve_resident(self._p, ctypes.byref(conf),
+                                                  int(zero_guess), ctypes.byref(info)))
+        return info
+
+    def get_solution(self):
+        x = np.empty(self.N)
+        self._check(self._L.aphgpu_get_solution(self._p, ptr(x)))
+        return x
+
+    def residual_norms(self):
+        r, b = _D(), _D()
+        self._check(self._L.aphgpu_residual_norms(self._p, ctypes.byref(r), ctypes.byref(b)))
+        return r.value, b.value
+
+    def flux_correct(self, out=True):
+        v = np.empty(3 * self.N) if out else None
+        self._check(self._L.aphgpu_flux_correct(self._p, ptr(v)))
+        return v
+
+    def acceleration(self):
+        a = np.empty(3 * self.N)
+        self._check(self._L.aphgpu_acceleration(self._p, ptr(a)))
+        return a
+
+    # ---- VOF ----
+    def vof_init(self, alpha, clipth=1e-10):
+        a = self._f64(alpha, self.N)
+        self._check(self._L.aphgpu_vof_init(self._p, ptr(a), clipth))
+
+    def vof_step(self, vflux, dt):
+        v = None if vflux is None else self._f64(vflux, 3 * self.N)
+        self._check(self._L.aphgpu_vof_step(self._p, ptr(v), dt))
+
+    def vof_get(self):
+        u = np.empty(self.N)
+        nrm = np.empty(3 * self.N)
+        a = np.empty(self.N)
+        m = np.empty(self.N, dtype=np.uint8)
+        self._check(self._L.aphgpu_vof_get(self._p, ptr(u), ptr(nrm), ptr(a), ptr(m)))
+        return u, nrm, a, m
+
+    def curvature(self, heights=False):
+        k = np.empty(self.N)
+        hg = np.empty(3 * self.N) if heights else None
+        self._check(self._L.aphgpu_curvature(self._p, ptr(k), ptr(hg)))
+        return (k, hg) if heights else k
+
+    def surface_tension(self, sigma, out=True):
+        f = np.empty(3 * self.N) if out else None
+        self._check(self._L.aphgpu_surface_tension(self._p, sigma, ptr(f)))
+        return f
+
+    def set_force_resident(self, on=True):
+        self._check(self._L.aphgpu_set_force_resident(self._p, int(on)))
+
+    def last_timing(self):
+        ms = _D()
+        n = ctypes.c_int64()
+        self._check(self._L.aphgpu_last_timing(self._p, ctypes.byref(ms), ctypes.byref(n)))
+        return ms.value, n.value
+
+    def mark(self, slot):
+        self._check(self._L.aphgpu_mark(self._p, slot))
+
+    def elapsed(self, s0, s1):
+        ms = _D()
+        self._check(self._L.aphgpu_elapsed(self._p, s0, s1, ctypes.byref(ms)))
+        return ms.value
+
+    def time_kernel(self, kernel, reps=10):
+        ms, b = _D(), _D()
+        self._check(self._L.aphgpu_time_kernel(self._p, kernel, reps, ctypes.byref(ms),
+                                               ctypes.byref(b)))
+        return ms.value, b.value
+
+    def device_bytes(self):
+        return int(self._L.aphgpu_device_bytes(self._p))

@@ -1,0 +1,351 @@
+// Internal definitions shared by the aphgpu translation units.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <cstdarg>
+#include <cstdio>
+#include <string>
+#include <vector>
+
+#include "aphgpu.h"
+
+namespace aphgpu {
+
+// ---------------------------------------------------------------------------
+// Grid geometry
+// ---------------------------------------------------------------------------
+
+struct Dims {
+  int nx, ny, nz;
+  __host__ __device__ int64_t cells() const {
+    return (int64_t)nx * ny * nz;
+  }
+  __host__ __device__ int64_t idx(int i, int j, int k) const {
+    return (int64_t)i + (int64_t)nx * ((int64_t)j + (int64_t)ny * k);
+  }
+};
+
+__device__ __forceinline__ int wrapm(int i, int n) {
+  return i < 0 ? i + n : i;
+}
+__device__ __forceinline__ int wrapp(int i, int n) {
+  return i >= n ? i - n : i;
+}
+__device__ __forceinline__ int wrapi(int i, int n) {
+  return i < 0 ? i + n : (i >= n ? i - n : i);
+}
+
+// Stencil tiles: a CTA of kTileX*kTileY threads owns an x-y tile and
+// marches over kTileZ planes in z.
+constexpr int kTileX = 32;
+constexpr int kTileY = 8;
+constexpr int kTileZ = 8;
+
+inline dim3 TileGrid(const Dims& d) {
+  return dim3((d.nx + kTileX - 1) / kTileX, (d.ny + kTileY - 1) / kTileY,
+              (d.nz + kTileZ - 1) / kTileZ);
+}
+inline dim3 TileBlock() {
+  return dim3(kTileX, kTileY, 1);
+}
+inline int64_t TileCount(const Dims& d) {
+  const dim3 g = TileGrid(d);
+  return (int64_t)g.x * g.y * g.z;
+}
+
+// Flat kernels: fixed-size grid (a multiple of the SM count) with a
+// grid-stride loop.
+constexpr int kFlatThreads = 256;
+int FlatBlocks(int64_t n);
+
+// ---------------------------------------------------------------------------
+// Deterministic grid-wide reductions.
+//
+// Each CTA reduces its values (warp shuffles, then shared memory), writes
+// one partial per value, and the last CTA to arrive (atomic ticket) sums the
+// partials in a fixed order.  The result does not depend on CTA scheduling,
+// so repeated solves are bit-identical.
+// ---------------------------------------------------------------------------
+
+struct RedBuf {
+  double* part;        // [kMaxRedVals][max_blocks]
+  unsigned int* ticket;
+  int max_blocks;
+};
+constexpr int kMaxRedVals = 4;
+
+// op: 0 = sum, 1 = max
+template <int NV>
+__device__ __forceinline__ void WarpReduce(double (&v)[NV], const int (&op)[NV]) {
+#pragma unroll
+  for (int q = 0; q < NV; ++q) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+      const double w = __shfl_down_sync(0xffffffffu, v[q], o);
+      v[q] = op[q] ? fmax(v[q], w) : v[q] + w;
+    }
+  }
+}
+
+// Returns true in all threads of the last CTA; `out[q]` then holds the
+// grid-wide result (visible to that CTA after the call).  nthreads: threads
+// per CTA (multiple of 32, <= 1024).  The CTA index is linearised over a
+// 3-D grid.
+template <int NV>
+__device__ bool GridReduce(double (&v)[NV], const int (&op)[NV], RedBuf rb,
+                           double* out) {
+  __shared__ double sm[32][NV];
+  __shared__ bool last;
+  const int tid = threadIdx.x + blockDim.x * (threadIdx.y + blockDim.y * threadIdx.z);
+  const int nthreads = blockDim.x * blockDim.y * blockDim.z;
+  const int bid = blockIdx.x + gridDim.x * (blockIdx.y + gridDim.y * blockIdx.z);
+  const int nblocks = gridDim.x * gridDim.y * gridDim.z;
+  WarpReduce<NV>(v, op);
+  const int lane = tid & 31, warp = tid >> 5;
+  if (lane == 0) {
+#pragma unroll
+    for (int q = 0; q < NV; ++q) sm[warp][q] = v[q];
+  }
+  __syncthreads();
+  if (warp == 0) {
+    const int nw = nthreads >> 5;
+#pragma unroll
+    for (int q = 0; q < NV; ++q) v[q] = lane < nw ? sm[lane][q] : (op[q] ? -1e308 : 0.0);
+    WarpReduce<NV>(v, op);
+    if (lane == 0) {
+#pragma unroll
+      for (int q = 0; q < NV; ++q) rb.part[q * rb.max_blocks + bid] = v[q];
+      __threadfence();
+      const unsigned t = atomicAdd(rb.ticket, 1u);
+      last = (t == (unsigned)nblocks - 1);
+    }
+  }
+  __syncthreads();
+  if (!last) return false;
+  __threadfence();
+  // last CTA: ordered reduction of the partials
+  double a[NV];
+#pragma unroll
+  for (int q = 0; q < NV; ++q) a[q] = op[q] ? -1e308 : 0.0;
+  for (int b = tid; b < nblocks; b += nthreads) {
+#pragma unroll
+    for (int q = 0; q < NV; ++q) {
+      const double w = ((volatile double*)rb.part)[q * rb.max_blocks + b];
+      a[q] = op[q] ? fmax(a[q], w) : a[q] + w;
+    }
+  }
+  WarpReduce<NV>(a, op);
+  if (lane == 0) {
+#pragma unroll
+    for (int q = 0; q < NV; ++q) sm[warp][q] = a[q];
+  }
+  __syncthreads();
+  if (tid == 0) {
+    const int nw = nthreads >> 5;
+#pragma unroll
+    for (int q = 0; q < NV; ++q) {
+      double s = sm[0][q];
+      for (int w = 1; w < nw; ++w) s = op[q] ? fmax(s, sm[w][q]) : s + sm[w][q];
+      out[q] = s;
+    }
+    *rb.ticket = 0;
+    __threadfence();
+  }
+  __syncthreads();
+  return true;
+}
+
+}  // namespace aphgpu
+
+// ---------------------------------------------------------------------------
+// Context
+// ---------------------------------------------------------------------------
+
+namespace aphgpu {
+
+// Scalars of an iterative solve, resident on the device so that the
+// iteration loop never waits for the host.
+struct SolveScalars {
+  double rr;        // r.r after the last update
+  double rr_prev;   // r.r before it
+  double pap;       // p.Ap
+  double rz;        // r.z (preconditioned)
+  double rz_prev;
+  double maxr;      // max |r|
+  double alpha, beta;
+  double residual;  // reported residual (norm of linear.ipp:102-114)
+  double tol;
+  double cellvol;
+  double res_scale; // multiplies the residual (inner solves)
+  double tmp[4];
+  int iter;
+  int miniter, maxiter, maxnorm;
+  int done;
+  int converged;
+  int pad[2];
+};
+
+template <class T>
+struct Level {
+  Dims d;
+  T* w[3];       // coupling to the minus neighbour in x, y, z (e[1], e[3], e[5])
+  T* invdiag;    // 1 / diagonal
+  T* diag;       // diagonal array (may be unused, see has_diag)
+  bool has_diag; // false: diagonal = -(sum of the six couplings)
+  T* x;          // iterate / correction
+  T* b;          // right-hand side
+  T* r;          // residual scratch
+};
+
+struct Multigrid {
+  int nlevels = 0;
+  std::vector<Level<double>> l64;  // level 0 aliases the fine system
+  std::vector<Level<float>> l32;
+  bool built64 = false, built32 = false;
+  // coarsest-level CG scratch (FP64)
+  double* cr = nullptr;
+  double* cp = nullptr;
+  double* cap = nullptr;
+  double* cx = nullptr;
+  double* cb = nullptr;
+};
+
+}  // namespace aphgpu
+
+struct aphgpu_ctx {
+  int device = 0;
+  aphgpu::Dims d{0, 0, 0};
+  int64_t N = 0;
+  double h = 0;
+  cudaStream_t stream = nullptr;
+  std::string err;
+  int64_t bytes = 0;
+  std::vector<void*> allocs;
+
+  // fine FP64 system: e1,e3,e5 of each cell, explicit diagonal when the
+  // system is not a pure flux-difference operator, b = -e7
+  double* w[3] = {nullptr, nullptr, nullptr};
+  double* diag = nullptr;      // NULL: diagonal = -(e1+...+e6) in order
+  bool diag_explicit = false;
+  double* invdiag = nullptr;   // 1/diagonal (multigrid smoother)
+  double* b = nullptr;
+  bool has_system = false;
+  double* e8 = nullptr;        // staging of aphgpu_set_system_expr (8N)
+
+  // projection: predicted fluxes with force (face blocks), resident force
+  double* vstar = nullptr;     // 3N
+  double* febp = nullptr;      // 3N
+  bool has_proj = false;
+  bool force_resident = false;
+  bool proj_force = false;     // the last assembly included a face force
+  double proj_rho[2] = {1, 1}; // rho1, rho2 of the last assembly
+  double* alpha_proj = nullptr;  // volume fraction of the last assembly
+
+  // solver vectors
+  double* x = nullptr;
+  double* r = nullptr;
+  double* p = nullptr;
+  double* ap = nullptr;
+  double* z = nullptr;
+  float* r32 = nullptr;
+  float* x32 = nullptr;        // inner correction
+  float* p32 = nullptr;
+  float* ap32 = nullptr;
+  float* z32 = nullptr;
+  float* rr32 = nullptr;       // inner residual
+  aphgpu::SolveScalars* scal = nullptr;   // outer
+  aphgpu::SolveScalars* scal2 = nullptr;  // inner
+  aphgpu::SolveScalars* hscal = nullptr;  // pinned host copy
+  aphgpu::RedBuf red{nullptr, nullptr, 0};
+  unsigned int* flags = nullptr;  // 4 counters for validation kernels
+  aphgpu::Multigrid mg;
+
+  // VOF state
+  double* u = nullptr;
+  double* u0 = nullptr;
+  double* nrm = nullptr;       // 3N AoS
+  double* pa = nullptr;        // plane constant
+  double* ffvu = nullptr;      // N, fluid flux of one direction
+  double* vflux_res = nullptr; // 3N resident corrected fluxes
+  bool has_vflux_res = false;
+  double* kappa = nullptr;
+  double* hgt = nullptr;       // 3N AoS
+  double clipth = 1e-10;
+  int vof_count = 0;
+  bool vof_ready = false;
+
+  // host staging (pinned)
+  void* pinned = nullptr;
+  size_t pinned_bytes = 0;
+
+  // timing
+  cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+  cudaEvent_t ev_slot[2] = {nullptr, nullptr};
+  cudaEvent_t marks[8] = {nullptr, nullptr, nullptr, nullptr,
+                          nullptr, nullptr, nullptr, nullptr};
+  double last_ms = 0;
+  int64_t last_launches = 0;
+  int64_t launches = 0;
+};
+
+namespace aphgpu {
+
+int SetError(aphgpu_ctx* ctx, int code, const char* fmt, ...);
+int CheckCuda(aphgpu_ctx* ctx, cudaError_t e, const char* what);
+template <class T>
+int Alloc(aphgpu_ctx* ctx, T** p, int64_t count) {
+  void* q = nullptr;
+  const size_t bytes = sizeof(T) * (size_t)(count > 0 ? count : 1);
+  const cudaError_t e = cudaMalloc(&q, bytes);
+  if (e != cudaSuccess) {
+    cudaGetLastError();
+    return SetError(ctx, APHGPU_ERR_NOMEM, "cudaMalloc of %zu bytes failed: %s",
+                    bytes, cudaGetErrorString(e));
+  }
+  ctx->allocs.push_back(q);
+  ctx->bytes += (int64_t)bytes;
+  *p = (T*)q;
+  return APHGPU_OK;
+}
+// Pinned host staging buffer of at least `bytes`.
+int Staging(aphgpu_ctx* ctx, size_t bytes, void** out);
+
+#define APH_TRY(expr)          \
+  do {                         \
+    const int rc_ = (expr);    \
+    if (rc_ != APHGPU_OK) return rc_; \
+  } while (0)
+#define APH_CUDA(ctx, expr) APH_TRY(::aphgpu::CheckCuda((ctx), (expr), #expr))
+#define APH_LAUNCHED(ctx)                                                \
+  do {                                                                   \
+    ++(ctx)->launches;                                                   \
+    const cudaError_t le_ = cudaGetLastError();                          \
+    if (le_ != cudaSuccess) return ::aphgpu::CheckCuda((ctx), le_, "kernel launch"); \
+  } while (0)
+
+// poisson.cu
+int EnsureSolverVectors(aphgpu_ctx* ctx);
+int SolveCG(aphgpu_ctx* ctx, const aphgpu_conf* conf, aphgpu_info* info);
+int SolveMGPCG(aphgpu_ctx* ctx, const aphgpu_conf* conf, aphgpu_info* info);
+int SolveMixed(aphgpu_ctx* ctx, const aphgpu_conf* conf, aphgpu_info* info);
+int SetSystemExprDevice(aphgpu_ctx* ctx, const double* d_expr8);
+int AssembleProjectionDevice(aphgpu_ctx* ctx, const double* d_alpha,
+                             double rho1, double rho2, const double* d_vflux,
+                             const double* d_febp, double dt, int remove_mean);
+int ResidualNorms(aphgpu_ctx* ctx, double* rnorm, double* bnorm);
+int SystemToExprDevice(aphgpu_ctx* ctx, double* d_e8);
+int FluxCorrect(aphgpu_ctx* ctx, double* d_out);
+int Acceleration(aphgpu_ctx* ctx, double* d_acc, const double* d_alpha,
+                 double rho1, double rho2);
+// vof.cu
+int VofReconstruct(aphgpu_ctx* ctx);
+int VofStepDevice(aphgpu_ctx* ctx, const double* d_vflux, double dt);
+int CurvatureDevice(aphgpu_ctx* ctx);
+int SurfaceTensionDevice(aphgpu_ctx* ctx, double sigma, double* d_febp);
+int TimeVofKernel(aphgpu_ctx* ctx, int kernel, int reps, double* ms, double* bytes,
+                  const double* d_vflux, double dt);
+int TimeSolverKernel(aphgpu_ctx* ctx, int kernel, int reps, double* ms, double* bytes);
+
+}  // namespace aphgpu

@@ -1,0 +1,1329 @@
+// Pressure Poisson solve of the projection step on one GB300.
+//
+// System storage (per cell, x-fastest, periodic):
+//   w[d][c]  = e[1+2d] of aphros's Expr: coupling of cell c to its minus
+//              neighbour in direction d.  The plus coupling e[2+2d] of c is
+//              w[d][c+e_d] (symmetric systems only).
+//   diag[c]  = e[0] when it differs from -(e1+...+e6); otherwise the
+//              diagonal is recomputed on the fly in the same order as
+//              GetFluxSum accumulates it (src/solver/proj.ipp:367-383).
+//   b[c]     = -e[7].
+// 24 B/cell of operator instead of the 64 B/cell AoS Expr.
+//
+// Solvers:
+//   CG     the algorithm of linear::SolverConjugate (src/linear/linear.ipp:
+//          24-129): three kernels per iteration, dot products reduced
+//          deterministically in one grid-wide pass, the stopping test
+//          evaluated on the device so that iterations run without host
+//          round trips.
+//   MGPCG  CG preconditioned by one geometric multigrid V-cycle (red-black
+//          Gauss-Seidel, summed restriction, constant prolongation, coarse
+//          operators from face-coefficient sums, FP64 CG on the coarsest
+//          level), all FP64.
+//   MIXED  FP64 defect correction: r = b - A x, the update and the outer
+//          norms in FP64; the correction equation solved by FP32 MG-PCG;
+//          the coarsest level solved in FP64.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <functional>
+
+#include "common.cuh"
+
+namespace aphgpu {
+
+int FlatBlocks(int64_t n) {
+  int dev = 0, sms = 152;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  const int64_t want = (n + kFlatThreads - 1) / kFlatThreads;
+  const int64_t cap = (int64_t)sms * 8;
+  return (int)std::max<int64_t>(1, std::min(want, cap));
+}
+
+namespace {
+
+// Explicitly rounded FP64 operations: the assembly and flux kernels must not
+// be contracted into fused multiply-adds, so that they reproduce the
+// reference's arithmetic bit for bit (the solver kernels may fuse).
+__device__ __forceinline__ double M(double a, double b) { return __dmul_rn(a, b); }
+__device__ __forceinline__ double A(double a, double b) { return __dadd_rn(a, b); }
+__device__ __forceinline__ double S(double a, double b) { return __dsub_rn(a, b); }
+
+// ---------------------------------------------------------------------------
+// Operator access
+// ---------------------------------------------------------------------------
+
+template <class T>
+struct Op {
+  Dims d;
+  const T* w0;
+  const T* w1;
+  const T* w2;
+  const T* diag;  // may be NULL: -(sum of the six couplings)
+};
+
+// Couplings of cell (i,j,k) in reference order xm,xp,ym,yp,zm,zp.
+template <class T>
+__device__ __forceinline__ void Couplings(const Op<T>& A, int i, int j, int k,
+                                          int64_t c, T e[6]) {
+  const Dims& d = A.d;
+  const int ip = wrapp(i + 1, d.nx), jp = wrapp(j + 1, d.ny), kp = wrapp(k + 1, d.nz);
+  e[0] = A.w0[c];
+  e[1] = A.w0[d.idx(ip, j, k)];
+  e[2] = A.w1[c];
+  e[3] = A.w1[d.idx(i, jp, k)];
+  e[4] = A.w2[c];
+  e[5] = A.w2[d.idx(i, j, kp)];
+}
+
+template <class T>
+__device__ __forceinline__ T Diag(const Op<T>& A, int64_t c, const T e[6]) {
+  if (A.diag) return A.diag[c];
+  T s = T(0);
+  s += e[0];
+  s += e[1];
+  s += e[2];
+  s += e[3];
+  s += e[4];
+  s += e[5];
+  return -s;
+}
+
+// sum_q e_q x_nb(q) + e0 x_c, in the order of linear.ipp:66-72
+template <class T>
+__device__ __forceinline__ T Apply(const Op<T>& A, const T* x, int i, int j,
+                                   int k, int64_t c) {
+  const Dims& d = A.d;
+  T e[6];
+  Couplings(A, i, j, k, c, e);
+  const T e0 = Diag(A, c, e);
+  const int im = wrapm(i - 1, d.nx), ip = wrapp(i + 1, d.nx);
+  const int jm = wrapm(j - 1, d.ny), jp = wrapp(j + 1, d.ny);
+  const int km = wrapm(k - 1, d.nz), kp = wrapp(k + 1, d.nz);
+  T u = x[c] * e0;
+  u += x[d.idx(im, j, k)] * e[0];
+  u += x[d.idx(ip, j, k)] * e[1];
+  u += x[d.idx(i, jm, k)] * e[2];
+  u += x[d.idx(i, jp, k)] * e[3];
+  u += x[d.idx(i, j, km)] * e[4];
+  u += x[d.idx(i, j, kp)] * e[5];
+  return u;
+}
+
+#define TILE_LOOP_BEGIN(dims)                                    \
+  const int i = blockIdx.x * kTileX + threadIdx.x;               \
+  const int j = blockIdx.y * kTileY + threadIdx.y;               \
+  const int kb = blockIdx.z * kTileZ;                            \
+  const int ke = min(kb + kTileZ, (dims).nz);                    \
+  const bool inxy = i < (dims).nx && j < (dims).ny;              \
+  for (int k = kb; k < ke; ++k) {                                \
+    if (!inxy) continue;                                         \
+    const int64_t c = (dims).idx(i, j, k);
+#define TILE_LOOP_END }
+
+// ---------------------------------------------------------------------------
+// System set-up
+// ---------------------------------------------------------------------------
+
+// flags[0]: asymmetric cells, flags[1]: cells whose e0 != -(sum of e_q)
+__global__ void KExprToSystem(Dims d, const double* __restrict__ e8,
+                              double* w0, double* w1, double* w2, double* diag,
+                              double* b, unsigned int* flags) {
+  unsigned int asym = 0, nonpure = 0;
+  TILE_LOOP_BEGIN(d)
+  const double* e = e8 + 8 * c;
+  w0[c] = e[1];
+  w1[c] = e[3];
+  w2[c] = e[5];
+  diag[c] = e[0];
+  b[c] = -e[7];
+  const int ip = wrapp(i + 1, d.nx), jp = wrapp(j + 1, d.ny), kp = wrapp(k + 1, d.nz);
+  if (e[2] != e8[8 * d.idx(ip, j, k) + 1]) ++asym;
+  if (e[4] != e8[8 * d.idx(i, jp, k) + 3]) ++asym;
+  if (e[6] != e8[8 * d.idx(i, j, kp) + 5]) ++asym;
+  double s = 0;
+  for (int q = 1; q <= 6; ++q) s += e[q];
+  if (e[0] != -s) ++nonpure;
+  TILE_LOOP_END
+  if (asym) atomicAdd(&flags[0], asym);
+  if (nonpure) atomicAdd(&flags[1], nonpure);
+}
+
+// Face coefficients and predicted fluxes (proj.ipp:343-360, 556-562):
+// rho = rho1*(1-a)+rho2*a (hydro.ipp:1818-1821), face density harmonic
+// (approx_eb.h:351-363), kk = -area/rho_f*dt, e0f = -(1/h)*kk; the Expr of
+// the plus cell gets e[1+2d] = -e0f.
+__global__ void KAssembleFaces(Dims d, const double* __restrict__ alpha,
+                               double rho1, double rho2,
+                               const double* __restrict__ vflux,
+                               const double* __restrict__ febp, double dt,
+                               double h, double* w0, double* w1, double* w2,
+                               double* vstar) {
+  const double area = h * h;
+  const double ainv = 1 / h;
+  const int64_t N = d.cells();
+  TILE_LOOP_BEGIN(d)
+  const double ac = alpha[c];
+  const double rc = A(M(rho1, S(1, ac)), M(rho2, ac));
+  const double invc = 1 / rc;
+  double* ws[3] = {w0, w1, w2};
+  for (int q = 0; q < 3; ++q) {
+    const int64_t cm = q == 0 ? d.idx(wrapm(i - 1, d.nx), j, k)
+                     : q == 1 ? d.idx(i, wrapm(j - 1, d.ny), k)
+                              : d.idx(i, j, wrapm(k - 1, d.nz));
+    const double am = alpha[cm];
+    const double rm = A(M(rho1, S(1, am)), M(rho2, am));
+    const double invm = 1 / rm;
+    const double rf = 1 / M(A(invc, invm), 0.5);
+    const double kk = M(-area / rf, dt);
+    const double e0f = M(-ainv, kk);
+    ws[q][c] = -e0f;
+    double v = vflux[q * N + c];
+    if (febp) v = A(v, M(M(febp[q * N + c] / rf, dt), area));
+    vstar[q * N + c] = v;
+  }
+  TILE_LOOP_END
+}
+
+// e7 = sum over q of outward v* (AppendExpr order), b = -e7; reduces sum e7.
+__global__ void KAssembleRhs(Dims d, const double* __restrict__ vstar,
+                             double* b, RedBuf rb, double* out) {
+  const int64_t N = d.cells();
+  double v[1] = {0};
+  const int op[1] = {0};
+  TILE_LOOP_BEGIN(d)
+  const int ip = wrapp(i + 1, d.nx), jp = wrapp(j + 1, d.ny), kp = wrapp(k + 1, d.nz);
+  double s = 0;
+  s = A(s, -vstar[c]);
+  s = A(s, vstar[d.idx(ip, j, k)]);
+  s = A(s, -vstar[N + c]);
+  s = A(s, vstar[N + d.idx(i, jp, k)]);
+  s = A(s, -vstar[2 * N + c]);
+  s = A(s, vstar[2 * N + d.idx(i, j, kp)]);
+  b[c] = -s;
+  v[0] += s;
+  TILE_LOOP_END
+  GridReduce<1>(v, op, rb, out);
+}
+
+// b = -(e7 - mean) with e7 = -b
+__global__ void KRemoveMean(int64_t n, double* b, const double* sum) {
+  const double mean = sum[0] / (double)n;
+  for (int64_t c = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; c < n;
+       c += (int64_t)gridDim.x * blockDim.x) {
+    const double e7 = -b[c];
+    b[c] = -S(e7, mean);
+  }
+}
+
+// Expr of every cell from the compact storage (inverse of KExprToSystem):
+// e0 as GetFluxSum accumulates it when no explicit diagonal is stored.
+__global__ void KSystemToExpr(Op<double> Aop, const double* __restrict__ b,
+                              double* e8) {
+  TILE_LOOP_BEGIN(Aop.d)
+  double e[6];
+  Couplings(Aop, i, j, k, c, e);
+  double* o = e8 + 8 * c;
+  if (Aop.diag) {
+    o[0] = Aop.diag[c];
+  } else {
+    double s = 0;
+    for (int q = 0; q < 6; ++q) s = A(s, -e[q]);
+    o[0] = s;
+  }
+  for (int q = 0; q < 6; ++q) o[1 + q] = e[q];
+  o[7] = -b[c];
+  TILE_LOOP_END
+}
+
+template <class T>
+__global__ void KInvDiag(Op<T> A, T* invdiag) {
+  TILE_LOOP_BEGIN(A.d)
+  T e[6];
+  Couplings(A, i, j, k, c, e);
+  invdiag[c] = T(1) / Diag(A, c, e);
+  TILE_LOOP_END
+}
+
+// ---------------------------------------------------------------------------
+// Plain CG (linear.ipp:24-129)
+// ---------------------------------------------------------------------------
+
+// r = -(x*e0 + e7 + sum x_nb e_q), p = r   (stage init, linear.ipp:42-61)
+__global__ void KCgInit(Op<double> A, const double* __restrict__ b,
+                        const double* x, double* r, double* p, int zero_guess) {
+  TILE_LOOP_BEGIN(A.d)
+  double u;
+  if (zero_guess) {
+    u = -b[c];
+  } else {
+    double e[6];
+    Couplings(A, i, j, k, c, e);
+    const double e0 = Diag(A, c, e);
+    const Dims& d = A.d;
+    u = x[c] * e0 + (-b[c]);
+    u += x[d.idx(wrapm(i - 1, d.nx), j, k)] * e[0];
+    u += x[d.idx(wrapp(i + 1, d.nx), j, k)] * e[1];
+    u += x[d.idx(i, wrapm(j - 1, d.ny), k)] * e[2];
+    u += x[d.idx(i, wrapp(j + 1, d.ny), k)] * e[3];
+    u += x[d.idx(i, j, wrapm(k - 1, d.nz))] * e[4];
+    u += x[d.idx(i, j, wrapp(k + 1, d.nz))] * e[5];
+  }
+  r[c] = -u;
+  p[c] = -u;
+  TILE_LOOP_END
+}
+
+// stage iter: lp = A p, dot_r_prev = r.r, dot_p_lp = p.lp
+__global__ void KCgApply(Op<double> A, const double* __restrict__ r,
+                         const double* __restrict__ p, double* ap,
+                         SolveScalars* s, RedBuf rb) {
+  if (s->done) return;
+  double v[2] = {0, 0};
+  const int op[2] = {0, 0};
+  TILE_LOOP_BEGIN(A.d)
+  const double y = Apply(A, p, i, j, k, c);
+  ap[c] = y;
+  v[0] += r[c] * r[c];
+  v[1] += p[c] * y;
+  TILE_LOOP_END
+  __shared__ double out[2];
+  if (GridReduce<2>(v, op, rb, out)) {
+    if (threadIdx.x == 0 && threadIdx.y == 0) {
+      s->rr_prev = out[0];
+      s->pap = out[1];
+      s->alpha = out[0] / (out[1] + 1e-100);
+    }
+  }
+}
+
+// stage iter2 + check: x += alpha p, r -= alpha lp, dot_r, max_r
+__global__ void KCgUpdate(Dims d, double* x, double* r,
+                          const double* __restrict__ p,
+                          const double* __restrict__ ap, SolveScalars* s,
+                          RedBuf rb) {
+  if (s->done) return;
+  const double alpha = s->alpha;
+  double v[2] = {0, 0};
+  const int op[2] = {0, 1};
+  TILE_LOOP_BEGIN(d)
+  x[c] += alpha * p[c];
+  const double rn = r[c] - alpha * ap[c];
+  r[c] = rn;
+  v[0] += rn * rn;
+  v[1] = fmax(v[1], fabs(rn));
+  TILE_LOOP_END
+  __shared__ double out[2];
+  if (GridReduce<2>(v, op, rb, out)) {
+    if (threadIdx.x == 0 && threadIdx.y == 0) {
+      s->rr = out[0];
+      s->maxr = out[1];
+      s->beta = out[0] / (s->rr_prev + 1e-100);
+      const double res = s->maxnorm ? out[1] / s->cellvol : sqrt(out[0] / s->cellvol);
+      s->residual = res * s->res_scale;
+      s->iter += 1;
+      if (s->iter >= s->miniter && (s->iter > s->maxiter || s->residual < s->tol)) {
+        s->done = 1;
+        s->converged = s->residual < s->tol;
+      }
+    }
+  }
+}
+
+// stage iter3: p = r + beta p
+__global__ void KCgP(Dims d, const double* __restrict__ r, double* p,
+                     const SolveScalars* s) {
+  if (s->done) return;
+  const double beta = s->beta;
+  TILE_LOOP_BEGIN(d)
+  p[c] = r[c] + beta * p[c];
+  TILE_LOOP_END
+}
+
+// ---------------------------------------------------------------------------
+// Preconditioned CG building blocks (templated on the vector precision)
+// ---------------------------------------------------------------------------
+
+// ap = A p, reduces p.ap -> alpha = rz / p.ap
+template <class T>
+__global__ void KPcgApply(Op<T> A, const T* __restrict__ p, T* ap,
+                          SolveScalars* s, RedBuf rb) {
+  if (s->done) return;
+  double v[1] = {0};
+  const int op[1] = {0};
+  TILE_LOOP_BEGIN(A.d)
+  const T y = Apply(A, p, i, j, k, c);
+  ap[c] = y;
+  v[0] += (double)p[c] * (double)y;
+  TILE_LOOP_END
+  __shared__ double out[1];
+  if (GridReduce<1>(v, op, rb, out)) {
+    if (threadIdx.x == 0 && threadIdx.y == 0) {
+      s->pap = out[0];
+      s->alpha = s->rz / (out[0] + 1e-300);
+    }
+  }
+}
+
+// x += alpha p, r -= alpha ap, reduces r.r and max|r|, then the stopping test
+template <class T>
+__global__ void KPcgUpdate(Dims d, T* x, T* r, const T* __restrict__ p,
+                           const T* __restrict__ ap, SolveScalars* s,
+                           RedBuf rb) {
+  if (s->done) return;
+  const T alpha = (T)s->alpha;
+  double v[2] = {0, 0};
+  const int op[2] = {0, 1};
+  TILE_LOOP_BEGIN(d)
+  x[c] += alpha * p[c];
+  const T rn = r[c] - alpha * ap[c];
+  r[c] = rn;
+  v[0] += (double)rn * (double)rn;
+  v[1] = fmax(v[1], fabs((double)rn));
+  TILE_LOOP_END
+  __shared__ double out[2];
+  if (GridReduce<2>(v, op, rb, out)) {
+    if (threadIdx.x == 0 && threadIdx.y == 0) {
+      s->rr = out[0];
+      s->maxr = out[1];
+      const double res = s->maxnorm ? out[1] / s->cellvol : sqrt(out[0] / s->cellvol);
+      s->residual = res * s->res_scale;
+      s->iter += 1;
+      if (s->iter >= s->miniter && (s->iter > s->maxiter || s->residual < s->tol)) {
+        s->done = 1;
+        s->converged = s->residual < s->tol;
+      }
+    }
+  }
+}
+
+// rz = r.z; first == 1: p = z (start), else beta = rz/rz_prev, p = z + beta p
+// (two passes: reduction kernel then update kernel)
+template <class T>
+__global__ void KDotRZ(Dims d, const T* __restrict__ r, const T* __restrict__ z,
+                       SolveScalars* s, RedBuf rb, int first) {
+  if (s->done) return;
+  double v[1] = {0};
+  const int op[1] = {0};
+  TILE_LOOP_BEGIN(d)
+  v[0] += (double)r[c] * (double)z[c];
+  TILE_LOOP_END
+  __shared__ double out[1];
+  if (GridReduce<1>(v, op, rb, out)) {
+    if (threadIdx.x == 0 && threadIdx.y == 0) {
+      s->rz_prev = first ? 0.0 : s->rz;
+      s->rz = out[0];
+      s->beta = first ? 0.0 : out[0] / (s->rz_prev + 1e-300);
+    }
+  }
+}
+
+template <class T>
+__global__ void KPcgP(Dims d, const T* __restrict__ z, T* p,
+                      const SolveScalars* s, int first) {
+  if (s->done) return;
+  const T beta = (T)s->beta;
+  TILE_LOOP_BEGIN(d)
+  p[c] = first ? z[c] : z[c] + beta * p[c];
+  TILE_LOOP_END
+}
+
+// ---------------------------------------------------------------------------
+// Multigrid kernels
+// ---------------------------------------------------------------------------
+
+// Red-black Gauss-Seidel half sweep on cells with (i+j+k)%2 == color:
+// x_c = (b_c - sum_q e_q x_nb) / e0.  zero_init: the other colour is
+// treated as zero (first half sweep from a zero guess).
+template <class T>
+__global__ void KSmooth(Op<T> A, const T* __restrict__ invdiag,
+                        const T* __restrict__ b, T* x, int color,
+                        int zero_init, const SolveScalars* s) {
+  if (s && s->done) return;
+  const Dims& d = A.d;
+  TILE_LOOP_BEGIN(d)
+  if (((i + j + k) & 1) != color) continue;
+  if (zero_init) {
+    x[c] = b[c] * invdiag[c];
+    continue;
+  }
+  T e[6];
+  Couplings(A, i, j, k, c, e);
+  T acc = b[c];
+  acc -= x[d.idx(wrapm(i - 1, d.nx), j, k)] * e[0];
+  acc -= x[d.idx(wrapp(i + 1, d.nx), j, k)] * e[1];
+  acc -= x[d.idx(i, wrapm(j - 1, d.ny), k)] * e[2];
+  acc -= x[d.idx(i, wrapp(j + 1, d.ny), k)] * e[3];
+  acc -= x[d.idx(i, j, wrapm(k - 1, d.nz))] * e[4];
+  acc -= x[d.idx(i, j, wrapp(k + 1, d.nz))] * e[5];
+  x[c] = acc * invdiag[c];
+  TILE_LOOP_END
+}
+
+// Residual of the fine level summed over the 8 children into the coarse
+// right-hand side.  One thread per coarse cell.
+template <class T, class TC>
+__global__ void KResidualRestrict(Op<T> A, const T* __restrict__ b,
+                                  const T* __restrict__ x, Dims dc, TC* bc,
+                                  const SolveScalars* s) {
+  if (s && s->done) return;
+  const int I = blockIdx.x * kTileX + threadIdx.x;
+  const int J = blockIdx.y * kTileY + threadIdx.y;
+  const int kb = blockIdx.z * kTileZ;
+  const int ke = min(kb + kTileZ, dc.nz);
+  if (I >= dc.nx || J >= dc.ny) return;
+  for (int K = kb; K < ke; ++K) {
+    T sum = T(0);
+#pragma unroll
+    for (int q = 0; q < 8; ++q) {
+      const int i = 2 * I + (q & 1), j = 2 * J + ((q >> 1) & 1), k = 2 * K + (q >> 2);
+      const int64_t c = A.d.idx(i, j, k);
+      sum += b[c] - Apply(A, x, i, j, k, c);
+    }
+    bc[dc.idx(I, J, K)] = (TC)sum;
+  }
+}
+
+// x_fine += x_coarse(parent)
+template <class T, class TC>
+__global__ void KProlong(Dims d, T* x, Dims dc, const TC* __restrict__ xc,
+                         const SolveScalars* s) {
+  if (s && s->done) return;
+  TILE_LOOP_BEGIN(d)
+  x[c] += (T)xc[dc.idx(i >> 1, j >> 1, k >> 1)];
+  TILE_LOOP_END
+}
+
+// Coarse operator: 0.5 * Galerkin with constant prolongation.
+// Coarse minus-face coupling = 0.5 * sum of the 4 fine minus-face
+// couplings; coarse diagonal = 0.5 * (sum of 8 fine diagonals + 2 * sum of
+// the 12 interior fine couplings).
+template <class T, class TC>
+__global__ void KCoarsenOp(Op<T> A, Dims dc, TC* w0, TC* w1, TC* w2, TC* diag,
+                           TC* invdiag) {
+  const int I = blockIdx.x * kTileX + threadIdx.x;
+  const int J = blockIdx.y * kTileY + threadIdx.y;
+  const int kb = blockIdx.z * kTileZ;
+  const int ke = min(kb + kTileZ, dc.nz);
+  if (I >= dc.nx || J >= dc.ny) return;
+  const Dims& d = A.d;
+  for (int K = kb; K < ke; ++K) {
+    double sw[3] = {0, 0, 0};
+    double sd = 0, sint = 0;
+    for (int q = 0; q < 8; ++q) {
+      const int a = q & 1, bb = (q >> 1) & 1, cc = q >> 2;
+      const int i = 2 * I + a, j = 2 * J + bb, k = 2 * K + cc;
+      const int64_t c = d.idx(i, j, k);
+      T e[6];
+      Couplings(A, i, j, k, c, e);
+      sd += (double)Diag(A, c, e);
+      if (a == 0) sw[0] += (double)e[0]; else sint += (double)e[0];
+      if (bb == 0) sw[1] += (double)e[2]; else sint += (double)e[2];
+      if (cc == 0) sw[2] += (double)e[4]; else sint += (double)e[4];
+    }
+    const int64_t C = dc.idx(I, J, K);
+    w0[C] = (TC)(0.5 * sw[0]);
+    w1[C] = (TC)(0.5 * sw[1]);
+    w2[C] = (TC)(0.5 * sw[2]);
+    const double dg = 0.5 * (sd + 2 * sint);
+    diag[C] = (TC)dg;
+    invdiag[C] = (TC)(1.0 / dg);
+  }
+}
+
+template <class TS, class TD>
+__global__ void KConvert(int64_t n, const TS* __restrict__ a, TD* out, double scale) {
+  for (int64_t c = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; c < n;
+       c += (int64_t)gridDim.x * blockDim.x)
+    out[c] = (TD)((double)a[c] * scale);
+}
+
+// Coarsest level: FP64 CG in a single CTA on <= 4096 cells, right-hand side
+// mean removed (the periodic operator is singular), solved to a relative
+// residual of 1e-13 (or 2000 iterations); the result overwrites xc.
+template <class TC>
+__global__ void __launch_bounds__(1024) KCoarsestCG(
+    Op<TC> A, const TC* __restrict__ bc, TC* xc, double* r, double* p,
+    double* ap, double* x, const SolveScalars* s) {
+  if (s && s->done) return;
+  const Dims& d = A.d;
+  const int n = (int)d.cells();
+  const int tid = threadIdx.x;
+  __shared__ double red[32];
+  __shared__ double bcast;
+  auto bsum = [&](double v) -> double {
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+    if ((tid & 31) == 0) red[tid >> 5] = v;
+    __syncthreads();
+    if (tid < 32) {
+      double w = tid < (int)(blockDim.x >> 5) ? red[tid] : 0.0;
+      for (int o = 16; o > 0; o >>= 1) w += __shfl_down_sync(0xffffffffu, w, o);
+      if (tid == 0) bcast = w;
+    }
+    __syncthreads();
+    const double out = bcast;
+    __syncthreads();
+    return out;
+  };
+  double sb = 0;
+  for (int c = tid; c < n; c += blockDim.x) sb += (double)bc[c];
+  const double mean = bsum(sb) / n;
+  double rr = 0;
+  for (int c = tid; c < n; c += blockDim.x) {
+    const double v = (double)bc[c] - mean;
+    r[c] = v;
+    p[c] = v;
+    x[c] = 0;
+    rr += v * v;
+  }
+  rr = bsum(rr);
+  const double stop = rr * 1e-26;
+  for (int it = 0; it < 2000 && rr > stop && rr > 0; ++it) {
+    double pap = 0;
+    for (int c = tid; c < n; c += blockDim.x) {
+      const int i = c % d.nx, j = (c / d.nx) % d.ny, k = c / (d.nx * d.ny);
+      double e[6];
+      {
+        TC et[6];
+        Couplings(A, i, j, k, c, et);
+        for (int q = 0; q < 6; ++q) e[q] = (double)et[q];
+      }
+      const double e0 = A.diag ? (double)A.diag[c]
+                               : -(e[0] + e[1] + e[2] + e[3] + e[4] + e[5]);
+      double y = p[c] * e0;
+      y += p[d.idx(wrapm(i - 1, d.nx), j, k)] * e[0];
+      y += p[d.idx(wrapp(i + 1, d.nx), j, k)] * e[1];
+      y += p[d.idx(i, wrapm(j - 1, d.ny), k)] * e[2];
+      y += p[d.idx(i, wrapp(j + 1, d.ny), k)] * e[3];
+      y += p[d.idx(i, j, wrapm(k - 1, d.nz))] * e[4];
+      y += p[d.idx(i, j, wrapp(k + 1, d.nz))] * e[5];
+      ap[c] = y;
+      pap += p[c] * y;
+    }
+    pap = bsum(pap);
+    if (!(pap > 0)) break;
+    const double alpha = rr / pap;
+    double rn = 0;
+    for (int c = tid; c < n; c += blockDim.x) {
+      x[c] += alpha * p[c];
+      r[c] -= alpha * ap[c];
+      rn += r[c] * r[c];
+    }
+    rn = bsum(rn);
+    const double beta = rn / rr;
+    rr = rn;
+    for (int c = tid; c < n; c += blockDim.x) p[c] = r[c] + beta * p[c];
+    __syncthreads();
+  }
+  for (int c = tid; c < n; c += blockDim.x) xc[c] = (TC)x[c];
+}
+
+// r = b - A x (FP64) with reductions r.r, max|r|, b.b; stopping test
+__global__ void KResidual64(Op<double> A, const double* __restrict__ b,
+                            const double* __restrict__ x, double* r,
+                            SolveScalars* s, RedBuf rb, int count_iter) {
+  double v[3] = {0, 0, 0};
+  const int op[3] = {0, 1, 0};
+  TILE_LOOP_BEGIN(A.d)
+  // r = -(x*e0 + e7 + sum x_nb e_q) as linear.ipp:47-53, e7 = -b
+  double e[6];
+  Couplings(A, i, j, k, c, e);
+  const double e0 = Diag(A, c, e);
+  const Dims& d = A.d;
+  double u = x[c] * e0 + (-b[c]);
+  u += x[d.idx(wrapm(i - 1, d.nx), j, k)] * e[0];
+  u += x[d.idx(wrapp(i + 1, d.nx), j, k)] * e[1];
+  u += x[d.idx(i, wrapm(j - 1, d.ny), k)] * e[2];
+  u += x[d.idx(i, wrapp(j + 1, d.ny), k)] * e[3];
+  u += x[d.idx(i, j, wrapm(k - 1, d.nz))] * e[4];
+  u += x[d.idx(i, j, wrapp(k + 1, d.nz))] * e[5];
+  const double rv = -u;
+  if (r) r[c] = rv;
+  v[0] += rv * rv;
+  v[1] = fmax(v[1], fabs(rv));
+  v[2] += b[c] * b[c];
+  TILE_LOOP_END
+  __shared__ double out[3];
+  if (GridReduce<3>(v, op, rb, out)) {
+    if (threadIdx.x == 0 && threadIdx.y == 0) {
+      s->rr = out[0];
+      s->maxr = out[1];
+      s->tmp[0] = out[2];
+      const double res = s->maxnorm ? out[1] / s->cellvol : sqrt(out[0] / s->cellvol);
+      s->residual = res;
+      if (count_iter) {
+        if (s->iter >= s->miniter && (s->iter > s->maxiter || s->residual < s->tol)) {
+          s->done = 1;
+          s->converged = s->residual < s->tol;
+        }
+      }
+    }
+  }
+}
+
+// x += scale * e
+__global__ void KAddCorrection(int64_t n, double* x, const float* __restrict__ e,
+                               const SolveScalars* s) {
+  const double scale = s->tmp[1];
+  for (int64_t c = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; c < n;
+       c += (int64_t)gridDim.x * blockDim.x)
+    x[c] += scale * (double)e[c];
+}
+
+// r32 = r / scale with scale = max|r| (s->maxr), stores scale in tmp[1]
+__global__ void KScaleResidual(int64_t n, const double* __restrict__ r, float* r32,
+                               SolveScalars* s) {
+  const double m = s->maxr;
+  const double scale = m > 0 ? m : 1.0;
+  if (blockIdx.x == 0 && threadIdx.x == 0) s->tmp[1] = scale;
+  const double inv = 1.0 / scale;
+  for (int64_t c = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; c < n;
+       c += (int64_t)gridDim.x * blockDim.x)
+    r32[c] = (float)(r[c] * inv);
+}
+
+__global__ void KZeroF(int64_t n, float* a) {
+  for (int64_t c = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; c < n;
+       c += (int64_t)gridDim.x * blockDim.x)
+    a[c] = 0.f;
+}
+
+// Corrected fluxes: v = p[cm]*k + p[cp]*(-k) + v*, k = -w (proj.ipp:399-403)
+__global__ void KFluxCorrect(Dims d, const double* __restrict__ w0,
+                             const double* __restrict__ w1,
+                             const double* __restrict__ w2,
+                             const double* __restrict__ p,
+                             const double* __restrict__ vstar, double* out) {
+  const int64_t N = d.cells();
+  TILE_LOOP_BEGIN(d)
+  const double* ws[3] = {w0, w1, w2};
+  for (int q = 0; q < 3; ++q) {
+    const int64_t cm = q == 0 ? d.idx(wrapm(i - 1, d.nx), j, k)
+                     : q == 1 ? d.idx(i, wrapm(j - 1, d.ny), k)
+                              : d.idx(i, j, wrapm(k - 1, d.nz));
+    const double e0 = -ws[q][c];
+    const double e1 = -e0;
+    out[q * N + c] = A(A(M(p[cm], e0), M(p[c], e1)), vstar[q * N + c]);
+  }
+  TILE_LOOP_END
+}
+
+// Cell acceleration of Proj::GetAcceleration (proj.ipp:408-433)
+__global__ void KAcceleration(Dims d, double h, const double* __restrict__ p,
+                              const double* __restrict__ alpha, double rho1,
+                              double rho2, const double* __restrict__ febp,
+                              double* acc) {
+  const int64_t N = d.cells();
+  TILE_LOOP_BEGIN(d)
+  double sacc[3] = {0, 0, 0};
+  for (int q = 0; q < 6; ++q) {
+    const int dd = q / 2;
+    const int o[3] = {dd == 0, dd == 1, dd == 2};
+    int64_t f, cm, cp;
+    if (q % 2 == 0) {
+      f = c;
+      cm = d.idx(wrapm(i - o[0], d.nx), wrapm(j - o[1], d.ny), wrapm(k - o[2], d.nz));
+      cp = c;
+    } else {
+      f = d.idx(wrapp(i + o[0], d.nx), wrapp(j + o[1], d.ny), wrapp(k + o[2], d.nz));
+      cm = c;
+      cp = f;
+    }
+    const double am = alpha[cm], ap = alpha[cp];
+    const double invm = 1 / A(M(rho1, S(1, am)), M(rho2, am));
+    const double invp = 1 / A(M(rho1, S(1, ap)), M(rho2, ap));
+    const double rf = 1 / M(A(invp, invm), 0.5);
+    const double gp = S(p[cp], p[cm]) / h;
+    const double fb = febp ? febp[dd * N + f] : 0.;
+    const double a = S(fb, gp) / rf;
+    for (int e = 0; e < 3; ++e) sacc[e] = A(sacc[e], M(e == dd ? 1. : 0., M(a, 0.5)));
+  }
+  acc[3 * c + 0] = sacc[0];
+  acc[3 * c + 1] = sacc[1];
+  acc[3 * c + 2] = sacc[2];
+  TILE_LOOP_END
+}
+
+// ---------------------------------------------------------------------------
+// Host helpers
+// ---------------------------------------------------------------------------
+
+template <class T>
+Op<T> MakeOp(const Level<T>& L) {
+  return Op<T>{L.d, L.w[0], L.w[1], L.w[2], L.has_diag ? L.diag : nullptr};
+}
+
+Op<double> FineOp(aphgpu_ctx* ctx) {
+  return Op<double>{ctx->d, ctx->w[0], ctx->w[1], ctx->w[2],
+                    ctx->diag_explicit ? ctx->diag : nullptr};
+}
+
+int InitScalars(aphgpu_ctx* ctx, SolveScalars* s, const aphgpu_conf* conf,
+                double res_scale) {
+  SolveScalars h{};
+  h.tol = conf->tol;
+  h.cellvol = ctx->h * ctx->h * ctx->h;
+  h.res_scale = res_scale;
+  h.miniter = conf->miniter;
+  h.maxiter = conf->maxiter;
+  h.maxnorm = conf->maxnorm;
+  APH_CUDA(ctx, cudaMemcpyAsync(s, &h, sizeof(h), cudaMemcpyHostToDevice, ctx->stream));
+  return APHGPU_OK;
+}
+
+int ReadScalars(aphgpu_ctx* ctx, const SolveScalars* s, SolveScalars* out) {
+  APH_CUDA(ctx, cudaMemcpyAsync(ctx->hscal, s, sizeof(SolveScalars),
+                                cudaMemcpyDeviceToHost, ctx->stream));
+  APH_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+  *out = *ctx->hscal;
+  return APHGPU_OK;
+}
+
+// Coarsening: halve while all dimensions are even and the level has more
+// than `coarse_max` cells.
+std::vector<Dims> LevelDims(Dims d, int coarse_max) {
+  std::vector<Dims> v{d};
+  while (true) {
+    const Dims& c = v.back();
+    if (c.cells() <= coarse_max) break;
+    if ((c.nx & 1) || (c.ny & 1) || (c.nz & 1)) break;
+    if (c.nx < 4 || c.ny < 4 || c.nz < 4) break;
+    v.push_back(Dims{c.nx / 2, c.ny / 2, c.nz / 2});
+  }
+  return v;
+}
+
+template <class T>
+int AllocLevel(aphgpu_ctx* ctx, Level<T>& L, bool op, bool vec) {
+  const int64_t n = L.d.cells();
+  if (op) {
+    for (int q = 0; q < 3; ++q) APH_TRY(Alloc(ctx, &L.w[q], n));
+    APH_TRY(Alloc(ctx, &L.diag, n));
+    APH_TRY(Alloc(ctx, &L.invdiag, n));
+  }
+  if (vec) {
+    APH_TRY(Alloc(ctx, &L.x, n));
+    APH_TRY(Alloc(ctx, &L.b, n));
+  }
+  return APHGPU_OK;
+}
+
+int EnsureCoarsestScratch(aphgpu_ctx* ctx, int64_t n) {
+  auto& mg = ctx->mg;
+  if (mg.cr) return APHGPU_OK;
+  const int64_t m = std::max<int64_t>(n, 4096);
+  APH_TRY(Alloc(ctx, &mg.cr, m));
+  APH_TRY(Alloc(ctx, &mg.cp, m));
+  APH_TRY(Alloc(ctx, &mg.cap, m));
+  APH_TRY(Alloc(ctx, &mg.cx, m));
+  APH_TRY(Alloc(ctx, &mg.cb, m));
+  return APHGPU_OK;
+}
+
+// Builds the FP64 (T=double) or FP32 hierarchy from the fine system.
+template <class T>
+int BuildHierarchy(aphgpu_ctx* ctx, std::vector<Level<T>>& lv, int coarse_max);
+
+template <>
+int BuildHierarchy<double>(aphgpu_ctx* ctx, std::vector<Level<double>>& lv,
+                           int coarse_max) {
+  const auto dims = LevelDims(ctx->d, coarse_max);
+  if (dims.back().cells() > 4096)
+    return SetError(ctx, APHGPU_ERR_UNSUPPORTED,
+                    "multigrid: coarsest level of %lld cells exceeds 4096 "
+                    "(grid %dx%dx%d does not coarsen)",
+                    (long long)dims.back().cells(), ctx->d.nx, ctx->d.ny, ctx->d.nz);
+  if (lv.size() != dims.size()) {
+    lv.assign(dims.size(), Level<double>{});
+    for (size_t l = 0; l < dims.size(); ++l) {
+      lv[l].d = dims[l];
+      if (l > 0) APH_TRY(AllocLevel(ctx, lv[l], true, true));
+      lv[l].has_diag = l > 0;
+    }
+  }
+  Level<double>& f = lv[0];
+  f.w[0] = ctx->w[0];
+  f.w[1] = ctx->w[1];
+  f.w[2] = ctx->w[2];
+  f.diag = ctx->diag;
+  f.has_diag = ctx->diag_explicit;
+  f.invdiag = ctx->invdiag;
+  for (size_t l = 1; l < lv.size(); ++l) {
+    const Op<double> A = MakeOp(lv[l - 1]);
+    KCoarsenOp<double, double><<<TileGrid(lv[l].d), TileBlock(), 0, ctx->stream>>>(
+        A, lv[l].d, lv[l].w[0], lv[l].w[1], lv[l].w[2], lv[l].diag, lv[l].invdiag);
+    APH_LAUNCHED(ctx);
+  }
+  APH_TRY(EnsureCoarsestScratch(ctx, lv.back().d.cells()));
+  return APHGPU_OK;
+}
+
+template <>
+int BuildHierarchy<float>(aphgpu_ctx* ctx, std::vector<Level<float>>& lv,
+                          int coarse_max) {
+  const auto dims = LevelDims(ctx->d, coarse_max);
+  if (dims.back().cells() > 4096)
+    return SetError(ctx, APHGPU_ERR_UNSUPPORTED,
+                    "multigrid: coarsest level of %lld cells exceeds 4096",
+                    (long long)dims.back().cells());
+  if (lv.size() != dims.size()) {
+    lv.assign(dims.size(), Level<float>{});
+    for (size_t l = 0; l < dims.size(); ++l) {
+      lv[l].d = dims[l];
+      APH_TRY(AllocLevel(ctx, lv[l], true, l > 0));
+      lv[l].has_diag = true;
+    }
+  }
+  // fine FP32 operator from the FP64 system: couplings rounded to FP32;
+  // the diagonal is -(sum of the FP32 couplings) for flux-difference
+  // systems (keeps the constant null space exact) or the rounded FP64
+  // diagonal otherwise
+  const int64_t N = ctx->N;
+  const int fb = FlatBlocks(N);
+  for (int q = 0; q < 3; ++q) {
+    KConvert<double, float><<<fb, kFlatThreads, 0, ctx->stream>>>(N, ctx->w[q], lv[0].w[q], 1.0);
+    APH_LAUNCHED(ctx);
+  }
+  if (!lv[0].diag) APH_TRY(Alloc(ctx, &lv[0].diag, N));
+  if (ctx->diag_explicit) {
+    KConvert<double, float><<<fb, kFlatThreads, 0, ctx->stream>>>(N, ctx->diag, lv[0].diag, 1.0);
+    APH_LAUNCHED(ctx);
+    const Op<float> A{lv[0].d, lv[0].w[0], lv[0].w[1], lv[0].w[2], lv[0].diag};
+    KInvDiag<float><<<TileGrid(ctx->d), TileBlock(), 0, ctx->stream>>>(A, lv[0].invdiag);
+    APH_LAUNCHED(ctx);
+  } else {
+    const Op<float> A{lv[0].d, lv[0].w[0], lv[0].w[1], lv[0].w[2], nullptr};
+    KInvDiag<float><<<TileGrid(ctx->d), TileBlock(), 0, ctx->stream>>>(A, lv[0].invdiag);
+    APH_LAUNCHED(ctx);
+  }
+  lv[0].has_diag = ctx->diag_explicit;
+  for (size_t l = 1; l < lv.size(); ++l) {
+    // coarse operators from the FP64 fine operator at level 1, FP32 below
+    if (l == 1) {
+      const Op<double> A = FineOp(ctx);
+      KCoarsenOp<double, float><<<TileGrid(lv[l].d), TileBlock(), 0, ctx->stream>>>(
+          A, lv[l].d, lv[l].w[0], lv[l].w[1], lv[l].w[2], lv[l].diag, lv[l].invdiag);
+    } else {
+      const Op<float> A = MakeOp(lv[l - 1]);
+      KCoarsenOp<float, float><<<TileGrid(lv[l].d), TileBlock(), 0, ctx->stream>>>(
+          A, lv[l].d, lv[l].w[0], lv[l].w[1], lv[l].w[2], lv[l].diag, lv[l].invdiag);
+    }
+    APH_LAUNCHED(ctx);
+  }
+  APH_TRY(EnsureCoarsestScratch(ctx, lv.back().d.cells()));
+  return APHGPU_OK;
+}
+
+// One V-cycle: lv[0].b -> lv[0].x (zero initial guess).
+template <class T>
+int VCycle(aphgpu_ctx* ctx, std::vector<Level<T>>& lv, int pre, int post,
+           const SolveScalars* s) {
+  const int L = (int)lv.size();
+  cudaStream_t st = ctx->stream;
+  for (int l = 0; l < L - 1; ++l) {
+    Level<T>& f = lv[l];
+    // the fine FP32 level keeps no diagonal array: diag = -(sum)
+    const Op<T> A = MakeOp(f);
+    for (int sw = 0; sw < pre; ++sw) {
+      KSmooth<T><<<TileGrid(f.d), TileBlock(), 0, st>>>(A, f.invdiag, f.b, f.x, 0, sw == 0, s);
+      APH_LAUNCHED(ctx);
+      KSmooth<T><<<TileGrid(f.d), TileBlock(), 0, st>>>(A, f.invdiag, f.b, f.x, 1, 0, s);
+      APH_LAUNCHED(ctx);
+    }
+    if (pre == 0) {
+      KSmooth<T><<<TileGrid(f.d), TileBlock(), 0, st>>>(A, f.invdiag, f.b, f.x, 0, 1, s);
+      APH_LAUNCHED(ctx);
+      KSmooth<T><<<TileGrid(f.d), TileBlock(), 0, st>>>(A, f.invdiag, f.b, f.x, 1, 1, s);
+      APH_LAUNCHED(ctx);
+    }
+    Level<T>& c = lv[l + 1];
+    KResidualRestrict<T, T><<<TileGrid(c.d), TileBlock(), 0, st>>>(A, f.b, f.x, c.d, c.b, s);
+    APH_LAUNCHED(ctx);
+  }
+  {
+    Level<T>& c = lv[L - 1];
+    const Op<T> A = MakeOp(c);
+    auto& mg = ctx->mg;
+    KCoarsestCG<T><<<1, 1024, 0, st>>>(A, c.b, c.x, mg.cr, mg.cp, mg.cap, mg.cx, s);
+    APH_LAUNCHED(ctx);
+  }
+  for (int l = L - 2; l >= 0; --l) {
+    Level<T>& f = lv[l];
+    Level<T>& c = lv[l + 1];
+    const Op<T> A = MakeOp(f);
+    KProlong<T, T><<<TileGrid(f.d), TileBlock(), 0, st>>>(f.d, f.x, c.d, c.x, s);
+    APH_LAUNCHED(ctx);
+    for (int sw = 0; sw < post; ++sw) {
+      KSmooth<T><<<TileGrid(f.d), TileBlock(), 0, st>>>(A, f.invdiag, f.b, f.x, 1, 0, s);
+      APH_LAUNCHED(ctx);
+      KSmooth<T><<<TileGrid(f.d), TileBlock(), 0, st>>>(A, f.invdiag, f.b, f.x, 0, 0, s);
+      APH_LAUNCHED(ctx);
+    }
+  }
+  return APHGPU_OK;
+}
+
+// Preconditioned CG on level 0 of `lv` with vectors x (solution, starting
+// from zero), r (holding b on entry), p, ap, z; scalars s.
+template <class T>
+int Pcg(aphgpu_ctx* ctx, std::vector<Level<T>>& lv, T* x, T* r, T* p, T* ap,
+        T* z, SolveScalars* s, const aphgpu_conf* conf, int check_every) {
+  Level<T>& f = lv[0];
+  const Dims d = f.d;
+  const Op<T> A = MakeOp(f);
+  cudaStream_t st = ctx->stream;
+  const dim3 tg = TileGrid(d), tb = TileBlock();
+  // z = M r ; p = z ; rz = r.z
+  f.b = r;
+  f.x = z;
+  APH_TRY(VCycle(ctx, lv, conf->mg_pre, conf->mg_post, s));
+  KDotRZ<T><<<tg, tb, 0, st>>>(d, r, z, s, ctx->red, 1);
+  APH_LAUNCHED(ctx);
+  KPcgP<T><<<tg, tb, 0, st>>>(d, z, p, s, 1);
+  APH_LAUNCHED(ctx);
+  // iterations are bounded on the device by maxiter (done flag); the host
+  // loop gives up after maxiter + 2 batches in any case
+  for (int batch = 0; batch <= conf->maxiter / check_every + 2; ++batch) {
+    for (int it = 0; it < check_every; ++it) {
+      KPcgApply<T><<<tg, tb, 0, st>>>(A, p, ap, s, ctx->red);
+      APH_LAUNCHED(ctx);
+      KPcgUpdate<T><<<tg, tb, 0, st>>>(d, x, r, p, ap, s, ctx->red);
+      APH_LAUNCHED(ctx);
+      APH_TRY(VCycle(ctx, lv, conf->mg_pre, conf->mg_post, s));
+      KDotRZ<T><<<tg, tb, 0, st>>>(d, r, z, s, ctx->red, 0);
+      APH_LAUNCHED(ctx);
+      KPcgP<T><<<tg, tb, 0, st>>>(d, z, p, s, 0);
+      APH_LAUNCHED(ctx);
+    }
+    SolveScalars hs;
+    APH_TRY(ReadScalars(ctx, s, &hs));
+    if (hs.done) break;
+  }
+  return APHGPU_OK;
+}
+
+}  // namespace
+
+// ---------------------------------------------------------------------------
+// Entry points used by api.cpp
+// ---------------------------------------------------------------------------
+
+int EnsureSolverVectors(aphgpu_ctx* ctx) {
+  if (ctx->r) return APHGPU_OK;
+  const int64_t N = ctx->N;
+  APH_TRY(Alloc(ctx, &ctx->r, N));
+  APH_TRY(Alloc(ctx, &ctx->p, N));
+  APH_TRY(Alloc(ctx, &ctx->ap, N));
+  APH_TRY(Alloc(ctx, &ctx->z, N));
+  APH_TRY(Alloc(ctx, &ctx->invdiag, N));
+  return APHGPU_OK;
+}
+
+int SetSystemExprDevice(aphgpu_ctx* ctx, const double* d_expr8) {
+  APH_TRY(EnsureSolverVectors(ctx));
+  if (!ctx->diag) APH_TRY(Alloc(ctx, &ctx->diag, ctx->N));
+  unsigned int* flags = ctx->flags;
+  APH_CUDA(ctx, cudaMemsetAsync(flags, 0, 2 * sizeof(unsigned), ctx->stream));
+  KExprToSystem<<<TileGrid(ctx->d), TileBlock(), 0, ctx->stream>>>(
+      ctx->d, d_expr8, ctx->w[0], ctx->w[1], ctx->w[2], ctx->diag, ctx->b, flags);
+  APH_LAUNCHED(ctx);
+  unsigned int hf[2] = {0, 0};
+  APH_CUDA(ctx, cudaMemcpyAsync(hf, flags, sizeof(hf), cudaMemcpyDeviceToHost, ctx->stream));
+  APH_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+  if (hf[0]) {
+    ctx->has_system = false;
+    return SetError(ctx, APHGPU_ERR_NOT_SYMMETRIC,
+                    "system is not symmetric in %u couplings", hf[0]);
+  }
+  ctx->diag_explicit = hf[1] != 0;
+  ctx->has_system = true;
+  ctx->has_proj = false;
+  ctx->mg.built64 = ctx->mg.built32 = false;
+  KInvDiag<double><<<TileGrid(ctx->d), TileBlock(), 0, ctx->stream>>>(FineOp(ctx), ctx->invdiag);
+  APH_LAUNCHED(ctx);
+  return APHGPU_OK;
+}
+
+int AssembleProjectionDevice(aphgpu_ctx* ctx, const double* d_alpha,
+                             double rho1, double rho2, const double* d_vflux,
+                             const double* d_febp, double dt, int remove_mean) {
+  APH_TRY(EnsureSolverVectors(ctx));
+  if (!ctx->vstar) APH_TRY(Alloc(ctx, &ctx->vstar, 3 * ctx->N));
+  KAssembleFaces<<<TileGrid(ctx->d), TileBlock(), 0, ctx->stream>>>(
+      ctx->d, d_alpha, rho1, rho2, d_vflux, d_febp, dt, ctx->h, ctx->w[0],
+      ctx->w[1], ctx->w[2], ctx->vstar);
+  APH_LAUNCHED(ctx);
+  double* sum = &ctx->scal->tmp[2];
+  KAssembleRhs<<<TileGrid(ctx->d), TileBlock(), 0, ctx->stream>>>(
+      ctx->d, ctx->vstar, ctx->b, ctx->red, sum);
+  APH_LAUNCHED(ctx);
+  if (remove_mean) {
+    KRemoveMean<<<FlatBlocks(ctx->N), kFlatThreads, 0, ctx->stream>>>(ctx->N, ctx->b, sum);
+    APH_LAUNCHED(ctx);
+  }
+  ctx->diag_explicit = false;
+  ctx->has_system = true;
+  ctx->has_proj = true;
+  ctx->mg.built64 = ctx->mg.built32 = false;
+  KInvDiag<double><<<TileGrid(ctx->d), TileBlock(), 0, ctx->stream>>>(FineOp(ctx), ctx->invdiag);
+  APH_LAUNCHED(ctx);
+  return APHGPU_OK;
+}
+
+int SolveCG(aphgpu_ctx* ctx, const aphgpu_conf* conf, aphgpu_info* info) {
+  const Op<double> A = FineOp(ctx);
+  const Dims d = ctx->d;
+  cudaStream_t st = ctx->stream;
+  const dim3 tg = TileGrid(d), tb = TileBlock();
+  APH_TRY(InitScalars(ctx, ctx->scal, conf, 1.0));
+  KCgInit<<<tg, tb, 0, st>>>(A, ctx->b, ctx->x, ctx->r, ctx->p, 0);
+  APH_LAUNCHED(ctx);
+  int batch = 4;
+  SolveScalars hs{};
+  int64_t launched = 0;
+  for (;;) {
+    for (int it = 0; it < batch; ++it) {
+      KCgApply<<<tg, tb, 0, st>>>(A, ctx->r, ctx->p, ctx->ap, ctx->scal, ctx->red);
+      APH_LAUNCHED(ctx);
+      KCgUpdate<<<tg, tb, 0, st>>>(d, ctx->x, ctx->r, ctx->p, ctx->ap, ctx->scal, ctx->red);
+      APH_LAUNCHED(ctx);
+      KCgP<<<tg, tb, 0, st>>>(d, ctx->r, ctx->p, ctx->scal);
+      APH_LAUNCHED(ctx);
+    }
+    APH_TRY(ReadScalars(ctx, ctx->scal, &hs));
+    launched += batch;
+    if (hs.done || launched > (int64_t)conf->maxiter + 2) break;
+    batch = std::min(batch * 2, 256);
+  }
+  info->residual = hs.residual;
+  info->iter = hs.iter;
+  info->inner_iter = 0;
+  info->converged = hs.converged;
+  return APHGPU_OK;
+}
+
+int SolveMGPCG(aphgpu_ctx* ctx, const aphgpu_conf* conf, aphgpu_info* info) {
+  auto& mg = ctx->mg;
+  if (!mg.built64) {
+    APH_TRY(BuildHierarchy<double>(ctx, mg.l64, conf->mg_coarse_max));
+    mg.built64 = true;
+  }
+  const Op<double> A = FineOp(ctx);
+  cudaStream_t st = ctx->stream;
+  APH_TRY(InitScalars(ctx, ctx->scal, conf, 1.0));
+  // r = b - A x0 (x holds the initial guess), then PCG on the correction
+  // would change the iterate; instead run PCG directly on x with r.
+  KResidual64<<<TileGrid(ctx->d), TileBlock(), 0, st>>>(A, ctx->b, ctx->x, ctx->r,
+                                                        ctx->scal, ctx->red, 0);
+  APH_LAUNCHED(ctx);
+  APH_TRY(Pcg<double>(ctx, mg.l64, ctx->x, ctx->r, ctx->p, ctx->ap, ctx->z,
+                      ctx->scal, conf, 2));
+  SolveScalars hs;
+  APH_TRY(ReadScalars(ctx, ctx->scal, &hs));
+  info->residual = hs.residual;
+  info->iter = hs.iter;
+  info->inner_iter = 0;
+  info->converged = hs.converged;
+  return APHGPU_OK;
+}
+
+int SolveMixed(aphgpu_ctx* ctx, const aphgpu_conf* conf, aphgpu_info* info) {
+  auto& mg = ctx->mg;
+  const int64_t N = ctx->N;
+  if (!ctx->r32) {
+    APH_TRY(Alloc(ctx, &ctx->r32, N));
+    APH_TRY(Alloc(ctx, &ctx->x32, N));
+    APH_TRY(Alloc(ctx, &ctx->p32, N));
+    APH_TRY(Alloc(ctx, &ctx->ap32, N));
+    APH_TRY(Alloc(ctx, &ctx->z32, N));
+  }
+  if (!mg.built32) {
+    APH_TRY(BuildHierarchy<float>(ctx, mg.l32, conf->mg_coarse_max));
+    mg.built32 = true;
+  }
+  const Op<double> A = FineOp(ctx);
+  cudaStream_t st = ctx->stream;
+  const int fb = FlatBlocks(N);
+  APH_TRY(InitScalars(ctx, ctx->scal, conf, 1.0));
+  SolveScalars hs{};
+  int outer = 0, inner_total = 0;
+  aphgpu_conf ic = *conf;
+  for (;;) {
+    // outer residual in FP64 and the stopping test (count as iteration)
+    KResidual64<<<TileGrid(ctx->d), TileBlock(), 0, st>>>(A, ctx->b, ctx->x, ctx->r,
+                                                          ctx->scal, ctx->red, 1);
+    APH_LAUNCHED(ctx);
+    APH_TRY(ReadScalars(ctx, ctx->scal, &hs));
+    if (hs.done || (outer >= conf->miniter && hs.residual < conf->tol)) {
+      hs.converged = hs.residual < conf->tol;
+      break;
+    }
+    if (outer > conf->maxiter) break;
+    // inner FP32 MG-PCG on A e = r / max|r|
+    KScaleResidual<<<fb, kFlatThreads, 0, st>>>(N, ctx->r, ctx->r32, ctx->scal);
+    APH_LAUNCHED(ctx);
+    KZeroF<<<fb, kFlatThreads, 0, st>>>(N, ctx->x32);
+    APH_LAUNCHED(ctx);
+    // inner stopping: residual (of the scaled system, L2 over cells) below
+    // inner_rtol times its initial value
+    const double scale = hs.maxr > 0 ? hs.maxr : 1.0;
+    const double r0 = std::sqrt(hs.rr / (ctx->h * ctx->h * ctx->h)) / scale;
+    ic.tol = conf->inner_rtol * r0;
+    ic.miniter = 1;
+    ic.maxiter = conf->inner_maxiter;
+    ic.maxnorm = 0;
+    APH_TRY(InitScalars(ctx, ctx->scal2, &ic, 1.0));
+    APH_TRY(Pcg<float>(ctx, mg.l32, ctx->x32, ctx->r32, ctx->p32, ctx->ap32,
+                       ctx->z32, ctx->scal2, &ic, 2));
+    SolveScalars is;
+    APH_TRY(ReadScalars(ctx, ctx->scal2, &is));
+    inner_total += is.iter;
+    KAddCorrection<<<fb, kFlatThreads, 0, st>>>(N, ctx->x, ctx->x32, ctx->scal);
+    APH_LAUNCHED(ctx);
+    ++outer;
+    // iteration count of the outer loop lives in scal->iter
+    SolveScalars up = hs;
+    up.iter = outer;
+    up.done = 0;
+    APH_CUDA(ctx, cudaMemcpyAsync(&ctx->scal->iter, &up.iter, sizeof(int),
+                                  cudaMemcpyHostToDevice, st));
+  }
+  info->residual = hs.residual;
+  info->iter = outer;
+  info->inner_iter = inner_total;
+  info->converged = hs.converged;
+  return APHGPU_OK;
+}
+
+int SystemToExprDevice(aphgpu_ctx* ctx, double* d_e8) {
+  KSystemToExpr<<<TileGrid(ctx->d), TileBlock(), 0, ctx->stream>>>(FineOp(ctx), ctx->b, d_e8);
+  APH_LAUNCHED(ctx);
+  return APHGPU_OK;
+}
+
+// Times one solver kernel on the resident data (see aphgpu_time_kernel).
+int TimeSolverKernel(aphgpu_ctx* ctx, int kernel, int reps, double* ms,
+                     double* bytes) {
+  cudaStream_t st = ctx->stream;
+  const Dims d = ctx->d;
+  const double N = (double)ctx->N;
+  auto& mg = ctx->mg;
+  std::function<void()> launch;
+  double b = 0;
+  switch (kernel) {
+    case APHGPU_K_SMOOTH32: {
+      if (!mg.built32 || !ctx->r32)
+        return SetError(ctx, APHGPU_ERR_STATE, "run a mixed solve first");
+      Level<float>& f = mg.l32[0];
+      const Op<float> A = MakeOp(f);
+      float* bb = ctx->r32;
+      float* x = ctx->z32;
+      launch = [=]() {
+        KSmooth<float><<<TileGrid(d), TileBlock(), 0, st>>>(A, f.invdiag, bb, x, 0, 0, nullptr);
+      };
+      // x read 4 + couplings 12 + half of (b 4, invdiag 4, x write 4)
+      b = N * (4 + 12 + 0.5 * 12);
+      break;
+    }
+    case APHGPU_K_SMOOTH64: {
+      if (!mg.built64) return SetError(ctx, APHGPU_ERR_STATE, "run an MG-PCG solve first");
+      Level<double>& f = mg.l64[0];
+      const Op<double> A = MakeOp(f);
+      const double* iv = ctx->invdiag;
+      double* bb = ctx->r;
+      double* x = ctx->z;
+      launch = [=]() {
+        KSmooth<double><<<TileGrid(d), TileBlock(), 0, st>>>(A, iv, bb, x, 0, 0, nullptr);
+      };
+      b = N * (8 + 24 + 0.5 * 24);
+      break;
+    }
+    case APHGPU_K_APPLY64: {
+      const Op<double> A = FineOp(ctx);
+      SolveScalars* s = ctx->scal2;
+      RedBuf rb = ctx->red;
+      const double* p = ctx->p;
+      double* ap = ctx->ap;
+      APH_CUDA(ctx, cudaMemsetAsync(s, 0, sizeof(SolveScalars), st));
+      launch = [=]() { KPcgApply<double><<<TileGrid(d), TileBlock(), 0, st>>>(A, p, ap, s, rb); };
+      b = N * (8 + 24 + 8);
+      break;
+    }
+    case APHGPU_K_APPLY32: {
+      if (!mg.built32 || !ctx->r32)
+        return SetError(ctx, APHGPU_ERR_STATE, "run a mixed solve first");
+      const Op<float> A = MakeOp(mg.l32[0]);
+      SolveScalars* s = ctx->scal2;
+      RedBuf rb = ctx->red;
+      const float* p = ctx->p32;
+      float* ap = ctx->ap32;
+      APH_CUDA(ctx, cudaMemsetAsync(s, 0, sizeof(SolveScalars), st));
+      launch = [=]() { KPcgApply<float><<<TileGrid(d), TileBlock(), 0, st>>>(A, p, ap, s, rb); };
+      b = N * (4 + 12 + 4);
+      break;
+    }
+    case APHGPU_K_RESTRICT32: {
+      if (!mg.built32 || mg.l32.size() < 2 || !ctx->r32)
+        return SetError(ctx, APHGPU_ERR_STATE, "run a mixed solve first");
+      Level<float>& f = mg.l32[0];
+      Level<float>& c = mg.l32[1];
+      const Op<float> A = MakeOp(f);
+      const float* bb = ctx->r32;
+      const float* x = ctx->z32;
+      launch = [=]() {
+        KResidualRestrict<float, float><<<TileGrid(c.d), TileBlock(), 0, st>>>(A, bb, x, c.d, c.b, nullptr);
+      };
+      b = N * (4 + 4 + 12) + N / 8 * 4;
+      break;
+    }
+    default:
+      return SetError(ctx, APHGPU_ERR_ARG, "unknown kernel %d", kernel);
+  }
+  launch();  // warm-up
+  APH_LAUNCHED(ctx);
+  APH_CUDA(ctx, cudaEventRecord(ctx->ev0, st));
+  for (int r = 0; r < reps; ++r) launch();
+  APH_LAUNCHED(ctx);
+  APH_CUDA(ctx, cudaEventRecord(ctx->ev1, st));
+  APH_CUDA(ctx, cudaEventSynchronize(ctx->ev1));
+  float t = 0;
+  APH_CUDA(ctx, cudaEventElapsedTime(&t, ctx->ev0, ctx->ev1));
+  *ms = (double)t / reps;
+  *bytes = b;
+  return APHGPU_OK;
+}
+
+int ResidualNorms(aphgpu_ctx* ctx, double* rnorm, double* bnorm) {
+  aphgpu_conf c;
+  aphgpu_conf_default(&c);
+  APH_TRY(InitScalars(ctx, ctx->scal2, &c, 1.0));
+  KResidual64<<<TileGrid(ctx->d), TileBlock(), 0, ctx->stream>>>(
+      FineOp(ctx), ctx->b, ctx->x, nullptr, ctx->scal2, ctx->red, 0);
+  APH_LAUNCHED(ctx);
+  SolveScalars hs;
+  APH_TRY(ReadScalars(ctx, ctx->scal2, &hs));
+  if (rnorm) *rnorm = std::sqrt(hs.rr);
+  if (bnorm) *bnorm = std::sqrt(hs.tmp[0]);
+  return APHGPU_OK;
+}
+
+int FluxCorrect(aphgpu_ctx* ctx, double* d_out) {
+  KFluxCorrect<<<TileGrid(ctx->d), TileBlock(), 0, ctx->stream>>>(
+      ctx->d, ctx->w[0], ctx->w[1], ctx->w[2], ctx->x, ctx->vstar, d_out);
+  APH_LAUNCHED(ctx);
+  return APHGPU_OK;
+}
+
+int Acceleration(aphgpu_ctx* ctx, double* d_acc, const double* d_alpha,
+                 double rho1, double rho2) {
+  KAcceleration<<<TileGrid(ctx->d), TileBlock(), 0, ctx->stream>>>(
+      ctx->d, ctx->h, ctx->x, d_alpha, rho1, rho2,
+      ctx->proj_force ? ctx->febp : nullptr, d_acc);
+  APH_LAUNCHED(ctx);
+  return APHGPU_OK;
+}
+
+}  // namespace aphgpu

@@ -1,0 +1,449 @@
+"""Benchmark of the projection-step pressure solve on GB300.
+
+Headline metric: Poisson solves/s at ||r||/||b|| = 1e-10 on the 512^3
+mixed-precision configuration (64 gas bubbles, density ratio 1000), with the
+plain FP64 multigrid solver on the same system beside it, and p50/p99 of the
+per-solve latency.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+                    [--workload c3|c2|c1]
+
+One step = one solve of the resident system from a zero initial guess.  The
+inputs (1 GB per FP64 field) are far larger than the 129 MB L2, so no flush
+is needed between steps.  `value` is device-timed (CUDA events on the
+library's stream); `e2e` goes through the C ABI drop-in with host buffers:
+the 8-coefficient Expr system (64 B/cell) copied from pinned host memory,
+the solve, and the pressure copied back, every step.
+
+N > 1 runs independent replicas (one per GPU, no collective on the data
+path): every rank solves its own copy; value = all ranks' solves / max time.
+
+--impl reference times the reference algorithm's CPU implementation on the
+host cores (the C restatement of aphros's SolverConjugate in oracle/, since
+the reference tree is not available where this runs) on bounded samples.
+"""
+import argparse
+import ctypes
+import json
+import math
+import os
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+if ROOT not in sys.path:
+    sys.path.insert(0, ROOT)
+
+METRIC = "Poisson solves/s at 1e-10 rel. residual (mixed vs FP64, same GB300); p50/p99 step latency"
+UNIT = "solves/s"
+
+WORKLOADS = {
+    "c3": "mixed-precision solve, 512^3 periodic cube, 64 gas spheres r in [0.02,0.05], "
+          "density ratio 1000, Taylor-Green + N(0,0.01) face noise, rel. residual 1e-10",
+    "c2": "256^3 periodic cube, 16 gas spheres r in [0.03,0.08], density ratio 1000, "
+          "rel. residual 1e-10",
+    "c1": "64^3 periodic cube, one sphere r=0.2, density ratio 1000, rel. residual 1e-10",
+}
+
+
+# ---------------------------------------------------------------------------
+# multi-rank helpers (replicas only)
+# ---------------------------------------------------------------------------
+
+def dist_env():
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", str(rank)))
+    return rank, world, local
+
+
+def replica_share(rank, world, units):
+    """Units of a job split over `world` replicas: (this rank's count,
+    first unit index)."""
+    base, extra = divmod(units, world)
+    count = base + (1 if rank < extra else 0)
+    return count, rank * base + min(rank, extra)
+
+
+def aggregate_over_ranks(units, seconds):
+    """(sum of units, max of seconds) over ranks (identity when not
+    distributed)."""
+    try:
+        import torch
+        import torch.distributed as dist
+    except ImportError:
+        return units, seconds
+    if not (dist.is_available() and dist.is_initialized()):
+        return units, seconds
+    dev = "cuda" if dist.get_backend() == "nccl" else "cpu"
+    u = torch.tensor([float(units)], dtype=torch.float64, device=dev)
+    s = torch.tensor([float(seconds)], dtype=torch.float64, device=dev)
+    dist.all_reduce(u, op=dist.ReduceOp.SUM)
+    dist.all_reduce(s, op=dist.ReduceOp.MAX)
+    return int(round(u.item())), s.item()
+
+
+def barrier():
+    try:
+        import torch.distributed as dist
+        if dist.is_available() and dist.is_initialized():
+            dist.barrier()
+    except ImportError:
+        pass
+
+
+# ---------------------------------------------------------------------------
+# clocks
+# ---------------------------------------------------------------------------
+
+class ClockSampler:
+    """nvidia-smi samples every 200 ms while the timed region runs."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device):
+        self.device = device
+        self.rows = []
+        self._stop = threading.Event()
+        self._t = None
+
+    def _run(self):
+        while not self._stop.is_set():
+            try:
+                out = subprocess.run(
+                    ["nvidia-smi", "-i", str(self.device), "--query-gpu=" + self.Q,
+                     "--format=csv,noheader,nounits"],
+                    capture_output=True, text=True, timeout=5).stdout.strip()
+                if out:
+                    self.rows.append([v.strip() for v in out.split(",")])
+            except Exception:
+                pass
+            self._stop.wait(0.2)
+
+    def __enter__(self):
+        self._t = threading.Thread(target=self._run, daemon=True)
+        self._t.start()
+        return self
+
+    def __exit__(self, *a):
+        self._stop.set()
+        if self._t:
+            self._t.join(timeout=10)
+
+    def summary(self):
+        if not self.rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
+        sm = [float(r[1]) for r in self.rows if r[1].replace(".", "").isdigit()]
+        mx = [float(r[2]) for r in self.rows if r[2].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = set()
+        for r in self.rows:
+            for i, nm in enumerate(names):
+                if len(r) > 5 + i and r[5 + i].lower() == "active":
+                    reasons.add(nm)
+        return {"sm_mhz": float(np.median(sm)) if sm else None,
+                "sm_max_mhz": max(mx) if mx else None,
+                "reasons": sorted(reasons), "samples": len(self.rows)}
+
+
+# ---------------------------------------------------------------------------
+# helpers
+# ---------------------------------------------------------------------------
+
+def measured_peak_gbs():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    try:
+        with open(p) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+def ncu_traffic(kernel_name, cells):
+    """DRAM bytes per launch of the kernel from the committed ncu summary
+    (profiles/traffic.json: bytes per cell of one launch, measured by ncu on
+    a smaller grid of the same kernel), scaled to `cells`; None if absent."""
+    p = os.path.join(ROOT, "profiles", "traffic.json")
+    try:
+        with open(p) as f:
+            d = json.load(f)
+        return float(d[kernel_name]["dram_bytes_per_cell"]) * cells
+    except Exception:
+        return None
+
+
+def rel_l2(a, b):
+    a = a - a.mean()
+    b = b - b.mean()
+    return float(np.linalg.norm(a - b) / max(np.linalg.norm(b), 1e-300))
+
+
+def pinned(count):
+    import torch
+    return torch.empty(count, dtype=torch.float64, pin_memory=True)
+
+
+def cpu_baseline(case, expr8_np, threads, budget_s=15.0, cg_iters_full=None):
+    """Times the oracle's CG (aphros's SolverConjugate algorithm) on the host
+    cores for a bounded number of iterations; solves/s extrapolated with the
+    iteration count of a full CG solve (`cg_iters_full`)."""
+    import oracle
+    n = case.n
+    # one iteration first to size the sample
+    t1 = oracle.cg_time_iters(n, expr8_np, 1, threads)
+    iters = max(2, min(50, int(budget_s / max(t1, 1e-6))))
+    t = oracle.cg_time_iters(n, expr8_np, iters, threads)
+    per_iter = t / iters
+    out = {"per_iter_s": per_iter, "iters_sampled": iters}
+    if cg_iters_full:
+        out["value"] = 1.0 / (per_iter * cg_iters_full)
+        out["cg_iters_full"] = cg_iters_full
+    return out
+
+
+def cg_iterations_estimate(case_name, n_full, device):
+    """Iterations aphros's CG needs on this bubble field at ||r||/||b||=1e-10:
+    measured with the GPU plain CG on the same field at n_full/4 and scaled
+    by 4 (CG iterations grow linearly with the grid edge)."""
+    from aphros_gb300 import _lib, workload
+    n = max(32, n_full // 4)
+    case = workload.config(case_name, n=n)
+    ctx = _lib.Context(n, case.h, device)
+    ctx.assemble_projection(case.alpha, case.rho1, case.rho2, case.flux, case.dt)
+    _, b = ctx.residual_norms()
+    tol = 1e-10 * b / math.sqrt(case.h ** 3)
+    _, info = ctx.solve(_lib.default_conf(solver=_lib.SOLVER_CG, tol=tol,
+                                          maxiter=200000), out=False)
+    ctx.close()
+    return int(info.iter * (n_full / n)), int(info.iter), n
+
+
+# ---------------------------------------------------------------------------
+# arms
+# ---------------------------------------------------------------------------
+
+def run_ours(args):
+    import torch
+    from aphros_gb300 import _lib, workload
+
+    rank, world, local = dist_env()
+    if world > 1:
+        import torch.distributed as dist
+        torch.cuda.set_device(local)
+        dist.init_process_group("nccl")
+    device = local
+    case = workload.config(args.workload)
+    N = case.N
+    ctx = _lib.Context(case.n, case.h, device)
+    ctx.assemble_projection(case.alpha, case.rho1, case.rho2, case.flux, case.dt)
+    _, bnorm = ctx.residual_norms()
+    tol = 1e-10 * bnorm / math.sqrt(case.h ** 3)
+    conf_mixed = _lib.default_conf(solver=_lib.SOLVER_MIXED, tol=tol, maxiter=100)
+    conf_fp64 = _lib.default_conf(solver=_lib.SOLVER_MGPCG, tol=tol, maxiter=1000)
+
+    def run_steps(conf, k, collect):
+        times, launches, infos = [], 0, []
+        ctx.mark(0)
+        for _ in range(k):
+            info = ctx.solve_resident(conf, zero_guess=True)
+            ms, nl = ctx.last_timing()
+            if collect:
+                times.append(ms)
+                launches += nl
+                infos.append(info)
+        ctx.mark(1)
+        total_ms = ctx.elapsed(0, 1)
+        return total_ms, times, launches, infos
+
+    # warm-up (builds both hierarchies)
+    for conf in (conf_mixed, conf_fp64):
+        run_steps(conf, args.warmup, False)
+    torch.cuda.synchronize(device)
+    barrier()
+    sampler = ClockSampler(device)
+    with sampler:
+        torch.cuda.synchronize(device)
+        barrier()
+        t_mixed, st_mixed, l_mixed, inf_mixed = run_steps(conf_mixed, args.steps, True)
+        torch.cuda.synchronize(device)
+        barrier()
+    p_mixed = ctx.get_solution()
+    rn, bn = ctx.residual_norms()
+    rel_res_mixed = rn / bn
+    t_fp64, st_fp64, l_fp64, inf_fp64 = run_steps(conf_fp64, args.steps, True)
+    p_fp64 = ctx.get_solution()
+    rn64, _ = ctx.residual_norms()
+    units, tmax = aggregate_over_ranks(args.steps, t_mixed / 1000.0)
+    units64, tmax64 = aggregate_over_ranks(args.steps, t_fp64 / 1000.0)
+    value = units / tmax
+    fp64_value = units64 / tmax64
+
+    # live roofline of the dominant kernel of the mixed solve
+    peak, peak_kind = measured_peak_gbs()
+    kms, kbytes = ctx.time_kernel(_lib.K_SMOOTH32, reps=20)
+    achieved = kbytes / (kms * 1e-3) / 1e9
+    kernel_table = {}
+    for kid in (_lib.K_SMOOTH32, _lib.K_APPLY32, _lib.K_RESTRICT32,
+                _lib.K_APPLY64, _lib.K_SMOOTH64):
+        try:
+            ms_k, b_k = ctx.time_kernel(kid, reps=10)
+            kernel_table[_lib.KERNEL_NAMES[kid]] = {
+                "ms": round(ms_k, 4), "GB/s": round(b_k / (ms_k * 1e-3) / 1e9, 1),
+                "frac": round(b_k / (ms_k * 1e-3) / 1e9 / peak, 3)}
+        except _lib.AphgpuError:
+            pass
+
+    # end to end through the drop-in with host buffers (pinned)
+    e2e = None
+    if not args.no_e2e:
+        expr = pinned(8 * N)
+        xout = pinned(N)
+        ctx._check(ctx._L.aphgpu_get_system_expr(ctx.handle, expr.data_ptr()))
+        e2e_steps = max(1, min(args.steps, 5))
+        info = _lib.Info()
+        t0 = time.perf_counter()
+        for _ in range(e2e_steps):
+            ctx._check(ctx._L.aphgpu_set_system_expr(ctx.handle, expr.data_ptr()))
+            ctx._check(ctx._L.aphgpu_solve(ctx.handle, ctypes.byref(conf_mixed), None,
+                                           xout.data_ptr(), ctypes.byref(info)))
+        t1 = time.perf_counter()
+        eu, et = aggregate_over_ranks(e2e_steps, t1 - t0)
+        e2e = {"value": eu / et, "unit": UNIT, "h2d_bytes_per_step": 8 * 8 * N,
+               "d2h_bytes_per_step": 8 * N, "steps": e2e_steps,
+               "path": "aphgpu_set_system_expr + aphgpu_solve (linear::Solver drop-in), "
+                       "pinned host buffers"}
+
+    cpu = None
+    if rank == 0 and not args.no_cpu:
+        threads = os.cpu_count() or 1
+        iters_full, iters_small, n_small = cg_iterations_estimate(args.workload, case.n, device)
+        expr_np = np.empty(8 * N)
+        ctx._check(ctx._L.aphgpu_get_system_expr(ctx.handle, _lib.ptr(expr_np)))
+        cb = cpu_baseline(case, expr_np, threads, budget_s=args.cpu_budget,
+                          cg_iters_full=iters_full)
+        cpu = {"value": cb.get("value"), "unit": UNIT, "cores": threads, "kind": "port",
+               "sample": "%d CG iterations of the C restatement of aphros SolverConjugate "
+                         "on the %d^3 system (%.3f s/iter, %d threads); full solve = %d "
+                         "iterations, from a GPU plain-CG solve of the same bubble field at "
+                         "%d^3 (%d iterations) scaled by the grid ratio"
+                         % (cb["iters_sampled"], case.n, cb["per_iter_s"], threads,
+                            iters_full, n_small, iters_small, )}
+
+    if rank != 0:
+        return None
+    lat = np.array(st_mixed)
+    line = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": float(t_mixed / args.steps),
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f32 multigrid in f64 defect correction (f64 residual, update, norms, coarsest solve)",
+        "data": "synthetic (seeded bubble field, Taylor-Green + noise)",
+        "config": {"workload": WORKLOADS[args.workload], "cells": N,
+                   "grid": [case.n] * 3, "bubbles": int(len(case.radii)),
+                   "density_ratio": case.rho1 / case.rho2,
+                   "l2": "inputs larger than L2 (1 GB per FP64 field), no flush",
+                   "parallelism": "replicas" if world > 1 else "single GPU"},
+        "p50_ms": float(np.percentile(lat, 50)), "p99_ms": float(np.percentile(lat, 99)),
+        "fp64": {"value": fp64_value, "unit": UNIT,
+                 "ms_per_step": float(t_fp64 / args.steps),
+                 "p50_ms": float(np.percentile(st_fp64, 50)),
+                 "p99_ms": float(np.percentile(st_fp64, 99)),
+                 "iters": inf_fp64[-1].iter if inf_fp64 else None},
+        "mixed_over_fp64": value / fp64_value,
+        "iters": {"outer": inf_mixed[-1].iter, "inner_fp32_pcg": inf_mixed[-1].inner_iter},
+        "rel_residual": rel_res_mixed,
+        "pressure_rel_err_vs_fp64": rel_l2(p_mixed, p_fp64),
+        "cells_per_s": value * N,
+        "roofline": {"bound": "hbm", "kernel": "KSmooth<float> (red-black half sweep, finest level)",
+                     "achieved": achieved, "peak": peak, "unit": "GB/s",
+                     "frac": achieved / peak, "peak_kind": peak_kind,
+                     "traffic": ncu_traffic("KSmooth<float>", N)},
+        "kernels": kernel_table,
+        "gpu_launches": int(l_mixed),
+        "e2e": e2e,
+        "cpu_baseline": cpu,
+        "clocks": sampler.summary(),
+    }
+    return line
+
+
+def run_reference(args):
+    """aphros's CG algorithm (oracle restatement) on the host cores."""
+    rank, world, _ = dist_env()
+    if rank != 0:
+        return None
+    import oracle
+    from aphros_gb300 import workload
+    case = workload.config(args.workload)
+    n, h = case.n, case.h
+    threads = os.cpu_count() or 1
+    e, _, _ = oracle.assemble_projection(n, h, case.dt, case.alpha, case.rho1,
+                                         case.rho2, case.flux)
+    # iterations of a full solve: measured on the CPU at n/8 (bounded time)
+    # and scaled with the grid edge
+    ns = max(16, n // 8)
+    cs = workload.config(args.workload, n=ns)
+    es, _, _ = oracle.assemble_projection(ns, cs.h, cs.dt, cs.alpha, cs.rho1, cs.rho2,
+                                          cs.flux)
+    _, info = oracle.cg_solve(ns, cs.h, es, oracle.rel_tol(es, cs.h, 1e-10),
+                              nthreads=threads)
+    iters_full = int(info.iter * n / ns)
+    per = []
+    for _ in range(args.warmup):
+        oracle.cg_time_iters(n, e, 1, threads)
+    sample_iters = 3
+    for _ in range(args.steps):
+        t = oracle.cg_time_iters(n, e, sample_iters, threads)
+        per.append(t / sample_iters)
+    per_iter = float(np.median(per))
+    value = 1.0 / (per_iter * iters_full)
+    return {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": per_iter * 1e3 * sample_iters,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f64", "data": "synthetic (seeded bubble field, Taylor-Green + noise)",
+        "config": {"workload": WORKLOADS[args.workload], "cells": case.N},
+        "impl": "reference",
+        "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port",
+                         "sample": "each step %d CG iterations at %d^3 (C restatement of "
+                                   "aphros SolverConjugate, %d threads); full solve %d "
+                                   "iterations (CPU CG at %d^3: %d, scaled)"
+                                   % (sample_iters, n, threads, iters_full, ns, info.iter)},
+        "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0,
+                "d2h_bytes_per_step": 0},
+    }
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--workload", choices=sorted(WORKLOADS), default="c3")
+    ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--cpu-budget", type=float, default=15.0)
+    args = ap.parse_args()
+    if args.warmup < 3:
+        args.warmup = 3
+    if args.impl == "reference":
+        line = run_reference(args)
+    else:
+        from aphros_gb300 import build
+        build.build()
+        line = run_ours(args)
+    if line is not None:
+        print(json.dumps(line), flush=True)
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,234 @@
+/*
+ * aphgpu: GB300-native (sm_103a) projection-step hot path of the aphros
+ * multiphase flow solver, behind a plain C ABI.
+ *
+ * One context (`aphgpu_ctx`) owns one periodic Cartesian domain of
+ * nx*ny*nz cells of size h resident on one GPU, with its own CUDA stream.
+ * Host arrays are x-fastest over the domain's cells (no halo cells), i.e.
+ * FieldCell values in the order of aphros's GIndex (geom/block.h:149-158).
+ * Face arrays hold three consecutive blocks (x, y, z faces) of nx*ny*nz
+ * values; entry c of block d is the face between cell c-e_d and cell c.
+ * Vector cell fields (normals) are AoS, 3 doubles per cell (FieldCell<Vect>).
+ *
+ * Every entry point returns APHGPU_OK (0) or an error code; the message of
+ * the last error of a context is returned by aphgpu_last_error().  No C++
+ * exception crosses this boundary.  All calls on one context must come from
+ * one host thread at a time.  Unless stated otherwise a call returns after
+ * its results are complete (host output arrays filled).
+ */
+#ifndef APHGPU_H_
+#define APHGPU_H_
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct aphgpu_ctx aphgpu_ctx;
+
+enum {
+  APHGPU_OK = 0,
+  APHGPU_ERR_ARG = 1,          /* invalid argument */
+  APHGPU_ERR_CUDA = 2,         /* CUDA runtime error */
+  APHGPU_ERR_NOMEM = 3,        /* device allocation failed */
+  APHGPU_ERR_NOT_SYMMETRIC = 4,/* system handed to a symmetric solver is not */
+  APHGPU_ERR_STATE = 5,        /* call order violated (e.g. no system set) */
+  APHGPU_ERR_UNSUPPORTED = 6   /* grid shape not supported by the solver */
+};
+
+/* Solver kinds (the `linsolver_symm` values `gpu_cg`, `gpu`, `gpu_mixed`). */
+enum {
+  APHGPU_SOLVER_CG = 0,    /* plain FP64 CG, the algorithm of SolverConjugate */
+  APHGPU_SOLVER_MGPCG = 1, /* FP64 CG preconditioned by an FP64 MG V-cycle */
+  APHGPU_SOLVER_MIXED = 2  /* FP64 defect correction around FP32 MG-PCG */
+};
+
+/* Stopping rule and limits; mirrors linear::Solver::Conf
+ * (src/linear/linear.h:21-25) plus the norm choice of
+ * SolverConjugate::Extra (linear.h:85-87). */
+typedef struct {
+  int solver;        /* APHGPU_SOLVER_* */
+  double tol;        /* absolute tolerance on the residual norm below */
+  int miniter;       /* minimum iterations (reference default 1) */
+  int maxiter;       /* maximum iterations */
+  int maxnorm;       /* 0: sqrt(sum r^2 / h^3), 1: max|r| / h^3 */
+  /* multigrid (ignored by APHGPU_SOLVER_CG) */
+  int mg_pre;        /* red-black Gauss-Seidel sweeps before restriction */
+  int mg_post;       /* sweeps after prolongation */
+  int mg_coarse_max; /* largest coarsest-level cell count (<= 4096) */
+  /* mixed precision: relative reduction asked of each inner FP32 solve */
+  double inner_rtol;
+  int inner_maxiter;
+} aphgpu_conf;
+
+/* Result; mirrors linear::Solver::Info (linear.h:27-30).  `iter` counts
+ * outer iterations; for APHGPU_SOLVER_MIXED `inner_iter` is the total
+ * number of FP32 PCG iterations. */
+typedef struct {
+  double residual;
+  int iter;
+  int inner_iter;
+  int converged;
+} aphgpu_info;
+
+/* Fills `conf` with defaults: MG-PCG, tol 0, miniter 1, maxiter 1000,
+ * L2 norm, 2+2 sweeps, coarsest <= 512 cells, inner_rtol 1e-4. */
+void aphgpu_conf_default(aphgpu_conf* conf);
+
+/* ---- context ---- */
+
+/* Creates a context for a periodic nx*ny*nz domain of cubic cells of edge h
+ * on CUDA device `device`.  Replaces the per-mesh device state that
+ * SolverConjugateCL keeps in its Shared struct
+ * (src/linear/conjugate_cl.ipp:155-187). */
+int aphgpu_create(aphgpu_ctx** ctx, int nx, int ny, int nz, double h,
+                  int device);
+void aphgpu_destroy(aphgpu_ctx* ctx);
+const char* aphgpu_last_error(const aphgpu_ctx* ctx);
+/* Bytes of device memory held by the context. */
+int64_t aphgpu_device_bytes(const aphgpu_ctx* ctx);
+/* Waits for all work of the context. */
+int aphgpu_sync(aphgpu_ctx* ctx);
+
+/* ---- Poisson / projection ---- */
+
+/* Sets the linear system from aphros's per-cell expressions
+ * e[0]*x[c] + sum_q e[1+q]*x[nb_q] + e[7] = 0, q = xm,xp,ym,yp,zm,zp,
+ * 8 doubles per cell (FieldCell<Expr>, src/geom/mesh.h:481-485), the input
+ * of linear::Solver::Solve (src/linear/linear.h:44-46).  The system must be
+ * symmetric (e[2] of c equals e[1] of c+x, etc.), as CG requires. */
+int aphgpu_set_system_expr(aphgpu_ctx* ctx, const double* expr8);
+
+/* Copies the current system back as per-cell expressions (8 doubles per
+ * cell, the layout of aphgpu_set_system_expr), e.g. to inspect the system
+ * assembled by aphgpu_assemble_projection. */
+int aphgpu_get_system_expr(aphgpu_ctx* ctx, double* expr8);
+
+/* Assembles the projection system on the device from the gas volume
+ * fraction and the predicted face fluxes, fusing
+ *   Hydro::CalcMixture density (src/kernel/hydro.ipp:1815-1822),
+ *   UEmbed::InterpolateHarmonic face density (src/solver/approx_eb.h:351-363),
+ *   the surface-tension face force term (src/solver/proj.ipp:556-562),
+ *   Proj::GetFlux and Proj::GetFluxSum (src/solver/proj.ipp:343-383).
+ * alpha: nx*ny*nz, or NULL to use the resident VOF volume fraction;
+ * vflux: 3 face blocks (u*.S); febp: face force per unit volume (NULL: none,
+ * or the resident surface-tension force after aphgpu_set_force_resident);
+ * dt: time step; remove_mean: subtract the mean of the constant term
+ * (src/solver/pois.h:41-47).  The fluxes stay resident for
+ * aphgpu_flux_correct(). */
+int aphgpu_assemble_projection(aphgpu_ctx* ctx, const double* alpha,
+                               double rho1, double rho2, const double* vflux,
+                               const double* febp, double dt, int remove_mean);
+
+/* Solves the current system: the drop-in for linear::Solver::Solve
+ * (src/linear/linear.h:44-46) as used by Proj::Project
+ * (src/solver/proj.ipp:396-398).  x0: initial guess (NULL: zero, may equal
+ * x); x: solution (NULL: keep it resident only).  Non-convergence is not an
+ * error: info->converged = 0 and info->iter > maxiter, like CG. */
+int aphgpu_solve(aphgpu_ctx* ctx, const aphgpu_conf* conf, const double* x0,
+                 double* x, aphgpu_info* info);
+
+/* Solves with the resident solution as initial guess (zero_guess = 0) or
+ * from zero, leaving the solution resident. */
+int aphgpu_solve_resident(aphgpu_ctx* ctx, const aphgpu_conf* conf,
+                          int zero_guess, aphgpu_info* info);
+
+/* Copies the resident solution (pressure) to the host. */
+int aphgpu_get_solution(aphgpu_ctx* ctx, double* x);
+
+/* Residual norm sqrt(sum r^2) and sqrt(sum b^2) of the resident solution,
+ * r = b - A x, b = -e[7] (FP64). */
+int aphgpu_residual_norms(aphgpu_ctx* ctx, double* rnorm, double* bnorm);
+
+/* Corrected face fluxes v = k*(p[cm] - p[cp]) + v* of Proj::Project
+ * (src/solver/proj.ipp:399-403, UEmbed::Eval src/solver/approx_eb.h:338-343)
+ * for the last assembled projection system and the resident pressure.
+ * vflux_out: 3 face blocks, host (NULL: keep resident as the advection
+ * flux of the next aphgpu_vof_step with vflux == NULL). */
+int aphgpu_flux_correct(aphgpu_ctx* ctx, double* vflux_out);
+
+/* Cell acceleration (febp - grad p)/rho_f averaged to cells, Proj
+ * GetAcceleration (src/solver/proj.ipp:408-433) without cell force, for the
+ * last assembled projection (its density and force) and the resident
+ * pressure; acc: 3 doubles per cell (AoS). */
+int aphgpu_acceleration(aphgpu_ctx* ctx, double* acc);
+
+/* ---- PLIC volume of fluid ---- */
+
+/* Sets the volume fraction and reconstructs the interface: the state of
+ * Vof after StartStep at t=0 (src/solver/vof.ipp:177-195, 70-90). */
+int aphgpu_vof_init(aphgpu_ctx* ctx, const double* alpha, double clipth);
+
+/* One advection step: Vof::MakeIteration (src/solver/vof.ipp:498-583),
+ * scheme weymouth, three directionally split sweeps (Vof::Sweep,
+ * vof.ipp:212-327) in the order selected by the step count, each followed
+ * by interface reconstruction; then FinishStep.  vflux: mixture face fluxes
+ * (host, 3 face blocks) or NULL to use the resident corrected fluxes of
+ * aphgpu_flux_correct().  Colour labelling is not part of this path. */
+int aphgpu_vof_step(aphgpu_ctx* ctx, const double* vflux, double dt);
+
+/* Copies the VOF state to the host; any pointer may be NULL.
+ * normals: AoS 3 per cell, NaN outside the interface; plane: plane
+ * constant, NaN outside; mask: 1 in interfacial cells (0<alpha<1). */
+int aphgpu_vof_get(aphgpu_ctx* ctx, double* alpha, double* normals,
+                   double* plane, uint8_t* mask);
+
+/* Height-function curvature of the current VOF state:
+ * curvature::Heights::CalcCurvature (src/solver/curv.ipp:358-414), one
+ * layer without colours.  kappa: NaN outside the interface; heights:
+ * optional AoS 3 per cell (NaN where undefined).  Either may be NULL
+ * (results stay resident for aphgpu_surface_tension). */
+int aphgpu_curvature(aphgpu_ctx* ctx, double* kappa, double* heights);
+
+/* Surface-tension face force sigma*kappa*grad(alpha) of
+ * AppendSurfaceTension (src/util/hydro.ipp:1289-1310) from the resident
+ * volume fraction and curvature.  febp: 3 face blocks (host) or NULL to keep
+ * it resident for the next aphgpu_assemble_projection(febp == NULL) call
+ * with use_resident_force set by aphgpu_set_force_resident(). */
+int aphgpu_surface_tension(aphgpu_ctx* ctx, double sigma, double* febp);
+
+/* Makes the next assemble calls use the resident surface-tension force
+ * (on != 0) when their febp argument is NULL. */
+int aphgpu_set_force_resident(aphgpu_ctx* ctx, int on);
+
+/* ---- timing of the last solve (CUDA events on the context stream) ---- */
+
+/* Milliseconds of the last solve, VOF step or curvature
+ * call measured on the device, and the number of kernels it launched. */
+int aphgpu_last_timing(const aphgpu_ctx* ctx, double* ms, int64_t* launches);
+
+/* Records event `slot` (0..7) on the context's stream; aphgpu_elapsed
+ * returns the milliseconds between two recorded slots (waits for the
+ * second). */
+int aphgpu_mark(aphgpu_ctx* ctx, int slot);
+int aphgpu_elapsed(aphgpu_ctx* ctx, int slot0, int slot1, double* ms);
+
+/* Kernel identifiers for aphgpu_time_kernel. */
+enum {
+  APHGPU_K_SMOOTH32 = 0,   /* FP32 red-black half sweep, finest level */
+  APHGPU_K_SMOOTH64 = 1,   /* FP64 red-black half sweep, finest level */
+  APHGPU_K_APPLY64 = 2,    /* FP64 y = A p with the p.y reduction */
+  APHGPU_K_APPLY32 = 3,    /* FP32 y = A p with the p.y reduction */
+  APHGPU_K_RESTRICT32 = 4, /* FP32 residual + restriction, finest level */
+  APHGPU_K_VOF_FLUX = 5,   /* VOF fluid fluxes of one direction */
+  APHGPU_K_VOF_UPDATE = 6, /* VOF update of one direction */
+  APHGPU_K_RECONSTRUCT = 7,/* interface normals and plane constants */
+  APHGPU_K_HEIGHTS = 8,    /* height functions */
+  APHGPU_K_CURVATURE = 9   /* curvature from heights */
+};
+
+/* Launches one kernel `reps` times on the context's stream on its resident
+ * data (after a solve / VOF step has prepared it) and returns the mean
+ * device milliseconds per launch, measured with CUDA events on that stream,
+ * and the algorithmic bytes one launch moves (compulsory traffic: each
+ * array element read or written once).  Kernels that update state in place
+ * leave it modified. */
+int aphgpu_time_kernel(aphgpu_ctx* ctx, int kernel, int reps, double* ms,
+                       double* bytes);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* APHGPU_H_ */

@@ -23,7 +23,7 @@
 //   overlap in out         rows (x y z hx hy hz cx cy cz r) -> GetSphereOverlap
 //   reconst in out         rows (n0 n1 n2 u a h0 h1 h2 q dt d) ->
 //                          GetLineA(n,u,h) GetLineU(n,a,h) GetLineFlux(...)
-//   height  in out         rows of 13 -> UHeight::Good
+//   height  in out         rows (column, optional n=N) -> UHeight::Good
 #include <cmath>
 #include <cstdio>
 #include <cstdlib>
@@ -392,9 +392,22 @@ int Table(const std::string& mode, const char* in, const char* out) {
       fo << R::GetLineA(n, v[3], h) << " " << R::GetLineU(n, v[4], h) << " "
          << R::GetLineFlux(n, v[4], h, v[8], v[9], size_t(v[10])) << "\n";
     } else if (mode == "height") {
-      std::vector<double> uu(13);
-      for (auto& x : uu) s >> x;
-      fo << UHeight<Scal>::Good(uu) << "\n";
+      // a column of any length; with a leading "n=<value>" token the
+      // two-argument Good(uu, n) is evaluated instead
+      std::vector<double> uu;
+      std::string tok;
+      bool with_n = false;
+      double nn = 0;
+      while (s >> tok) {
+        if (tok.rfind("n=", 0) == 0) {
+          with_n = true;
+          nn = std::atof(tok.c_str() + 2);
+        } else {
+          uu.push_back(std::atof(tok.c_str()));
+        }
+      }
+      fo << (with_n ? UHeight<Scal>::Good(uu, nn) : UHeight<Scal>::Good(uu))
+         << "\n";
     }
   }
   return 0;

@@ -1,0 +1,218 @@
+"""Generates the golden fixtures of tests/golden/ by running aphros's OWN code
+(oracle/_ref/ref_harness, built from the reference sources by
+oracle/ref/Makefile) and by reading the reference's committed test data.
+
+Run from the repository root, where the reference tree is available:
+    python tests/golden/make_golden.py [--ref /path/to/aphros]
+
+Fixtures:
+  advection3d.npz  the reference's 3-D advection test (test/advection,
+                   24x24x16, uniform velocity (0.6,0.5,0.3), Weymouth):
+                   initial field and golden result from its ref/3d/*.dat, and
+                   aphros's own run of the 58 steps on one block (u, normals,
+                   plane constants, curvature).
+  proj16.npz       projection step on 16^3 (sphere r=0.2, density ratio
+                   1000, Taylor-Green + noise): inputs, aphros's assembled
+                   system, CG solution at ||r||/||b|| = 1e-10, corrected
+                   fluxes, iteration count.
+  vof32.npz        3 VOF steps + Heights curvature on 32^3 (sphere r=0.2,
+                   Taylor-Green flux at CFL 0.5): aphros's results.
+  reconst.txt      random planes: GetLineA, GetLineU, GetLineFlux.
+  height.txt       UHeight::Good on the reference's unit-test columns
+                   (test/util/main.cpp) and on random 13-cell columns.
+  overlap.txt      GetSphereOverlap on random boxes (pins the generator).
+"""
+import argparse
+import math
+import os
+import re
+import subprocess
+import sys
+import tempfile
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.dirname(os.path.dirname(os.path.abspath(__file__))))
+sys.path.insert(0, ROOT)
+from aphros_gb300 import workload  # noqa: E402
+
+OUT = os.path.dirname(os.path.abspath(__file__))
+HARNESS = os.path.join(ROOT, "oracle", "_ref", "ref_harness")
+
+
+def read_plain(path):
+    with open(path) as f:
+        dims = [int(v) for v in f.readline().split()]
+        data = np.array(f.read().split(), dtype=float)
+    return dims, data
+
+
+def run(args, cwd):
+    env = dict(os.environ, OMP_NUM_THREADS="1")
+    subprocess.run([HARNESS] + args, cwd=cwd, check=True, env=env)
+
+
+def advection3d(ref, tmp):
+    d = os.path.join(ref, "src", "test", "advection", "ref", "3d")
+    dims, u0 = read_plain(os.path.join(d, "u_0000.dat"))
+    _, u2 = read_plain(os.path.join(d, "u_0002.dat"))
+    n3 = tuple(dims)
+    h = 1.0 / max(n3)
+    vel = (0.6, 0.5, 0.3)
+    flux = workload.uniform_flux(n3, h, vel)
+    # dt = cfl / maxvel with cfl 0.25 (test/advection/std.conf, main.cpp:234-241)
+    area, vol = h * h, h * h * h
+    maxvel = max(abs(flux[:]).max() / vol, 0.0)
+    dt = float(0.25 / maxvel)
+    steps = 58  # first dump time >= tmax with dump_field_dt 0.5, tmax 1
+    u0.tofile(os.path.join(tmp, "u0.bin"))
+    flux.tofile(os.path.join(tmp, "f.bin"))
+    run(["vof", "%d,%d,%d" % n3, "%d,%d,%d" % n3, repr(h), repr(dt), str(steps),
+         "u0.bin", "f.bin", "adv"], tmp)
+    r = lambda s: np.fromfile(os.path.join(tmp, "adv." + s))
+    np.savez_compressed(os.path.join(OUT, "advection3d.npz"), n=np.array(n3), h=h,
+                        dt=dt, steps=steps, vel=np.array(vel), u_init=u0,
+                        u_golden=u2, u_ref=r("u"), n_ref=r("n"), a_ref=r("a"),
+                        k_ref=r("k"))
+
+
+def proj16(tmp):
+    case = workload.config("c1", n=16)
+    n, h = case.n, case.h
+    case.alpha.tofile(os.path.join(tmp, "alpha.bin"))
+    case.flux.tofile(os.path.join(tmp, "vf.bin"))
+    # tolerance for ||r||/||b|| = 1e-10 in the reference's norm
+    import oracle
+    e, _, _ = oracle.assemble_projection(n, h, case.dt, case.alpha, case.rho1,
+                                         case.rho2, case.flux)
+    tol = oracle.rel_tol(e, h, 1e-10)
+    run(["proj", str(n), str(n), repr(h), repr(case.dt), repr(case.rho1),
+         repr(case.rho2), repr(tol), "100000", "alpha.bin", "vf.bin", "pr"], tmp)
+    r = lambda s: np.fromfile(os.path.join(tmp, "pr." + s))
+    info = open(os.path.join(tmp, "pr.info")).read().split()
+    np.savez_compressed(os.path.join(OUT, "proj16.npz"), n=n, h=h, dt=case.dt,
+                        rho1=case.rho1, rho2=case.rho2, tol=tol, alpha=case.alpha,
+                        vflux=case.flux, expr_ref=r("expr"), p_ref=r("p"),
+                        flux_ref=r("flux"), residual=float(info[0]),
+                        iters=int(info[1]))
+
+
+def vof32(tmp):
+    case = workload.config("c1", n=32)
+    n, h = case.n, case.h
+    dt = case.cfl_dt(0.5)
+    case.alpha.tofile(os.path.join(tmp, "a.bin"))
+    case.flux.tofile(os.path.join(tmp, "f.bin"))
+    run(["vof", str(n), str(n), repr(h), repr(dt), "3", "a.bin", "f.bin", "v"], tmp)
+    r = lambda s: np.fromfile(os.path.join(tmp, "v." + s))
+    np.savez_compressed(os.path.join(OUT, "vof32.npz"), n=n, h=h, dt=dt, steps=3,
+                        u_ref=r("u"), n_ref=r("n"), a_ref=r("a"), k_ref=r("k"),
+                        alpha_sum=float(case.alpha.sum()))
+
+
+def reconst(tmp, rows=300):
+    rng = np.random.default_rng(7)
+    lines = []
+    for i in range(rows):
+        n = rng.normal(size=3)
+        if i % 5 == 0:
+            n[rng.integers(3)] = 0.0
+        if i % 11 == 0:
+            n[:] = 0
+            n[rng.integers(3)] = 1.0
+        n /= np.abs(n).sum()
+        h = rng.uniform(0.5, 2.0, size=3) if i % 3 == 0 else np.full(3, 1.0 / 32)
+        u = rng.uniform(0, 1)
+        if i % 7 == 0:
+            u = rng.choice([1e-9, 0.5, 1 - 1e-9])
+        a = rng.uniform(-0.5, 0.5) * np.abs(n * h).sum()
+        d = int(rng.integers(3))
+        area = h.prod() / h[d]
+        dt = 0.01
+        q = rng.uniform(-0.9, 0.9) * h[d] * area / dt
+        lines.append(" ".join(repr(float(v)) for v in
+                              [*n, u, a, *h, q, dt, d]))
+    src = os.path.join(tmp, "rin.txt")
+    open(src, "w").write("\n".join(lines) + "\n")
+    run(["reconst", "rin.txt", "rout.txt"], tmp)
+    out = open(os.path.join(tmp, "rout.txt")).read().split("\n")
+    with open(os.path.join(OUT, "reconst.txt"), "w") as f:
+        f.write("# n0 n1 n2 u a h0 h1 h2 q dt d | GetLineA(n,u,h) GetLineU(n,a,h) "
+                "GetLineFlux(n,a,h,q,dt,d) from aphros (src/solver/reconst.h)\n")
+        for a, b in zip(lines, out):
+            f.write(a + " | " + b + "\n")
+
+
+def height(ref, tmp, rows=300):
+    src = open(os.path.join(ref, "src", "test", "util", "main.cpp")).read()
+    cols = []
+    # t({...}, n, bool) in TestGood and t({...}, value) in TestGood2
+    for m in re.finditer(r"t\(\{([^}]*)\},\s*([-\w.]+)\s*(?:,\s*(true|false))?\)", src):
+        vals = [float(v) for v in m.group(1).split(",")]
+        if m.group(3) is not None:
+            cols.append((vals, float(m.group(2)), m.group(3)))
+        else:
+            cols.append((vals, None, m.group(2)))
+    rng = np.random.default_rng(11)
+    for i in range(rows):
+        c = np.where(rng.uniform(size=13) < 0.5, 0.0, 1.0)
+        k = int(rng.integers(2, 11))
+        c[k - 2:k + 3] = np.sort(rng.uniform(size=5))[:: (1 if i % 2 else -1)]
+        c[6] = rng.uniform(0.05, 0.95)
+        cols.append(([float(v) for v in c], None, "random"))
+    lines = []
+    for vals, nn, _ in cols:
+        lines.append(("n=%r " % nn if nn is not None else "") +
+                     " ".join(repr(v) for v in vals))
+    open(os.path.join(tmp, "hin.txt"), "w").write("\n".join(lines) + "\n")
+    run(["height", "hin.txt", "hout.txt"], tmp)
+    out = open(os.path.join(tmp, "hout.txt")).read().split("\n")
+    with open(os.path.join(OUT, "height.txt"), "w") as f:
+        f.write("# column (n=<normal> for the two-argument form) | UHeight::Good "
+                "from aphros (src/util/height.h) | expectation of "
+                "test/util/main.cpp or 'random'\n")
+        for (vals, nn, exp), line, res in zip(cols, lines, out):
+            f.write(line + " | " + res + " | " + exp + "\n")
+
+
+def overlap(tmp, rows=200):
+    rng = np.random.default_rng(13)
+    lines = []
+    for i in range(rows):
+        r = rng.uniform(0.05, 0.3)
+        c = rng.uniform(0.2, 0.8, size=3)
+        h = np.full(3, rng.choice([1 / 16, 1 / 32, 1 / 64]))
+        # box centres near the sphere surface
+        dirn = rng.normal(size=3)
+        dirn /= np.linalg.norm(dirn)
+        x = c + dirn * (r + rng.uniform(-1.5, 1.5) * h[0])
+        lines.append(" ".join(repr(float(v)) for v in [*x, *h, *c, r]))
+    open(os.path.join(tmp, "oin.txt"), "w").write("\n".join(lines) + "\n")
+    run(["overlap", "oin.txt", "oout.txt"], tmp)
+    out = open(os.path.join(tmp, "oout.txt")).read().split("\n")
+    with open(os.path.join(OUT, "overlap.txt"), "w") as f:
+        f.write("# x y z hx hy hz cx cy cz r | GetSphereOverlap from aphros "
+                "(src/overlap/overlap.h)\n")
+        for a, b in zip(lines, out):
+            f.write(a + " | " + b + "\n")
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--ref", default="/root/reference")
+    args = ap.parse_args()
+    if not os.path.exists(HARNESS):
+        sys.exit("build the reference harness first: python -m aphros_gb300.build")
+    with tempfile.TemporaryDirectory() as tmp:
+        advection3d(args.ref, tmp)
+        proj16(tmp)
+        vof32(tmp)
+        reconst(tmp)
+        height(args.ref, tmp)
+        overlap(tmp)
+    for f in sorted(os.listdir(OUT)):
+        print(f, os.path.getsize(os.path.join(OUT, f)))
+
+
+if __name__ == "__main__":
+    main()

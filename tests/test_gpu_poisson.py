@@ -1,0 +1,214 @@
+"""GPU parity of the pressure Poisson path against the oracle and aphros's
+own outputs (golden fixtures).  Calls go through the C ABI (ctypes).
+
+Tolerances: the projection assembly and the flux correction are bit-exact;
+solutions are compared after mean removal (the periodic operator fixes p up
+to a constant) in relative L2 norm: <= 1e-9 for the plain FP64 CG against
+aphros's CG, both at ||r||/||b|| = 1e-10, and <= 1e-9 for MG-PCG / mixed
+precision solved to ||r||/||b|| = 1e-12 against the oracle CG solved to the
+same level (the error bound at 1e-10 is recorded separately).
+"""
+import math
+
+import numpy as np
+import pytest
+
+import oracle
+from aphros_gb300 import _lib, linear, workload
+from conftest import golden
+
+pytestmark = pytest.mark.gpu
+
+
+def rel_l2(a, b):
+    a = a - a.mean()
+    b = b - b.mean()
+    return float(np.linalg.norm(a - b) / np.linalg.norm(b))
+
+
+@pytest.fixture(scope="module")
+def proj16():
+    return np.load(golden("proj16.npz"))
+
+
+def _ctx16(fx):
+    n, h = int(fx["n"]), float(fx["h"])
+    ctx = _lib.Context(n, h)
+    ctx.assemble_projection(fx["alpha"], float(fx["rho1"]), float(fx["rho2"]),
+                            fx["vflux"], float(fx["dt"]))
+    return ctx
+
+
+def test_assembly_bit_exact(proj16):
+    """P1-P5 fused on the device equal aphros's Proj::GetFlux/GetFluxSum
+    system bit for bit (RHS mean removed)."""
+    ctx = _ctx16(proj16)
+    e = ctx.get_system_expr()
+    ref = proj16["expr_ref"]
+    # the mean of e7 is summed in a different order on the device
+    mask = np.ones(8, bool)
+    mask[7] = False
+    assert np.array_equal(e.reshape(-1, 8)[:, mask], ref.reshape(-1, 8)[:, mask])
+    assert np.max(np.abs(e[7::8] - ref[7::8])) <= 1e-17 * np.max(np.abs(ref[7::8])) + 1e-30
+
+
+def test_cg_matches_reference_cg(proj16):
+    """Plain FP64 CG (the algorithm of SolverConjugate) against aphros's CG
+    on the same system and stopping rule."""
+    ctx = _ctx16(proj16)
+    conf = _lib.default_conf(solver=_lib.SOLVER_CG, tol=float(proj16["tol"]),
+                             maxiter=100000)
+    x, info = ctx.solve(conf)
+    assert info.converged
+    ref_iters = int(proj16["iters"])
+    assert abs(info.iter - ref_iters) <= max(2, ref_iters // 50)
+    assert rel_l2(x, proj16["p_ref"]) <= 1e-9
+
+
+@pytest.mark.parametrize("solver", [_lib.SOLVER_MGPCG, _lib.SOLVER_MIXED])
+def test_multigrid_solvers_match_reference(proj16, solver):
+    n, h = int(proj16["n"]), float(proj16["h"])
+    ctx = _ctx16(proj16)
+    e = proj16["expr_ref"]
+    b = -e[7::8]
+    tol12 = 1e-12 * math.sqrt(float(b @ b) / h ** 3)
+    conf = _lib.default_conf(solver=solver, tol=tol12, maxiter=500)
+    x, info = ctx.solve(conf)
+    assert info.converged, info.residual
+    xo, _ = oracle.cg_solve(n, h, e, tol12)
+    assert rel_l2(x, xo) <= 1e-9
+    # at the production tolerance the error against aphros's CG solution
+    conf.tol = float(proj16["tol"])
+    x10, info10 = ctx.solve(conf)
+    assert info10.converged
+    assert rel_l2(x10, proj16["p_ref"]) <= 1e-7
+
+
+def test_expr_path_equals_assembly_path(proj16):
+    """The linear::Solver drop-in (Expr AoS input) solves the same operator
+    as the fused assembly: identical solutions."""
+    ctx = _ctx16(proj16)
+    conf = _lib.default_conf(solver=_lib.SOLVER_MGPCG, tol=float(proj16["tol"]))
+    x1, i1 = ctx.solve(conf)
+    ctx2 = _lib.Context(int(proj16["n"]), float(proj16["h"]))
+    ctx2.set_system_expr(ctx.get_system_expr())
+    x2, i2 = ctx2.solve(conf)
+    assert i1.iter == i2.iter
+    assert np.array_equal(x1, x2)
+
+
+def test_drop_in_solver_interface(proj16):
+    """aphros_gb300.linear mirrors linear::Solver::Solve: fc_init may alias
+    fc_sol, the result is written in place."""
+    m = linear.Mesh(int(proj16["n"]), float(proj16["h"]))
+    var = {"linsolver_symm": "gpu", "hypre_symm_tol": repr(float(proj16["tol"])),
+           "hypre_symm_maxiter": "200"}
+    solver = linear.MakeLinearSolver(var, "symm", m)
+    sol = np.zeros(m.ncells())
+    info = solver.Solve(proj16["expr_ref"], sol, sol, m)
+    assert info.converged and info.residual < float(proj16["tol"])
+    assert rel_l2(sol, proj16["p_ref"]) <= 1e-7
+
+
+def test_non_symmetric_system_is_rejected(proj16):
+    e = proj16["expr_ref"].copy()
+    e[8 * 5 + 2] *= 1.5
+    ctx = _lib.Context(int(proj16["n"]), float(proj16["h"]))
+    with pytest.raises(_lib.AphgpuError) as err:
+        ctx.set_system_expr(e)
+    assert err.value.code == _lib.ERR_NOT_SYMMETRIC
+
+
+def test_flux_correction_bit_exact(proj16):
+    """Proj::Project flux update on the GPU's own pressure equals the
+    oracle's formula bit for bit; with aphros's pressure the fluxes agree to
+    the solver tolerance."""
+    n, h = int(proj16["n"]), float(proj16["h"])
+    ctx = _ctx16(proj16)
+    conf = _lib.default_conf(solver=_lib.SOLVER_MGPCG, tol=float(proj16["tol"]))
+    x, _ = ctx.solve(conf)
+    f = ctx.flux_correct()
+    _, fk, fv = oracle.assemble_projection(n, h, float(proj16["dt"]), proj16["alpha"],
+                                           float(proj16["rho1"]), float(proj16["rho2"]),
+                                           proj16["vflux"])
+    assert np.array_equal(f, oracle.flux_correct(n, fk, fv, x))
+    # corrected fluxes are discretely divergence-free to the residual level
+    F = f.reshape(3, n, n, n)
+    div = (np.roll(F[0], -1, axis=2) - F[0] + np.roll(F[1], -1, axis=1) - F[1]
+           + np.roll(F[2], -1, axis=0) - F[2])
+    assert np.max(np.abs(div)) < 1e-8 * np.max(np.abs(proj16["vflux"]))
+
+
+def test_acceleration_bit_exact(proj16):
+    n, h = int(proj16["n"]), float(proj16["h"])
+    ctx = _ctx16(proj16)
+    x, _ = ctx.solve(_lib.default_conf(tol=float(proj16["tol"])))
+    acc = ctx.acceleration()
+    ref = oracle.acceleration(n, h, x, proj16["alpha"], float(proj16["rho1"]),
+                              float(proj16["rho2"]))
+    assert np.array_equal(acc, ref)
+
+
+def _diffusion_system(n, seed=3, shift=0.3):
+    """A symmetric 7-point system with an explicit diagonal (the shape of
+    the implicit-diffusion systems Proj also hands to linsolver_symm)."""
+    N = n ** 3
+    rng = np.random.default_rng(seed)
+    w = -rng.uniform(0.1, 10.0, size=(3, N))
+    e = np.zeros((N, 8))
+    idx = np.arange(N).reshape(n, n, n)
+    for d, axis in ((0, 2), (1, 1), (2, 0)):
+        e[:, 1 + 2 * d] = w[d]
+        e[:, 2 + 2 * d] = w[d][np.roll(idx, -1, axis=axis).ravel()]
+    e[:, 0] = -e[:, 1:7].sum(axis=1) + shift
+    e[:, 7] = rng.normal(size=N)
+    return e.ravel()
+
+
+@pytest.mark.parametrize("solver", [_lib.SOLVER_CG, _lib.SOLVER_MGPCG, _lib.SOLVER_MIXED])
+def test_diffusion_type_system(solver):
+    n, h = 16, 1 / 16
+    e = _diffusion_system(n)
+    tol = oracle.rel_tol(e, h, 1e-11)
+    xo, io = oracle.cg_solve(n, h, e, tol)
+    ctx = _lib.Context(n, h)
+    ctx.set_system_expr(e)
+    x, info = ctx.solve(_lib.default_conf(solver=solver, tol=tol, maxiter=5000))
+    assert info.converged
+    assert np.linalg.norm(x - xo) / np.linalg.norm(xo) < 1e-9
+
+
+@pytest.mark.parametrize("n", [24, 48])
+def test_c1_sizes_and_warm_start(n):
+    """Non-power-of-two grids coarsen to small odd levels; a warm start from
+    the converged pressure converges immediately (miniter = 1)."""
+    case = workload.config("c1", n=n)
+    ctx = _lib.Context(n, case.h)
+    ctx.assemble_projection(case.alpha, case.rho1, case.rho2, case.flux, case.dt)
+    r0, b = ctx.residual_norms()
+    tol = 1e-10 * b / math.sqrt(case.h ** 3)
+    for solver in (_lib.SOLVER_MGPCG, _lib.SOLVER_MIXED):
+        x, info = ctx.solve(_lib.default_conf(solver=solver, tol=tol))
+        assert info.converged
+        rn, bn = ctx.residual_norms()
+        assert rn / bn < 1.2e-10
+    info = ctx.solve_resident(_lib.default_conf(solver=_lib.SOLVER_MGPCG, tol=tol),
+                              zero_guess=False)
+    assert info.iter == 1
+
+
+def test_full_size_property_256():
+    """At 256^3 (16 bubbles, ratio 1000) both multigrid solvers reach
+    ||r||/||b|| <= 1e-10 (recomputed in FP64) and agree with each other."""
+    case = workload.config("c2")
+    ctx = _lib.Context(case.n, case.h)
+    ctx.assemble_projection(case.alpha, case.rho1, case.rho2, case.flux, case.dt)
+    _, b = ctx.residual_norms()
+    tol = 1e-10 * b / math.sqrt(case.h ** 3)
+    x64, i64 = ctx.solve(_lib.default_conf(solver=_lib.SOLVER_MGPCG, tol=tol))
+    rn, bn = ctx.residual_norms()
+    assert i64.converged and rn / bn <= 1.01e-10
+    x32, i32 = ctx.solve(_lib.default_conf(solver=_lib.SOLVER_MIXED, tol=tol))
+    rn, bn = ctx.residual_norms()
+    assert i32.converged and rn / bn <= 1.01e-10
+    assert rel_l2(x32, x64) <= 1e-7

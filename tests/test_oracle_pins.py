@@ -1,0 +1,203 @@
+"""Pins the CPU oracle against aphros itself (CPU, no GPU needed).
+
+Every check compares the C restatement (oracle/aphros_oracle.c) with values
+produced by aphros's own code: the golden fixtures made by
+tests/golden/make_golden.py from oracle/_ref/ref_harness, and the
+reference's committed golden files where the reference tree is present.
+"""
+import math
+import os
+
+import numpy as np
+import pytest
+
+import oracle
+from aphros_gb300 import workload
+from conftest import REFERENCE, golden, read_table
+
+
+def _bits_equal(a, b):
+    a = np.asarray(a, dtype=np.float64)
+    b = np.asarray(b, dtype=np.float64)
+    both_nan = np.isnan(a) & np.isnan(b)
+    return np.all((a == b) | both_nan)
+
+
+def test_reconst_geometry_matches_reference():
+    """GetLineA / GetLineU / GetLineFlux (src/solver/reconst.h) on random
+    planes: identical bits."""
+    rows = read_table("reconst.txt")
+    assert len(rows) >= 200
+    mism = 0
+    for inp, out in rows:
+        v = [float(x) for x in inp.split()]
+        n, u, a, h, q, dt, d = v[0:3], v[3], v[4], v[5:8], v[8], v[9], int(v[10])
+        ra, ru, rf = [float(x) for x in out.split()]
+        ga = oracle.line_a(n, u, h)
+        gu = oracle.line_u(n, a, h)
+        gf = oracle.line_flux(n, a, h, q, dt, d)
+        for x, y in ((ga, ra), (gu, ru), (gf, rf)):
+            if not (x == y or (math.isnan(x) and math.isnan(y))):
+                mism += 1
+                assert abs(x - y) <= 1e-14 * max(1.0, abs(y)), (inp, x, y)
+    # libm may differ in the last bit on another platform; here it is exact
+    assert mism <= len(rows) // 20
+
+
+def test_reconst_identities():
+    """Known answers of test/reconst/main.cpp:116-124 and u(a(u)) = u."""
+    one = (1.0, 1.0, 1.0)
+    assert abs(oracle.line_u((0.0, 1.0, 0.0), 0.0, one) - 0.5) < 1e-12
+    assert abs(oracle.line_u((1.0, 1.0, 1.0), -1.5, one) - 0.0) < 1e-12
+    assert abs(oracle.line_u((1.0, 1.0, 1.0), 1.5, one) - 1.0) < 1e-12
+    assert abs(oracle.line_u((1.0, 1.0, 1.0), -0.5, one) - 1.0 / 6.0) < 1e-12
+    rng = np.random.default_rng(0)
+    for _ in range(2000):
+        n = rng.uniform(size=3) * rng.integers(0, 2, size=3)
+        if not n.any():
+            n[0] = 1
+        n /= np.linalg.norm(n)
+        u = rng.uniform()
+        h = (0.1, 0.2, 0.3)
+        a = oracle.line_a(n, u, h)
+        assert abs(oracle.line_u(n, a, h) - u) < 1e-10
+
+
+def test_height_good_matches_reference():
+    rows = read_table("height.txt")
+    ntest = 0
+    for inp, out, exp in rows:
+        toks = inp.split()
+        nn = None
+        if toks[0].startswith("n="):
+            nn = float(toks[0][2:])
+            toks = toks[1:]
+        uu = [float(t) for t in toks]
+        g = oracle.height_good_n(uu, nn) if nn is not None else oracle.height_good(uu)
+        r = float(out)
+        assert (g == r) or (math.isnan(g) and math.isnan(r)), (inp, g, r)
+        # the reference unit test's own expectation (test/util/main.cpp)
+        if exp in ("true", "false"):
+            assert (not math.isnan(g)) == (exp == "true")
+            ntest += 1
+        elif exp != "random":
+            e = float(exp)
+            assert (math.isnan(g) and math.isnan(e)) or abs(g - e) < 1e-6
+            ntest += 1
+    assert ntest >= 20
+
+
+def test_generator_overlap_matches_reference():
+    """Our sphere/cell overlap (workload generator) against aphros's
+    GetSphereOverlap (src/overlap/overlap.cpp)."""
+    g = workload.gen()
+    rows = read_table("overlap.txt")
+    worst = 0.0
+    for inp, out in rows:
+        x, y, z, hx, hy, hz, cx, cy, cz, r = [float(t) for t in inp.split()]
+        ref = float(out)
+        vol = g.aphgen_box_sphere(x - hx / 2 - cx, x + hx / 2 - cx, y - hy / 2 - cy,
+                                  y + hy / 2 - cy, z - hz / 2 - cz, z + hz / 2 - cz, r)
+        frac = vol / (hx * hy * hz)
+        worst = max(worst, abs(frac - ref))
+    assert worst < 1e-10, worst
+
+
+def _advection3d_oracle(fx):
+    n3 = tuple(int(v) for v in fx["n"])
+    h = float(fx["h"])
+    flux = workload.uniform_flux(n3, h, fx["vel"])
+    st = oracle.VofState(n3, h, fx["u_init"])
+    for _ in range(int(fx["steps"])):
+        st.step(flux, float(fx["dt"]))
+    return st
+
+
+def test_advection3d_reference_golden():
+    """The reference's own 3-D advection test (test/advection, 3d.conf):
+    58 Weymouth steps of a sphere in uniform flow.  Against the committed
+    golden u_0002.dat with the test's threshold 1e-11 (test/advection/test:78)
+    and bit for bit against aphros run on one block."""
+    fx = np.load(golden("advection3d.npz"))
+    st = _advection3d_oracle(fx)
+    assert np.nanmax(np.abs(st.u - fx["u_golden"])) <= 1e-11
+    assert _bits_equal(st.u, fx["u_ref"])
+    assert _bits_equal(st.nrm, fx["n_ref"])
+    assert _bits_equal(st.a, fx["a_ref"])
+    assert _bits_equal(st.curvature(), fx["k_ref"])
+
+
+@pytest.mark.skipif(not os.path.isdir(os.path.join(REFERENCE, "src")),
+                    reason="reference tree not present")
+def test_advection3d_fixture_is_reference_file():
+    """The fixture's golden field is the reference's file itself."""
+    path = os.path.join(REFERENCE, "src/test/advection/ref/3d/u_0002.dat")
+    with open(path) as f:
+        f.readline()
+        u2 = np.array(f.read().split(), dtype=float)
+    fx = np.load(golden("advection3d.npz"))
+    assert np.array_equal(u2, fx["u_golden"])
+
+
+def test_projection_assembly_and_cg_match_reference():
+    """Proj::GetFlux/GetFluxSum assembly and SolverConjugate on 16^3,
+    density ratio 1000: identical system, identical CG iterates (the
+    reference ran on one block, so its reductions are sequential too)."""
+    fx = np.load(golden("proj16.npz"))
+    n, h = int(fx["n"]), float(fx["h"])
+    e, fk, fv = oracle.assemble_projection(n, h, float(fx["dt"]), fx["alpha"],
+                                           float(fx["rho1"]), float(fx["rho2"]),
+                                           fx["vflux"])
+    assert _bits_equal(e, fx["expr_ref"])
+    x, info = oracle.cg_solve(n, h, e, float(fx["tol"]))
+    assert info.iter == int(fx["iters"])
+    assert _bits_equal(x, fx["p_ref"])
+    f = oracle.flux_correct(n, fk, fv, x)
+    assert _bits_equal(f, fx["flux_ref"])
+
+
+def test_vof32_matches_reference():
+    """3 Weymouth steps (all three split orders) and Heights curvature on
+    the 32^3 sphere in Taylor-Green flow."""
+    fx = np.load(golden("vof32.npz"))
+    case = workload.config("c1", n=int(fx["n"]))
+    assert abs(case.alpha.sum() - float(fx["alpha_sum"])) < 1e-9
+    st = oracle.VofState(case.n, case.h, case.alpha)
+    for _ in range(int(fx["steps"])):
+        st.step(case.flux, float(fx["dt"]))
+    assert np.max(np.abs(st.u - fx["u_ref"])) <= 1e-13
+    k = st.curvature()
+    m = ~np.isnan(fx["k_ref"])
+    assert np.array_equal(np.isnan(k), ~m)
+    assert np.max(np.abs(k[m] - fx["k_ref"][m])) <= 1e-9
+
+
+def test_sphere_curvature_close_to_exact():
+    """Heights curvature of a sphere r=0.2 on 64^3 is close to 2/r = 10."""
+    case = workload.config("c1", n=64)
+    st = oracle.VofState(64, case.h, case.alpha)
+    # reconstruct without advecting: a zero-flux step
+    st.step(np.zeros(3 * case.N), 1e-3)
+    k = st.curvature()
+    kk = k[~np.isnan(k)]
+    assert len(kk) > 1000
+    assert abs(np.median(kk) - 10.0) < 0.3
+
+
+def test_cg_converges_on_random_spd():
+    """The oracle CG solves a small diffusion system (explicit diagonal)."""
+    n = 8
+    N = n ** 3
+    rng = np.random.default_rng(3)
+    w = -rng.uniform(0.5, 2.0, size=(3, N))
+    e = np.zeros((N, 8))
+    idx = np.arange(N).reshape(n, n, n)  # [k, j, i]
+    for d, axis in ((0, 2), (1, 1), (2, 0)):
+        e[:, 1 + 2 * d] = w[d]
+        e[:, 2 + 2 * d] = w[d][np.roll(idx, -1, axis=axis).ravel()]
+    e[:, 0] = -e[:, 1:7].sum(axis=1) + 0.5
+    xs = rng.normal(size=N)
+    r, _ = oracle.residual(n, e.ravel(), xs)  # r = -(A xs + e7) with e7 = 0
+    e[:, 7] = r  # now A xs + e7 = 0
+    x, info = oracle.cg_solve(n, 1.0, e.ravel(), 1e-12)
+    assert np.max(np.abs(x - xs)) < 1e-8
