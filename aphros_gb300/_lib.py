@@ -29,6 +29,7 @@ KERNEL_NAMES = {0: "KSmooth<float>", 1: "KSmooth<double>", 2: "KPcgApply<double>
 SOLVER_CG = 0
 SOLVER_MGPCG = 1
 SOLVER_MIXED = 2
+SOLVER_MGPCG32 = 3
 
 _D = ctypes.c_double
 _I = ctypes.c_int
@@ -41,6 +42,7 @@ class Conf(ctypes.Structure):
         ("solver", _I), ("tol", _D), ("miniter", _I), ("maxiter", _I),
         ("maxnorm", _I), ("mg_pre", _I), ("mg_post", _I),
         ("mg_coarse_max", _I), ("inner_rtol", _D), ("inner_maxiter", _I),
+        ("inner_flags", _I),
     ]
 
 
@@ -95,6 +97,8 @@ def lib():
     L.aphgpu_set_force_resident.argtypes = [_P, _I]
     L.aphgpu_last_timing.argtypes = [_P, _PD, ctypes.POINTER(ctypes.c_int64)]
     L.aphgpu_mark.argtypes = [_P, _I]
+    L.aphgpu_residual_history.argtypes = [_P, _I, _P, _I, ctypes.POINTER(_I)]
+    L.aphgpu_residual_history.restype = _I
     L.aphgpu_elapsed.argtypes = [_P, _I, _I, _PD]
     L.aphgpu_time_kernel.argtypes = [_P, _I, _I, _PD, _PD]
     for name in ("aphgpu_create", "aphgpu_sync", "aphgpu_set_system_expr",
@@ -263,6 +267,14 @@ class Context:
         n = ctypes.c_int64()
         self._check(self._L.aphgpu_last_timing(self._p, ctypes.byref(ms), ctypes.byref(n)))
         return ms.value, n.value
+
+    def residual_history(self, which=0):
+        n = _I()
+        self._check(self._L.aphgpu_residual_history(self._p, which, None, 0, ctypes.byref(n)))
+        out = np.empty(n.value)
+        self._check(self._L.aphgpu_residual_history(self._p, which, ptr(out), n.value,
+                                                    ctypes.byref(n)))
+        return out
 
     def mark(self, slot):
         self._check(self._L.aphgpu_mark(self._p, slot))

@@ -173,6 +173,7 @@ void aphgpu_conf_default(aphgpu_conf* c) {
   c->mg_coarse_max = 64;
   c->inner_rtol = 1e-4;
   c->inner_maxiter = 200;
+  c->inner_flags = 0;
 }
 
 int aphgpu_create(aphgpu_ctx** out, int nx, int ny, int nz, double h, int device) {
@@ -212,6 +213,7 @@ int aphgpu_create(aphgpu_ctx** out, int nx, int ny, int nz, double h, int device
   if ((rc = Alloc(ctx, &ctx->scal, 1))) return fail(rc);
   if ((rc = Alloc(ctx, &ctx->scal2, 1))) return fail(rc);
   if ((rc = Alloc(ctx, &ctx->flags, 4))) return fail(rc);
+  if ((rc = Alloc(ctx, &ctx->hist, 2 * (int64_t)kHistCap))) return fail(rc);
   ctx->red.max_blocks = (int)std::max<int64_t>(TileCount(ctx->d), 1024);
   if ((rc = Alloc(ctx, &ctx->red.part, (int64_t)kMaxRedVals * ctx->red.max_blocks)))
     return fail(rc);
@@ -346,6 +348,7 @@ int aphgpu_solve_resident(aphgpu_ctx* ctx, const aphgpu_conf* conf, int zero_gue
     case APHGPU_SOLVER_CG: rc = SolveCG(ctx, conf, info); break;
     case APHGPU_SOLVER_MGPCG: rc = SolveMGPCG(ctx, conf, info); break;
     case APHGPU_SOLVER_MIXED: rc = SolveMixed(ctx, conf, info); break;
+    case APHGPU_SOLVER_MGPCG32: rc = SolveMGPCG32(ctx, conf, info); break;
     default: return SetError(ctx, APHGPU_ERR_ARG, "unknown solver %d", conf->solver);
   }
   t.Stop();
@@ -359,6 +362,17 @@ int aphgpu_solve(aphgpu_ctx* ctx, const aphgpu_conf* conf, const double* x0, dou
   if (x0) APH_TRY(H2D(ctx, ctx->x, x0, sizeof(double) * ctx->N));
   APH_TRY(aphgpu_solve_resident(ctx, conf, x0 ? 0 : 1, info));
   if (x) APH_TRY(D2H(ctx, x, ctx->x, sizeof(double) * ctx->N));
+  return APHGPU_OK;
+}
+
+int aphgpu_residual_history(aphgpu_ctx* ctx, int which, double* out, int cap,
+                            int* count) {
+  if (!Valid(ctx) || (which != 0 && which != 1) || cap < 0) return APHGPU_ERR_ARG;
+  const std::vector<double>& h = which == 0 ? ctx->hist_outer : ctx->hist_inner;
+  if (count) *count = (int)h.size();
+  if (out) {
+    for (int i = 0; i < cap && i < (int)h.size(); ++i) out[i] = h[i];
+  }
   return APHGPU_OK;
 }
 

@@ -75,6 +75,7 @@ struct RedBuf {
   int max_blocks;
 };
 constexpr int kMaxRedVals = 4;
+constexpr int kHistCap = 4096;
 
 // op: 0 = sum, 1 = max
 template <int NV>
@@ -180,11 +181,16 @@ struct SolveScalars {
   double cellvol;
   double res_scale; // multiplies the residual (inner solves)
   double tmp[4];
+  double apsum;     // sum of A p (constant-mode projection)
+  double rzold;     // r_new . z_old (flexible beta)
+  double* hist;     // residual after each iteration (may be NULL)
+  int hist_cap;
   int iter;
   int miniter, maxiter, maxnorm;
   int done;
   int converged;
-  int pad[2];
+  int flags;        // bit 0 project constant mode, bit 1 flexible beta
+  int pad;
 };
 
 template <class T>
@@ -254,10 +260,12 @@ struct aphgpu_ctx {
   float* p32 = nullptr;
   float* ap32 = nullptr;
   float* z32 = nullptr;
-  float* rr32 = nullptr;       // inner residual
+  float* zold32 = nullptr;     // previous preconditioned residual (flexible CG)
   aphgpu::SolveScalars* scal = nullptr;   // outer
   aphgpu::SolveScalars* scal2 = nullptr;  // inner
   aphgpu::SolveScalars* hscal = nullptr;  // pinned host copy
+  double* hist = nullptr;      // device residual history, 2 x kHistCap
+  std::vector<double> hist_outer, hist_inner;
   aphgpu::RedBuf red{nullptr, nullptr, 0};
   unsigned int* flags = nullptr;  // 4 counters for validation kernels
   aphgpu::Multigrid mg;
@@ -330,6 +338,7 @@ int EnsureSolverVectors(aphgpu_ctx* ctx);
 int SolveCG(aphgpu_ctx* ctx, const aphgpu_conf* conf, aphgpu_info* info);
 int SolveMGPCG(aphgpu_ctx* ctx, const aphgpu_conf* conf, aphgpu_info* info);
 int SolveMixed(aphgpu_ctx* ctx, const aphgpu_conf* conf, aphgpu_info* info);
+int SolveMGPCG32(aphgpu_ctx* ctx, const aphgpu_conf* conf, aphgpu_info* info);
 int SetSystemExprDevice(aphgpu_ctx* ctx, const double* d_expr8);
 int AssembleProjectionDevice(aphgpu_ctx* ctx, const double* d_alpha,
                              double rho1, double rho2, const double* d_vflux,

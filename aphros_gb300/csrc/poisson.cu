@@ -324,6 +324,7 @@ __global__ void KCgUpdate(Dims d, double* x, double* r,
       s->beta = out[0] / (s->rr_prev + 1e-100);
       const double res = s->maxnorm ? out[1] / s->cellvol : sqrt(out[0] / s->cellvol);
       s->residual = res * s->res_scale;
+      if (s->hist && s->iter < s->hist_cap) s->hist[s->iter] = s->residual;
       s->iter += 1;
       if (s->iter >= s->miniter && (s->iter > s->maxiter || s->residual < s->tol)) {
         s->done = 1;
@@ -347,39 +348,44 @@ __global__ void KCgP(Dims d, const double* __restrict__ r, double* p,
 // Preconditioned CG building blocks (templated on the vector precision)
 // ---------------------------------------------------------------------------
 
-// ap = A p, reduces p.ap -> alpha = rz / p.ap
+// ap = A p, reduces p.ap -> alpha = rz / p.ap (and sum ap when projecting
+// the constant mode)
 template <class T>
 __global__ void KPcgApply(Op<T> A, const T* __restrict__ p, T* ap,
                           SolveScalars* s, RedBuf rb) {
   if (s->done) return;
-  double v[1] = {0};
-  const int op[1] = {0};
+  double v[2] = {0, 0};
+  const int op[2] = {0, 0};
   TILE_LOOP_BEGIN(A.d)
   const T y = Apply(A, p, i, j, k, c);
   ap[c] = y;
   v[0] += (double)p[c] * (double)y;
+  v[1] += (double)y;
   TILE_LOOP_END
-  __shared__ double out[1];
-  if (GridReduce<1>(v, op, rb, out)) {
+  __shared__ double out[2];
+  if (GridReduce<2>(v, op, rb, out)) {
     if (threadIdx.x == 0 && threadIdx.y == 0) {
       s->pap = out[0];
+      s->apsum = out[1];
       s->alpha = s->rz / (out[0] + 1e-300);
     }
   }
 }
 
-// x += alpha p, r -= alpha ap, reduces r.r and max|r|, then the stopping test
+// x += alpha p, r -= alpha (ap - mean(ap) when projecting), reduces r.r and
+// max|r|, then the stopping test
 template <class T>
 __global__ void KPcgUpdate(Dims d, T* x, T* r, const T* __restrict__ p,
                            const T* __restrict__ ap, SolveScalars* s,
                            RedBuf rb) {
   if (s->done) return;
   const T alpha = (T)s->alpha;
+  const T apm = (s->flags & 1) ? (T)(s->apsum / (double)d.cells()) : T(0);
   double v[2] = {0, 0};
   const int op[2] = {0, 1};
   TILE_LOOP_BEGIN(d)
   x[c] += alpha * p[c];
-  const T rn = r[c] - alpha * ap[c];
+  const T rn = r[c] - alpha * (ap[c] - apm);
   r[c] = rn;
   v[0] += (double)rn * (double)rn;
   v[1] = fmax(v[1], fabs((double)rn));
@@ -391,6 +397,7 @@ __global__ void KPcgUpdate(Dims d, T* x, T* r, const T* __restrict__ p,
       s->maxr = out[1];
       const double res = s->maxnorm ? out[1] / s->cellvol : sqrt(out[0] / s->cellvol);
       s->residual = res * s->res_scale;
+      if (s->hist && s->iter < s->hist_cap) s->hist[s->iter] = s->residual;
       s->iter += 1;
       if (s->iter >= s->miniter && (s->iter > s->maxiter || s->residual < s->tol)) {
         s->done = 1;
@@ -400,23 +407,29 @@ __global__ void KPcgUpdate(Dims d, T* x, T* r, const T* __restrict__ p,
   }
 }
 
-// rz = r.z; first == 1: p = z (start), else beta = rz/rz_prev, p = z + beta p
+// rz = r.z; first == 1: p = z (start), else beta = rz/rz_prev, or with the
+// flexible variant (flags bit 1) beta = (r.z - r.z_old)/rz_prev
 // (two passes: reduction kernel then update kernel)
 template <class T>
 __global__ void KDotRZ(Dims d, const T* __restrict__ r, const T* __restrict__ z,
-                       SolveScalars* s, RedBuf rb, int first) {
+                       const T* __restrict__ zold, SolveScalars* s, RedBuf rb,
+                       int first) {
   if (s->done) return;
-  double v[1] = {0};
-  const int op[1] = {0};
+  const bool flex = (s->flags & 2) && !first && zold;
+  double v[2] = {0, 0};
+  const int op[2] = {0, 0};
   TILE_LOOP_BEGIN(d)
   v[0] += (double)r[c] * (double)z[c];
+  if (flex) v[1] += (double)r[c] * (double)zold[c];
   TILE_LOOP_END
-  __shared__ double out[1];
-  if (GridReduce<1>(v, op, rb, out)) {
+  __shared__ double out[2];
+  if (GridReduce<2>(v, op, rb, out)) {
     if (threadIdx.x == 0 && threadIdx.y == 0) {
       s->rz_prev = first ? 0.0 : s->rz;
       s->rz = out[0];
-      s->beta = first ? 0.0 : out[0] / (s->rz_prev + 1e-300);
+      s->rzold = out[1];
+      const double num = flex ? out[0] - out[1] : out[0];
+      s->beta = first ? 0.0 : num / (s->rz_prev + 1e-300);
     }
   }
 }
@@ -762,8 +775,11 @@ Op<double> FineOp(aphgpu_ctx* ctx) {
 }
 
 int InitScalars(aphgpu_ctx* ctx, SolveScalars* s, const aphgpu_conf* conf,
-                double res_scale) {
+                double res_scale, double* hist = nullptr, int flags = 0) {
   SolveScalars h{};
+  h.hist = hist;
+  h.hist_cap = hist ? kHistCap : 0;
+  h.flags = flags;
   h.tol = conf->tol;
   h.cellvol = ctx->h * ctx->h * ctx->h;
   h.res_scale = res_scale;
@@ -966,21 +982,28 @@ int VCycle(aphgpu_ctx* ctx, std::vector<Level<T>>& lv, int pre, int post,
   return APHGPU_OK;
 }
 
-// Preconditioned CG on level 0 of `lv` with vectors x (solution, starting
-// from zero), r (holding b on entry), p, ap, z; scalars s.
-template <class T>
-int Pcg(aphgpu_ctx* ctx, std::vector<Level<T>>& lv, T* x, T* r, T* p, T* ap,
-        T* z, SolveScalars* s, const aphgpu_conf* conf, int check_every) {
-  Level<T>& f = lv[0];
-  const Dims d = f.d;
-  const Op<T> A = MakeOp(f);
+int SaveHistory(aphgpu_ctx* ctx, const double* d_hist, int n,
+                std::vector<double>& out) {
+  out.assign(std::min(n, kHistCap), 0.0);
+  if (!d_hist || out.empty()) return APHGPU_OK;
+  APH_CUDA(ctx, cudaMemcpyAsync(out.data(), d_hist, sizeof(double) * out.size(),
+                                cudaMemcpyDeviceToHost, ctx->stream));
+  APH_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+  return APHGPU_OK;
+}
+
+// Preconditioned CG with operator A and preconditioner `precond(r, z)`
+// on vectors x (iterate), r (residual on entry), p, ap, z, zold (zold only
+// for the flexible variant); scalars s (tolerances set by the caller).
+template <class T, class Precond>
+int Pcg(aphgpu_ctx* ctx, const Op<T>& A, Precond precond, T* x, T* r, T* p,
+        T* ap, T* z, T* zold, SolveScalars* s, const aphgpu_conf* conf,
+        int check_every) {
+  const Dims d = A.d;
   cudaStream_t st = ctx->stream;
   const dim3 tg = TileGrid(d), tb = TileBlock();
-  // z = M r ; p = z ; rz = r.z
-  f.b = r;
-  f.x = z;
-  APH_TRY(VCycle(ctx, lv, conf->mg_pre, conf->mg_post, s));
-  KDotRZ<T><<<tg, tb, 0, st>>>(d, r, z, s, ctx->red, 1);
+  APH_TRY(precond(r, z));
+  KDotRZ<T><<<tg, tb, 0, st>>>(d, r, z, nullptr, s, ctx->red, 1);
   APH_LAUNCHED(ctx);
   KPcgP<T><<<tg, tb, 0, st>>>(d, z, p, s, 1);
   APH_LAUNCHED(ctx);
@@ -992,8 +1015,9 @@ int Pcg(aphgpu_ctx* ctx, std::vector<Level<T>>& lv, T* x, T* r, T* p, T* ap,
       APH_LAUNCHED(ctx);
       KPcgUpdate<T><<<tg, tb, 0, st>>>(d, x, r, p, ap, s, ctx->red);
       APH_LAUNCHED(ctx);
-      APH_TRY(VCycle(ctx, lv, conf->mg_pre, conf->mg_post, s));
-      KDotRZ<T><<<tg, tb, 0, st>>>(d, r, z, s, ctx->red, 0);
+      if (zold) std::swap(z, zold);
+      APH_TRY(precond(r, z));
+      KDotRZ<T><<<tg, tb, 0, st>>>(d, r, z, zold, s, ctx->red, 0);
       APH_LAUNCHED(ctx);
       KPcgP<T><<<tg, tb, 0, st>>>(d, z, p, s, 0);
       APH_LAUNCHED(ctx);
@@ -1078,7 +1102,7 @@ int SolveCG(aphgpu_ctx* ctx, const aphgpu_conf* conf, aphgpu_info* info) {
   const Dims d = ctx->d;
   cudaStream_t st = ctx->stream;
   const dim3 tg = TileGrid(d), tb = TileBlock();
-  APH_TRY(InitScalars(ctx, ctx->scal, conf, 1.0));
+  APH_TRY(InitScalars(ctx, ctx->scal, conf, 1.0, ctx->hist));
   KCgInit<<<tg, tb, 0, st>>>(A, ctx->b, ctx->x, ctx->r, ctx->p, 0);
   APH_LAUNCHED(ctx);
   int batch = 4;
@@ -1098,10 +1122,23 @@ int SolveCG(aphgpu_ctx* ctx, const aphgpu_conf* conf, aphgpu_info* info) {
     if (hs.done || launched > (int64_t)conf->maxiter + 2) break;
     batch = std::min(batch * 2, 256);
   }
+  APH_TRY(SaveHistory(ctx, ctx->hist, hs.iter, ctx->hist_outer));
   info->residual = hs.residual;
   info->iter = hs.iter;
   info->inner_iter = 0;
   info->converged = hs.converged;
+  return APHGPU_OK;
+}
+
+int EnsureMixedVectors(aphgpu_ctx* ctx) {
+  if (ctx->r32) return APHGPU_OK;
+  const int64_t N = ctx->N;
+  APH_TRY(Alloc(ctx, &ctx->r32, N));
+  APH_TRY(Alloc(ctx, &ctx->x32, N));
+  APH_TRY(Alloc(ctx, &ctx->p32, N));
+  APH_TRY(Alloc(ctx, &ctx->ap32, N));
+  APH_TRY(Alloc(ctx, &ctx->z32, N));
+  APH_TRY(Alloc(ctx, &ctx->zold32, N));
   return APHGPU_OK;
 }
 
@@ -1113,16 +1150,63 @@ int SolveMGPCG(aphgpu_ctx* ctx, const aphgpu_conf* conf, aphgpu_info* info) {
   }
   const Op<double> A = FineOp(ctx);
   cudaStream_t st = ctx->stream;
-  APH_TRY(InitScalars(ctx, ctx->scal, conf, 1.0));
-  // r = b - A x0 (x holds the initial guess), then PCG on the correction
-  // would change the iterate; instead run PCG directly on x with r.
+  APH_TRY(InitScalars(ctx, ctx->scal, conf, 1.0, ctx->hist));
+  // r = b - A x0 (x holds the initial guess)
   KResidual64<<<TileGrid(ctx->d), TileBlock(), 0, st>>>(A, ctx->b, ctx->x, ctx->r,
                                                         ctx->scal, ctx->red, 0);
   APH_LAUNCHED(ctx);
-  APH_TRY(Pcg<double>(ctx, mg.l64, ctx->x, ctx->r, ctx->p, ctx->ap, ctx->z,
-                      ctx->scal, conf, 2));
+  auto& lv = mg.l64;
+  SolveScalars* s = ctx->scal;
+  auto precond = [&](double* r, double* z) -> int {
+    lv[0].b = r;
+    lv[0].x = z;
+    return VCycle(ctx, lv, conf->mg_pre, conf->mg_post, s);
+  };
+  APH_TRY(Pcg<double>(ctx, A, precond, ctx->x, ctx->r, ctx->p, ctx->ap, ctx->z,
+                      (double*)nullptr, s, conf, 2));
   SolveScalars hs;
-  APH_TRY(ReadScalars(ctx, ctx->scal, &hs));
+  APH_TRY(ReadScalars(ctx, s, &hs));
+  APH_TRY(SaveHistory(ctx, ctx->hist, hs.iter, ctx->hist_outer));
+  info->residual = hs.residual;
+  info->iter = hs.iter;
+  info->inner_iter = 0;
+  info->converged = hs.converged;
+  return APHGPU_OK;
+}
+
+// FP64 CG with an FP32 V-cycle as preconditioner (z = V32(r) converted).
+int SolveMGPCG32(aphgpu_ctx* ctx, const aphgpu_conf* conf, aphgpu_info* info) {
+  auto& mg = ctx->mg;
+  APH_TRY(EnsureMixedVectors(ctx));
+  if (!mg.built32) {
+    APH_TRY(BuildHierarchy<float>(ctx, mg.l32, conf->mg_coarse_max));
+    mg.built32 = true;
+  }
+  const Op<double> A = FineOp(ctx);
+  cudaStream_t st = ctx->stream;
+  const int64_t N = ctx->N;
+  const int fb = FlatBlocks(N);
+  APH_TRY(InitScalars(ctx, ctx->scal, conf, 1.0, ctx->hist));
+  KResidual64<<<TileGrid(ctx->d), TileBlock(), 0, st>>>(A, ctx->b, ctx->x, ctx->r,
+                                                        ctx->scal, ctx->red, 0);
+  APH_LAUNCHED(ctx);
+  auto& lv = mg.l32;
+  SolveScalars* s = ctx->scal;
+  auto precond = [&](double* r, double* z) -> int {
+    KConvert<double, float><<<fb, kFlatThreads, 0, st>>>(N, r, ctx->r32, 1.0);
+    APH_LAUNCHED(ctx);
+    lv[0].b = ctx->r32;
+    lv[0].x = ctx->z32;
+    APH_TRY(VCycle(ctx, lv, conf->mg_pre, conf->mg_post, s));
+    KConvert<float, double><<<fb, kFlatThreads, 0, st>>>(N, ctx->z32, z, 1.0);
+    APH_LAUNCHED(ctx);
+    return APHGPU_OK;
+  };
+  APH_TRY(Pcg<double>(ctx, A, precond, ctx->x, ctx->r, ctx->p, ctx->ap, ctx->z,
+                      (double*)nullptr, s, conf, 2));
+  SolveScalars hs;
+  APH_TRY(ReadScalars(ctx, s, &hs));
+  APH_TRY(SaveHistory(ctx, ctx->hist, hs.iter, ctx->hist_outer));
   info->residual = hs.residual;
   info->iter = hs.iter;
   info->inner_iter = 0;
@@ -1133,30 +1217,35 @@ int SolveMGPCG(aphgpu_ctx* ctx, const aphgpu_conf* conf, aphgpu_info* info) {
 int SolveMixed(aphgpu_ctx* ctx, const aphgpu_conf* conf, aphgpu_info* info) {
   auto& mg = ctx->mg;
   const int64_t N = ctx->N;
-  if (!ctx->r32) {
-    APH_TRY(Alloc(ctx, &ctx->r32, N));
-    APH_TRY(Alloc(ctx, &ctx->x32, N));
-    APH_TRY(Alloc(ctx, &ctx->p32, N));
-    APH_TRY(Alloc(ctx, &ctx->ap32, N));
-    APH_TRY(Alloc(ctx, &ctx->z32, N));
-  }
+  APH_TRY(EnsureMixedVectors(ctx));
   if (!mg.built32) {
     APH_TRY(BuildHierarchy<float>(ctx, mg.l32, conf->mg_coarse_max));
     mg.built32 = true;
   }
   const Op<double> A = FineOp(ctx);
+  const Op<float> A32 = MakeOp(mg.l32[0]);
   cudaStream_t st = ctx->stream;
   const int fb = FlatBlocks(N);
   APH_TRY(InitScalars(ctx, ctx->scal, conf, 1.0));
+  ctx->hist_outer.clear();
+  ctx->hist_inner.clear();
   SolveScalars hs{};
   int outer = 0, inner_total = 0;
   aphgpu_conf ic = *conf;
+  auto& lv = mg.l32;
+  SolveScalars* s2 = ctx->scal2;
+  auto precond = [&](float* r, float* z) -> int {
+    lv[0].b = r;
+    lv[0].x = z;
+    return VCycle(ctx, lv, conf->mg_pre, conf->mg_post, s2);
+  };
   for (;;) {
-    // outer residual in FP64 and the stopping test (count as iteration)
+    // outer residual in FP64 and the stopping test
     KResidual64<<<TileGrid(ctx->d), TileBlock(), 0, st>>>(A, ctx->b, ctx->x, ctx->r,
                                                           ctx->scal, ctx->red, 1);
     APH_LAUNCHED(ctx);
     APH_TRY(ReadScalars(ctx, ctx->scal, &hs));
+    ctx->hist_outer.push_back(hs.residual);
     if (hs.done || (outer >= conf->miniter && hs.residual < conf->tol)) {
       hs.converged = hs.residual < conf->tol;
       break;
@@ -1167,29 +1256,30 @@ int SolveMixed(aphgpu_ctx* ctx, const aphgpu_conf* conf, aphgpu_info* info) {
     APH_LAUNCHED(ctx);
     KZeroF<<<fb, kFlatThreads, 0, st>>>(N, ctx->x32);
     APH_LAUNCHED(ctx);
-    // inner stopping: residual (of the scaled system, L2 over cells) below
-    // inner_rtol times its initial value
     const double scale = hs.maxr > 0 ? hs.maxr : 1.0;
     const double r0 = std::sqrt(hs.rr / (ctx->h * ctx->h * ctx->h)) / scale;
     ic.tol = conf->inner_rtol * r0;
     ic.miniter = 1;
     ic.maxiter = conf->inner_maxiter;
     ic.maxnorm = 0;
-    APH_TRY(InitScalars(ctx, ctx->scal2, &ic, 1.0));
-    APH_TRY(Pcg<float>(ctx, mg.l32, ctx->x32, ctx->r32, ctx->p32, ctx->ap32,
-                       ctx->z32, ctx->scal2, &ic, 2));
+    APH_TRY(InitScalars(ctx, s2, &ic, 1.0, ctx->hist + kHistCap, conf->inner_flags));
+    APH_TRY(Pcg<float>(ctx, A32, precond, ctx->x32, ctx->r32, ctx->p32, ctx->ap32,
+                       ctx->z32, (conf->inner_flags & 2) ? ctx->zold32 : (float*)nullptr,
+                       s2, &ic, 2));
     SolveScalars is;
-    APH_TRY(ReadScalars(ctx, ctx->scal2, &is));
+    APH_TRY(ReadScalars(ctx, s2, &is));
     inner_total += is.iter;
+    std::vector<double> h;
+    APH_TRY(SaveHistory(ctx, ctx->hist + kHistCap, is.iter, h));
+    for (double v : h) ctx->hist_inner.push_back(v / r0);
+    ctx->hist_inner.push_back(-1.0);  // separator between inner solves
     KAddCorrection<<<fb, kFlatThreads, 0, st>>>(N, ctx->x, ctx->x32, ctx->scal);
     APH_LAUNCHED(ctx);
     ++outer;
-    // iteration count of the outer loop lives in scal->iter
-    SolveScalars up = hs;
-    up.iter = outer;
-    up.done = 0;
-    APH_CUDA(ctx, cudaMemcpyAsync(&ctx->scal->iter, &up.iter, sizeof(int),
+    const int it = outer;
+    APH_CUDA(ctx, cudaMemcpyAsync(&ctx->scal->iter, &it, sizeof(int),
                                   cudaMemcpyHostToDevice, st));
+    APH_CUDA(ctx, cudaStreamSynchronize(st));
   }
   info->residual = hs.residual;
   info->iter = outer;
@@ -1198,13 +1288,6 @@ int SolveMixed(aphgpu_ctx* ctx, const aphgpu_conf* conf, aphgpu_info* info) {
   return APHGPU_OK;
 }
 
-int SystemToExprDevice(aphgpu_ctx* ctx, double* d_e8) {
-  KSystemToExpr<<<TileGrid(ctx->d), TileBlock(), 0, ctx->stream>>>(FineOp(ctx), ctx->b, d_e8);
-  APH_LAUNCHED(ctx);
-  return APHGPU_OK;
-}
-
-// Times one solver kernel on the resident data (see aphgpu_time_kernel).
 int TimeSolverKernel(aphgpu_ctx* ctx, int kernel, int reps, double* ms,
                      double* bytes) {
   cudaStream_t st = ctx->stream;

@@ -41,7 +41,8 @@ enum {
 enum {
   APHGPU_SOLVER_CG = 0,    /* plain FP64 CG, the algorithm of SolverConjugate */
   APHGPU_SOLVER_MGPCG = 1, /* FP64 CG preconditioned by an FP64 MG V-cycle */
-  APHGPU_SOLVER_MIXED = 2  /* FP64 defect correction around FP32 MG-PCG */
+  APHGPU_SOLVER_MIXED = 2, /* FP64 defect correction around FP32 MG-PCG */
+  APHGPU_SOLVER_MGPCG32 = 3 /* FP64 CG preconditioned by an FP32 V-cycle */
 };
 
 /* Stopping rule and limits; mirrors linear::Solver::Conf
@@ -60,6 +61,11 @@ typedef struct {
   /* mixed precision: relative reduction asked of each inner FP32 solve */
   double inner_rtol;
   int inner_maxiter;
+  /* inner FP32 PCG options: bit 0 keeps the residual free of the constant
+   * (null-space) component that FP32 rounding adds to A p; bit 1 uses the
+   * flexible (Polak-Ribiere) beta, robust to the FP32 preconditioner's
+   * rounding */
+  int inner_flags;
 } aphgpu_conf;
 
 /* Result; mirrors linear::Solver::Info (linear.h:27-30).  `iter` counts
@@ -133,6 +139,13 @@ int aphgpu_solve(aphgpu_ctx* ctx, const aphgpu_conf* conf, const double* x0,
  * from zero, leaving the solution resident. */
 int aphgpu_solve_resident(aphgpu_ctx* ctx, const aphgpu_conf* conf,
                           int zero_guess, aphgpu_info* info);
+
+/* Residual history of the last solve: which = 0 the (outer) iterations,
+ * which = 1 the inner FP32 iterations of a mixed solve (all inner solves
+ * concatenated).  Copies at most cap values; *count receives the number
+ * available. */
+int aphgpu_residual_history(aphgpu_ctx* ctx, int which, double* out, int cap,
+                            int* count);
 
 /* Copies the resident solution (pressure) to the host. */
 int aphgpu_get_solution(aphgpu_ctx* ctx, double* x);

@@ -90,11 +90,19 @@ def proj16(tmp):
          repr(case.rho2), repr(tol), "100000", "alpha.bin", "vf.bin", "pr"], tmp)
     r = lambda s: np.fromfile(os.path.join(tmp, "pr." + s))
     info = open(os.path.join(tmp, "pr.info")).read().split()
+    expr_ref, p_ref, flux_ref = r("expr"), r("p"), r("flux")
+    # the same solve on 8 blocks of 8^3: the reference's own spread due to
+    # the order of its reductions
+    run(["proj", str(n), "8", repr(h), repr(case.dt), repr(case.rho1),
+         repr(case.rho2), repr(tol), "100000", "alpha.bin", "vf.bin", "pr8"], tmp)
+    info8 = open(os.path.join(tmp, "pr8.info")).read().split()
+    p8 = np.fromfile(os.path.join(tmp, "pr8.p"))
     np.savez_compressed(os.path.join(OUT, "proj16.npz"), n=n, h=h, dt=case.dt,
                         rho1=case.rho1, rho2=case.rho2, tol=tol, alpha=case.alpha,
-                        vflux=case.flux, expr_ref=r("expr"), p_ref=r("p"),
-                        flux_ref=r("flux"), residual=float(info[0]),
-                        iters=int(info[1]))
+                        vflux=case.flux, expr_ref=expr_ref, p_ref=p_ref,
+                        flux_ref=flux_ref, residual=float(info[0]),
+                        iters=int(info[1]), iters_blocks8=int(info8[1]),
+                        p_blocks8=p8)
 
 
 def vof32(tmp):
