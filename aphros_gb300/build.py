@@ -69,7 +69,9 @@ def build_cuda(verbose=False):
                 print(out)
     lib = os.path.join(BUILD, "libaphgpu.so")
     if _newer(lib, objs):
-        _run([NVCC] + ARCH + ["-shared", "-o", lib] + objs + ["-lcudart"])
+        # --no-undefined: a missing definition fails the build, not the load
+        _run([NVCC] + ARCH + ["-shared", "-o", lib] + objs +
+             ["-lcudart", "-Xlinker", "--no-undefined"])
     return lib
 
 

@@ -1379,6 +1379,12 @@ int TimeSolverKernel(aphgpu_ctx* ctx, int kernel, int reps, double* ms,
   return APHGPU_OK;
 }
 
+int SystemToExprDevice(aphgpu_ctx* ctx, double* d_e8) {
+  KSystemToExpr<<<TileGrid(ctx->d), TileBlock(), 0, ctx->stream>>>(FineOp(ctx), ctx->b, d_e8);
+  APH_LAUNCHED(ctx);
+  return APHGPU_OK;
+}
+
 int ResidualNorms(aphgpu_ctx* ctx, double* rnorm, double* bnorm) {
   aphgpu_conf c;
   aphgpu_conf_default(&c);
