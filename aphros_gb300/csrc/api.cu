@@ -171,9 +171,9 @@ void aphgpu_conf_default(aphgpu_conf* c) {
   c->mg_pre = 2;
   c->mg_post = 2;
   c->mg_coarse_max = 64;
-  c->inner_rtol = 1e-4;
+  c->inner_rtol = 1e-3;
   c->inner_maxiter = 200;
-  c->inner_flags = 0;
+  c->inner_flags = 3;
 }
 
 int aphgpu_create(aphgpu_ctx** out, int nx, int ny, int nz, double h, int device) {

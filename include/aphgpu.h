@@ -79,7 +79,8 @@ typedef struct {
 } aphgpu_info;
 
 /* Fills `conf` with defaults: MG-PCG, tol 0, miniter 1, maxiter 1000,
- * L2 norm, 2+2 sweeps, coarsest <= 512 cells, inner_rtol 1e-4. */
+ * L2 norm, 2+2 sweeps, coarsest <= 64 cells, inner_rtol 1e-3,
+ * inner_maxiter 200, inner_flags 3 (projection and flexible beta). */
 void aphgpu_conf_default(aphgpu_conf* conf);
 
 /* ---- context ---- */
