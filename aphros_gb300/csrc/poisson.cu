@@ -1262,7 +1262,11 @@ int SolveMixed(aphgpu_ctx* ctx, const aphgpu_conf* conf, aphgpu_info* info) {
     ic.miniter = 1;
     ic.maxiter = conf->inner_maxiter;
     ic.maxnorm = 0;
-    APH_TRY(InitScalars(ctx, s2, &ic, 1.0, ctx->hist + kHistCap, conf->inner_flags));
+    // the constant-mode projection is only valid for the singular
+    // flux-difference operator (constant null space), not for systems with
+    // an explicit diagonal shift
+    const int flags = ctx->diag_explicit ? (conf->inner_flags & ~1) : conf->inner_flags;
+    APH_TRY(InitScalars(ctx, s2, &ic, 1.0, ctx->hist + kHistCap, flags));
     APH_TRY(Pcg<float>(ctx, A32, precond, ctx->x32, ctx->r32, ctx->p32, ctx->ap32,
                        ctx->z32, (conf->inner_flags & 2) ? ctx->zold32 : (float*)nullptr,
                        s2, &ic, 2));
