@@ -34,6 +34,7 @@ CU_UNITS = {
     "api.cu": [],
     "poisson.cu": [],
     "vof.cu": ["-fmad=false"],
+    "noalloc.cu": [],
 }
 
 

@@ -212,6 +212,31 @@ int aphgpu_set_force_resident(aphgpu_ctx* ctx, int on);
  * call measured on the device, and the number of kernels it launched. */
 int aphgpu_last_timing(const aphgpu_ctx* ctx, double* ms, int64_t* launches);
 
+/* Plain FP64 CG solve (the algorithm of aphgpu_solve with
+ * APHGPU_SOLVER_CG) that allocates no memory at all.  This entry point has
+ * no counterpart in the reference; it exists for callers that cannot call
+ * cudaMalloc: code recording a CUDA graph, host callbacks and real-time step
+ * loops that must not block on the allocator, or plug-ins in a process whose
+ * device memory pool is owned by someone else.  Such callers already own
+ * their inputs and outputs; the solver's work vectors live in one fixed
+ * device array inside the library (about 1.6 MB, held on every GPU that
+ * loads the library until the process exits).
+ *   d_expr8: device array, 8 doubles per cell (see aphgpu_set_system_expr);
+ *   d_x0: device initial guess or NULL (zero), may equal d_x;
+ *   d_x: device solution;  cellvol: h^3 of the residual norm;
+ *   tol, miniter, maxiter, maxnorm: as in aphgpu_conf;  stream: the
+ *   cudaStream_t to run on (NULL: the default stream).
+ * Limits: at most 65536 cells (e.g. 64x32x32 or 40^3) and every dimension
+ * >= 3; larger grids return APHGPU_ERR_ARG (no context, so no message).
+ * The first call on a device looks up the array's device address while that
+ * device is current: make it before any stream capture.  All calls share
+ * the array: calls whose work overlaps on the GPU race and must be
+ * serialized by the caller.  Returns after the solve has finished. */
+int aphgpu_cg_solve_noalloc(int nx, int ny, int nz, double cellvol,
+                            const double* d_expr8, const double* d_x0,
+                            double* d_x, double tol, int miniter, int maxiter,
+                            int maxnorm, void* stream, aphgpu_info* info);
+
 /* Records event `slot` (0..7) on the context's stream; aphgpu_elapsed
  * returns the milliseconds between two recorded slots (waits for the
  * second). */
