@@ -214,7 +214,7 @@ int aphgpu_create(aphgpu_ctx** out, int nx, int ny, int nz, double h, int device
   if ((rc = Alloc(ctx, &ctx->scal2, 1))) return fail(rc);
   if ((rc = Alloc(ctx, &ctx->flags, 4))) return fail(rc);
   if ((rc = Alloc(ctx, &ctx->hist, 2 * (int64_t)kHistCap))) return fail(rc);
-  ctx->red.max_blocks = (int)std::max<int64_t>(TileCount(ctx->d), 1024);
+  ctx->red.max_blocks = (int)std::max<int64_t>(TileCount(ctx->d), 4096);
   if ((rc = Alloc(ctx, &ctx->red.part, (int64_t)kMaxRedVals * ctx->red.max_blocks)))
     return fail(rc);
   if ((rc = Alloc(ctx, &ctx->red.ticket, 1))) return fail(rc);

@@ -216,7 +216,13 @@ struct Multigrid {
   double* cap = nullptr;
   double* cx = nullptr;
   double* cb = nullptr;
+  // dense inverse of the coarsest operator (A + 11^T mean(diag)/n),
+  // FP64, one per hierarchy (n x n, n <= kDenseMax)
+  double* cinv64 = nullptr;
+  double* cinv32 = nullptr;
+  int cn64 = 0, cn32 = 0;
 };
+constexpr int kDenseMax = 1024;
 
 }  // namespace aphgpu
 

@@ -476,6 +476,376 @@ __global__ void KSmooth(Op<T> A, const T* __restrict__ invdiag,
   TILE_LOOP_END
 }
 
+// ---------------------------------------------------------------------------
+// Vectorized FP32 kernels (nx % 4 == 0): each thread owns 4 consecutive
+// cells in x (one float4), a CTA of 32x8 threads covers 128 x 8 cells of a
+// plane and marches over kVecZ planes in z, keeping the z neighbours in
+// registers.  x neighbours across float4 boundaries come from warp shuffles
+// (global loads at warp and domain edges, periodic wrap).
+// ---------------------------------------------------------------------------
+
+constexpr int kVecZ = 16;
+
+inline dim3 VecGrid(const Dims& d) {
+  const int nq = d.nx / 4;
+  return dim3((nq + 31) / 32, (d.ny + 7) / 8, (d.nz + kVecZ - 1) / kVecZ);
+}
+inline bool VecOk(const Dims& d) { return (d.nx % 4) == 0 && d.nx >= 8; }
+
+__device__ __forceinline__ float4 Ld4(const float* p) {
+  return *reinterpret_cast<const float4*>(p);
+}
+__device__ __forceinline__ void St4(float* p, float4 v) {
+  *reinterpret_cast<float4*>(p) = v;
+}
+__device__ __forceinline__ float El(const float4& v, int e) {
+  return e == 0 ? v.x : e == 1 ? v.y : e == 2 ? v.z : v.w;
+}
+__device__ __forceinline__ void SetEl(float4& v, int e, float a) {
+  if (e == 0) v.x = a; else if (e == 1) v.y = a; else if (e == 2) v.z = a; else v.w = a;
+}
+
+// Left value (cell 4q-1) and right value (cell 4q+4) of a float4 row segment;
+// every lane of the warp must call it (inactive lanes pass anything).
+__device__ __forceinline__ void XHalo(const float* row, float4 v, int q, int nq,
+                                      bool act, float& l, float& r) {
+  const int lane = threadIdx.x;
+  l = __shfl_up_sync(0xffffffffu, v.w, 1);
+  r = __shfl_down_sync(0xffffffffu, v.x, 1);
+  if (act) {
+    if (lane == 0 || q == 0) l = row[q == 0 ? 4 * nq - 1 : 4 * q - 1];
+    if (lane == 31 || q == nq - 1) r = row[q == nq - 1 ? 0 : 4 * q + 4];
+  }
+}
+
+// One red-black half sweep (FP32, vectorized); see KSmooth for the update.
+// The diagonal is recomputed from the six couplings (read anyway) unless the
+// operator stores one.
+__global__ void __launch_bounds__(256) KSmooth4(Op<float> A, const float* __restrict__ b,
+                                                float* x, int color, int zero_init,
+                                                const SolveScalars* s) {
+  if (s && s->done) return;
+  const Dims d = A.d;
+  const int nq = d.nx >> 2;
+  const int q = blockIdx.x * 32 + threadIdx.x;
+  const int j = blockIdx.y * 8 + threadIdx.y;
+  const bool act = q < nq && j < d.ny;
+  const int kb = blockIdx.z * kVecZ;
+  const int ke = min(kb + kVecZ, d.nz);
+  const int jm = wrapm(j - 1, d.ny), jp = wrapp(j + 1, d.ny);
+  const int i0 = 4 * q;
+  float4 xz0 = make_float4(0, 0, 0, 0), xz1 = xz0, xz2 = xz0, wz1 = xz0, wz2 = xz0;
+  if (act && !zero_init) {
+    xz0 = Ld4(x + d.idx(i0, j, wrapm(kb - 1, d.nz)));
+    xz1 = Ld4(x + d.idx(i0, j, kb));
+  }
+  if (act) wz1 = Ld4(A.w2 + d.idx(i0, j, kb));
+  for (int k = kb; k < ke; ++k) {
+    const int kp = wrapp(k + 1, d.nz);
+    const int64_t c = d.idx(i0, j, k);
+    float4 w0v = xz0, w1v = xz0, w1n = xz0, bv = xz0, xjm = xz0, xjp = xz0;
+    if (act) {
+      wz2 = Ld4(A.w2 + d.idx(i0, j, kp));
+      w0v = Ld4(A.w0 + c);
+      w1v = Ld4(A.w1 + c);
+      w1n = Ld4(A.w1 + d.idx(i0, jp, k));
+      bv = Ld4(b + c);
+      if (!zero_init) {
+        xz2 = Ld4(x + d.idx(i0, j, kp));
+        xjm = Ld4(x + d.idx(i0, jm, k));
+        xjp = Ld4(x + d.idx(i0, jp, k));
+      }
+    }
+    float xl, xr, wl, wr;
+    XHalo(x + d.idx(0, j, k), xz1, q, nq, act && !zero_init, xl, xr);
+    XHalo(A.w0 + d.idx(0, j, k), w0v, q, nq, act, wl, wr);
+    (void)wl;
+    if (act) {
+      float4 out = xz1;
+      const int e0 = (color + j + k) & 1;
+#pragma unroll
+      for (int e = 0; e < 4; ++e) {
+        if ((e & 1) != e0) continue;
+        const float cxm = El(w0v, e);
+        const float cxp = e == 3 ? wr : El(w0v, e + 1);
+        const float cym = El(w1v, e), cyp = El(w1n, e);
+        const float czm = El(wz1, e), czp = El(wz2, e);
+        const float dg = A.diag ? A.diag[c + e]
+                                : -(((((cxm + cxp) + cym) + cyp) + czm) + czp);
+        float acc = El(bv, e);
+        if (!zero_init) {
+          const float vxm = e == 0 ? xl : El(xz1, e - 1);
+          const float vxp = e == 3 ? xr : El(xz1, e + 1);
+          acc -= cxm * vxm;
+          acc -= cxp * vxp;
+          acc -= cym * El(xjm, e);
+          acc -= cyp * El(xjp, e);
+          acc -= czm * El(xz0, e);
+          acc -= czp * El(xz2, e);
+        }
+        SetEl(out, e, acc / dg);
+      }
+      St4(x + c, out);
+    }
+    xz0 = xz1;
+    xz1 = xz2;
+    wz1 = wz2;
+  }
+}
+
+// y = A p (FP32, vectorized) with the reductions p.y and sum y of KPcgApply
+__global__ void __launch_bounds__(256) KPcgApply4(Op<float> A, const float* __restrict__ p,
+                                                  float* ap, SolveScalars* s, RedBuf rb) {
+  if (s->done) return;
+  const Dims d = A.d;
+  const int nq = d.nx >> 2;
+  const int q = blockIdx.x * 32 + threadIdx.x;
+  const int j = blockIdx.y * 8 + threadIdx.y;
+  const bool act = q < nq && j < d.ny;
+  const int kb = blockIdx.z * kVecZ;
+  const int ke = min(kb + kVecZ, d.nz);
+  const int jm = wrapm(j - 1, d.ny), jp = wrapp(j + 1, d.ny);
+  const int i0 = 4 * q;
+  // per-thread sums in FP32 (at most 4 * kVecZ terms), CTA and grid sums in
+  // FP64: FP64 arithmetic is scarce on GB300
+  float fa0 = 0.f, fa1 = 0.f;
+  float4 z0 = make_float4(0, 0, 0, 0), z1 = z0, z2 = z0, wz1 = z0, wz2 = z0;
+  if (act) {
+    z0 = Ld4(p + d.idx(i0, j, wrapm(kb - 1, d.nz)));
+    z1 = Ld4(p + d.idx(i0, j, kb));
+    wz1 = Ld4(A.w2 + d.idx(i0, j, kb));
+  }
+  for (int k = kb; k < ke; ++k) {
+    const int kp = wrapp(k + 1, d.nz);
+    const int64_t c = d.idx(i0, j, k);
+    float4 w0v = z0, w1v = z0, w1n = z0, pjm = z0, pjp = z0;
+    if (act) {
+      z2 = Ld4(p + d.idx(i0, j, kp));
+      wz2 = Ld4(A.w2 + d.idx(i0, j, kp));
+      w0v = Ld4(A.w0 + c);
+      w1v = Ld4(A.w1 + c);
+      w1n = Ld4(A.w1 + d.idx(i0, jp, k));
+      pjm = Ld4(p + d.idx(i0, jm, k));
+      pjp = Ld4(p + d.idx(i0, jp, k));
+    }
+    float pl, pr, wl, wr;
+    XHalo(p + d.idx(0, j, k), z1, q, nq, act, pl, pr);
+    XHalo(A.w0 + d.idx(0, j, k), w0v, q, nq, act, wl, wr);
+    (void)wl;
+    if (act) {
+      float4 out;
+#pragma unroll
+      for (int e = 0; e < 4; ++e) {
+        const float cxm = El(w0v, e);
+        const float cxp = e == 3 ? wr : El(w0v, e + 1);
+        const float cym = El(w1v, e), cyp = El(w1n, e);
+        const float czm = El(wz1, e), czp = El(wz2, e);
+        const float dg = A.diag ? A.diag[c + e]
+                                : -(((((cxm + cxp) + cym) + cyp) + czm) + czp);
+        const float pc = El(z1, e);
+        float y = pc * dg;
+        y += (e == 0 ? pl : El(z1, e - 1)) * cxm;
+        y += (e == 3 ? pr : El(z1, e + 1)) * cxp;
+        y += El(pjm, e) * cym;
+        y += El(pjp, e) * cyp;
+        y += El(z0, e) * czm;
+        y += El(z2, e) * czp;
+        SetEl(out, e, y);
+        fa0 += pc * y;
+        fa1 += y;
+      }
+      St4(ap + c, out);
+    }
+    z0 = z1;
+    z1 = z2;
+    wz1 = wz2;
+  }
+  double v[2] = {(double)fa0, (double)fa1};
+  const int op[2] = {0, 0};
+  __shared__ double out2[2];
+  if (GridReduce<2>(v, op, rb, out2)) {
+    if (threadIdx.x == 0 && threadIdx.y == 0) {
+      s->pap = out2[0];
+      s->apsum = out2[1];
+      s->alpha = s->rz / (out2[0] + 1e-300);
+    }
+  }
+}
+
+// x_fine += x_coarse(parent), FP32 vectorized (one float4 = 2 coarse cells)
+__global__ void KProlong4(Dims d, float* x, Dims dc, const float* __restrict__ xc,
+                          const SolveScalars* s) {
+  if (s && s->done) return;
+  const int nq = d.nx >> 2;
+  const int q = blockIdx.x * 32 + threadIdx.x;
+  const int j = blockIdx.y * 8 + threadIdx.y;
+  if (q >= nq || j >= d.ny) return;
+  const int kb = blockIdx.z * kVecZ;
+  const int ke = min(kb + kVecZ, d.nz);
+  for (int k = kb; k < ke; ++k) {
+    const int64_t c = d.idx(4 * q, j, k);
+    const float2 e = *reinterpret_cast<const float2*>(xc + dc.idx(2 * q, j >> 1, k >> 1));
+    float4 v = Ld4(x + c);
+    v.x += e.x;
+    v.y += e.x;
+    v.z += e.y;
+    v.w += e.y;
+    St4(x + c, v);
+  }
+}
+
+// x += alpha p, r -= alpha (ap - mean(ap)), reductions and stopping test of
+// KPcgUpdate, FP32 vectorized over flat float4s (n % 4 == 0)
+__global__ void __launch_bounds__(256) KPcgUpdate4(int64_t n4, float* x, float* r,
+                                                   const float* __restrict__ p,
+                                                   const float* __restrict__ ap,
+                                                   SolveScalars* s, RedBuf rb, int64_t ncells) {
+  if (s->done) return;
+  const float alpha = (float)s->alpha;
+  const float apm = (s->flags & 1) ? (float)(s->apsum / (double)ncells) : 0.f;
+  float r2 = 0.f, rmax = 0.f;
+  for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < n4;
+       t += (int64_t)gridDim.x * blockDim.x) {
+    float4 xv = Ld4(x + 4 * t), rv = Ld4(r + 4 * t);
+    const float4 pv = Ld4(p + 4 * t), av = Ld4(ap + 4 * t);
+    xv.x += alpha * pv.x; xv.y += alpha * pv.y; xv.z += alpha * pv.z; xv.w += alpha * pv.w;
+    rv.x -= alpha * (av.x - apm); rv.y -= alpha * (av.y - apm);
+    rv.z -= alpha * (av.z - apm); rv.w -= alpha * (av.w - apm);
+    St4(x + 4 * t, xv);
+    St4(r + 4 * t, rv);
+    r2 += rv.x * rv.x + rv.y * rv.y + rv.z * rv.z + rv.w * rv.w;
+    rmax = fmaxf(rmax, fmaxf(fmaxf(fabsf(rv.x), fabsf(rv.y)), fmaxf(fabsf(rv.z), fabsf(rv.w))));
+  }
+  double v[2] = {(double)r2, (double)rmax};
+  const int op[2] = {0, 1};
+  __shared__ double out[2];
+  if (GridReduce<2>(v, op, rb, out)) {
+    if (threadIdx.x == 0) {
+      s->rr = out[0];
+      s->maxr = out[1];
+      const double res = s->maxnorm ? out[1] / s->cellvol : sqrt(out[0] / s->cellvol);
+      s->residual = res * s->res_scale;
+      if (s->hist && s->iter < s->hist_cap) s->hist[s->iter] = s->residual;
+      s->iter += 1;
+      if (s->iter >= s->miniter && (s->iter > s->maxiter || s->residual < s->tol)) {
+        s->done = 1;
+        s->converged = s->residual < s->tol;
+      }
+    }
+  }
+}
+
+// r.z (and r.z_old for the flexible beta), FP32 vectorized; see KDotRZ
+__global__ void __launch_bounds__(256) KDotRZ4(int64_t n4, const float* __restrict__ r,
+                                               const float* __restrict__ z,
+                                               const float* __restrict__ zold,
+                                               SolveScalars* s, RedBuf rb, int first) {
+  if (s->done) return;
+  const bool flex = (s->flags & 2) && !first && zold;
+  float a = 0.f, b = 0.f;
+  for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < n4;
+       t += (int64_t)gridDim.x * blockDim.x) {
+    const float4 rv = Ld4(r + 4 * t), zv = Ld4(z + 4 * t);
+    a += rv.x * zv.x + rv.y * zv.y + rv.z * zv.z + rv.w * zv.w;
+    if (flex) {
+      const float4 ov = Ld4(zold + 4 * t);
+      b += rv.x * ov.x + rv.y * ov.y + rv.z * ov.z + rv.w * ov.w;
+    }
+  }
+  double v[2] = {(double)a, (double)b};
+  const int op[2] = {0, 0};
+  __shared__ double out[2];
+  if (GridReduce<2>(v, op, rb, out)) {
+    if (threadIdx.x == 0) {
+      s->rz_prev = first ? 0.0 : s->rz;
+      s->rz = out[0];
+      s->rzold = out[1];
+      const double num = flex ? out[0] - out[1] : out[0];
+      s->beta = first ? 0.0 : num / (s->rz_prev + 1e-300);
+    }
+  }
+}
+
+// p = z + beta p (p = z when first), FP32 vectorized
+__global__ void KPcgP4(int64_t n4, const float* __restrict__ z, float* p,
+                       const SolveScalars* s, int first) {
+  if (s->done) return;
+  const float beta = (float)s->beta;
+  for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < n4;
+       t += (int64_t)gridDim.x * blockDim.x) {
+    const float4 zv = Ld4(z + 4 * t);
+    float4 pv = first ? zv : Ld4(p + 4 * t);
+    if (!first) {
+      pv.x = zv.x + beta * pv.x; pv.y = zv.y + beta * pv.y;
+      pv.z = zv.z + beta * pv.z; pv.w = zv.w + beta * pv.w;
+    }
+    St4(p + 4 * t, pv);
+  }
+}
+
+// Residual of a fine FP32 level summed over the 8 children into the coarse
+// right-hand side, vectorized: a thread owns one fine float4 (2 coarse
+// cells in x) of a coarse row and marches over coarse planes.
+__global__ void __launch_bounds__(256) KResidualRestrict4(Op<float> A, const float* __restrict__ b,
+                                                          const float* __restrict__ x, Dims dc,
+                                                          float* bc, const SolveScalars* s) {
+  if (s && s->done) return;
+  const Dims d = A.d;
+  const int nq = d.nx >> 2;
+  const int q = blockIdx.x * 32 + threadIdx.x;
+  const int J = blockIdx.y * 8 + threadIdx.y;
+  const bool act = q < nq && J < dc.ny;
+  const int Kb = blockIdx.z * 8;
+  const int Ke = min(Kb + 8, dc.nz);
+  const int i0 = 4 * q;
+  for (int K = Kb; K < Ke; ++K) {
+    float acc0 = 0.f, acc1 = 0.f;
+#pragma unroll
+    for (int sub = 0; sub < 4; ++sub) {
+      const int j = 2 * J + (sub & 1);
+      const int k = 2 * K + (sub >> 1);
+      const int jm = wrapm(j - 1, d.ny), jp = wrapp(j + 1, d.ny);
+      const int km = wrapm(k - 1, d.nz), kp = wrapp(k + 1, d.nz);
+      const int64_t c = d.idx(i0, act ? j : 0, k);
+      float4 xv = make_float4(0, 0, 0, 0), w0v = xv;
+      if (act) {
+        xv = Ld4(x + c);
+        w0v = Ld4(A.w0 + c);
+      }
+      float xl, xr, wl, wr;
+      XHalo(x + d.idx(0, act ? j : 0, k), xv, q, nq, act, xl, xr);
+      XHalo(A.w0 + d.idx(0, act ? j : 0, k), w0v, q, nq, act, wl, wr);
+      (void)wl;
+      if (act) {
+        const float4 w1v = Ld4(A.w1 + c), w1n = Ld4(A.w1 + d.idx(i0, jp, k));
+        const float4 w2v = Ld4(A.w2 + c), w2n = Ld4(A.w2 + d.idx(i0, j, kp));
+        const float4 xjm = Ld4(x + d.idx(i0, jm, k)), xjp = Ld4(x + d.idx(i0, jp, k));
+        const float4 xkm = Ld4(x + d.idx(i0, j, km)), xkp = Ld4(x + d.idx(i0, j, kp));
+        const float4 bv = Ld4(b + c);
+#pragma unroll
+        for (int e = 0; e < 4; ++e) {
+          const float cxm = El(w0v, e);
+          const float cxp = e == 3 ? wr : El(w0v, e + 1);
+          const float cym = El(w1v, e), cyp = El(w1n, e);
+          const float czm = El(w2v, e), czp = El(w2n, e);
+          const float dg = A.diag ? A.diag[c + e]
+                                  : -(((((cxm + cxp) + cym) + cyp) + czm) + czp);
+          float y = El(xv, e) * dg;
+          y += (e == 0 ? xl : El(xv, e - 1)) * cxm;
+          y += (e == 3 ? xr : El(xv, e + 1)) * cxp;
+          y += El(xjm, e) * cym;
+          y += El(xjp, e) * cyp;
+          y += El(xkm, e) * czm;
+          y += El(xkp, e) * czp;
+          const float rv = El(bv, e) - y;
+          if (e < 2) acc0 += rv; else acc1 += rv;
+        }
+      }
+    }
+    if (act) *reinterpret_cast<float2*>(bc + dc.idx(2 * q, J, K)) = make_float2(acc0, acc1);
+  }
+}
+
 // Residual of the fine level summed over the 8 children into the coarse
 // right-hand side.  One thread per coarse cell.
 template <class T, class TC>
@@ -632,6 +1002,41 @@ __global__ void __launch_bounds__(1024) KCoarsestCG(
     __syncthreads();
   }
   for (int c = tid; c < n; c += blockDim.x) xc[c] = (TC)x[c];
+}
+
+// Coarsest level, direct: x = B^{-1} (b - mean(b)) with the precomputed
+// dense inverse of B = A + 11^T c (c > 0), which equals the solution of the
+// periodic (singular) A x = b - mean(b) with zero mean.  FP64 throughout.
+template <class TC>
+__global__ void __launch_bounds__(1024) KCoarsestDense(int n, const double* __restrict__ binv,
+                                                       const TC* __restrict__ bc, TC* xc,
+                                                       const SolveScalars* s) {
+  if (s && s->done) return;
+  __shared__ double sb[kDenseMax];
+  __shared__ double red[32];
+  const int tid = threadIdx.x;
+  double part = 0;
+  for (int c = tid; c < n; c += blockDim.x) {
+    const double v = (double)bc[c];
+    sb[c] = v;
+    part += v;
+  }
+  for (int o = 16; o > 0; o >>= 1) part += __shfl_down_sync(0xffffffffu, part, o);
+  if ((tid & 31) == 0) red[tid >> 5] = part;
+  __syncthreads();
+  if (tid == 0) {
+    double t = 0;
+    for (int w = 0; w < (int)(blockDim.x >> 5); ++w) t += red[w];
+    red[0] = t / n;
+  }
+  __syncthreads();
+  const double mean = red[0];
+  for (int r = tid; r < n; r += blockDim.x) {
+    const double* row = binv + (int64_t)r * n;
+    double acc = 0;
+    for (int c = 0; c < n; ++c) acc += row[c] * (sb[c] - mean);
+    xc[r] = (TC)acc;
+  }
 }
 
 // r = b - A x (FP64) with reductions r.r, max|r|, b.b; stopping test
@@ -839,6 +1244,88 @@ int EnsureCoarsestScratch(aphgpu_ctx* ctx, int64_t n) {
   return APHGPU_OK;
 }
 
+// Dense inverse of the coarsest operator B = A + 11^T c, c = mean(diag)/n,
+// by Cholesky on the host (n <= kDenseMax cells; built once per system).
+template <class T>
+int BuildCoarsestInverse(aphgpu_ctx* ctx, const Level<T>& L, double** dinv, int* dn) {
+  const Dims d = L.d;
+  const int n = (int)d.cells();
+  if (n > kDenseMax) {
+    *dn = 0;
+    return APHGPU_OK;
+  }
+  std::vector<T> w0(n), w1(n), w2(n), dg(n);
+  cudaStream_t st = ctx->stream;
+  APH_CUDA(ctx, cudaMemcpyAsync(w0.data(), L.w[0], sizeof(T) * n, cudaMemcpyDeviceToHost, st));
+  APH_CUDA(ctx, cudaMemcpyAsync(w1.data(), L.w[1], sizeof(T) * n, cudaMemcpyDeviceToHost, st));
+  APH_CUDA(ctx, cudaMemcpyAsync(w2.data(), L.w[2], sizeof(T) * n, cudaMemcpyDeviceToHost, st));
+  if (L.has_diag)
+    APH_CUDA(ctx, cudaMemcpyAsync(dg.data(), L.diag, sizeof(T) * n, cudaMemcpyDeviceToHost, st));
+  APH_CUDA(ctx, cudaStreamSynchronize(st));
+  std::vector<double> B((size_t)n * n, 0.0);
+  auto at = [&](int r, int c) -> double& { return B[(size_t)r * n + c]; };
+  double dsum = 0;
+  for (int k = 0; k < d.nz; ++k)
+    for (int j = 0; j < d.ny; ++j)
+      for (int i = 0; i < d.nx; ++i) {
+        const int c = (int)d.idx(i, j, k);
+        const int xm = (int)d.idx((i + d.nx - 1) % d.nx, j, k);
+        const int xp = (int)d.idx((i + 1) % d.nx, j, k);
+        const int ym = (int)d.idx(i, (j + d.ny - 1) % d.ny, k);
+        const int yp = (int)d.idx(i, (j + 1) % d.ny, k);
+        const int zm = (int)d.idx(i, j, (k + d.nz - 1) % d.nz);
+        const int zp = (int)d.idx(i, j, (k + 1) % d.nz);
+        const double e[6] = {(double)w0[c], (double)w0[xp], (double)w1[c],
+                             (double)w1[yp], (double)w2[c], (double)w2[zp]};
+        const int nb[6] = {xm, xp, ym, yp, zm, zp};
+        double diag = 0;
+        for (int q = 0; q < 6; ++q) {
+          at(c, nb[q]) += e[q];
+          diag -= e[q];
+        }
+        if (L.has_diag) diag = (double)dg[c];
+        at(c, c) += diag;
+        dsum += diag;
+      }
+  const double cshift = dsum / n / n;
+  for (auto& v : B) v += cshift;
+  // Cholesky B = L L^T, then B^{-1} column by column
+  std::vector<double> Lm((size_t)n * n, 0.0);
+  for (int j = 0; j < n; ++j) {
+    double sjj = at(j, j);
+    for (int k = 0; k < j; ++k) sjj -= Lm[(size_t)j * n + k] * Lm[(size_t)j * n + k];
+    if (!(sjj > 0))
+      return SetError(ctx, APHGPU_ERR_UNSUPPORTED,
+                      "coarsest operator is not positive semidefinite");
+    const double ljj = std::sqrt(sjj);
+    Lm[(size_t)j * n + j] = ljj;
+    for (int i = j + 1; i < n; ++i) {
+      double sij = at(i, j);
+      for (int k = 0; k < j; ++k) sij -= Lm[(size_t)i * n + k] * Lm[(size_t)j * n + k];
+      Lm[(size_t)i * n + j] = sij / ljj;
+    }
+  }
+  std::vector<double> inv((size_t)n * n, 0.0), y(n);
+  for (int col = 0; col < n; ++col) {
+    for (int i = 0; i < n; ++i) {
+      double v = (i == col) ? 1.0 : 0.0;
+      for (int k = 0; k < i; ++k) v -= Lm[(size_t)i * n + k] * y[k];
+      y[i] = v / Lm[(size_t)i * n + i];
+    }
+    for (int i = n - 1; i >= 0; --i) {
+      double v = y[i];
+      for (int k = i + 1; k < n; ++k) v -= Lm[(size_t)k * n + i] * inv[(size_t)k * n + col];
+      inv[(size_t)i * n + col] = v / Lm[(size_t)i * n + i];
+    }
+  }
+  if (!*dinv) APH_TRY(Alloc(ctx, dinv, (int64_t)kDenseMax * kDenseMax));
+  APH_CUDA(ctx, cudaMemcpyAsync(*dinv, inv.data(), sizeof(double) * inv.size(),
+                                cudaMemcpyHostToDevice, st));
+  APH_CUDA(ctx, cudaStreamSynchronize(st));
+  *dn = n;
+  return APHGPU_OK;
+}
+
 // Builds the FP64 (T=double) or FP32 hierarchy from the fine system.
 template <class T>
 int BuildHierarchy(aphgpu_ctx* ctx, std::vector<Level<T>>& lv, int coarse_max);
@@ -874,6 +1361,7 @@ int BuildHierarchy<double>(aphgpu_ctx* ctx, std::vector<Level<double>>& lv,
     APH_LAUNCHED(ctx);
   }
   APH_TRY(EnsureCoarsestScratch(ctx, lv.back().d.cells()));
+  APH_TRY(BuildCoarsestInverse(ctx, lv.back(), &ctx->mg.cinv64, &ctx->mg.cn64));
   return APHGPU_OK;
 }
 
@@ -930,7 +1418,118 @@ int BuildHierarchy<float>(aphgpu_ctx* ctx, std::vector<Level<float>>& lv,
     APH_LAUNCHED(ctx);
   }
   APH_TRY(EnsureCoarsestScratch(ctx, lv.back().d.cells()));
+  APH_TRY(BuildCoarsestInverse(ctx, lv.back(), &ctx->mg.cinv32, &ctx->mg.cn32));
   return APHGPU_OK;
+}
+
+// Launch helpers: the vectorized FP32 kernels where the level allows them.
+template <class T>
+void LaunchSmooth(aphgpu_ctx* ctx, const Level<T>& f, const Op<T>& A, int color,
+                  int zero_init, const SolveScalars* s) {
+  KSmooth<T><<<TileGrid(f.d), TileBlock(), 0, ctx->stream>>>(A, f.invdiag, f.b, f.x,
+                                                             color, zero_init, s);
+}
+template <>
+void LaunchSmooth<float>(aphgpu_ctx* ctx, const Level<float>& f, const Op<float>& A,
+                         int color, int zero_init, const SolveScalars* s) {
+  if (VecOk(f.d)) {
+    KSmooth4<<<VecGrid(f.d), TileBlock(), 0, ctx->stream>>>(A, f.b, f.x, color, zero_init, s);
+  } else {
+    KSmooth<float><<<TileGrid(f.d), TileBlock(), 0, ctx->stream>>>(A, f.invdiag, f.b, f.x,
+                                                                   color, zero_init, s);
+  }
+}
+template <class T>
+void LaunchProlong(aphgpu_ctx* ctx, const Level<T>& f, const Level<T>& c,
+                   const SolveScalars* s) {
+  KProlong<T, T><<<TileGrid(f.d), TileBlock(), 0, ctx->stream>>>(f.d, f.x, c.d, c.x, s);
+}
+template <>
+void LaunchProlong<float>(aphgpu_ctx* ctx, const Level<float>& f, const Level<float>& c,
+                          const SolveScalars* s) {
+  if (VecOk(f.d)) {
+    KProlong4<<<VecGrid(f.d), TileBlock(), 0, ctx->stream>>>(f.d, f.x, c.d, c.x, s);
+  } else {
+    KProlong<float, float><<<TileGrid(f.d), TileBlock(), 0, ctx->stream>>>(f.d, f.x, c.d,
+                                                                            c.x, s);
+  }
+}
+template <class T>
+void LaunchRestrict(aphgpu_ctx* ctx, const Level<T>& f, const Level<T>& c, const Op<T>& A,
+                    const SolveScalars* s) {
+  KResidualRestrict<T, T><<<TileGrid(c.d), TileBlock(), 0, ctx->stream>>>(A, f.b, f.x, c.d,
+                                                                           c.b, s);
+}
+template <>
+void LaunchRestrict<float>(aphgpu_ctx* ctx, const Level<float>& f, const Level<float>& c,
+                           const Op<float>& A, const SolveScalars* s) {
+  if (VecOk(f.d)) {
+    const dim3 g((f.d.nx / 4 + 31) / 32, (c.d.ny + 7) / 8, (c.d.nz + 7) / 8);
+    KResidualRestrict4<<<g, TileBlock(), 0, ctx->stream>>>(A, f.b, f.x, c.d, c.b, s);
+  } else {
+    KResidualRestrict<float, float><<<TileGrid(c.d), TileBlock(), 0, ctx->stream>>>(
+        A, f.b, f.x, c.d, c.b, s);
+  }
+}
+template <class T>
+void LaunchApply(aphgpu_ctx* ctx, const Op<T>& A, const T* p, T* ap, SolveScalars* s) {
+  KPcgApply<T><<<TileGrid(A.d), TileBlock(), 0, ctx->stream>>>(A, p, ap, s, ctx->red);
+}
+template <>
+void LaunchApply<float>(aphgpu_ctx* ctx, const Op<float>& A, const float* p, float* ap,
+                        SolveScalars* s) {
+  if (VecOk(A.d)) {
+    KPcgApply4<<<VecGrid(A.d), TileBlock(), 0, ctx->stream>>>(A, p, ap, s, ctx->red);
+  } else {
+    KPcgApply<float><<<TileGrid(A.d), TileBlock(), 0, ctx->stream>>>(A, p, ap, s, ctx->red);
+  }
+}
+
+template <class T>
+void LaunchUpdate(aphgpu_ctx* ctx, Dims d, T* x, T* r, const T* p, const T* ap,
+                  SolveScalars* s) {
+  KPcgUpdate<T><<<TileGrid(d), TileBlock(), 0, ctx->stream>>>(d, x, r, p, ap, s, ctx->red);
+}
+template <>
+void LaunchUpdate<float>(aphgpu_ctx* ctx, Dims d, float* x, float* r, const float* p,
+                         const float* ap, SolveScalars* s) {
+  const int64_t n = d.cells();
+  if (n % 4 == 0) {
+    KPcgUpdate4<<<FlatBlocks(n / 4), kFlatThreads, 0, ctx->stream>>>(n / 4, x, r, p, ap, s,
+                                                                     ctx->red, n);
+  } else {
+    KPcgUpdate<float><<<TileGrid(d), TileBlock(), 0, ctx->stream>>>(d, x, r, p, ap, s, ctx->red);
+  }
+}
+template <class T>
+void LaunchDotRZ(aphgpu_ctx* ctx, Dims d, const T* r, const T* z, const T* zold,
+                 SolveScalars* s, int first) {
+  KDotRZ<T><<<TileGrid(d), TileBlock(), 0, ctx->stream>>>(d, r, z, zold, s, ctx->red, first);
+}
+template <>
+void LaunchDotRZ<float>(aphgpu_ctx* ctx, Dims d, const float* r, const float* z,
+                        const float* zold, SolveScalars* s, int first) {
+  const int64_t n = d.cells();
+  if (n % 4 == 0) {
+    KDotRZ4<<<FlatBlocks(n / 4), kFlatThreads, 0, ctx->stream>>>(n / 4, r, z, zold, s, ctx->red,
+                                                                 first);
+  } else {
+    KDotRZ<float><<<TileGrid(d), TileBlock(), 0, ctx->stream>>>(d, r, z, zold, s, ctx->red, first);
+  }
+}
+template <class T>
+void LaunchP(aphgpu_ctx* ctx, Dims d, const T* z, T* p, const SolveScalars* s, int first) {
+  KPcgP<T><<<TileGrid(d), TileBlock(), 0, ctx->stream>>>(d, z, p, s, first);
+}
+template <>
+void LaunchP<float>(aphgpu_ctx* ctx, Dims d, const float* z, float* p, const SolveScalars* s,
+                    int first) {
+  const int64_t n = d.cells();
+  if (n % 4 == 0) {
+    KPcgP4<<<FlatBlocks(n / 4), kFlatThreads, 0, ctx->stream>>>(n / 4, z, p, s, first);
+  } else {
+    KPcgP<float><<<TileGrid(d), TileBlock(), 0, ctx->stream>>>(d, z, p, s, first);
+  }
 }
 
 // One V-cycle: lv[0].b -> lv[0].x (zero initial guess).
@@ -941,41 +1540,47 @@ int VCycle(aphgpu_ctx* ctx, std::vector<Level<T>>& lv, int pre, int post,
   cudaStream_t st = ctx->stream;
   for (int l = 0; l < L - 1; ++l) {
     Level<T>& f = lv[l];
-    // the fine FP32 level keeps no diagonal array: diag = -(sum)
     const Op<T> A = MakeOp(f);
     for (int sw = 0; sw < pre; ++sw) {
-      KSmooth<T><<<TileGrid(f.d), TileBlock(), 0, st>>>(A, f.invdiag, f.b, f.x, 0, sw == 0, s);
+      LaunchSmooth<T>(ctx, f, A, 0, sw == 0, s);
       APH_LAUNCHED(ctx);
-      KSmooth<T><<<TileGrid(f.d), TileBlock(), 0, st>>>(A, f.invdiag, f.b, f.x, 1, 0, s);
+      LaunchSmooth<T>(ctx, f, A, 1, 0, s);
       APH_LAUNCHED(ctx);
     }
     if (pre == 0) {
-      KSmooth<T><<<TileGrid(f.d), TileBlock(), 0, st>>>(A, f.invdiag, f.b, f.x, 0, 1, s);
+      LaunchSmooth<T>(ctx, f, A, 0, 1, s);
       APH_LAUNCHED(ctx);
-      KSmooth<T><<<TileGrid(f.d), TileBlock(), 0, st>>>(A, f.invdiag, f.b, f.x, 1, 1, s);
+      LaunchSmooth<T>(ctx, f, A, 1, 1, s);
       APH_LAUNCHED(ctx);
     }
     Level<T>& c = lv[l + 1];
-    KResidualRestrict<T, T><<<TileGrid(c.d), TileBlock(), 0, st>>>(A, f.b, f.x, c.d, c.b, s);
+    LaunchRestrict<T>(ctx, f, c, A, s);
     APH_LAUNCHED(ctx);
   }
   {
     Level<T>& c = lv[L - 1];
     const Op<T> A = MakeOp(c);
     auto& mg = ctx->mg;
-    KCoarsestCG<T><<<1, 1024, 0, st>>>(A, c.b, c.x, mg.cr, mg.cp, mg.cap, mg.cx, s);
+    const bool is64 = sizeof(T) == 8;
+    const int dn = is64 ? mg.cn64 : mg.cn32;
+    const double* dinv = is64 ? mg.cinv64 : mg.cinv32;
+    if (dn == (int)c.d.cells() && dinv) {
+      KCoarsestDense<T><<<1, dn < 1024 ? ((dn + 31) / 32) * 32 : 1024, 0, st>>>(dn, dinv, c.b, c.x, s);
+    } else {
+      KCoarsestCG<T><<<1, 1024, 0, st>>>(A, c.b, c.x, mg.cr, mg.cp, mg.cap, mg.cx, s);
+    }
     APH_LAUNCHED(ctx);
   }
   for (int l = L - 2; l >= 0; --l) {
     Level<T>& f = lv[l];
     Level<T>& c = lv[l + 1];
     const Op<T> A = MakeOp(f);
-    KProlong<T, T><<<TileGrid(f.d), TileBlock(), 0, st>>>(f.d, f.x, c.d, c.x, s);
+    LaunchProlong<T>(ctx, f, c, s);
     APH_LAUNCHED(ctx);
     for (int sw = 0; sw < post; ++sw) {
-      KSmooth<T><<<TileGrid(f.d), TileBlock(), 0, st>>>(A, f.invdiag, f.b, f.x, 1, 0, s);
+      LaunchSmooth<T>(ctx, f, A, 1, 0, s);
       APH_LAUNCHED(ctx);
-      KSmooth<T><<<TileGrid(f.d), TileBlock(), 0, st>>>(A, f.invdiag, f.b, f.x, 0, 0, s);
+      LaunchSmooth<T>(ctx, f, A, 0, 0, s);
       APH_LAUNCHED(ctx);
     }
   }
@@ -1003,23 +1608,23 @@ int Pcg(aphgpu_ctx* ctx, const Op<T>& A, Precond precond, T* x, T* r, T* p,
   cudaStream_t st = ctx->stream;
   const dim3 tg = TileGrid(d), tb = TileBlock();
   APH_TRY(precond(r, z));
-  KDotRZ<T><<<tg, tb, 0, st>>>(d, r, z, nullptr, s, ctx->red, 1);
+  LaunchDotRZ<T>(ctx, d, r, z, (const T*)nullptr, s, 1);
   APH_LAUNCHED(ctx);
-  KPcgP<T><<<tg, tb, 0, st>>>(d, z, p, s, 1);
+  LaunchP<T>(ctx, d, z, p, s, 1);
   APH_LAUNCHED(ctx);
   // iterations are bounded on the device by maxiter (done flag); the host
   // loop gives up after maxiter + 2 batches in any case
   for (int batch = 0; batch <= conf->maxiter / check_every + 2; ++batch) {
     for (int it = 0; it < check_every; ++it) {
-      KPcgApply<T><<<tg, tb, 0, st>>>(A, p, ap, s, ctx->red);
+      LaunchApply<T>(ctx, A, p, ap, s);
       APH_LAUNCHED(ctx);
-      KPcgUpdate<T><<<tg, tb, 0, st>>>(d, x, r, p, ap, s, ctx->red);
+      LaunchUpdate<T>(ctx, d, x, r, p, ap, s);
       APH_LAUNCHED(ctx);
       if (zold) std::swap(z, zold);
       APH_TRY(precond(r, z));
-      KDotRZ<T><<<tg, tb, 0, st>>>(d, r, z, zold, s, ctx->red, 0);
+      LaunchDotRZ<T>(ctx, d, r, z, zold, s, 0);
       APH_LAUNCHED(ctx);
-      KPcgP<T><<<tg, tb, 0, st>>>(d, z, p, s, 0);
+      LaunchP<T>(ctx, d, z, p, s, 0);
       APH_LAUNCHED(ctx);
     }
     SolveScalars hs;
@@ -1308,9 +1913,10 @@ int TimeSolverKernel(aphgpu_ctx* ctx, int kernel, int reps, double* ms,
       const Op<float> A = MakeOp(f);
       float* bb = ctx->r32;
       float* x = ctx->z32;
-      launch = [=]() {
-        KSmooth<float><<<TileGrid(d), TileBlock(), 0, st>>>(A, f.invdiag, bb, x, 0, 0, nullptr);
-      };
+      Level<float> fl = f;
+      fl.b = bb;
+      fl.x = x;
+      launch = [=]() { LaunchSmooth<float>(ctx, fl, A, 0, 0, nullptr); };
       // x read 4 + couplings 12 + half of (b 4, invdiag 4, x write 4)
       b = N * (4 + 12 + 0.5 * 12);
       break;
@@ -1348,7 +1954,8 @@ int TimeSolverKernel(aphgpu_ctx* ctx, int kernel, int reps, double* ms,
       const float* p = ctx->p32;
       float* ap = ctx->ap32;
       APH_CUDA(ctx, cudaMemsetAsync(s, 0, sizeof(SolveScalars), st));
-      launch = [=]() { KPcgApply<float><<<TileGrid(d), TileBlock(), 0, st>>>(A, p, ap, s, rb); };
+      (void)rb;
+      launch = [=]() { LaunchApply<float>(ctx, A, p, ap, s); };
       b = N * (4 + 12 + 4);
       break;
     }
