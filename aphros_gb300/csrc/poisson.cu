@@ -1967,9 +1967,10 @@ int TimeSolverKernel(aphgpu_ctx* ctx, int kernel, int reps, double* ms,
       const Op<float> A = MakeOp(f);
       const float* bb = ctx->r32;
       const float* x = ctx->z32;
-      launch = [=]() {
-        KResidualRestrict<float, float><<<TileGrid(c.d), TileBlock(), 0, st>>>(A, bb, x, c.d, c.b, nullptr);
-      };
+      Level<float> fl = f;
+      fl.b = (float*)bb;
+      fl.x = (float*)x;
+      launch = [=]() { LaunchRestrict<float>(ctx, fl, c, A, nullptr); };
       b = N * (4 + 4 + 12) + N / 8 * 4;
       break;
     }

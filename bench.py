@@ -208,21 +208,20 @@ def cpu_baseline(case, expr8_np, threads, budget_s=15.0, cg_iters_full=None):
     return out
 
 
-def cg_iterations_estimate(case_name, n_full, device):
-    """Iterations aphros's CG needs on this bubble field at ||r||/||b||=1e-10:
-    measured with the GPU plain CG on the same field at n_full/4 and scaled
-    by 4 (CG iterations grow linearly with the grid edge)."""
-    from aphros_gb300 import _lib, workload
-    n = max(32, n_full // 4)
-    case = workload.config(case_name, n=n)
-    ctx = _lib.Context(n, case.h, device)
-    ctx.assemble_projection(case.alpha, case.rho1, case.rho2, case.flux, case.dt)
-    _, b = ctx.residual_norms()
-    tol = 1e-10 * b / math.sqrt(case.h ** 3)
-    _, info = ctx.solve(_lib.default_conf(solver=_lib.SOLVER_CG, tol=tol,
-                                          maxiter=200000), out=False)
-    ctx.close()
-    return int(info.iter * (n_full / n)), int(info.iter), n
+def cg_iterations_estimate(case_name, n_full, threads):
+    """Iterations aphros's CG needs on this bubble field at ||r||/||b||=1e-10,
+    measured with the CPU oracle CG on the same bubbles at n_full/8 (at
+    least 32^3) and scaled by the grid ratio (CG iterations grow linearly
+    with the grid edge on this operator)."""
+    import oracle
+    from aphros_gb300 import workload
+    ns = max(32, n_full // 8)
+    cs = workload.config(case_name, n=ns)
+    es, _, _ = oracle.assemble_projection(ns, cs.h, cs.dt, cs.alpha, cs.rho1, cs.rho2,
+                                          cs.flux)
+    _, info = oracle.cg_solve(ns, cs.h, es, oracle.rel_tol(es, cs.h, 1e-10),
+                              nthreads=threads)
+    return int(round(info.iter * n_full / ns)), int(info.iter), ns
 
 
 # ---------------------------------------------------------------------------
@@ -323,7 +322,7 @@ def run_ours(args):
     cpu = None
     if rank == 0 and not args.no_cpu:
         threads = os.cpu_count() or 1
-        iters_full, iters_small, n_small = cg_iterations_estimate(args.workload, case.n, device)
+        iters_full, iters_small, n_small = cg_iterations_estimate(args.workload, case.n, threads)
         expr_np = np.empty(8 * N)
         ctx._check(ctx._L.aphgpu_get_system_expr(ctx.handle, _lib.ptr(expr_np)))
         cb = cpu_baseline(case, expr_np, threads, budget_s=args.cpu_budget,
@@ -331,7 +330,7 @@ def run_ours(args):
         cpu = {"value": cb.get("value"), "unit": UNIT, "cores": threads, "kind": "port",
                "sample": "%d CG iterations of the C restatement of aphros SolverConjugate "
                          "on the %d^3 system (%.3f s/iter, %d threads); full solve = %d "
-                         "iterations, from a GPU plain-CG solve of the same bubble field at "
+                         "iterations, from the same CG on the same bubble field at "
                          "%d^3 (%d iterations) scaled by the grid ratio"
                          % (cb["iters_sampled"], case.n, cb["per_iter_s"], threads,
                             iters_full, n_small, iters_small, )}
@@ -387,15 +386,8 @@ def run_reference(args):
     threads = os.cpu_count() or 1
     e, _, _ = oracle.assemble_projection(n, h, case.dt, case.alpha, case.rho1,
                                          case.rho2, case.flux)
-    # iterations of a full solve: measured on the CPU at n/8 (bounded time)
-    # and scaled with the grid edge
-    ns = max(16, n // 8)
-    cs = workload.config(args.workload, n=ns)
-    es, _, _ = oracle.assemble_projection(ns, cs.h, cs.dt, cs.alpha, cs.rho1, cs.rho2,
-                                          cs.flux)
-    _, info = oracle.cg_solve(ns, cs.h, es, oracle.rel_tol(es, cs.h, 1e-10),
-                              nthreads=threads)
-    iters_full = int(info.iter * n / ns)
+    # iterations of a full solve: measured on the CPU at n/8 and scaled
+    iters_full, iters_small, ns = cg_iterations_estimate(args.workload, n, threads)
     per = []
     for _ in range(args.warmup):
         oracle.cg_time_iters(n, e, 1, threads)
@@ -415,11 +407,28 @@ def run_reference(args):
         "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port",
                          "sample": "each step %d CG iterations at %d^3 (C restatement of "
                                    "aphros SolverConjugate, %d threads); full solve %d "
-                                   "iterations (CPU CG at %d^3: %d, scaled)"
-                                   % (sample_iters, n, threads, iters_full, ns, info.iter)},
+                                   "iterations (same CG at %d^3: %d, scaled by the grid ratio)"
+                                   % (sample_iters, n, threads, iters_full, ns, iters_small)},
         "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0,
                 "d2h_bytes_per_step": 0},
     }
+
+
+def run_profile(args):
+    """Solves only (for ncu launch lists and captures)."""
+    from aphros_gb300 import _lib, build, workload
+    build.build()
+    case = workload.config(args.workload)
+    ctx = _lib.Context(case.n, case.h, 0)
+    ctx.assemble_projection(case.alpha, case.rho1, case.rho2, case.flux, case.dt)
+    _, bnorm = ctx.residual_norms()
+    tol = 1e-10 * bnorm / math.sqrt(case.h ** 3)
+    solver = _lib.SOLVER_MIXED if args.profile == "mixed" else _lib.SOLVER_MGPCG
+    conf = _lib.default_conf(solver=solver, tol=tol)
+    for _ in range(args.warmup + args.steps):
+        info = ctx.solve_resident(conf, zero_guess=True)
+    print("profile %s: %d iterations (%d inner), %d launches in the last solve"
+          % (args.profile, info.iter, info.inner_iter, ctx.last_timing()[1]))
 
 
 def main():
@@ -432,7 +441,12 @@ def main():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--cpu-budget", type=float, default=15.0)
+    ap.add_argument("--profile", choices=["mixed", "fp64"], default=None,
+                    help="profiling run: assemble, then `steps` solves of one solver "
+                         "after `warmup` solves, no other work and no output line")
     args = ap.parse_args()
+    if args.profile:
+        return run_profile(args)
     if args.warmup < 3:
         args.warmup = 3
     if args.impl == "reference":
