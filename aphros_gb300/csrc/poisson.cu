@@ -479,16 +479,24 @@ __global__ void KSmooth(Op<T> A, const T* __restrict__ invdiag,
 // ---------------------------------------------------------------------------
 // Vectorized FP32 kernels (nx % 4 == 0): each thread owns 4 consecutive
 // cells in x (one float4), a CTA of 32x8 threads covers 128 x 8 cells of a
-// plane and marches over kVecZ planes in z, keeping the z neighbours in
+// plane and marches over kz planes in z (VecZ), keeping the z neighbours in
 // registers.  x neighbours across float4 boundaries come from warp shuffles
 // (global loads at warp and domain edges, periodic wrap).
 // ---------------------------------------------------------------------------
 
-constexpr int kVecZ = 16;
-
+// z planes per thread: 16 on large levels, halved until the grid has at
+// least 4 CTAs per SM (small levels would otherwise leave SMs idle)
+inline int VecZ(const Dims& d) {
+  const int nq = d.nx / 4;
+  const int64_t xy = (int64_t)((nq + 31) / 32) * ((d.ny + 7) / 8);
+  int kz = 16;
+  while (kz > 1 && xy * ((d.nz + kz - 1) / kz) < 4 * 152) kz /= 2;
+  return kz;
+}
 inline dim3 VecGrid(const Dims& d) {
   const int nq = d.nx / 4;
-  return dim3((nq + 31) / 32, (d.ny + 7) / 8, (d.nz + kVecZ - 1) / kVecZ);
+  const int kz = VecZ(d);
+  return dim3((nq + 31) / 32, (d.ny + 7) / 8, (d.nz + kz - 1) / kz);
 }
 inline bool VecOk(const Dims& d) { return (d.nx % 4) == 0 && d.nx >= 8; }
 
@@ -523,15 +531,15 @@ __device__ __forceinline__ void XHalo(const float* row, float4 v, int q, int nq,
 // operator stores one.
 __global__ void __launch_bounds__(256) KSmooth4(Op<float> A, const float* __restrict__ b,
                                                 float* x, int color, int zero_init,
-                                                const SolveScalars* s) {
+                                                const SolveScalars* s, int kz) {
   if (s && s->done) return;
   const Dims d = A.d;
   const int nq = d.nx >> 2;
   const int q = blockIdx.x * 32 + threadIdx.x;
   const int j = blockIdx.y * 8 + threadIdx.y;
   const bool act = q < nq && j < d.ny;
-  const int kb = blockIdx.z * kVecZ;
-  const int ke = min(kb + kVecZ, d.nz);
+  const int kb = blockIdx.z * kz;
+  const int ke = min(kb + kz, d.nz);
   const int jm = wrapm(j - 1, d.ny), jp = wrapp(j + 1, d.ny);
   const int i0 = 4 * q;
   float4 xz0 = make_float4(0, 0, 0, 0), xz1 = xz0, xz2 = xz0, wz1 = xz0, wz2 = xz0;
@@ -595,18 +603,18 @@ __global__ void __launch_bounds__(256) KSmooth4(Op<float> A, const float* __rest
 
 // y = A p (FP32, vectorized) with the reductions p.y and sum y of KPcgApply
 __global__ void __launch_bounds__(256) KPcgApply4(Op<float> A, const float* __restrict__ p,
-                                                  float* ap, SolveScalars* s, RedBuf rb) {
+                                                  float* ap, SolveScalars* s, RedBuf rb, int kz) {
   if (s->done) return;
   const Dims d = A.d;
   const int nq = d.nx >> 2;
   const int q = blockIdx.x * 32 + threadIdx.x;
   const int j = blockIdx.y * 8 + threadIdx.y;
   const bool act = q < nq && j < d.ny;
-  const int kb = blockIdx.z * kVecZ;
-  const int ke = min(kb + kVecZ, d.nz);
+  const int kb = blockIdx.z * kz;
+  const int ke = min(kb + kz, d.nz);
   const int jm = wrapm(j - 1, d.ny), jp = wrapp(j + 1, d.ny);
   const int i0 = 4 * q;
-  // per-thread sums in FP32 (at most 4 * kVecZ terms), CTA and grid sums in
+  // per-thread sums in FP32 (at most 4 * kz terms), CTA and grid sums in
   // FP64: FP64 arithmetic is scarce on GB300
   float fa0 = 0.f, fa1 = 0.f;
   float4 z0 = make_float4(0, 0, 0, 0), z1 = z0, z2 = z0, wz1 = z0, wz2 = z0;
@@ -674,14 +682,14 @@ __global__ void __launch_bounds__(256) KPcgApply4(Op<float> A, const float* __re
 
 // x_fine += x_coarse(parent), FP32 vectorized (one float4 = 2 coarse cells)
 __global__ void KProlong4(Dims d, float* x, Dims dc, const float* __restrict__ xc,
-                          const SolveScalars* s) {
+                          const SolveScalars* s, int kz) {
   if (s && s->done) return;
   const int nq = d.nx >> 2;
   const int q = blockIdx.x * 32 + threadIdx.x;
   const int j = blockIdx.y * 8 + threadIdx.y;
   if (q >= nq || j >= d.ny) return;
-  const int kb = blockIdx.z * kVecZ;
-  const int ke = min(kb + kVecZ, d.nz);
+  const int kb = blockIdx.z * kz;
+  const int ke = min(kb + kz, d.nz);
   for (int k = kb; k < ke; ++k) {
     const int64_t c = d.idx(4 * q, j, k);
     const float2 e = *reinterpret_cast<const float2*>(xc + dc.idx(2 * q, j >> 1, k >> 1));
@@ -788,15 +796,16 @@ __global__ void KPcgP4(int64_t n4, const float* __restrict__ z, float* p,
 // cells in x) of a coarse row and marches over coarse planes.
 __global__ void __launch_bounds__(256) KResidualRestrict4(Op<float> A, const float* __restrict__ b,
                                                           const float* __restrict__ x, Dims dc,
-                                                          float* bc, const SolveScalars* s) {
+                                                          float* bc, const SolveScalars* s,
+                                                          int kz) {
   if (s && s->done) return;
   const Dims d = A.d;
   const int nq = d.nx >> 2;
   const int q = blockIdx.x * 32 + threadIdx.x;
   const int J = blockIdx.y * 8 + threadIdx.y;
   const bool act = q < nq && J < dc.ny;
-  const int Kb = blockIdx.z * 8;
-  const int Ke = min(Kb + 8, dc.nz);
+  const int Kb = blockIdx.z * kz;
+  const int Ke = min(Kb + kz, dc.nz);
   const int i0 = 4 * q;
   for (int K = Kb; K < Ke; ++K) {
     float acc0 = 0.f, acc1 = 0.f;
@@ -1433,7 +1442,8 @@ template <>
 void LaunchSmooth<float>(aphgpu_ctx* ctx, const Level<float>& f, const Op<float>& A,
                          int color, int zero_init, const SolveScalars* s) {
   if (VecOk(f.d)) {
-    KSmooth4<<<VecGrid(f.d), TileBlock(), 0, ctx->stream>>>(A, f.b, f.x, color, zero_init, s);
+    KSmooth4<<<VecGrid(f.d), TileBlock(), 0, ctx->stream>>>(A, f.b, f.x, color, zero_init, s,
+                                                            VecZ(f.d));
   } else {
     KSmooth<float><<<TileGrid(f.d), TileBlock(), 0, ctx->stream>>>(A, f.invdiag, f.b, f.x,
                                                                    color, zero_init, s);
@@ -1448,7 +1458,7 @@ template <>
 void LaunchProlong<float>(aphgpu_ctx* ctx, const Level<float>& f, const Level<float>& c,
                           const SolveScalars* s) {
   if (VecOk(f.d)) {
-    KProlong4<<<VecGrid(f.d), TileBlock(), 0, ctx->stream>>>(f.d, f.x, c.d, c.x, s);
+    KProlong4<<<VecGrid(f.d), TileBlock(), 0, ctx->stream>>>(f.d, f.x, c.d, c.x, s, VecZ(f.d));
   } else {
     KProlong<float, float><<<TileGrid(f.d), TileBlock(), 0, ctx->stream>>>(f.d, f.x, c.d,
                                                                             c.x, s);
@@ -1464,8 +1474,11 @@ template <>
 void LaunchRestrict<float>(aphgpu_ctx* ctx, const Level<float>& f, const Level<float>& c,
                            const Op<float>& A, const SolveScalars* s) {
   if (VecOk(f.d)) {
-    const dim3 g((f.d.nx / 4 + 31) / 32, (c.d.ny + 7) / 8, (c.d.nz + 7) / 8);
-    KResidualRestrict4<<<g, TileBlock(), 0, ctx->stream>>>(A, f.b, f.x, c.d, c.b, s);
+    const int64_t xy = (int64_t)((f.d.nx / 4 + 31) / 32) * ((c.d.ny + 7) / 8);
+    int kz = 8;
+    while (kz > 1 && xy * ((c.d.nz + kz - 1) / kz) < 4 * 152) kz /= 2;
+    const dim3 g((f.d.nx / 4 + 31) / 32, (c.d.ny + 7) / 8, (c.d.nz + kz - 1) / kz);
+    KResidualRestrict4<<<g, TileBlock(), 0, ctx->stream>>>(A, f.b, f.x, c.d, c.b, s, kz);
   } else {
     KResidualRestrict<float, float><<<TileGrid(c.d), TileBlock(), 0, ctx->stream>>>(
         A, f.b, f.x, c.d, c.b, s);
@@ -1479,7 +1492,7 @@ template <>
 void LaunchApply<float>(aphgpu_ctx* ctx, const Op<float>& A, const float* p, float* ap,
                         SolveScalars* s) {
   if (VecOk(A.d)) {
-    KPcgApply4<<<VecGrid(A.d), TileBlock(), 0, ctx->stream>>>(A, p, ap, s, ctx->red);
+    KPcgApply4<<<VecGrid(A.d), TileBlock(), 0, ctx->stream>>>(A, p, ap, s, ctx->red, VecZ(A.d));
   } else {
     KPcgApply<float><<<TileGrid(A.d), TileBlock(), 0, ctx->stream>>>(A, p, ap, s, ctx->red);
   }
