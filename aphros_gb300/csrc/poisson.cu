@@ -529,7 +529,7 @@ __device__ __forceinline__ void XHalo(const float* row, float4 v, int q, int nq,
 // One red-black half sweep (FP32, vectorized); see KSmooth for the update.
 // The diagonal is recomputed from the six couplings (read anyway) unless the
 // operator stores one.
-__global__ void __launch_bounds__(256) KSmooth4(Op<float> A, const float* __restrict__ b,
+__global__ void __launch_bounds__(256, 4) KSmooth4(Op<float> A, const float* __restrict__ b,
                                                 float* x, int color, int zero_init,
                                                 const SolveScalars* s, int kz) {
   if (s && s->done) return;
@@ -602,7 +602,7 @@ __global__ void __launch_bounds__(256) KSmooth4(Op<float> A, const float* __rest
 }
 
 // y = A p (FP32, vectorized) with the reductions p.y and sum y of KPcgApply
-__global__ void __launch_bounds__(256) KPcgApply4(Op<float> A, const float* __restrict__ p,
+__global__ void __launch_bounds__(256, 4) KPcgApply4(Op<float> A, const float* __restrict__ p,
                                                   float* ap, SolveScalars* s, RedBuf rb, int kz) {
   if (s->done) return;
   const Dims d = A.d;
@@ -794,7 +794,7 @@ __global__ void KPcgP4(int64_t n4, const float* __restrict__ z, float* p,
 // Residual of a fine FP32 level summed over the 8 children into the coarse
 // right-hand side, vectorized: a thread owns one fine float4 (2 coarse
 // cells in x) of a coarse row and marches over coarse planes.
-__global__ void __launch_bounds__(256) KResidualRestrict4(Op<float> A, const float* __restrict__ b,
+__global__ void __launch_bounds__(256, 4) KResidualRestrict4(Op<float> A, const float* __restrict__ b,
                                                           const float* __restrict__ x, Dims dc,
                                                           float* bc, const SolveScalars* s,
                                                           int kz) {

@@ -1,6 +1,6 @@
 """Summarizes an ncu launch list (--metrics gpu__time_duration.sum --csv)
 into per-kernel launches, total time and share.  Usage:
-    python profiles/summarize_launches.py launches.csv
+    python -m aphros_gb300.ncu_summary launches.csv
 """
 import csv
 import re
