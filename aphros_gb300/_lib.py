@@ -42,7 +42,7 @@ class Conf(ctypes.Structure):
         ("solver", _I), ("tol", _D), ("miniter", _I), ("maxiter", _I),
         ("maxnorm", _I), ("mg_pre", _I), ("mg_post", _I),
         ("mg_coarse_max", _I), ("inner_rtol", _D), ("inner_maxiter", _I),
-        ("inner_flags", _I),
+        ("inner_flags", _I), ("rtol", _D),
     ]
 
 
@@ -86,6 +86,8 @@ def lib():
     L.aphgpu_solve.argtypes = [_P, ctypes.POINTER(Conf), _P, _P, ctypes.POINTER(Info)]
     L.aphgpu_solve_resident.argtypes = [_P, ctypes.POINTER(Conf), _I, ctypes.POINTER(Info)]
     L.aphgpu_get_solution.argtypes = [_P, _P]
+    L.aphgpu_set_solution.argtypes = [_P, _P]
+    L.aphgpu_set_solution.restype = _I
     L.aphgpu_residual_norms.argtypes = [_P, _PD, _PD]
     L.aphgpu_flux_correct.argtypes = [_P, _P]
     L.aphgpu_acceleration.argtypes = [_P, _P]

@@ -35,6 +35,7 @@ CU_UNITS = {
     "poisson.cu": [],
     "vof.cu": ["-fmad=false"],
     "noalloc.cu": [],
+    "server.cu": [],
 }
 
 

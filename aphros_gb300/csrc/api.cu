@@ -2,6 +2,7 @@
 // staging through pinned buffers, and dispatch to the solver and VOF code.
 #include <cuda_runtime.h>
 
+#include <algorithm>
 #include <cmath>
 #include <cstdarg>
 #include <cstdio>
@@ -174,6 +175,7 @@ void aphgpu_conf_default(aphgpu_conf* c) {
   c->inner_rtol = 1e-3;
   c->inner_maxiter = 200;
   c->inner_flags = 3;
+  c->rtol = 0;
 }
 
 int aphgpu_create(aphgpu_ctx** out, int nx, int ny, int nz, double h, int device) {
@@ -342,6 +344,14 @@ int aphgpu_solve_resident(aphgpu_ctx* ctx, const aphgpu_conf* conf, int zero_gue
   APH_TRY(SetDevice(ctx));
   APH_TRY(EnsureSolverVectors(ctx));
   if (zero_guess) APH_CUDA(ctx, cudaMemsetAsync(ctx->x, 0, sizeof(double) * ctx->N, ctx->stream));
+  aphgpu_conf cf = *conf;
+  if (conf->rtol > 0) {
+    double rn = 0, bn = 0;
+    APH_TRY(ResidualNorms(ctx, &rn, &bn));
+    const double t = conf->rtol * bn / std::sqrt(ctx->h * ctx->h * ctx->h);
+    cf.tol = std::max(cf.tol, t);
+  }
+  conf = &cf;
   Timer t(ctx);
   int rc;
   switch (conf->solver) {
@@ -374,6 +384,12 @@ int aphgpu_residual_history(aphgpu_ctx* ctx, int which, double* out, int cap,
     for (int i = 0; i < cap && i < (int)h.size(); ++i) out[i] = h[i];
   }
   return APHGPU_OK;
+}
+
+int aphgpu_set_solution(aphgpu_ctx* ctx, const double* x) {
+  if (!Valid(ctx) || !x) return APHGPU_ERR_ARG;
+  APH_TRY(SetDevice(ctx));
+  return H2D(ctx, ctx->x, x, sizeof(double) * ctx->N);
 }
 
 int aphgpu_get_solution(aphgpu_ctx* ctx, double* x) {

@@ -66,6 +66,10 @@ typedef struct {
    * flexible (Polak-Ribiere) beta, robust to the FP32 preconditioner's
    * rounding */
   int inner_flags;
+  /* relative tolerance: when > 0 the solve stops at
+   * max(tol, rtol * sqrt(sum b^2 / h^3)), i.e. ||r||/||b|| <= rtol from a
+   * zero guess */
+  double rtol;
 } aphgpu_conf;
 
 /* Result; mirrors linear::Solver::Info (linear.h:27-30).  `iter` counts
@@ -147,6 +151,10 @@ int aphgpu_solve_resident(aphgpu_ctx* ctx, const aphgpu_conf* conf,
  * available. */
 int aphgpu_residual_history(aphgpu_ctx* ctx, int which, double* out, int cap,
                             int* count);
+
+/* Sets the resident solution (initial guess of aphgpu_solve_resident with
+ * zero_guess = 0), e.g. to restore a checkpointed pressure. */
+int aphgpu_set_solution(aphgpu_ctx* ctx, const double* x);
 
 /* Copies the resident solution (pressure) to the host. */
 int aphgpu_get_solution(aphgpu_ctx* ctx, double* x);
@@ -236,6 +244,68 @@ int aphgpu_cg_solve_noalloc(int nx, int ny, int nz, double cellvol,
                             const double* d_expr8, const double* d_x0,
                             double* d_x, double tol, int miniter, int maxiter,
                             int maxnorm, void* stream, aphgpu_info* info);
+
+/* ---- serving loop ----
+ *
+ * Time-step requests for many simulations resident on one GPU, run with
+ * continuous batching: `slots` worker threads start requests as they
+ * arrive, requests of different simulations run concurrently on their own
+ * streams (their kernels overlap on the device), steps of one simulation
+ * run in submission order.  A request is one full step: projection
+ * (assembly from the resident volume fraction, the request's predicted face
+ * fluxes and the resident surface-tension force; solve warm-started from
+ * the resident pressure; corrected fluxes), PLIC advection with the
+ * corrected fluxes, height curvature, and the surface-tension force for the
+ * next step.  Simulations are admitted while their device memory fits the
+ * budget; to admit one, the least recently used idle simulations are
+ * evicted to host memory and restored bit-exactly later.  There is no
+ * counterpart in the reference (its time loop steps one simulation). */
+typedef struct aphgpu_server aphgpu_server;
+
+typedef struct {
+  int64_t ticket;
+  int sim;
+  int status;          /* APHGPU_OK or the error of the step */
+  int iters;           /* solver iterations (outer for the mixed solver) */
+  int inner_iters;
+  int converged;
+  double residual;
+  double queue_ms;     /* submission -> start */
+  double latency_ms;   /* submission -> completion */
+  double device_ms;    /* device time of solve + advection + curvature */
+} aphgpu_step_result;
+
+typedef struct {
+  int sims;
+  int resident;
+  int64_t resident_bytes;
+  int64_t budget_bytes;
+  int64_t completed;
+  int64_t queued;
+  int64_t evictions;
+  int64_t admissions;
+} aphgpu_server_stats;
+
+/* conf: solver of every step (NULL: mixed precision, rtol 1e-10). */
+int aphgpu_server_create(aphgpu_server** server, int device, double budget_bytes,
+                         int slots, const aphgpu_conf* conf);
+void aphgpu_server_destroy(aphgpu_server* server);
+/* Registers a simulation (periodic nx*ny*nz, cell h, gas volume fraction
+ * alpha, densities, surface tension sigma); admitted at its first step. */
+int aphgpu_server_add_sim(aphgpu_server* server, int nx, int ny, int nz, double h,
+                          const double* alpha, double rho1, double rho2,
+                          double sigma, int* sim);
+/* Queues one step (vflux copied at submission: 3 face blocks). */
+int aphgpu_server_submit(aphgpu_server* server, int sim, const double* vflux,
+                         double dt, int64_t* ticket);
+/* Waits for a step and returns its result (each ticket once). */
+int aphgpu_server_wait(aphgpu_server* server, int64_t ticket,
+                       aphgpu_step_result* result);
+/* Volume fraction and pressure of a simulation after its queued steps
+ * that have started have finished (either pointer may be NULL). */
+int aphgpu_server_get_state(aphgpu_server* server, int sim, double* alpha,
+                            double* pressure);
+int aphgpu_server_get_stats(aphgpu_server* server, aphgpu_server_stats* stats);
 
 /* Records event `slot` (0..7) on the context's stream; aphgpu_elapsed
  * returns the milliseconds between two recorded slots (waits for the

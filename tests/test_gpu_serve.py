@@ -1,0 +1,82 @@
+"""Serving loop (aphgpu_server_*): each simulation's result is the same alone
+and in a concurrent mix, and after eviction to host memory and restore;
+admission keeps the resident device memory within the budget."""
+import numpy as np
+import pytest
+
+from aphros_gb300 import _lib, serve, workload
+
+pytestmark = pytest.mark.gpu
+
+
+def _cases():
+    out = []
+    for i, n in enumerate((24, 32, 40, 32, 24, 48)):
+        c, r = workload.place_spheres(100 + i, 1 + i % 3, 0.08, 0.2, gap=0.02)
+        out.append(workload.Case(n, c, r, rho1=1.0, rho2=1e-3, seed=200 + i))
+    return out
+
+
+def _run(cases, order, slots, budget, steps=3, sigma=0.05):
+    """Submits `steps` steps of the simulations in `order` (indices into
+    cases), round-robin, and returns the final states."""
+    with serve.Server(budget_bytes=budget, slots=slots) as srv:
+        sims = {i: srv.add(cases[i], sigma=sigma) for i in order}
+        tickets = []
+        for _ in range(steps):
+            for i in order:
+                c = cases[i]
+                dt = 0.5 * c.cfl_dt(0.5)
+                tickets.append(srv.submit(sims[i], c.flux, dt))
+        res = [srv.wait(t) for t in tickets]
+        assert all(r.status == _lib.OK for r in res)
+        assert all(r.converged for r in res)
+        states = {i: srv.state(sims[i]) for i in order}
+        return states, res, srv.stats()
+
+
+def test_alone_and_in_the_mix_are_identical():
+    cases = _cases()
+    alone, res_alone, _ = _run(cases, [2], slots=1, budget=100e9)
+    mixed, res_mix, st = _run(cases, list(range(len(cases))), slots=4, budget=100e9)
+    a0, p0 = alone[2]
+    a1, p1 = mixed[2]
+    assert np.array_equal(a0, a1)
+    assert np.array_equal(p0, p1)
+    assert st.completed == 3 * len(cases)
+    assert st.evictions == 0
+
+
+def test_eviction_and_restore_are_exact():
+    cases = _cases()
+    order = list(range(len(cases)))
+    big, _, st_big = _run(cases, order, slots=2, budget=100e9)
+    # room for about two of the larger simulations: forces evictions
+    small, _, st_small = _run(cases, order, slots=2, budget=2.5 * 440 * 48 ** 3)
+    assert st_small.evictions > 0
+    assert st_small.resident_bytes <= st_small.budget_bytes
+    for i in order:
+        assert np.array_equal(big[i][0], small[i][0])
+        assert np.array_equal(big[i][1], small[i][1])
+
+
+def test_server_step_equals_manual_step():
+    """A served step is the same sequence as the C-ABI calls on a context."""
+    c = _cases()[1]
+    dt = 0.5 * c.cfl_dt(0.5)
+    states, _, _ = _run([c], [0], slots=1, budget=100e9, steps=1, sigma=0.0)
+    ctx = _lib.Context(c.n, c.h)
+    ctx.vof_init(c.alpha)
+    ctx.assemble_projection(None, c.rho1, c.rho2, c.flux, dt)
+    ctx.solve_resident(_lib.default_conf(solver=_lib.SOLVER_MIXED, rtol=1e-10))
+    ctx.flux_correct(out=False)
+    ctx.vof_step(None, dt)
+    assert np.array_equal(ctx.vof_get()[0], states[0][0])
+    assert np.array_equal(ctx.get_solution(), states[0][1])
+
+
+def test_oversized_simulation_is_rejected():
+    c = _cases()[5]
+    with serve.Server(budget_bytes=1e6, slots=1) as srv:
+        with pytest.raises(_lib.AphgpuError):
+            srv.add(c)
