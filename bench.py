@@ -414,6 +414,69 @@ def run_reference(args):
     }
 
 
+def run_serve(args):
+    """Served stream: Poisson-arrival step requests for resident simulations
+    of edge 32-128 (log-uniform, multiples of 8, 1-8 bubbles, density ratio
+    1000) on a continuous-batching server, against the same requests run one
+    by one with the plain FP64 solver."""
+    import random
+
+    from aphros_gb300 import _lib, build, serve, workload
+    build.build()
+    cases = workload.served_cases(args.sims)
+    dts = [0.5 * c.cfl_dt(0.5) for c in cases]
+    rng = random.Random(5)
+    order = [rng.randrange(len(cases)) for _ in range(args.requests)]
+
+    def drive(slots, conf, rate):
+        with serve.Server(budget_bytes=args.budget_gb * 1e9, slots=slots, conf=conf) as srv:
+            sims = [srv.add(c, sigma=0.05) for c in cases]
+            # warm-up: one step of every simulation (admission, hierarchy)
+            for t in [srv.submit(sims[i], cases[i].flux, dts[i]) for i in range(len(cases))]:
+                srv.wait(t)
+            tickets = []
+            t0 = time.perf_counter()
+            clock = 0.0
+            for i in order:
+                if rate > 0:
+                    clock += rng.expovariate(rate)
+                    delay = t0 + clock - time.perf_counter()
+                    if delay > 0:
+                        time.sleep(delay)
+                tickets.append(srv.submit(sims[i], cases[i].flux, dts[i]))
+            res = [srv.wait(t) for t in tickets]
+            t1 = time.perf_counter()
+            st = srv.stats()
+        lat = np.array([r.latency_ms for r in res])
+        ok = all(r.status == _lib.OK and r.converged for r in res)
+        return {"steps_per_s": len(res) / (t1 - t0), "p50_ms": float(np.percentile(lat, 50)),
+                "p99_ms": float(np.percentile(lat, 99)), "all_converged": ok,
+                "evictions": int(st.evictions), "resident_gb": st.resident_bytes / 1e9}
+
+    mixed = _lib.default_conf(solver=_lib.SOLVER_MIXED, rtol=1e-10)
+    plain = _lib.default_conf(solver=_lib.SOLVER_MGPCG, rtol=1e-10)
+    one_by_one = drive(1, plain, 0.0)
+    saturated = drive(args.slots, mixed, 0.0)
+    rates = {}
+    for rate in args.rates:
+        rates[str(rate)] = drive(args.slots, mixed, rate)
+    cells = [c.N for c in cases]
+    return {
+        "metric": "served steps/s and p50/p99 step latency (projection + PLIC advection + "
+                  "curvature per step)",
+        "value": saturated["steps_per_s"], "unit": "steps/s", "n_gpus": 1,
+        "higher_is_better": True,
+        "config": {"workload": "served stream, %d resident simulations of edge 32-128 "
+                               "(log-uniform, multiples of 8), 1-8 bubbles, density ratio "
+                               "1000, %d requests, %d slots, %g GB budget"
+                               % (len(cases), args.requests, args.slots, args.budget_gb),
+                   "cells_mean": float(np.mean(cells))},
+        "served_saturated": saturated, "served_at_rate": rates,
+        "one_by_one_plain_fp64": one_by_one,
+        "speedup_vs_one_by_one": saturated["steps_per_s"] / one_by_one["steps_per_s"],
+    }
+
+
 def run_profile(args):
     """Solves only (for ncu launch lists and captures)."""
     from aphros_gb300 import _lib, build, workload
@@ -444,9 +507,19 @@ def main():
     ap.add_argument("--profile", choices=["mixed", "fp64"], default=None,
                     help="profiling run: assemble, then `steps` solves of one solver "
                          "after `warmup` solves, no other work and no output line")
+    ap.add_argument("--serve", action="store_true",
+                    help="served-stream benchmark instead of the solve benchmark")
+    ap.add_argument("--sims", type=int, default=64)
+    ap.add_argument("--requests", type=int, default=256)
+    ap.add_argument("--slots", type=int, default=8)
+    ap.add_argument("--budget-gb", type=float, default=150.0)
+    ap.add_argument("--rates", type=float, nargs="*", default=[50.0, 200.0])
     args = ap.parse_args()
     if args.profile:
         return run_profile(args)
+    if args.serve:
+        print(json.dumps(run_serve(args)), flush=True)
+        return
     if args.warmup < 3:
         args.warmup = 3
     if args.impl == "reference":
