@@ -238,6 +238,8 @@ void aphgpu_destroy(aphgpu_ctx* ctx) {
   if (!ctx) return;
   cudaSetDevice(ctx->device);
   if (ctx->stream) cudaStreamSynchronize(ctx->stream);
+  for (auto& g : ctx->graphs)
+    if (g.exec) cudaGraphExecDestroy(g.exec);
   for (void* p : ctx->allocs) cudaFree(p);
   ctx->allocs.clear();
   if (ctx->hscal) cudaFreeHost(ctx->hscal);

@@ -294,6 +294,16 @@ struct aphgpu_ctx {
   void* pinned = nullptr;
   size_t pinned_bytes = 0;
 
+  // CUDA graphs of PCG iteration batches (one per solver role), keyed by
+  // the pointers and settings they were captured with
+  struct GraphSlot {
+    cudaGraphExec_t exec = nullptr;
+    uint64_t key = 0;
+    int64_t kernels = 0;
+  } graphs[4];
+  int64_t mg_epoch = 0;        // bumped whenever a hierarchy is (re)allocated
+  bool use_graphs = true;
+
   // timing
   cudaEvent_t ev0 = nullptr, ev1 = nullptr;
   cudaEvent_t ev_slot[2] = {nullptr, nullptr};

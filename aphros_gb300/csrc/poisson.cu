@@ -35,9 +35,16 @@
 namespace aphgpu {
 
 int FlatBlocks(int64_t n) {
-  int dev = 0, sms = 152;
-  cudaGetDevice(&dev);
-  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  // SM count of device 0, read once (no runtime queries while a stream is
+  // being captured into a graph)
+  static const int sms = [] {
+    int v = 152;
+    if (cudaDeviceGetAttribute(&v, cudaDevAttrMultiProcessorCount, 0) != cudaSuccess) {
+      cudaGetLastError();
+      v = 152;
+    }
+    return v;
+  }();
   const int64_t want = (n + kFlatThreads - 1) / kFlatThreads;
   const int64_t cap = (int64_t)sms * 8;
   return (int)std::max<int64_t>(1, std::min(want, cap));
@@ -1349,6 +1356,7 @@ int BuildHierarchy<double>(aphgpu_ctx* ctx, std::vector<Level<double>>& lv,
                     "(grid %dx%dx%d does not coarsen)",
                     (long long)dims.back().cells(), ctx->d.nx, ctx->d.ny, ctx->d.nz);
   if (lv.size() != dims.size()) {
+    ctx->mg_epoch += 1;
     lv.assign(dims.size(), Level<double>{});
     for (size_t l = 0; l < dims.size(); ++l) {
       lv[l].d = dims[l];
@@ -1383,6 +1391,7 @@ int BuildHierarchy<float>(aphgpu_ctx* ctx, std::vector<Level<float>>& lv,
                     "multigrid: coarsest level of %lld cells exceeds 4096",
                     (long long)dims.back().cells());
   if (lv.size() != dims.size()) {
+    ctx->mg_epoch += 1;
     lv.assign(dims.size(), Level<float>{});
     for (size_t l = 0; l < dims.size(); ++l) {
       lv[l].d = dims[l];
@@ -1613,21 +1622,29 @@ int SaveHistory(aphgpu_ctx* ctx, const double* d_hist, int n,
 // Preconditioned CG with operator A and preconditioner `precond(r, z)`
 // on vectors x (iterate), r (residual on entry), p, ap, z, zold (zold only
 // for the flexible variant); scalars s (tolerances set by the caller).
+inline uint64_t Mix(uint64_t h, uint64_t v) {
+  h ^= v + 0x9E3779B97F4A7C15ull + (h << 6) + (h >> 2);
+  return h;
+}
+
+// Preconditioned CG with operator A and preconditioner `precond(r, z)`
+// on vectors x (iterate), r (residual on entry), p, ap, z, zold (zold only
+// for the flexible variant); scalars s (tolerances set by the caller).
+// Batches of `check_every` iterations (even) are captured once into a CUDA
+// graph (slot `graph_slot` of the context, -1: no graph) and replayed; the
+// host reads the device's stopping flag after each batch.
 template <class T, class Precond>
 int Pcg(aphgpu_ctx* ctx, const Op<T>& A, Precond precond, T* x, T* r, T* p,
         T* ap, T* z, T* zold, SolveScalars* s, const aphgpu_conf* conf,
-        int check_every) {
+        int check_every, int graph_slot = -1) {
   const Dims d = A.d;
   cudaStream_t st = ctx->stream;
-  const dim3 tg = TileGrid(d), tb = TileBlock();
   APH_TRY(precond(r, z));
   LaunchDotRZ<T>(ctx, d, r, z, (const T*)nullptr, s, 1);
   APH_LAUNCHED(ctx);
   LaunchP<T>(ctx, d, z, p, s, 1);
   APH_LAUNCHED(ctx);
-  // iterations are bounded on the device by maxiter (done flag); the host
-  // loop gives up after maxiter + 2 batches in any case
-  for (int batch = 0; batch <= conf->maxiter / check_every + 2; ++batch) {
+  auto body = [&]() -> int {
     for (int it = 0; it < check_every; ++it) {
       LaunchApply<T>(ctx, A, p, ap, s);
       APH_LAUNCHED(ctx);
@@ -1639,6 +1656,60 @@ int Pcg(aphgpu_ctx* ctx, const Op<T>& A, Precond precond, T* x, T* r, T* p,
       APH_LAUNCHED(ctx);
       LaunchP<T>(ctx, d, z, p, s, 0);
       APH_LAUNCHED(ctx);
+    }
+    return APHGPU_OK;
+  };
+  cudaGraphExec_t exec = nullptr;
+  int64_t graph_kernels = 0;
+  if (graph_slot >= 0 && ctx->use_graphs && (check_every % 2 == 0 || !zold)) {
+    auto& g = ctx->graphs[graph_slot];
+    uint64_t key = 1469598103934665603ull;
+    const void* ptrs[] = {x, r, p, ap, z, zold, s, A.w0, A.w1, A.w2, A.diag};
+    for (const void* q : ptrs) key = Mix(key, (uint64_t)(uintptr_t)q);
+    key = Mix(key, (uint64_t)ctx->mg_epoch);
+    key = Mix(key, (uint64_t)(conf->mg_pre * 1000 + conf->mg_post));
+    key = Mix(key, (uint64_t)check_every);
+    key = Mix(key, (uint64_t)sizeof(T));
+    if (g.exec && g.key == key) {
+      exec = g.exec;
+      graph_kernels = g.kernels;
+    } else {
+      if (g.exec) {
+        cudaGraphExecDestroy(g.exec);
+        g.exec = nullptr;
+      }
+      const int64_t l0 = ctx->launches;
+      cudaGraph_t graph = nullptr;
+      T* z0 = z;
+      T* zo0 = zold;
+      bool ok = cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal) == cudaSuccess;
+      int rc = ok ? body() : APHGPU_OK;
+      ok = (cudaStreamEndCapture(st, &graph) == cudaSuccess) && ok && rc == APHGPU_OK;
+      z = z0;
+      zold = zo0;
+      ctx->launches = l0;  // captured launches are counted when replayed
+      if (ok && cudaGraphInstantiate(&g.exec, graph, 0) == cudaSuccess) {
+        g.key = key;
+        g.kernels = 0;
+        size_t nn = 0;
+        if (cudaGraphGetNodes(graph, nullptr, &nn) == cudaSuccess) g.kernels = (int64_t)nn;
+        exec = g.exec;
+        graph_kernels = g.kernels;
+      } else {
+        g.exec = nullptr;
+      }
+      if (graph) cudaGraphDestroy(graph);
+      cudaGetLastError();
+    }
+  }
+  // iterations are bounded on the device by maxiter (done flag); the host
+  // loop gives up after maxiter + 2 batches in any case
+  for (int batch = 0; batch <= conf->maxiter / check_every + 2; ++batch) {
+    if (exec) {
+      APH_CUDA(ctx, cudaGraphLaunch(exec, st));
+      ctx->launches += graph_kernels;
+    } else {
+      APH_TRY(body());
     }
     SolveScalars hs;
     APH_TRY(ReadScalars(ctx, s, &hs));
@@ -1781,7 +1852,7 @@ int SolveMGPCG(aphgpu_ctx* ctx, const aphgpu_conf* conf, aphgpu_info* info) {
     return VCycle(ctx, lv, conf->mg_pre, conf->mg_post, s);
   };
   APH_TRY(Pcg<double>(ctx, A, precond, ctx->x, ctx->r, ctx->p, ctx->ap, ctx->z,
-                      (double*)nullptr, s, conf, 2));
+                      (double*)nullptr, s, conf, 2, 0));
   SolveScalars hs;
   APH_TRY(ReadScalars(ctx, s, &hs));
   APH_TRY(SaveHistory(ctx, ctx->hist, hs.iter, ctx->hist_outer));
@@ -1821,7 +1892,7 @@ int SolveMGPCG32(aphgpu_ctx* ctx, const aphgpu_conf* conf, aphgpu_info* info) {
     return APHGPU_OK;
   };
   APH_TRY(Pcg<double>(ctx, A, precond, ctx->x, ctx->r, ctx->p, ctx->ap, ctx->z,
-                      (double*)nullptr, s, conf, 2));
+                      (double*)nullptr, s, conf, 2, 1));
   SolveScalars hs;
   APH_TRY(ReadScalars(ctx, s, &hs));
   APH_TRY(SaveHistory(ctx, ctx->hist, hs.iter, ctx->hist_outer));
@@ -1887,7 +1958,7 @@ int SolveMixed(aphgpu_ctx* ctx, const aphgpu_conf* conf, aphgpu_info* info) {
     APH_TRY(InitScalars(ctx, s2, &ic, 1.0, ctx->hist + kHistCap, flags));
     APH_TRY(Pcg<float>(ctx, A32, precond, ctx->x32, ctx->r32, ctx->p32, ctx->ap32,
                        ctx->z32, (conf->inner_flags & 2) ? ctx->zold32 : (float*)nullptr,
-                       s2, &ic, 2));
+                       s2, &ic, 4, 2));
     SolveScalars is;
     APH_TRY(ReadScalars(ctx, s2, &is));
     inner_total += is.iter;
