@@ -7,7 +7,7 @@ bubbles; liquid density rho1 = 1, gas rho2 = rho1 / ratio):
   c3   512^3, 64 spheres r in [0.02,0.05], seed 3
   c4   batch of domains, edge in {32,48,64,96}, 1-8 spheres of radius
        0.05-0.2 of the edge, ratio log-uniform in [10,1000], seed 4
-  c5   served stream, edge 32-128 log-uniform rounded to a multiple of 8,
+  c5   served stream, edge 32-128 log-uniform rounded to a multiple of 16,
        1-8 bubbles, ratio 1000, seed 5
 Predicted face fluxes: Taylor-Green (U=1) at face centres plus Gaussian
 noise of standard deviation 0.01 per face, times the face area.
@@ -149,9 +149,10 @@ def batch_cases(count, seed=4, edges=(32, 48, 64, 96)):
     return out
 
 
-def served_cases(count, seed=5, nmin=32, nmax=128, quantum=8):
+def served_cases(count, seed=5, nmin=32, nmax=128, quantum=16):
     """Served configuration: edge log-uniform in [nmin,nmax] rounded to a
-    multiple of `quantum` (so that multigrid coarsens to a small level)."""
+    multiple of `quantum`; with 16 every edge coarsens to a level of at most
+    7^3 cells, solved by the dense coarsest inverse."""
     g = gen()
     out = []
     for i in range(count):

@@ -416,7 +416,7 @@ def run_reference(args):
 
 def run_serve(args):
     """Served stream: Poisson-arrival step requests for resident simulations
-    of edge 32-128 (log-uniform, multiples of 8, 1-8 bubbles, density ratio
+    of edge 32-128 (log-uniform, multiples of 16, 1-8 bubbles, density ratio
     1000) on a continuous-batching server, against the same requests run one
     by one with the plain FP64 solver."""
     import random
@@ -467,7 +467,7 @@ def run_serve(args):
         "value": saturated["steps_per_s"], "unit": "steps/s", "n_gpus": 1,
         "higher_is_better": True,
         "config": {"workload": "served stream, %d resident simulations of edge 32-128 "
-                               "(log-uniform, multiples of 8), 1-8 bubbles, density ratio "
+                               "(log-uniform, multiples of 16), 1-8 bubbles, density ratio "
                                "1000, %d requests, %d slots, %g GB budget"
                                % (len(cases), args.requests, args.slots, args.budget_gb),
                    "cells_mean": float(np.mean(cells))},
