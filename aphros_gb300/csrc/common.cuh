@@ -91,18 +91,16 @@ __device__ __forceinline__ void WarpReduce(double (&v)[NV], const int (&op)[NV])
 }
 
 // Returns true in all threads of the last CTA; `out[q]` then holds the
-// grid-wide result (visible to that CTA after the call).  nthreads: threads
-// per CTA (multiple of 32, <= 1024).  The CTA index is linearised over a
-// 3-D grid.
+// result over the `nblocks` CTAs sharing `rb` (visible to that CTA after
+// the call).  bid: index of this CTA among them.  nthreads: threads per
+// CTA (multiple of 32, <= 1024).
 template <int NV>
-__device__ bool GridReduce(double (&v)[NV], const int (&op)[NV], RedBuf rb,
-                           double* out) {
+__device__ bool GroupReduce(double (&v)[NV], const int (&op)[NV], RedBuf rb,
+                            double* out, int bid, int nblocks) {
   __shared__ double sm[32][NV];
   __shared__ bool last;
   const int tid = threadIdx.x + blockDim.x * (threadIdx.y + blockDim.y * threadIdx.z);
   const int nthreads = blockDim.x * blockDim.y * blockDim.z;
-  const int bid = blockIdx.x + gridDim.x * (blockIdx.y + gridDim.y * blockIdx.z);
-  const int nblocks = gridDim.x * gridDim.y * gridDim.z;
   WarpReduce<NV>(v, op);
   const int lane = tid & 31, warp = tid >> 5;
   if (lane == 0) {
@@ -156,6 +154,15 @@ __device__ bool GridReduce(double (&v)[NV], const int (&op)[NV], RedBuf rb,
   }
   __syncthreads();
   return true;
+}
+
+// GroupReduce over the whole grid (CTA index linearised over a 3-D grid).
+template <int NV>
+__device__ __forceinline__ bool GridReduce(double (&v)[NV], const int (&op)[NV],
+                                           RedBuf rb, double* out) {
+  const int bid = blockIdx.x + gridDim.x * (blockIdx.y + gridDim.y * blockIdx.z);
+  const int nblocks = gridDim.x * gridDim.y * gridDim.z;
+  return GroupReduce<NV>(v, op, rb, out, bid, nblocks);
 }
 
 }  // namespace aphgpu
