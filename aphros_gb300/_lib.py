@@ -103,6 +103,17 @@ def lib():
     L.aphgpu_residual_history.restype = _I
     L.aphgpu_elapsed.argtypes = [_P, _I, _I, _PD]
     L.aphgpu_time_kernel.argtypes = [_P, _I, _I, _PD, _PD]
+    L.aphgpu_batch_create.argtypes = [ctypes.POINTER(_P), _I, ctypes.POINTER(_P)]
+    L.aphgpu_batch_destroy.argtypes = [_P]
+    L.aphgpu_batch_destroy.restype = None
+    L.aphgpu_batch_last_error.argtypes = [_P]
+    L.aphgpu_batch_last_error.restype = ctypes.c_char_p
+    L.aphgpu_batch_solve.argtypes = [_P, ctypes.POINTER(Conf), _P]
+    L.aphgpu_batch_tune.argtypes = [_P, ctypes.POINTER(Conf), _PD]
+    L.aphgpu_batch_last_ms.argtypes = [_P, _PD, ctypes.POINTER(ctypes.c_int64)]
+    for name in ("aphgpu_batch_create", "aphgpu_batch_solve", "aphgpu_batch_tune",
+                 "aphgpu_batch_last_ms"):
+        getattr(L, name).restype = _I
     for name in ("aphgpu_create", "aphgpu_sync", "aphgpu_set_system_expr",
                  "aphgpu_get_system_expr",
                  "aphgpu_assemble_projection", "aphgpu_solve",
@@ -294,3 +305,52 @@ class Context:
 
     def device_bytes(self):
         return int(self._L.aphgpu_device_bytes(self._p))
+
+
+class Batch:
+    """Batched mixed-precision solve over many contexts (aphgpu_batch): one
+    kernel launch per multigrid level covers every domain."""
+
+    def __init__(self, ctxs):
+        self._L = lib()
+        self.ctxs = list(ctxs)
+        arr = (_P * len(self.ctxs))(*[c.handle for c in self.ctxs])
+        p = _P()
+        rc = self._L.aphgpu_batch_create(ctypes.byref(p), len(self.ctxs), arr)
+        if rc != OK:
+            raise AphgpuError(rc, "aphgpu_batch_create failed")
+        self._p = p
+
+    def close(self):
+        if getattr(self, "_p", None):
+            self._L.aphgpu_batch_destroy(self._p)
+            self._p = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def _check(self, rc):
+        if rc != OK:
+            msg = self._L.aphgpu_batch_last_error(self._p)
+            raise AphgpuError(rc, msg.decode() if msg else "")
+
+    def solve(self, conf):
+        """Solves every domain; returns one Info per domain."""
+        infos = (Info * len(self.ctxs))()
+        self._check(self._L.aphgpu_batch_solve(self._p, ctypes.byref(conf),
+                                               ctypes.cast(infos, _P)))
+        return list(infos)
+
+    def tune(self, conf):
+        """Autotunes tiles and sweeps; updates conf and returns the best ms."""
+        ms = _D()
+        self._check(self._L.aphgpu_batch_tune(self._p, ctypes.byref(conf), ctypes.byref(ms)))
+        return ms.value
+
+    def last(self):
+        ms, n = _D(), ctypes.c_int64()
+        self._check(self._L.aphgpu_batch_last_ms(self._p, ctypes.byref(ms), ctypes.byref(n)))
+        return ms.value, int(n.value)

@@ -36,6 +36,7 @@ CU_UNITS = {
     "vof.cu": ["-fmad=false"],
     "noalloc.cu": [],
     "server.cu": [],
+    "batch.cu": [],
 }
 
 

@@ -362,6 +362,8 @@ int SolveCG(aphgpu_ctx* ctx, const aphgpu_conf* conf, aphgpu_info* info);
 int SolveMGPCG(aphgpu_ctx* ctx, const aphgpu_conf* conf, aphgpu_info* info);
 int SolveMixed(aphgpu_ctx* ctx, const aphgpu_conf* conf, aphgpu_info* info);
 int SolveMGPCG32(aphgpu_ctx* ctx, const aphgpu_conf* conf, aphgpu_info* info);
+int EnsureMixedVectors(aphgpu_ctx* ctx);
+int EnsureMixedHierarchy(aphgpu_ctx* ctx, const aphgpu_conf* conf);
 int SetSystemExprDevice(aphgpu_ctx* ctx, const double* d_expr8);
 int AssembleProjectionDevice(aphgpu_ctx* ctx, const double* d_alpha,
                              double rho1, double rho2, const double* d_vflux,

@@ -1259,7 +1259,8 @@ int BuildCoarsestInverse(aphgpu_ctx* ctx, const Level<T>& L, double** dinv, int*
       inv[(size_t)i * n + col] = v / Lm[(size_t)i * n + i];
     }
   }
-  if (!*dinv) APH_TRY(Alloc(ctx, dinv, (int64_t)kDenseMax * kDenseMax));
+  // sized for this level (a context keeps its grid, so n does not grow)
+  if (!*dinv || *dn < n) APH_TRY(Alloc(ctx, dinv, (int64_t)n * n));
   APH_CUDA(ctx, cudaMemcpyAsync(*dinv, inv.data(), sizeof(double) * inv.size(),
                                 cudaMemcpyHostToDevice, st));
   APH_CUDA(ctx, cudaStreamSynchronize(st));
@@ -1753,6 +1754,15 @@ int EnsureMixedVectors(aphgpu_ctx* ctx) {
   APH_TRY(Alloc(ctx, &ctx->ap32, N));
   APH_TRY(Alloc(ctx, &ctx->z32, N));
   APH_TRY(Alloc(ctx, &ctx->zold32, N));
+  return APHGPU_OK;
+}
+
+int EnsureMixedHierarchy(aphgpu_ctx* ctx, const aphgpu_conf* conf) {
+  APH_TRY(EnsureMixedVectors(ctx));
+  if (!ctx->mg.built32) {
+    APH_TRY(BuildHierarchy<float>(ctx, ctx->mg.l32, conf->mg_coarse_max));
+    ctx->mg.built32 = true;
+  }
   return APHGPU_OK;
 }
 

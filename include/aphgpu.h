@@ -307,6 +307,35 @@ int aphgpu_server_get_state(aphgpu_server* server, int sim, double* alpha,
                             double* pressure);
 int aphgpu_server_get_stats(aphgpu_server* server, aphgpu_server_stats* stats);
 
+/* Batched solve of many independent periodic domains of uneven size, each
+ * with its own context holding an assembled system (set_system_expr or
+ * assemble_projection): the mixed-precision solver of every domain, with
+ * every kernel launch covering all domains at one multigrid level through
+ * per-level tile tables, per-domain reductions and stopping flags, and
+ * batches of inner iterations replayed from a CUDA graph.  Domains converge
+ * independently; each domain's result is what its own mixed solve computes
+ * up to the order of floating-point sums.  The coarsest level of every
+ * domain must be small enough for the dense direct solve (at most 1024
+ * cells).  Every context must live on the same device; the batch runs on the
+ * stream of the first context and waits for the others' pending work.  The
+ * solution is left resident in each context (aphgpu_get_solution).  There
+ * is no counterpart in the reference (it solves one domain per process). */
+typedef struct aphgpu_batch aphgpu_batch;
+
+int aphgpu_batch_create(aphgpu_batch** batch, int count, aphgpu_ctx* const* ctxs);
+void aphgpu_batch_destroy(aphgpu_batch* batch);
+const char* aphgpu_batch_last_error(const aphgpu_batch* batch);
+/* Solves every domain from a zero initial guess with the mixed-precision
+ * settings of conf (solver field ignored); infos (may be NULL) receives one
+ * aphgpu_info per domain. */
+int aphgpu_batch_solve(aphgpu_batch* batch, const aphgpu_conf* conf, aphgpu_info* infos);
+/* Autotuner: times solves over the planes per thread of the batched tiles
+ * and the smoothing sweeps, keeps the fastest tiles in the batch and writes
+ * its sweeps into conf (mg_pre = mg_post); best_ms may be NULL. */
+int aphgpu_batch_tune(aphgpu_batch* batch, aphgpu_conf* conf, double* best_ms);
+/* Device milliseconds of the last solve and kernels launched so far. */
+int aphgpu_batch_last_ms(const aphgpu_batch* batch, double* ms, int64_t* launches);
+
 /* Records event `slot` (0..7) on the context's stream; aphgpu_elapsed
  * returns the milliseconds between two recorded slots (waits for the
  * second). */
