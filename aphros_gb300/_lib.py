@@ -111,8 +111,10 @@ def lib():
     L.aphgpu_batch_solve.argtypes = [_P, ctypes.POINTER(Conf), _P]
     L.aphgpu_batch_tune.argtypes = [_P, ctypes.POINTER(Conf), _PD]
     L.aphgpu_batch_last_ms.argtypes = [_P, _PD, ctypes.POINTER(ctypes.c_int64)]
+    L.aphgpu_batch_set_tiles.argtypes = [_P, _I, _I]
+    L.aphgpu_batch_get_tiles.argtypes = [_P, ctypes.POINTER(_I), ctypes.POINTER(_I)]
     for name in ("aphgpu_batch_create", "aphgpu_batch_solve", "aphgpu_batch_tune",
-                 "aphgpu_batch_last_ms"):
+                 "aphgpu_batch_last_ms", "aphgpu_batch_set_tiles", "aphgpu_batch_get_tiles"):
         getattr(L, name).restype = _I
     for name in ("aphgpu_create", "aphgpu_sync", "aphgpu_set_system_expr",
                  "aphgpu_get_system_expr",
@@ -349,6 +351,15 @@ class Batch:
         ms = _D()
         self._check(self._L.aphgpu_batch_tune(self._p, ctypes.byref(conf), ctypes.byref(ms)))
         return ms.value
+
+    def set_tiles(self, planes, coarse_cells):
+        self._check(self._L.aphgpu_batch_set_tiles(self._p, planes, coarse_cells))
+
+    def tiles(self):
+        """(z planes per tile, coarse-level cells of the per-domain cycle)."""
+        a, b = _I(), _I()
+        self._check(self._L.aphgpu_batch_get_tiles(self._p, ctypes.byref(a), ctypes.byref(b)))
+        return a.value, b.value
 
     def last(self):
         ms, n = _D(), ctypes.c_int64()

@@ -32,6 +32,7 @@
 
 #include "common.cuh"
 #include "stencil.cuh"
+#include "vec.cuh"
 
 namespace aphgpu {
 
@@ -436,32 +437,6 @@ inline dim3 VecGrid(const Dims& d) {
 }
 inline bool VecOk(const Dims& d) { return (d.nx % 4) == 0 && d.nx >= 8; }
 
-__device__ __forceinline__ float4 Ld4(const float* p) {
-  return *reinterpret_cast<const float4*>(p);
-}
-__device__ __forceinline__ void St4(float* p, float4 v) {
-  *reinterpret_cast<float4*>(p) = v;
-}
-__device__ __forceinline__ float El(const float4& v, int e) {
-  return e == 0 ? v.x : e == 1 ? v.y : e == 2 ? v.z : v.w;
-}
-__device__ __forceinline__ void SetEl(float4& v, int e, float a) {
-  if (e == 0) v.x = a; else if (e == 1) v.y = a; else if (e == 2) v.z = a; else v.w = a;
-}
-
-// Left value (cell 4q-1) and right value (cell 4q+4) of a float4 row segment;
-// every lane of the warp must call it (inactive lanes pass anything).
-__device__ __forceinline__ void XHalo(const float* row, float4 v, int q, int nq,
-                                      bool act, float& l, float& r) {
-  const int lane = threadIdx.x;
-  l = __shfl_up_sync(0xffffffffu, v.w, 1);
-  r = __shfl_down_sync(0xffffffffu, v.x, 1);
-  if (act) {
-    if (lane == 0 || q == 0) l = row[q == 0 ? 4 * nq - 1 : 4 * q - 1];
-    if (lane == 31 || q == nq - 1) r = row[q == nq - 1 ? 0 : 4 * q + 4];
-  }
-}
-
 // One red-black half sweep (FP32, vectorized); see KSmooth for the update.
 // The diagonal is recomputed from the six couplings (read anyway) unless the
 // operator stores one.
@@ -469,141 +444,21 @@ __global__ void __launch_bounds__(256, 4) KSmooth4(Op<float> A, const float* __r
                                                 float* x, int color, int zero_init,
                                                 const SolveScalars* s, int kz) {
   if (s && s->done) return;
-  const Dims d = A.d;
-  const int nq = d.nx >> 2;
-  const int q = blockIdx.x * 32 + threadIdx.x;
-  const int j = blockIdx.y * 8 + threadIdx.y;
-  const bool act = q < nq && j < d.ny;
   const int kb = blockIdx.z * kz;
-  const int ke = min(kb + kz, d.nz);
-  const int jm = wrapm(j - 1, d.ny), jp = wrapp(j + 1, d.ny);
-  const int i0 = 4 * q;
-  float4 xz0 = make_float4(0, 0, 0, 0), xz1 = xz0, xz2 = xz0, wz1 = xz0, wz2 = xz0;
-  if (act && !zero_init) {
-    xz0 = Ld4(x + d.idx(i0, j, wrapm(kb - 1, d.nz)));
-    xz1 = Ld4(x + d.idx(i0, j, kb));
-  }
-  if (act) wz1 = Ld4(A.w2 + d.idx(i0, j, kb));
-  for (int k = kb; k < ke; ++k) {
-    const int kp = wrapp(k + 1, d.nz);
-    const int64_t c = d.idx(i0, j, k);
-    float4 w0v = xz0, w1v = xz0, w1n = xz0, bv = xz0, xjm = xz0, xjp = xz0;
-    if (act) {
-      wz2 = Ld4(A.w2 + d.idx(i0, j, kp));
-      w0v = Ld4(A.w0 + c);
-      w1v = Ld4(A.w1 + c);
-      w1n = Ld4(A.w1 + d.idx(i0, jp, k));
-      bv = Ld4(b + c);
-      if (!zero_init) {
-        xz2 = Ld4(x + d.idx(i0, j, kp));
-        xjm = Ld4(x + d.idx(i0, jm, k));
-        xjp = Ld4(x + d.idx(i0, jp, k));
-      }
-    }
-    float xl, xr, wl, wr;
-    XHalo(x + d.idx(0, j, k), xz1, q, nq, act && !zero_init, xl, xr);
-    XHalo(A.w0 + d.idx(0, j, k), w0v, q, nq, act, wl, wr);
-    (void)wl;
-    if (act) {
-      float4 out = xz1;
-      const int e0 = (color + j + k) & 1;
-#pragma unroll
-      for (int e = 0; e < 4; ++e) {
-        if ((e & 1) != e0) continue;
-        const float cxm = El(w0v, e);
-        const float cxp = e == 3 ? wr : El(w0v, e + 1);
-        const float cym = El(w1v, e), cyp = El(w1n, e);
-        const float czm = El(wz1, e), czp = El(wz2, e);
-        const float dg = A.diag ? A.diag[c + e]
-                                : -(((((cxm + cxp) + cym) + cyp) + czm) + czp);
-        float acc = El(bv, e);
-        if (!zero_init) {
-          const float vxm = e == 0 ? xl : El(xz1, e - 1);
-          const float vxp = e == 3 ? xr : El(xz1, e + 1);
-          acc -= cxm * vxm;
-          acc -= cxp * vxp;
-          acc -= cym * El(xjm, e);
-          acc -= cyp * El(xjp, e);
-          acc -= czm * El(xz0, e);
-          acc -= czp * El(xz2, e);
-        }
-        SetEl(out, e, acc / dg);
-      }
-      St4(x + c, out);
-    }
-    xz0 = xz1;
-    xz1 = xz2;
-    wz1 = wz2;
-  }
+  Smooth4Body(A, b, x, color, zero_init, blockIdx.x * 32 + threadIdx.x,
+              blockIdx.y * 8 + threadIdx.y, kb, min(kb + kz, A.d.nz));
 }
 
 // y = A p (FP32, vectorized) with the reductions p.y and sum y of KPcgApply
 __global__ void __launch_bounds__(256, 4) KPcgApply4(Op<float> A, const float* __restrict__ p,
                                                   float* ap, SolveScalars* s, RedBuf rb, int kz) {
   if (s->done) return;
-  const Dims d = A.d;
-  const int nq = d.nx >> 2;
-  const int q = blockIdx.x * 32 + threadIdx.x;
-  const int j = blockIdx.y * 8 + threadIdx.y;
-  const bool act = q < nq && j < d.ny;
   const int kb = blockIdx.z * kz;
-  const int ke = min(kb + kz, d.nz);
-  const int jm = wrapm(j - 1, d.ny), jp = wrapp(j + 1, d.ny);
-  const int i0 = 4 * q;
   // per-thread sums in FP32 (at most 4 * kz terms), CTA and grid sums in
   // FP64: FP64 arithmetic is scarce on GB300
   float fa0 = 0.f, fa1 = 0.f;
-  float4 z0 = make_float4(0, 0, 0, 0), z1 = z0, z2 = z0, wz1 = z0, wz2 = z0;
-  if (act) {
-    z0 = Ld4(p + d.idx(i0, j, wrapm(kb - 1, d.nz)));
-    z1 = Ld4(p + d.idx(i0, j, kb));
-    wz1 = Ld4(A.w2 + d.idx(i0, j, kb));
-  }
-  for (int k = kb; k < ke; ++k) {
-    const int kp = wrapp(k + 1, d.nz);
-    const int64_t c = d.idx(i0, j, k);
-    float4 w0v = z0, w1v = z0, w1n = z0, pjm = z0, pjp = z0;
-    if (act) {
-      z2 = Ld4(p + d.idx(i0, j, kp));
-      wz2 = Ld4(A.w2 + d.idx(i0, j, kp));
-      w0v = Ld4(A.w0 + c);
-      w1v = Ld4(A.w1 + c);
-      w1n = Ld4(A.w1 + d.idx(i0, jp, k));
-      pjm = Ld4(p + d.idx(i0, jm, k));
-      pjp = Ld4(p + d.idx(i0, jp, k));
-    }
-    float pl, pr, wl, wr;
-    XHalo(p + d.idx(0, j, k), z1, q, nq, act, pl, pr);
-    XHalo(A.w0 + d.idx(0, j, k), w0v, q, nq, act, wl, wr);
-    (void)wl;
-    if (act) {
-      float4 out;
-#pragma unroll
-      for (int e = 0; e < 4; ++e) {
-        const float cxm = El(w0v, e);
-        const float cxp = e == 3 ? wr : El(w0v, e + 1);
-        const float cym = El(w1v, e), cyp = El(w1n, e);
-        const float czm = El(wz1, e), czp = El(wz2, e);
-        const float dg = A.diag ? A.diag[c + e]
-                                : -(((((cxm + cxp) + cym) + cyp) + czm) + czp);
-        const float pc = El(z1, e);
-        float y = pc * dg;
-        y += (e == 0 ? pl : El(z1, e - 1)) * cxm;
-        y += (e == 3 ? pr : El(z1, e + 1)) * cxp;
-        y += El(pjm, e) * cym;
-        y += El(pjp, e) * cyp;
-        y += El(z0, e) * czm;
-        y += El(z2, e) * czp;
-        SetEl(out, e, y);
-        fa0 += pc * y;
-        fa1 += y;
-      }
-      St4(ap + c, out);
-    }
-    z0 = z1;
-    z1 = z2;
-    wz1 = wz2;
-  }
+  Apply4Body(A, p, ap, blockIdx.x * 32 + threadIdx.x, blockIdx.y * 8 + threadIdx.y, kb,
+             min(kb + kz, A.d.nz), fa0, fa1);
   double v[2] = {(double)fa0, (double)fa1};
   const int op[2] = {0, 0};
   __shared__ double out2[2];
@@ -620,22 +475,9 @@ __global__ void __launch_bounds__(256, 4) KPcgApply4(Op<float> A, const float* _
 __global__ void KProlong4(Dims d, float* x, Dims dc, const float* __restrict__ xc,
                           const SolveScalars* s, int kz) {
   if (s && s->done) return;
-  const int nq = d.nx >> 2;
-  const int q = blockIdx.x * 32 + threadIdx.x;
-  const int j = blockIdx.y * 8 + threadIdx.y;
-  if (q >= nq || j >= d.ny) return;
   const int kb = blockIdx.z * kz;
-  const int ke = min(kb + kz, d.nz);
-  for (int k = kb; k < ke; ++k) {
-    const int64_t c = d.idx(4 * q, j, k);
-    const float2 e = *reinterpret_cast<const float2*>(xc + dc.idx(2 * q, j >> 1, k >> 1));
-    float4 v = Ld4(x + c);
-    v.x += e.x;
-    v.y += e.x;
-    v.z += e.y;
-    v.w += e.y;
-    St4(x + c, v);
-  }
+  Prolong4Body(d, x, dc, xc, blockIdx.x * 32 + threadIdx.x, blockIdx.y * 8 + threadIdx.y, kb,
+               min(kb + kz, d.nz));
 }
 
 // x += alpha p, r -= alpha (ap - mean(ap)), reductions and stopping test of
@@ -735,60 +577,9 @@ __global__ void __launch_bounds__(256, 4) KResidualRestrict4(Op<float> A, const 
                                                           float* bc, const SolveScalars* s,
                                                           int kz) {
   if (s && s->done) return;
-  const Dims d = A.d;
-  const int nq = d.nx >> 2;
-  const int q = blockIdx.x * 32 + threadIdx.x;
-  const int J = blockIdx.y * 8 + threadIdx.y;
-  const bool act = q < nq && J < dc.ny;
   const int Kb = blockIdx.z * kz;
-  const int Ke = min(Kb + kz, dc.nz);
-  const int i0 = 4 * q;
-  for (int K = Kb; K < Ke; ++K) {
-    float acc0 = 0.f, acc1 = 0.f;
-#pragma unroll
-    for (int sub = 0; sub < 4; ++sub) {
-      const int j = 2 * J + (sub & 1);
-      const int k = 2 * K + (sub >> 1);
-      const int jm = wrapm(j - 1, d.ny), jp = wrapp(j + 1, d.ny);
-      const int km = wrapm(k - 1, d.nz), kp = wrapp(k + 1, d.nz);
-      const int64_t c = d.idx(i0, act ? j : 0, k);
-      float4 xv = make_float4(0, 0, 0, 0), w0v = xv;
-      if (act) {
-        xv = Ld4(x + c);
-        w0v = Ld4(A.w0 + c);
-      }
-      float xl, xr, wl, wr;
-      XHalo(x + d.idx(0, act ? j : 0, k), xv, q, nq, act, xl, xr);
-      XHalo(A.w0 + d.idx(0, act ? j : 0, k), w0v, q, nq, act, wl, wr);
-      (void)wl;
-      if (act) {
-        const float4 w1v = Ld4(A.w1 + c), w1n = Ld4(A.w1 + d.idx(i0, jp, k));
-        const float4 w2v = Ld4(A.w2 + c), w2n = Ld4(A.w2 + d.idx(i0, j, kp));
-        const float4 xjm = Ld4(x + d.idx(i0, jm, k)), xjp = Ld4(x + d.idx(i0, jp, k));
-        const float4 xkm = Ld4(x + d.idx(i0, j, km)), xkp = Ld4(x + d.idx(i0, j, kp));
-        const float4 bv = Ld4(b + c);
-#pragma unroll
-        for (int e = 0; e < 4; ++e) {
-          const float cxm = El(w0v, e);
-          const float cxp = e == 3 ? wr : El(w0v, e + 1);
-          const float cym = El(w1v, e), cyp = El(w1n, e);
-          const float czm = El(w2v, e), czp = El(w2n, e);
-          const float dg = A.diag ? A.diag[c + e]
-                                  : -(((((cxm + cxp) + cym) + cyp) + czm) + czp);
-          float y = El(xv, e) * dg;
-          y += (e == 0 ? xl : El(xv, e - 1)) * cxm;
-          y += (e == 3 ? xr : El(xv, e + 1)) * cxp;
-          y += El(xjm, e) * cym;
-          y += El(xjp, e) * cyp;
-          y += El(xkm, e) * czm;
-          y += El(xkp, e) * czp;
-          const float rv = El(bv, e) - y;
-          if (e < 2) acc0 += rv; else acc1 += rv;
-        }
-      }
-    }
-    if (act) *reinterpret_cast<float2*>(bc + dc.idx(2 * q, J, K)) = make_float2(acc0, acc1);
-  }
+  ResidualRestrict4Body(A, b, x, dc, bc, blockIdx.x * 32 + threadIdx.x,
+                        blockIdx.y * 8 + threadIdx.y, Kb, min(Kb + kz, dc.nz));
 }
 
 // Residual of the fine level summed over the 8 children into the coarse

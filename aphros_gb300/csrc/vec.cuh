@@ -1,0 +1,259 @@
+// Vectorized FP32 stencil bodies (nx % 4 == 0) shared by the single-domain
+// kernels of poisson.cu and the batched kernels of batch.cu.
+//
+// Each thread owns 4 consecutive cells in x (one float4) at float4 column q
+// and row j, and marches over the planes [kb, ke) in z, keeping the z
+// neighbours in registers.  A warp holds 32 / tx row segments of tx
+// consecutive columns (tx a power of two <= 32: rows narrower than 32
+// float4s do not leave lanes idle); x neighbours across float4 boundaries
+// come from warp shuffles within a segment (global loads at segment and
+// domain edges, periodic wrap), so every lane of a warp must call a body,
+// active or not (act = q < nq and the row is inside the level); a CTA is
+// 32 x 8 threads.
+#pragma once
+
+#include "stencil.cuh"
+
+namespace aphgpu {
+
+__device__ __forceinline__ float4 Ld4(const float* p) {
+  return *reinterpret_cast<const float4*>(p);
+}
+__device__ __forceinline__ void St4(float* p, float4 v) {
+  *reinterpret_cast<float4*>(p) = v;
+}
+__device__ __forceinline__ float El(const float4& v, int e) {
+  return e == 0 ? v.x : e == 1 ? v.y : e == 2 ? v.z : v.w;
+}
+__device__ __forceinline__ void SetEl(float4& v, int e, float a) {
+  if (e == 0) v.x = a; else if (e == 1) v.y = a; else if (e == 2) v.z = a; else v.w = a;
+}
+
+// Left value (cell 4q-1) and right value (cell 4q+4) of a float4 row segment
+// of tx lanes; every lane of the warp must call it (inactive lanes pass
+// anything).
+__device__ __forceinline__ void XHalo(const float* row, float4 v, int q, int nq,
+                                      bool act, float& l, float& r, int tx = 32) {
+  const int sl = threadIdx.x & (tx - 1);
+  l = __shfl_up_sync(0xffffffffu, v.w, 1);
+  r = __shfl_down_sync(0xffffffffu, v.x, 1);
+  if (act) {
+    if (sl == 0 || q == 0) l = row[q == 0 ? 4 * nq - 1 : 4 * q - 1];
+    if (sl == tx - 1 || q == nq - 1) r = row[q == nq - 1 ? 0 : 4 * q + 4];
+  }
+}
+
+// One red-black half sweep of colour `color` on planes [kb, ke): x = (b -
+// sum of the couplings times the neighbours) / diagonal; zero_init: the
+// neighbours are taken as zero.  The diagonal is recomputed from the six
+// couplings (read anyway) unless the operator stores one.
+__device__ __forceinline__ void Smooth4Body(const Op<float>& A, const float* __restrict__ b,
+                                            float* x, int color, int zero_init, int q, int j,
+                                            int kb, int ke, int tx = 32) {
+  const Dims d = A.d;
+  const int nq = d.nx >> 2;
+  const bool act = q < nq && j < d.ny;
+  const int jm = wrapm(j - 1, d.ny), jp = wrapp(j + 1, d.ny);
+  const int i0 = 4 * q;
+  float4 xz0 = make_float4(0, 0, 0, 0), xz1 = xz0, xz2 = xz0, wz1 = xz0, wz2 = xz0;
+  if (act && !zero_init) {
+    xz0 = Ld4(x + d.idx(i0, j, wrapm(kb - 1, d.nz)));
+    xz1 = Ld4(x + d.idx(i0, j, kb));
+  }
+  if (act) wz1 = Ld4(A.w2 + d.idx(i0, j, kb));
+  for (int k = kb; k < ke; ++k) {
+    const int kp = wrapp(k + 1, d.nz);
+    const int64_t c = d.idx(i0, j, k);
+    float4 w0v = xz0, w1v = xz0, w1n = xz0, bv = xz0, xjm = xz0, xjp = xz0;
+    if (act) {
+      wz2 = Ld4(A.w2 + d.idx(i0, j, kp));
+      w0v = Ld4(A.w0 + c);
+      w1v = Ld4(A.w1 + c);
+      w1n = Ld4(A.w1 + d.idx(i0, jp, k));
+      bv = Ld4(b + c);
+      if (!zero_init) {
+        xz2 = Ld4(x + d.idx(i0, j, kp));
+        xjm = Ld4(x + d.idx(i0, jm, k));
+        xjp = Ld4(x + d.idx(i0, jp, k));
+      }
+    }
+    float xl, xr, wl, wr;
+    XHalo(x + d.idx(0, act ? j : 0, k), xz1, q, nq, act && !zero_init, xl, xr, tx);
+    XHalo(A.w0 + d.idx(0, act ? j : 0, k), w0v, q, nq, act, wl, wr, tx);
+    (void)wl;
+    if (act) {
+      float4 out = xz1;
+      const int e0 = (color + j + k) & 1;
+#pragma unroll
+      for (int e = 0; e < 4; ++e) {
+        if ((e & 1) != e0) continue;
+        const float cxm = El(w0v, e);
+        const float cxp = e == 3 ? wr : El(w0v, e + 1);
+        const float cym = El(w1v, e), cyp = El(w1n, e);
+        const float czm = El(wz1, e), czp = El(wz2, e);
+        const float dg = A.diag ? A.diag[c + e]
+                                : -(((((cxm + cxp) + cym) + cyp) + czm) + czp);
+        float acc = El(bv, e);
+        if (!zero_init) {
+          const float vxm = e == 0 ? xl : El(xz1, e - 1);
+          const float vxp = e == 3 ? xr : El(xz1, e + 1);
+          acc -= cxm * vxm;
+          acc -= cxp * vxp;
+          acc -= cym * El(xjm, e);
+          acc -= cyp * El(xjp, e);
+          acc -= czm * El(xz0, e);
+          acc -= czp * El(xz2, e);
+        }
+        SetEl(out, e, acc / dg);
+      }
+      St4(x + c, out);
+    }
+    xz0 = xz1;
+    xz1 = xz2;
+    wz1 = wz2;
+  }
+}
+
+// y = A p on planes [kb, ke); per-thread FP32 sums of p.y (fa0) and of y
+// (fa1) are added to the arguments.
+__device__ __forceinline__ void Apply4Body(const Op<float>& A, const float* __restrict__ p,
+                                           float* ap, int q, int j, int kb, int ke,
+                                           float& fa0, float& fa1, int tx = 32) {
+  const Dims d = A.d;
+  const int nq = d.nx >> 2;
+  const bool act = q < nq && j < d.ny;
+  const int jm = wrapm(j - 1, d.ny), jp = wrapp(j + 1, d.ny);
+  const int i0 = 4 * q;
+  float4 z0 = make_float4(0, 0, 0, 0), z1 = z0, z2 = z0, wz1 = z0, wz2 = z0;
+  if (act) {
+    z0 = Ld4(p + d.idx(i0, j, wrapm(kb - 1, d.nz)));
+    z1 = Ld4(p + d.idx(i0, j, kb));
+    wz1 = Ld4(A.w2 + d.idx(i0, j, kb));
+  }
+  for (int k = kb; k < ke; ++k) {
+    const int kp = wrapp(k + 1, d.nz);
+    const int64_t c = d.idx(i0, j, k);
+    float4 w0v = z0, w1v = z0, w1n = z0, pjm = z0, pjp = z0;
+    if (act) {
+      z2 = Ld4(p + d.idx(i0, j, kp));
+      wz2 = Ld4(A.w2 + d.idx(i0, j, kp));
+      w0v = Ld4(A.w0 + c);
+      w1v = Ld4(A.w1 + c);
+      w1n = Ld4(A.w1 + d.idx(i0, jp, k));
+      pjm = Ld4(p + d.idx(i0, jm, k));
+      pjp = Ld4(p + d.idx(i0, jp, k));
+    }
+    float pl, pr, wl, wr;
+    XHalo(p + d.idx(0, act ? j : 0, k), z1, q, nq, act, pl, pr, tx);
+    XHalo(A.w0 + d.idx(0, act ? j : 0, k), w0v, q, nq, act, wl, wr, tx);
+    (void)wl;
+    if (act) {
+      float4 out;
+#pragma unroll
+      for (int e = 0; e < 4; ++e) {
+        const float cxm = El(w0v, e);
+        const float cxp = e == 3 ? wr : El(w0v, e + 1);
+        const float cym = El(w1v, e), cyp = El(w1n, e);
+        const float czm = El(wz1, e), czp = El(wz2, e);
+        const float dg = A.diag ? A.diag[c + e]
+                                : -(((((cxm + cxp) + cym) + cyp) + czm) + czp);
+        const float pc = El(z1, e);
+        float y = pc * dg;
+        y += (e == 0 ? pl : El(z1, e - 1)) * cxm;
+        y += (e == 3 ? pr : El(z1, e + 1)) * cxp;
+        y += El(pjm, e) * cym;
+        y += El(pjp, e) * cyp;
+        y += El(z0, e) * czm;
+        y += El(z2, e) * czp;
+        SetEl(out, e, y);
+        fa0 += pc * y;
+        fa1 += y;
+      }
+      St4(ap + c, out);
+    }
+    z0 = z1;
+    z1 = z2;
+    wz1 = wz2;
+  }
+}
+
+// x_fine += x_coarse(parent) on fine planes [kb, ke) (one float4 = 2 coarse
+// cells)
+__device__ __forceinline__ void Prolong4Body(const Dims& d, float* x, const Dims& dc,
+                                             const float* __restrict__ xc, int q, int j,
+                                             int kb, int ke) {
+  const int nq = d.nx >> 2;
+  if (q >= nq || j >= d.ny) return;
+  for (int k = kb; k < ke; ++k) {
+    const int64_t c = d.idx(4 * q, j, k);
+    const float2 e = *reinterpret_cast<const float2*>(xc + dc.idx(2 * q, j >> 1, k >> 1));
+    float4 v = Ld4(x + c);
+    v.x += e.x;
+    v.y += e.x;
+    v.z += e.y;
+    v.w += e.y;
+    St4(x + c, v);
+  }
+}
+
+// Residual b - A x of the fine level summed over the 8 children into the
+// coarse right-hand side bc: the thread owns one fine float4 (2 coarse cells
+// in x) of coarse row J and marches over the coarse planes [Kb, Ke).
+__device__ __forceinline__ void ResidualRestrict4Body(const Op<float>& A,
+                                                      const float* __restrict__ b,
+                                                      const float* __restrict__ x,
+                                                      const Dims& dc, float* bc, int q, int J,
+                                                      int Kb, int Ke, int tx = 32) {
+  const Dims d = A.d;
+  const int nq = d.nx >> 2;
+  const bool act = q < nq && J < dc.ny;
+  const int i0 = 4 * q;
+  for (int K = Kb; K < Ke; ++K) {
+    float acc0 = 0.f, acc1 = 0.f;
+#pragma unroll
+    for (int sub = 0; sub < 4; ++sub) {
+      const int j = 2 * J + (sub & 1);
+      const int k = 2 * K + (sub >> 1);
+      const int jm = wrapm(j - 1, d.ny), jp = wrapp(j + 1, d.ny);
+      const int km = wrapm(k - 1, d.nz), kp = wrapp(k + 1, d.nz);
+      const int64_t c = d.idx(i0, act ? j : 0, k);
+      float4 xv = make_float4(0, 0, 0, 0), w0v = xv;
+      if (act) {
+        xv = Ld4(x + c);
+        w0v = Ld4(A.w0 + c);
+      }
+      float xl, xr, wl, wr;
+      XHalo(x + d.idx(0, act ? j : 0, k), xv, q, nq, act, xl, xr, tx);
+      XHalo(A.w0 + d.idx(0, act ? j : 0, k), w0v, q, nq, act, wl, wr, tx);
+      (void)wl;
+      if (act) {
+        const float4 w1v = Ld4(A.w1 + c), w1n = Ld4(A.w1 + d.idx(i0, jp, k));
+        const float4 w2v = Ld4(A.w2 + c), w2n = Ld4(A.w2 + d.idx(i0, j, kp));
+        const float4 xjm = Ld4(x + d.idx(i0, jm, k)), xjp = Ld4(x + d.idx(i0, jp, k));
+        const float4 xkm = Ld4(x + d.idx(i0, j, km)), xkp = Ld4(x + d.idx(i0, j, kp));
+        const float4 bv = Ld4(b + c);
+#pragma unroll
+        for (int e = 0; e < 4; ++e) {
+          const float cxm = El(w0v, e);
+          const float cxp = e == 3 ? wr : El(w0v, e + 1);
+          const float cym = El(w1v, e), cyp = El(w1n, e);
+          const float czm = El(w2v, e), czp = El(w2n, e);
+          const float dg = A.diag ? A.diag[c + e]
+                                  : -(((((cxm + cxp) + cym) + cyp) + czm) + czp);
+          float y = El(xv, e) * dg;
+          y += (e == 0 ? xl : El(xv, e - 1)) * cxm;
+          y += (e == 3 ? xr : El(xv, e + 1)) * cxp;
+          y += El(xjm, e) * cym;
+          y += El(xjp, e) * cyp;
+          y += El(xkm, e) * czm;
+          y += El(xkp, e) * czp;
+          const float rv = El(bv, e) - y;
+          if (e < 2) acc0 += rv; else acc1 += rv;
+        }
+      }
+    }
+    if (act) *reinterpret_cast<float2*>(bc + dc.idx(2 * q, J, K)) = make_float2(acc0, acc1);
+  }
+}
+
+}  // namespace aphgpu

@@ -507,7 +507,11 @@ def run_batch(args):
     conf = _lib.default_conf(solver=_lib.SOLVER_MIXED, tol=0.0, rtol=1e-10)
     batch = _lib.Batch(ctxs)
     t0 = time.perf_counter()
-    tuned_ms = batch.tune(conf)
+    if args.tiles:
+        batch.set_tiles(*args.tiles)
+        tuned_ms = None
+    else:
+        tuned_ms = batch.tune(conf)
     tune_s = time.perf_counter() - t0
     for _ in range(args.warmup):
         infos = batch.solve(conf)
@@ -570,11 +574,15 @@ def run_batch(args):
         "config": {"workload": "batched: %d periodic domains, edge in {32,48,64,96}, 1-8 "
                                "bubbles, density ratio log-uniform [10,1000], %d cells total; "
                                "inputs %.1f GB > L2, no flush" % (n, cells, cells * 40 / 1e9),
-                   "tuned": {"mg_sweeps": conf.mg_pre, "tune_s": tune_s,
+                   "tuned": {"mg_sweeps": conf.mg_pre, "tile_planes": batch.tiles()[0],
+                             "coarse_cells": batch.tiles()[1], "tune_s": tune_s,
                              "best_tune_ms": tuned_ms}},
         "wall_ms_per_step": float(np.median(wall_ms)),
         "gpu_launches": launches,
         "all_converged": conv, "worst_rel_residual": worst,
+        "outer_iters_mean": float(np.mean([i.iter for i in infos])),
+        "inner_iters_mean": float(np.mean([i.inner_iter for i in infos])),
+        "inner_iters_max": int(max(i.inner_iter for i in infos)),
         "max_rel_l2_vs_per_domain_mixed": max(dev),
         "one_by_one_mixed_ms": mixed_ms, "one_by_one_fp64_ms": fp64_ms,
         "speedup_vs_one_by_one_mixed": mixed_ms / ms,
@@ -593,6 +601,26 @@ def run_profile(args):
     """Solves only (for ncu launch lists and captures)."""
     from aphros_gb300 import _lib, build, workload
     build.build()
+    if args.profile == "batch":
+        ctxs = []
+        for c in workload.batch_cases(args.domains):
+            ctx = _lib.Context(c.n, c.h, 0)
+            ctx.assemble_projection(c.alpha, c.rho1, c.rho2, c.flux, c.dt)
+            ctxs.append(ctx)
+        batch = _lib.Batch(ctxs)
+        if args.tiles:
+            batch.set_tiles(*args.tiles)
+        conf = _lib.default_conf(solver=_lib.SOLVER_MIXED, tol=0.0, rtol=1e-10)
+        l0 = 0
+        for s in range(args.warmup + args.steps):
+            if s == args.warmup:
+                l0 = batch.last()[1]
+            infos = batch.solve(conf)
+        print("profile batch: %d domains, %.3f ms last solve, %d launches per solve, "
+              "inner iterations max %d" % (len(ctxs), batch.last()[0],
+                                           (batch.last()[1] - l0) // max(args.steps, 1),
+                                           max(i.inner_iter for i in infos)))
+        return
     case = workload.config(args.workload)
     ctx = _lib.Context(case.n, case.h, 0)
     ctx.assemble_projection(case.alpha, case.rho1, case.rho2, case.flux, case.dt)
@@ -616,7 +644,7 @@ def main():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--cpu-budget", type=float, default=15.0)
-    ap.add_argument("--profile", choices=["mixed", "fp64"], default=None,
+    ap.add_argument("--profile", choices=["mixed", "fp64", "batch"], default=None,
                     help="profiling run: assemble, then `steps` solves of one solver "
                          "after `warmup` solves, no other work and no output line")
     ap.add_argument("--serve", action="store_true",
@@ -629,6 +657,9 @@ def main():
     ap.add_argument("--batch", action="store_true",
                     help="batched-domains benchmark instead of the solve benchmark")
     ap.add_argument("--domains", type=int, default=512)
+    ap.add_argument("--tiles", type=int, nargs=2, default=None,
+                    metavar=("PLANES", "COARSE_CELLS"),
+                    help="batched tiling instead of the autotuner")
     args = ap.parse_args()
     if args.profile:
         return run_profile(args)

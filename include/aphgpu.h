@@ -329,9 +329,15 @@ const char* aphgpu_batch_last_error(const aphgpu_batch* batch);
  * settings of conf (solver field ignored); infos (may be NULL) receives one
  * aphgpu_info per domain. */
 int aphgpu_batch_solve(aphgpu_batch* batch, const aphgpu_conf* conf, aphgpu_info* infos);
-/* Autotuner: times solves over the planes per thread of the batched tiles
- * and the smoothing sweeps, keeps the fastest tiles in the batch and writes
- * its sweeps into conf (mg_pre = mg_post); best_ms may be NULL. */
+/* Tiling of the batched launches: z planes per thread of a tile (1..64,
+ * default 4) and the size in cells at or below which a domain's coarse
+ * levels are cycled by one CTA per domain in a single launch (default
+ * 4096; 0: only the coarsest level). */
+int aphgpu_batch_set_tiles(aphgpu_batch* batch, int planes, int coarse_cells);
+int aphgpu_batch_get_tiles(const aphgpu_batch* batch, int* planes, int* coarse_cells);
+/* Autotuner: times solves over the tile planes and the coarse-level size,
+ * then over the smoothing sweeps; keeps the fastest tiling in the batch and
+ * writes its sweeps into conf (mg_pre = mg_post); best_ms may be NULL. */
 int aphgpu_batch_tune(aphgpu_batch* batch, aphgpu_conf* conf, double* best_ms);
 /* Device milliseconds of the last solve and kernels launched so far. */
 int aphgpu_batch_last_ms(const aphgpu_batch* batch, double* ms, int64_t* launches);

@@ -131,6 +131,29 @@ def test_repeat_is_bit_identical_and_domains_stop_independently():
     batch.close()
 
 
+@pytest.mark.parametrize("planes,coarse_cells", [(1, 0), (2, 512), (8, 32768), (4, 10 ** 6)])
+def test_tilings_agree(planes, coarse_cells):
+    """Every tiling (planes per tile; coarse levels cycled per domain from
+    only the coarsest up to whole domains) converges to the same pressure."""
+    ctxs = _contexts(_domains())
+    conf = _conf()
+    ref = []
+    for ctx in ctxs:
+        ctx.solve_resident(conf, zero_guess=True)
+        ref.append(ctx.get_solution())
+    batch = _lib.Batch(ctxs)
+    batch.set_tiles(planes, coarse_cells)
+    assert batch.tiles() == (planes, coarse_cells)
+    infos = batch.solve(conf)
+    for q, (ctx, info) in enumerate(zip(ctxs, infos)):
+        assert info.converged, q
+        rn, bn = ctx.residual_norms()
+        assert rn / bn <= 1.01 * RTOL, q
+        a, b = _demean(ctx.get_solution()), _demean(ref[q])
+        assert np.linalg.norm(a - b) / np.linalg.norm(b) < 1e-7, q
+    batch.close()
+
+
 def test_tune_keeps_results_converged():
     ctxs = _contexts(_domains()[:5], diffusion=False)
     batch = _lib.Batch(ctxs)
