@@ -18,6 +18,7 @@ ERR_NOMEM = 3
 ERR_NOT_SYMMETRIC = 4
 ERR_STATE = 5
 ERR_UNSUPPORTED = 6
+ERR_TIMEOUT = 7
 
 K_SMOOTH32, K_SMOOTH64, K_APPLY64, K_APPLY32, K_RESTRICT32 = 0, 1, 2, 3, 4
 K_VOF_FLUX, K_VOF_UPDATE, K_RECONSTRUCT, K_HEIGHTS, K_CURVATURE = 5, 6, 7, 8, 9
@@ -263,10 +264,14 @@ class Context:
         self._check(self._L.aphgpu_vof_get(self._p, ptr(u), ptr(nrm), ptr(a), ptr(m)))
         return u, nrm, a, m
 
-    def curvature(self, heights=False):
-        k = np.empty(self.N)
-        hg = np.empty(3 * self.N) if heights else None
+    def curvature(self, heights=False, out=True):
+        """Height-function curvature of the resident volume fraction; out=False
+        leaves it on the device (returns None)."""
+        k = np.empty(self.N) if out else None
+        hg = np.empty(3 * self.N) if heights and out else None
         self._check(self._L.aphgpu_curvature(self._p, ptr(k), ptr(hg)))
+        if not out:
+            return None
         return (k, hg) if heights else k
 
     def surface_tension(self, sigma, out=True):

@@ -145,6 +145,23 @@ int Admit(aphgpu_server* S, Sim& s) {
   return APHGPU_OK;
 }
 
+// Completes the oldest queued request of simulation `sim` with error `rc`.
+// Called with the lock held.
+void FailOldest(aphgpu_server* S, int sim, int rc, const char* why) {
+  S->err = why;
+  for (auto q = S->queue.begin(); q != S->queue.end(); ++q) {
+    if (q->sim != sim) continue;
+    aphgpu_step_result res{};
+    res.ticket = q->ticket;
+    res.sim = sim;
+    res.status = rc;
+    S->done[q->ticket] = res;
+    S->queue.erase(q);
+    S->cv_done.notify_all();
+    return;
+  }
+}
+
 // Makes room for `need` bytes by evicting idle simulations, least recently
 // used first.  Called with the lock held.  Returns false if impossible now.
 bool MakeRoom(aphgpu_server* S, int64_t need, int except) {
@@ -213,31 +230,39 @@ void Worker(aphgpu_server* S) {
       if (s.busy) continue;
       if (!s.ctx) {
         const int64_t need = s.bytes;
+        if (need > S->budget) {
+          // its measured footprint outgrew the budget: it can never be
+          // re-admitted, so its oldest request fails instead of waiting
+          FailOldest(S, s.id, APHGPU_ERR_NOMEM, "simulation larger than the budget");
+          rescan = true;
+          break;
+        }
         if (!MakeRoom(S, need, s.id)) continue;
         s.busy = true;  // reserve while admitting without the lock
         S->resident_bytes += need;
         lock.unlock();
         const int rc = Admit(S, s);
         lock.lock();
-        s.busy = false;
         if (rc != APHGPU_OK) {
           // the simulation's oldest request fails with the admission error
+          s.busy = false;
           S->resident_bytes -= need;
-          S->err = "admission failed";
-          for (auto q2 = S->queue.begin(); q2 != S->queue.end(); ++q2) {
-            if (q2->sim != s.id) continue;
-            aphgpu_step_result res{};
-            res.ticket = q2->ticket;
-            res.sim = s.id;
-            res.status = rc;
-            S->done[q2->ticket] = res;
-            S->queue.erase(q2);
-            S->cv_done.notify_all();
+          FailOldest(S, s.id, rc, "admission failed");
+          rescan = true;
+          break;
+        }
+        // run the admitted simulation's oldest request now, still reserved:
+        // released idle, another worker making room would evict it again
+        // before its step (admission/eviction thrash)
+        for (auto q2 = S->queue.begin(); q2 != S->queue.end(); ++q2)
+          if (q2->sim == s.id) {
+            it = q2;
             break;
           }
+        if (it == S->queue.end()) {
+          s.busy = false;
+          rescan = true;
         }
-        // the queue may have changed while unlocked: scan again
-        rescan = true;
         break;
       }
       it = q;
@@ -359,10 +384,21 @@ int aphgpu_server_submit(aphgpu_server* S, int sim, const double* vflux, double 
 }
 
 int aphgpu_server_wait(aphgpu_server* S, int64_t ticket, aphgpu_step_result* out) {
+  return aphgpu_server_wait_timeout(S, ticket, -1.0, out);
+}
+
+int aphgpu_server_wait_timeout(aphgpu_server* S, int64_t ticket, double timeout_ms,
+                               aphgpu_step_result* out) {
   if (!S || !out) return APHGPU_ERR_ARG;
   std::unique_lock<std::mutex> lock(S->mu);
   if (ticket <= 0 || ticket >= S->next_ticket) return APHGPU_ERR_ARG;
-  S->cv_done.wait(lock, [&] { return S->done.count(ticket) > 0; });
+  auto ready = [&] { return S->done.count(ticket) > 0; };
+  if (timeout_ms < 0) {
+    S->cv_done.wait(lock, ready);
+  } else if (!S->cv_done.wait_for(lock, std::chrono::duration<double, std::milli>(timeout_ms),
+                                  ready)) {
+    return APHGPU_ERR_TIMEOUT;  // still pending: may be waited for again
+  }
   *out = S->done[ticket];
   S->done.erase(ticket);
   return APHGPU_OK;

@@ -41,10 +41,13 @@ def _bind():
     L.aphgpu_server_submit.argtypes = [P, ctypes.c_int, P, ctypes.c_double,
                                        ctypes.POINTER(_I64)]
     L.aphgpu_server_wait.argtypes = [P, _I64, ctypes.POINTER(StepResult)]
+    L.aphgpu_server_wait_timeout.argtypes = [P, _I64, ctypes.c_double,
+                                             ctypes.POINTER(StepResult)]
     L.aphgpu_server_get_state.argtypes = [P, ctypes.c_int, P, P]
     L.aphgpu_server_get_stats.argtypes = [P, ctypes.POINTER(Stats)]
     for n in ("aphgpu_server_create", "aphgpu_server_add_sim", "aphgpu_server_submit",
-              "aphgpu_server_wait", "aphgpu_server_get_state", "aphgpu_server_get_stats"):
+              "aphgpu_server_wait", "aphgpu_server_wait_timeout", "aphgpu_server_get_state",
+              "aphgpu_server_get_stats"):
         getattr(L, n).restype = ctypes.c_int
     return L
 
@@ -92,9 +95,13 @@ class Server:
                                                  ctypes.byref(t)), "submit")
         return t.value
 
-    def wait(self, ticket):
+    def wait(self, ticket, timeout_s=None):
+        """Result of a step; with timeout_s, raises AphgpuError(TIMEOUT) if it
+        has not completed by then (the ticket stays pending)."""
         r = StepResult()
-        self._check(self._L.aphgpu_server_wait(self._p, ticket, ctypes.byref(r)), "wait")
+        ms = -1.0 if timeout_s is None else 1e3 * timeout_s
+        self._check(self._L.aphgpu_server_wait_timeout(self._p, ticket, ms, ctypes.byref(r)),
+                    "wait")
         return r
 
     def state(self, sim):

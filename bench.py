@@ -224,6 +224,78 @@ def cg_iterations_estimate(case_name, n_full, threads):
     return int(round(info.iter * n_full / ns)), int(info.iter), ns
 
 
+# algorithmic bytes per cell (compulsory traffic, each array element read or
+# written once): one PLIC step = three directional sweeps, each with its
+# re-reconstruction (volume fraction r/w 16, normals 24, plane constant 8,
+# face flux 8, fluid flux 8, reconstruction 41), and the height curvature
+# (second and fourth differences 80, heights 80, curvature with its inputs 40)
+VOF_STEP_BYTES = 315
+CURVATURE_BYTES = 200
+
+
+def measure_vof(ctx, case, peak, peak_kind, steps, cpu=True):
+    """PLIC advection + height curvature of the workload's bubble field with
+    the resident corrected fluxes of the last solve: device time per step
+    (CUDA events on the library stream), per-kernel bandwidth, and the
+    oracle's VOF step + curvature on the host cores on a bounded sample."""
+    from aphros_gb300 import _lib
+    N = case.N
+    ctx.flux_correct(out=False)
+    ctx.vof_init(case.alpha)
+    dt = case.cfl_dt(0.5)
+    adv, curv = [], []
+    for s in range(steps + 2):
+        ctx.vof_step(None, dt)
+        a = ctx.last_timing()[0]
+        ctx.curvature(out=False)
+        k = ctx.last_timing()[0]
+        if s >= 2:
+            adv.append(a)
+            curv.append(k)
+    kernels = {}
+    for kid in (_lib.K_VOF_FLUX, _lib.K_VOF_UPDATE, _lib.K_RECONSTRUCT, _lib.K_HEIGHTS,
+                _lib.K_CURVATURE):
+        ms_k, b_k = ctx.time_kernel(kid, reps=5)
+        kernels[_lib.KERNEL_NAMES[kid]] = {"ms": round(ms_k, 4),
+                                          "GB/s": round(b_k / (ms_k * 1e-3) / 1e9, 1)}
+    adv_ms, curv_ms = float(np.median(adv)), float(np.median(curv))
+    ach_a = VOF_STEP_BYTES * N / (adv_ms * 1e-3) / 1e9
+    ach_k = CURVATURE_BYTES * N / (curv_ms * 1e-3) / 1e9
+    out = {"dt_cfl": 0.5, "steps": steps,
+           "advection_ms_per_step": adv_ms, "curvature_ms": curv_ms,
+           "cell_steps_per_s": N / ((adv_ms + curv_ms) * 1e-3),
+           "roofline": {"bound": "hbm", "unit": "GB/s", "peak": peak, "peak_kind": peak_kind,
+                        "advection": {"bytes_per_cell": VOF_STEP_BYTES, "achieved": ach_a,
+                                      "frac": ach_a / peak},
+                        "curvature": {"bytes_per_cell": CURVATURE_BYTES, "achieved": ach_k,
+                                      "frac": ach_k / peak}},
+           "kernels": kernels}
+    if cpu:
+        import oracle
+        from aphros_gb300 import workload
+        threads = os.cpu_count() or 1
+        ns = max(32, case.n // 4)
+        cs = workload.Case(ns, case.centres, case.radii, rho1=case.rho1, rho2=case.rho2,
+                           seed=case.seed)
+        st = oracle.VofState(ns, cs.h, cs.alpha)
+        f = cs.flux
+        dts = cs.cfl_dt(0.5)
+        st.step(f, dts, nthreads=threads)
+        t0 = time.perf_counter()
+        reps = 3
+        for _ in range(reps):
+            st.step(f, dts, nthreads=threads)
+            st.curvature()
+        per = (time.perf_counter() - t0) / reps
+        out["cpu_baseline"] = {"value": ns ** 3 / per, "unit": "cell-steps/s", "cores": threads,
+                               "kind": "port",
+                               "sample": "%d steps of the C restatement of aphros Vof "
+                                         "(Weymouth sweeps) + Heights curvature at %d^3 on "
+                                         "the same bubbles and Taylor-Green flux"
+                                         % (reps, ns)}
+    return out
+
+
 # ---------------------------------------------------------------------------
 # arms
 # ---------------------------------------------------------------------------
@@ -299,6 +371,11 @@ def run_ours(args):
         except _lib.AphgpuError:
             pass
 
+    vof = None
+    if not args.no_vof:
+        vof = measure_vof(ctx, case, peak, peak_kind, max(3, min(args.steps, 10)),
+                          cpu=(rank == 0 and not args.no_cpu))
+
     # end to end through the drop-in with host buffers (pinned)
     e2e = None
     if not args.no_e2e:
@@ -366,6 +443,7 @@ def run_ours(args):
                      "frac": achieved / peak, "peak_kind": peak_kind,
                      "traffic": ncu_traffic("KSmooth<float>", N)},
         "kernels": kernel_table,
+        "vof": vof,
         "gpu_launches": int(l_mixed),
         "e2e": e2e,
         "cpu_baseline": cpu,
@@ -643,6 +721,8 @@ def main():
     ap.add_argument("--workload", choices=sorted(WORKLOADS), default="c3")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-vof", action="store_true",
+                    help="skip the PLIC advection + curvature measurement")
     ap.add_argument("--cpu-budget", type=float, default=15.0)
     ap.add_argument("--profile", choices=["mixed", "fp64", "batch"], default=None,
                     help="profiling run: assemble, then `steps` solves of one solver "

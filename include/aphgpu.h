@@ -34,7 +34,8 @@ enum {
   APHGPU_ERR_NOMEM = 3,        /* device allocation failed */
   APHGPU_ERR_NOT_SYMMETRIC = 4,/* system handed to a symmetric solver is not */
   APHGPU_ERR_STATE = 5,        /* call order violated (e.g. no system set) */
-  APHGPU_ERR_UNSUPPORTED = 6   /* grid shape not supported by the solver */
+  APHGPU_ERR_UNSUPPORTED = 6,  /* grid shape not supported by the solver */
+  APHGPU_ERR_TIMEOUT = 7       /* bounded wait ended before completion */
 };
 
 /* Solver kinds (the `linsolver_symm` values `gpu_cg`, `gpu`, `gpu_mixed`). */
@@ -301,6 +302,10 @@ int aphgpu_server_submit(aphgpu_server* server, int sim, const double* vflux,
 /* Waits for a step and returns its result (each ticket once). */
 int aphgpu_server_wait(aphgpu_server* server, int64_t ticket,
                        aphgpu_step_result* result);
+/* As aphgpu_server_wait, giving up after timeout_ms (< 0: no limit) with
+ * APHGPU_ERR_TIMEOUT; the ticket then stays pending. */
+int aphgpu_server_wait_timeout(aphgpu_server* server, int64_t ticket, double timeout_ms,
+                               aphgpu_step_result* result);
 /* Volume fraction and pressure of a simulation after its queued steps
  * that have started have finished (either pointer may be NULL). */
 int aphgpu_server_get_state(aphgpu_server* server, int sim, double* alpha,

@@ -28,7 +28,17 @@ def _run(cases, order, slots, budget, steps=3, sigma=0.05):
                 c = cases[i]
                 dt = 0.5 * c.cfl_dt(0.5)
                 tickets.append(srv.submit(sims[i], c.flux, dt))
-        res = [srv.wait(t) for t in tickets]
+        res = []
+        for t in tickets:
+            try:
+                res.append(srv.wait(t, timeout_s=120))
+            except _lib.AphgpuError as e:
+                st = srv.stats()
+                raise AssertionError(
+                    "ticket %d not done (%s): completed %d queued %d resident %d "
+                    "resident_bytes %d budget %d evictions %d admissions %d"
+                    % (t, e, st.completed, st.queued, st.resident, st.resident_bytes,
+                       st.budget_bytes, st.evictions, st.admissions))
         assert all(r.status == _lib.OK for r in res)
         assert all(r.converged for r in res)
         states = {i: srv.state(sims[i]) for i in order}
@@ -51,8 +61,13 @@ def test_eviction_and_restore_are_exact():
     cases = _cases()
     order = list(range(len(cases)))
     big, _, st_big = _run(cases, order, slots=2, budget=100e9)
-    # room for about two of the larger simulations: forces evictions
-    small, _, st_small = _run(cases, order, slots=2, budget=2.5 * 440 * 48 ** 3)
+    # room for about half of the simulations' measured device memory, and for
+    # the admission estimate of the largest one (440 B/cell + 1 MiB): forces
+    # evictions
+    assert st_big.evictions == 0 and st_big.resident_bytes > 0
+    budget = max(0.5 * st_big.resident_bytes, 1.05 * (440 * 48 ** 3 + 2 ** 20))
+    assert budget < st_big.resident_bytes
+    small, _, st_small = _run(cases, order, slots=2, budget=budget)
     assert st_small.evictions > 0
     assert st_small.resident_bytes <= st_small.budget_bytes
     for i in order:
