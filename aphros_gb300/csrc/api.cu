@@ -137,6 +137,9 @@ struct Timer {
 int EnsureVof(aphgpu_ctx* ctx) {
   if (ctx->u) return APHGPU_OK;
   const int64_t N = ctx->N;
+  // the interface-cell lists of the advection hold 32-bit cell indices
+  if (N >= INT32_MAX)
+    return SetError(ctx, APHGPU_ERR_UNSUPPORTED, "VOF needs fewer than 2^31 cells");
   APH_TRY(Alloc(ctx, &ctx->u, N));
   APH_TRY(Alloc(ctx, &ctx->u0, N));
   APH_TRY(Alloc(ctx, &ctx->nrm, 3 * N));
@@ -561,7 +564,7 @@ int aphgpu_time_kernel(aphgpu_ctx* ctx, int kernel, int reps, double* ms, double
     if (!ctx->vof_ready) return SetError(ctx, APHGPU_ERR_STATE, "vof not initialised");
     double* d_vf = nullptr;
     APH_TRY(FaceScratch(ctx, &d_vf));
-    return TimeVofKernel(ctx, kernel, reps, ms, bytes, d_vf, 0.0);
+    return TimeVofKernel(ctx, kernel, reps, ms, bytes, d_vf, ctx->vof_dt);
   }
   return TimeSolverKernel(ctx, kernel, reps, ms, bytes);
 }

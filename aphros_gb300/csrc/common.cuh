@@ -295,6 +295,7 @@ struct aphgpu_ctx {
   double* hgt = nullptr;       // 3N AoS
   double clipth = 1e-10;
   int vof_count = 0;
+  double vof_dt = 0;  // time step of the last VOF step (kernel timing)
   bool vof_ready = false;
 
   // host staging (pinned)

@@ -9,11 +9,15 @@
 // in the cubic branch of the plane-constant solve.
 //
 // Per step (Vof::MakeIteration, weymouth scheme, vof.ipp:498-583):
-//   KFcuu                fcuu = u < 0.5 ? 0 : 1 (1 byte/cell)
-//   3 x { KSweepFlux     fluid flux through the faces of one direction
-//         KSweepUpdate   u += fcuu*ds - dl, clipping
-//         KReconstruct } normals (Youngs + height) and plane constants of
+//   KListInterface       fcuu = u < 0.5 ? 0 : 1 (1 byte/cell), list of the
+//                        interfacial cells (0 < u < 1)
+//   3 x { KSweepFlux     fluid flux v*u(upwind) through the faces of one
+//                        direction with a non-interfacial upwind cell
+//         KSweepFluxList PLIC fluxes of the faces with a listed upwind cell
+//         KSweepUpdate   u += fcuu*ds - dl, clipping; lists the new
 //                        interfacial cells
+//         KReconstructList } normals (Youngs + height) and plane constants
+//                        of the listed cells
 // Curvature (Heights::CalcCurvature, curv.ipp:358-414):
 //   KHeights             13-cell columns rebuilt from the same two-step and
 //                        four-step differences as CalcDiff2/CalcDiff4, then
@@ -21,6 +25,7 @@
 //   KCurvature           height-function curvature of interfacial cells
 #include <cuda_runtime.h>
 
+#include <algorithm>
 #include <cmath>
 
 #include "common.cuh"
@@ -231,6 +236,23 @@ __device__ void NormalCell(const double u3[27], double nout[3]) {
 
 __device__ __forceinline__ bool IsInterface(double u) { return u > 0 && u < 1; }
 
+// Tests on the bit pattern of a double, exact and free of FP64 instructions
+// (FP64 issue is the scarce resource on this GPU): positive doubles order
+// like their bits as signed integers, negative ones have negative bits.
+__device__ __forceinline__ long long Bits(double v) { return __double_as_longlong(v); }
+constexpr long long kOneBits = 0x3FF0000000000000LL;
+constexpr long long kHalfBits = 0x3FE0000000000000LL;
+constexpr long long kInfBits = 0x7FF0000000000000LL;
+// 0 < v < 1 (false for NaN)
+__device__ __forceinline__ bool InterfaceBits(long long b) { return b > 0 && b < kOneBits; }
+// v > 0 (false for NaN)
+__device__ __forceinline__ bool PositiveBits(long long b) { return b > 0 && b <= kInfBits; }
+__device__ __forceinline__ bool NanBits(long long b) {
+  return (b & 0x7FFFFFFFFFFFFFFFLL) > kInfBits;
+}
+// biased exponent (0x7FF for inf and NaN)
+__device__ __forceinline__ int ExpBits(long long b) { return (int)((b >> 52) & 0x7FF); }
+
 #define VOF_CELL_LOOP(dims)                                      \
   const int i = blockIdx.x * kTileX + threadIdx.x;               \
   const int j = blockIdx.y * kTileY + threadIdx.y;               \
@@ -244,96 +266,215 @@ __device__ __forceinline__ bool IsInterface(double u) { return u > 0 && u < 1; }
 // Kernels
 // ---------------------------------------------------------------------------
 
-// Vof::ReconstPlanes (vof.ipp:70-90) on interfacial cells only; values of
-// other cells are left untouched (they are never read).
-__global__ void KReconstruct(Dims d, double hx, double hy, double hz,
-                             const double* __restrict__ u, double* nrm,
-                             double* pa) {
-  VOF_CELL_LOOP(d)
-  const double uc = u[c];
-  if (!IsInterface(uc)) continue;
-  double u3[27];
-#pragma unroll
-  for (int dz = -1; dz <= 1; ++dz) {
-    const int kk = wrapi(k + dz, d.nz);
-#pragma unroll
-    for (int dy = -1; dy <= 1; ++dy) {
-      const int jj = wrapi(j + dy, d.ny);
-#pragma unroll
-      for (int dx = -1; dx <= 1; ++dx) {
-        const int ii = wrapi(i + dx, d.nx);
-        u3[(dx + 1) + 3 * (dy + 1) + 9 * (dz + 1)] = u[d.idx(ii, jj, kk)];
-      }
-    }
-  }
-  double n[3];
-  NormalCell(u3, n);
-  const double h[3] = {hx, hy, hz};
-  nrm[3 * c + 0] = n[0];
-  nrm[3 * c + 1] = n[1];
-  nrm[3 * c + 2] = n[2];
-  pa[c] = LineA(n, uc, h);
+// Interface-cell lists.  Only cells with 0 < u < 1 need the plane
+// reconstruction and the geometric fluxes; scattered over the grid they would
+// leave most lanes of a warp idle in the long FP64 branches, so they are
+// gathered into a list (warp-aggregated appends, order irrelevant: every
+// list entry is processed independently) and processed densely by
+// grid-stride kernels that read the list length on the device.
+
+// Appends c to the list when `want`; every lane of the warp must call it.
+__device__ __forceinline__ void ListAppend(bool want, int c, int* list, int* count) {
+  const unsigned m = __ballot_sync(0xffffffffu, want);
+  if (!m) return;
+  const int lane = (threadIdx.x + blockDim.x * threadIdx.y) & 31;
+  const int leader = __ffs(m) - 1;
+  int base = 0;
+  if (lane == leader) base = atomicAdd(count, __popc(m));
+  base = __shfl_sync(0xffffffffu, base, leader);
+  if (want) list[base + __popc(m & ((1u << lane) - 1u))] = c;
+}
+
+__device__ __forceinline__ void CellIJK(const Dims& d, int64_t c, int& i, int& j, int& k) {
+  i = (int)(c % d.nx);
+  const int64_t r = c / d.nx;
+  j = (int)(r % d.ny);
+  k = (int)(r / d.ny);
+}
+
+// Lists the interfacial cells of u and, when fcuu != NULL, sets
+// fcuu = u < 0.5 ? 0 : 1 (vof.ipp:516-519), 1 byte per cell.
+__global__ void KListInterface(Dims d, const double* __restrict__ u, uint8_t* fcuu,
+                               int* list, int* count) {
+  const int i = blockIdx.x * kTileX + threadIdx.x;
+  const int j = blockIdx.y * kTileY + threadIdx.y;
+  const int kb = blockIdx.z * kTileZ;
+  const int ke = min(kb + kTileZ, d.nz);
+  const bool in = i < d.nx && j < d.ny;
+  for (int k = kb; k < ke; ++k) {
+    const int64_t c = in ? d.idx(i, j, k) : 0;
+    const long long ub = in ? Bits(u[c]) : 0;
+    // u < 0.5 <=> bits below those of 0.5, NaN excluded
+    if (in && fcuu) fcuu[c] = (!NanBits(ub) && ub < kHalfBits) ? 0 : 1;
+    ListAppend(in && InterfaceBits(ub), (int)c, list, count);
   }
 }
 
-__global__ void KFcuu(int64_t n, const double* __restrict__ u, uint8_t* fcuu) {
-  for (int64_t c = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; c < n;
-       c += (int64_t)gridDim.x * blockDim.x)
-    fcuu[c] = u[c] < 0.5 ? 0 : 1;
+// Vof::ReconstPlanes (vof.ipp:70-90) on the listed interfacial cells;
+// values of other cells are left untouched (they are never read).
+__global__ void KReconstructList(Dims d, double hx, double hy, double hz,
+                                 const double* __restrict__ u, double* nrm, double* pa,
+                                 const int* __restrict__ list, const int* count) {
+  const int n = *count;
+  for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < n; t += gridDim.x * blockDim.x) {
+    const int64_t c = list[t];
+    int i, j, k;
+    CellIJK(d, c, i, j, k);
+    const double uc = u[c];
+    double u3[27];
+#pragma unroll
+    for (int dz = -1; dz <= 1; ++dz) {
+      const int kk = wrapi(k + dz, d.nz);
+#pragma unroll
+      for (int dy = -1; dy <= 1; ++dy) {
+        const int jj = wrapi(j + dy, d.ny);
+#pragma unroll
+        for (int dx = -1; dx <= 1; ++dx) {
+          const int ii = wrapi(i + dx, d.nx);
+          u3[(dx + 1) + 3 * (dy + 1) + 9 * (dz + 1)] = u[d.idx(ii, jj, kk)];
+        }
+      }
+    }
+    double nv[3];
+    NormalCell(u3, nv);
+    const double h[3] = {hx, hy, hz};
+    nrm[3 * c + 0] = nv[0];
+    nrm[3 * c + 1] = nv[1];
+    nrm[3 * c + 2] = nv[2];
+    pa[c] = LineA(nv, uc, h);
+  }
 }
 
 // Fluxes of Vof::Sweep (vof.ipp:228-256) through the faces of direction dir
-__global__ void KSweepFlux(Dims d, int dir, double hx, double hy, double hz,
-                           const double* __restrict__ u,
-                           const double* __restrict__ vflux,
-                           const double* __restrict__ nrm,
-                           const double* __restrict__ pa, double dt,
-                           double* ffvu) {
-  const double h[3] = {hx, hy, hz};
+// whose upwind cell is not interfacial: v * u(upwind) (the face flux v / 1.
+// of the reference is v); faces with an interfacial upwind cell are written
+// by KSweepFluxList.
+__global__ void KSweepFlux(Dims d, int dir, const double* __restrict__ u,
+                           const double* __restrict__ vflux, double* ffvu) {
   VOF_CELL_LOOP(d)
   const int64_t cm = dir == 0 ? d.idx(wrapm(i - 1, d.nx), j, k)
                    : dir == 1 ? d.idx(i, wrapm(j - 1, d.ny), k)
                               : d.idx(i, j, wrapm(k - 1, d.nz));
   const double v = vflux[c];
-  const double v0 = v / 1.;
-  const int64_t up = v > 0 ? cm : c;
+  const long long vb = Bits(v);
+  const int64_t up = PositiveBits(vb) ? cm : c;
   const double uu = u[up];
+  const long long ub = Bits(uu);
+  if (InterfaceBits(ub)) continue;
+  // finite v: v * (+0) is the zero with the sign of v, v * 1 is v
+  const bool fin = ExpBits(vb) != 0x7FF;
   double f;
-  if (uu > 0 && uu < 1) {
-    const double n[3] = {nrm[3 * up], nrm[3 * up + 1], nrm[3 * up + 2]};
-    const double sq = ((0 + sqr(n[0])) + sqr(n[1])) + sqr(n[2]);
-    if (sq > 0) {
-      f = LineFlux(n, pa[up], h, v0, dt, dir);
-    } else {
-      f = v0 * uu;
-    }
-  } else {
-    f = v0 * uu;
-  }
+  if (fin && ub == 0) f = copysign(0.0, v);
+  else if (fin && ub == kOneBits) f = v;
+  else f = v * uu;
   ffvu[c] = f;
   }
 }
 
-// Update of Vof::Sweep (vof.ipp:287-326), weymouth, with clipping
+// Flux of a face with interfacial upwind cell (normal n, plane constant a,
+// volume fraction uu): the PLIC flux when the normal is nonzero, else v*uu
+__device__ __forceinline__ double InterfaceFlux(const double n[3], double a, double uu,
+                                                const double h[3], double v, double dt,
+                                                int dir) {
+  const double sq = ((0 + sqr(n[0])) + sqr(n[1])) + sqr(n[2]);
+  if (sq > 0) return LineFlux(n, a, h, v, dt, dir);
+  return v * uu;
+}
+
+// The faces of direction dir whose upwind cell is a listed interfacial cell
+// c: its lower face (index c) when the flux there is not positive, its upper
+// face (index c + e_dir) when the flux there is positive.
+__global__ void KSweepFluxList(Dims d, int dir, double hx, double hy, double hz,
+                               const double* __restrict__ u,
+                               const double* __restrict__ vflux,
+                               const double* __restrict__ nrm,
+                               const double* __restrict__ pa, double dt, double* ffvu,
+                               const int* __restrict__ list, const int* count) {
+  const double h[3] = {hx, hy, hz};
+  const int n = *count;
+  for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < n; t += gridDim.x * blockDim.x) {
+    const int64_t c = list[t];
+    int i, j, k;
+    CellIJK(d, c, i, j, k);
+    const int64_t fp = dir == 0 ? d.idx(wrapp(i + 1, d.nx), j, k)
+                     : dir == 1 ? d.idx(i, wrapp(j + 1, d.ny), k)
+                                : d.idx(i, j, wrapp(k + 1, d.nz));
+    const double nv[3] = {nrm[3 * c], nrm[3 * c + 1], nrm[3 * c + 2]};
+    const double a = pa[c], uu = u[c];
+    const double vl = vflux[c], vu = vflux[fp];
+    if (!(vl > 0)) ffvu[c] = InterfaceFlux(nv, a, uu, h, vl, dt, dir);
+    if (vu > 0) ffvu[fp] = InterfaceFlux(nv, a, uu, h, vu, dt, dir);
+  }
+}
+
+// Update of Vof::Sweep (vof.ipp:287-326), weymouth, with clipping:
+//   u += fcuu * ds - dl,  ds = (v+ - v-) dt / vol,  dl = (f+ - f-) dt / vol
+// (the reference divides each face flux by 1 + 1e-16, which is 1 in
+// double).  The FP64 divisions (slow on this GPU) are skipped where IEEE
+// arithmetic makes them unnecessary, with bit-identical results: a zero
+// numerator gives a zero of the same sign; fcuu = 0 makes fcuu * ds a zero
+// with the sign of ds (finite); fcuu = 1 with equal numerators makes
+// ds - dl = +0.  That covers every cell away from the interface.  Cells
+// interfacial after the update are appended to the list.
 __global__ void KSweepUpdate(Dims d, int dir, double vol, double* u,
                              const double* __restrict__ vflux,
                              const double* __restrict__ ffvu,
                              const uint8_t* __restrict__ fcuu, double dt,
-                             double clipth) {
-  VOF_CELL_LOOP(d)
-  const int64_t fp = dir == 0 ? d.idx(wrapp(i + 1, d.nx), j, k)
-                   : dir == 1 ? d.idx(i, wrapp(j + 1, d.ny), k)
-                              : d.idx(i, j, wrapp(k + 1, d.nz));
-  const double ds = (vflux[fp] / (1 + 1e-16) - vflux[c] / (1 + 1e-16)) * dt / vol;
-  const double dl = (ffvu[fp] - ffvu[c]) * dt / vol;
-  double w = u[c];
-  w += (double)fcuu[c] * ds - dl;
-  if (!(w >= clipth)) {
-    w = 0;
-  } else if (!(w <= 1 - clipth)) {
-    w = 1;
-  }
-  u[c] = w;
+                             double clipth, int emax, int full_ok, int* list,
+                             int* count) {
+  const int i = blockIdx.x * kTileX + threadIdx.x;
+  const int j = blockIdx.y * kTileY + threadIdx.y;
+  const int kb = blockIdx.z * kTileZ;
+  const int ke = min(kb + kTileZ, d.nz);
+  const bool in = i < d.nx && j < d.ny;
+  const double big = vol * 1e300;  // |num| below this: num / vol is finite
+  for (int k = kb; k < ke; ++k) {
+    int64_t c = 0;
+    bool want = false;
+    if (in) {
+      c = d.idx(i, j, k);
+      const int64_t fp = dir == 0 ? d.idx(wrapp(i + 1, d.nx), j, k)
+                       : dir == 1 ? d.idx(i, wrapp(j + 1, d.ny), k)
+                                  : d.idx(i, j, wrapp(k + 1, d.nz));
+      const int fc = fcuu[c];
+      const double v0 = vflux[c], v1 = vflux[fp], f0 = ffvu[c], f1 = ffvu[fp];
+      const long long ub = Bits(u[c]);
+      const long long a0 = Bits(v0), a1 = Bits(v1), b0 = Bits(f0), b1 = Bits(f1);
+      // magnitudes below 2^(emax-1023): every difference times dt / vol
+      // below is finite
+      const bool fin =
+          ExpBits(a0) < emax && ExpBits(a1) < emax && ExpBits(b0) < emax && ExpBits(b1) < emax;
+      // bulk cells, no FP64 instruction: empty (u = +0, fcuu = 0, zero
+      // fluid fluxes: u + (0*ds - dl) is +0 and stays +0 when clipped) and
+      // full (u = 1, fcuu = 1, fluid fluxes equal to the face fluxes:
+      // ds - dl = +0, u stays 1 for clipth <= 1); u is unchanged
+      const bool bulk =
+          fin && ((ub == 0 && fc == 0 && ((b0 | b1) << 1) == 0) ||
+                  (full_ok && ub == kOneBits && fc == 1 && a0 == b0 && a1 == b1));
+      if (!bulk) {
+        const double dsn = (v1 - v0) * dt;
+        const double dln = (f1 - f0) * dt;
+        const double dl = dln == 0 ? dln : dln / vol;
+        double t;
+        if (fc == 0 && fabs(dsn) <= big) {
+          t = copysign(0.0, dsn) - dl;
+        } else if (fc == 1 && fabs(dsn) <= big && Bits(dsn) == Bits(dln)) {
+          t = 0.0;
+        } else {
+          t = (double)fc * (dsn / vol) - dl;
+        }
+        double w = __longlong_as_double(ub);
+        w += t;
+        if (!(w >= clipth)) {
+          w = 0;
+        } else if (!(w <= 1 - clipth)) {
+          w = 1;
+        }
+        u[c] = w;
+        want = InterfaceBits(Bits(w));
+      }
+    }
+    ListAppend(want, (int)c, list, count);
   }
 }
 
@@ -491,40 +632,113 @@ __global__ void KSurfaceTension(Dims d, double h, double sigma,
 
 }  // namespace
 
-int VofReconstruct(aphgpu_ctx* ctx) {
-  const double h = ctx->h;
-  KReconstruct<<<TileGrid(ctx->d), TileBlock(), 0, ctx->stream>>>(
-      ctx->d, h, h, h, ctx->u, ctx->nrm, ctx->pa);
+namespace {
+
+// Scratch of a VOF step inside the context's u0 array (8 bytes per cell):
+// fcuu (1 byte per cell), then the interface list (4 bytes per cell, room
+// for every cell) and its length.
+struct VofScratch {
+  uint8_t* fcuu;
+  int* list;
+  int* count;
+};
+
+VofScratch Scratch(aphgpu_ctx* ctx) {
+  char* base = (char*)ctx->u0;
+  const size_t off = ((size_t)ctx->N + 15) & ~(size_t)15;
+  return VofScratch{(uint8_t*)base, (int*)(base + off), (int*)(base + off + 4 * ctx->N)};
+}
+
+// grid of the list kernels: 4 CTAs of 256 threads per SM, looping over the
+// list
+int ListGrid(aphgpu_ctx* ctx) {
+  int sms = 0;
+  if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, ctx->device) != cudaSuccess ||
+      sms < 1) {
+    cudaGetLastError();
+    sms = 132;
+  }
+  return 4 * sms;
+}
+
+// interface list (and fcuu when `fcuu`) of the current volume fraction
+int ListInterface(aphgpu_ctx* ctx, const VofScratch& sc, bool fcuu) {
+  APH_CUDA(ctx, cudaMemsetAsync(sc.count, 0, sizeof(int), ctx->stream));
+  KListInterface<<<TileGrid(ctx->d), TileBlock(), 0, ctx->stream>>>(
+      ctx->d, ctx->u, fcuu ? sc.fcuu : nullptr, sc.list, sc.count);
   APH_LAUNCHED(ctx);
   return APHGPU_OK;
 }
 
-int VofStepDevice(aphgpu_ctx* ctx, const double* d_vflux, double dt) {
+int ReconstructListed(aphgpu_ctx* ctx, const VofScratch& sc) {
   const double h = ctx->h;
-  const Dims d = ctx->d;
-  const int64_t N = ctx->N;
-  cudaStream_t st = ctx->stream;
-  uint8_t* fcuu = (uint8_t*)ctx->u0;  // byte view of the scratch array
-  KFcuu<<<FlatBlocks(N), kFlatThreads, 0, st>>>(N, ctx->u, fcuu);
+  KReconstructList<<<ListGrid(ctx), 256, 0, ctx->stream>>>(ctx->d, h, h, h, ctx->u, ctx->nrm,
+                                                            ctx->pa, sc.list, sc.count);
   APH_LAUNCHED(ctx);
+  return APHGPU_OK;
+}
+
+int SweepFlux(aphgpu_ctx* ctx, const VofScratch& sc, int dir, const double* vf, double dt) {
+  const double h = ctx->h;
+  KSweepFlux<<<TileGrid(ctx->d), TileBlock(), 0, ctx->stream>>>(ctx->d, dir, ctx->u, vf,
+                                                                 ctx->ffvu);
+  APH_LAUNCHED(ctx);
+  KSweepFluxList<<<ListGrid(ctx), 256, 0, ctx->stream>>>(ctx->d, dir, h, h, h, ctx->u, vf,
+                                                          ctx->nrm, ctx->pa, dt, ctx->ffvu,
+                                                          sc.list, sc.count);
+  APH_LAUNCHED(ctx);
+  return APHGPU_OK;
+}
+
+int SweepUpdate(aphgpu_ctx* ctx, const VofScratch& sc, int dir, const double* vf, double dt) {
+  const double h = ctx->h;
+  APH_CUDA(ctx, cudaMemsetAsync(sc.count, 0, sizeof(int), ctx->stream));
+  const double vol = (h * h) * h;
+  // face values of magnitude below 2^(emax-1023) keep the differences
+  // (below 2^(emax-1022)), their products with dt and the quotients by vol
+  // below 2^1000: finite on the bulk path
+  const double adt = std::fabs(dt);
+  const double ratio = adt / vol;
+  int emax = 0;
+  if (std::isfinite(ratio) && std::isfinite(adt)) {
+    double e = 2045.0;
+    if (ratio > 0) e = std::min(e, std::floor(2021.0 - std::log2(ratio)));
+    if (adt > 1) e = std::min(e, std::floor(2021.0 - std::log2(adt)));
+    emax = (int)std::max(0.0, e);
+  }
+  KSweepUpdate<<<TileGrid(ctx->d), TileBlock(), 0, ctx->stream>>>(
+      ctx->d, dir, vol, ctx->u, vf, ctx->ffvu, sc.fcuu, dt, ctx->clipth, emax,
+      ctx->clipth <= 1 ? 1 : 0, sc.list, sc.count);
+  APH_LAUNCHED(ctx);
+  return APHGPU_OK;
+}
+
+}  // namespace
+
+int VofReconstruct(aphgpu_ctx* ctx) {
+  const VofScratch sc = Scratch(ctx);
+  APH_TRY(ListInterface(ctx, sc, false));
+  return ReconstructListed(ctx, sc);
+}
+
+int VofStepDevice(aphgpu_ctx* ctx, const double* d_vflux, double dt) {
+  const int64_t N = ctx->N;
+  const VofScratch sc = Scratch(ctx);
+  APH_TRY(ListInterface(ctx, sc, true));
   int dd[3];
   const int cnt = ctx->vof_count % 3;  // vof.ipp:428-435
   if (cnt == 0) { dd[0] = 0; dd[1] = 1; dd[2] = 2; }
   else if (cnt == 1) { dd[0] = 1; dd[1] = 2; dd[2] = 0; }
   else { dd[0] = 2; dd[1] = 0; dd[2] = 1; }
-  const double vol = (h * h) * h;
   for (int id = 0; id < 3; ++id) {
     const int dir = dd[id];
     const double* vf = d_vflux + (int64_t)dir * N;
-    KSweepFlux<<<TileGrid(d), TileBlock(), 0, st>>>(d, dir, h, h, h, ctx->u, vf,
-                                                    ctx->nrm, ctx->pa, dt, ctx->ffvu);
-    APH_LAUNCHED(ctx);
-    KSweepUpdate<<<TileGrid(d), TileBlock(), 0, st>>>(d, dir, vol, ctx->u, vf,
-                                                      ctx->ffvu, fcuu, dt, ctx->clipth);
-    APH_LAUNCHED(ctx);
-    APH_TRY(VofReconstruct(ctx));
+    APH_TRY(SweepFlux(ctx, sc, dir, vf, dt));
+    APH_TRY(SweepUpdate(ctx, sc, dir, vf, dt));
+    APH_TRY(ReconstructListed(ctx, sc));
   }
   ctx->vof_count += 1;
+  ctx->vof_dt = dt;
   return APHGPU_OK;
 }
 
@@ -545,21 +759,32 @@ int TimeVofKernel(aphgpu_ctx* ctx, int kernel, int reps, double* ms, double* byt
   const Dims d = ctx->d;
   const double N = (double)ctx->N;
   cudaStream_t st = ctx->stream;
-  uint8_t* fcuu = (uint8_t*)ctx->u0;
+  const VofScratch sc = Scratch(ctx);
+  // the interface list and fcuu of the current volume fraction
+  APH_TRY(ListInterface(ctx, sc, true));
+  int nif = 0;
+  APH_CUDA(ctx, cudaMemcpyAsync(&nif, sc.count, sizeof(int), cudaMemcpyDeviceToHost, st));
+  APH_CUDA(ctx, cudaStreamSynchronize(st));
   double b = 0;
-  auto launch = [&]() {
+  switch (kernel) {
+    // bulk faces: u (upwind), flux, ffvu; interfacial cells: index, normal,
+    // plane constant, u, two faces each way
+    case APHGPU_K_VOF_FLUX: b = N * (8 + 8 + 8) + nif * (4.0 + 24 + 8 + 8 + 32); break;
+    // u r/w, flux, ffvu, fcuu, list entries
+    case APHGPU_K_VOF_UPDATE: b = N * (8 + 8 + 8 + 8 + 1) + nif * 4.0; break;
+    // listed cells: index, u, normal and plane constant written
+    case APHGPU_K_RECONSTRUCT: b = nif * (4.0 + 8 + 24 + 8); break;
+    case APHGPU_K_HEIGHTS: b = N * 8; break;
+    case APHGPU_K_CURVATURE: b = N * (8 + 8); break;  // u, kappa
+    default: return SetError(ctx, APHGPU_ERR_ARG, "unknown kernel %d", kernel);
+  }
+  // flux and update of the x direction with the last step's time step: the
+  // update advances u again (state left modified)
+  auto launch = [&]() -> int {
     switch (kernel) {
-      case APHGPU_K_VOF_FLUX:
-        KSweepFlux<<<TileGrid(d), TileBlock(), 0, st>>>(d, 0, h, h, h, ctx->u, d_vflux,
-                                                        ctx->nrm, ctx->pa, dt, ctx->ffvu);
-        break;
-      case APHGPU_K_VOF_UPDATE:
-        KSweepUpdate<<<TileGrid(d), TileBlock(), 0, st>>>(d, 0, h * h * h, ctx->u, d_vflux,
-                                                          ctx->ffvu, fcuu, 0.0, ctx->clipth);
-        break;
-      case APHGPU_K_RECONSTRUCT:
-        KReconstruct<<<TileGrid(d), TileBlock(), 0, st>>>(d, h, h, h, ctx->u, ctx->nrm, ctx->pa);
-        break;
+      case APHGPU_K_VOF_FLUX: return SweepFlux(ctx, sc, 0, d_vflux, dt);
+      case APHGPU_K_VOF_UPDATE: return SweepUpdate(ctx, sc, 0, d_vflux, dt);
+      case APHGPU_K_RECONSTRUCT: return ReconstructListed(ctx, sc);
       case APHGPU_K_HEIGHTS:
         KHeights<<<TileGrid(d), TileBlock(), 0, st>>>(d, h, h, h, ctx->u, ctx->hgt);
         break;
@@ -568,20 +793,12 @@ int TimeVofKernel(aphgpu_ctx* ctx, int kernel, int reps, double* ms, double* byt
                                                         ctx->hgt, ctx->kappa);
         break;
     }
+    APH_LAUNCHED(ctx);
+    return APHGPU_OK;
   };
-  switch (kernel) {
-    case APHGPU_K_VOF_FLUX: b = N * (8 + 8 + 8); break;          // u, flux, ffvu
-    case APHGPU_K_VOF_UPDATE: b = N * (8 + 8 + 8 + 1 + 8); break;  // u r/w, flux, ffvu, fcuu
-    case APHGPU_K_RECONSTRUCT: b = N * 8; break;                  // u (+ interface cells)
-    case APHGPU_K_HEIGHTS: b = N * 8; break;
-    case APHGPU_K_CURVATURE: b = N * (8 + 8); break;              // u, kappa
-    default: return SetError(ctx, APHGPU_ERR_ARG, "unknown kernel %d", kernel);
-  }
-  launch();
-  APH_LAUNCHED(ctx);
+  APH_TRY(launch());
   APH_CUDA(ctx, cudaEventRecord(ctx->ev0, st));
-  for (int r = 0; r < reps; ++r) launch();
-  APH_LAUNCHED(ctx);
+  for (int r = 0; r < reps; ++r) APH_TRY(launch());
   APH_CUDA(ctx, cudaEventRecord(ctx->ev1, st));
   APH_CUDA(ctx, cudaEventSynchronize(ctx->ev1));
   float t = 0;
