@@ -19,13 +19,16 @@ ERR_NOT_SYMMETRIC = 4
 ERR_STATE = 5
 ERR_UNSUPPORTED = 6
 ERR_TIMEOUT = 7
+OPT_GRAPHS = 0
+OPT_FUSED_SWEEPS = 1
 
 K_SMOOTH32, K_SMOOTH64, K_APPLY64, K_APPLY32, K_RESTRICT32 = 0, 1, 2, 3, 4
 K_VOF_FLUX, K_VOF_UPDATE, K_RECONSTRUCT, K_HEIGHTS, K_CURVATURE = 5, 6, 7, 8, 9
+K_SWEEP32 = 10
 KERNEL_NAMES = {0: "KSmooth<float>", 1: "KSmooth<double>", 2: "KPcgApply<double>",
                 3: "KPcgApply<float>", 4: "KResidualRestrict<float>",
                 5: "KSweepFlux", 6: "KSweepUpdate", 7: "KReconstruct",
-                8: "KHeights", 9: "KCurvature"}
+                8: "KHeights", 9: "KCurvature", 10: "KSweepRB4"}
 
 SOLVER_CG = 0
 SOLVER_MGPCG = 1
@@ -100,6 +103,8 @@ def lib():
     L.aphgpu_set_force_resident.argtypes = [_P, _I]
     L.aphgpu_last_timing.argtypes = [_P, _PD, ctypes.POINTER(ctypes.c_int64)]
     L.aphgpu_mark.argtypes = [_P, _I]
+    L.aphgpu_set_option.argtypes = [_P, _I, _I]
+    L.aphgpu_set_option.restype = _I
     L.aphgpu_residual_history.argtypes = [_P, _I, _P, _I, ctypes.POINTER(_I)]
     L.aphgpu_residual_history.restype = _I
     L.aphgpu_elapsed.argtypes = [_P, _I, _I, _PD]
@@ -295,6 +300,10 @@ class Context:
         self._check(self._L.aphgpu_residual_history(self._p, which, ptr(out), n.value,
                                                     ctypes.byref(n)))
         return out
+
+    def set_option(self, option, value):
+        """OPT_GRAPHS / OPT_FUSED_SWEEPS (aphgpu_set_option)."""
+        self._check(self._L.aphgpu_set_option(self._p, option, int(value)))
 
     def mark(self, slot):
         self._check(self._L.aphgpu_mark(self._p, slot))

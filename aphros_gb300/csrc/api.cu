@@ -539,6 +539,15 @@ int aphgpu_set_force_resident(aphgpu_ctx* ctx, int on) {
   return APHGPU_OK;
 }
 
+int aphgpu_set_option(aphgpu_ctx* ctx, int option, int value) {
+  if (!Valid(ctx)) return APHGPU_ERR_ARG;
+  switch (option) {
+    case APHGPU_OPT_GRAPHS: ctx->use_graphs = value != 0; return APHGPU_OK;
+    case APHGPU_OPT_FUSED_SWEEPS: ctx->use_fused = value != 0; return APHGPU_OK;
+    default: return SetError(ctx, APHGPU_ERR_ARG, "unknown option %d", option);
+  }
+}
+
 int aphgpu_mark(aphgpu_ctx* ctx, int slot) {
   if (!Valid(ctx) || slot < 0 || slot >= 8) return APHGPU_ERR_ARG;
   APH_TRY(SetDevice(ctx));
@@ -560,7 +569,7 @@ int aphgpu_elapsed(aphgpu_ctx* ctx, int s0, int s1, double* ms) {
 int aphgpu_time_kernel(aphgpu_ctx* ctx, int kernel, int reps, double* ms, double* bytes) {
   if (!Valid(ctx) || !ms || !bytes || reps < 1) return APHGPU_ERR_ARG;
   APH_TRY(SetDevice(ctx));
-  if (kernel >= APHGPU_K_VOF_FLUX) {
+  if (kernel >= APHGPU_K_VOF_FLUX && kernel <= APHGPU_K_CURVATURE) {
     if (!ctx->vof_ready) return SetError(ctx, APHGPU_ERR_STATE, "vof not initialised");
     double* d_vf = nullptr;
     APH_TRY(FaceScratch(ctx, &d_vf));

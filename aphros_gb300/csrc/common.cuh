@@ -311,6 +311,7 @@ struct aphgpu_ctx {
   } graphs[4];
   int64_t mg_epoch = 0;        // bumped whenever a hierarchy is (re)allocated
   bool use_graphs = true;
+  bool use_fused = false;  // fused out-of-place red-black sweeps (FP32 levels)
 
   // timing
   cudaEvent_t ev0 = nullptr, ev1 = nullptr;

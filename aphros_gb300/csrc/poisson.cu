@@ -449,6 +449,26 @@ __global__ void __launch_bounds__(256, 4) KSmooth4(Op<float> A, const float* __r
               blockIdx.y * 8 + threadIdx.y, kb, min(kb + kz, A.d.nz));
 }
 
+// One red-black sweep, both colours fused, out of place (SweepRB4Tile):
+// c0 the first colour, zero_init the zero initial guess of the first colour.
+__global__ void __launch_bounds__(256, 3) KSweepRB4(Op<float> A, const float* __restrict__ b,
+                                                   const float* xin, float* xout, int c0,
+                                                   int zero_init, const SolveScalars* s, int kz) {
+  if (s && s->done) return;
+  __shared__ SweepPlanes sF;
+  const int kb = blockIdx.z * kz;
+  SweepRB4Tile(A, b, xin, xout, c0, zero_init, blockIdx.x, blockIdx.y, kb,
+               min(kb + kz, A.d.nz), sF);
+}
+
+// levels the fused sweep handles
+inline bool FusedOk(const Dims& d) { return VecOk(d); }
+inline dim3 SweepGrid(const Dims& d) {
+  const int nq = d.nx / 4;
+  const int kz = VecZ(d);
+  return dim3((nq + 31) / 32, (d.ny + kSweepRows - 1) / kSweepRows, (d.nz + kz - 1) / kz);
+}
+
 // y = A p (FP32, vectorized) with the reductions p.y and sum y of KPcgApply
 __global__ void __launch_bounds__(256, 4) KPcgApply4(Op<float> A, const float* __restrict__ p,
                                                   float* ap, SolveScalars* s, RedBuf rb, int kz) {
@@ -1113,6 +1133,8 @@ int BuildHierarchy<float>(aphgpu_ctx* ctx, std::vector<Level<float>>& lv,
     for (size_t l = 0; l < dims.size(); ++l) {
       lv[l].d = dims[l];
       APH_TRY(AllocLevel(ctx, lv[l], true, l > 0));
+      // scratch of the out-of-place fused sweeps (when enabled)
+      if (ctx->use_fused && FusedOk(dims[l])) APH_TRY(Alloc(ctx, &lv[l].r, dims[l].cells()));
       lv[l].has_diag = true;
     }
   }
@@ -1175,6 +1197,40 @@ void LaunchSmooth<float>(aphgpu_ctx* ctx, const Level<float>& f, const Op<float>
                                                                    color, zero_init, s);
   }
 }
+// n red-black sweeps on level f (first colour c0; zero_first: the first
+// sweep starts from a zero guess) with the fused out-of-place kernel,
+// alternating between f.x and the level's scratch f.r so that the result
+// ends in f.x.  Returns kNotFused (nothing launched) where the level or the
+// context does not allow it, else APHGPU_OK or the launch error.
+constexpr int kNotFused = -1;
+template <class T>
+int FusedSweeps(aphgpu_ctx*, Level<T>&, const Op<T>&, int, int, bool, const SolveScalars*) {
+  return kNotFused;
+}
+template <>
+int FusedSweeps<float>(aphgpu_ctx* ctx, Level<float>& f, const Op<float>& A, int n, int c0,
+                       bool zero_first, const SolveScalars* s) {
+  if (!ctx->use_fused || n < 1 || !f.r || !FusedOk(f.d)) return kNotFused;
+  const dim3 g = SweepGrid(f.d);
+  const int kz = VecZ(f.d);
+  float* in = f.x;
+  // outputs: the last sweep writes f.x; a zero-guess first sweep reads
+  // nothing, so it may write f.x too
+  for (int k = 0; k < n; ++k) {
+    const bool last_to_x = ((n - 1 - k) % 2) == 0;
+    float* out = last_to_x ? f.x : f.r;
+    if (out == in && !(k == 0 && zero_first)) out = f.r;  // never in place
+    KSweepRB4<<<g, TileBlock(), 0, ctx->stream>>>(A, f.b, in, out, c0, (k == 0 && zero_first),
+                                                  s, kz);
+    APH_LAUNCHED(ctx);
+    in = out;
+  }
+  if (in != f.x)
+    APH_CUDA(ctx, cudaMemcpyAsync(f.x, in, sizeof(float) * f.d.cells(),
+                                  cudaMemcpyDeviceToDevice, ctx->stream));
+  return APHGPU_OK;
+}
+
 template <class T>
 void LaunchProlong(aphgpu_ctx* ctx, const Level<T>& f, const Level<T>& c,
                    const SolveScalars* s) {
@@ -1280,7 +1336,9 @@ int VCycle(aphgpu_ctx* ctx, std::vector<Level<T>>& lv, int pre, int post,
   for (int l = 0; l < L - 1; ++l) {
     Level<T>& f = lv[l];
     const Op<T> A = MakeOp(f);
-    for (int sw = 0; sw < pre; ++sw) {
+    const int fused = pre > 0 ? FusedSweeps<T>(ctx, f, A, pre, 0, true, s) : kNotFused;
+    if (fused != kNotFused) APH_TRY(fused);
+    for (int sw = 0; fused == kNotFused && sw < pre; ++sw) {
       LaunchSmooth<T>(ctx, f, A, 0, sw == 0, s);
       APH_LAUNCHED(ctx);
       LaunchSmooth<T>(ctx, f, A, 1, 0, s);
@@ -1316,7 +1374,9 @@ int VCycle(aphgpu_ctx* ctx, std::vector<Level<T>>& lv, int pre, int post,
     const Op<T> A = MakeOp(f);
     LaunchProlong<T>(ctx, f, c, s);
     APH_LAUNCHED(ctx);
-    for (int sw = 0; sw < post; ++sw) {
+    const int fused = post > 0 ? FusedSweeps<T>(ctx, f, A, post, 1, false, s) : kNotFused;
+    if (fused != kNotFused) APH_TRY(fused);
+    for (int sw = 0; fused == kNotFused && sw < post; ++sw) {
       LaunchSmooth<T>(ctx, f, A, 1, 0, s);
       APH_LAUNCHED(ctx);
       LaunchSmooth<T>(ctx, f, A, 0, 0, s);
@@ -1387,6 +1447,7 @@ int Pcg(aphgpu_ctx* ctx, const Op<T>& A, Precond precond, T* x, T* r, T* p,
     key = Mix(key, (uint64_t)(conf->mg_pre * 1000 + conf->mg_post));
     key = Mix(key, (uint64_t)check_every);
     key = Mix(key, (uint64_t)sizeof(T));
+    key = Mix(key, (uint64_t)(ctx->use_fused ? 1 : 0));
     if (g.exec && g.key == key) {
       exec = g.exec;
       graph_kernels = g.kernels;
@@ -1729,6 +1790,23 @@ int TimeSolverKernel(aphgpu_ctx* ctx, int kernel, int reps, double* ms,
       launch = [=]() { LaunchSmooth<float>(ctx, fl, A, 0, 0, nullptr); };
       // x read 4 + couplings 12 + half of (b 4, invdiag 4, x write 4)
       b = N * (4 + 12 + 0.5 * 12);
+      break;
+    }
+    case APHGPU_K_SWEEP32: {
+      if (!mg.built32 || !ctx->r32 || !mg.l32[0].r)
+        return SetError(ctx, APHGPU_ERR_STATE, "run a mixed solve first (fused level)");
+      Level<float>& f = mg.l32[0];
+      const Op<float> A = MakeOp(f);
+      const float* bb = ctx->r32;
+      const float* x = ctx->z32;
+      float* xo = f.r;
+      const dim3 g = SweepGrid(d);
+      const int kz = VecZ(d);
+      launch = [=]() {
+        KSweepRB4<<<g, TileBlock(), 0, st>>>(A, bb, x, xo, 0, 0, nullptr, kz);
+      };
+      // couplings 12, b 4, x read 4, x written 4 (once each per full sweep)
+      b = N * 24;
       break;
     }
     case APHGPU_K_SMOOTH64: {

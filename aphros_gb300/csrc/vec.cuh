@@ -256,4 +256,248 @@ __device__ __forceinline__ void ResidualRestrict4Body(const Op<float>& A,
   }
 }
 
+// ---------------------------------------------------------------------------
+// Fused red-black Gauss-Seidel sweep, out of place: both colours in one pass
+// over the level, so the couplings and the right-hand side are read once
+// per sweep instead of once per half sweep.
+//
+// The CTA owns a tile of ncol <= 128 cells (32 float4 lanes) x nrow <= 29
+// rows and marches over the planes [kb, ke); its 8 warps take the rows (and
+// the two halo rows) in turn.  At plane step m it computes the first
+// colour c0 of plane m+1 from x_in (old second-colour values) on its rows,
+// on one halo row and one halo column on either side, into a ring of three
+// planes in shared memory; then the second colour of plane m from the new
+// first-colour values of planes m-1, m, m+1, and writes both colours of
+// plane m to x_out.  Halo values are recomputed, not exchanged, and x_in is
+// only read, so CTAs never race.  Every value is computed by the same
+// operations as the two in-place half sweeps of Smooth4Body.
+// Requires nx % 4 == 0, nx >= 8; x_out != x_in.
+// ---------------------------------------------------------------------------
+
+constexpr int kSweepRows = 29;  // interior rows of a tile (31 with the halos)
+constexpr int kSweepCols = 128 + 2;
+typedef float SweepPlanes[3][kSweepRows + 2][kSweepCols];
+
+// Row-segment edges with the loads issued before the shuffles (no second
+// round trip to memory): l / r take the neighbours of the float4 from the
+// adjacent lanes, or at segment and domain edges from the row in memory.
+__device__ __forceinline__ void XEdges(const float* row, int q, int nq, bool act, float& el,
+                                       float& er) {
+  const int sl = threadIdx.x & 31;
+  el = 0.f;
+  er = 0.f;
+  if (act && (sl == 0 || q == 0)) el = row[q == 0 ? 4 * nq - 1 : 4 * q - 1];
+  if (act && (sl == 31 || q == nq - 1)) er = row[q == nq - 1 ? 0 : 4 * q + 4];
+}
+__device__ __forceinline__ void XHaloPre(float4 v, int q, int nq, bool act, float el, float er,
+                                         float& l, float& r) {
+  const int sl = threadIdx.x & 31;
+  l = __shfl_up_sync(0xffffffffu, v.w, 1);
+  r = __shfl_down_sync(0xffffffffu, v.x, 1);
+  if (act && (sl == 0 || q == 0)) l = el;
+  if (act && (sl == 31 || q == nq - 1)) r = er;
+}
+
+// First colour of the float4 at column q, row j, plane p (other positions
+// 0); every lane of the warp must call it.  All loads are issued first.
+__device__ __forceinline__ float4 FirstColor4(const Op<float>& A, const float* __restrict__ b,
+                                              const float* __restrict__ xin, int c0,
+                                              int zero_init, int q, int j, int p, bool act) {
+  const Dims d = A.d;
+  const int nq = d.nx >> 2;
+  const int i0 = 4 * q;
+  const int jm = wrapm(j - 1, d.ny), jp = wrapp(j + 1, d.ny);
+  const int pm = wrapm(p - 1, d.nz), pp = wrapp(p + 1, d.nz);
+  const int64_t c = d.idx(i0, act ? j : 0, p);
+  const float4 z4 = make_float4(0, 0, 0, 0);
+  float4 xc = z4, w0v = z4, w1v = z4, w1n = z4, wz1 = z4, wz2 = z4, bv = z4;
+  float4 xjm = z4, xjp = z4, xz0 = z4, xz2 = z4;
+  float xel = 0.f, xer = 0.f, wel = 0.f, wer = 0.f;
+  const int64_t row = d.idx(0, act ? j : 0, p);
+  if (act) {
+    w0v = Ld4(A.w0 + c);
+    w1v = Ld4(A.w1 + c);
+    w1n = Ld4(A.w1 + d.idx(i0, jp, p));
+    wz1 = Ld4(A.w2 + c);
+    wz2 = Ld4(A.w2 + d.idx(i0, j, pp));
+    bv = Ld4(b + c);
+    if (!zero_init) {
+      xc = Ld4(xin + c);
+      xjm = Ld4(xin + d.idx(i0, jm, p));
+      xjp = Ld4(xin + d.idx(i0, jp, p));
+      xz0 = Ld4(xin + d.idx(i0, j, pm));
+      xz2 = Ld4(xin + d.idx(i0, j, pp));
+    }
+  }
+  XEdges(A.w0 + row, q, nq, act, wel, wer);
+  if (!zero_init) XEdges(xin + row, q, nq, act, xel, xer);
+  float xl, xr, wl, wr;
+  XHaloPre(xc, q, nq, act && !zero_init, xel, xer, xl, xr);
+  XHaloPre(w0v, q, nq, act, wel, wer, wl, wr);
+  (void)wl;
+  float4 out = z4;
+  if (act) {
+    const int e0 = (c0 + j + p) & 1;
+#pragma unroll
+    for (int e = 0; e < 4; ++e) {
+      if ((e & 1) != e0) continue;
+      const float cxm = El(w0v, e);
+      const float cxp = e == 3 ? wr : El(w0v, e + 1);
+      const float cym = El(w1v, e), cyp = El(w1n, e);
+      const float czm = El(wz1, e), czp = El(wz2, e);
+      const float dg = A.diag ? A.diag[c + e]
+                              : -(((((cxm + cxp) + cym) + cyp) + czm) + czp);
+      float acc = El(bv, e);
+      if (!zero_init) {
+        const float vxm = e == 0 ? xl : El(xc, e - 1);
+        const float vxp = e == 3 ? xr : El(xc, e + 1);
+        acc -= cxm * vxm;
+        acc -= cxp * vxp;
+        acc -= cym * El(xjm, e);
+        acc -= cyp * El(xjp, e);
+        acc -= czm * El(xz0, e);
+        acc -= czp * El(xz2, e);
+      }
+      SetEl(out, e, acc / dg);
+    }
+  }
+  return out;
+}
+
+// First colour of the single cell (i, j, p), 0 for the second colour.
+__device__ __forceinline__ float FirstColor1(const Op<float>& A, const float* __restrict__ b,
+                                             const float* __restrict__ xin, int c0,
+                                             int zero_init, int i, int j, int p) {
+  if (((i + j + p) & 1) != c0) return 0.f;
+  const Dims d = A.d;
+  const int im = wrapm(i - 1, d.nx), ip = wrapp(i + 1, d.nx);
+  const int jm = wrapm(j - 1, d.ny), jp = wrapp(j + 1, d.ny);
+  const int pm = wrapm(p - 1, d.nz), pp = wrapp(p + 1, d.nz);
+  const int64_t c = d.idx(i, j, p);
+  const float cxm = A.w0[c], cxp = A.w0[d.idx(ip, j, p)];
+  const float cym = A.w1[c], cyp = A.w1[d.idx(i, jp, p)];
+  const float czm = A.w2[c], czp = A.w2[d.idx(i, j, pp)];
+  const float dg = A.diag ? A.diag[c] : -(((((cxm + cxp) + cym) + cyp) + czm) + czp);
+  float acc = b[c];
+  if (!zero_init) {
+    acc -= cxm * xin[d.idx(im, j, p)];
+    acc -= cxp * xin[d.idx(ip, j, p)];
+    acc -= cym * xin[d.idx(i, jm, p)];
+    acc -= cyp * xin[d.idx(i, jp, p)];
+    acc -= czm * xin[d.idx(i, j, pm)];
+    acc -= czp * xin[d.idx(i, j, pp)];
+  }
+  return acc / dg;
+}
+
+// First colour of plane p (unwrapped, kb-1 <= p <= ke) of the tile into
+// plane buffer P: rows -1..nrow and columns -1..ncol (shared index +1).
+__device__ __forceinline__ void SweepFirstPlane(const Op<float>& A, const float* __restrict__ b,
+                                                const float* __restrict__ xin, int c0,
+                                                int zero_init, int bx, int j0, int nrow,
+                                                int p, float (*P)[kSweepCols]) {
+  const Dims d = A.d;
+  const int nq = d.nx >> 2;
+  const int pw = p < 0 ? p + d.nz : (p >= d.nz ? p - d.nz : p);
+  const int lane = threadIdx.x;
+  const int q = bx * 32 + lane;
+  const bool act = q < nq;
+  const int i0 = bx * 128;
+  const int ncol = min(128, d.nx - i0);
+  // halo columns of rows -1..nrow first: one scalar cell per thread, all
+  // loads in flight together
+  const int tid = lane + 32 * threadIdx.y;
+  if (tid < 2 * (nrow + 2)) {
+    const int t = tid >> 1, side = tid & 1;
+    const int r = t - 1;
+    const int j = r < 0 ? wrapm(j0 - 1, d.ny) : wrapp(j0 + r, d.ny);
+    const int ih = side ? wrapp(i0 + ncol, d.nx) : wrapm(i0 - 1, d.nx);
+    P[t][side ? ncol + 1 : 0] = FirstColor1(A, b, xin, c0, zero_init, ih, j, pw);
+  }
+  for (int t = threadIdx.y; t < nrow + 2; t += blockDim.y) {
+    const int r = t - 1;
+    const int j = r < 0 ? wrapm(j0 - 1, d.ny) : wrapp(j0 + r, d.ny);
+    const float4 v = FirstColor4(A, b, xin, c0, zero_init, q, j, pw, act);
+    if (act) {
+      P[t][4 * lane + 1] = v.x;
+      P[t][4 * lane + 2] = v.y;
+      P[t][4 * lane + 3] = v.z;
+      P[t][4 * lane + 4] = v.w;
+    }
+  }
+}
+
+// One fused sweep over the planes [kb, ke) of tile (bx, by); every thread of
+// the 32 x 8 CTA must call it (barriers inside).
+__device__ __forceinline__ void SweepRB4Tile(const Op<float>& A, const float* __restrict__ b,
+                                             const float* __restrict__ xin, float* xout,
+                                             int c0, int zero_init, int bx, int by, int kb,
+                                             int ke, SweepPlanes& sF) {
+  const Dims d = A.d;
+  const int nq = d.nx >> 2;
+  const int j0 = by * kSweepRows;
+  const int nrow = min(kSweepRows, d.ny - j0);
+  const int lane = threadIdx.x;
+  const int q = bx * 32 + lane;
+  const bool act = q < nq;
+  SweepFirstPlane(A, b, xin, c0, zero_init, bx, j0, nrow, kb - 1, sF[0]);
+  SweepFirstPlane(A, b, xin, c0, zero_init, bx, j0, nrow, kb, sF[1]);
+  __syncthreads();
+  for (int m = kb; m < ke; ++m) {
+    const int sm = (m - kb) % 3, s0 = (m - kb + 1) % 3, sp = (m - kb + 2) % 3;
+    SweepFirstPlane(A, b, xin, c0, zero_init, bx, j0, nrow, m + 1, sF[sp]);
+    __syncthreads();
+    // second colour of plane m from the new first-colour values
+    const int pp = wrapp(m + 1, d.nz);
+    for (int rr = threadIdx.y; rr < nrow; rr += blockDim.y) {
+      const int j = j0 + rr;
+      const int jp = wrapp(j + 1, d.ny);
+      const int64_t c = d.idx(4 * q, j, m);
+      const float4 z4 = make_float4(0, 0, 0, 0);
+      float4 w0v = z4, w1v = z4, w1n = z4, wz1 = z4, wz2 = z4, bv = z4;
+      if (act) {
+        w0v = Ld4(A.w0 + c);
+        w1v = Ld4(A.w1 + c);
+        w1n = Ld4(A.w1 + d.idx(4 * q, jp, m));
+        wz1 = Ld4(A.w2 + c);
+        wz2 = Ld4(A.w2 + d.idx(4 * q, j, pp));
+        bv = Ld4(b + c);
+      }
+      float wel, wer, wl, wr;
+      XEdges(A.w0 + d.idx(0, j, m), q, nq, act, wel, wer);
+      XHaloPre(w0v, q, nq, act, wel, wer, wl, wr);
+      (void)wl;
+      if (act) {
+        float4 out;
+        const int e0 = (c0 + j + m) & 1;  // first-colour positions
+        const int r = rr + 1;
+#pragma unroll
+        for (int e = 0; e < 4; ++e) {
+          const int lc = 4 * lane + e + 1;
+          if ((e & 1) == e0) {
+            SetEl(out, e, sF[s0][r][lc]);
+            continue;
+          }
+          const float cxm = El(w0v, e);
+          const float cxp = e == 3 ? wr : El(w0v, e + 1);
+          const float cym = El(w1v, e), cyp = El(w1n, e);
+          const float czm = El(wz1, e), czp = El(wz2, e);
+          const float dg = A.diag ? A.diag[c + e]
+                                  : -(((((cxm + cxp) + cym) + cyp) + czm) + czp);
+          float acc = El(bv, e);
+          acc -= cxm * sF[s0][r][lc - 1];
+          acc -= cxp * sF[s0][r][lc + 1];
+          acc -= cym * sF[s0][r - 1][lc];
+          acc -= cyp * sF[s0][r + 1][lc];
+          acc -= czm * sF[sm][r][lc];
+          acc -= czp * sF[sp][r][lc];
+          SetEl(out, e, acc / dg);
+        }
+        St4(xout + c, out);
+      }
+    }
+    __syncthreads();
+  }
+}
+
 }  // namespace aphgpu

@@ -350,6 +350,19 @@ int aphgpu_batch_last_ms(const aphgpu_batch* batch, double* ms, int64_t* launche
 /* Records event `slot` (0..7) on the context's stream; aphgpu_elapsed
  * returns the milliseconds between two recorded slots (waits for the
  * second). */
+/* Execution options of a context (results do not depend on them; they
+ * exist to measure and check the variants):
+ *   APHGPU_OPT_GRAPHS        1 (default): replay batches of PCG iterations
+ *                            from CUDA graphs; 0: launch every kernel
+ *   APHGPU_OPT_FUSED_SWEEPS  1: FP32 multigrid levels of at least 8 cells in
+ *                            x (a multiple of 4) smooth with fused
+ *                            out-of-place red-black sweeps (half the DRAM
+ *                            traffic, but latency-bound and slower on GB300;
+ *                            set before the first solve); 0 (default): two
+ *                            in-place half sweeps per sweep */
+enum { APHGPU_OPT_GRAPHS = 0, APHGPU_OPT_FUSED_SWEEPS = 1 };
+int aphgpu_set_option(aphgpu_ctx* ctx, int option, int value);
+
 int aphgpu_mark(aphgpu_ctx* ctx, int slot);
 int aphgpu_elapsed(aphgpu_ctx* ctx, int slot0, int slot1, double* ms);
 
@@ -364,7 +377,9 @@ enum {
   APHGPU_K_VOF_UPDATE = 6, /* VOF update of one direction */
   APHGPU_K_RECONSTRUCT = 7,/* interface normals and plane constants */
   APHGPU_K_HEIGHTS = 8,    /* height functions */
-  APHGPU_K_CURVATURE = 9   /* curvature from heights */
+  APHGPU_K_CURVATURE = 9,  /* curvature from heights */
+  APHGPU_K_SWEEP32 = 10    /* FP32 fused red-black sweep (both colours, out of
+                              place), finest level */
 };
 
 /* Launches one kernel `reps` times on the context's stream on its resident
