@@ -704,8 +704,20 @@ def run_profile(args):
     ctx.assemble_projection(case.alpha, case.rho1, case.rho2, case.flux, case.dt)
     _, bnorm = ctx.residual_norms()
     tol = 1e-10 * bnorm / math.sqrt(case.h ** 3)
-    solver = _lib.SOLVER_MIXED if args.profile == "mixed" else _lib.SOLVER_MGPCG
+    solver = _lib.SOLVER_MGPCG if args.profile == "fp64" else _lib.SOLVER_MIXED
     conf = _lib.default_conf(solver=solver, tol=tol)
+    if args.profile == "vof":
+        # one solve, the corrected fluxes, then `warmup` + `steps` PLIC steps
+        # with the height curvature after each
+        ctx.solve_resident(conf, zero_guess=True)
+        ctx.flux_correct(out=False)
+        ctx.vof_init(case.alpha)
+        dt = case.cfl_dt(0.5)
+        for _ in range(args.warmup + args.steps):
+            ctx.vof_step(None, dt)
+            ctx.curvature(out=False)
+        print("profile vof: %d steps of %d^3" % (args.warmup + args.steps, case.n))
+        return
     for _ in range(args.warmup + args.steps):
         info = ctx.solve_resident(conf, zero_guess=True)
     print("profile %s: %d iterations (%d inner), %d launches in the last solve"
@@ -724,7 +736,7 @@ def main():
     ap.add_argument("--no-vof", action="store_true",
                     help="skip the PLIC advection + curvature measurement")
     ap.add_argument("--cpu-budget", type=float, default=15.0)
-    ap.add_argument("--profile", choices=["mixed", "fp64", "batch"], default=None,
+    ap.add_argument("--profile", choices=["mixed", "fp64", "batch", "vof"], default=None,
                     help="profiling run: assemble, then `steps` solves of one solver "
                          "after `warmup` solves, no other work and no output line")
     ap.add_argument("--serve", action="store_true",
