@@ -1,0 +1,127 @@
+// src/linear/linear_aphgpu.cpp (reference side)
+#include <memory>
+#include <vector>
+
+#include "aphgpu.h"
+#include "linear/linear.h"
+#include "util/module.h"
+
+namespace linear {
+
+template <class M>
+class SolverGpu : public Solver<M> {
+ public:
+  using Base = Solver<M>;
+  using Scal = typename M::Scal;
+  using Expr = typename M::Expr;
+  using MIdx = typename M::MIdx;
+  using Conf = typename Base::Conf;
+  using Info = typename Base::Info;
+
+  SolverGpu(const Conf& conf, int kind, int maxnorm, const M& m)
+      : Base(conf), kind_(kind), maxnorm_(maxnorm) {
+    if (m.IsLead()) {
+      shared_obj_ = std::make_unique<Shared>();
+      shared_ = shared_obj_.get();
+    }
+  }
+
+  Info Solve(
+      const FieldCell<Expr>& fc_system, const FieldCell<Scal>* fc_init,
+      FieldCell<Scal>& fc_sol, M& m) override {
+    auto sem = m.GetSem(__func__);
+    auto& ms = m.GetShared();
+    if (sem()) {
+      m.BcastFromLead(&shared_);  // every block sees the lead's buffers
+    }
+    Shared& s = *shared_;  // valid after the first stage
+    const MIdx gs = ms.GetGlobalSize();
+    auto flat = [&gs](MIdx w) {  // x fastest, as aphgpu expects
+      return size_t(w[0]) + size_t(gs[0]) * (size_t(w[1]) + size_t(gs[1]) * w[2]);
+    };
+    if (sem("gather")) {
+      if (m.IsLead()) {
+        const size_t n = size_t(gs.prod());
+        s.expr.resize(8 * n);
+        s.x0.resize(n);
+        s.x.resize(n);
+      }
+      // blocks of one rank share memory: each writes its own cells
+      for (auto c : m.CellsM()) {
+        const size_t i = flat(MIdx(c));
+        for (int q = 0; q < 8; ++q) s.expr[8 * i + q] = fc_system[c][q];
+        s.x0[i] = fc_init ? (*fc_init)[c] : 0;
+      }
+    }
+    if (sem("solve") && m.IsLead()) {
+      fassert(m.flags.is_periodic[0] && m.flags.is_periodic[1] &&
+              m.flags.is_periodic[2], "gpu solver: periodic domains only");
+      size_t ncells = 0;  // the rank must own the whole domain
+      for (auto c : ms.CellsM()) {
+        (void)c;
+        ++ncells;
+      }
+      fassert_equal(ncells, size_t(gs.prod()));
+      if (!s.ctx) {
+        const auto h = ms.GetCellSize();
+        fassert(h[0] == h[1] && h[1] == h[2], "gpu solver: cubic cells only");
+        fassert_equal(aphgpu_create(&s.ctx, gs[0], gs[1], gs[2], h[0], 0), APHGPU_OK);
+      }
+      int rc = aphgpu_set_system_expr(s.ctx, s.expr.data());
+      aphgpu_conf c;
+      aphgpu_conf_default(&c);
+      c.solver = kind_;
+      c.tol = this->conf.tol;
+      c.miniter = this->conf.miniter;
+      c.maxiter = this->conf.maxiter;
+      c.maxnorm = maxnorm_;
+      aphgpu_info info;
+      if (rc == APHGPU_OK)
+        rc = aphgpu_solve(s.ctx, &c, fc_init ? s.x0.data() : nullptr, s.x.data(), &info);
+      fassert(rc == APHGPU_OK, std::string("aphgpu: ") + aphgpu_last_error(s.ctx));
+      s.info.residual = info.residual;
+      s.info.iter = info.iter;
+    }
+    if (sem("scatter")) {
+      for (auto c : m.CellsM()) fc_sol[c] = s.x[flat(MIdx(c))];
+      m.Comm(&fc_sol, M::CommStencil::direct_one);
+    }
+    return s.info;
+  }
+
+ private:
+  struct Shared {
+    ~Shared() { aphgpu_destroy(ctx); }
+    aphgpu_ctx* ctx = nullptr;
+    std::vector<double> expr, x0, x;
+    Info info{};
+  };
+  int kind_;
+  int maxnorm_;
+  std::unique_ptr<Shared> shared_obj_;  // lead block only
+  Shared* shared_ = nullptr;
+};
+
+template <class M, int Kind>
+class ModuleLinearGpu : public ModuleLinear<M> {
+ public:
+  ModuleLinearGpu()
+      : ModuleLinear<M>(Kind == APHGPU_SOLVER_CG      ? "gpu_cg"
+                        : Kind == APHGPU_SOLVER_MGPCG ? "gpu"
+                                                      : "gpu_mixed") {}
+  std::unique_ptr<Solver<M>> Make(
+      const Vars& var, std::string prefix, const M& m) override {
+    const int maxnorm = var.Int["linsolver_" + prefix + "_maxnorm"];
+    return std::make_unique<SolverGpu<M>>(
+        this->GetConf(var, prefix), Kind, maxnorm, m);
+  }
+};
+
+using M3 = MeshCartesian<double, 3>;
+bool kReg_aphgpu[] = {
+    RegisterModule<ModuleLinearGpu<M3, APHGPU_SOLVER_CG>>(),
+    RegisterModule<ModuleLinearGpu<M3, APHGPU_SOLVER_MGPCG>>(),
+    RegisterModule<ModuleLinearGpu<M3, APHGPU_SOLVER_MIXED>>(),
+};
+
+}  // namespace linear
