@@ -544,6 +544,10 @@ int aphgpu_set_option(aphgpu_ctx* ctx, int option, int value) {
   switch (option) {
     case APHGPU_OPT_GRAPHS: ctx->use_graphs = value != 0; return APHGPU_OK;
     case APHGPU_OPT_FUSED_SWEEPS: ctx->use_fused = value != 0; return APHGPU_OK;
+    case APHGPU_OPT_HALF_COUPLINGS:
+      ctx->use_half = value != 0;
+      ctx->mg.built32 = false;  // rebuilt with or without them at the next solve
+      return APHGPU_OK;
     default: return SetError(ctx, APHGPU_ERR_ARG, "unknown option %d", option);
   }
 }

@@ -210,6 +210,10 @@ struct Level {
   T* x;          // iterate / correction
   T* b;          // right-hand side
   T* r;          // residual scratch
+  // FP16 copy of the couplings scaled by hscale (a power of two), used by
+  // the smoother and the restriction of the finest FP32 level when set
+  uint16_t* wh[3];
+  float hscale;
 };
 
 struct Multigrid {
@@ -312,6 +316,7 @@ struct aphgpu_ctx {
   int64_t mg_epoch = 0;        // bumped whenever a hierarchy is (re)allocated
   bool use_graphs = true;
   bool use_fused = false;  // fused out-of-place red-black sweeps (FP32 levels)
+  bool use_half = true;    // FP16 couplings for the finest-level smoother
 
   // timing
   cudaEvent_t ev0 = nullptr, ev1 = nullptr;

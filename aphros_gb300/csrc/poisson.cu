@@ -440,13 +440,16 @@ inline bool VecOk(const Dims& d) { return (d.nx % 4) == 0 && d.nx >= 8; }
 // One red-black half sweep (FP32, vectorized); see KSmooth for the update.
 // The diagonal is recomputed from the six couplings (read anyway) unless the
 // operator stores one.
-__global__ void __launch_bounds__(256, 4) KSmooth4(Op<float> A, const float* __restrict__ b,
+// (W = __half: FP16 couplings scaled by bscale)
+template <class W>
+__global__ void __launch_bounds__(256, std::is_same<W, float>::value ? 4 : 3)
+    KSmooth4(Op<W> A, const float* __restrict__ b,
                                                 float* x, int color, int zero_init,
-                                                const SolveScalars* s, int kz) {
+                                                const SolveScalars* s, int kz, float bscale) {
   if (s && s->done) return;
   const int kb = blockIdx.z * kz;
   Smooth4Body(A, b, x, color, zero_init, blockIdx.x * 32 + threadIdx.x,
-              blockIdx.y * 8 + threadIdx.y, kb, min(kb + kz, A.d.nz));
+              blockIdx.y * 8 + threadIdx.y, kb, min(kb + kz, A.d.nz), 32, bscale);
 }
 
 // One red-black sweep, both colours fused, out of place (SweepRB4Tile):
@@ -592,14 +595,15 @@ __global__ void KPcgP4(int64_t n4, const float* __restrict__ z, float* p,
 // Residual of a fine FP32 level summed over the 8 children into the coarse
 // right-hand side, vectorized: a thread owns one fine float4 (2 coarse
 // cells in x) of a coarse row and marches over coarse planes.
-__global__ void __launch_bounds__(256, 4) KResidualRestrict4(Op<float> A, const float* __restrict__ b,
+template <class W>
+__global__ void __launch_bounds__(256, 4) KResidualRestrict4(Op<W> A, const float* __restrict__ b,
                                                           const float* __restrict__ x, Dims dc,
                                                           float* bc, const SolveScalars* s,
-                                                          int kz) {
+                                                          int kz, float rscale) {
   if (s && s->done) return;
   const int Kb = blockIdx.z * kz;
   ResidualRestrict4Body(A, b, x, dc, bc, blockIdx.x * 32 + threadIdx.x,
-                        blockIdx.y * 8 + threadIdx.y, Kb, min(Kb + kz, dc.nz));
+                        blockIdx.y * 8 + threadIdx.y, Kb, min(Kb + kz, dc.nz), 32, rscale);
 }
 
 // Residual of the fine level summed over the 8 children into the coarse
@@ -634,6 +638,37 @@ __global__ void KProlong(Dims d, T* x, Dims dc, const TC* __restrict__ xc,
   TILE_LOOP_BEGIN(d)
   x[c] += (T)xc[dc.idx(i >> 1, j >> 1, k >> 1)];
   TILE_LOOP_END
+}
+
+// Largest and smallest nonzero magnitude of three FP32 arrays, as float bits
+// (non-negative floats order like unsigned integers): out[0] max, out[1]
+// min (atomics on order-independent extrema, so deterministic).
+__global__ void KAbsRange(int64_t n, const float* __restrict__ a, const float* __restrict__ b,
+                          const float* __restrict__ c, unsigned int* out) {
+  unsigned int mx = 0u, mn = 0x7f800000u;
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
+       i += (int64_t)gridDim.x * blockDim.x) {
+    const unsigned int v[3] = {__float_as_uint(fabsf(a[i])), __float_as_uint(fabsf(b[i])),
+                               __float_as_uint(fabsf(c[i]))};
+#pragma unroll
+    for (int q = 0; q < 3; ++q) {
+      mx = max(mx, v[q]);
+      if (v[q] != 0u) mn = min(mn, v[q]);
+    }
+  }
+  mx = __reduce_max_sync(0xffffffffu, mx);
+  mn = __reduce_min_sync(0xffffffffu, mn);
+  if ((threadIdx.x & 31) == 0) {
+    atomicMax(&out[0], mx);
+    atomicMin(&out[1], mn);
+  }
+}
+
+// w16 = half(w * scale), scale a power of two (exact before the rounding)
+__global__ void KToHalf(int64_t n, const float* __restrict__ w, __half* w16, float scale) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
+       i += (int64_t)gridDim.x * blockDim.x)
+    w16[i] = __float2half_rn(w[i] * scale);
 }
 
 // Coarse operator: 0.5 * Galerkin with constant prolongation.
@@ -1083,6 +1118,41 @@ int BuildCoarsestInverse(aphgpu_ctx* ctx, const Level<T>& L, double** dinv, int*
 template <class T>
 int BuildHierarchy(aphgpu_ctx* ctx, std::vector<Level<T>>& lv, int coarse_max);
 
+// FP16 copy of the finest FP32 couplings for the smoother and the
+// restriction (the PCG operator keeps FP32), scaled by the power of two that
+// puts the largest magnitude in [2^13, 2^14).  Left out (hscale = 0) for
+// systems with an explicit diagonal, for levels the vectorized kernels do not
+// handle, and when the smallest nonzero magnitude would leave the FP16
+// normal range.
+int BuildHalfCouplings(aphgpu_ctx* ctx, Level<float>& L) {
+  L.hscale = 0.f;
+  if (!ctx->use_half || L.has_diag || !VecOk(L.d)) return APHGPU_OK;
+  const int64_t n = L.d.cells();
+  cudaStream_t st = ctx->stream;
+  const unsigned int init[2] = {0u, 0x7f800000u};
+  APH_CUDA(ctx, cudaMemcpyAsync(ctx->flags + 2, init, sizeof(init), cudaMemcpyHostToDevice, st));
+  KAbsRange<<<FlatBlocks(n), kFlatThreads, 0, st>>>(n, L.w[0], L.w[1], L.w[2], ctx->flags + 2);
+  APH_LAUNCHED(ctx);
+  unsigned int r[2] = {0u, 0u};
+  APH_CUDA(ctx, cudaMemcpyAsync(r, ctx->flags + 2, sizeof(r), cudaMemcpyDeviceToHost, st));
+  APH_CUDA(ctx, cudaStreamSynchronize(st));
+  float mx, mn;
+  std::memcpy(&mx, &r[0], sizeof(float));
+  std::memcpy(&mn, &r[1], sizeof(float));
+  if (!(mx > 0.f) || !std::isfinite(mx)) return APHGPU_OK;
+  int e = 0;
+  std::frexp(mx, &e);
+  const float scale = std::ldexp(1.f, 14 - e);
+  if (mn * scale < 6.2e-5f) return APHGPU_OK;  // below the FP16 normal range
+  for (int q = 0; q < 3; ++q) {
+    if (!L.wh[q]) APH_TRY(Alloc(ctx, &L.wh[q], n));
+    KToHalf<<<FlatBlocks(n), kFlatThreads, 0, st>>>(n, L.w[q], (__half*)L.wh[q], scale);
+    APH_LAUNCHED(ctx);
+  }
+  L.hscale = scale;
+  return APHGPU_OK;
+}
+
 template <>
 int BuildHierarchy<double>(aphgpu_ctx* ctx, std::vector<Level<double>>& lv,
                            int coarse_max) {
@@ -1161,6 +1231,7 @@ int BuildHierarchy<float>(aphgpu_ctx* ctx, std::vector<Level<float>>& lv,
     APH_LAUNCHED(ctx);
   }
   lv[0].has_diag = ctx->diag_explicit;
+  APH_TRY(BuildHalfCouplings(ctx, lv[0]));
   for (size_t l = 1; l < lv.size(); ++l) {
     // coarse operators from the FP64 fine operator at level 1, FP32 below
     if (l == 1) {
@@ -1189,9 +1260,14 @@ void LaunchSmooth(aphgpu_ctx* ctx, const Level<T>& f, const Op<T>& A, int color,
 template <>
 void LaunchSmooth<float>(aphgpu_ctx* ctx, const Level<float>& f, const Op<float>& A,
                          int color, int zero_init, const SolveScalars* s) {
-  if (VecOk(f.d)) {
-    KSmooth4<<<VecGrid(f.d), TileBlock(), 0, ctx->stream>>>(A, f.b, f.x, color, zero_init, s,
-                                                            VecZ(f.d));
+  if (VecOk(f.d) && f.wh[0] && f.hscale > 0.f) {
+    const Op<__half> H{f.d, (const __half*)f.wh[0], (const __half*)f.wh[1],
+                       (const __half*)f.wh[2], nullptr};
+    KSmooth4<__half><<<VecGrid(f.d), TileBlock(), 0, ctx->stream>>>(
+        H, f.b, f.x, color, zero_init, s, VecZ(f.d), f.hscale);
+  } else if (VecOk(f.d)) {
+    KSmooth4<float><<<VecGrid(f.d), TileBlock(), 0, ctx->stream>>>(A, f.b, f.x, color,
+                                                                   zero_init, s, VecZ(f.d), 1.f);
   } else {
     KSmooth<float><<<TileGrid(f.d), TileBlock(), 0, ctx->stream>>>(A, f.invdiag, f.b, f.x,
                                                                    color, zero_init, s);
@@ -1260,7 +1336,15 @@ void LaunchRestrict<float>(aphgpu_ctx* ctx, const Level<float>& f, const Level<f
     int kz = 8;
     while (kz > 1 && xy * ((c.d.nz + kz - 1) / kz) < 4 * 152) kz /= 2;
     const dim3 g((f.d.nx / 4 + 31) / 32, (c.d.ny + 7) / 8, (c.d.nz + kz - 1) / kz);
-    KResidualRestrict4<<<g, TileBlock(), 0, ctx->stream>>>(A, f.b, f.x, c.d, c.b, s, kz);
+    if (f.wh[0] && f.hscale > 0.f) {
+      const Op<__half> H{f.d, (const __half*)f.wh[0], (const __half*)f.wh[1],
+                         (const __half*)f.wh[2], nullptr};
+      KResidualRestrict4<__half><<<g, TileBlock(), 0, ctx->stream>>>(H, f.b, f.x, c.d, c.b, s,
+                                                                      kz, 1.f / f.hscale);
+    } else {
+      KResidualRestrict4<float><<<g, TileBlock(), 0, ctx->stream>>>(A, f.b, f.x, c.d, c.b, s,
+                                                                     kz, 1.f);
+    }
   } else {
     KResidualRestrict<float, float><<<TileGrid(c.d), TileBlock(), 0, ctx->stream>>>(
         A, f.b, f.x, c.d, c.b, s);
@@ -1448,6 +1532,11 @@ int Pcg(aphgpu_ctx* ctx, const Op<T>& A, Precond precond, T* x, T* r, T* p,
     key = Mix(key, (uint64_t)check_every);
     key = Mix(key, (uint64_t)sizeof(T));
     key = Mix(key, (uint64_t)(ctx->use_fused ? 1 : 0));
+    // the FP16 coupling scale is a kernel argument: part of the key
+    float hs = ctx->mg.l32.empty() ? 0.f : ctx->mg.l32[0].hscale;
+    uint32_t hb;
+    std::memcpy(&hb, &hs, sizeof(hb));
+    key = Mix(key, (uint64_t)hb);
     if (g.exec && g.key == key) {
       exec = g.exec;
       graph_kernels = g.kernels;
@@ -1788,8 +1877,9 @@ int TimeSolverKernel(aphgpu_ctx* ctx, int kernel, int reps, double* ms,
       fl.b = bb;
       fl.x = x;
       launch = [=]() { LaunchSmooth<float>(ctx, fl, A, 0, 0, nullptr); };
-      // x read 4 + couplings 12 + half of (b 4, invdiag 4, x write 4)
-      b = N * (4 + 12 + 0.5 * 12);
+      // x read 4 + couplings 12 (6 as FP16) + half of (b 4, invdiag 4,
+      // x write 4)
+      b = N * (4 + (f.hscale > 0.f ? 6 : 12) + 0.5 * 12);
       break;
     }
     case APHGPU_K_SWEEP32: {

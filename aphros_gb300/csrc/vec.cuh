@@ -12,6 +12,10 @@
 // 32 x 8 threads.
 #pragma once
 
+#include <cuda_fp16.h>
+
+#include <type_traits>
+
 #include "stencil.cuh"
 
 namespace aphgpu {
@@ -29,27 +33,47 @@ __device__ __forceinline__ void SetEl(float4& v, int e, float a) {
   if (e == 0) v.x = a; else if (e == 1) v.y = a; else if (e == 2) v.z = a; else v.w = a;
 }
 
+// Couplings are FP32, or FP16 scaled by a power of two (the finest-level
+// smoother and restriction, Level::wh): loaders to FP32.
+__device__ __forceinline__ float ToF(float v) { return v; }
+__device__ __forceinline__ float ToF(__half v) { return __half2float(v); }
+template <class W>
+__device__ __forceinline__ float4 LdW4(const W* p) {
+  if constexpr (std::is_same<W, float>::value) {
+    return Ld4(p);
+  } else {
+    const uint2 u = *reinterpret_cast<const uint2*>(p);
+    const float2 a = __half22float2(*reinterpret_cast<const __half2*>(&u.x));
+    const float2 b = __half22float2(*reinterpret_cast<const __half2*>(&u.y));
+    return make_float4(a.x, a.y, b.x, b.y);
+  }
+}
+
 // Left value (cell 4q-1) and right value (cell 4q+4) of a float4 row segment
 // of tx lanes; every lane of the warp must call it (inactive lanes pass
 // anything).
-__device__ __forceinline__ void XHalo(const float* row, float4 v, int q, int nq,
+template <class W = float>
+__device__ __forceinline__ void XHalo(const W* row, float4 v, int q, int nq,
                                       bool act, float& l, float& r, int tx = 32) {
   const int sl = threadIdx.x & (tx - 1);
   l = __shfl_up_sync(0xffffffffu, v.w, 1);
   r = __shfl_down_sync(0xffffffffu, v.x, 1);
   if (act) {
-    if (sl == 0 || q == 0) l = row[q == 0 ? 4 * nq - 1 : 4 * q - 1];
-    if (sl == tx - 1 || q == nq - 1) r = row[q == nq - 1 ? 0 : 4 * q + 4];
+    if (sl == 0 || q == 0) l = ToF(row[q == 0 ? 4 * nq - 1 : 4 * q - 1]);
+    if (sl == tx - 1 || q == nq - 1) r = ToF(row[q == nq - 1 ? 0 : 4 * q + 4]);
   }
 }
 
 // One red-black half sweep of colour `color` on planes [kb, ke): x = (b -
 // sum of the couplings times the neighbours) / diagonal; zero_init: the
 // neighbours are taken as zero.  The diagonal is recomputed from the six
-// couplings (read anyway) unless the operator stores one.
-__device__ __forceinline__ void Smooth4Body(const Op<float>& A, const float* __restrict__ b,
+// couplings (read anyway) unless the operator stores one.  FP16 couplings
+// (W = __half) are scaled by bscale: the update is (bscale b - sum) / diag
+// in the scaled units.
+template <class W = float>
+__device__ __forceinline__ void Smooth4Body(const Op<W>& A, const float* __restrict__ b,
                                             float* x, int color, int zero_init, int q, int j,
-                                            int kb, int ke, int tx = 32) {
+                                            int kb, int ke, int tx = 32, float bscale = 1.f) {
   const Dims d = A.d;
   const int nq = d.nx >> 2;
   const bool act = q < nq && j < d.ny;
@@ -60,16 +84,16 @@ __device__ __forceinline__ void Smooth4Body(const Op<float>& A, const float* __r
     xz0 = Ld4(x + d.idx(i0, j, wrapm(kb - 1, d.nz)));
     xz1 = Ld4(x + d.idx(i0, j, kb));
   }
-  if (act) wz1 = Ld4(A.w2 + d.idx(i0, j, kb));
+  if (act) wz1 = LdW4(A.w2 + d.idx(i0, j, kb));
   for (int k = kb; k < ke; ++k) {
     const int kp = wrapp(k + 1, d.nz);
     const int64_t c = d.idx(i0, j, k);
     float4 w0v = xz0, w1v = xz0, w1n = xz0, bv = xz0, xjm = xz0, xjp = xz0;
     if (act) {
-      wz2 = Ld4(A.w2 + d.idx(i0, j, kp));
-      w0v = Ld4(A.w0 + c);
-      w1v = Ld4(A.w1 + c);
-      w1n = Ld4(A.w1 + d.idx(i0, jp, k));
+      wz2 = LdW4(A.w2 + d.idx(i0, j, kp));
+      w0v = LdW4(A.w0 + c);
+      w1v = LdW4(A.w1 + c);
+      w1n = LdW4(A.w1 + d.idx(i0, jp, k));
       bv = Ld4(b + c);
       if (!zero_init) {
         xz2 = Ld4(x + d.idx(i0, j, kp));
@@ -91,9 +115,10 @@ __device__ __forceinline__ void Smooth4Body(const Op<float>& A, const float* __r
         const float cxp = e == 3 ? wr : El(w0v, e + 1);
         const float cym = El(w1v, e), cyp = El(w1n, e);
         const float czm = El(wz1, e), czp = El(wz2, e);
-        const float dg = A.diag ? A.diag[c + e]
+        const float dg = A.diag ? ToF(A.diag[c + e])
                                 : -(((((cxm + cxp) + cym) + cyp) + czm) + czp);
         float acc = El(bv, e);
+        if constexpr (!std::is_same<W, float>::value) acc *= bscale;
         if (!zero_init) {
           const float vxm = e == 0 ? xl : El(xz1, e - 1);
           const float vxp = e == 3 ? xr : El(xz1, e + 1);
@@ -199,11 +224,15 @@ __device__ __forceinline__ void Prolong4Body(const Dims& d, float* x, const Dims
 // Residual b - A x of the fine level summed over the 8 children into the
 // coarse right-hand side bc: the thread owns one fine float4 (2 coarse cells
 // in x) of coarse row J and marches over the coarse planes [Kb, Ke).
-__device__ __forceinline__ void ResidualRestrict4Body(const Op<float>& A,
+// (FP16 couplings, W = __half: A x is computed in the scaled units and
+// multiplied by rscale, the inverse scale)
+template <class W = float>
+__device__ __forceinline__ void ResidualRestrict4Body(const Op<W>& A,
                                                       const float* __restrict__ b,
                                                       const float* __restrict__ x,
                                                       const Dims& dc, float* bc, int q, int J,
-                                                      int Kb, int Ke, int tx = 32) {
+                                                      int Kb, int Ke, int tx = 32,
+                                                      float rscale = 1.f) {
   const Dims d = A.d;
   const int nq = d.nx >> 2;
   const bool act = q < nq && J < dc.ny;
@@ -220,15 +249,15 @@ __device__ __forceinline__ void ResidualRestrict4Body(const Op<float>& A,
       float4 xv = make_float4(0, 0, 0, 0), w0v = xv;
       if (act) {
         xv = Ld4(x + c);
-        w0v = Ld4(A.w0 + c);
+        w0v = LdW4(A.w0 + c);
       }
       float xl, xr, wl, wr;
       XHalo(x + d.idx(0, act ? j : 0, k), xv, q, nq, act, xl, xr, tx);
       XHalo(A.w0 + d.idx(0, act ? j : 0, k), w0v, q, nq, act, wl, wr, tx);
       (void)wl;
       if (act) {
-        const float4 w1v = Ld4(A.w1 + c), w1n = Ld4(A.w1 + d.idx(i0, jp, k));
-        const float4 w2v = Ld4(A.w2 + c), w2n = Ld4(A.w2 + d.idx(i0, j, kp));
+        const float4 w1v = LdW4(A.w1 + c), w1n = LdW4(A.w1 + d.idx(i0, jp, k));
+        const float4 w2v = LdW4(A.w2 + c), w2n = LdW4(A.w2 + d.idx(i0, j, kp));
         const float4 xjm = Ld4(x + d.idx(i0, jm, k)), xjp = Ld4(x + d.idx(i0, jp, k));
         const float4 xkm = Ld4(x + d.idx(i0, j, km)), xkp = Ld4(x + d.idx(i0, j, kp));
         const float4 bv = Ld4(b + c);
@@ -238,7 +267,7 @@ __device__ __forceinline__ void ResidualRestrict4Body(const Op<float>& A,
           const float cxp = e == 3 ? wr : El(w0v, e + 1);
           const float cym = El(w1v, e), cyp = El(w1n, e);
           const float czm = El(w2v, e), czp = El(w2n, e);
-          const float dg = A.diag ? A.diag[c + e]
+          const float dg = A.diag ? ToF(A.diag[c + e])
                                   : -(((((cxm + cxp) + cym) + cyp) + czm) + czp);
           float y = El(xv, e) * dg;
           y += (e == 0 ? xl : El(xv, e - 1)) * cxm;
@@ -247,6 +276,7 @@ __device__ __forceinline__ void ResidualRestrict4Body(const Op<float>& A,
           y += El(xjp, e) * cyp;
           y += El(xkm, e) * czm;
           y += El(xkp, e) * czp;
+          if constexpr (!std::is_same<W, float>::value) y *= rscale;
           const float rv = El(bv, e) - y;
           if (e < 2) acc0 += rv; else acc1 += rv;
         }

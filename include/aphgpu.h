@@ -359,8 +359,14 @@ int aphgpu_batch_last_ms(const aphgpu_batch* batch, double* ms, int64_t* launche
  *                            out-of-place red-black sweeps (half the DRAM
  *                            traffic, but latency-bound and slower on GB300;
  *                            set before the first solve); 0 (default): two
- *                            in-place half sweeps per sweep */
-enum { APHGPU_OPT_GRAPHS = 0, APHGPU_OPT_FUSED_SWEEPS = 1 };
+ *                            in-place half sweeps per sweep
+ *   APHGPU_OPT_HALF_COUPLINGS 1 (default): the smoother and the restriction
+ *                            of the finest FP32 level read an FP16 copy of
+ *                            the couplings scaled by a power of two (the
+ *                            PCG operator and the FP64 defect correction
+ *                            keep FP32 / FP64: only the preconditioner
+ *                            changes); 0: FP32 couplings */
+enum { APHGPU_OPT_GRAPHS = 0, APHGPU_OPT_FUSED_SWEEPS = 1, APHGPU_OPT_HALF_COUPLINGS = 2 };
 int aphgpu_set_option(aphgpu_ctx* ctx, int option, int value);
 
 int aphgpu_mark(aphgpu_ctx* ctx, int slot);

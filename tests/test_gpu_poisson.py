@@ -230,6 +230,9 @@ def test_fused_sweeps_bit_identical(solver, shape):
     c, r = workload.place_spheres(11, 3, 0.1, 0.2, gap=0.02)
     case = workload.Case(nx, c, r, rho1=1.0, rho2=1e-3, seed=12)
     ctx = _lib.Context(shape, h)
+    # the fused sweep reads the FP32 couplings: compare against the FP32
+    # half sweeps
+    ctx.set_option(_lib.OPT_HALF_COUPLINGS, 0)
     N = nx * ny * nz
     alpha = workload.alpha_spheres(nx, c, r)[:N] if nx == ny == nz else np.zeros(N)
     flux = workload.tg_flux(max(shape), seed=5)
@@ -249,3 +252,25 @@ def test_fused_sweeps_bit_identical(solver, shape):
     for key, val in out.items():
         assert np.array_equal(val[0], ref[0]), key
         assert val[1:] == ref[1:], key
+
+
+@pytest.mark.parametrize("n", [64, 96])
+def test_half_couplings_preconditioner(n):
+    """The FP16 copy of the finest couplings changes only the preconditioner:
+    the mixed solve reaches the same residual with the same outer iteration
+    count, and the pressures agree to the solver tolerance."""
+    case = workload.config("c1", n=n)
+    ctx = _lib.Context(n, case.h)
+    ctx.assemble_projection(case.alpha, case.rho1, case.rho2, case.flux, case.dt)
+    _, bn = ctx.residual_norms()
+    conf = _lib.default_conf(solver=_lib.SOLVER_MIXED, tol=1e-10 * bn / math.sqrt(case.h ** 3))
+    out = {}
+    for half in (1, 0):
+        ctx.set_option(_lib.OPT_HALF_COUPLINGS, half)
+        x, info = ctx.solve(conf)
+        rn, bn2 = ctx.residual_norms()
+        assert info.converged and rn / bn2 <= 1.01e-10
+        out[half] = (x, info)
+    assert abs(out[1][1].iter - out[0][1].iter) <= 1
+    assert abs(out[1][1].inner_iter - out[0][1].inner_iter) <= 0.2 * out[0][1].inner_iter + 2
+    assert rel_l2(out[1][0], out[0][0]) < 1e-7
