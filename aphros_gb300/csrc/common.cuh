@@ -316,7 +316,7 @@ struct aphgpu_ctx {
   int64_t mg_epoch = 0;        // bumped whenever a hierarchy is (re)allocated
   bool use_graphs = true;
   bool use_fused = false;  // fused out-of-place red-black sweeps (FP32 levels)
-  bool use_half = true;    // FP16 couplings for the finest-level smoother
+  bool use_half = false;   // FP16 couplings for the finest-level smoother
 
   // timing
   cudaEvent_t ev0 = nullptr, ev1 = nullptr;

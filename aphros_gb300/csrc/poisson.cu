@@ -442,8 +442,7 @@ inline bool VecOk(const Dims& d) { return (d.nx % 4) == 0 && d.nx >= 8; }
 // operator stores one.
 // (W = __half: FP16 couplings scaled by bscale)
 template <class W>
-__global__ void __launch_bounds__(256, std::is_same<W, float>::value ? 4 : 3)
-    KSmooth4(Op<W> A, const float* __restrict__ b,
+__global__ void __launch_bounds__(256, 4) KSmooth4(Op<W> A, const float* __restrict__ b,
                                                 float* x, int color, int zero_init,
                                                 const SolveScalars* s, int kz, float bscale) {
   if (s && s->done) return;

@@ -49,6 +49,13 @@ __device__ __forceinline__ float4 LdW4(const W* p) {
   }
 }
 
+// L2 prefetch (PTX prefetch.global.L2): starts the next plane's loads one
+// plane early without holding registers; the plane loops are bound by the
+// memory round trip per plane, not by bandwidth.
+__device__ __forceinline__ void PrefetchL2(const void* p) {
+  asm volatile("prefetch.global.L2 [%0];" ::"l"(p));
+}
+
 // Left value (cell 4q-1) and right value (cell 4q+4) of a float4 row segment
 // of tx lanes; every lane of the warp must call it (inactive lanes pass
 // anything).
@@ -89,6 +96,22 @@ __device__ __forceinline__ void Smooth4Body(const Op<W>& A, const float* __restr
     const int kp = wrapp(k + 1, d.nz);
     const int64_t c = d.idx(i0, j, k);
     float4 w0v = xz0, w1v = xz0, w1n = xz0, bv = xz0, xjm = xz0, xjp = xz0;
+    if (act && k + 1 < ke) {
+      // what the next plane loads: couplings, b and the y neighbours of
+      // plane k+1, w2 and x of plane k+2
+      const int kq = wrapp(kp + 1, d.nz);
+      const int64_t cn = d.idx(i0, j, kp);
+      PrefetchL2(A.w0 + cn);
+      PrefetchL2(A.w1 + cn);
+      PrefetchL2(A.w1 + d.idx(i0, jp, kp));
+      PrefetchL2(A.w2 + d.idx(i0, j, kq));
+      PrefetchL2(b + cn);
+      if (!zero_init) {
+        PrefetchL2(x + d.idx(i0, j, kq));
+        PrefetchL2(x + d.idx(i0, jm, kp));
+        PrefetchL2(x + d.idx(i0, jp, kp));
+      }
+    }
     if (act) {
       wz2 = LdW4(A.w2 + d.idx(i0, j, kp));
       w0v = LdW4(A.w0 + c);
@@ -159,6 +182,17 @@ __device__ __forceinline__ void Apply4Body(const Op<float>& A, const float* __re
     const int kp = wrapp(k + 1, d.nz);
     const int64_t c = d.idx(i0, j, k);
     float4 w0v = z0, w1v = z0, w1n = z0, pjm = z0, pjp = z0;
+    if (act && k + 1 < ke) {
+      const int kq = wrapp(kp + 1, d.nz);
+      const int64_t cn = d.idx(i0, j, kp);
+      PrefetchL2(A.w0 + cn);
+      PrefetchL2(A.w1 + cn);
+      PrefetchL2(A.w1 + d.idx(i0, jp, kp));
+      PrefetchL2(A.w2 + d.idx(i0, j, kq));
+      PrefetchL2(p + d.idx(i0, j, kq));
+      PrefetchL2(p + d.idx(i0, jm, kp));
+      PrefetchL2(p + d.idx(i0, jp, kp));
+    }
     if (act) {
       z2 = Ld4(p + d.idx(i0, j, kp));
       wz2 = Ld4(A.w2 + d.idx(i0, j, kp));

@@ -360,12 +360,13 @@ int aphgpu_batch_last_ms(const aphgpu_batch* batch, double* ms, int64_t* launche
  *                            traffic, but latency-bound and slower on GB300;
  *                            set before the first solve); 0 (default): two
  *                            in-place half sweeps per sweep
- *   APHGPU_OPT_HALF_COUPLINGS 1 (default): the smoother and the restriction
- *                            of the finest FP32 level read an FP16 copy of
- *                            the couplings scaled by a power of two (the
- *                            PCG operator and the FP64 defect correction
- *                            keep FP32 / FP64: only the preconditioner
- *                            changes); 0: FP32 couplings */
+ *   APHGPU_OPT_HALF_COUPLINGS 1: the smoother and the restriction of the
+ *                            finest FP32 level read an FP16 copy of the
+ *                            couplings scaled by a power of two (the PCG
+ *                            operator and the FP64 defect correction keep
+ *                            FP32 / FP64: only the preconditioner changes;
+ *                            about 1 % faster at 512^3); 0 (default): FP32
+ *                            couplings */
 enum { APHGPU_OPT_GRAPHS = 0, APHGPU_OPT_FUSED_SWEEPS = 1, APHGPU_OPT_HALF_COUPLINGS = 2 };
 int aphgpu_set_option(aphgpu_ctx* ctx, int option, int value);
 
