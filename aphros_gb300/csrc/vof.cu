@@ -355,10 +355,12 @@ __global__ void KSweepFlux(Dims d, int dir, const double* __restrict__ u,
   const int64_t cm = dir == 0 ? d.idx(wrapm(i - 1, d.nx), j, k)
                    : dir == 1 ? d.idx(i, wrapm(j - 1, d.ny), k)
                               : d.idx(i, j, wrapm(k - 1, d.nz));
+  // both candidate upwind values are loaded with the flux (one round trip
+  // to memory instead of two dependent ones)
   const double v = vflux[c];
+  const double um = u[cm], uc = u[c];
   const long long vb = Bits(v);
-  const int64_t up = PositiveBits(vb) ? cm : c;
-  const double uu = u[up];
+  const double uu = PositiveBits(vb) ? um : uc;
   const long long ub = Bits(uu);
   if (InterfaceBits(ub)) continue;
   // finite v: v * (+0) is the zero with the sign of v, v * 1 is v
