@@ -544,6 +544,10 @@ int aphgpu_set_option(aphgpu_ctx* ctx, int option, int value) {
   switch (option) {
     case APHGPU_OPT_GRAPHS: ctx->use_graphs = value != 0; return APHGPU_OK;
     case APHGPU_OPT_FUSED_SWEEPS: ctx->use_fused = value != 0; return APHGPU_OK;
+    case APHGPU_OPT_CYCLE:
+      if (value < 0 || value > 2) return SetError(ctx, APHGPU_ERR_ARG, "cycle must be 0, 1 or 2");
+      ctx->mg_gamma = value;
+      return APHGPU_OK;
     case APHGPU_OPT_HALF_COUPLINGS:
       ctx->use_half = value != 0;
       ctx->mg.built32 = false;  // rebuilt with or without them at the next solve

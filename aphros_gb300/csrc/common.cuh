@@ -317,6 +317,7 @@ struct aphgpu_ctx {
   bool use_graphs = true;
   bool use_fused = false;  // fused out-of-place red-black sweeps (FP32 levels)
   bool use_half = false;   // FP16 couplings for the finest-level smoother
+  int mg_gamma = 0;        // cycles of each level below the finest (1 V, 2 W, 0 auto)
 
   // timing
   cudaEvent_t ev0 = nullptr, ev1 = nullptr;

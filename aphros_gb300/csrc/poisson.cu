@@ -1410,34 +1410,25 @@ void LaunchP<float>(aphgpu_ctx* ctx, Dims d, const float* z, float* p, const Sol
   }
 }
 
-// One V-cycle: lv[0].b -> lv[0].x (zero initial guess).
+// Cycles of each level below the finest: the context's choice, or W (2)
+// on grids of at least 256^3 cells, where the coarse visits are cheap next
+// to the finest level, and V (1) below (launch latency dominates there).
+inline int CycleGamma(const aphgpu_ctx* ctx) {
+  if (ctx->mg_gamma == 1 || ctx->mg_gamma == 2) return ctx->mg_gamma;
+  return ctx->N >= (int64_t)256 * 256 * 256 ? 2 : 1;
+}
+
+// Multigrid cycle from level l: pre-smoothing (from a zero guess on the
+// level's first visit of the cycle, else from its current x), restriction
+// of the residual, `gamma` cycles of level l+1 (1 from the finest level;
+// ctx->mg_gamma below it: 1 V-cycle, 2 W-cycle), prolongation of the
+// correction, post-smoothing.  The coarsest level is solved directly.
 template <class T>
-int VCycle(aphgpu_ctx* ctx, std::vector<Level<T>>& lv, int pre, int post,
-           const SolveScalars* s) {
+int CycleLevel(aphgpu_ctx* ctx, std::vector<Level<T>>& lv, int l, bool first, int pre,
+               int post, const SolveScalars* s) {
   const int L = (int)lv.size();
   cudaStream_t st = ctx->stream;
-  for (int l = 0; l < L - 1; ++l) {
-    Level<T>& f = lv[l];
-    const Op<T> A = MakeOp(f);
-    const int fused = pre > 0 ? FusedSweeps<T>(ctx, f, A, pre, 0, true, s) : kNotFused;
-    if (fused != kNotFused) APH_TRY(fused);
-    for (int sw = 0; fused == kNotFused && sw < pre; ++sw) {
-      LaunchSmooth<T>(ctx, f, A, 0, sw == 0, s);
-      APH_LAUNCHED(ctx);
-      LaunchSmooth<T>(ctx, f, A, 1, 0, s);
-      APH_LAUNCHED(ctx);
-    }
-    if (pre == 0) {
-      LaunchSmooth<T>(ctx, f, A, 0, 1, s);
-      APH_LAUNCHED(ctx);
-      LaunchSmooth<T>(ctx, f, A, 1, 1, s);
-      APH_LAUNCHED(ctx);
-    }
-    Level<T>& c = lv[l + 1];
-    LaunchRestrict<T>(ctx, f, c, A, s);
-    APH_LAUNCHED(ctx);
-  }
-  {
+  if (l == L - 1) {
     Level<T>& c = lv[L - 1];
     const Op<T> A = MakeOp(c);
     auto& mg = ctx->mg;
@@ -1450,23 +1441,46 @@ int VCycle(aphgpu_ctx* ctx, std::vector<Level<T>>& lv, int pre, int post,
       KCoarsestCG<T><<<1, 1024, 0, st>>>(A, c.b, c.x, mg.cr, mg.cp, mg.cap, mg.cx, s);
     }
     APH_LAUNCHED(ctx);
+    return APHGPU_OK;
   }
-  for (int l = L - 2; l >= 0; --l) {
-    Level<T>& f = lv[l];
-    Level<T>& c = lv[l + 1];
-    const Op<T> A = MakeOp(f);
-    LaunchProlong<T>(ctx, f, c, s);
+  Level<T>& f = lv[l];
+  const Op<T> A = MakeOp(f);
+  const int fused = pre > 0 ? FusedSweeps<T>(ctx, f, A, pre, 0, first, s) : kNotFused;
+  if (fused != kNotFused) APH_TRY(fused);
+  for (int sw = 0; fused == kNotFused && sw < pre; ++sw) {
+    LaunchSmooth<T>(ctx, f, A, 0, first && sw == 0, s);
     APH_LAUNCHED(ctx);
-    const int fused = post > 0 ? FusedSweeps<T>(ctx, f, A, post, 1, false, s) : kNotFused;
-    if (fused != kNotFused) APH_TRY(fused);
-    for (int sw = 0; fused == kNotFused && sw < post; ++sw) {
-      LaunchSmooth<T>(ctx, f, A, 1, 0, s);
-      APH_LAUNCHED(ctx);
-      LaunchSmooth<T>(ctx, f, A, 0, 0, s);
-      APH_LAUNCHED(ctx);
-    }
+    LaunchSmooth<T>(ctx, f, A, 1, 0, s);
+    APH_LAUNCHED(ctx);
+  }
+  if (pre == 0 && first) {
+    LaunchSmooth<T>(ctx, f, A, 0, 1, s);
+    APH_LAUNCHED(ctx);
+    LaunchSmooth<T>(ctx, f, A, 1, 1, s);
+    APH_LAUNCHED(ctx);
+  }
+  LaunchRestrict<T>(ctx, f, lv[l + 1], A, s);
+  APH_LAUNCHED(ctx);
+  const int gamma = l == 0 ? 1 : CycleGamma(ctx);
+  for (int g = 0; g < gamma; ++g) APH_TRY(CycleLevel<T>(ctx, lv, l + 1, g == 0, pre, post, s));
+  LaunchProlong<T>(ctx, f, lv[l + 1], s);
+  APH_LAUNCHED(ctx);
+  const int fused2 = post > 0 ? FusedSweeps<T>(ctx, f, A, post, 1, false, s) : kNotFused;
+  if (fused2 != kNotFused) APH_TRY(fused2);
+  for (int sw = 0; fused2 == kNotFused && sw < post; ++sw) {
+    LaunchSmooth<T>(ctx, f, A, 1, 0, s);
+    APH_LAUNCHED(ctx);
+    LaunchSmooth<T>(ctx, f, A, 0, 0, s);
+    APH_LAUNCHED(ctx);
   }
   return APHGPU_OK;
+}
+
+// One cycle: lv[0].b -> lv[0].x (zero initial guess).
+template <class T>
+int VCycle(aphgpu_ctx* ctx, std::vector<Level<T>>& lv, int pre, int post,
+           const SolveScalars* s) {
+  return CycleLevel<T>(ctx, lv, 0, true, pre, post, s);
 }
 
 int SaveHistory(aphgpu_ctx* ctx, const double* d_hist, int n,
@@ -1531,6 +1545,7 @@ int Pcg(aphgpu_ctx* ctx, const Op<T>& A, Precond precond, T* x, T* r, T* p,
     key = Mix(key, (uint64_t)check_every);
     key = Mix(key, (uint64_t)sizeof(T));
     key = Mix(key, (uint64_t)(ctx->use_fused ? 1 : 0));
+    key = Mix(key, (uint64_t)CycleGamma(ctx));
     // the FP16 coupling scale is a kernel argument: part of the key
     float hs = ctx->mg.l32.empty() ? 0.f : ctx->mg.l32[0].hscale;
     uint32_t hb;

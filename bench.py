@@ -314,6 +314,9 @@ def run_ours(args):
     N = case.N
     ctx = _lib.Context(case.n, case.h, device)
     ctx.assemble_projection(case.alpha, case.rho1, case.rho2, case.flux, case.dt)
+    # the configuration's V-cycles; the W-cycle (library default at this
+    # size) is measured beside them
+    ctx.set_option(_lib.OPT_CYCLE, 1)
     _, bnorm = ctx.residual_norms()
     tol = 1e-10 * bnorm / math.sqrt(case.h ** 3)
     conf_mixed = _lib.default_conf(solver=_lib.SOLVER_MIXED, tol=tol, maxiter=100)
@@ -355,6 +358,27 @@ def run_ours(args):
     units64, tmax64 = aggregate_over_ranks(args.steps, t_fp64 / 1000.0)
     value = units / tmax
     fp64_value = units64 / tmax64
+
+    # the same solves with W-cycles below the finest level
+    w_cycle = None
+    if not args.no_w_cycle:
+        ctx.set_option(_lib.OPT_CYCLE, 2)
+        kw = max(1, min(args.steps, 5))
+        run_steps(conf_mixed, 1, False)
+        run_steps(conf_fp64, 1, False)
+        tw, stw, _, infw = run_steps(conf_mixed, kw, True)
+        rnw, bnw = ctx.residual_norms()
+        pw = ctx.get_solution()
+        tw64, _, _, infw64 = run_steps(conf_fp64, kw, True)
+        ctx.set_option(_lib.OPT_CYCLE, 1)
+        uw, tmw = aggregate_over_ranks(kw, tw / 1000.0)
+        uw64, tmw64 = aggregate_over_ranks(kw, tw64 / 1000.0)
+        w_cycle = {"value": uw / tmw, "unit": UNIT, "ms_per_step": float(tw / kw),
+                   "iters": {"outer": infw[-1].iter, "inner_fp32_pcg": infw[-1].inner_iter},
+                   "rel_residual": rnw / bnw, "pressure_rel_err_vs_fp64_v": rel_l2(pw, p_fp64),
+                   "fp64": {"value": uw64 / tmw64, "ms_per_step": float(tw64 / kw),
+                            "iters": infw64[-1].iter},
+                   "mixed_over_fp64": (uw / tmw) / (uw64 / tmw64)}
 
     # live roofline of the dominant kernel of the mixed solve
     peak, peak_kind = measured_peak_gbs()
@@ -434,6 +458,7 @@ def run_ours(args):
                  "p99_ms": float(np.percentile(st_fp64, 99)),
                  "iters": inf_fp64[-1].iter if inf_fp64 else None},
         "mixed_over_fp64": value / fp64_value,
+        "w_cycle": w_cycle,
         "iters": {"outer": inf_mixed[-1].iter, "inner_fp32_pcg": inf_mixed[-1].inner_iter},
         "rel_residual": rel_res_mixed,
         "pressure_rel_err_vs_fp64": rel_l2(p_mixed, p_fp64),
@@ -733,6 +758,8 @@ def main():
     ap.add_argument("--workload", choices=sorted(WORKLOADS), default="c3")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-w-cycle", action="store_true",
+                    help="skip the W-cycle measurement beside the V-cycle headline")
     ap.add_argument("--no-vof", action="store_true",
                     help="skip the PLIC advection + curvature measurement")
     ap.add_argument("--cpu-budget", type=float, default=15.0)

@@ -366,8 +366,17 @@ int aphgpu_batch_last_ms(const aphgpu_batch* batch, double* ms, int64_t* launche
  *                            operator and the FP64 defect correction keep
  *                            FP32 / FP64: only the preconditioner changes;
  *                            about 1 % faster at 512^3); 0 (default): FP32
- *                            couplings */
-enum { APHGPU_OPT_GRAPHS = 0, APHGPU_OPT_FUSED_SWEEPS = 1, APHGPU_OPT_HALF_COUPLINGS = 2 };
+ *                            couplings
+ *   APHGPU_OPT_CYCLE         multigrid cycle below the finest level: 1
+ *                            V-cycle, 2 W-cycle (each coarse level visited
+ *                            twice per visit of the level above), 0
+ *                            (default) W from 256^3 cells up, V below */
+enum {
+  APHGPU_OPT_GRAPHS = 0,
+  APHGPU_OPT_FUSED_SWEEPS = 1,
+  APHGPU_OPT_HALF_COUPLINGS = 2,
+  APHGPU_OPT_CYCLE = 3
+};
 int aphgpu_set_option(aphgpu_ctx* ctx, int option, int value);
 
 int aphgpu_mark(aphgpu_ctx* ctx, int slot);
