@@ -121,6 +121,10 @@ def lib():
     L.aphgpu_batch_last_ms.argtypes = [_P, _PD, ctypes.POINTER(ctypes.c_int64)]
     L.aphgpu_batch_set_tiles.argtypes = [_P, _I, _I]
     L.aphgpu_batch_get_tiles.argtypes = [_P, ctypes.POINTER(_I), ctypes.POINTER(_I)]
+    L.aphgpu_batch_set_cycle.argtypes = [_P, _I]
+    L.aphgpu_batch_get_cycle.argtypes = [_P, ctypes.POINTER(_I)]
+    L.aphgpu_batch_set_cycle.restype = _I
+    L.aphgpu_batch_get_cycle.restype = _I
     for name in ("aphgpu_batch_create", "aphgpu_batch_solve", "aphgpu_batch_tune",
                  "aphgpu_batch_last_ms", "aphgpu_batch_set_tiles", "aphgpu_batch_get_tiles"):
         getattr(L, name).restype = _I
@@ -376,6 +380,14 @@ class Batch:
         a, b = _I(), _I()
         self._check(self._L.aphgpu_batch_get_tiles(self._p, ctypes.byref(a), ctypes.byref(b)))
         return a.value, b.value
+
+    def set_cycle(self, cycle):
+        self._check(self._L.aphgpu_batch_set_cycle(self._p, cycle))
+
+    def cycle(self):
+        v = _I()
+        self._check(self._L.aphgpu_batch_get_cycle(self._p, ctypes.byref(v)))
+        return v.value
 
     def last(self):
         ms, n = _D(), ctypes.c_int64()

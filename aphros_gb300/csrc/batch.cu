@@ -447,36 +447,66 @@ __device__ void CtaDense(const BDom& D) {
   }
 }
 
-// Levels lc .. nlev-1 of every domain: the V-cycle of those levels (same
-// order as the batched levels: pre-smoothing colours 0 then 1, post
-// colours 1 then 0), CTA barriers between the passes.
+// Levels lc .. nlev-1 of every domain: one multigrid cycle of those levels
+// (pre-smoothing colours 0 then 1, post colours 1 then 0, as the batched
+// levels), each level below lc visited `gamma` times per visit of the level
+// above (1 V-cycle, 2 W-cycle; the exactly solved coarsest level once),
+// CTA barriers between the passes.  The cycle is iterative: todo[l] counts
+// the visits of level l+1 still to make from level l.
 __global__ void __launch_bounds__(kCoarseThreads) KBCoarseCycle(const BDom* __restrict__ doms,
-                                                                int pre, int post) {
+                                                                int pre, int post, int gamma) {
   const BDom& D = doms[blockIdx.x];
   if (D.si->done) return;
   const int L = D.nlev;
-  for (int l = D.lc; l < L - 1; ++l) {
-    const BLevel& F = D.lv[l];
-    for (int sw = 0; sw < max(pre, 1); ++sw) {
-      CtaSmooth(F, 0, sw == 0);
+  int todo[kMaxLev];
+  int l = D.lc;
+  bool first = true;
+  for (;;) {
+    if (l < L - 1) {
+      // enter level l: pre-smoothing (zero guess on its first visit) and
+      // restriction of its residual
+      const BLevel& F = D.lv[l];
+      if (pre > 0) {
+        for (int sw = 0; sw < pre; ++sw) {
+          CtaSmooth(F, 0, first && sw == 0);
+          __syncthreads();
+          CtaSmooth(F, 1, 0);
+          __syncthreads();
+        }
+      } else if (first) {
+        CtaSmooth(F, 0, 1);
+        __syncthreads();
+        CtaSmooth(F, 1, 1);
+        __syncthreads();
+      }
+      CtaRestrict(F, D.lv[l + 1]);
       __syncthreads();
-      CtaSmooth(F, 1, pre == 0);
-      __syncthreads();
+      todo[l] = l + 1 == L - 1 ? 1 : gamma;
+      ++l;
+      first = true;
+      continue;
     }
-    CtaRestrict(F, D.lv[l + 1]);
+    CtaDense(D);
     __syncthreads();
-  }
-  CtaDense(D);
-  __syncthreads();
-  for (int l = L - 2; l >= D.lc; --l) {
-    const BLevel& F = D.lv[l];
-    CtaProlong(F, D.lv[l + 1]);
-    __syncthreads();
-    for (int sw = 0; sw < post; ++sw) {
-      CtaSmooth(F, 1, 0);
+    // leave levels upward until one still has a visit of its coarser level
+    // to make
+    for (;;) {
+      --l;
+      if (l < D.lc) return;
+      if (--todo[l] > 0) {
+        ++l;
+        first = false;
+        break;
+      }
+      const BLevel& F = D.lv[l];
+      CtaProlong(F, D.lv[l + 1]);
       __syncthreads();
-      CtaSmooth(F, 0, 0);
-      __syncthreads();
+      for (int sw = 0; sw < post; ++sw) {
+        CtaSmooth(F, 1, 0);
+        __syncthreads();
+        CtaSmooth(F, 0, 0);
+        __syncthreads();
+      }
     }
   }
 }
@@ -706,6 +736,7 @@ struct aphgpu_batch {
   int nlev_max = 0;
   int kz = 4;                 // planes per thread of the batched tiles
   int coarse_cells = 4096;    // levels with at most this many cells: per-domain CTA
+  int cycle = 1;              // visits of each per-domain coarse level (1 V, 2 W)
   int device = 0;
   int sms = 0;
   cudaStream_t st = nullptr;  // stream of the first context
@@ -1013,7 +1044,7 @@ int BVCycle(aphgpu_batch* B, int pre, int post) {
     }
     B_TABLE_LAUNCH(B, KBRestrict, B->res[l], l, kz);
   }
-  KBCoarseCycle<<<B->ndom, kCoarseThreads, 0, B->st>>>(B->d_doms, pre, post);
+  KBCoarseCycle<<<B->ndom, kCoarseThreads, 0, B->st>>>(B->d_doms, pre, post, B->cycle);
   B_LAUNCHED(B);
   for (int l = nb - 1; l >= 0; --l) {
     B_TABLE_LAUNCH(B, KBProlong, B->lev[l], l, kz);
@@ -1042,6 +1073,7 @@ int BEnsureGraph(aphgpu_batch* B, const aphgpu_conf* conf, int every) {
   uint64_t key = B->layout_key;
   key = BMix(key, (uint64_t)(conf->mg_pre * 1000 + conf->mg_post));
   key = BMix(key, (uint64_t)every);
+  key = BMix(key, (uint64_t)B->cycle);
   if (B->graph && B->graph_key == key) return APHGPU_OK;
   if (B->graph) cudaGraphExecDestroy(B->graph);
   B->graph = nullptr;
@@ -1244,32 +1276,50 @@ int aphgpu_batch_get_tiles(const aphgpu_batch* B, int* planes, int* coarse_cells
   return APHGPU_OK;
 }
 
+int aphgpu_batch_set_cycle(aphgpu_batch* B, int cycle) {
+  if (!B || cycle < 1 || cycle > 2) return APHGPU_ERR_ARG;
+  B->cycle = cycle;
+  return APHGPU_OK;
+}
+
+int aphgpu_batch_get_cycle(const aphgpu_batch* B, int* cycle) {
+  if (!B || !cycle) return APHGPU_ERR_ARG;
+  *cycle = B->cycle;
+  return APHGPU_OK;
+}
+
 int aphgpu_batch_tune(aphgpu_batch* B, aphgpu_conf* conf, double* best_ms) {
   if (!B || !conf) return APHGPU_ERR_ARG;
-  // coordinate search: tile planes x coarse-level size at the given sweeps,
-  // then the sweeps at the best tiles
+  // coordinate search: tile planes x coarse-level size x cycle at the given
+  // sweeps, then the sweeps at the best of those
   const int kzs[] = {2, 4, 8};
   const int coarse[] = {512, 4096, 32768};
+  const int cycles[] = {1, 2};
   const int sweeps[] = {1, 2, 3};
   double best = 1e300;
-  int best_kz = B->kz, best_cc = B->coarse_cells, best_sw = conf->mg_pre;
+  int best_kz = B->kz, best_cc = B->coarse_cells, best_cy = B->cycle, best_sw = conf->mg_pre;
   aphgpu_conf c = *conf;
   c.mg_post = c.mg_pre;
   for (int kz : kzs) {
     for (int cc : coarse) {
-      B->kz = kz;
-      B->coarse_cells = cc;
-      const int rc = aphgpu_batch_solve(B, &c, nullptr);
-      if (rc != APHGPU_OK) return rc;
-      if (B->last_ms < best) {
-        best = B->last_ms;
-        best_kz = kz;
-        best_cc = cc;
+      for (int cy : cycles) {
+        B->kz = kz;
+        B->coarse_cells = cc;
+        B->cycle = cy;
+        const int rc = aphgpu_batch_solve(B, &c, nullptr);
+        if (rc != APHGPU_OK) return rc;
+        if (B->last_ms < best) {
+          best = B->last_ms;
+          best_kz = kz;
+          best_cc = cc;
+          best_cy = cy;
+        }
       }
     }
   }
   B->kz = best_kz;
   B->coarse_cells = best_cc;
+  B->cycle = best_cy;
   for (int sw : sweeps) {
     if (sw == c.mg_pre) continue;
     aphgpu_conf t = c;

@@ -678,6 +678,7 @@ def run_batch(args):
                                "bubbles, density ratio log-uniform [10,1000], %d cells total; "
                                "inputs %.1f GB > L2, no flush" % (n, cells, cells * 40 / 1e9),
                    "tuned": {"mg_sweeps": conf.mg_pre, "tile_planes": batch.tiles()[0],
+                             "coarse_cycle": "W" if batch.cycle() == 2 else "V",
                              "coarse_cells": batch.tiles()[1], "tune_s": tune_s,
                              "best_tune_ms": tuned_ms}},
         "wall_ms_per_step": float(np.median(wall_ms)),

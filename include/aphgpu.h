@@ -340,9 +340,14 @@ int aphgpu_batch_solve(aphgpu_batch* batch, const aphgpu_conf* conf, aphgpu_info
  * 4096; 0: only the coarsest level). */
 int aphgpu_batch_set_tiles(aphgpu_batch* batch, int planes, int coarse_cells);
 int aphgpu_batch_get_tiles(const aphgpu_batch* batch, int* planes, int* coarse_cells);
-/* Autotuner: times solves over the tile planes and the coarse-level size,
- * then over the smoothing sweeps; keeps the fastest tiling in the batch and
- * writes its sweeps into conf (mg_pre = mg_post); best_ms may be NULL. */
+/* Cycle of the per-domain coarse levels: 1 (default) V, 2 W (each level
+ * below the first per-domain level visited twice per visit of its parent). */
+int aphgpu_batch_set_cycle(aphgpu_batch* batch, int cycle);
+int aphgpu_batch_get_cycle(const aphgpu_batch* batch, int* cycle);
+/* Autotuner: times solves over the tile planes, the coarse-level size and
+ * the cycle, then over the smoothing sweeps; keeps the fastest tiling and
+ * cycle in the batch and writes its sweeps into conf (mg_pre = mg_post);
+ * best_ms may be NULL. */
 int aphgpu_batch_tune(aphgpu_batch* batch, aphgpu_conf* conf, double* best_ms);
 /* Device milliseconds of the last solve and kernels launched so far. */
 int aphgpu_batch_last_ms(const aphgpu_batch* batch, double* ms, int64_t* launches);

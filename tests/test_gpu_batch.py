@@ -131,10 +131,12 @@ def test_repeat_is_bit_identical_and_domains_stop_independently():
     batch.close()
 
 
-@pytest.mark.parametrize("planes,coarse_cells", [(1, 0), (2, 512), (8, 32768), (4, 10 ** 6)])
-def test_tilings_agree(planes, coarse_cells):
+@pytest.mark.parametrize("planes,coarse_cells,cycle", [(1, 0, 1), (2, 512, 2), (8, 32768, 1),
+                                                     (8, 32768, 2), (4, 10 ** 6, 2)])
+def test_tilings_agree(planes, coarse_cells, cycle):
     """Every tiling (planes per tile; coarse levels cycled per domain from
-    only the coarsest up to whole domains) converges to the same pressure."""
+    only the coarsest up to whole domains; V- or W-cycles there) converges
+    to the same pressure."""
     ctxs = _contexts(_domains())
     conf = _conf()
     ref = []
@@ -143,7 +145,8 @@ def test_tilings_agree(planes, coarse_cells):
         ref.append(ctx.get_solution())
     batch = _lib.Batch(ctxs)
     batch.set_tiles(planes, coarse_cells)
-    assert batch.tiles() == (planes, coarse_cells)
+    batch.set_cycle(cycle)
+    assert batch.tiles() == (planes, coarse_cells) and batch.cycle() == cycle
     infos = batch.solve(conf)
     for q, (ctx, info) in enumerate(zip(ctxs, infos)):
         assert info.converged, q
