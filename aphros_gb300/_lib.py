@@ -23,6 +23,7 @@ OPT_GRAPHS = 0
 OPT_FUSED_SWEEPS = 1
 OPT_HALF_COUPLINGS = 2
 OPT_CYCLE = 3
+OPT_COARSE_SERIES = 4
 
 K_SMOOTH32, K_SMOOTH64, K_APPLY64, K_APPLY32, K_RESTRICT32 = 0, 1, 2, 3, 4
 K_VOF_FLUX, K_VOF_UPDATE, K_RECONSTRUCT, K_HEIGHTS, K_CURVATURE = 5, 6, 7, 8, 9
@@ -308,7 +309,7 @@ class Context:
         return out
 
     def set_option(self, option, value):
-        """OPT_GRAPHS / OPT_FUSED_SWEEPS (aphgpu_set_option)."""
+        """One of the OPT_* execution options (aphgpu_set_option)."""
         self._check(self._L.aphgpu_set_option(self._p, option, int(value)))
 
     def mark(self, slot):

@@ -548,6 +548,14 @@ int aphgpu_set_option(aphgpu_ctx* ctx, int option, int value) {
       if (value < 0 || value > 2) return SetError(ctx, APHGPU_ERR_ARG, "cycle must be 0, 1 or 2");
       ctx->mg_gamma = value;
       return APHGPU_OK;
+    case APHGPU_OPT_COARSE_SERIES:
+      if (value < 0 || value > 100)
+        return SetError(ctx, APHGPU_ERR_ARG, "coarse series weight must be 0..100");
+      if (value != ctx->mg_series_pct) {
+        ctx->mg_series_pct = value;
+        ctx->mg.built64 = ctx->mg.built32 = false;  // rebuilt at the next solve
+      }
+      return APHGPU_OK;
     case APHGPU_OPT_HALF_COUPLINGS:
       ctx->use_half = value != 0;
       ctx->mg.built32 = false;  // rebuilt with or without them at the next solve

@@ -318,6 +318,7 @@ struct aphgpu_ctx {
   bool use_fused = false;  // fused out-of-place red-black sweeps (FP32 levels)
   bool use_half = false;   // FP16 couplings for the finest-level smoother
   int mg_gamma = 0;        // cycles of each level below the finest (1 V, 2 W, 0 auto)
+  int mg_series_pct = 60;  // weight (%) of the series couplings in the coarse operators
 
   // timing
   cudaEvent_t ev0 = nullptr, ev1 = nullptr;

@@ -670,38 +670,102 @@ __global__ void KToHalf(int64_t n, const float* __restrict__ w, __half* w16, flo
     w16[i] = __float2half_rn(w[i] * scale);
 }
 
-// Coarse operator: 0.5 * Galerkin with constant prolongation.
-// Coarse minus-face coupling = 0.5 * sum of the 4 fine minus-face
-// couplings; coarse diagonal = 0.5 * (sum of 8 fine diagonals + 2 * sum of
-// the 12 interior fine couplings).
+// Coupling of the minus face of coarse cell (I,J,K) along axis q, summed
+// over the 4 fine lines that cross the face.  Per line, a blend of two
+// estimates of the conductance between the two coarse centres:
+//   Galerkin: 0.5 * e_bc, the Galerkin coupling of constant prolongation
+//     scaled by one half (over-correction; exact for a constant
+//     coefficient);
+//   series: 1 / (0.5 / e_ab + 1 / e_bc + 0.5 / e_cd), the three fine
+//     couplings on the line in series (e_bc the fine face on the coarse
+//     face, e_ab and e_cd the fine faces inside the two coarse cells, each
+//     crossed over half its length).
+// Both equal e/2 where the three couplings are equal; across a density
+// jump the series value follows the weak side, the Galerkin value the
+// strong one.  `series` is the weight of the series value; lines whose
+// couplings are not all of one sign keep the Galerkin value.
+template <class T>
+__device__ double CoarseFace(const Op<T>& A, int q, int I, int J, int K, double series) {
+  const Dims& d = A.d;
+  const T* w = q == 0 ? A.w0 : (q == 1 ? A.w1 : A.w2);
+  double s = 0;
+  for (int m = 0; m < 4; ++m) {
+    const int u = m & 1, v = m >> 1;
+    int i = 2 * I, j = 2 * J, k = 2 * K;
+    if (q == 0) {
+      j += u;
+      k += v;
+    } else if (q == 1) {
+      i += u;
+      k += v;
+    } else {
+      i += u;
+      j += v;
+    }
+    int64_t cab, ccd;
+    if (q == 0) {
+      cab = d.idx(wrapm(i - 1, d.nx), j, k);
+      ccd = d.idx(i + 1, j, k);
+    } else if (q == 1) {
+      cab = d.idx(i, wrapm(j - 1, d.ny), k);
+      ccd = d.idx(i, j + 1, k);
+    } else {
+      cab = d.idx(i, j, wrapm(k - 1, d.nz));
+      ccd = d.idx(i, j, k + 1);
+    }
+    const double bc = (double)w[d.idx(i, j, k)];
+    double line = 0.5 * bc;
+    if (series > 0.0) {
+      const double ab = (double)w[cab], cd = (double)w[ccd];
+      const bool neg = ab < 0.0 && bc < 0.0 && cd < 0.0;
+      const bool pos = ab > 0.0 && bc > 0.0 && cd > 0.0;
+      if (neg || pos)
+        line = (1.0 - series) * line + series * (1.0 / (0.5 / ab + 1.0 / bc + 0.5 / cd));
+    }
+    s += line;
+  }
+  return s;
+}
+
+// Coarse operator of constant prolongation and summed restriction: face
+// couplings from CoarseFace; the diagonal is minus the sum of the six
+// coarse couplings plus half the summed diagonal shifts of the 8 children
+// (shift = diagonal + sum of the couplings; zero for flux-difference
+// systems, so the constant null space is kept).  With series = 0 this is
+// 0.5 * Galerkin.
 template <class T, class TC>
 __global__ void KCoarsenOp(Op<T> A, Dims dc, TC* w0, TC* w1, TC* w2, TC* diag,
-                           TC* invdiag) {
+                           TC* invdiag, double series) {
   const int I = blockIdx.x * kTileX + threadIdx.x;
   const int J = blockIdx.y * kTileY + threadIdx.y;
   const int kb = blockIdx.z * kTileZ;
   const int ke = min(kb + kTileZ, dc.nz);
   if (I >= dc.nx || J >= dc.ny) return;
   const Dims& d = A.d;
+  const int Ip = wrapp(I + 1, dc.nx), Jp = wrapp(J + 1, dc.ny);
   for (int K = kb; K < ke; ++K) {
-    double sw[3] = {0, 0, 0};
-    double sd = 0, sint = 0;
+    double shift = 0;
     for (int q = 0; q < 8; ++q) {
-      const int a = q & 1, bb = (q >> 1) & 1, cc = q >> 2;
-      const int i = 2 * I + a, j = 2 * J + bb, k = 2 * K + cc;
+      const int i = 2 * I + (q & 1), j = 2 * J + ((q >> 1) & 1), k = 2 * K + (q >> 2);
       const int64_t c = d.idx(i, j, k);
       T e[6];
       Couplings(A, i, j, k, c, e);
-      sd += (double)Diag(A, c, e);
-      if (a == 0) sw[0] += (double)e[0]; else sint += (double)e[0];
-      if (bb == 0) sw[1] += (double)e[2]; else sint += (double)e[2];
-      if (cc == 0) sw[2] += (double)e[4]; else sint += (double)e[4];
+      double row = (double)Diag(A, c, e);
+      for (int m = 0; m < 6; ++m) row += (double)e[m];
+      shift += row;
     }
+    const int Kp = wrapp(K + 1, dc.nz);
+    const double cx = CoarseFace(A, 0, I, J, K, series);
+    const double cy = CoarseFace(A, 1, I, J, K, series);
+    const double cz = CoarseFace(A, 2, I, J, K, series);
+    const double sum = cx + CoarseFace(A, 0, Ip, J, K, series) + cy +
+                       CoarseFace(A, 1, I, Jp, K, series) + cz +
+                       CoarseFace(A, 2, I, J, Kp, series);
     const int64_t C = dc.idx(I, J, K);
-    w0[C] = (TC)(0.5 * sw[0]);
-    w1[C] = (TC)(0.5 * sw[1]);
-    w2[C] = (TC)(0.5 * sw[2]);
-    const double dg = 0.5 * (sd + 2 * sint);
+    w0[C] = (TC)cx;
+    w1[C] = (TC)cy;
+    w2[C] = (TC)cz;
+    const double dg = 0.5 * shift - sum;
     diag[C] = (TC)dg;
     invdiag[C] = (TC)(1.0 / dg);
   }
@@ -989,6 +1053,9 @@ int ReadScalars(aphgpu_ctx* ctx, const SolveScalars* s, SolveScalars* out) {
   return APHGPU_OK;
 }
 
+// Weight of the series coupling in the coarse operators (KCoarsenOp).
+inline double CoarseSeries(const aphgpu_ctx* ctx) { return 0.01 * ctx->mg_series_pct; }
+
 // Coarsening: halve while all dimensions are even and the level has more
 // than `coarse_max` cells.
 std::vector<Dims> LevelDims(Dims d, int coarse_max) {
@@ -1180,7 +1247,8 @@ int BuildHierarchy<double>(aphgpu_ctx* ctx, std::vector<Level<double>>& lv,
   for (size_t l = 1; l < lv.size(); ++l) {
     const Op<double> A = MakeOp(lv[l - 1]);
     KCoarsenOp<double, double><<<TileGrid(lv[l].d), TileBlock(), 0, ctx->stream>>>(
-        A, lv[l].d, lv[l].w[0], lv[l].w[1], lv[l].w[2], lv[l].diag, lv[l].invdiag);
+        A, lv[l].d, lv[l].w[0], lv[l].w[1], lv[l].w[2], lv[l].diag, lv[l].invdiag,
+        CoarseSeries(ctx));
     APH_LAUNCHED(ctx);
   }
   APH_TRY(EnsureCoarsestScratch(ctx, lv.back().d.cells()));
@@ -1236,11 +1304,13 @@ int BuildHierarchy<float>(aphgpu_ctx* ctx, std::vector<Level<float>>& lv,
     if (l == 1) {
       const Op<double> A = FineOp(ctx);
       KCoarsenOp<double, float><<<TileGrid(lv[l].d), TileBlock(), 0, ctx->stream>>>(
-          A, lv[l].d, lv[l].w[0], lv[l].w[1], lv[l].w[2], lv[l].diag, lv[l].invdiag);
+          A, lv[l].d, lv[l].w[0], lv[l].w[1], lv[l].w[2], lv[l].diag, lv[l].invdiag,
+          CoarseSeries(ctx));
     } else {
       const Op<float> A = MakeOp(lv[l - 1]);
       KCoarsenOp<float, float><<<TileGrid(lv[l].d), TileBlock(), 0, ctx->stream>>>(
-          A, lv[l].d, lv[l].w[0], lv[l].w[1], lv[l].w[2], lv[l].diag, lv[l].invdiag);
+          A, lv[l].d, lv[l].w[0], lv[l].w[1], lv[l].w[2], lv[l].diag, lv[l].invdiag,
+          CoarseSeries(ctx));
     }
     APH_LAUNCHED(ctx);
   }

@@ -369,18 +369,26 @@ int aphgpu_batch_last_ms(const aphgpu_batch* batch, double* ms, int64_t* launche
  *                            finest FP32 level read an FP16 copy of the
  *                            couplings scaled by a power of two (the PCG
  *                            operator and the FP64 defect correction keep
- *                            FP32 / FP64: only the preconditioner changes;
- *                            about 1 % faster at 512^3); 0 (default): FP32
- *                            couplings
+ *                            FP32 / FP64: only the preconditioner changes,
+ *                            and its rounding can cost inner iterations);
+ *                            0 (default): FP32 couplings
  *   APHGPU_OPT_CYCLE         multigrid cycle below the finest level: 1
  *                            V-cycle, 2 W-cycle (each coarse level visited
  *                            twice per visit of the level above), 0
- *                            (default) W from 256^3 cells up, V below */
+ *                            (default) W from 256^3 cells up, V below
+ *   APHGPU_OPT_COARSE_SERIES weight in percent (0..100, default 60) of the
+ *                            series combination of the fine couplings in
+ *                            the coarse-level couplings; the rest is the
+ *                            Galerkin coupling of constant prolongation
+ *                            scaled by one half (0 = that operator alone).
+ *                            Changes the preconditioner only; the coarse
+ *                            operators are rebuilt at the next solve */
 enum {
   APHGPU_OPT_GRAPHS = 0,
   APHGPU_OPT_FUSED_SWEEPS = 1,
   APHGPU_OPT_HALF_COUPLINGS = 2,
-  APHGPU_OPT_CYCLE = 3
+  APHGPU_OPT_CYCLE = 3,
+  APHGPU_OPT_COARSE_SERIES = 4
 };
 int aphgpu_set_option(aphgpu_ctx* ctx, int option, int value);
 
