@@ -175,7 +175,7 @@ void aphgpu_conf_default(aphgpu_conf* c) {
   c->mg_pre = 2;
   c->mg_post = 2;
   c->mg_coarse_max = 64;
-  c->inner_rtol = 1e-3;
+  c->inner_rtol = 3e-4;
   c->inner_maxiter = 200;
   c->inner_flags = 3;
   c->rtol = 0;

@@ -209,7 +209,11 @@ __global__ void KBInnerInit(BDom* doms, int ndom, double inner_rtol, int inner_m
   const SolveScalars* so = D.so;
   SolveScalars z{};
   const double scale = so->maxr > 0 ? so->maxr : 1.0;
-  z.tol = inner_rtol * sqrt(so->rr / so->cellvol) / scale;
+  // inner_rtol, or only the reduction left to the outer tolerance (with a
+  // margin of 0.3) when that is less
+  double f = inner_rtol;
+  if (so->tol > 0 && so->residual > 0) f = fmax(f, fmin(0.5, 0.3 * so->tol / so->residual));
+  z.tol = f * sqrt(so->rr / so->cellvol) / scale;
   z.cellvol = so->cellvol;
   z.res_scale = 1.0;
   z.miniter = 1;

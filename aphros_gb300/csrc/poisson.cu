@@ -1863,6 +1863,16 @@ int SolveMGPCG32(aphgpu_ctx* ctx, const aphgpu_conf* conf, aphgpu_info* info) {
   return APHGPU_OK;
 }
 
+// Relative reduction asked of an inner FP32 solve when the outer residual
+// is `residual`: inner_rtol, or only what is left to reach the tolerance
+// (times a margin of 0.3 for the difference between the FP32 recursive
+// residual and the recomputed FP64 one) when that is less.
+inline double InnerReduction(const aphgpu_conf* conf, double residual) {
+  double f = conf->inner_rtol;
+  if (conf->tol > 0 && residual > 0) f = std::max(f, std::min(0.5, 0.3 * conf->tol / residual));
+  return f;
+}
+
 int SolveMixed(aphgpu_ctx* ctx, const aphgpu_conf* conf, aphgpu_info* info) {
   auto& mg = ctx->mg;
   const int64_t N = ctx->N;
@@ -1907,7 +1917,7 @@ int SolveMixed(aphgpu_ctx* ctx, const aphgpu_conf* conf, aphgpu_info* info) {
     APH_LAUNCHED(ctx);
     const double scale = hs.maxr > 0 ? hs.maxr : 1.0;
     const double r0 = std::sqrt(hs.rr / (ctx->h * ctx->h * ctx->h)) / scale;
-    ic.tol = conf->inner_rtol * r0;
+    ic.tol = InnerReduction(conf, hs.residual) * r0;
     ic.miniter = 1;
     ic.maxiter = conf->inner_maxiter;
     ic.maxnorm = 0;

@@ -59,7 +59,9 @@ typedef struct {
   int mg_pre;        /* red-black Gauss-Seidel sweeps before restriction */
   int mg_post;       /* sweeps after prolongation */
   int mg_coarse_max; /* largest coarsest-level cell count (<= 4096) */
-  /* mixed precision: relative reduction asked of each inner FP32 solve */
+  /* mixed precision: relative reduction asked of each inner FP32 solve
+   * (less when less is left to reach the tolerance: the reduction left
+   * times 0.3) */
   double inner_rtol;
   int inner_maxiter;
   /* inner FP32 PCG options: bit 0 keeps the residual free of the constant
@@ -84,7 +86,7 @@ typedef struct {
 } aphgpu_info;
 
 /* Fills `conf` with defaults: MG-PCG, tol 0, miniter 1, maxiter 1000,
- * L2 norm, 2+2 sweeps, coarsest <= 64 cells, inner_rtol 1e-3,
+ * L2 norm, 2+2 sweeps, coarsest <= 64 cells, inner_rtol 3e-4,
  * inner_maxiter 200, inner_flags 3 (projection and flexible beta). */
 void aphgpu_conf_default(aphgpu_conf* conf);
 
