@@ -548,6 +548,10 @@ int aphgpu_set_option(aphgpu_ctx* ctx, int option, int value) {
       if (value < 0 || value > 2) return SetError(ctx, APHGPU_ERR_ARG, "cycle must be 0, 1 or 2");
       ctx->mg_gamma = value;
       return APHGPU_OK;
+    case APHGPU_OPT_SWEEP_GROWTH:
+      if (value < 0 || value > 3) return SetError(ctx, APHGPU_ERR_ARG, "sweep growth must be 0..3");
+      ctx->mg_growth = value;
+      return APHGPU_OK;
     case APHGPU_OPT_COARSE_SERIES:
       if (value < 0 || value > 100)
         return SetError(ctx, APHGPU_ERR_ARG, "coarse series weight must be 0..100");

@@ -319,6 +319,7 @@ struct aphgpu_ctx {
   bool use_half = false;   // FP16 couplings for the finest-level smoother
   int mg_gamma = 0;        // cycles of each level below the finest (1 V, 2 W, 0 auto)
   int mg_series_pct = 60;  // weight (%) of the series couplings in the coarse operators
+  int mg_growth = 0;       // sweeps below the finest level (1 same, 2 linear, 3 doubling, 0 auto)
 
   // timing
   cudaEvent_t ev0 = nullptr, ev1 = nullptr;

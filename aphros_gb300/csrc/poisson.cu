@@ -682,67 +682,66 @@ __global__ void KToHalf(int64_t n, const float* __restrict__ w, __half* w16, flo
 //     crossed over half its length).
 // Both equal e/2 where the three couplings are equal; across a density
 // jump the series value follows the weak side, the Galerkin value the
-// strong one.  `series` is the weight of the series value; lines whose
-// couplings are not all of one sign keep the Galerkin value.
+// strong one.  `series` is the weight of the series value.  The series
+// factor t = series / e_bc = a c / (0.5 c + a c + 0.5 a), a = e_ab / e_bc,
+// c = e_cd / e_bc, is computed in FP32 (it only shapes the preconditioner;
+// FP64 division is slow on this GPU); lines whose couplings are not all of
+// one sign, or whose ratios do not fit FP32, keep the Galerkin value.
 template <class T>
 __device__ double CoarseFace(const Op<T>& A, int q, int I, int J, int K, double series) {
   const Dims& d = A.d;
   const T* w = q == 0 ? A.w0 : (q == 1 ? A.w1 : A.w2);
   double s = 0;
+#pragma unroll
   for (int m = 0; m < 4; ++m) {
     const int u = m & 1, v = m >> 1;
     int i = 2 * I, j = 2 * J, k = 2 * K;
+    int64_t cab, ccd;
     if (q == 0) {
       j += u;
       k += v;
-    } else if (q == 1) {
-      i += u;
-      k += v;
-    } else {
-      i += u;
-      j += v;
-    }
-    int64_t cab, ccd;
-    if (q == 0) {
       cab = d.idx(wrapm(i - 1, d.nx), j, k);
       ccd = d.idx(i + 1, j, k);
     } else if (q == 1) {
+      i += u;
+      k += v;
       cab = d.idx(i, wrapm(j - 1, d.ny), k);
       ccd = d.idx(i, j + 1, k);
     } else {
+      i += u;
+      j += v;
       cab = d.idx(i, j, wrapm(k - 1, d.nz));
       ccd = d.idx(i, j, k + 1);
     }
     const double bc = (double)w[d.idx(i, j, k)];
     double line = 0.5 * bc;
     if (series > 0.0) {
-      const double ab = (double)w[cab], cd = (double)w[ccd];
-      const bool neg = ab < 0.0 && bc < 0.0 && cd < 0.0;
-      const bool pos = ab > 0.0 && bc > 0.0 && cd > 0.0;
-      if (neg || pos)
-        line = (1.0 - series) * line + series * (1.0 / (0.5 / ab + 1.0 / bc + 0.5 / cd));
+      const float rb = 1.0f / (float)bc;
+      const float a = (float)w[cab] * rb, c = (float)w[ccd] * rb;
+      if (a > 0.0f && c > 0.0f) {
+        const float ac = a * c;
+        const float t = ac / (0.5f * c + ac + 0.5f * a);
+        if (t > 0.0f && t <= 1.0f) line = (1.0 - series) * line + series * (double)t * bc;
+      }
     }
     s += line;
   }
   return s;
 }
 
-// Coarse operator of constant prolongation and summed restriction: face
-// couplings from CoarseFace; the diagonal is minus the sum of the six
-// coarse couplings plus half the summed diagonal shifts of the 8 children
-// (shift = diagonal + sum of the couplings; zero for flux-difference
-// systems, so the constant null space is kept).  With series = 0 this is
-// 0.5 * Galerkin.
+// Coarse operator of constant prolongation and summed restriction, pass 1:
+// the three minus-face couplings of each coarse cell (CoarseFace) and, in
+// `diag`, half the summed diagonal shifts of its 8 children (shift =
+// diagonal + sum of the couplings; zero for flux-difference systems).
 template <class T, class TC>
-__global__ void KCoarsenOp(Op<T> A, Dims dc, TC* w0, TC* w1, TC* w2, TC* diag,
-                           TC* invdiag, double series) {
+__global__ void KCoarsenFaces(Op<T> A, Dims dc, TC* w0, TC* w1, TC* w2, TC* diag,
+                              double series) {
   const int I = blockIdx.x * kTileX + threadIdx.x;
   const int J = blockIdx.y * kTileY + threadIdx.y;
   const int kb = blockIdx.z * kTileZ;
   const int ke = min(kb + kTileZ, dc.nz);
   if (I >= dc.nx || J >= dc.ny) return;
   const Dims& d = A.d;
-  const int Ip = wrapp(I + 1, dc.nx), Jp = wrapp(J + 1, dc.ny);
   for (int K = kb; K < ke; ++K) {
     double shift = 0;
     for (int q = 0; q < 8; ++q) {
@@ -754,21 +753,37 @@ __global__ void KCoarsenOp(Op<T> A, Dims dc, TC* w0, TC* w1, TC* w2, TC* diag,
       for (int m = 0; m < 6; ++m) row += (double)e[m];
       shift += row;
     }
-    const int Kp = wrapp(K + 1, dc.nz);
-    const double cx = CoarseFace(A, 0, I, J, K, series);
-    const double cy = CoarseFace(A, 1, I, J, K, series);
-    const double cz = CoarseFace(A, 2, I, J, K, series);
-    const double sum = cx + CoarseFace(A, 0, Ip, J, K, series) + cy +
-                       CoarseFace(A, 1, I, Jp, K, series) + cz +
-                       CoarseFace(A, 2, I, J, Kp, series);
     const int64_t C = dc.idx(I, J, K);
-    w0[C] = (TC)cx;
-    w1[C] = (TC)cy;
-    w2[C] = (TC)cz;
-    const double dg = 0.5 * shift - sum;
-    diag[C] = (TC)dg;
-    invdiag[C] = (TC)(1.0 / dg);
+    w0[C] = (TC)CoarseFace(A, 0, I, J, K, series);
+    w1[C] = (TC)CoarseFace(A, 1, I, J, K, series);
+    w2[C] = (TC)CoarseFace(A, 2, I, J, K, series);
+    diag[C] = (TC)(0.5 * shift);
   }
+}
+
+// Pass 2: diagonal = half shift (from pass 1) minus the sum of the six
+// stored coarse couplings (so the row sums of the stored operator are the
+// shifts: the constant null space stays exact), and its inverse.
+template <class TC>
+__global__ void KCoarsenDiag(Op<TC> C, TC* diag, TC* invdiag) {
+  TILE_LOOP_BEGIN(C.d)
+  TC e[6];
+  Couplings(C, i, j, k, c, e);
+  double sum = 0;
+  for (int m = 0; m < 6; ++m) sum += (double)e[m];
+  const double dg = (double)diag[c] - sum;
+  diag[c] = (TC)dg;
+  invdiag[c] = (TC)(1.0 / dg);
+  TILE_LOOP_END
+}
+
+// Coarse level `lc` from the fine operator A (both passes).
+template <class T, class TC>
+void CoarsenOp(cudaStream_t st, const Op<T>& A, Level<TC>& lc, double series) {
+  KCoarsenFaces<T, TC><<<TileGrid(lc.d), TileBlock(), 0, st>>>(A, lc.d, lc.w[0], lc.w[1],
+                                                                lc.w[2], lc.diag, series);
+  const Op<TC> C{lc.d, lc.w[0], lc.w[1], lc.w[2], nullptr};
+  KCoarsenDiag<TC><<<TileGrid(lc.d), TileBlock(), 0, st>>>(C, lc.diag, lc.invdiag);
 }
 
 template <class TS, class TD>
@@ -1053,7 +1068,7 @@ int ReadScalars(aphgpu_ctx* ctx, const SolveScalars* s, SolveScalars* out) {
   return APHGPU_OK;
 }
 
-// Weight of the series coupling in the coarse operators (KCoarsenOp).
+// Weight of the series coupling in the coarse operators (CoarseFace).
 inline double CoarseSeries(const aphgpu_ctx* ctx) { return 0.01 * ctx->mg_series_pct; }
 
 // Coarsening: halve while all dimensions are even and the level has more
@@ -1246,9 +1261,8 @@ int BuildHierarchy<double>(aphgpu_ctx* ctx, std::vector<Level<double>>& lv,
   f.invdiag = ctx->invdiag;
   for (size_t l = 1; l < lv.size(); ++l) {
     const Op<double> A = MakeOp(lv[l - 1]);
-    KCoarsenOp<double, double><<<TileGrid(lv[l].d), TileBlock(), 0, ctx->stream>>>(
-        A, lv[l].d, lv[l].w[0], lv[l].w[1], lv[l].w[2], lv[l].diag, lv[l].invdiag,
-        CoarseSeries(ctx));
+    CoarsenOp<double, double>(ctx->stream, A, lv[l], CoarseSeries(ctx));
+    ctx->launches += 1;  // two kernels
     APH_LAUNCHED(ctx);
   }
   APH_TRY(EnsureCoarsestScratch(ctx, lv.back().d.cells()));
@@ -1303,15 +1317,12 @@ int BuildHierarchy<float>(aphgpu_ctx* ctx, std::vector<Level<float>>& lv,
     // coarse operators from the FP64 fine operator at level 1, FP32 below
     if (l == 1) {
       const Op<double> A = FineOp(ctx);
-      KCoarsenOp<double, float><<<TileGrid(lv[l].d), TileBlock(), 0, ctx->stream>>>(
-          A, lv[l].d, lv[l].w[0], lv[l].w[1], lv[l].w[2], lv[l].diag, lv[l].invdiag,
-          CoarseSeries(ctx));
+      CoarsenOp<double, float>(ctx->stream, A, lv[l], CoarseSeries(ctx));
     } else {
       const Op<float> A = MakeOp(lv[l - 1]);
-      KCoarsenOp<float, float><<<TileGrid(lv[l].d), TileBlock(), 0, ctx->stream>>>(
-          A, lv[l].d, lv[l].w[0], lv[l].w[1], lv[l].w[2], lv[l].diag, lv[l].invdiag,
-          CoarseSeries(ctx));
+      CoarsenOp<float, float>(ctx->stream, A, lv[l], CoarseSeries(ctx));
     }
+    ctx->launches += 1;  // two kernels
     APH_LAUNCHED(ctx);
   }
   APH_TRY(EnsureCoarsestScratch(ctx, lv.back().d.cells()));
@@ -1488,6 +1499,27 @@ inline int CycleGamma(const aphgpu_ctx* ctx) {
   return ctx->N >= (int64_t)256 * 256 * 256 ? 2 : 1;
 }
 
+// Growth of the smoothing sweeps below the finest level: the context's
+// choice (1 none, 2 linear, 3 doubling), or linear for V-cycles on grids of
+// at least 256^3 cells and none otherwise (the extra coarse sweeps are
+// cheap next to the finest level there; on small grids their launches cost
+// more than the iterations they save, and W-cycles multiply them).
+inline int SweepGrowth(const aphgpu_ctx* ctx) {
+  if (ctx->mg_growth >= 1 && ctx->mg_growth <= 3) return ctx->mg_growth;
+  return CycleGamma(ctx) == 1 && ctx->N >= (int64_t)256 * 256 * 256 ? 2 : 1;
+}
+
+// Smoothing sweeps on level l for a configured count n: n on the finest
+// level; below it n (growth 1), n * (l + 1) (growth 2, a variable V-cycle
+// in the sense of Bramble, Pasciak and Xu) or n * 2^l up to 16 (growth 3).
+// More coarse sweeps make the coarse-grid correction more accurate.
+inline int LevelSweeps(const aphgpu_ctx* ctx, int n, int l) {
+  const int g = SweepGrowth(ctx);
+  if (g == 2) return n * (l + 1);
+  if (g == 3) return n > 0 ? std::min(n << std::min(l, 4), std::max(n, 16)) : 0;
+  return n;
+}
+
 // Multigrid cycle from level l: pre-smoothing (from a zero guess on the
 // level's first visit of the cycle, else from its current x), restriction
 // of the residual, `gamma` cycles of level l+1 (1 from the finest level;
@@ -1515,15 +1547,16 @@ int CycleLevel(aphgpu_ctx* ctx, std::vector<Level<T>>& lv, int l, bool first, in
   }
   Level<T>& f = lv[l];
   const Op<T> A = MakeOp(f);
-  const int fused = pre > 0 ? FusedSweeps<T>(ctx, f, A, pre, 0, first, s) : kNotFused;
+  const int np = LevelSweeps(ctx, pre, l), nq = LevelSweeps(ctx, post, l);
+  const int fused = np > 0 ? FusedSweeps<T>(ctx, f, A, np, 0, first, s) : kNotFused;
   if (fused != kNotFused) APH_TRY(fused);
-  for (int sw = 0; fused == kNotFused && sw < pre; ++sw) {
+  for (int sw = 0; fused == kNotFused && sw < np; ++sw) {
     LaunchSmooth<T>(ctx, f, A, 0, first && sw == 0, s);
     APH_LAUNCHED(ctx);
     LaunchSmooth<T>(ctx, f, A, 1, 0, s);
     APH_LAUNCHED(ctx);
   }
-  if (pre == 0 && first) {
+  if (np == 0 && first) {
     LaunchSmooth<T>(ctx, f, A, 0, 1, s);
     APH_LAUNCHED(ctx);
     LaunchSmooth<T>(ctx, f, A, 1, 1, s);
@@ -1535,9 +1568,9 @@ int CycleLevel(aphgpu_ctx* ctx, std::vector<Level<T>>& lv, int l, bool first, in
   for (int g = 0; g < gamma; ++g) APH_TRY(CycleLevel<T>(ctx, lv, l + 1, g == 0, pre, post, s));
   LaunchProlong<T>(ctx, f, lv[l + 1], s);
   APH_LAUNCHED(ctx);
-  const int fused2 = post > 0 ? FusedSweeps<T>(ctx, f, A, post, 1, false, s) : kNotFused;
+  const int fused2 = nq > 0 ? FusedSweeps<T>(ctx, f, A, nq, 1, false, s) : kNotFused;
   if (fused2 != kNotFused) APH_TRY(fused2);
-  for (int sw = 0; fused2 == kNotFused && sw < post; ++sw) {
+  for (int sw = 0; fused2 == kNotFused && sw < nq; ++sw) {
     LaunchSmooth<T>(ctx, f, A, 1, 0, s);
     APH_LAUNCHED(ctx);
     LaunchSmooth<T>(ctx, f, A, 0, 0, s);
@@ -1616,6 +1649,7 @@ int Pcg(aphgpu_ctx* ctx, const Op<T>& A, Precond precond, T* x, T* r, T* p,
     key = Mix(key, (uint64_t)sizeof(T));
     key = Mix(key, (uint64_t)(ctx->use_fused ? 1 : 0));
     key = Mix(key, (uint64_t)CycleGamma(ctx));
+    key = Mix(key, (uint64_t)SweepGrowth(ctx));
     // the FP16 coupling scale is a kernel argument: part of the key
     float hs = ctx->mg.l32.empty() ? 0.f : ctx->mg.l32[0].hscale;
     uint32_t hb;

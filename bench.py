@@ -450,8 +450,9 @@ def run_ours(args):
                    "grid": [case.n] * 3, "bubbles": int(len(case.radii)),
                    "density_ratio": case.rho1 / case.rho2,
                    "l2": "inputs larger than L2 (1 GB per FP64 field), no flush",
-                   "multigrid": "V-cycle, RB Gauss-Seidel 2+2, coarse couplings 60 % series "
-                                "+ 40 % half-Galerkin (library defaults)",
+                   "multigrid": "V-cycle, RB Gauss-Seidel 2+2 on the finest level and "
+                                "2(l+1)+2(l+1) on level l below it, coarse couplings 60 % "
+                                "series + 40 % half-Galerkin (library defaults)",
                    "parallelism": "replicas" if world > 1 else "single GPU"},
         "p50_ms": float(np.percentile(lat, 50)), "p99_ms": float(np.percentile(lat, 99)),
         "fp64": {"value": fp64_value, "unit": UNIT,

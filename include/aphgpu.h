@@ -384,13 +384,19 @@ int aphgpu_batch_last_ms(const aphgpu_batch* batch, double* ms, int64_t* launche
  *                            Galerkin coupling of constant prolongation
  *                            scaled by one half (0 = that operator alone).
  *                            Changes the preconditioner only; the coarse
- *                            operators are rebuilt at the next solve */
+ *                            operators are rebuilt at the next solve
+ *   APHGPU_OPT_SWEEP_GROWTH  smoothing sweeps on level l below the finest
+ *                            (mg_pre / mg_post on the finest): 1 the same
+ *                            count, 2 count * (l + 1), 3 count * 2^l (at
+ *                            most 16), 0 (default) 2 for V-cycles from
+ *                            256^3 cells up and 1 otherwise */
 enum {
   APHGPU_OPT_GRAPHS = 0,
   APHGPU_OPT_FUSED_SWEEPS = 1,
   APHGPU_OPT_HALF_COUPLINGS = 2,
   APHGPU_OPT_CYCLE = 3,
-  APHGPU_OPT_COARSE_SERIES = 4
+  APHGPU_OPT_COARSE_SERIES = 4,
+  APHGPU_OPT_SWEEP_GROWTH = 5
 };
 int aphgpu_set_option(aphgpu_ctx* ctx, int option, int value);
 

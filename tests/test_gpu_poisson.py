@@ -305,3 +305,32 @@ def test_coarse_series_weight(solver):
     for bad in (-1, 101):
         with pytest.raises(_lib.AphgpuError):
             ctx.set_option(_lib.OPT_COARSE_SERIES, bad)
+
+
+@pytest.mark.parametrize("cycle", [1, 2])
+def test_sweep_growth(cycle):
+    """More smoothing sweeps below the finest level (APHGPU_OPT_SWEEP_GROWTH)
+    change only the preconditioner: every growth reaches the tolerance with
+    the same pressure, and with V-cycles the linear growth needs fewer
+    iterations than none."""
+    case = workload.config("c3", n=128)
+    ctx = _lib.Context(case.n, case.h)
+    ctx.assemble_projection(case.alpha, case.rho1, case.rho2, case.flux, case.dt)
+    ctx.set_option(_lib.OPT_CYCLE, cycle)
+    _, bn = ctx.residual_norms()
+    tol = 1e-10 * bn / math.sqrt(case.h ** 3)
+    out = {}
+    for growth in (1, 2, 3, 0):
+        ctx.set_option(_lib.OPT_SWEEP_GROWTH, growth)
+        for solver in (_lib.SOLVER_MGPCG, _lib.SOLVER_MIXED):
+            x, info = ctx.solve(_lib.default_conf(solver=solver, tol=tol, maxiter=300))
+            rn, bn2 = ctx.residual_norms()
+            assert info.converged and rn / bn2 <= 1.01e-10, (growth, solver)
+            out[(growth, solver)] = (x, info.iter if solver == _lib.SOLVER_MGPCG else info.inner_iter)
+    ref = out[(1, _lib.SOLVER_MGPCG)][0]
+    for key, (x, _) in out.items():
+        assert rel_l2(x, ref) < 1e-7, key
+    if cycle == 1:
+        assert out[(2, _lib.SOLVER_MGPCG)][1] < out[(1, _lib.SOLVER_MGPCG)][1]
+    with pytest.raises(_lib.AphgpuError):
+        ctx.set_option(_lib.OPT_SWEEP_GROWTH, 4)
