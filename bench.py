@@ -735,6 +735,7 @@ def run_profile(args):
     tol = 1e-10 * bnorm / math.sqrt(case.h ** 3)
     solver = _lib.SOLVER_MGPCG if args.profile == "fp64" else _lib.SOLVER_MIXED
     conf = _lib.default_conf(solver=solver, tol=tol)
+    ctx.set_option(_lib.OPT_CYCLE, args.cycle)
     if args.profile == "vof":
         # one solve, the corrected fluxes, then `warmup` + `steps` PLIC steps
         # with the height curvature after each
@@ -767,6 +768,8 @@ def main():
     ap.add_argument("--no-vof", action="store_true",
                     help="skip the PLIC advection + curvature measurement")
     ap.add_argument("--cpu-budget", type=float, default=15.0)
+    ap.add_argument("--cycle", type=int, choices=[0, 1, 2], default=0,
+                    help="--profile: multigrid cycle (0 library default, 1 V, 2 W)")
     ap.add_argument("--profile", choices=["mixed", "fp64", "batch", "vof"], default=None,
                     help="profiling run: assemble, then `steps` solves of one solver "
                          "after `warmup` solves, no other work and no output line")
