@@ -297,6 +297,19 @@ def measure_vof(ctx, case, peak, peak_kind, steps, cpu=True):
 
 
 # ---------------------------------------------------------------------------
+# The configuration's V-cycle: one red-black sweep before and after the
+# coarse correction on the finest level, and twice as many on each coarser
+# level (at most 16), the shape that is fastest at 512^3 (finest-level
+# sweeps dominate the cost; coarse ones are cheap and improve the coarse
+# correction).  Library defaults otherwise.
+HEADLINE_MG = {"mg_pre": 1, "mg_post": 1}
+
+
+def set_headline_cycle(ctx, _lib):
+    ctx.set_option(_lib.OPT_CYCLE, 1)
+    ctx.set_option(_lib.OPT_SWEEP_GROWTH, 3)
+
+
 # arms
 # ---------------------------------------------------------------------------
 
@@ -316,11 +329,11 @@ def run_ours(args):
     ctx.assemble_projection(case.alpha, case.rho1, case.rho2, case.flux, case.dt)
     # the configuration's V-cycles; the W-cycle (library default at this
     # size) is measured beside them
-    ctx.set_option(_lib.OPT_CYCLE, 1)
+    set_headline_cycle(ctx, _lib)
     _, bnorm = ctx.residual_norms()
     tol = 1e-10 * bnorm / math.sqrt(case.h ** 3)
-    conf_mixed = _lib.default_conf(solver=_lib.SOLVER_MIXED, tol=tol, maxiter=100)
-    conf_fp64 = _lib.default_conf(solver=_lib.SOLVER_MGPCG, tol=tol, maxiter=1000)
+    conf_mixed = _lib.default_conf(solver=_lib.SOLVER_MIXED, tol=tol, maxiter=100, **HEADLINE_MG)
+    conf_fp64 = _lib.default_conf(solver=_lib.SOLVER_MGPCG, tol=tol, maxiter=1000, **HEADLINE_MG)
 
     def run_steps(conf, k, collect):
         times, launches, infos = [], 0, []
@@ -362,15 +375,19 @@ def run_ours(args):
     # the same solves with W-cycles below the finest level
     w_cycle = None
     if not args.no_w_cycle:
-        ctx.set_option(_lib.OPT_CYCLE, 2)
+        # library defaults: W below the finest level, 2+2 sweeps on every level
+        ctx.set_option(_lib.OPT_CYCLE, 0)
+        ctx.set_option(_lib.OPT_SWEEP_GROWTH, 0)
+        conf_mixed_w = _lib.default_conf(solver=_lib.SOLVER_MIXED, tol=tol, maxiter=100)
+        conf_fp64_w = _lib.default_conf(solver=_lib.SOLVER_MGPCG, tol=tol, maxiter=1000)
         kw = max(1, min(args.steps, 5))
-        run_steps(conf_mixed, 1, False)
-        run_steps(conf_fp64, 1, False)
-        tw, stw, _, infw = run_steps(conf_mixed, kw, True)
+        run_steps(conf_mixed_w, 1, False)
+        run_steps(conf_fp64_w, 1, False)
+        tw, stw, _, infw = run_steps(conf_mixed_w, kw, True)
         rnw, bnw = ctx.residual_norms()
         pw = ctx.get_solution()
-        tw64, _, _, infw64 = run_steps(conf_fp64, kw, True)
-        ctx.set_option(_lib.OPT_CYCLE, 1)
+        tw64, _, _, infw64 = run_steps(conf_fp64_w, kw, True)
+        set_headline_cycle(ctx, _lib)
         uw, tmw = aggregate_over_ranks(kw, tw / 1000.0)
         uw64, tmw64 = aggregate_over_ranks(kw, tw64 / 1000.0)
         w_cycle = {"value": uw / tmw, "unit": UNIT, "ms_per_step": float(tw / kw),
@@ -450,9 +467,10 @@ def run_ours(args):
                    "grid": [case.n] * 3, "bubbles": int(len(case.radii)),
                    "density_ratio": case.rho1 / case.rho2,
                    "l2": "inputs larger than L2 (1 GB per FP64 field), no flush",
-                   "multigrid": "V-cycle, RB Gauss-Seidel 2+2 on the finest level and "
-                                "2(l+1)+2(l+1) on level l below it, coarse couplings 60 % "
-                                "series + 40 % half-Galerkin (library defaults)",
+                   "multigrid": "V-cycle, red-black Gauss-Seidel 1+1 on the finest level "
+                                "and 2^l+2^l (at most 16) on level l below it, coarse "
+                                "couplings 60 % series + 40 % half-Galerkin; w_cycle: "
+                                "library defaults (W below the finest level, 2+2 sweeps)",
                    "parallelism": "replicas" if world > 1 else "single GPU"},
         "p50_ms": float(np.percentile(lat, 50)), "p99_ms": float(np.percentile(lat, 99)),
         "fp64": {"value": fp64_value, "unit": UNIT,
@@ -734,8 +752,13 @@ def run_profile(args):
     _, bnorm = ctx.residual_norms()
     tol = 1e-10 * bnorm / math.sqrt(case.h ** 3)
     solver = _lib.SOLVER_MGPCG if args.profile == "fp64" else _lib.SOLVER_MIXED
-    conf = _lib.default_conf(solver=solver, tol=tol)
-    ctx.set_option(_lib.OPT_CYCLE, args.cycle)
+    if args.cycle == 1:
+        # the configuration's V-cycle (as in the headline)
+        set_headline_cycle(ctx, _lib)
+        conf = _lib.default_conf(solver=solver, tol=tol, **HEADLINE_MG)
+    else:
+        ctx.set_option(_lib.OPT_CYCLE, args.cycle)
+        conf = _lib.default_conf(solver=solver, tol=tol)
     if args.profile == "vof":
         # one solve, the corrected fluxes, then `warmup` + `steps` PLIC steps
         # with the height curvature after each
@@ -769,7 +792,8 @@ def main():
                     help="skip the PLIC advection + curvature measurement")
     ap.add_argument("--cpu-budget", type=float, default=15.0)
     ap.add_argument("--cycle", type=int, choices=[0, 1, 2], default=0,
-                    help="--profile: multigrid cycle (0 library default, 1 V, 2 W)")
+                    help="--profile: 1 the headline's V-cycle configuration, 2 W, 0 "
+                         "library default")
     ap.add_argument("--profile", choices=["mixed", "fp64", "batch", "vof"], default=None,
                     help="profiling run: assemble, then `steps` solves of one solver "
                          "after `warmup` solves, no other work and no output line")
