@@ -359,13 +359,15 @@ int aphgpu_solve_resident(aphgpu_ctx* ctx, const aphgpu_conf* conf, int zero_gue
   conf = &cf;
   Timer t(ctx);
   int rc;
+  ctx->x_zero = zero_guess != 0;
   switch (conf->solver) {
     case APHGPU_SOLVER_CG: rc = SolveCG(ctx, conf, info); break;
     case APHGPU_SOLVER_MGPCG: rc = SolveMGPCG(ctx, conf, info); break;
     case APHGPU_SOLVER_MIXED: rc = SolveMixed(ctx, conf, info); break;
     case APHGPU_SOLVER_MGPCG32: rc = SolveMGPCG32(ctx, conf, info); break;
-    default: return SetError(ctx, APHGPU_ERR_ARG, "unknown solver %d", conf->solver);
+    default: ctx->x_zero = false; return SetError(ctx, APHGPU_ERR_ARG, "unknown solver %d", conf->solver);
   }
+  ctx->x_zero = false;
   t.Stop();
   return rc;
 }

@@ -131,16 +131,20 @@ __global__ void KBResidual64(const BDom* __restrict__ doms, const BTile* __restr
   const int op[3] = {0, 1, 0};
   const double* x = D.x64;
   BT_CELLS_BEGIN(d, w, VEC ? D.lv[0].tx : kTileX)
-  double e[6];
-  Couplings(A, i, j, k, c, e);
-  const double e0 = Diag(A, c, e);
-  double u = x[c] * e0 + (-D.b64[c]);
-  u += x[d.idx(wrapm(i - 1, d.nx), j, k)] * e[0];
-  u += x[d.idx(wrapp(i + 1, d.nx), j, k)] * e[1];
-  u += x[d.idx(i, wrapm(j - 1, d.ny), k)] * e[2];
-  u += x[d.idx(i, wrapp(j + 1, d.ny), k)] * e[3];
-  u += x[d.idx(i, j, wrapm(k - 1, d.nz))] * e[4];
-  u += x[d.idx(i, j, wrapp(k + 1, d.nz))] * e[5];
+  // the first outer residual is that of the zero initial guess: r = b
+  double u = -D.b64[c];
+  if (!first) {
+    double e[6];
+    Couplings(A, i, j, k, c, e);
+    const double e0 = Diag(A, c, e);
+    u = x[c] * e0 + (-D.b64[c]);
+    u += x[d.idx(wrapm(i - 1, d.nx), j, k)] * e[0];
+    u += x[d.idx(wrapp(i + 1, d.nx), j, k)] * e[1];
+    u += x[d.idx(i, wrapm(j - 1, d.ny), k)] * e[2];
+    u += x[d.idx(i, wrapp(j + 1, d.ny), k)] * e[3];
+    u += x[d.idx(i, j, wrapm(k - 1, d.nz))] * e[4];
+    u += x[d.idx(i, j, wrapp(k + 1, d.nz))] * e[5];
+  }
   const double rv = -u;
   D.r64[c] = rv;
   v[0] += rv * rv;
@@ -907,7 +911,7 @@ int BuildTables(aphgpu_batch* B, const aphgpu_conf* conf) {
       L.vec = BVec(lv[l].d) && (l == 0 || l < D.lc) ? 1 : 0;
       L.tx = L.vec ? TxOf(lv[l].d.nx / 4) : kTileX;
     }
-    D.A64 = Op<double>{c->d, c->w[0], c->w[1], c->w[2], c->diag_explicit ? c->diag : nullptr};
+    D.A64 = Op<double>{c->d, c->w[0], c->w[1], c->w[2], c->diag_valid ? c->diag : nullptr};
     D.b64 = c->b;
     D.x64 = c->x;
     D.r64 = c->r;

@@ -252,6 +252,8 @@ struct aphgpu_ctx {
   double* w[3] = {nullptr, nullptr, nullptr};
   double* diag = nullptr;      // NULL: diagonal = -(e1+...+e6) in order
   bool diag_explicit = false;
+  bool diag_valid = false;  // `diag` holds the FP64 diagonal (explicit or computed)
+  bool x_zero = false;      // x was zeroed for the solve being run
   double* invdiag = nullptr;   // 1/diagonal (multigrid smoother)
   double* b = nullptr;
   bool has_system = false;
