@@ -18,8 +18,16 @@ class SolverGpu : public Solver<M> {
   using Conf = typename Base::Conf;
   using Info = typename Base::Info;
 
-  SolverGpu(const Conf& conf, int kind, int maxnorm, const M& m)
-      : Base(conf), kind_(kind), maxnorm_(maxnorm) {
+  // Optional multigrid settings (gpu_<prefix>_* variables); negative or
+  // zero values keep the library defaults.
+  struct Tuning {
+    int mg_pre = -1, mg_post = -1, inner_maxiter = -1;
+    double inner_rtol = -1;
+    int cycle = 0, sweep_growth = 0, coarse_series = -1;
+  };
+
+  SolverGpu(const Conf& conf, int kind, int maxnorm, const Tuning& tuning, const M& m)
+      : Base(conf), kind_(kind), maxnorm_(maxnorm), tuning_(tuning) {
     if (m.IsLead()) {
       shared_obj_ = std::make_unique<Shared>();
       shared_ = shared_obj_.get();
@@ -66,6 +74,15 @@ class SolverGpu : public Solver<M> {
         const auto h = ms.GetCellSize();
         fassert(h[0] == h[1] && h[1] == h[2], "gpu solver: cubic cells only");
         fassert_equal(aphgpu_create(&s.ctx, gs[0], gs[1], gs[2], h[0], 0), APHGPU_OK);
+        fassert_equal(aphgpu_set_option(s.ctx, APHGPU_OPT_CYCLE, tuning_.cycle), APHGPU_OK);
+        fassert_equal(
+            aphgpu_set_option(s.ctx, APHGPU_OPT_SWEEP_GROWTH, tuning_.sweep_growth),
+            APHGPU_OK);
+        if (tuning_.coarse_series >= 0) {
+          fassert_equal(
+              aphgpu_set_option(s.ctx, APHGPU_OPT_COARSE_SERIES, tuning_.coarse_series),
+              APHGPU_OK);
+        }
       }
       int rc = aphgpu_set_system_expr(s.ctx, s.expr.data());
       aphgpu_conf c;
@@ -75,6 +92,10 @@ class SolverGpu : public Solver<M> {
       c.miniter = this->conf.miniter;
       c.maxiter = this->conf.maxiter;
       c.maxnorm = maxnorm_;
+      if (tuning_.mg_pre >= 0) c.mg_pre = tuning_.mg_pre;
+      if (tuning_.mg_post >= 0) c.mg_post = tuning_.mg_post;
+      if (tuning_.inner_maxiter > 0) c.inner_maxiter = tuning_.inner_maxiter;
+      if (tuning_.inner_rtol > 0) c.inner_rtol = tuning_.inner_rtol;
       aphgpu_info info;
       if (rc == APHGPU_OK)
         rc = aphgpu_solve(s.ctx, &c, fc_init ? s.x0.data() : nullptr, s.x.data(), &info);
@@ -98,6 +119,7 @@ class SolverGpu : public Solver<M> {
   };
   int kind_;
   int maxnorm_;
+  Tuning tuning_;
   std::unique_ptr<Shared> shared_obj_;  // lead block only
   Shared* shared_ = nullptr;
 };
@@ -112,8 +134,17 @@ class ModuleLinearGpu : public ModuleLinear<M> {
   std::unique_ptr<Solver<M>> Make(
       const Vars& var, std::string prefix, const M& m) override {
     const int maxnorm = var.Int["linsolver_" + prefix + "_maxnorm"];
+    const std::string g = "gpu_" + prefix + "_";
+    typename SolverGpu<M>::Tuning t;
+    t.mg_pre = var.Int(g + "mg_pre", -1);
+    t.mg_post = var.Int(g + "mg_post", -1);
+    t.inner_maxiter = var.Int(g + "inner_maxiter", -1);
+    t.inner_rtol = var.Double(g + "inner_rtol", -1.);
+    t.cycle = var.Int(g + "cycle", 0);
+    t.sweep_growth = var.Int(g + "sweep_growth", 0);
+    t.coarse_series = var.Int(g + "coarse_series", -1);
     return std::make_unique<SolverGpu<M>>(
-        this->GetConf(var, prefix), Kind, maxnorm, m);
+        this->GetConf(var, prefix), Kind, maxnorm, t, m);
   }
 };
 

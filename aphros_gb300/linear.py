@@ -67,6 +67,11 @@ class Solver:
         raise NotImplementedError
 
 
+# gpu_<prefix>_<name> variables that set context options (aphgpu_set_option)
+_OPTIONS = {"cycle": _lib.OPT_CYCLE, "sweep_growth": _lib.OPT_SWEEP_GROWTH,
+            "coarse_series": _lib.OPT_COARSE_SERIES}
+
+
 class SolverGpu(Solver):
     """Drop-in `linsolver_symm gpu*`: the device state lives in a context
     keyed by the mesh size, like SolverConjugateCL::Shared
@@ -79,7 +84,7 @@ class SolverGpu(Solver):
     non-symmetric system raises AphgpuError(ERR_NOT_SYMMETRIC).
     """
 
-    def __init__(self, conf, kind="gpu", residual_max=False, device=0, **mg):
+    def __init__(self, conf, kind="gpu", residual_max=False, device=0, options=None, **mg):
         super().__init__(conf)
         if kind not in _KINDS:
             raise ValueError("unknown solver kind '%s'" % kind)
@@ -87,6 +92,8 @@ class SolverGpu(Solver):
         self.residual_max = residual_max
         self.device = device
         self.mg = mg
+        # context options by name: cycle, sweep_growth, coarse_series
+        self.options = dict(options or {})
         self._ctx = None
 
     def context(self, m):
@@ -94,6 +101,8 @@ class SolverGpu(Solver):
             if self._ctx is not None:
                 self._ctx.close()
             self._ctx = _lib.Context(m.n, m.h, self.device)
+            for name, value in self.options.items():
+                self._ctx.set_option(_OPTIONS[name], value)
         return self._ctx
 
     def native_conf(self):
@@ -153,9 +162,14 @@ class ModuleLinearGpu(ModuleLinear):
         v = var.get("gpu_%s_inner_rtol" % prefix)
         if v is not None:
             extra["inner_rtol"] = float(v)
+        options = {}
+        for key in _OPTIONS:
+            v = var.get("gpu_%s_%s" % (prefix, key))
+            if v is not None:
+                options[key] = int(v)
         return SolverGpu(self.GetConf(var, prefix), kind=self.name,
                          residual_max=bool(int(var.get("linsolver_%s_maxnorm" % prefix, 0))),
-                         **extra)
+                         options=options, **extra)
 
 
 for _name in _KINDS:

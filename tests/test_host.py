@@ -14,7 +14,8 @@ def test_registry_mirrors_linsolver_symm():
     assert linear.ModuleLinear.GetInstance("conjugate") is None
     var = {"linsolver_symm": "gpu_mixed", "hypre_symm_tol": "1e-8",
            "hypre_symm_maxiter": "50", "linsolver_symm_maxnorm": "1",
-           "gpu_symm_mg_pre": "3", "gpu_symm_inner_rtol": "1e-3"}
+           "gpu_symm_mg_pre": "3", "gpu_symm_inner_rtol": "1e-3",
+           "gpu_symm_cycle": "1", "gpu_symm_sweep_growth": "3"}
     s = linear.MakeLinearSolver(var, "symm", linear.Mesh(16, 1 / 16))
     assert isinstance(s, linear.SolverGpu)
     assert s.kind == "gpu_mixed"
@@ -22,6 +23,7 @@ def test_registry_mirrors_linsolver_symm():
     assert s.GetConf().miniter == 0  # ModuleLinear::GetConf default
     assert s.residual_max
     assert s.mg == {"mg_pre": 3, "inner_rtol": 1e-3}
+    assert s.options == {"cycle": 1, "sweep_growth": 3}
     with pytest.raises(RuntimeError):
         linear.MakeLinearSolver({"linsolver_symm": "hypre"}, "symm", None)
 
