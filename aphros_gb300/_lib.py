@@ -25,6 +25,7 @@ OPT_HALF_COUPLINGS = 2
 OPT_CYCLE = 3
 OPT_COARSE_SERIES = 4
 OPT_SWEEP_GROWTH = 5
+OPT_CTA_COARSE = 6
 
 K_SMOOTH32, K_SMOOTH64, K_APPLY64, K_APPLY32, K_RESTRICT32 = 0, 1, 2, 3, 4
 K_VOF_FLUX, K_VOF_UPDATE, K_RECONSTRUCT, K_HEIGHTS, K_CURVATURE = 5, 6, 7, 8, 9

@@ -550,6 +550,7 @@ int aphgpu_set_option(aphgpu_ctx* ctx, int option, int value) {
       if (value < 0 || value > 2) return SetError(ctx, APHGPU_ERR_ARG, "cycle must be 0, 1 or 2");
       ctx->mg_gamma = value;
       return APHGPU_OK;
+    case APHGPU_OPT_CTA_COARSE: ctx->use_cta_coarse = value != 0; return APHGPU_OK;
     case APHGPU_OPT_SWEEP_GROWTH:
       if (value < 0 || value > 3) return SetError(ctx, APHGPU_ERR_ARG, "sweep growth must be 0..3");
       ctx->mg_growth = value;

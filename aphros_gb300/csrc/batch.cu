@@ -34,7 +34,7 @@
 namespace aphgpu {
 namespace {
 
-constexpr int kMaxLev = 12;
+constexpr int kMaxLev = kMgMaxLevels;
 constexpr int kCoarseThreads = 512;
 
 struct BLevel {
@@ -455,25 +455,26 @@ __device__ void CtaDense(const BDom& D) {
   }
 }
 
-// Levels lc .. nlev-1 of every domain: one multigrid cycle of those levels
-// (pre-smoothing colours 0 then 1, post colours 1 then 0, as the batched
+// Levels lc .. nlev-1 of one domain: one multigrid cycle of those levels
+// (pre-smoothing colours 0 then 1, post colours 1 then 0, as the launched
 // levels), each level below lc visited `gamma` times per visit of the level
 // above (1 V-cycle, 2 W-cycle; the exactly solved coarsest level once),
-// CTA barriers between the passes.  The cycle is iterative: todo[l] counts
-// the visits of level l+1 still to make from level l.
-__global__ void __launch_bounds__(kCoarseThreads) KBCoarseCycle(const BDom* __restrict__ doms,
-                                                                int pre, int post, int gamma) {
-  const BDom& D = doms[blockIdx.x];
-  if (D.si->done) return;
+// CTA barriers between the passes; sweeps(l, 0) / sweeps(l, 1) are the
+// pre / post sweeps of level l.  `first`: level lc starts from a zero
+// guess (else from its current x, a repeated W-cycle visit).  The cycle is
+// iterative: todo[l] counts the visits of level l+1 still to make from
+// level l.
+template <class Sweeps>
+__device__ void CoarseCycleBody(const BDom& D, Sweeps sweeps, int gamma, bool first) {
   const int L = D.nlev;
   int todo[kMaxLev];
   int l = D.lc;
-  bool first = true;
   for (;;) {
     if (l < L - 1) {
       // enter level l: pre-smoothing (zero guess on its first visit) and
       // restriction of its residual
       const BLevel& F = D.lv[l];
+      const int pre = sweeps(l, 0);
       if (pre > 0) {
         for (int sw = 0; sw < pre; ++sw) {
           CtaSmooth(F, 0, first && sw == 0);
@@ -509,6 +510,7 @@ __global__ void __launch_bounds__(kCoarseThreads) KBCoarseCycle(const BDom* __re
       const BLevel& F = D.lv[l];
       CtaProlong(F, D.lv[l + 1]);
       __syncthreads();
+      const int post = sweeps(l, 1);
       for (int sw = 0; sw < post; ++sw) {
         CtaSmooth(F, 1, 0);
         __syncthreads();
@@ -517,6 +519,30 @@ __global__ void __launch_bounds__(kCoarseThreads) KBCoarseCycle(const BDom* __re
       }
     }
   }
+}
+
+// The coarse levels of every domain of a batch (one CTA per domain).
+__global__ void __launch_bounds__(kCoarseThreads) KBCoarseCycle(const BDom* __restrict__ doms,
+                                                                int pre, int post, int gamma) {
+  const BDom& D = doms[blockIdx.x];
+  if (D.si->done) return;
+  CoarseCycleBody(D, [=](int, int which) { return which ? post : pre; }, gamma, true);
+}
+
+// The smallest levels of one single-domain hierarchy in one CTA (their
+// launches would be latency-bound), with per-level sweep counts.
+struct LevelSweepCounts {
+  int pre[kMaxLev];
+  int post[kMaxLev];
+};
+
+__global__ void __launch_bounds__(kCoarseThreads) KCoarseCycleOne(const BDom* __restrict__ dom,
+                                                                  LevelSweepCounts sw, int gamma,
+                                                                  int first,
+                                                                  const SolveScalars* s) {
+  if (s && s->done) return;
+  CoarseCycleBody(*dom, [&](int l, int which) { return which ? sw.post[l] : sw.pre[l]; },
+                  gamma, first != 0);
 }
 
 // ---------------------------------------------------------------------------
@@ -1352,3 +1378,63 @@ int aphgpu_batch_last_ms(const aphgpu_batch* B, double* ms, int64_t* launches) {
 }
 
 }  // extern "C"
+
+// ---------------------------------------------------------------------------
+// Single-domain hierarchies: the smallest FP32 levels in one CTA
+// ---------------------------------------------------------------------------
+
+namespace aphgpu {
+
+// Levels of at most this many cells (and below) are cycled by one CTA.
+constexpr int64_t kCoarseOneCells = 4096;
+
+int CoarseOneSetup(aphgpu_ctx* ctx) {
+  Multigrid& mg = ctx->mg;
+  const std::vector<Level<float>>& lv = mg.l32;
+  const int L = (int)lv.size();
+  mg.clc = -1;
+  if (L < 3 || L > kMaxLev || !mg.cinv32 || mg.cn32 != (int)lv.back().d.cells())
+    return APHGPU_OK;
+  int lc = L - 1;
+  while (lc - 1 >= 1 && lv[lc - 1].d.cells() <= kCoarseOneCells) --lc;
+  if (lc > L - 2) return APHGPU_OK;  // no level to smooth besides the coarsest
+  BDom D{};
+  D.nlev = L;
+  D.lc = lc;
+  for (int l = lc; l < L; ++l) {
+    BLevel& b = D.lv[l];
+    b.A = MakeOp(lv[l]);
+    b.x = lv[l].x;
+    b.b = lv[l].b;
+    b.invdiag = lv[l].invdiag;
+    b.vec = 0;
+    b.tx = 0;
+  }
+  D.cinv = mg.cinv32;
+  D.cn = mg.cn32;
+  if (!mg.cdom) {
+    char* p = nullptr;
+    APH_TRY(Alloc(ctx, &p, (int64_t)sizeof(BDom)));
+    mg.cdom = p;
+  }
+  APH_CUDA(ctx, cudaMemcpyAsync(mg.cdom, &D, sizeof(BDom), cudaMemcpyHostToDevice, ctx->stream));
+  APH_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+  mg.clc = lc;
+  return APHGPU_OK;
+}
+
+int CoarseOneLaunch(aphgpu_ctx* ctx, const int* pre, const int* post, int gamma, bool first,
+                    const SolveScalars* s) {
+  const Multigrid& mg = ctx->mg;
+  LevelSweepCounts sw{};
+  for (int l = 0; l < kMaxLev; ++l) {
+    sw.pre[l] = pre[l];
+    sw.post[l] = post[l];
+  }
+  KCoarseCycleOne<<<1, kCoarseThreads, 0, ctx->stream>>>((const BDom*)mg.cdom, sw, gamma,
+                                                          first ? 1 : 0, s);
+  APH_LAUNCHED(ctx);
+  return APHGPU_OK;
+}
+
+}  // namespace aphgpu

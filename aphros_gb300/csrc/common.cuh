@@ -232,6 +232,10 @@ struct Multigrid {
   double* cinv64 = nullptr;
   double* cinv32 = nullptr;
   int cn64 = 0, cn32 = 0;
+  // one-CTA cycle of the smallest FP32 levels: device description of the
+  // levels and the first level it covers (-1: not used)
+  void* cdom = nullptr;
+  int clc = -1;
 };
 constexpr int kDenseMax = 1024;
 
@@ -322,6 +326,7 @@ struct aphgpu_ctx {
   int mg_gamma = 0;        // cycles of each level below the finest (1 V, 2 W, 0 auto)
   int mg_series_pct = 60;  // weight (%) of the series couplings in the coarse operators
   int mg_growth = 0;       // sweeps below the finest level (1 same, 2 linear, 3 doubling, 0 auto)
+  bool use_cta_coarse = true;  // smallest FP32 levels cycled by one CTA
 
   // timing
   cudaEvent_t ev0 = nullptr, ev1 = nullptr;
@@ -376,6 +381,13 @@ int SolveMixed(aphgpu_ctx* ctx, const aphgpu_conf* conf, aphgpu_info* info);
 int SolveMGPCG32(aphgpu_ctx* ctx, const aphgpu_conf* conf, aphgpu_info* info);
 int EnsureMixedVectors(aphgpu_ctx* ctx);
 int EnsureMixedHierarchy(aphgpu_ctx* ctx, const aphgpu_conf* conf);
+// One-CTA cycle of the smallest FP32 levels of a single-domain hierarchy
+// (batch.cu): set up after the hierarchy is built; launched from the cycle
+// with the pre / post sweeps of every level (kMgMaxLevels entries).
+constexpr int kMgMaxLevels = 12;
+int CoarseOneSetup(aphgpu_ctx* ctx);
+int CoarseOneLaunch(aphgpu_ctx* ctx, const int* pre, const int* post, int gamma, bool first,
+                    const SolveScalars* s);
 int SetSystemExprDevice(aphgpu_ctx* ctx, const double* d_expr8);
 int AssembleProjectionDevice(aphgpu_ctx* ctx, const double* d_alpha,
                              double rho1, double rho2, const double* d_vflux,

@@ -29,6 +29,7 @@
 #include <cmath>
 #include <cstring>
 #include <functional>
+#include <type_traits>
 
 #include "common.cuh"
 #include "stencil.cuh"
@@ -1347,7 +1348,7 @@ int BuildHierarchy<float>(aphgpu_ctx* ctx, std::vector<Level<float>>& lv,
   }
   APH_TRY(EnsureCoarsestScratch(ctx, lv.back().d.cells()));
   APH_TRY(BuildCoarsestInverse(ctx, lv.back(), &ctx->mg.cinv32, &ctx->mg.cn32));
-  return APHGPU_OK;
+  return CoarseOneSetup(ctx);
 }
 
 // Launch helpers: the vectorized FP32 kernels where the level allows them.
@@ -1550,6 +1551,17 @@ int CycleLevel(aphgpu_ctx* ctx, std::vector<Level<T>>& lv, int l, bool first, in
                int post, const SolveScalars* s) {
   const int L = (int)lv.size();
   cudaStream_t st = ctx->stream;
+  if constexpr (std::is_same<T, float>::value) {
+    // the smallest levels in one CTA (no launch per pass)
+    if (ctx->use_cta_coarse && l >= 1 && l == ctx->mg.clc && &lv == &ctx->mg.l32) {
+      int np[kMgMaxLevels], nq[kMgMaxLevels];
+      for (int q = 0; q < kMgMaxLevels; ++q) {
+        np[q] = LevelSweeps(ctx, pre, q);
+        nq[q] = LevelSweeps(ctx, post, q);
+      }
+      return CoarseOneLaunch(ctx, np, nq, CycleGamma(ctx), first, s);
+    }
+  }
   if (l == L - 1) {
     Level<T>& c = lv[L - 1];
     const Op<T> A = MakeOp(c);
@@ -1670,6 +1682,7 @@ int Pcg(aphgpu_ctx* ctx, const Op<T>& A, Precond precond, T* x, T* r, T* p,
     key = Mix(key, (uint64_t)(ctx->use_fused ? 1 : 0));
     key = Mix(key, (uint64_t)CycleGamma(ctx));
     key = Mix(key, (uint64_t)SweepGrowth(ctx));
+    key = Mix(key, (uint64_t)(ctx->use_cta_coarse ? 1 + ctx->mg.clc : 0));
     // the FP16 coupling scale is a kernel argument: part of the key
     float hs = ctx->mg.l32.empty() ? 0.f : ctx->mg.l32[0].hscale;
     uint32_t hb;

@@ -389,14 +389,20 @@ int aphgpu_batch_last_ms(const aphgpu_batch* batch, double* ms, int64_t* launche
  *                            (mg_pre / mg_post on the finest): 1 the same
  *                            count, 2 count * (l + 1), 3 count * 2^l (at
  *                            most 16), 0 (default) 2 for V-cycles from
- *                            256^3 cells up and 1 otherwise */
+ *                            256^3 cells up and 1 otherwise
+ *   APHGPU_OPT_CTA_COARSE    1 (default): the FP32 levels of at most 4096
+ *                            cells (16^3) below the finest are cycled by
+ *                            one CTA per visit of their parent level (the
+ *                            batch's per-domain coarse cycle); 0: one
+ *                            launch per pass on every level */
 enum {
   APHGPU_OPT_GRAPHS = 0,
   APHGPU_OPT_FUSED_SWEEPS = 1,
   APHGPU_OPT_HALF_COUPLINGS = 2,
   APHGPU_OPT_CYCLE = 3,
   APHGPU_OPT_COARSE_SERIES = 4,
-  APHGPU_OPT_SWEEP_GROWTH = 5
+  APHGPU_OPT_SWEEP_GROWTH = 5,
+  APHGPU_OPT_CTA_COARSE = 6
 };
 int aphgpu_set_option(aphgpu_ctx* ctx, int option, int value);
 

@@ -334,3 +334,41 @@ def test_sweep_growth(cycle):
         assert out[(2, _lib.SOLVER_MGPCG)][1] < out[(1, _lib.SOLVER_MGPCG)][1]
     with pytest.raises(_lib.AphgpuError):
         ctx.set_option(_lib.OPT_SWEEP_GROWTH, 4)
+
+
+@pytest.mark.parametrize("cycle", [1, 2])
+@pytest.mark.parametrize("shape", [(128, 128, 128), (96, 48, 40)])
+def test_cta_coarse_cycle(cycle, shape):
+    """The smallest FP32 levels cycled by one CTA (APHGPU_OPT_CTA_COARSE)
+    run the same smoothing, restriction, prolongation and dense coarsest
+    solve as the launched passes: the mixed and MG-PCG32 solves reach the
+    tolerance with the same pressure and (rounding aside) the same
+    iteration counts, with and without CUDA graphs."""
+    nx, ny, nz = shape
+    h = 1.0 / nx
+    c, r = workload.place_spheres(21, 6, 0.06, 0.15, gap=0.02)
+    N = nx * ny * nz
+    alpha = workload.alpha_spheres(nx, c, r)[:N] if nx == ny == nz else np.zeros(N)
+    flux = workload.tg_flux(max(shape), seed=7)
+    flux = np.concatenate([flux[d * max(shape) ** 3:d * max(shape) ** 3 + N] for d in range(3)])
+    ctx = _lib.Context(shape, h)
+    ctx.assemble_projection(alpha, 1.0, 1e-3, flux, 1e-3)
+    ctx.set_option(_lib.OPT_CYCLE, cycle)
+    _, bn = ctx.residual_norms()
+    tol = 1e-10 * bn / math.sqrt(h ** 3)
+    for solver in (_lib.SOLVER_MIXED, _lib.SOLVER_MGPCG32):
+        out = {}
+        for cta in (0, 1):
+            for graphs in (1, 0):
+                ctx.set_option(_lib.OPT_CTA_COARSE, cta)
+                ctx.set_option(_lib.OPT_GRAPHS, graphs)
+                x, info = ctx.solve(_lib.default_conf(solver=solver, tol=tol, maxiter=300))
+                rn, bn2 = ctx.residual_norms()
+                assert info.converged and rn / bn2 <= 1.01e-10, (solver, cta, graphs)
+                out[(cta, graphs)] = (x, info.iter + info.inner_iter)
+        ref = out[(0, 0)]
+        for key, (x, its) in out.items():
+            assert rel_l2(x, ref[0]) < 1e-7, (solver, key)
+            assert abs(its - ref[1]) <= 2, (solver, key, its, ref[1])
+        # graphs do not change the results
+        assert np.array_equal(out[(1, 1)][0], out[(1, 0)][0])
