@@ -536,13 +536,68 @@ struct LevelSweepCounts {
   int post[kMaxLev];
 };
 
+// Floats per cell of a level staged in shared memory: x, b, three
+// couplings, diagonal, inverse diagonal.
+constexpr int kStagedFloats = 7;
+
+// The levels lc .. nlev-1 are staged in dynamic shared memory for the whole
+// cycle (their couplings, diagonals and level lc's right-hand side and,
+// on a repeated visit, its x are read once; level lc's x is written back
+// at the end), and the cycle runs on the staged copies.
 __global__ void __launch_bounds__(kCoarseThreads) KCoarseCycleOne(const BDom* __restrict__ dom,
                                                                   LevelSweepCounts sw, int gamma,
                                                                   int first,
                                                                   const SolveScalars* s) {
   if (s && s->done) return;
-  CoarseCycleBody(*dom, [&](int l, int which) { return which ? sw.post[l] : sw.pre[l]; },
+  extern __shared__ float staged[];
+  __shared__ BDom S;
+  const int tid = threadIdx.x;
+  if (tid == 0) {
+    S = *dom;
+    int64_t off = 0;
+    for (int l = S.lc; l < S.nlev; ++l) {
+      BLevel& L = S.lv[l];
+      const int64_t n = L.A.d.cells();
+      float* base = staged + off;
+      L.x = base;
+      L.b = base + n;
+      L.A.w0 = base + 2 * n;
+      L.A.w1 = base + 3 * n;
+      L.A.w2 = base + 4 * n;
+      L.A.diag = L.A.diag ? base + 5 * n : nullptr;
+      L.invdiag = base + 6 * n;
+      off += kStagedFloats * n;
+    }
+  }
+  __syncthreads();
+  const BDom& G = *dom;
+  for (int l = S.lc; l < S.nlev; ++l) {
+    const BLevel& g = G.lv[l];
+    const BLevel& t = S.lv[l];
+    const int n = (int)g.A.d.cells();
+    float* w0 = const_cast<float*>(t.A.w0);
+    float* w1 = const_cast<float*>(t.A.w1);
+    float* w2 = const_cast<float*>(t.A.w2);
+    float* dg = const_cast<float*>(t.A.diag);
+    float* idg = const_cast<float*>(t.invdiag);
+    for (int c = tid; c < n; c += blockDim.x) {
+      w0[c] = g.A.w0[c];
+      w1[c] = g.A.w1[c];
+      w2[c] = g.A.w2[c];
+      if (dg) dg[c] = g.A.diag[c];
+      idg[c] = g.invdiag[c];
+      if (l == S.lc) {
+        t.b[c] = g.b[c];
+        if (!first) t.x[c] = g.x[c];
+      }
+    }
+  }
+  __syncthreads();
+  CoarseCycleBody(S, [&](int l, int which) { return which ? sw.post[l] : sw.pre[l]; },
                   gamma, first != 0);
+  __syncthreads();
+  const int n = (int)G.lv[S.lc].A.d.cells();
+  for (int c = tid; c < n; c += blockDim.x) G.lv[S.lc].x[c] = S.lv[S.lc].x[c];
 }
 
 // ---------------------------------------------------------------------------
@@ -1385,8 +1440,12 @@ int aphgpu_batch_last_ms(const aphgpu_batch* B, double* ms, int64_t* launches) {
 
 namespace aphgpu {
 
-// Levels of at most this many cells (and below) are cycled by one CTA.
+// Levels of at most this many cells (and below) are cycled by one CTA,
+// staged in at most this much dynamic shared memory (the kernel's static
+// shared memory, the coarsest right-hand side and the copy of the level
+// description, stays within the 227 KB of a CTA).
 constexpr int64_t kCoarseOneCells = 4096;
+constexpr size_t kCoarseOneSmem = 200 * 1024;
 
 int CoarseOneSetup(aphgpu_ctx* ctx) {
   Multigrid& mg = ctx->mg;
@@ -1412,6 +1471,14 @@ int CoarseOneSetup(aphgpu_ctx* ctx) {
   }
   D.cinv = mg.cinv32;
   D.cn = mg.cn32;
+  // the staged levels must fit the shared memory of one CTA
+  int64_t staged = 0;
+  for (int l = lc; l < L; ++l) staged += kStagedFloats * lv[l].d.cells();
+  const size_t bytes = sizeof(float) * (size_t)staged;
+  if (bytes > kCoarseOneSmem) return APHGPU_OK;
+  APH_CUDA(ctx, cudaFuncSetAttribute(KCoarseCycleOne, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                     (int)kCoarseOneSmem));
+  mg.csmem = (int)bytes;
   if (!mg.cdom) {
     char* p = nullptr;
     APH_TRY(Alloc(ctx, &p, (int64_t)sizeof(BDom)));
@@ -1431,8 +1498,8 @@ int CoarseOneLaunch(aphgpu_ctx* ctx, const int* pre, const int* post, int gamma,
     sw.pre[l] = pre[l];
     sw.post[l] = post[l];
   }
-  KCoarseCycleOne<<<1, kCoarseThreads, 0, ctx->stream>>>((const BDom*)mg.cdom, sw, gamma,
-                                                          first ? 1 : 0, s);
+  KCoarseCycleOne<<<1, kCoarseThreads, mg.csmem, ctx->stream>>>((const BDom*)mg.cdom, sw,
+                                                                 gamma, first ? 1 : 0, s);
   APH_LAUNCHED(ctx);
   return APHGPU_OK;
 }

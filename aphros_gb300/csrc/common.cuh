@@ -236,6 +236,7 @@ struct Multigrid {
   // levels and the first level it covers (-1: not used)
   void* cdom = nullptr;
   int clc = -1;
+  int csmem = 0;  // dynamic shared memory of that cycle (bytes)
 };
 constexpr int kDenseMax = 1024;
 
@@ -326,7 +327,7 @@ struct aphgpu_ctx {
   int mg_gamma = 0;        // cycles of each level below the finest (1 V, 2 W, 0 auto)
   int mg_series_pct = 60;  // weight (%) of the series couplings in the coarse operators
   int mg_growth = 0;       // sweeps below the finest level (1 same, 2 linear, 3 doubling, 0 auto)
-  bool use_cta_coarse = true;  // smallest FP32 levels cycled by one CTA
+  bool use_cta_coarse = false;  // smallest FP32 levels cycled by one CTA
 
   // timing
   cudaEvent_t ev0 = nullptr, ev1 = nullptr;
