@@ -735,6 +735,8 @@ def run_profile(args):
         batch = _lib.Batch(ctxs)
         if args.tiles:
             batch.set_tiles(*args.tiles)
+        if args.cycle in (1, 2):
+            batch.set_cycle(args.cycle)
         conf = _lib.default_conf(solver=_lib.SOLVER_MIXED, tol=0.0, rtol=1e-10)
         l0 = 0
         for s in range(args.warmup + args.steps):
@@ -793,7 +795,7 @@ def main():
     ap.add_argument("--cpu-budget", type=float, default=15.0)
     ap.add_argument("--cycle", type=int, choices=[0, 1, 2], default=0,
                     help="--profile: 1 the headline's V-cycle configuration, 2 W, 0 "
-                         "library default")
+                         "library default (batch: the per-domain coarse cycle)")
     ap.add_argument("--profile", choices=["mixed", "fp64", "batch", "vof"], default=None,
                     help="profiling run: assemble, then `steps` solves of one solver "
                          "after `warmup` solves, no other work and no output line")
