@@ -364,15 +364,45 @@ __global__ void __launch_bounds__(256, 4) KBProlong(const BDom* __restrict__ dom
 // Per-domain cycle of the coarse levels (one CTA per domain)
 // ---------------------------------------------------------------------------
 
+// Coordinates (i, j, k) of the cells start, start + stride, ... of a level,
+// advanced without integer divisions (the divisions per cell made the
+// one-CTA passes issue-bound).
+struct CellWalk {
+  int i, j, k, si, sj, sk;
+  __device__ CellWalk(const Dims& d, int start, int stride) {
+    i = start % d.nx;
+    const int r = start / d.nx;
+    j = r % d.ny;
+    k = r / d.ny;
+    si = stride % d.nx;
+    const int rs = stride / d.nx;
+    sj = rs % d.ny;
+    sk = rs / d.ny;
+  }
+  __device__ void Next(const Dims& d) {
+    i += si;
+    int cj = sj;
+    if (i >= d.nx) {
+      i -= d.nx;
+      ++cj;
+    }
+    j += cj;
+    int ck = sk;
+    if (j >= d.ny) {
+      j -= d.ny;
+      ++ck;
+    }
+    k += ck;
+  }
+};
+
 __device__ void CtaSmooth(const BLevel& L, int color, int zero_init) {
   const Dims& d = L.A.d;
   const int n = (int)d.cells();
   float* x = L.x;
-  for (int c = threadIdx.x; c < n; c += blockDim.x) {
-    const int i = c % d.nx;
-    const int r = c / d.nx;
-    const int j = r % d.ny;
-    const int k = r / d.ny;
+  CellWalk w(d, threadIdx.x, blockDim.x);
+  for (int c = threadIdx.x; c < n; c += blockDim.x, w.Next(d)) {
+    const int i = w.i, j = w.j, k = w.k;
     if (((i + j + k) & 1) != color) continue;
     if (zero_init) {
       x[c] = L.b[c] * L.invdiag[c];
@@ -394,11 +424,9 @@ __device__ void CtaSmooth(const BLevel& L, int color, int zero_init) {
 __device__ void CtaRestrict(const BLevel& F, const BLevel& C) {
   const Dims& dc = C.A.d;
   const int n = (int)dc.cells();
-  for (int cc = threadIdx.x; cc < n; cc += blockDim.x) {
-    const int I = cc % dc.nx;
-    const int r = cc / dc.nx;
-    const int J = r % dc.ny;
-    const int K = r / dc.ny;
+  CellWalk w(dc, threadIdx.x, blockDim.x);
+  for (int cc = threadIdx.x; cc < n; cc += blockDim.x, w.Next(dc)) {
+    const int I = w.i, J = w.j, K = w.k;
     float sum = 0.f;
 #pragma unroll
     for (int q = 0; q < 8; ++q) {
@@ -414,12 +442,9 @@ __device__ void CtaProlong(const BLevel& F, const BLevel& C) {
   const Dims& d = F.A.d;
   const Dims& dc = C.A.d;
   const int n = (int)d.cells();
-  for (int c = threadIdx.x; c < n; c += blockDim.x) {
-    const int i = c % d.nx;
-    const int r = c / d.nx;
-    const int j = r % d.ny;
-    const int k = r / d.ny;
-    F.x[c] += C.x[dc.idx(i >> 1, j >> 1, k >> 1)];
+  CellWalk w(d, threadIdx.x, blockDim.x);
+  for (int c = threadIdx.x; c < n; c += blockDim.x, w.Next(d)) {
+    F.x[c] += C.x[dc.idx(w.i >> 1, w.j >> 1, w.k >> 1)];
   }
 }
 
