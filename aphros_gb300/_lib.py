@@ -26,6 +26,8 @@ OPT_CYCLE = 3
 OPT_COARSE_SERIES = 4
 OPT_SWEEP_GROWTH = 5
 OPT_CTA_COARSE = 6
+FIELD_PRESSURE, FIELD_RHS, FIELD_VF, FIELD_CURVATURE = 0, 1, 2, 3
+DUMP_UINT16, DUMP_FLOAT32, DUMP_FLOAT64 = 0, 1, 2
 
 K_SMOOTH32, K_SMOOTH64, K_APPLY64, K_APPLY32, K_RESTRICT32 = 0, 1, 2, 3, 4
 K_VOF_FLUX, K_VOF_UPDATE, K_RECONSTRUCT, K_HEIGHTS, K_CURVATURE = 5, 6, 7, 8, 9
@@ -110,6 +112,10 @@ def lib():
     L.aphgpu_mark.argtypes = [_P, _I]
     L.aphgpu_set_option.argtypes = [_P, _I, _I]
     L.aphgpu_set_option.restype = _I
+    L.aphgpu_dump_raw.argtypes = [_P, _I, _I, ctypes.c_char_p, ctypes.c_char_p]
+    L.aphgpu_read_raw.argtypes = [_P, _I, ctypes.c_char_p, ctypes.c_char_p]
+    L.aphgpu_xmf_text.argtypes = [_I, _I, _I, _D, ctypes.c_char_p, ctypes.c_char_p, _I,
+                                  ctypes.c_char_p, _I, ctypes.POINTER(_I)]
     L.aphgpu_residual_history.argtypes = [_P, _I, _P, _I, ctypes.POINTER(_I)]
     L.aphgpu_residual_history.restype = _I
     L.aphgpu_elapsed.argtypes = [_P, _I, _I, _PD]
@@ -159,6 +165,21 @@ def default_conf(**kw):
     for k, v in kw.items():
         setattr(c, k, v)
     return c
+
+
+def xmf_text(n, h, name, binpath, dtype=DUMP_FLOAT64):
+    """The XMF metadata aphgpu_dump_raw writes (host only)."""
+    n = (n, n, n) if isinstance(n, int) else tuple(n)
+    L = lib()
+    ln = _I()
+    rc = L.aphgpu_xmf_text(n[0], n[1], n[2], h, name.encode(), binpath.encode(), dtype,
+                           None, 0, ctypes.byref(ln))
+    if rc != OK:
+        raise AphgpuError(rc, "aphgpu_xmf_text failed")
+    buf = ctypes.create_string_buffer(ln.value + 1)
+    L.aphgpu_xmf_text(n[0], n[1], n[2], h, name.encode(), binpath.encode(), dtype,
+                      buf, ln.value + 1, None)
+    return buf.value.decode()
 
 
 class Context:
@@ -241,6 +262,10 @@ class Context:
                                                   int(zero_guess), ctypes.byref(info)))
         return info
 
+    def set_solution(self, x):
+        a = self._f64(x, self.N)
+        self._check(self._L.aphgpu_set_solution(self._p, ptr(a)))
+
     def get_solution(self):
         x = np.empty(self.N)
         self._check(self._L.aphgpu_get_solution(self._p, ptr(x)))
@@ -313,6 +338,17 @@ class Context:
     def set_option(self, option, value):
         """One of the OPT_* execution options (aphgpu_set_option)."""
         self._check(self._L.aphgpu_set_option(self._p, option, int(value)))
+
+    def dump_raw(self, field, rawpath, name, dtype=DUMP_FLOAT64):
+        """Writes a field to rawpath and its XMF beside it (aphgpu_dump_raw)."""
+        self._check(self._L.aphgpu_dump_raw(self._p, field, dtype, str(rawpath).encode(),
+                                            name.encode()))
+
+    def read_raw(self, field, xmfpath, rawpath=None):
+        """Reads a field from a raw + XMF dump (aphgpu_read_raw)."""
+        self._check(self._L.aphgpu_read_raw(
+            self._p, field, str(xmfpath).encode(),
+            None if rawpath is None else str(rawpath).encode()))
 
     def mark(self, slot):
         self._check(self._L.aphgpu_mark(self._p, slot))

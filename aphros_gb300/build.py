@@ -37,6 +37,7 @@ CU_UNITS = {
     "noalloc.cu": [],
     "server.cu": [],
     "batch.cu": [],
+    "dump.cu": [],
 }
 
 

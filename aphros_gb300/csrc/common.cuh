@@ -309,6 +309,8 @@ struct aphgpu_ctx {
   double vof_dt = 0;  // time step of the last VOF step (kernel timing)
   bool vof_ready = false;
 
+  // device scratch of the field dumps (dump.cu)
+  void* dump_scratch = nullptr;
   // host staging (pinned)
   void* pinned = nullptr;
   size_t pinned_bytes = 0;

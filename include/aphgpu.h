@@ -436,6 +436,40 @@ enum {
 int aphgpu_time_kernel(aphgpu_ctx* ctx, int kernel, int reps, double* ms,
                        double* bytes);
 
+/* ---- field dumps (aphros raw + XMF format) ---- */
+
+/* Fields of a context: pressure (the solution x), the right-hand side of
+ * the system, the volume fraction and the curvature (after aphgpu_vof_init;
+ * the curvature of the last aphgpu_curvature). */
+enum {
+  APHGPU_FIELD_PRESSURE = 0,
+  APHGPU_FIELD_RHS = 1,
+  APHGPU_FIELD_VF = 2,
+  APHGPU_FIELD_CURVATURE = 3
+};
+/* Element types of a raw file, in the order of dump::Type (dump/xmf.h:13). */
+enum { APHGPU_DUMP_UINT16 = 0, APHGPU_DUMP_FLOAT32 = 1, APHGPU_DUMP_FLOAT64 = 2 };
+
+/* Writes `field` to `rawpath` (cells x-fastest, converted to `type` as C++
+ * converts a double; UInt16 values outside [0, 65535] are clamped) and its
+ * metadata, with dataset name `name` and binpath `rawpath`, to the path of
+ * `rawpath` with the extension replaced by ".xmf".  Replaces
+ * dump::Raw<M>::WriteWithXmf (src/dump/raw.ipp:204-226) on one block; the
+ * files are those the reference writes. */
+int aphgpu_dump_raw(aphgpu_ctx* ctx, int field, int type, const char* rawpath, const char* name);
+/* Reads `field` from a raw file described by `xmfpath` (the binpath there,
+ * or `rawpath` if not NULL): the whole array of the context's dimensions,
+ * start 0 and stride 1, from byte `Seek`.  Replaces dump::Raw<M>::Read with
+ * dump::Xmf::ReadXmf (src/dump/raw.ipp:257-363, src/dump/xmf.ipp:103-140)
+ * for the sequential reader's case.  Fields derived from the volume
+ * fraction (normals, plane constants) are recomputed by the next step. */
+int aphgpu_read_raw(aphgpu_ctx* ctx, int field, const char* xmfpath, const char* rawpath);
+/* The XMF text aphgpu_dump_raw writes for an nx*ny*nz mesh of cell edge h
+ * (host only; no GPU needed).  Copies at most cap-1 bytes and a NUL to out
+ * (may be NULL) and the full length to *len (may be NULL). */
+int aphgpu_xmf_text(int nx, int ny, int nz, double h, const char* name, const char* binpath,
+                    int type, char* out, int cap, int* len);
+
 #ifdef __cplusplus
 }
 #endif

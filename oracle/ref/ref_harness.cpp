@@ -24,6 +24,13 @@
 //   reconst in out         rows (n0 n1 n2 u a h0 h1 h2 q dt d) ->
 //                          GetLineA(n,u,h) GetLineU(n,a,h) GetLineFlux(...)
 //   height  in out         rows (column, optional n=N) -> UHeight::Good
+//   xmf   n h name binpath type out.xmf
+//     dump::Xmf::WriteXmf of the metadata that dump::Raw::WriteWithXmf
+//     writes for a field of an n-cell mesh with cell size h (dump/raw.ipp:
+//     204-226); type is Double, Float or UShort.
+//   raw   n type in.f64 out.raw
+//     dump::Raw::WriteBlocks of one block covering the mesh (the
+//     sequential writer, dump/raw.ipp:73-158), values converted to type.
 #include <cmath>
 #include <cstdio>
 #include <cstdlib>
@@ -35,6 +42,8 @@
 #include <vector>
 
 #include "distr/distrbasic.h"
+#include "dump/raw.h"
+#include "dump/xmf.h"
 #include "linear/linear.h"
 #include "overlap/overlap.h"
 #include "parse/vof.h"
@@ -415,8 +424,41 @@ int Table(const std::string& mode, const char* in, const char* out) {
 
 } // namespace
 
+int Dump(int argc, const char** argv) {
+  const std::string mode = argv[1];
+  const MIdx nsz = ParseSize(argv[2]);
+  if (mode == "xmf") {
+    if (argc != 8) return 1;
+    using X = dump::Xmf<Vect>;
+    X::Meta meta;
+    meta.name = argv[4];
+    meta.binpath = argv[5];
+    meta.type = dump::StringToType(argv[6]);
+    meta.dimensions = nsz;
+    meta.count = nsz;
+    meta.origin = Vect(0);
+    meta.spacing = Vect(std::atof(argv[3]));
+    X::WriteXmf(std::string(argv[7]), meta, false);
+    return 0;
+  }
+  if (argc != 6) return 1;
+  const size_t n = size_t(nsz.prod());
+  const std::vector<double> v = ReadRaw(argv[4], n);
+  MpiWrapper mpi;
+  const std::vector<MIdx> starts{MIdx(0)}, sizes{nsz};
+  const std::vector<std::vector<double>> data{v};
+  dump::Raw<M>::WriteBlocks<double>(
+      argv[5], starts, sizes, data, nsz, dump::StringToType(argv[3]), 0, mpi,
+      true);
+  return 0;
+}
+
 int main(int argc, const char** argv) {
   const std::string mode = argc > 1 ? argv[1] : "";
+  if (mode == "xmf" || mode == "raw") {
+    if (argc < 3) return 1;
+    return Dump(argc, argv);
+  }
   if (mode == "overlap" || mode == "reconst" || mode == "height") {
     if (argc != 4) return 1;
     return Table(mode, argv[2], argv[3]);

@@ -21,6 +21,10 @@ Fixtures:
   height.txt       UHeight::Good on the reference's unit-test columns
                    (test/util/main.cpp) and on random 13-cell columns.
   overlap.txt      GetSphereOverlap on random boxes (pins the generator).
+  dumps.npz        dump::Xmf::WriteXmf texts of dump::Raw::WriteWithXmf
+                   metadata for several meshes and element types, and
+                   dump::Raw::WriteBlocks output of a 3x4x5 array converted
+                   to Double, Float and UShort.
 """
 import argparse
 import math
@@ -205,6 +209,34 @@ def overlap(tmp, rows=200):
             f.write(a + " | " + b + "\n")
 
 
+XMF_CASES = [  # (nx, ny, nz, h, name, binpath, type)
+    (16, 16, 16, 1 / 16, "vf", "vf.raw", "Double"),
+    (32, 24, 16, 1 / 32, "p", "out/p_0001.raw", "Float"),
+    (8, 8, 8, 0.125, "cl", "cl.raw", "UShort"),
+    (48, 48, 48, 1 / 48, "kappa", "/tmp/k.raw", "Double"),
+]
+
+
+def dumps(tmp):
+    out = {}
+    for q, (nx, ny, nz, h, name, binpath, typ) in enumerate(XMF_CASES):
+        path = os.path.join(tmp, "x%d.xmf" % q)
+        run(["xmf", "%d,%d,%d" % (nx, ny, nz), repr(h), name, binpath, typ, path], tmp)
+        out["xmf%d" % q] = np.array(open(path).read())
+    # a 3x4x5 array: fractions, values that round differently in float32,
+    # and values whose truncation to uint16 is exact
+    rng = np.random.default_rng(17)
+    v = rng.uniform(0, 60000, size=60) + rng.uniform(0, 1, size=60) / 3
+    v[:4] = [0.0, 1.5, 65535.25, 1 / 3]
+    v.astype(np.float64).tofile(os.path.join(tmp, "v.f64"))
+    out["values"] = v
+    for typ in ("Double", "Float", "UShort"):
+        path = os.path.join(tmp, "v_%s.raw" % typ)
+        run(["raw", "3,4,5", typ, "v.f64", path], tmp)
+        out["raw_" + typ] = np.fromfile(path, dtype=np.uint8)
+    np.savez(os.path.join(OUT, "dumps.npz"), **out)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--ref", default="/root/reference")
@@ -218,6 +250,7 @@ def main():
         reconst(tmp)
         height(args.ref, tmp)
         overlap(tmp)
+        dumps(tmp)
     for f in sorted(os.listdir(OUT)):
         print(f, os.path.getsize(os.path.join(OUT, f)))
 
