@@ -305,6 +305,9 @@ int aphgpu_read_raw(aphgpu_ctx* ctx, int field, const char* xmfpath, const char*
     if (rc == APHGPU_OK) rc = CheckCuda(ctx, cudaStreamSynchronize(ctx->stream), "read sync");
   }
   std::fclose(f);
+  // a volume fraction read back gets its interface reconstructed (normals,
+  // plane constants), as at aphgpu_vof_init; the step count is kept
+  if (rc == APHGPU_OK && field == APHGPU_FIELD_VF) rc = VofReconstruct(ctx);
   return rc;
 }
 

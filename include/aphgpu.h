@@ -461,8 +461,10 @@ int aphgpu_dump_raw(aphgpu_ctx* ctx, int field, int type, const char* rawpath, c
  * or `rawpath` if not NULL): the whole array of the context's dimensions,
  * start 0 and stride 1, from byte `Seek`.  Replaces dump::Raw<M>::Read with
  * dump::Xmf::ReadXmf (src/dump/raw.ipp:257-363, src/dump/xmf.ipp:103-140)
- * for the sequential reader's case.  Fields derived from the volume
- * fraction (normals, plane constants) are recomputed by the next step. */
+ * for the sequential reader's case.  A volume fraction read back gets its
+ * interface reconstructed (normals, plane constants) as at
+ * aphgpu_vof_init; the context's step count (which orders the directional
+ * sweeps, vof.ipp:428-435) is kept. */
 int aphgpu_read_raw(aphgpu_ctx* ctx, int field, const char* xmfpath, const char* rawpath);
 /* The XMF text aphgpu_dump_raw writes for an nx*ny*nz mesh of cell edge h
  * (host only; no GPU needed).  Copies at most cap-1 bytes and a NUL to out

@@ -73,7 +73,8 @@ def test_dump_raw_bytes_and_read_back(lib, fx, tmp_path, typ):
 def test_volume_fraction_checkpoint(lib, tmp_path):
     """A served simulation's volume fraction survives a dump and a read
     bit for bit, and the next step from the restored field equals the step
-    from the original."""
+    from the original (the restored context has made as many steps, so that
+    both sweep in the same order)."""
     from aphros_gb300 import workload
     case = workload.config("c1", n=32)
     a = lib.Context(32, case.h)
@@ -86,13 +87,19 @@ def test_volume_fraction_checkpoint(lib, tmp_path):
     b = lib.Context(32, case.h)
     b.assemble_projection(case.alpha, case.rho1, case.rho2, case.flux, case.dt)
     b.vof_init(np.zeros(32 ** 3))
+    b.vof_step(case.flux, dt)
     b.read_raw(lib.FIELD_VF, os.path.splitext(raw)[0] + ".xmf")
     ua = a.vof_get()[0]
     assert np.array_equal(b.vof_get()[0], ua)
     a.vof_step(case.flux, dt)
     b.vof_step(case.flux, dt)
     assert np.array_equal(a.vof_get()[0], b.vof_get()[0])
+    # dimensions that differ from the context's, and a field not yet there
+    c = lib.Context(16, 1 / 16)
     with pytest.raises(lib.AphgpuError):
-        lib.Context(16, 1 / 16).read_raw(lib.FIELD_VF, os.path.splitext(raw)[0] + ".xmf")
-    a.close()
-    b.close()
+        c.read_raw(lib.FIELD_VF, os.path.splitext(raw)[0] + ".xmf")
+    c.vof_init(np.zeros(16 ** 3))
+    with pytest.raises(lib.AphgpuError):
+        c.read_raw(lib.FIELD_VF, os.path.splitext(raw)[0] + ".xmf")
+    for ctx in (a, b, c):
+        ctx.close()
