@@ -185,3 +185,30 @@ def test_coarsest_too_large_is_rejected():
         batch.solve(_conf())
     batch.close()
     assert math.isfinite(ctx.residual_norms()[1])
+
+
+def test_ragged_domains_in_one_batch():
+    """Domains whose x size is not a multiple of 4 (scalar tiles; they
+    coarsen once, to an odd size whose cube the dense coarsest inverse
+    takes) batched with float4 ones: each converges and equals its own
+    mixed solve."""
+    cases = []
+    for i, n in enumerate((18, 14, 32, 10, 24)):
+        c, r = workload.place_spheres(500 + i, 2, 0.08, 0.2, gap=0.02)
+        cases.append(workload.Case(n, c, r, rho1=1.0, rho2=1e-3, seed=600 + i))
+    ctxs = _contexts(cases, diffusion=False)
+    conf = _conf()
+    ref = []
+    for ctx in ctxs:
+        info = ctx.solve_resident(conf, zero_guess=True)
+        assert info.converged
+        ref.append(ctx.get_solution())
+    batch = _lib.Batch(ctxs)
+    infos = batch.solve(conf)
+    for q, (ctx, info) in enumerate(zip(ctxs, infos)):
+        assert info.converged, q
+        rn, bn = ctx.residual_norms()
+        assert rn / bn <= 1.01 * RTOL, q
+        a, b = _demean(ctx.get_solution()), _demean(ref[q])
+        assert np.linalg.norm(a - b) / np.linalg.norm(b) < 1e-7, q
+    batch.close()
