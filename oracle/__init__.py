@@ -200,6 +200,9 @@ class VofState:
         self.mask = np.empty(N, dtype=np.uint8)
         self.clipth = clipth
         self.count = 0
+        # colours as the reference's Vof starts them from a zero colour
+        # field: 0 where u > 0, none (-1) elsewhere (vof.ipp:53-57)
+        self.cl = np.where(self.u > 0, 0.0, -1.0)
 
     def step(self, vflux, dt, nthreads=1):
         o = lib()
@@ -210,6 +213,14 @@ class VofState:
                        self.count, 1 if self.count == 0 else 0,
                        self.mask.ctypes.data_as(_P), _p(self.nrm), _p(self.a))
         self.count += 1
+
+    def recolor(self):
+        """Connected-component colours of the current field (the resetcolor,
+        union-find recolor and propagate stages of Vof::MakeIteration)."""
+        out = np.empty(self.N)
+        lib().orc_recolor(self.n3c, _p(self.u), _p(self.cl), _p(out))
+        self.cl = out
+        return out
 
     def curvature(self, heights=False):
         o = lib()

@@ -901,3 +901,146 @@ void orc_heights_curvature(
   free(du4);
   if (!hgt_out) free(hgt);
 }
+
+/* ------------------------------------------------------------------------
+ * Connected-component colours of the volume fraction, one block, periodic:
+ * the union-find recolouring of Vof::MakeIteration (src/solver/vof.ipp:
+ * 546-578) with UVof::Imp::RecolorUnionFind (src/util/vof.ipp:982-1150):
+ *   resetcolor  gas cells (u > 0.5) get colour 0, others none (-1);
+ *   recolor     26-connected gas cells form components; each takes the
+ *               smallest unique initial colour in it, i.e. the ordinal of
+ *               its first cell in x-fastest order (InitUniqueColors,
+ *               util/vof.ipp:824-870); PairToMap (util/vof.ipp:612-650)
+ *               maps each component to the previous colour of its first
+ *               cell, in the order of the cells with two halo layers, that
+ *               has one; ReduceColor (util/vof.ipp:740-803) keeps that
+ *               colour unless taken, else gives the next unused one;
+ *   propagate   cells without colour with 0 < u take the colour of a face
+ *               neighbour with larger u, faces in the mesh's order
+ *               (direction-major, x-fastest; geom/blockface.h:29-48), halo
+ *               cells holding the values from before the pass.
+ * cl_prev: colours before resetcolor; cl: result.
+ * ------------------------------------------------------------------------ */
+
+static int64_t uf_find(int64_t* p, int64_t x) {
+  while (p[x] != x) {
+    p[x] = p[p[x]];
+    x = p[x];
+  }
+  return x;
+}
+
+static int wrapi(int i, int n) { return i < 0 ? i + n : (i >= n ? i - n : i); }
+
+#define XIDX(i, j, k) ((int64_t)(i) + (int64_t)nx * ((int64_t)(j) + (int64_t)ny * (int64_t)(k)))
+
+void orc_recolor(const int n[3], const double* u, const double* cl_prev, double* cl) {
+  const int nx = n[0], ny = n[1], nz = n[2];
+  const int64_t N = (int64_t)nx * ny * nz;
+  int64_t* p = (int64_t*)malloc(sizeof(int64_t) * N);
+  for (int64_t c = 0; c < N; ++c) p[c] = u[c] > 0.5 ? c : -1;
+  for (int k = 0; k < nz; ++k)
+    for (int j = 0; j < ny; ++j)
+      for (int i = 0; i < nx; ++i) {
+        const int64_t c = XIDX(i, j, k);
+        if (p[c] < 0) continue;
+        for (int dk = -1; dk <= 1; ++dk)
+          for (int dj = -1; dj <= 1; ++dj)
+            for (int di = -1; di <= 1; ++di) {
+              const int64_t cn = XIDX(wrapi(i + di, nx), wrapi(j + dj, ny), wrapi(k + dk, nz));
+              if (p[cn] < 0) continue;
+              int64_t a = uf_find(p, c), b = uf_find(p, cn);
+              if (a != b) {
+                if (a < b) p[b] = a;  /* the smaller root stays: root = min */
+                else p[a] = b;
+              }
+            }
+      }
+  /* components in order of their roots (first cells) */
+  int64_t ncomp = 0;
+  int64_t* slot = (int64_t*)malloc(sizeof(int64_t) * N);
+  for (int64_t c = 0; c < N; ++c) {
+    slot[c] = -1;
+    if (p[c] >= 0) p[c] = uf_find(p, c);
+    if (p[c] == c) slot[c] = ncomp++;
+  }
+  double* stable = (double*)malloc(sizeof(double) * (ncomp + 1));
+  char* has = (char*)calloc(ncomp + 1, 1);
+  /* PairToMap over the cells with two halo layers */
+  for (int k = -2; k < nz + 2; ++k)
+    for (int j = -2; j < ny + 2; ++j)
+      for (int i = -2; i < nx + 2; ++i) {
+        const int64_t c = XIDX(wrapi(i, nx), wrapi(j, ny), wrapi(k, nz));
+        if (p[c] < 0 || cl_prev[c] == -1) continue;
+        const int64_t s = slot[p[c]];
+        if (!has[s]) {
+          has[s] = 1;
+          stable[s] = cl_prev[c];
+        }
+      }
+  /* ReduceColor: colours in increasing order of the components' keys */
+  double next = 0;
+  for (int64_t s = 0; s < ncomp; ++s)
+    if (has[s] && stable[s] > next) next = stable[s];
+  next += 1;
+  double* color = (double*)malloc(sizeof(double) * (ncomp + 1));
+  /* used colours: a sorted list is enough for the sizes of the tests */
+  double* used = (double*)malloc(sizeof(double) * (ncomp + 1));
+  int64_t nused = 0;
+  for (int64_t s = 0; s < ncomp; ++s) {
+    int taken = 0;
+    if (has[s])
+      for (int64_t q = 0; q < nused; ++q)
+        if (used[q] == stable[s]) taken = 1;
+    if (!has[s] || taken) {
+      color[s] = next;
+      next += 1;
+    } else {
+      color[s] = stable[s];
+    }
+    used[nused++] = color[s];
+  }
+  for (int64_t c = 0; c < N; ++c) cl[c] = p[c] >= 0 ? color[slot[p[c]]] : -1;
+  /* propagate */
+  double* pre = (double*)malloc(sizeof(double) * N);
+  memcpy(pre, cl, sizeof(double) * N);
+  for (int d = 0; d < 3; ++d) {
+    const int e[3] = {d == 0, d == 1, d == 2};
+    for (int k = 0; k < nz + e[2]; ++k)
+      for (int j = 0; j < ny + e[1]; ++j)
+        for (int i = 0; i < nx + e[0]; ++i) {
+          const int w[3] = {i, j, k};
+          /* the two cells of the face: c0 = w - e_d, c1 = w; a cell outside
+             the block is a halo copy of its periodic image, with the values
+             from before the pass, local to this face */
+          double clh[2], uh[2];
+          int64_t cc[2];
+          for (int q = 0; q < 2; ++q) {
+            int v[3] = {w[0] - (q == 0 ? e[0] : 0), w[1] - (q == 0 ? e[1] : 0),
+                        w[2] - (q == 0 ? e[2] : 0)};
+            const int out = v[d] < 0 || v[d] >= n[d];
+            for (int a = 0; a < 3; ++a) v[a] = wrapi(v[a], n[a]);
+            const int64_t c = XIDX(v[0], v[1], v[2]);
+            cc[q] = out ? -1 : c;
+            clh[q] = out ? pre[c] : cl[c];
+            uh[q] = u[c];
+          }
+          for (int q = 0; q < 2; ++q) {
+            const int o = 1 - q;
+            const double clc = cc[q] >= 0 ? cl[cc[q]] : clh[q];
+            const double cln = cc[o] >= 0 ? cl[cc[o]] : clh[o];
+            if (clc == -1 && uh[q] > 0 && uh[o] > uh[q] && cln != -1) {
+              if (cc[q] >= 0) cl[cc[q]] = cln;
+              else clh[q] = cln;
+            }
+          }
+        }
+  }
+  free(pre);
+  free(used);
+  free(color);
+  free(has);
+  free(stable);
+  free(slot);
+  free(p);
+}

@@ -166,6 +166,12 @@ void orc_heights_curvature(
     const int n[3], const double h[3], const double* u, const double* nrm,
     double* kappa, double* hgt);
 
+/* Connected-component colours after a VOF step on one periodic block
+ * (Vof::MakeIteration resetcolor + union-find recolor + propagate,
+ * src/solver/vof.ipp:546-578): cl_prev the colours before, cl the result
+ * (-1: no colour). */
+void orc_recolor(const int n[3], const double* u, const double* cl_prev, double* cl);
+
 #ifdef __cplusplus
 }
 #endif

@@ -19,7 +19,9 @@
 //     Vof (scheme weymouth) StartStep/MakeIteration/FinishStep/PostStep and
 //     curvature::Heights::CalcCurvature per step, as in
 //     test/advection/main.cpp:242-256.  Writes out.u, out.n (3N AoS),
-//     out.a, out.k (after the last step) and out.sumu (text, per step).
+//     out.a, out.k, out.cl (Vof::GetColor, the connected-component colours
+//     of the default union-find recolouring; after the last step) and
+//     out.sumu (text, per step).
 //   overlap in out         rows (x y z hx hy hz cx cy cz r) -> GetSphereOverlap
 //   reconst in out         rows (n0 n1 n2 u a h0 h1 h2 q dt d) ->
 //                          GetLineA(n,u,h) GetLineU(n,a,h) GetLineFlux(...)
@@ -92,7 +94,7 @@ struct Global {
   Scal dt = 0, rho1 = 1, rho2 = 1;
   int steps = 0;
   std::vector<double> alpha, vflux, u;
-  std::vector<double> out_expr, out_p, out_flux, out_u, out_n, out_a, out_k;
+  std::vector<double> out_expr, out_p, out_flux, out_u, out_n, out_a, out_k, out_cl;
   std::vector<double> sumu;
   std::string out;
   Scal residual = 0;
@@ -299,9 +301,11 @@ void RunVof(M& m, Vars& var) {
     auto& u = t.as->GetField();
     auto& a = t.as->GetAlpha();
     auto& nn = t.as->GetNormal();
+    auto& cl = t.as->GetColor();
     for (auto c : m.Cells()) {
       const size_t i = GIdx(m.GetIndexCells().GetMIdx(c));
       g.out_u[i] = u[c];
+      g.out_cl[i] = cl[c];
       g.out_a[i] = a[c];
       g.out_k[i] = t.fck[0][c];
       for (int d = 0; d < 3; ++d) {
@@ -367,6 +371,7 @@ int Main(int argc, const char** argv) {
     g.out_u.assign(NCells(), 0);
     g.out_a.assign(NCells(), 0);
     g.out_k.assign(NCells(), 0);
+    g.out_cl.assign(NCells(), 0);
     g.out_n.assign(3 * NCells(), 0);
     std::string conf = MeshConf(nsz, bs);
     conf += "\nset string vof_scheme weymouth";
@@ -477,6 +482,7 @@ int main(int argc, const char** argv) {
     WriteRaw(g.out + ".n", g.out_n);
     WriteRaw(g.out + ".a", g.out_a);
     WriteRaw(g.out + ".k", g.out_k);
+    WriteRaw(g.out + ".cl", g.out_cl);
     std::ofstream fo(g.out + ".sumu");
     fo.precision(17);
     for (auto s : g.sumu) fo << s << "\n";

@@ -21,6 +21,11 @@ Fixtures:
   height.txt       UHeight::Good on the reference's unit-test columns
                    (test/util/main.cpp) and on random 13-cell columns.
   overlap.txt      GetSphereOverlap on random boxes (pins the generator).
+  colors.npz       Vof::GetColor (union-find recolouring) after 1, 3 and 8
+                   steps on one 32^3 block: 8 separate bubbles, 10 bubbles
+                   some of which touch, and spheres across the periodic
+                   boundary with a touching pair (inputs from the workload
+                   generator, stored as parameters).
   dumps.npz        dump::Xmf::WriteXmf texts of dump::Raw::WriteWithXmf
                    metadata for several meshes and element types, and
                    dump::Raw::WriteBlocks output of a 3x4x5 array converted
@@ -209,6 +214,39 @@ def overlap(tmp, rows=200):
             f.write(a + " | " + b + "\n")
 
 
+COLOR_STEPS = (1, 3, 8)
+
+
+def color_cases():
+    """(name, n, centres, radii, flux seed) of the colour fixtures."""
+    c0, r0 = workload.place_spheres(31, 8, 0.06, 0.14, gap=0.03)
+    c1, r1 = workload.place_spheres(77, 10, 0.08, 0.16, gap=0.0)
+    c2 = np.array([[0.02, 0.5, 0.5], [0.5, 0.97, 0.03], [0.5, 0.5, 0.5], [0.62, 0.5, 0.5]])
+    r2 = np.array([0.12, 0.1, 0.07, 0.07])
+    return [("separate", 32, c0, r0, 32), ("touching", 32, c1, r1, 9),
+            ("periodic", 32, c2, r2, 9)]
+
+
+def colors(tmp):
+    out = {"steps": np.array(COLOR_STEPS)}
+    for q, (name, n, c, r, seed) in enumerate(color_cases()):
+        case = workload.Case(n, c, r, seed=seed)
+        dt = case.cfl_dt(0.5)
+        case.alpha.tofile(os.path.join(tmp, "ca.bin"))
+        case.flux.tofile(os.path.join(tmp, "cf.bin"))
+        out["n%d" % q] = n
+        out["centres%d" % q] = np.asarray(c)
+        out["radii%d" % q] = np.asarray(r)
+        out["seed%d" % q] = seed
+        for s in COLOR_STEPS:
+            run(["vof", str(n), str(n), repr(case.h), repr(dt), str(s), "ca.bin", "cf.bin",
+                 "cv"], tmp)
+            cl = np.fromfile(os.path.join(tmp, "cv.cl"))
+            assert np.all(cl == np.round(cl)) and cl.min() >= -1 and cl.max() < 32767
+            out["cl%d_%d" % (q, s)] = cl.astype(np.int16)
+    np.savez_compressed(os.path.join(OUT, "colors.npz"), **out)
+
+
 XMF_CASES = [  # (nx, ny, nz, h, name, binpath, type)
     (16, 16, 16, 1 / 16, "vf", "vf.raw", "Double"),
     (32, 24, 16, 1 / 32, "p", "out/p_0001.raw", "Float"),
@@ -251,6 +289,7 @@ def main():
         height(args.ref, tmp)
         overlap(tmp)
         dumps(tmp)
+        colors(tmp)
     for f in sorted(os.listdir(OUT)):
         print(f, os.path.getsize(os.path.join(OUT, f)))
 

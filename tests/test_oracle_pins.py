@@ -201,3 +201,22 @@ def test_cg_converges_on_random_spd():
     e[:, 7] = r  # now A xs + e7 = 0
     x, info = oracle.cg_solve(n, 1.0, e.ravel(), 1e-12)
     assert np.max(np.abs(x - xs)) < 1e-8
+
+
+def test_oracle_colors_equal_reference():
+    """The oracle's union-find recolouring (resetcolor, recolor with the
+    stable colour map, propagate) gives aphros's own Vof::GetColor after 1,
+    3 and 8 steps: separate bubbles, touching bubbles that merge, and
+    spheres across the periodic boundary."""
+    fx = np.load(golden("colors.npz"))
+    steps = [int(s) for s in fx["steps"]]
+    for q in range(3):
+        n = int(fx["n%d" % q])
+        case = workload.Case(n, fx["centres%d" % q], fx["radii%d" % q], seed=int(fx["seed%d" % q]))
+        dt = case.cfl_dt(0.5)
+        st = oracle.VofState(n, case.h, case.alpha)
+        for s in range(1, max(steps) + 1):
+            st.step(case.flux, dt)
+            cl = st.recolor()
+            if s in steps:
+                assert np.array_equal(cl, fx["cl%d_%d" % (q, s)].astype(np.float64)), (q, s)
