@@ -112,6 +112,8 @@ def lib():
     L.aphgpu_mark.argtypes = [_P, _I]
     L.aphgpu_set_option.argtypes = [_P, _I, _I]
     L.aphgpu_set_option.restype = _I
+    L.aphgpu_vof_recolor.argtypes = [_P]
+    L.aphgpu_vof_colors.argtypes = [_P, _P]
     L.aphgpu_dump_raw.argtypes = [_P, _I, _I, ctypes.c_char_p, ctypes.c_char_p]
     L.aphgpu_read_raw.argtypes = [_P, _I, ctypes.c_char_p, ctypes.c_char_p]
     L.aphgpu_xmf_text.argtypes = [_I, _I, _I, _D, ctypes.c_char_p, ctypes.c_char_p, _I,
@@ -338,6 +340,15 @@ class Context:
     def set_option(self, option, value):
         """One of the OPT_* execution options (aphgpu_set_option)."""
         self._check(self._L.aphgpu_set_option(self._p, option, int(value)))
+
+    def vof_recolor(self):
+        """Connected-component colours of the current volume fraction."""
+        self._check(self._L.aphgpu_vof_recolor(self._p))
+
+    def vof_colors(self):
+        cl = np.empty(self.N)
+        self._check(self._L.aphgpu_vof_colors(self._p, ptr(cl)))
+        return cl
 
     def dump_raw(self, field, rawpath, name, dtype=DUMP_FLOAT64):
         """Writes a field to rawpath and its XMF beside it (aphgpu_dump_raw)."""

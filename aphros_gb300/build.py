@@ -38,6 +38,7 @@ CU_UNITS = {
     "server.cu": [],
     "batch.cu": [],
     "dump.cu": [],
+    "label.cu": [],
 }
 
 

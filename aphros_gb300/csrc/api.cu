@@ -453,9 +453,27 @@ int aphgpu_vof_init(aphgpu_ctx* ctx, const double* alpha, double clipth) {
   ctx->vof_count = 0;
   Timer t(ctx);
   APH_TRY(VofReconstruct(ctx));
+  APH_TRY(ColorInit(ctx));
   t.Stop();
   ctx->vof_ready = true;
   return APHGPU_OK;
+}
+
+int aphgpu_vof_recolor(aphgpu_ctx* ctx) {
+  if (!Valid(ctx)) return APHGPU_ERR_ARG;
+  if (!ctx->vof_ready) return SetError(ctx, APHGPU_ERR_STATE, "vof not initialised");
+  APH_TRY(SetDevice(ctx));
+  Timer t(ctx);
+  APH_TRY(Recolor(ctx));
+  t.Stop();
+  return APHGPU_OK;
+}
+
+int aphgpu_vof_colors(aphgpu_ctx* ctx, double* cl) {
+  if (!Valid(ctx) || !cl) return APHGPU_ERR_ARG;
+  if (!ctx->vof_ready) return SetError(ctx, APHGPU_ERR_STATE, "vof not initialised");
+  APH_TRY(SetDevice(ctx));
+  return D2H(ctx, cl, ctx->cl, sizeof(double) * ctx->N);
 }
 
 int aphgpu_vof_step(aphgpu_ctx* ctx, const double* vflux, double dt) {

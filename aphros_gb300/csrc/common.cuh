@@ -311,6 +311,18 @@ struct aphgpu_ctx {
 
   // device scratch of the field dumps (dump.cu)
   void* dump_scratch = nullptr;
+  // connected-component colours of the volume fraction (label.cu; -1 none)
+  double* cl = nullptr;
+  struct {
+    int* par = nullptr;     // union-find parent, then root (-1: not gas)
+    int* slot = nullptr;    // component slot of each root
+    int* croot = nullptr;   // root of each slot
+    unsigned long long* first = nullptr;  // first halo-order position per slot
+    double* stable = nullptr;  // previous colour at that position
+    double* color = nullptr;   // new colour per slot
+    double* pre = nullptr;     // colours before the propagation pass
+    int* ctl = nullptr;        // component count, error flag
+  } lab;
   // host staging (pinned)
   void* pinned = nullptr;
   size_t pinned_bytes = 0;
@@ -402,6 +414,8 @@ int Acceleration(aphgpu_ctx* ctx, double* d_acc, const double* d_alpha,
                  double rho1, double rho2);
 // vof.cu
 int VofReconstruct(aphgpu_ctx* ctx);
+int ColorInit(aphgpu_ctx* ctx);
+int Recolor(aphgpu_ctx* ctx);
 int VofStepDevice(aphgpu_ctx* ctx, const double* d_vflux, double dt);
 int CurvatureDevice(aphgpu_ctx* ctx);
 int SurfaceTensionDevice(aphgpu_ctx* ctx, double sigma, double* d_febp);

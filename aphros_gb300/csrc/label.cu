@@ -1,0 +1,318 @@
+// Connected-component colours of the volume fraction on one periodic block:
+// the resetcolor, union-find recolor and propagate stages of
+// Vof::MakeIteration (src/solver/vof.ipp:546-578) with
+// UVof::Imp::RecolorUnionFind (src/util/vof.ipp:982-1150), same results.
+//
+//   components  gas cells (u > 0.5), 26-connected across the periodic
+//               boundaries, by a lock-free union-find: a root is only ever
+//               hooked under a smaller root (atomicCAS), so each
+//               component's root is its first cell in x-fastest order, the
+//               cell whose unique initial colour the reference keeps;
+//   stable map  per component, the previous colour of its first cell in
+//               the order of the cells with two halo layers that has one
+//               (atomicMin of that order's 64-bit index);
+//   reduction   on the host over the components (few): the stable colour
+//               unless already given, else the next unused one;
+//   propagate   cells without colour with 0 < u take the colour of a face
+//               neighbour with larger u, faces in the mesh's order.  Faces of
+//               one direction that share no cell lie on different lines
+//               along that direction, so one thread replays one line in
+//               order; halo cells hold the colours from before the pass.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cstdint>
+#include <numeric>
+#include <set>
+#include <vector>
+
+#include "common.cuh"
+
+namespace aphgpu {
+namespace {
+
+constexpr int kLabelThreads = 256;
+constexpr int kMaxComponents = 1 << 21;
+constexpr unsigned long long kNoFirst = ~0ull;
+
+__device__ __forceinline__ int Wrap(int i, int n) { return i < 0 ? i + n : (i >= n ? i - n : i); }
+
+// Root of x (bounded walk; the tree depth is below the cell count).
+__device__ __forceinline__ int Find(const volatile int* par, int x, int64_t cap) {
+  for (int64_t it = 0; it < cap; ++it) {
+    const int p = par[x];
+    if (p == x) return x;
+    x = p;
+  }
+  return x;
+}
+
+__global__ void KLabelInit(int64_t n, const double* __restrict__ u, int* par) {
+  for (int64_t c = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; c < n;
+       c += (int64_t)gridDim.x * blockDim.x)
+    par[c] = u[c] > 0.5 ? (int)c : -1;
+}
+
+// Union of every gas cell with its gas neighbours in the 13 offsets of one
+// half of the 3x3x3 stencil (the other half is the same pairs reversed).
+__global__ void KLabelUnion(Dims d, int* par, int* err) {
+  const int64_t n = d.cells();
+  volatile int* vp = par;
+  for (int64_t c = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; c < n;
+       c += (int64_t)gridDim.x * blockDim.x) {
+    if (vp[c] < 0) continue;
+    const int i = (int)(c % d.nx), j = (int)((c / d.nx) % d.ny), k = (int)(c / ((int64_t)d.nx * d.ny));
+    for (int o = 0; o < 13; ++o) {
+      // offsets with dz > 0, or dz == 0 and dy > 0, or dz == dy == 0, dx > 0
+      const int q = o + 14;  // 14..26 in the 27-point numbering
+      const int dx = q % 3 - 1, dy = (q / 3) % 3 - 1, dz = q / 9 - 1;
+      const int64_t cn = d.idx(Wrap(i + dx, d.nx), Wrap(j + dy, d.ny), Wrap(k + dz, d.nz));
+      if (cn == c || vp[cn] < 0) continue;
+      int a = (int)c, b = (int)cn;
+      bool done = false;
+      for (int it = 0; it < (1 << 20) && !done; ++it) {
+        a = Find(vp, a, n);
+        b = Find(vp, b, n);
+        if (a == b) {
+          done = true;
+        } else {
+          if (a < b) {
+            const int t = a;
+            a = b;
+            b = t;
+          }
+          // hook the larger root under the smaller, if still a root
+          if (atomicCAS(&par[a], a, b) == a) done = true;
+        }
+      }
+      if (!done) atomicExch(err, 1);
+    }
+  }
+}
+
+// Roots of all gas cells; each root gets a component slot.
+__global__ void KLabelFlatten(int64_t n, int* par, int* slot, int* ncomp, int* croot, int cap,
+                              int* err) {
+  volatile int* vp = par;
+  for (int64_t c = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; c < n;
+       c += (int64_t)gridDim.x * blockDim.x) {
+    if (vp[c] < 0) continue;
+    const int r = Find(vp, (int)c, n);
+    if (r == (int)c) {
+      const int s = atomicAdd(ncomp, 1);
+      if (s < cap) {
+        slot[c] = s;
+        croot[s] = (int)c;
+      } else {
+        atomicExch(err, 2);
+      }
+    }
+  }
+}
+
+__global__ void KLabelRoot(int64_t n, int* par) {
+  volatile int* vp = par;
+  for (int64_t c = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; c < n;
+       c += (int64_t)gridDim.x * blockDim.x) {
+    if (vp[c] < 0) continue;
+    par[c] = Find(vp, (int)c, n);
+  }
+}
+
+// The first position, in the order of the cells with two halo layers
+// (x-fastest over [-2, n+2) per axis), of a gas cell of each component that
+// has a previous colour.  A cell's smallest position takes its left halo
+// copy where it has one (the last two cells of an axis).
+__global__ void KLabelFirst(Dims d, const int* __restrict__ root, const int* __restrict__ slot,
+                            const double* __restrict__ clprev, unsigned long long* first) {
+  const int64_t n = d.cells();
+  const unsigned long long ex = d.nx + 4, ey = d.ny + 4;
+  for (int64_t c = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; c < n;
+       c += (int64_t)gridDim.x * blockDim.x) {
+    const int r = root[c];
+    if (r < 0 || clprev[c] == -1.0) continue;
+    const int i = (int)(c % d.nx), j = (int)((c / d.nx) % d.ny), k = (int)(c / ((int64_t)d.nx * d.ny));
+    const int xi = i >= d.nx - 2 ? i - d.nx + 2 : i + 2;
+    const int yj = j >= d.ny - 2 ? j - d.ny + 2 : j + 2;
+    const int zk = k >= d.nz - 2 ? k - d.nz + 2 : k + 2;
+    const unsigned long long e = ((unsigned long long)zk * ey + yj) * ex + xi;
+    atomicMin(&first[slot[r]], e);
+  }
+}
+
+// Previous colour at each component's first position.
+__global__ void KLabelStable(Dims d, int nc, const unsigned long long* __restrict__ first,
+                             const double* __restrict__ clprev, double* stable) {
+  const unsigned long long ex = d.nx + 4, ey = d.ny + 4;
+  for (int s = blockIdx.x * blockDim.x + threadIdx.x; s < nc; s += gridDim.x * blockDim.x) {
+    const unsigned long long e = first[s];
+    if (e == kNoFirst) {
+      stable[s] = -1.0;
+      continue;
+    }
+    const int i = Wrap((int)(e % ex) - 2, d.nx);
+    const int j = Wrap((int)((e / ex) % ey) - 2, d.ny);
+    const int k = Wrap((int)(e / (ex * ey)) - 2, d.nz);
+    stable[s] = clprev[d.idx(i, j, k)];
+  }
+}
+
+// New colours (and their copy from before the propagation pass).
+__global__ void KLabelApply(int64_t n, const int* __restrict__ root, const int* __restrict__ slot,
+                            const double* __restrict__ color, double* cl, double* pre) {
+  for (int64_t c = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; c < n;
+       c += (int64_t)gridDim.x * blockDim.x) {
+    const int r = root[c];
+    const double v = r < 0 ? -1.0 : color[slot[r]];
+    cl[c] = v;
+    pre[c] = v;
+  }
+}
+
+// The faces of direction `dir` of one line, in order: face w lies between
+// the line's cells w-1 and w; at w = 0 and w = m the outer cell is the
+// halo copy of the line's other end, with the colour from before the pass.
+__global__ void KLabelPropagate(Dims d, int dir, const double* __restrict__ u, double* cl,
+                                const double* __restrict__ pre) {
+  const int m = dir == 0 ? d.nx : dir == 1 ? d.ny : d.nz;
+  const int64_t stride = dir == 0 ? 1 : dir == 1 ? (int64_t)d.nx : (int64_t)d.nx * d.ny;
+  const int64_t nlines = d.cells() / m;
+  for (int64_t l = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; l < nlines;
+       l += (int64_t)gridDim.x * blockDim.x) {
+    int64_t base;
+    if (dir == 0) {
+      base = l * d.nx;
+    } else if (dir == 1) {
+      const int64_t x = l % d.nx, z = l / d.nx;
+      base = x + z * (int64_t)d.nx * d.ny;
+    } else {
+      base = l;
+    }
+    const int64_t last = base + (int64_t)(m - 1) * stride;
+    double cl0 = pre[last], u0 = u[last];  // halo copy before cell 0
+    for (int w = 0; w <= m; ++w) {
+      const int64_t c1 = base + (int64_t)w * stride;
+      double cl1, u1;
+      if (w < m) {
+        cl1 = cl[c1];
+        u1 = u[c1];
+      } else {
+        cl1 = pre[base];  // halo copy after the last cell
+        u1 = u[base];
+      }
+      if (cl0 == -1.0 && u0 > 0 && u1 > u0 && cl1 != -1.0) {
+        cl0 = cl1;
+        if (w > 0) cl[c1 - stride] = cl0;
+      }
+      if (cl1 == -1.0 && u1 > 0 && u0 > u1 && cl0 != -1.0) {
+        cl1 = cl0;
+        if (w < m) cl[c1] = cl1;
+      }
+      cl0 = cl1;
+      u0 = u1;
+    }
+  }
+}
+
+__global__ void KColorInit(int64_t n, const double* __restrict__ u, double* cl) {
+  for (int64_t c = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; c < n;
+       c += (int64_t)gridDim.x * blockDim.x)
+    cl[c] = u[c] > 0 ? 0.0 : -1.0;
+}
+
+int Blocks(int64_t n) { return FlatBlocks(n); }
+
+}  // namespace
+
+// Colours as the reference's Vof starts them from a zero colour field:
+// 0 where u > 0, none elsewhere (src/solver/vof.ipp:53-57).
+int ColorInit(aphgpu_ctx* ctx) {
+  const int64_t N = ctx->N;
+  if (!ctx->cl) APH_TRY(Alloc(ctx, &ctx->cl, N));
+  KColorInit<<<Blocks(N), kLabelThreads, 0, ctx->stream>>>(N, ctx->u, ctx->cl);
+  APH_LAUNCHED(ctx);
+  return APHGPU_OK;
+}
+
+int Recolor(aphgpu_ctx* ctx) {
+  const Dims d = ctx->d;
+  const int64_t N = ctx->N;
+  cudaStream_t st = ctx->stream;
+  auto& L = ctx->lab;
+  if (!L.par) {
+    APH_TRY(Alloc(ctx, &L.par, N));
+    APH_TRY(Alloc(ctx, &L.slot, N));
+    APH_TRY(Alloc(ctx, &L.croot, kMaxComponents));
+    APH_TRY(Alloc(ctx, &L.first, kMaxComponents));
+    APH_TRY(Alloc(ctx, &L.stable, kMaxComponents));
+    APH_TRY(Alloc(ctx, &L.color, kMaxComponents));
+    APH_TRY(Alloc(ctx, &L.pre, N));
+    APH_TRY(Alloc(ctx, &L.ctl, 4));
+  }
+  const int nb = Blocks(N);
+  APH_CUDA(ctx, cudaMemsetAsync(L.ctl, 0, 4 * sizeof(int), st));
+  KLabelInit<<<nb, kLabelThreads, 0, st>>>(N, ctx->u, L.par);
+  APH_LAUNCHED(ctx);
+  KLabelUnion<<<nb, kLabelThreads, 0, st>>>(d, L.par, L.ctl + 1);
+  APH_LAUNCHED(ctx);
+  KLabelFlatten<<<nb, kLabelThreads, 0, st>>>(N, L.par, L.slot, L.ctl, L.croot, kMaxComponents,
+                                              L.ctl + 1);
+  APH_LAUNCHED(ctx);
+  KLabelRoot<<<nb, kLabelThreads, 0, st>>>(N, L.par);
+  APH_LAUNCHED(ctx);
+  int hc[2] = {0, 0};
+  APH_CUDA(ctx, cudaMemcpyAsync(hc, L.ctl, sizeof(hc), cudaMemcpyDeviceToHost, st));
+  APH_CUDA(ctx, cudaStreamSynchronize(st));
+  if (hc[1] == 1) return SetError(ctx, APHGPU_ERR_TIMEOUT, "recolor: union did not settle");
+  if (hc[1] == 2 || hc[0] > kMaxComponents)
+    return SetError(ctx, APHGPU_ERR_UNSUPPORTED, "recolor: more than %d components",
+                    kMaxComponents);
+  const int nc = hc[0];
+  std::vector<double> color(std::max(nc, 1));
+  if (nc > 0) {
+    APH_CUDA(ctx, cudaMemsetAsync(L.first, 0xff, sizeof(unsigned long long) * nc, st));
+    KLabelFirst<<<nb, kLabelThreads, 0, st>>>(d, L.par, L.slot, ctx->cl, L.first);
+    APH_LAUNCHED(ctx);
+    KLabelStable<<<Blocks(nc), kLabelThreads, 0, st>>>(d, nc, L.first, ctx->cl, L.stable);
+    APH_LAUNCHED(ctx);
+    std::vector<int> croot(nc);
+    std::vector<double> stable(nc);
+    APH_CUDA(ctx, cudaMemcpyAsync(croot.data(), L.croot, sizeof(int) * nc, cudaMemcpyDeviceToHost, st));
+    APH_CUDA(ctx, cudaMemcpyAsync(stable.data(), L.stable, sizeof(double) * nc,
+                                  cudaMemcpyDeviceToHost, st));
+    APH_CUDA(ctx, cudaStreamSynchronize(st));
+    // ReduceColor over the components in the order of their first cells
+    std::vector<int> order(nc);
+    std::iota(order.begin(), order.end(), 0);
+    std::sort(order.begin(), order.end(), [&](int a, int b) { return croot[a] < croot[b]; });
+    double next = 0;
+    for (int s = 0; s < nc; ++s)
+      if (stable[s] != -1.0) next = std::max(next, stable[s]);
+    next += 1;
+    std::set<double> used;
+    for (int s : order) {
+      if (stable[s] == -1.0 || used.count(stable[s])) {
+        color[s] = next;
+        next += 1;
+      } else {
+        color[s] = stable[s];
+      }
+      used.insert(color[s]);
+    }
+    APH_CUDA(ctx, cudaMemcpyAsync(L.color, color.data(), sizeof(double) * nc,
+                                  cudaMemcpyHostToDevice, st));
+  }
+  KLabelApply<<<nb, kLabelThreads, 0, st>>>(N, L.par, L.slot, L.color, ctx->cl, L.pre);
+  APH_LAUNCHED(ctx);
+  for (int dir = 0; dir < 3; ++dir) {
+    const int m = dir == 0 ? d.nx : dir == 1 ? d.ny : d.nz;
+    const int64_t nlines = N / m;
+    KLabelPropagate<<<Blocks(nlines), kLabelThreads, 0, st>>>(d, dir, ctx->u, ctx->cl, L.pre);
+    APH_LAUNCHED(ctx);
+  }
+  // the host vector of colours stays alive until the copy has completed
+  APH_CUDA(ctx, cudaStreamSynchronize(st));
+  return APHGPU_OK;
+}
+
+}  // namespace aphgpu

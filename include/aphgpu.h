@@ -436,6 +436,20 @@ enum {
 int aphgpu_time_kernel(aphgpu_ctx* ctx, int kernel, int reps, double* ms,
                        double* bytes);
 
+/* ---- connected-component colours of the volume fraction ---- */
+
+/* Recolours the current volume fraction as Vof::MakeIteration does after
+ * its sweeps (src/solver/vof.ipp:546-578, union-find recolouring of
+ * src/util/vof.ipp:982-1150 with the stable colour map): gas cells (u >
+ * 0.5) connected through faces, edges or corners, across the periodic
+ * boundaries, share a colour; a bubble keeps its colour from the previous
+ * call (or from aphgpu_vof_init: 0 where u > 0); cells with 0 < u <= 0.5
+ * take the colour of a face neighbour with larger u.  Call after each
+ * aphgpu_vof_step for the reference's colours. */
+int aphgpu_vof_recolor(aphgpu_ctx* ctx);
+/* Colours of the cells (-1: none), N doubles (Vof::GetColor). */
+int aphgpu_vof_colors(aphgpu_ctx* ctx, double* cl);
+
 /* ---- field dumps (aphros raw + XMF format) ---- */
 
 /* Fields of a context: pressure (the solution x), the right-hand side of

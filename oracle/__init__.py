@@ -230,6 +230,16 @@ class VofState:
         return (k, hg) if heights else k
 
 
+def recolor(n, u, cl_prev):
+    """Colours of volume fraction u given the colours before (orc_recolor)."""
+    n3c, n3 = _n3(n)
+    u = np.ascontiguousarray(u, dtype=np.float64)
+    cp = np.ascontiguousarray(cl_prev, dtype=np.float64)
+    out = np.empty(n3[0] * n3[1] * n3[2])
+    lib().orc_recolor(n3c, _p(u), _p(cp), _p(out))
+    return out
+
+
 def line_a(n, u, h):
     return lib().orc_line_a(_D3(*n), u, _D3(*h))
 
