@@ -34,7 +34,10 @@ def test_colors_equal_reference():
             assert np.array_equal(cl, oracle.recolor(n, u, prev)), (q, s)
             st.step(case.flux, dt)
             st.recolor()
-            if s in steps and np.array_equal(u, st.u):
+            if s in steps:
+                # the oracle's field is aphros's (pinned on the CPU); on
+                # these 32^3 cases the GPU's field is the same bits
+                assert np.array_equal(u, st.u), (q, s)
                 assert np.array_equal(cl, fx["cl%d_%d" % (q, s)].astype(np.float64)), (q, s)
         ctx.close()
 
