@@ -35,9 +35,10 @@ def test_colors_equal_reference():
             st.step(case.flux, dt)
             st.recolor()
             if s in steps:
-                # the oracle's field is aphros's (pinned on the CPU); on
-                # these 32^3 cases the GPU's field is the same bits
-                assert np.array_equal(u, st.u), (q, s)
+                # the oracle's field is aphros's (pinned on the CPU); the
+                # GPU's agrees to round-off (not always to the last bit),
+                # far from the colour thresholds here
+                assert np.max(np.abs(u - st.u)) <= 1e-12, (q, s)
                 assert np.array_equal(cl, fx["cl%d_%d" % (q, s)].astype(np.float64)), (q, s)
         ctx.close()
 
