@@ -322,6 +322,7 @@ struct aphgpu_ctx {
     double* color = nullptr;   // new colour per slot
     double* pre = nullptr;     // colours before the propagation pass
     int* ctl = nullptr;        // component count, error flag
+    unsigned char* flag = nullptr;  // lines the propagation pass visits
   } lab;
   // host staging (pinned)
   void* pinned = nullptr;

@@ -157,15 +157,27 @@ __global__ void KLabelStable(Dims d, int nc, const unsigned long long* __restric
   }
 }
 
-// New colours (and their copy from before the propagation pass).
-__global__ void KLabelApply(int64_t n, const int* __restrict__ root, const int* __restrict__ slot,
-                            const double* __restrict__ color, double* cl, double* pre) {
+// New colours (and their copy from before the propagation pass).  Cells
+// the propagation may colour (none, u > 0) flag their line of each
+// direction; a line without such a cell cannot change and is skipped.
+__global__ void KLabelApply(Dims d, const int* __restrict__ root, const int* __restrict__ slot,
+                            const double* __restrict__ color, const double* __restrict__ u,
+                            double* cl, double* pre, unsigned char* flag) {
+  const int64_t n = d.cells();
+  unsigned char* f1 = flag + (int64_t)d.ny * d.nz;
+  unsigned char* f2 = f1 + (int64_t)d.nx * d.nz;
   for (int64_t c = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; c < n;
        c += (int64_t)gridDim.x * blockDim.x) {
     const int r = root[c];
     const double v = r < 0 ? -1.0 : color[slot[r]];
     cl[c] = v;
     pre[c] = v;
+    if (v == -1.0 && u[c] > 0) {
+      const int64_t x = c % d.nx, y = (c / d.nx) % d.ny, z = c / ((int64_t)d.nx * d.ny);
+      flag[c / d.nx] = 1;
+      f1[x + z * d.nx] = 1;
+      f2[x + y * d.nx] = 1;
+    }
   }
 }
 
@@ -173,12 +185,14 @@ __global__ void KLabelApply(int64_t n, const int* __restrict__ root, const int* 
 // the line's cells w-1 and w; at w = 0 and w = m the outer cell is the
 // halo copy of the line's other end, with the colour from before the pass.
 __global__ void KLabelPropagate(Dims d, int dir, const double* __restrict__ u, double* cl,
-                                const double* __restrict__ pre) {
+                                const double* __restrict__ pre,
+                                const unsigned char* __restrict__ flag) {
   const int m = dir == 0 ? d.nx : dir == 1 ? d.ny : d.nz;
   const int64_t stride = dir == 0 ? 1 : dir == 1 ? (int64_t)d.nx : (int64_t)d.nx * d.ny;
   const int64_t nlines = d.cells() / m;
   for (int64_t l = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; l < nlines;
        l += (int64_t)gridDim.x * blockDim.x) {
+    if (!flag[l]) continue;
     int64_t base;
     if (dir == 0) {
       base = l * d.nx;
@@ -222,6 +236,12 @@ __global__ void KColorInit(int64_t n, const double* __restrict__ u, double* cl) 
 
 int Blocks(int64_t n) { return FlatBlocks(n); }
 
+// Line flags of the three directions: ny*nz x-lines, nx*nz y-lines, nx*ny
+// z-lines.
+int64_t LineFlags(const Dims& d) {
+  return (int64_t)d.ny * d.nz + (int64_t)d.nx * d.nz + (int64_t)d.nx * d.ny;
+}
+
 }  // namespace
 
 // Colours as the reference's Vof starts them from a zero colour field:
@@ -248,6 +268,7 @@ int Recolor(aphgpu_ctx* ctx) {
     APH_TRY(Alloc(ctx, &L.color, kMaxComponents));
     APH_TRY(Alloc(ctx, &L.pre, N));
     APH_TRY(Alloc(ctx, &L.ctl, 4));
+    APH_TRY(Alloc(ctx, &L.flag, LineFlags(d)));
   }
   const int nb = Blocks(N);
   APH_CUDA(ctx, cudaMemsetAsync(L.ctl, 0, 4 * sizeof(int), st));
@@ -302,13 +323,17 @@ int Recolor(aphgpu_ctx* ctx) {
     APH_CUDA(ctx, cudaMemcpyAsync(L.color, color.data(), sizeof(double) * nc,
                                   cudaMemcpyHostToDevice, st));
   }
-  KLabelApply<<<nb, kLabelThreads, 0, st>>>(N, L.par, L.slot, L.color, ctx->cl, L.pre);
+  APH_CUDA(ctx, cudaMemsetAsync(L.flag, 0, (size_t)LineFlags(d), st));
+  KLabelApply<<<nb, kLabelThreads, 0, st>>>(d, L.par, L.slot, L.color, ctx->u, ctx->cl, L.pre,
+                                            L.flag);
   APH_LAUNCHED(ctx);
+  const unsigned char* fl = L.flag;
   for (int dir = 0; dir < 3; ++dir) {
     const int m = dir == 0 ? d.nx : dir == 1 ? d.ny : d.nz;
     const int64_t nlines = N / m;
-    KLabelPropagate<<<Blocks(nlines), kLabelThreads, 0, st>>>(d, dir, ctx->u, ctx->cl, L.pre);
+    KLabelPropagate<<<Blocks(nlines), kLabelThreads, 0, st>>>(d, dir, ctx->u, ctx->cl, L.pre, fl);
     APH_LAUNCHED(ctx);
+    fl += nlines;
   }
   // the host vector of colours stays alive until the copy has completed
   APH_CUDA(ctx, cudaStreamSynchronize(st));
