@@ -220,3 +220,51 @@ def test_oracle_colors_equal_reference():
             cl = st.recolor()
             if s in steps:
                 assert np.array_equal(cl, fx["cl%d_%d" % (q, s)].astype(np.float64)), (q, s)
+
+
+def test_oracle_colors_properties():
+    """Properties of the recolouring on random fields: every gas cell is
+    coloured, 26-adjacent gas cells (periodic) share a colour, distinct
+    components get distinct colours, and recolouring an unchanged field
+    keeps every colour."""
+    rng = np.random.default_rng(23)
+    for n in ((12, 10, 8), (9, 9, 9)):
+        u = rng.uniform(size=n[0] * n[1] * n[2])
+        u[u < 0.4] = 0.0
+        prev = np.where(u > 0, 0.0, -1.0)
+        cl = oracle.recolor(n, u, prev)
+        gas = u > 0.5
+        assert np.all(cl[gas] >= 0)
+        g = gas.reshape(n[2], n[1], n[0])
+        c3 = cl.reshape(n[2], n[1], n[0])
+        for dz in (-1, 0, 1):
+            for dy in (-1, 0, 1):
+                for dx in (-1, 0, 1):
+                    gn = np.roll(g, (-dz, -dy, -dx), axis=(0, 1, 2))
+                    cn = np.roll(c3, (-dz, -dy, -dx), axis=(0, 1, 2))
+                    both = g & gn
+                    assert np.array_equal(c3[both], cn[both])
+        # distinct components: the colours of gas cells number the
+        # components (scipy's labelling with periodic merging as the check)
+        from scipy import ndimage
+        lab, nlab = ndimage.label(g, structure=np.ones((3, 3, 3)))
+        # merge labels across the periodic boundaries
+        parent = list(range(nlab + 1))
+
+        def find(a):
+            while parent[a] != a:
+                parent[a] = parent[parent[a]]
+                a = parent[a]
+            return a
+        for ax in range(3):
+            a = np.take(lab, 0, axis=ax)
+            for sh in (-1, 0, 1):
+                for sh2 in (-1, 0, 1):
+                    b = np.take(lab, -1, axis=ax)
+                    b = np.roll(np.roll(b, sh, axis=0), sh2, axis=1)
+                    m = (a > 0) & (b > 0)
+                    for x, y in zip(a[m], b[m]):
+                        parent[find(x)] = find(y)
+        ncomp = len({find(v) for v in np.unique(lab[lab > 0])})
+        assert len(np.unique(cl[gas])) == ncomp
+        assert np.array_equal(oracle.recolor(n, u, cl), cl)
