@@ -445,7 +445,10 @@ int aphgpu_time_kernel(aphgpu_ctx* ctx, int kernel, int reps, double* ms,
  * boundaries, share a colour; a bubble keeps its colour from the previous
  * call (or from aphgpu_vof_init: 0 where u > 0); cells with 0 < u <= 0.5
  * take the colour of a face neighbour with larger u.  Call after each
- * aphgpu_vof_step for the reference's colours. */
+ * aphgpu_vof_step for the reference's colours.  Errors: APHGPU_ERR_STATE
+ * before aphgpu_vof_init; APHGPU_ERR_UNSUPPORTED beyond 2^21 components;
+ * APHGPU_ERR_TIMEOUT if the bounded union-find loop did not settle (the
+ * colours are then left unchanged). */
 int aphgpu_vof_recolor(aphgpu_ctx* ctx);
 /* Colours of the cells (-1: none), N doubles (Vof::GetColor). */
 int aphgpu_vof_colors(aphgpu_ctx* ctx, double* cl);
