@@ -3,9 +3,11 @@ curvature estimator, running on the GPU through libaphgpu.
 
 `Vof` follows AdvectionSolver/Vof (src/solver/advection.h:58-100,
 src/solver/vof.h:62-112): StartStep / MakeIteration / FinishStep / PostStep,
-GetField / GetAlpha / GetNormal / GetMask / GetPlic.  `Heights` follows
-curvature::Heights::CalcCurvature (src/solver/curv.h:70-90).  Scheme is
-weymouth (the VofPar default, src/solver/vof.h:44); no colour labelling.
+GetField / GetAlpha / GetNormal / GetMask / GetColor / GetPlic.  `Heights`
+follows curvature::Heights::CalcCurvature (src/solver/curv.h:70-90).
+Scheme is weymouth (the VofPar default, src/solver/vof.h:44); with
+`recolor=True` each MakeIteration also recolours the field as the
+reference's default union-find labelling does (vof.ipp:546-578).
 """
 import numpy as np
 
@@ -32,10 +34,11 @@ class Vof:
 
     m: linear.Mesh; fcu: initial volume fraction (ncells); fev: face fluxes
     (3 face blocks, see include/aphgpu.h); dt: time step; clipth: VofPar
-    clipping threshold (default 1e-10)."""
+    clipping threshold (default 1e-10); recolor: connected-component
+    colours after every iteration (GetColor)."""
 
     def __init__(self, m, fcu, fev, t=0.0, dt=0.0, clipth=1e-10, device=0,
-                 ctx=None):
+                 ctx=None, recolor=False):
         self.m = m
         self.ctx = ctx if ctx is not None else _lib.Context(m.n, m.h, device)
         self.fev = None if fev is None else np.ascontiguousarray(fev, dtype=np.float64)
@@ -45,6 +48,7 @@ class Vof:
         self._u0 = np.ascontiguousarray(fcu, dtype=np.float64)
         self._started = False
         self._cache = None
+        self.recolor = recolor
 
     def SetTimeStep(self, dt):
         self.dt = dt
@@ -68,6 +72,8 @@ class Vof:
 
     def MakeIteration(self):
         self.ctx.vof_step(self.fev, self.dt)
+        if self.recolor:
+            self.ctx.vof_recolor()
         self._cache = None
 
     def FinishStep(self):
@@ -92,6 +98,10 @@ class Vof:
 
     def GetMask(self):
         return self._state()[3]
+
+    def GetColor(self):
+        """Vof::GetColor (vof.ipp:741-743): -1 where no colour."""
+        return self.ctx.vof_colors()
 
     def GetPlic(self):
         return Plic(self)
