@@ -240,6 +240,19 @@ def recolor(n, u, cl_prev):
     return out
 
 
+def interpolate_bcg(n, h, u, vflux, src, dt):
+    """Face values of the BCG predictor (orc_interpolate_bcg): 3 face blocks."""
+    n3c, n3 = _n3(n)
+    N = n3[0] * n3[1] * n3[2]
+    u = np.ascontiguousarray(u, dtype=np.float64)
+    s = np.ascontiguousarray(src, dtype=np.float64)
+    vf, vfp = _faces(vflux, N)
+    out = np.empty(3 * N)
+    oa, op = _faces(out, N)
+    lib().orc_interpolate_bcg(n3c, _D(h), _p(u), vfp, _p(s), _D(dt), op)
+    return oa
+
+
 def line_a(n, u, h):
     return lib().orc_line_a(_D3(*n), u, _D3(*h))
 

@@ -1044,3 +1044,68 @@ void orc_recolor(const int n[3], const double* u, const double* cl_prev, double*
   free(slot);
   free(p);
 }
+
+/* ------------------------------------------------------------------------
+ * BCG face predictor of a cell field on a periodic mesh of cubic cells:
+ * UEmbed::InterpolateBcg (src/solver/approx_eb.ipp:753-821) without
+ * boundary conditions, with UEmbed::Gradient (approx_eb.ipp:882-890).
+ * Faces of direction d are stored at the index of their plus cell
+ * (between c - e_d and c).  u: cell field; vflux: face volume fluxes;
+ * src: cell source (the acceleration component); out: face values.
+ * ------------------------------------------------------------------------ */
+void orc_interpolate_bcg(const int n[3], double h, const double* u,
+                         const double* const vflux[3], const double* src, double dt,
+                         double* const out[3]) {
+  const int nx = n[0], ny = n[1], nz = n[2];
+  const int64_t N = (int64_t)nx * ny * nz;
+  const double area = h * h;
+  /* face gradients (u(cp) - u(cm)) / h */
+  double* g[3];
+  for (int d = 0; d < 3; ++d) {
+    g[d] = (double*)malloc(sizeof(double) * N);
+    for (int k = 0; k < nz; ++k)
+      for (int j = 0; j < ny; ++j)
+        for (int i = 0; i < nx; ++i) {
+          const int64_t c = XIDX(i, j, k);
+          const int64_t cm = XIDX(wrapi(i - (d == 0), nx), wrapi(j - (d == 1), ny),
+                                  wrapi(k - (d == 2), nz));
+          g[d][c] = (u[c] - u[cm]) / h;
+        }
+  }
+  for (int d0 = 0; d0 < 3; ++d0)
+    for (int k = 0; k < nz; ++k)
+      for (int j = 0; j < ny; ++j)
+        for (int i = 0; i < nx; ++i) {
+          const int64_t cp = XIDX(i, j, k);
+          const int ci[3] = {wrapi(i - (d0 == 0), nx), wrapi(j - (d0 == 1), ny),
+                             wrapi(k - (d0 == 2), nz)};
+          const int64_t cm = XIDX(ci[0], ci[1], ci[2]);
+          const double v = vflux[d0][cp];
+          const double sgn = v > 0 ? 1 : -1;
+          /* upwind cell and its coordinates */
+          const int64_t c = sgn > 0 ? cm : cp;
+          const int w[3] = {sgn > 0 ? ci[0] : i, sgn > 0 ? ci[1] : j, sgn > 0 ? ci[2] : k};
+          double ut = (src[cm] + src[cp]) * 0.5;
+          double ux = 0;
+          int d = d0;
+          {
+            /* faces of the upwind cell in -d (its own index) and +d */
+            const int64_t fm = c;
+            const int64_t fp = XIDX(wrapi(w[0] + (d == 0), nx), wrapi(w[1] + (d == 1), ny),
+                                    wrapi(w[2] + (d == 2), nz));
+            ux += (g[d][fm] + g[d][fp]) * 0.5;
+            const double vel = v / area;
+            ut -= ux * vel;
+          }
+          for (int t = 0; t < 2; ++t) {
+            d = (d + 1) % 3;
+            const int64_t fm = c;
+            const int64_t fp = XIDX(wrapi(w[0] + (d == 0), nx), wrapi(w[1] + (d == 1), ny),
+                                    wrapi(w[2] + (d == 2), nz));
+            const double vel = (vflux[d][fm] + vflux[d][fp]) / (area + area);
+            ut -= g[d][vel > 0 ? fm : fp] * vel;
+          }
+          out[d0][cp] = u[c] + ux * (sgn * 0.5 * h) + ut * (0.5 * dt);
+        }
+  for (int d = 0; d < 3; ++d) free(g[d]);
+}

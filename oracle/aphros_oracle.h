@@ -172,6 +172,13 @@ void orc_heights_curvature(
  * (-1: no colour). */
 void orc_recolor(const int n[3], const double* u, const double* cl_prev, double* cl);
 
+/* BCG face predictor of a cell field, periodic, cubic cells of edge h
+ * (UEmbed::InterpolateBcg, src/solver/approx_eb.ipp:753-821); face arrays
+ * of direction d at the index of the plus cell. */
+void orc_interpolate_bcg(const int n[3], double h, const double* u,
+                         const double* const vflux[3], const double* src, double dt,
+                         double* const out[3]);
+
 #ifdef __cplusplus
 }
 #endif

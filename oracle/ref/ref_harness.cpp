@@ -26,6 +26,10 @@
 //   reconst in out         rows (n0 n1 n2 u a h0 h1 h2 q dt d) ->
 //                          GetLineA(n,u,h) GetLineU(n,a,h) GetLineFlux(...)
 //   height  in out         rows (column, optional n=N) -> UHeight::Good
+//   bcg   n bs dt u.bin vflux.bin src.bin out
+//     UEmbed::InterpolateBcg (solver/approx_eb.ipp:753-821), periodic (no
+//     boundary conditions): the cell field u advected to the faces by dt/2
+//     with the face fluxes and the cell source src.  Writes out.ffu (3N).
 //   xmf   n h name binpath type out.xmf
 //     dump::Xmf::WriteXmf of the metadata that dump::Raw::WriteWithXmf
 //     writes for a field of an n-cell mesh with cell size h (dump/raw.ipp:
@@ -222,6 +226,36 @@ void RunProj(M& m, Vars& var) {
   }
 }
 
+void RunBcg(M& m, Vars&) {
+  auto sem = m.GetSem(__func__);
+  if (sem("bcg")) {
+    FieldCell<Scal> fcu(m), fcs(m);
+    for (auto c : m.AllCells()) {
+      const size_t i = GIdx(m.GetIndexCells().GetMIdx(c));
+      fcu[c] = g.u[i];
+      fcs[c] = g.alpha[i];
+    }
+    FieldFace<Scal> ffv(m, 0);
+    for (auto f : m.AllFaces()) {
+      ffv[f] = FaceInput(m, f, g.vflux);
+    }
+    const FieldFace<Scal> ffu =
+        UEB::InterpolateBcg(fcu, MapEmbed<BCond<Scal>>(), ffv, fcs, g.dt, m);
+    for (auto f : m.Faces()) {
+      const auto p = m.GetIndexFaces().GetMIdxDir(f);
+      const MIdx w = p.first;
+      bool inner = true;
+      for (int d = 0; d < 3; ++d) {
+        if (w[d] < 0 || w[d] >= g.nn[d]) inner = false;
+      }
+      if (!inner) continue;
+      g.out_flux[p.second.raw() * NCells() + GIdx(w)] = ffu[f];
+    }
+  }
+  if (sem()) {
+  }
+}
+
 void RunVof(M& m, Vars& var) {
   auto sem = m.GetSem(__func__);
   struct {
@@ -357,6 +391,20 @@ int Main(int argc, const char** argv) {
     int r = RunMpiBasicString<M>(mpi, RunProj, conf);
     return r;
   }
+  if (mode == "bcg") {
+    if (argc != 9) return 1;
+    const MIdx nsz = ParseSize(argv[2]);
+    for (int d = 0; d < 3; ++d) g.nn[d] = nsz[d];
+    const MIdx bs = ParseSize(argv[3]);
+    g.dt = std::atof(argv[4]);
+    g.u = ReadRaw(argv[5], NCells());
+    g.vflux = ReadRaw(argv[6], 3 * NCells());
+    g.alpha = ReadRaw(argv[7], NCells());  // the source
+    g.out = argv[8];
+    g.out_flux.assign(3 * NCells(), 0);
+    MpiWrapper mpi(&argc, &argv);
+    return RunMpiBasicString<M>(mpi, RunBcg, MeshConf(nsz, bs));
+  }
   if (mode == "vof") {
     if (argc != 10) return 1;
     const MIdx nsz = ParseSize(argv[2]);
@@ -477,6 +525,8 @@ int main(int argc, const char** argv) {
     std::ofstream fo(g.out + ".info");
     fo.precision(17);
     fo << g.residual << " " << g.iter << "\n";
+  } else if (mode == "bcg") {
+    WriteRaw(g.out + ".ffu", g.out_flux);
   } else if (mode == "vof") {
     WriteRaw(g.out + ".u", g.out_u);
     WriteRaw(g.out + ".n", g.out_n);

@@ -26,6 +26,9 @@ Fixtures:
                    some of which touch, and spheres across the periodic
                    boundary with a touching pair (inputs from the workload
                    generator, stored as parameters).
+  bcg.npz          UEmbed::InterpolateBcg face values on periodic 12x10x8
+                   and 8^3 meshes (random cell field, face fluxes and
+                   source).
   dumps.npz        dump::Xmf::WriteXmf texts of dump::Raw::WriteWithXmf
                    metadata for several meshes and element types, and
                    dump::Raw::WriteBlocks output of a 3x4x5 array converted
@@ -214,6 +217,27 @@ def overlap(tmp, rows=200):
             f.write(a + " | " + b + "\n")
 
 
+def bcg(tmp):
+    rng = np.random.default_rng(5)
+    out = {}
+    for q, n3 in enumerate(((12, 10, 8), (8, 8, 8))):
+        N = n3[0] * n3[1] * n3[2]
+        h = 1.0 / max(n3)
+        u = rng.normal(size=N)
+        vf = rng.normal(size=3 * N) * h * h
+        src = rng.normal(size=N)
+        dt = 0.01
+        u.tofile(os.path.join(tmp, "bu.bin"))
+        vf.tofile(os.path.join(tmp, "bv.bin"))
+        src.tofile(os.path.join(tmp, "bs.bin"))
+        ns = "%d,%d,%d" % n3
+        run(["bcg", ns, ns, repr(dt), "bu.bin", "bv.bin", "bs.bin", "bo"], tmp)
+        out.update({"n%d" % q: np.array(n3), "h%d" % q: h, "dt%d" % q: dt, "u%d" % q: u,
+                    "vflux%d" % q: vf, "src%d" % q: src,
+                    "ffu%d" % q: np.fromfile(os.path.join(tmp, "bo.ffu"))})
+    np.savez_compressed(os.path.join(OUT, "bcg.npz"), **out)
+
+
 COLOR_STEPS = (1, 3, 8)
 
 
@@ -290,6 +314,7 @@ def main():
         overlap(tmp)
         dumps(tmp)
         colors(tmp)
+        bcg(tmp)
     for f in sorted(os.listdir(OUT)):
         print(f, os.path.getsize(os.path.join(OUT, f)))
 

@@ -268,3 +268,15 @@ def test_oracle_colors_properties():
         ncomp = len({find(v) for v in np.unique(lab[lab > 0])})
         assert len(np.unique(cl[gas])) == ncomp
         assert np.array_equal(oracle.recolor(n, u, cl), cl)
+
+
+def test_oracle_bcg_predictor_equals_reference():
+    """UEmbed::InterpolateBcg (the BCG face predictor of Proj::StartStep) on
+    periodic 12x10x8 and 8^3 meshes: the oracle's face values are aphros's
+    bit for bit."""
+    fx = np.load(golden("bcg.npz"))
+    for q in range(2):
+        n3 = tuple(int(v) for v in fx["n%d" % q])
+        ffu = oracle.interpolate_bcg(n3, float(fx["h%d" % q]), fx["u%d" % q], fx["vflux%d" % q],
+                                     fx["src%d" % q], float(fx["dt%d" % q]))
+        assert np.array_equal(ffu, fx["ffu%d" % q]), q
