@@ -56,6 +56,7 @@ def lib():
         o.orc_height_good.restype = _D
         o.orc_height_good.argtypes = [_P, ctypes.c_int]
         o.orc_height_good_n.restype = _D
+        o.orc_fluid_step.restype = ctypes.c_int
         o.orc_height_good_n.argtypes = [_P, ctypes.c_int, _D]
         _o = o
     return _o
@@ -238,6 +239,36 @@ def recolor(n, u, cl_prev):
     out = np.empty(n3[0] * n3[1] * n3[2])
     lib().orc_recolor(n3c, _p(u), _p(cp), _p(out))
     return out
+
+
+class FluidState:
+    """Proj (src/solver/proj.ipp) state between steps, periodic, default
+    ProjPar, no forces: velocity (3 blocks), pressure, predictor pressure,
+    face fluxes of the time layer."""
+
+    def __init__(self, n, h, vel, rho, mu, tol=1e-8, maxiter=100000):
+        self.n3c, self.n3 = _n3(n)
+        N = self.n3[0] * self.n3[1] * self.n3[2]
+        self.N, self.h = N, h
+        self.vel = np.array(vel, dtype=np.float64)
+        self.rho = np.ascontiguousarray(rho, dtype=np.float64)
+        self.mu = np.ascontiguousarray(mu, dtype=np.float64)
+        self.p = np.zeros(N)
+        self.ppred = np.zeros(N)
+        self.flux = np.empty(3 * N)
+        self.tol, self.maxiter = tol, maxiter
+        self.t_steps = 0
+        fa, fp = _faces(self.flux, N)
+        self.flux, self._fp = fa, fp
+        lib().orc_fluid_init(self.n3c, _D(h), _p(self.vel), fp)
+
+    def step(self, dt, nthreads=1):
+        it = lib().orc_fluid_step(self.n3c, _D(self.h), _D(dt), _p(self.rho), _p(self.mu),
+                                  _p(self.vel), _p(self.p), _p(self.ppred), self._fp,
+                                  1 if self.t_steps == 0 else 0, _D(self.tol),
+                                  ctypes.c_int(self.maxiter), ctypes.c_int(nthreads))
+        self.t_steps += 1
+        return it
 
 
 def interpolate_bcg(n, h, u, vflux, src, dt):

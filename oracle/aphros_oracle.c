@@ -1109,3 +1109,232 @@ void orc_interpolate_bcg(const int n[3], double h, const double* u,
         }
   for (int d = 0; d < 3; ++d) free(g[d]);
 }
+
+/* ------------------------------------------------------------------------
+ * One time step of the projection fluid solver Proj (src/solver/proj.ipp)
+ * with the default ProjPar (BCG advection, implicit diffusion, one
+ * iteration per step, conjugate solver), periodic, no forces or sources:
+ * StartStep (proj.ipp:309-322), MakeIteration (:455-603), FinishStep
+ * (:604-613).  State, all in/out: vel (3 blocks of N, the velocity), p
+ * (pressure), ppred (pressure of the predictor projection, the next
+ * step's guess), flux (3 face blocks, the volume fluxes of the time
+ * layer); first: the first step (t = 0: initial pressure, proj.ipp:
+ * 111-127).  rho, mu: cell density and dynamic viscosity.  Every linear
+ * system is solved by orc_cg_solve (the conjugate solver) to tol.
+ * Returns the total CG iteration count.
+ * ------------------------------------------------------------------------ */
+
+/* face values (u[cp] + u[cm]) * 0.5 of a cell field (approx_eb.ipp:
+ * 828-836) dotted with the face surface (proj.ipp:64-67) */
+static void fl_face_flux(const int n[3], double area, const double* vel, double* const out[3]) {
+  const int nx = n[0], ny = n[1], nz = n[2];
+  const int64_t N = (int64_t)nx * ny * nz;
+  for (int d = 0; d < 3; ++d)
+    for (int k = 0; k < nz; ++k)
+      for (int j = 0; j < ny; ++j)
+        for (int i = 0; i < nx; ++i) {
+          const int64_t cp = XIDX(i, j, k);
+          const int64_t cm = XIDX(wrapi(i - (d == 0), nx), wrapi(j - (d == 1), ny),
+                                  wrapi(k - (d == 2), nz));
+          double sum = 0;
+          for (int e = 0; e < 3; ++e) {
+            const double v = (vel[e * N + cp] + vel[e * N + cm]) * 0.5;
+            sum += (v - 0.) * (e == d ? area : 0.);
+          }
+          out[d][cp] = sum;
+        }
+}
+
+/* Proj::Project (proj.ipp:384-407): assembly, CG from the guess in p,
+ * corrected fluxes in place */
+static int fl_project(const int n[3], double h, double* const rho_f[3], double* p,
+                      double* const ffv[3], double dt, double tol, int maxiter, int nthreads) {
+  const int64_t N = (int64_t)n[0] * n[1] * n[2];
+  double* e = (double*)malloc(sizeof(double) * 8 * N);
+  double* fk[3];
+  double* fv[3];
+  for (int d = 0; d < 3; ++d) {
+    fk[d] = (double*)malloc(sizeof(double) * N);
+    fv[d] = (double*)malloc(sizeof(double) * N);
+  }
+  orc_assemble_projection(n, h, dt, rho_f, ffv, NULL, e, fk, fv);
+  const orc_info info = orc_cg_solve(n, h * h * h, e, p, p, tol, 0, maxiter, 0, NULL, nthreads);
+  orc_flux_correct(n, fk, fv, p, (double**)ffv);
+  for (int d = 0; d < 3; ++d) {
+    free(fk[d]);
+    free(fv[d]);
+  }
+  free(e);
+  return info.iter;
+}
+
+void orc_fluid_init(const int n[3], double h, const double* vel, double* flux[3]) {
+  const double V = (h * h) * h;
+  fl_face_flux(n, V / h, vel, flux);
+}
+
+int orc_fluid_step(const int n[3], double h, double dt, const double* rho, const double* mu,
+                   double* vel, double* p, double* ppred, double* flux[3], int first,
+                   double tol, int maxiter, int nthreads) {
+  const int nx = n[0], ny = n[1], nz = n[2];
+  const int64_t N = (int64_t)nx * ny * nz;
+  const double V = (h * h) * h;
+  const double area = V / h;
+  int iters = 0;
+  double* rho_f[3];
+  double* mu_f[3];
+  double* ffv[3];
+  double* ffu[3];
+  for (int d = 0; d < 3; ++d) {
+    rho_f[d] = (double*)malloc(sizeof(double) * N);
+    mu_f[d] = (double*)malloc(sizeof(double) * N);
+    ffv[d] = (double*)malloc(sizeof(double) * N);
+    ffu[d] = (double*)malloc(sizeof(double) * N);
+  }
+  orc_face_density(n, rho, rho_f);
+  for (int d = 0; d < 3; ++d)
+    for (int k = 0; k < nz; ++k)
+      for (int j = 0; j < ny; ++j)
+        for (int i = 0; i < nx; ++i) {
+          const int64_t cp = XIDX(i, j, k);
+          const int64_t cm = XIDX(wrapi(i - (d == 0), nx), wrapi(j - (d == 1), ny),
+                                  wrapi(k - (d == 2), nz));
+          mu_f[d][cp] = (mu[cp] + mu[cm]) * 0.5;
+        }
+  double* vi = (double*)malloc(sizeof(double) * 3 * N);   /* iteration layer */
+  double* acc = (double*)malloc(sizeof(double) * 3 * N);  /* AoS */
+  double* accd = (double*)malloc(sizeof(double) * N);
+  double* guess = (double*)malloc(sizeof(double) * 3 * N);
+  memcpy(vi, vel, sizeof(double) * 3 * N);
+  for (int d = 0; d < 3; ++d) memcpy(ffv[d], flux[d], sizeof(double) * N);
+  if (first) {
+    /* CalcInitialPressure: face velocity of the iteration layer plus the
+       (zero) balanced force, projected with dt */
+    fl_face_flux(n, area, vi, ffv);
+    for (int d = 0; d < 3; ++d)
+      for (int64_t c = 0; c < N; ++c) ffv[d][c] += 0. / rho_f[d][c] * dt * area;
+    iters += fl_project(n, h, rho_f, p, ffv, dt, tol, maxiter, nthreads);
+  }
+  orc_acceleration(n, h, p, rho_f, NULL, acc);
+  /* predicted fluxes: BCG face velocities of the time layer with its fluxes */
+  {
+    /* orc_interpolate_bcg writes one face block per direction; the three
+       components of the face velocity come from three calls */
+    double* comp[3][3];
+    for (int e = 0; e < 3; ++e)
+      for (int d = 0; d < 3; ++d) comp[e][d] = (double*)malloc(sizeof(double) * N);
+    for (int e = 0; e < 3; ++e) {
+      for (int64_t c = 0; c < N; ++c) accd[c] = acc[3 * c + e];
+      orc_interpolate_bcg(n, h, vel + e * N, (const double* const*)flux, accd, dt, comp[e]);
+    }
+    for (int d = 0; d < 3; ++d)
+      for (int64_t c = 0; c < N; ++c) {
+        double sum = 0;
+        for (int e = 0; e < 3; ++e) sum += (comp[e][d][c] - 0.) * (e == d ? area : 0.);
+        ffv[d][c] = sum;
+      }
+    for (int e = 0; e < 3; ++e)
+      for (int d = 0; d < 3; ++d) free(comp[e][d]);
+  }
+  iters += fl_project(n, h, rho_f, ppred, ffv, dt * 0.5, tol, maxiter, nthreads);
+  /* advection (proj.ipp:128-190): BCG face values with the predicted
+     fluxes, flux sum, explicit update from the time layer */
+  memcpy(vi, vel, sizeof(double) * 3 * N);
+  for (int d = 0; d < 3; ++d) {
+    for (int64_t c = 0; c < N; ++c) accd[c] = acc[3 * c + d];
+    orc_interpolate_bcg(n, h, vi + d * N, (const double* const*)ffv, accd, dt, ffu);
+    for (int k = 0; k < nz; ++k)
+      for (int j = 0; j < ny; ++j)
+        for (int i = 0; i < nx; ++i) {
+          const int64_t c = XIDX(i, j, k);
+          double sum = 0;
+          for (int q = 0; q < 6; ++q) {
+            const int dd = q / 2;
+            const int64_t f = (q % 2 == 0)
+                                  ? c
+                                  : XIDX(wrapi(i + (dd == 0), nx), wrapi(j + (dd == 1), ny),
+                                         wrapi(k + (dd == 2), nz));
+            const double fl = -ffu[dd][f] * ffv[dd][f];
+            sum += fl * (double)(-1 + (q % 2) * 2);
+          }
+          vi[d * N + c] = vel[d * N + c] + sum * dt / V;
+        }
+  }
+  for (int d = 0; d < 3; ++d)
+    for (int64_t c = 0; c < N; ++c) vi[d * N + c] += acc[3 * c + d] * dt;
+  /* implicit diffusion (proj.ipp:241-307), guess = velocity after
+     advection, one iteration */
+  memcpy(guess, vi, sizeof(double) * 3 * N);
+  {
+    double* e = (double*)malloc(sizeof(double) * 8 * N);
+    double* x = (double*)malloc(sizeof(double) * N);
+    const double a = 1 / h;
+    for (int d = 0; d < 3; ++d) {
+      const double* g = guess + d * N;
+      for (int k = 0; k < nz; ++k)
+        for (int j = 0; j < ny; ++j)
+          for (int i = 0; i < nx; ++i) {
+            const int64_t c = XIDX(i, j, k);
+            double s[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+            for (int q = 0; q < 6; ++q) {
+              const int dd = q / 2;
+              const int64_t f = (q % 2 == 0)
+                                    ? c
+                                    : XIDX(wrapi(i + (dd == 0), nx), wrapi(j + (dd == 1), ny),
+                                           wrapi(k + (dd == 2), nz));
+              const int64_t fcm =
+                  (q % 2 == 0) ? XIDX(wrapi(i - (dd == 0), nx), wrapi(j - (dd == 1), ny),
+                                      wrapi(k - (dd == 2), nz))
+                               : c;
+              const int64_t fcp = f;
+              /* GradientImplicit(fcu, ...) (approx_eb.ipp:1471-1480) */
+              double fe[3] = {-a, a, 0};
+              const double grad = (g[fcp] - g[fcm]) / h;
+              const double ev = g[fcm] * fe[0] + g[fcp] * fe[1] + fe[2];
+              fe[2] += grad - ev;
+              const double o = (double)(-1 + (q % 2) * 2);
+              double v[3];
+              for (int t = 0; t < 3; ++t) v[t] = fe[t] * mu_f[dd][f] * area * o;
+              s[0] += v[1 - q % 2];
+              s[1 + q] += v[q % 2];
+              s[7] += v[2];
+            }
+            double* ec = e + 8 * c;
+            for (int t = 0; t < 8; ++t) ec[t] = -s[t];
+            double td[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+            td[0] = 1 / dt;
+            td[7] = -vi[d * N + c] / dt;
+            for (int t = 0; t < 8; ++t) ec[t] += td[t] * V * rho[c];
+          }
+      iters += orc_cg_solve(n, V, e, g, x, tol, 0, maxiter, 0, NULL, nthreads).iter;
+      memcpy(vi + d * N, x, sizeof(double) * N);
+    }
+    free(x);
+    free(e);
+  }
+  /* face acceleration: remove the old acceleration, face fluxes, project */
+  for (int d = 0; d < 3; ++d)
+    for (int64_t c = 0; c < N; ++c) vi[d * N + c] -= acc[3 * c + d] * dt;
+  fl_face_flux(n, area, vi, ffv);
+  for (int d = 0; d < 3; ++d)
+    for (int64_t c = 0; c < N; ++c) ffv[d][c] += 0. / rho_f[d][c] * dt * area;
+  iters += fl_project(n, h, rho_f, p, ffv, dt, tol, maxiter, nthreads);
+  /* cell acceleration */
+  orc_acceleration(n, h, p, rho_f, NULL, acc);
+  for (int d = 0; d < 3; ++d)
+    for (int64_t c = 0; c < N; ++c) vi[d * N + c] += acc[3 * c + d] * dt;
+  /* FinishStep: the iteration layer becomes the time layer */
+  memcpy(vel, vi, sizeof(double) * 3 * N);
+  for (int d = 0; d < 3; ++d) memcpy(flux[d], ffv[d], sizeof(double) * N);
+  free(guess);
+  free(accd);
+  free(acc);
+  free(vi);
+  for (int d = 0; d < 3; ++d) {
+    free(rho_f[d]);
+    free(mu_f[d]);
+    free(ffv[d]);
+    free(ffu[d]);
+  }
+  return iters;
+}

@@ -179,6 +179,16 @@ void orc_interpolate_bcg(const int n[3], double h, const double* u,
                          const double* const vflux[3], const double* src, double dt,
                          double* const out[3]);
 
+/* One time step of the projection fluid solver Proj (src/solver/proj.ipp)
+ * with the default ProjPar, periodic, no forces: state vel (3 blocks of N),
+ * p, ppred and flux (3 face blocks) in/out; first at t = 0.  Returns the
+ * total CG iterations.  orc_fluid_init: the initial fluxes of a velocity
+ * (proj.ipp:62-67). */
+void orc_fluid_init(const int n[3], double h, const double* vel, double* flux[3]);
+int orc_fluid_step(const int n[3], double h, double dt, const double* rho, const double* mu,
+                   double* vel, double* p, double* ppred, double* flux[3], int first,
+                   double tol, int maxiter, int nthreads);
+
 #ifdef __cplusplus
 }
 #endif

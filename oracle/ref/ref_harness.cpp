@@ -30,6 +30,13 @@
 //     UEmbed::InterpolateBcg (solver/approx_eb.ipp:753-821), periodic (no
 //     boundary conditions): the cell field u advected to the faces by dt/2
 //     with the face fluxes and the cell source src.  Writes out.ffu (3N).
+//   fluid n bs dt steps rho1 rho2 mu1 mu2 tol maxiter alpha.bin vel.bin out
+//     Proj (solver/proj.ipp, default ProjPar: BCG, implicit diffusion,
+//     conjugate solver "symm") for `steps` time steps of one iteration each
+//     (StartStep, MakeIteration, FinishStep) on a periodic mesh, density and
+//     dynamic viscosity the mixtures rho1 (1 - alpha) + rho2 alpha and
+//     mu1 (1 - alpha) + mu2 alpha, initial cell velocity vel (3 blocks of N),
+//     no forces.  Writes out.vel (3 blocks), out.p, out.flux (3N).
 //   xmf   n h name binpath type out.xmf
 //     dump::Xmf::WriteXmf of the metadata that dump::Raw::WriteWithXmf
 //     writes for a field of an n-cell mesh with cell size h (dump/raw.ipp:
@@ -54,6 +61,7 @@
 #include "overlap/overlap.h"
 #include "parse/vof.h"
 #include "solver/approx_eb.h"
+#include "solver/proj.h"
 #include "solver/curv.h"
 #include "solver/reconst.h"
 #include "solver/vof.h"
@@ -256,6 +264,90 @@ void RunBcg(M& m, Vars&) {
   }
 }
 
+struct FluidIn {
+  Scal mu1 = 0, mu2 = 0;
+  std::vector<double> vel;
+} gf;
+
+void RunFluid(M& m, Vars& var) {
+  auto sem = m.GetSem(__func__);
+  struct {
+    FieldCell<Scal> fcr, fcd, fcsv, fcsm;
+    FieldCell<Vect> fcf, fcvel;
+    FieldEmbed<Scal> ffbp;
+    MapEmbed<BCondFluid<Vect>> mebc;
+    MapCell<std::shared_ptr<CondCellFluid>> mcc;
+    std::unique_ptr<Proj<M>> fs;
+    int step = 0;
+  } * ctx(sem);
+  auto& t = *ctx;
+  if (sem("init")) {
+    t.fcr.Reinit(m);
+    t.fcd.Reinit(m);
+    t.fcvel.Reinit(m);
+    const size_t N = NCells();
+    for (auto c : m.AllCells()) {
+      const size_t i = GIdx(m.GetIndexCells().GetMIdx(c));
+      const Scal a = g.alpha[i];
+      t.fcr[c] = g.rho1 * (1 - a) + g.rho2 * a;
+      t.fcd[c] = gf.mu1 * (1 - a) + gf.mu2 * a;
+      t.fcvel[c] = Vect(gf.vel[i], gf.vel[N + i], gf.vel[2 * N + i]);
+    }
+    t.fcsv.Reinit(m, 0);
+    t.fcsm.Reinit(m, 0);
+    t.fcf.Reinit(m, Vect(0));
+    t.ffbp = FieldEmbed<Scal>(m, 0);
+    auto factory = linear::ModuleLinear<M>::GetInstance("conjugate");
+    fassert(factory, "conjugate solver not found");
+    std::shared_ptr<linear::Solver<M>> solver = factory->Make(var, "symm", m);
+    ProjArgs<M> args{t.fcvel, t.mebc, t.mcc, &t.fcr, &t.fcd, &t.fcf, &t.ffbp,
+                     &t.fcsv, &t.fcsm, 0., g.dt, solver, ProjPar<Vect>()};
+    t.fs.reset(new Proj<M>(m, m, args));
+  }
+  sem.LoopBegin();
+  if (sem("check")) {
+    if (t.step >= g.steps) {
+      sem.LoopBreak();
+    }
+  }
+  if (sem.Nested("start")) {
+    t.fs->StartStep();
+  }
+  if (sem.Nested("iter")) {
+    t.fs->MakeIteration();
+  }
+  if (sem.Nested("finish")) {
+    t.fs->FinishStep();
+  }
+  if (sem("inc")) {
+    ++t.step;
+  }
+  sem.LoopEnd();
+  if (sem("out")) {
+    const size_t N = NCells();
+    auto& vel = t.fs->GetVelocity();
+    auto& p = t.fs->GetPressure();
+    auto& ff = t.fs->GetVolumeFlux();
+    for (auto c : m.Cells()) {
+      const size_t i = GIdx(m.GetIndexCells().GetMIdx(c));
+      for (int d = 0; d < 3; ++d) g.out_u[d * N + i] = vel[c][d];
+      g.out_p[i] = p[c];
+    }
+    for (auto f : m.Faces()) {
+      const auto q = m.GetIndexFaces().GetMIdxDir(f);
+      const MIdx w = q.first;
+      bool inner = true;
+      for (int d = 0; d < 3; ++d) {
+        if (w[d] < 0 || w[d] >= g.nn[d]) inner = false;
+      }
+      if (!inner) continue;
+      g.out_flux[q.second.raw() * N + GIdx(w)] = ff[f];
+    }
+  }
+  if (sem()) {
+  }
+}
+
 void RunVof(M& m, Vars& var) {
   auto sem = m.GetSem(__func__);
   struct {
@@ -390,6 +482,33 @@ int Main(int argc, const char** argv) {
     MpiWrapper mpi(&argc, &argv);
     int r = RunMpiBasicString<M>(mpi, RunProj, conf);
     return r;
+  }
+  if (mode == "fluid") {
+    if (argc != 15) return 1;
+    const MIdx nsz = ParseSize(argv[2]);
+    for (int d = 0; d < 3; ++d) g.nn[d] = nsz[d];
+    const MIdx bs = ParseSize(argv[3]);
+    g.dt = std::atof(argv[4]);
+    g.steps = std::atoi(argv[5]);
+    g.rho1 = std::atof(argv[6]);
+    g.rho2 = std::atof(argv[7]);
+    gf.mu1 = std::atof(argv[8]);
+    gf.mu2 = std::atof(argv[9]);
+    const std::string tol = argv[10];
+    const std::string maxiter = argv[11];
+    g.alpha = ReadRaw(argv[12], NCells());
+    gf.vel = ReadRaw(argv[13], 3 * NCells());
+    g.out = argv[14];
+    g.out_u.assign(3 * NCells(), 0);
+    g.out_p.assign(NCells(), 0);
+    g.out_flux.assign(3 * NCells(), 0);
+    std::string conf = MeshConf(nsz, bs);
+    conf += "\nset double hypre_symm_tol " + tol;
+    conf += "\nset int hypre_symm_maxiter " + maxiter;
+    conf += "\nset int hypre_symm_miniter 0";
+    conf += "\nset int linsolver_symm_maxnorm 0";
+    MpiWrapper mpi(&argc, &argv);
+    return RunMpiBasicString<M>(mpi, RunFluid, conf);
   }
   if (mode == "bcg") {
     if (argc != 9) return 1;
@@ -527,6 +646,10 @@ int main(int argc, const char** argv) {
     fo << g.residual << " " << g.iter << "\n";
   } else if (mode == "bcg") {
     WriteRaw(g.out + ".ffu", g.out_flux);
+  } else if (mode == "fluid") {
+    WriteRaw(g.out + ".vel", g.out_u);
+    WriteRaw(g.out + ".p", g.out_p);
+    WriteRaw(g.out + ".flux", g.out_flux);
   } else if (mode == "vof") {
     WriteRaw(g.out + ".u", g.out_u);
     WriteRaw(g.out + ".n", g.out_n);

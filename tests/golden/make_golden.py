@@ -26,6 +26,11 @@ Fixtures:
                    some of which touch, and spheres across the periodic
                    boundary with a touching pair (inputs from the workload
                    generator, stored as parameters).
+  fluid.npz        the projection fluid solver Proj (default ProjPar: BCG,
+                   implicit diffusion) run by aphros for 1 and 4 steps on a
+                   12^3 sphere and a 16^3 four-bubble field (density ratio
+                   1000, Taylor-Green start): SHA-256 digests of the
+                   velocity, pressure and face fluxes, and a few values.
   bcg.npz          UEmbed::InterpolateBcg face values on periodic 12x10x8
                    and 8^3 meshes (random cell field, face fluxes and
                    source).
@@ -238,6 +243,47 @@ def bcg(tmp):
     np.savez_compressed(os.path.join(OUT, "bcg.npz"), **out)
 
 
+FLUID = dict(rho1=1.0, rho2=0.001, mu1=0.01, mu2=0.0001, dt=0.002, tol=1e-8)
+FLUID_STEPS = (1, 4)
+
+
+def taylor_green_cells(n):
+    """Cell velocity (3 blocks) of the Taylor-Green vortex, periodic unit cube."""
+    h = 1.0 / n
+    k, j, i = np.indices((n, n, n))
+    x, y, z = (i + 0.5) * h, (j + 0.5) * h, (k + 0.5) * h
+    vx = np.sin(2 * np.pi * x) * np.cos(2 * np.pi * y) * np.cos(2 * np.pi * z)
+    vy = -np.cos(2 * np.pi * x) * np.sin(2 * np.pi * y) * np.cos(2 * np.pi * z)
+    return np.concatenate([vx.ravel(), vy.ravel(), np.zeros(n ** 3)])
+
+
+def fluid_cases():
+    c, r = workload.place_spheres(9, 4, 0.1, 0.18, gap=0.03)
+    return [(12, np.array([[0.5, 0.5, 0.5]]), np.array([0.2])), (16, c, r)]
+
+
+def fluid(tmp):
+    import hashlib
+    out = {"steps": np.array(FLUID_STEPS)}
+    for q, (n, c, r) in enumerate(fluid_cases()):
+        case = workload.Case(n, c, r, seed=1)
+        case.alpha.tofile(os.path.join(tmp, "fa.bin"))
+        taylor_green_cells(n).tofile(os.path.join(tmp, "fv.bin"))
+        out["n%d" % q] = n
+        out["centres%d" % q] = np.asarray(c)
+        out["radii%d" % q] = np.asarray(r)
+        for s in FLUID_STEPS:
+            f = FLUID
+            run(["fluid", str(n), str(n), repr(f["dt"]), str(s), repr(f["rho1"]), repr(f["rho2"]),
+                 repr(f["mu1"]), repr(f["mu2"]), repr(f["tol"]), "100000", "fa.bin", "fv.bin",
+                 "fo"], tmp)
+            for name in ("vel", "p", "flux"):
+                a = np.fromfile(os.path.join(tmp, "fo." + name))
+                out["%s%d_%d" % (name, q, s)] = np.array(hashlib.sha256(a.tobytes()).hexdigest())
+                out["%s%d_%d_head" % (name, q, s)] = a[:8]
+    np.savez(os.path.join(OUT, "fluid.npz"), **out)
+
+
 COLOR_STEPS = (1, 3, 8)
 
 
@@ -315,6 +361,7 @@ def main():
         dumps(tmp)
         colors(tmp)
         bcg(tmp)
+        fluid(tmp)
     for f in sorted(os.listdir(OUT)):
         print(f, os.path.getsize(os.path.join(OUT, f)))
 

@@ -280,3 +280,32 @@ def test_oracle_bcg_predictor_equals_reference():
         ffu = oracle.interpolate_bcg(n3, float(fx["h%d" % q]), fx["u%d" % q], fx["vflux%d" % q],
                                      fx["src%d" % q], float(fx["dt%d" % q]))
         assert np.array_equal(ffu, fx["ffu%d" % q]), q
+
+
+def test_oracle_fluid_step_equals_reference():
+    """The oracle's projection fluid step (Proj with the default ProjPar:
+    initial pressure, BCG predictor and its projection, advection, implicit
+    diffusion, projection, acceleration) gives aphros's velocity, pressure
+    and face fluxes bit for bit after 1 and 4 steps (digests of aphros's
+    own run, tests/golden/fluid.npz)."""
+    import hashlib
+    import sys
+    sys.path.insert(0, os.path.dirname(golden("fluid.npz")))
+    from make_golden import FLUID, taylor_green_cells
+    fx = np.load(golden("fluid.npz"))
+    steps = [int(s) for s in fx["steps"]]
+    for q in range(2):
+        n = int(fx["n%d" % q])
+        case = workload.Case(n, fx["centres%d" % q], fx["radii%d" % q], seed=1)
+        a = case.alpha
+        rho = FLUID["rho1"] * (1 - a) + FLUID["rho2"] * a
+        mu = FLUID["mu1"] * (1 - a) + FLUID["mu2"] * a
+        st = oracle.FluidState(n, 1.0 / n, taylor_green_cells(n), rho, mu, tol=FLUID["tol"])
+        for s in range(1, max(steps) + 1):
+            st.step(FLUID["dt"])
+            if s not in steps:
+                continue
+            for name, v in (("vel", st.vel), ("p", st.p), ("flux", st.flux)):
+                key = "%s%d_%d" % (name, q, s)
+                assert np.array_equal(v[:8], fx[key + "_head"]), key
+                assert hashlib.sha256(v.tobytes()).hexdigest() == str(fx[key]), key
