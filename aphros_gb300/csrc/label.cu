@@ -37,12 +37,19 @@ constexpr unsigned long long kNoFirst = ~0ull;
 
 __device__ __forceinline__ int Wrap(int i, int n) { return i < 0 ? i + n : (i >= n ? i - n : i); }
 
-// Root of x (bounded walk; the tree depth is below the cell count).
-__device__ __forceinline__ int Find(const volatile int* par, int x, int64_t cap) {
+// Root of x (bounded walk; the tree depth is below the cell count), with
+// path halving: each visited cell is pointed at its grandparent (as in the
+// ECL-CC labelling of Jaiganesh and Burtscher).  A cell that is not a root
+// has a smaller parent, and only roots are ever hooked, so the grandparent
+// is an ancestor of the cell whatever the other threads do, and a plain
+// store cannot lose a hooking.
+__device__ __forceinline__ int Find(volatile int* par, int x, int64_t cap) {
   for (int64_t it = 0; it < cap; ++it) {
     const int p = par[x];
     if (p == x) return x;
-    x = p;
+    const int gp = par[p];
+    if (gp != p) par[x] = gp;
+    x = gp;
   }
   return x;
 }
