@@ -20,7 +20,9 @@ PKG = os.path.join(ROOT, "aphros_gb300")
 CSRC = os.path.join(PKG, "csrc")
 BUILD = os.path.join(PKG, "_build")
 ORACLE = os.path.join(ROOT, "oracle")
-REFERENCE_SRC = os.environ.get("APHROS_REFERENCE_SRC", "/root/reference/src")
+# the reference installed as sources by oracle/ref/stage_reference.sh
+REFERENCE_SRC = os.environ.get(
+    "APHROS_REFERENCE_SRC", os.path.join(ROOT, "baseline", "_ref", "aphros", "src"))
 
 NVCC = os.environ.get("NVCC", shutil.which("nvcc") or "/usr/local/cuda/bin/nvcc")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
@@ -106,7 +108,12 @@ def build_reference():
     if not os.path.isdir(REFERENCE_SRC):
         return None
     jobs = str(min(16, os.cpu_count() or 4))
-    _run(["make", "-C", os.path.join(ORACLE, "ref"), "REF=" + REFERENCE_SRC, "-j" + jobs])
+    try:
+        _run(["make", "-C", os.path.join(ORACLE, "ref"), "REF=" + REFERENCE_SRC, "-j" + jobs])
+    except RuntimeError as e:
+        # the checker is optional: the product library does not depend on it
+        print("reference harness not built: %s" % str(e)[-2000:], file=sys.stderr)
+        return None
     return os.path.join(ORACLE, "_ref", "ref_harness")
 
 

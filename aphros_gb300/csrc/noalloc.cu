@@ -1,13 +1,18 @@
 // aphgpu_cg_solve_noalloc: the plain FP64 CG solve without any device
 // allocation, for callers that cannot call cudaMalloc.
 //
-// Who needs it: code that runs where allocating device memory is not
-// allowed or not possible -- inside a region that is being recorded into a
-// CUDA graph by the caller, inside a host callback or a real-time step loop
-// that must not block on the allocator, or a plug-in living in a process
-// whose memory pool is owned by someone else.  Such a caller owns its input
-// and output arrays already; the solver's own work vectors live in a fixed
-// device array in this file instead of on the heap.
+// Who needs it: a solver plug-in loaded into a host application that owns
+// the GPU's memory (it reserves the device memory up front for its own pool
+// allocator, so a cudaMalloc from the plug-in fails or fragments that
+// pool), and step loops with a fixed time budget, where cudaMalloc and
+// cudaFree would synchronize the device and stall the loop for an unbounded
+// time.  Such a caller owns its input and output arrays already; the
+// solver's own work vectors live in a fixed device array in this file
+// instead of on the heap.
+//
+// The call blocks: every few iterations it synchronizes the given stream
+// and copies the solver's convergence flag to the host, and it returns once
+// the solve has finished.
 //
 // Scratch: one file-scope __device__ array `g_noalloc_scratch` of
 // kScratchDoubles doubles (about 1.6 MB).  Every GPU that loads the library
@@ -107,15 +112,14 @@ __global__ void KNaSetup(SolveScalars* s, unsigned int* ticket, double tol,
   *ticket = 0;
 }
 
-// stage init of linear.ipp:42-61: x = x0 (or 0), r = -(A x + e7), p = r
+// stage init of linear.ipp:42-61: r = -(A x0 + e7) (x0 = 0 when absent),
+// p = r; x itself is set afterwards by KNaCopyGuess
 __global__ void KNaInit(Dims d, const double* __restrict__ e8,
-                        const double* x0, double* x, double* r, double* p) {
+                        const double* x0, double* r, double* p) {
   NA_LOOP_BEGIN(d)
   const double* e = e8 + 8 * c;
   double u;
   if (x0) {
-    // x0 may alias x: every thread reads and writes only its own cell of x
-    // here, neighbours are read from x0 (unchanged in this kernel)
     u = x0[c] * e[0] + e[7];
     u += x0[d.idx(wrapm(i - 1, d.nx), j, k)] * e[1];
     u += x0[d.idx(wrapp(i + 1, d.nx), j, k)] * e[2];
@@ -131,6 +135,8 @@ __global__ void KNaInit(Dims d, const double* __restrict__ e8,
   NA_LOOP_END
 }
 
+// x = x0 (or 0), after KNaInit has read x0; x0 may alias x, the copy is
+// then a no-op (each thread reads and writes only its own cell)
 __global__ void KNaCopyGuess(int64_t n, const double* x0, double* x) {
   for (int64_t c = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; c < n;
        c += (int64_t)gridDim.x * blockDim.x)
@@ -247,7 +253,7 @@ extern "C" int aphgpu_cg_solve_noalloc(int nx, int ny, int nz, double cellvol,
   cudaStream_t st = (cudaStream_t)stream;
   const dim3 tg = TileGrid(d), tb = TileBlock();
   KNaSetup<<<1, 1, 0, st>>>(sc.s, sc.red.ticket, tol, cellvol, miniter, maxiter, maxnorm);
-  KNaInit<<<tg, tb, 0, st>>>(d, d_expr8, d_x0, d_x, sc.r, sc.p);
+  KNaInit<<<tg, tb, 0, st>>>(d, d_expr8, d_x0, sc.r, sc.p);
   KNaCopyGuess<<<FlatBlocks(n), kFlatThreads, 0, st>>>(n, d_x0, d_x);
   if (cudaGetLastError() != cudaSuccess) return APHGPU_ERR_CUDA;
   SolveScalars hs{};

@@ -95,8 +95,10 @@ namespace {
 
 int64_t Cells(const Sim& s) { return (int64_t)s.n[0] * s.n[1] * s.n[2]; }
 
-// Copies a simulation's state to the host and destroys its context.
-int Evict(aphgpu_server* S, Sim& s) {
+// Copies a simulation's state to the host and destroys its context.  Runs
+// without the lock on a victim that SelectVictims reserved (busy, bytes
+// already taken off the resident total); counters are updated by the caller.
+int Evict(Sim& s) {
   const int64_t N = Cells(s);
   s.alpha.resize(N);
   int rc = aphgpu_vof_get(s.ctx, s.alpha.data(), nullptr, nullptr, nullptr);
@@ -107,11 +109,10 @@ int Evict(aphgpu_server* S, Sim& s) {
   // the surface-tension force is not copied: it is a function of the
   // volume fraction and is recomputed on re-admission
   if (rc != APHGPU_OK) return rc;
-  S->resident_bytes -= s.bytes;
+  // the sweep order of the next step follows the steps the context took
+  s.steps = s.ctx->vof_count;
   aphgpu_destroy(s.ctx);
   s.ctx = nullptr;
-  s.evictions += 1;
-  S->evictions += 1;
   return APHGPU_OK;
 }
 
@@ -162,20 +163,57 @@ void FailOldest(aphgpu_server* S, int sim, int rc, const char* why) {
   }
 }
 
-// Makes room for `need` bytes by evicting idle simulations, least recently
-// used first.  Called with the lock held.  Returns false if impossible now.
-bool MakeRoom(aphgpu_server* S, int64_t need, int except) {
-  while (S->resident_bytes + need > S->budget) {
+// Picks idle resident simulations, least recently used first, whose
+// eviction makes room for `need` bytes, reserves them (busy) and takes their
+// bytes off the resident total.  Called with the lock held; the evictions
+// themselves run without it (EvictReserved).  Returns false, reserving
+// nothing, if not enough idle simulations exist now.
+bool SelectVictims(aphgpu_server* S, int64_t need, int except, std::vector<Sim*>* out) {
+  out->clear();
+  int64_t freed = 0;
+  while (S->resident_bytes - freed + need > S->budget) {
     Sim* victim = nullptr;
     for (auto& kv : S->sims) {
       Sim& s = *kv.second;
       if (s.id == except || !s.ctx || s.busy) continue;
+      if (std::find(out->begin(), out->end(), &s) != out->end()) continue;
       if (!victim || s.last_use < victim->last_use) victim = &s;
     }
-    if (!victim) return false;
-    if (Evict(S, *victim) != APHGPU_OK) return false;
+    if (!victim) {
+      out->clear();
+      return false;
+    }
+    out->push_back(victim);
+    freed += victim->bytes;
+  }
+  for (Sim* v : *out) {
+    v->busy = true;
+    S->resident_bytes -= v->bytes;
   }
   return true;
+}
+
+// Evicts the reserved victims; called without the lock, which it takes to
+// release them.  A victim whose copy failed stays resident.  Returns false
+// if any eviction failed.
+bool EvictReserved(aphgpu_server* S, const std::vector<Sim*>& victims,
+                   std::unique_lock<std::mutex>& lock) {
+  std::vector<int> rcs;
+  for (Sim* v : victims) rcs.push_back(Evict(*v));
+  lock.lock();
+  bool ok = true;
+  for (size_t i = 0; i < victims.size(); ++i) {
+    Sim* v = victims[i];
+    v->busy = false;
+    if (rcs[i] == APHGPU_OK) {
+      v->evictions += 1;
+      S->evictions += 1;
+    } else {
+      S->resident_bytes += v->bytes;
+      ok = false;
+    }
+  }
+  return ok;
 }
 
 // One step of a simulation (see the file comment).  Runs without the lock.
@@ -237,10 +275,24 @@ void Worker(aphgpu_server* S) {
           rescan = true;
           break;
         }
-        if (!MakeRoom(S, need, s.id)) continue;
-        s.busy = true;  // reserve while admitting without the lock
+        std::vector<Sim*> victims;
+        if (!SelectVictims(S, need, s.id, &victims)) continue;
+        s.busy = true;  // reserve while evicting and admitting without the lock
         S->resident_bytes += need;
         lock.unlock();
+        if (!victims.empty()) {
+          // EvictReserved returns with the lock held
+          if (!EvictReserved(S, victims, lock)) {
+            // a copy failed and its victim stayed resident: release the
+            // reservation and fail the request that needed the room
+            s.busy = false;
+            S->resident_bytes -= need;
+            FailOldest(S, s.id, APHGPU_ERR_CUDA, "eviction failed");
+            rescan = true;
+            break;
+          }
+          lock.unlock();
+        }
         const int rc = Admit(S, s);
         lock.lock();
         if (rc != APHGPU_OK) {
@@ -291,7 +343,7 @@ void Worker(aphgpu_server* S) {
     const int64_t measured = aphgpu_device_bytes(s.ctx);
     S->resident_bytes += measured - s.bytes;
     s.bytes = measured;
-    s.steps += 1;
+    if (res.status == APHGPU_OK) s.steps += 1;
     s.busy = false;
     res.queue_ms = std::chrono::duration<double, std::milli>(t_start - r.submitted).count();
     res.latency_ms = std::chrono::duration<double, std::milli>(t_end - r.submitted).count();

@@ -225,13 +225,13 @@ int aphgpu_last_timing(const aphgpu_ctx* ctx, double* ms, int64_t* launches);
 
 /* Plain FP64 CG solve (the algorithm of aphgpu_solve with
  * APHGPU_SOLVER_CG) that allocates no memory at all.  This entry point has
- * no counterpart in the reference; it exists for callers that cannot call
- * cudaMalloc: code recording a CUDA graph, host callbacks and real-time step
- * loops that must not block on the allocator, or plug-ins in a process whose
- * device memory pool is owned by someone else.  Such callers already own
- * their inputs and outputs; the solver's work vectors live in one fixed
- * device array inside the library (about 1.6 MB, held on every GPU that
- * loads the library until the process exits).
+ * no counterpart in the reference.  It is for callers that cannot call
+ * cudaMalloc: a solver plug-in inside a host application that reserves the
+ * GPU's memory for its own pool allocator, or a step loop with a fixed time
+ * budget, where cudaMalloc/cudaFree would synchronize the device.  Such
+ * callers already own their inputs and outputs; the solver's work vectors
+ * live in one fixed device array inside the library (about 1.6 MB, held on
+ * every GPU that loads the library until the process exits).
  *   d_expr8: device array, 8 doubles per cell (see aphgpu_set_system_expr);
  *   d_x0: device initial guess or NULL (zero), may equal d_x;
  *   d_x: device solution;  cellvol: h^3 of the residual norm;
@@ -242,7 +242,9 @@ int aphgpu_last_timing(const aphgpu_ctx* ctx, double* ms, int64_t* launches);
  * The first call on a device looks up the array's device address while that
  * device is current: make it before any stream capture.  All calls share
  * the array: calls whose work overlaps on the GPU race and must be
- * serialized by the caller.  Returns after the solve has finished. */
+ * serialized by the caller.  The call blocks: it synchronizes `stream`
+ * every few iterations to read the convergence flag and returns after the
+ * solve has finished. */
 int aphgpu_cg_solve_noalloc(int nx, int ny, int nz, double cellvol,
                             const double* d_expr8, const double* d_x0,
                             double* d_x, double tol, int miniter, int maxiter,

@@ -8,7 +8,9 @@ if ROOT not in sys.path:
     sys.path.insert(0, ROOT)
 
 GOLDEN = os.path.join(ROOT, "tests", "golden")
-REFERENCE = os.environ.get("APHROS_REFERENCE", "/root/reference")
+# aphros as staged by oracle/ref/stage_reference.sh
+REFERENCE = os.environ.get(
+    "APHROS_REFERENCE", os.path.join(ROOT, "baseline", "_ref", "aphros"))
 
 
 def pytest_configure(config):

@@ -15,6 +15,11 @@ Fixtures:
                    1000, Taylor-Green + noise): inputs, aphros's assembled
                    system, CG solution at ||r||/||b|| = 1e-10, corrected
                    fluxes, iteration count.
+  proj64.npz       C1 projection system on 64^3 (sphere r=0.2, density
+                   ratio 1000, Taylor-Green + noise, from the workload
+                   generator; SHA-256 of the inputs stored): aphros's CG
+                   solution at ||r||/||b|| = 1e-13 (blocks of 16^3, all
+                   host threads), its residual and iteration count.
   vof32.npz        3 VOF steps + Heights curvature on 32^3 (sphere r=0.2,
                    Taylor-Green flux at CFL 0.5): aphros's results.
   reconst.txt      random planes: GetLineA, GetLineU, GetLineFlux.
@@ -64,8 +69,8 @@ def read_plain(path):
     return dims, data
 
 
-def run(args, cwd):
-    env = dict(os.environ, OMP_NUM_THREADS="1")
+def run(args, cwd, threads=1):
+    env = dict(os.environ, OMP_NUM_THREADS=str(threads))
     subprocess.run([HARNESS] + args, cwd=cwd, check=True, env=env)
 
 
@@ -120,6 +125,29 @@ def proj16(tmp):
                         flux_ref=flux_ref, residual=float(info[0]),
                         iters=int(info[1]), iters_blocks8=int(info8[1]),
                         p_blocks8=p8)
+
+
+def proj64(tmp):
+    import hashlib
+
+    import oracle
+    case = workload.config("c1", n=64)
+    n, h = case.n, case.h
+    case.alpha.tofile(os.path.join(tmp, "alpha.bin"))
+    case.flux.tofile(os.path.join(tmp, "vf.bin"))
+    e, _, _ = oracle.assemble_projection(n, h, case.dt, case.alpha, case.rho1,
+                                         case.rho2, case.flux)
+    tol = oracle.rel_tol(e, h, 1e-13)
+    run(["proj", str(n), "16", repr(h), repr(case.dt), repr(case.rho1),
+         repr(case.rho2), repr(tol), "1000000", "alpha.bin", "vf.bin", "p64"], tmp,
+        threads=os.cpu_count() or 1)
+    info = open(os.path.join(tmp, "p64.info")).read().split()
+    sha = lambda a: hashlib.sha256(np.ascontiguousarray(a).tobytes()).hexdigest()
+    np.savez_compressed(os.path.join(OUT, "proj64.npz"), n=n, h=h, dt=case.dt,
+                        rho1=case.rho1, rho2=case.rho2, tol=tol, rtol=1e-13,
+                        alpha_sha256=sha(case.alpha), flux_sha256=sha(case.flux),
+                        p_ref=np.fromfile(os.path.join(tmp, "p64.p")),
+                        residual=float(info[0]), iters=int(info[1]))
 
 
 def vof32(tmp):
@@ -347,21 +375,20 @@ def dumps(tmp):
 
 def main():
     ap = argparse.ArgumentParser()
-    ap.add_argument("--ref", default="/root/reference")
+    ap.add_argument("--ref", default=os.path.join(ROOT, "baseline", "_ref", "aphros"))
+    ap.add_argument("--only", default="", help="comma-separated fixture names")
     args = ap.parse_args()
     if not os.path.exists(HARNESS):
         sys.exit("build the reference harness first: python -m aphros_gb300.build")
+    makers = [("advection3d", lambda t: advection3d(args.ref, t)), ("proj16", proj16),
+              ("proj64", proj64), ("vof32", vof32), ("reconst", reconst),
+              ("height", lambda t: height(args.ref, t)), ("overlap", overlap),
+              ("dumps", dumps), ("colors", colors), ("bcg", bcg), ("fluid", fluid)]
+    only = set(filter(None, args.only.split(",")))
     with tempfile.TemporaryDirectory() as tmp:
-        advection3d(args.ref, tmp)
-        proj16(tmp)
-        vof32(tmp)
-        reconst(tmp)
-        height(args.ref, tmp)
-        overlap(tmp)
-        dumps(tmp)
-        colors(tmp)
-        bcg(tmp)
-        fluid(tmp)
+        for name, make in makers:
+            if not only or name in only:
+                make(tmp)
     for f in sorted(os.listdir(OUT)):
         print(f, os.path.getsize(os.path.join(OUT, f)))
 

@@ -1,0 +1,121 @@
+"""The pressure bar of the solvers at the production tolerance: solved to
+||r||/||b|| = 1e-10 from a zero guess, every solver's pressure is within
+1e-9 (relative L2, mean removed) of a tight FP64 reference solved to
+||r||/||b|| = 1e-13:
+
+  * aphros's own CG (SolverConjugate, linear.ipp:24-129) on the C1
+    projection system at 64^3 (fixture proj64.npz, made by aphros's code);
+  * the oracle's CG (the same algorithm, restated in C) on the C1 system at
+    64^3 and on the 64-bubble field at 128^3, computed here on the host.
+
+The comparison against a tight reference measures each solver's own error:
+two solves that both stop at 1e-10 can differ by more than either one's
+error.  Calls go through the C ABI.
+"""
+import hashlib
+import math
+import os
+
+import numpy as np
+import pytest
+
+import oracle
+from aphros_gb300 import _lib, workload
+from conftest import golden
+
+pytestmark = pytest.mark.gpu
+
+BAR = 1e-9
+RTOL = 1e-10
+THREADS = os.cpu_count() or 1
+
+# the benchmark's V-cycle (one finest sweep, doubling below) beside the
+# library defaults
+SETTINGS = {
+    "defaults": ({}, 0, 0),
+    "bench_vcycle": ({"mg_pre": 1, "mg_post": 1}, 1, 3),
+}
+
+
+def rel_l2(a, b):
+    a = a - a.mean()
+    b = b - b.mean()
+    return float(np.linalg.norm(a - b) / np.linalg.norm(b))
+
+
+def _sha(a):
+    return hashlib.sha256(np.ascontiguousarray(a).tobytes()).hexdigest()
+
+
+def _context(case):
+    ctx = _lib.Context(case.n, case.h)
+    ctx.assemble_projection(case.alpha, case.rho1, case.rho2, case.flux, case.dt)
+    return ctx
+
+
+def _solve_all(ctx, case, p_tight, solvers):
+    _, bn = ctx.residual_norms()
+    tol = RTOL * bn / math.sqrt(case.h ** 3)
+    errs = {}
+    for sname, (mg, cycle, growth) in SETTINGS.items():
+        ctx.set_option(_lib.OPT_CYCLE, cycle)
+        ctx.set_option(_lib.OPT_SWEEP_GROWTH, growth)
+        for solver in solvers:
+            if solver == _lib.SOLVER_CG and sname != "defaults":
+                continue
+            x, info = ctx.solve(_lib.default_conf(solver=solver, tol=tol, maxiter=200000, **mg))
+            rn, bn2 = ctx.residual_norms()
+            assert info.converged and rn / bn2 <= 1.01 * RTOL, (sname, solver)
+            errs[(sname, solver)] = rel_l2(x, p_tight)
+    return errs
+
+
+@pytest.fixture(scope="module")
+def c1_64():
+    case = workload.config("c1", n=64)
+    fx = np.load(golden("proj64.npz"))
+    # the fixture was made from these very inputs
+    assert _sha(case.alpha) == str(fx["alpha_sha256"])
+    assert _sha(case.flux) == str(fx["flux_sha256"])
+    return case, fx
+
+
+def test_oracle_tight_solution_equals_aphros_c1_64(c1_64):
+    """The oracle's CG at 1e-13 is aphros's CG at 1e-13 (pins the tight
+    reference used below)."""
+    case, fx = c1_64
+    e, _, _ = oracle.assemble_projection(case.n, case.h, case.dt, case.alpha, case.rho1,
+                                         case.rho2, case.flux)
+    xo, info = oracle.cg_solve(case.n, case.h, e, oracle.rel_tol(e, case.h, 1e-13),
+                               nthreads=THREADS)
+    assert info.converged
+    assert rel_l2(xo, fx["p_ref"]) <= 1e-11
+
+
+def test_c1_64_within_bar_of_aphros_cg(c1_64):
+    """C1 (64^3, sphere r = 0.2, ratio 1000): every solver at 1e-10 is
+    within 1e-9 of aphros's CG solution at 1e-13."""
+    case, fx = c1_64
+    ctx = _context(case)
+    errs = _solve_all(ctx, case, fx["p_ref"],
+                      (_lib.SOLVER_CG, _lib.SOLVER_MGPCG, _lib.SOLVER_MIXED))
+    ctx.close()
+    bad = {k: v for k, v in errs.items() if not v <= BAR}
+    assert not bad, bad
+
+
+def test_c3_field_128_within_bar_of_oracle_cg():
+    """The 64-bubble field (radii 0.02-0.05, ratio 1000) at 128^3: the
+    multigrid solvers at 1e-10 are within 1e-9 of the oracle's CG at
+    1e-13."""
+    case = workload.config("c3", n=128)
+    e, _, _ = oracle.assemble_projection(case.n, case.h, case.dt, case.alpha, case.rho1,
+                                         case.rho2, case.flux)
+    xo, info = oracle.cg_solve(case.n, case.h, e, oracle.rel_tol(e, case.h, 1e-13),
+                               nthreads=THREADS)
+    assert info.converged
+    ctx = _context(case)
+    errs = _solve_all(ctx, case, xo, (_lib.SOLVER_MGPCG, _lib.SOLVER_MIXED))
+    ctx.close()
+    bad = {k: v for k, v in errs.items() if not v <= BAR}
+    assert not bad, bad

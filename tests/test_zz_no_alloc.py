@@ -1,6 +1,7 @@
 """GPU test of aphgpu_cg_solve_noalloc, the CG entry point that allocates
-nothing (for callers that cannot call cudaMalloc: graph-recording code, host
-callbacks, real-time step loops, plug-ins that do not own the memory pool).
+nothing (for callers that cannot call cudaMalloc: a plug-in inside an
+application that reserves the GPU's memory for its own pool, a step loop
+with a fixed time budget where cudaMalloc would synchronize the device).
 
 It is called through the C ABI on device arrays owned by the caller (torch
 tensors here) and must give the same solution as the regular entry point
