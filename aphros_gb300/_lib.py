@@ -105,6 +105,10 @@ def lib():
     L.aphgpu_vof_init.argtypes = [_P, _P, _D]
     L.aphgpu_vof_step.argtypes = [_P, _P, _D]
     L.aphgpu_vof_get.argtypes = [_P, _P, _P, _P, _P]
+    L.aphgpu_vof_set_source.argtypes = [_P, _P]
+    L.aphgpu_vof_set_source.restype = _I
+    L.aphgpu_apply_cell_cond.argtypes = [_P, ctypes.c_int64, _P, _P]
+    L.aphgpu_apply_cell_cond.restype = _I
     L.aphgpu_curvature.argtypes = [_P, _P, _P]
     L.aphgpu_surface_tension.argtypes = [_P, _D, _P]
     L.aphgpu_set_force_resident.argtypes = [_P, _I]
@@ -296,6 +300,19 @@ class Context:
     def vof_step(self, vflux, dt):
         v = None if vflux is None else self._f64(vflux, 3 * self.N)
         self._check(self._L.aphgpu_vof_step(self._p, ptr(v), dt))
+
+    def vof_set_source(self, src):
+        """Volume source of the following VOF steps (None: none)."""
+        v = None if src is None else self._f64(src, self.N)
+        self._check(self._L.aphgpu_vof_set_source(self._p, ptr(v)))
+
+    def apply_cell_cond(self, cells, values):
+        """Given-pressure cells of Proj::ApplyCellCond on the current system."""
+        c = np.ascontiguousarray(cells, dtype=np.int64)
+        v = np.ascontiguousarray(values, dtype=np.float64)
+        if c.shape != v.shape:
+            raise ValueError("cells and values differ in length")
+        self._check(self._L.aphgpu_apply_cell_cond(self._p, len(c), ptr(c), ptr(v)))
 
     def vof_get(self):
         u = np.empty(self.N)

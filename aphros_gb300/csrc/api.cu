@@ -281,6 +281,45 @@ int aphgpu_set_system_expr(aphgpu_ctx* ctx, const double* expr8) {
   return SetSystemExprDevice(ctx, ctx->e8);
 }
 
+int aphgpu_apply_cell_cond(aphgpu_ctx* ctx, int64_t count, const int64_t* cells,
+                           const double* values) {
+  if (!Valid(ctx) || count < 0 || (count > 0 && (!cells || !values))) return APHGPU_ERR_ARG;
+  if (!ctx->has_system) return SetError(ctx, APHGPU_ERR_STATE, "no system set");
+  std::vector<int64_t> sorted(cells, cells + count);
+  std::sort(sorted.begin(), sorted.end());
+  for (int64_t t = 0; t < count; ++t) {
+    if (sorted[t] < 0 || sorted[t] >= ctx->N)
+      return SetError(ctx, APHGPU_ERR_ARG, "cell %lld outside the domain",
+                      (long long)sorted[t]);
+    if (t > 0 && sorted[t] == sorted[t - 1])
+      return SetError(ctx, APHGPU_ERR_ARG, "cell %lld given twice", (long long)sorted[t]);
+  }
+  APH_TRY(SetDevice(ctx));
+  if (count > ctx->cc_cap) {
+    if (ctx->cc_buf) {
+      for (size_t i = 0; i < ctx->allocs.size(); ++i) {
+        if (ctx->allocs[i] == ctx->cc_buf) {
+          APH_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+          cudaFree(ctx->cc_buf);
+          ctx->allocs.erase(ctx->allocs.begin() + i);
+          ctx->bytes -= (int64_t)sizeof(double) * 2 * ctx->cc_cap;
+          break;
+        }
+      }
+      ctx->cc_buf = nullptr;
+      ctx->cc_cap = 0;
+    }
+    APH_TRY(Alloc(ctx, &ctx->cc_buf, 2 * count));
+    ctx->cc_cap = count;
+  }
+  if (count > 0) {
+    APH_TRY(H2D(ctx, ctx->cc_buf, values, sizeof(double) * count));
+    APH_TRY(H2D(ctx, ctx->cc_buf + ctx->cc_cap, cells, sizeof(int64_t) * count));
+  }
+  return ApplyCellCondDevice(ctx, count, (const int64_t*)(ctx->cc_buf + ctx->cc_cap),
+                             ctx->cc_buf);
+}
+
 int aphgpu_get_system_expr(aphgpu_ctx* ctx, double* expr8) {
   if (!Valid(ctx) || !expr8) return APHGPU_ERR_ARG;
   if (!ctx->has_system) return SetError(ctx, APHGPU_ERR_STATE, "no system set");
@@ -491,6 +530,20 @@ int aphgpu_vof_step(aphgpu_ctx* ctx, const double* vflux, double dt) {
   Timer t(ctx);
   APH_TRY(VofStepDevice(ctx, d_vf, dt));
   t.Stop();
+  return APHGPU_OK;
+}
+
+int aphgpu_vof_set_source(aphgpu_ctx* ctx, const double* src) {
+  if (!Valid(ctx)) return APHGPU_ERR_ARG;
+  if (!ctx->vof_ready) return SetError(ctx, APHGPU_ERR_STATE, "vof not initialised");
+  APH_TRY(SetDevice(ctx));
+  if (!src) {
+    ctx->has_vof_src = false;
+    return APHGPU_OK;
+  }
+  if (!ctx->vof_src) APH_TRY(Alloc(ctx, &ctx->vof_src, ctx->N));
+  APH_TRY(H2D(ctx, ctx->vof_src, src, sizeof(double) * ctx->N));
+  ctx->has_vof_src = true;
   return APHGPU_OK;
 }
 

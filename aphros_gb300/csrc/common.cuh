@@ -304,6 +304,12 @@ struct aphgpu_ctx {
   bool has_vflux_res = false;
   double* kappa = nullptr;
   double* hgt = nullptr;       // 3N AoS
+  // given-pressure cells of the last aphgpu_apply_cell_cond: values, then
+  // cell indices (int64), room for cc_cap cells
+  double* cc_buf = nullptr;
+  int64_t cc_cap = 0;
+  double* vof_src = nullptr;   // N, volume source of the VOF step
+  bool has_vof_src = false;
   double clipth = 1e-10;
   int vof_count = 0;
   double vof_dt = 0;  // time step of the last VOF step (kernel timing)
@@ -405,6 +411,8 @@ int CoarseOneSetup(aphgpu_ctx* ctx);
 int CoarseOneLaunch(aphgpu_ctx* ctx, const int* pre, const int* post, int gamma, bool first,
                     const SolveScalars* s);
 int SetSystemExprDevice(aphgpu_ctx* ctx, const double* d_expr8);
+int ApplyCellCondDevice(aphgpu_ctx* ctx, int64_t count, const int64_t* d_cells,
+                        const double* d_values);
 int AssembleProjectionDevice(aphgpu_ctx* ctx, const double* d_alpha,
                              double rho1, double rho2, const double* d_vflux,
                              const double* d_febp, double dt, int remove_mean);

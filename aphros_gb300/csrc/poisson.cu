@@ -1781,6 +1781,36 @@ int SetSystemExprDevice(aphgpu_ctx* ctx, const double* d_expr8) {
   return APHGPU_OK;
 }
 
+// Proj::ApplyCellCond (proj.ipp:326-338) for given-pressure cells:
+// e[0] += 1 and e[7] -= pc, i.e. diag += 1 and b += pc (b = -e[7]); each
+// listed cell at most once.
+__global__ void KCellCond(int64_t count, const int64_t* __restrict__ cells,
+                          const double* __restrict__ values, double* diag, double* b) {
+  for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < count;
+       t += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t c = cells[t];
+    diag[c] += 1.;
+    b[c] += values[t];
+  }
+}
+
+int ApplyCellCondDevice(aphgpu_ctx* ctx, int64_t count, const int64_t* d_cells,
+                        const double* d_values) {
+  if (count > 0) {
+    KCellCond<<<FlatBlocks(count), kFlatThreads, 0, ctx->stream>>>(count, d_cells, d_values,
+                                                                   ctx->diag, ctx->b);
+    APH_LAUNCHED(ctx);
+  }
+  // the diagonal is no longer minus the sum of the couplings: the system is
+  // not singular any more, and the FP32 and coarse levels take the stored
+  // diagonal
+  ctx->diag_explicit = true;
+  ctx->mg.built64 = ctx->mg.built32 = false;
+  KInvDiag<double><<<TileGrid(ctx->d), TileBlock(), 0, ctx->stream>>>(FineOp(ctx), ctx->invdiag);
+  APH_LAUNCHED(ctx);
+  return APHGPU_OK;
+}
+
 int AssembleProjectionDevice(aphgpu_ctx* ctx, const double* d_alpha,
                              double rho1, double rho2, const double* d_vflux,
                              const double* d_febp, double dt, int remove_mean) {

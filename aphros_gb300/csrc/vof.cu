@@ -310,6 +310,40 @@ __global__ void KListInterface(Dims d, const double* __restrict__ u, uint8_t* fc
   }
 }
 
+// Init stage of Vof::MakeIteration with a volume source (vof.ipp:504-514):
+// u = u + dt * src * (1 - u) in every cell and fcuu of that field, and the
+// list of the interfacial cells of that field.  A listed cell that was not
+// interfacial before has no plane from the previous reconstruction: its
+// normal is zeroed, so its faces carry v*u (InterfaceFlux), as the
+// reference's NaN normal does (vof.ipp:233-255); cells interfacial before
+// keep their previous planes, as in the reference's first sweep.
+__global__ void KSourceList(Dims d, double dt, const double* __restrict__ src, double* u,
+                            uint8_t* fcuu, double* nrm, int* list, int* count) {
+  const int i = blockIdx.x * kTileX + threadIdx.x;
+  const int j = blockIdx.y * kTileY + threadIdx.y;
+  const int kb = blockIdx.z * kTileZ;
+  const int ke = min(kb + kTileZ, d.nz);
+  const bool in = i < d.nx && j < d.ny;
+  for (int k = kb; k < ke; ++k) {
+    const int64_t c = in ? d.idx(i, j, k) : 0;
+    bool want = false;
+    if (in) {
+      const double um = u[c];
+      const double un = um + dt * src[c] * (1. - um);
+      u[c] = un;
+      const long long ub = Bits(un);
+      fcuu[c] = (!NanBits(ub) && ub < kHalfBits) ? 0 : 1;
+      want = InterfaceBits(ub);
+      if (want && !InterfaceBits(Bits(um))) {
+        nrm[3 * c] = 0.;
+        nrm[3 * c + 1] = 0.;
+        nrm[3 * c + 2] = 0.;
+      }
+    }
+    ListAppend(want, (int)c, list, count);
+  }
+}
+
 // Vof::ReconstPlanes (vof.ipp:70-90) on the listed interfacial cells;
 // values of other cells are left untouched (they are never read).
 __global__ void KReconstructList(Dims d, double hx, double hy, double hz,
@@ -726,7 +760,14 @@ int VofReconstruct(aphgpu_ctx* ctx) {
 int VofStepDevice(aphgpu_ctx* ctx, const double* d_vflux, double dt) {
   const int64_t N = ctx->N;
   const VofScratch sc = Scratch(ctx);
-  APH_TRY(ListInterface(ctx, sc, true));
+  if (ctx->has_vof_src) {
+    APH_CUDA(ctx, cudaMemsetAsync(sc.count, 0, sizeof(int), ctx->stream));
+    KSourceList<<<TileGrid(ctx->d), TileBlock(), 0, ctx->stream>>>(
+        ctx->d, dt, ctx->vof_src, ctx->u, sc.fcuu, ctx->nrm, sc.list, sc.count);
+    APH_LAUNCHED(ctx);
+  } else {
+    APH_TRY(ListInterface(ctx, sc, true));
+  }
   int dd[3];
   const int cnt = ctx->vof_count % 3;  // vof.ipp:428-435
   if (cnt == 0) { dd[0] = 0; dd[1] = 1; dd[2] = 2; }

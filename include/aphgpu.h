@@ -114,6 +114,15 @@ int aphgpu_sync(aphgpu_ctx* ctx);
  * symmetric (e[2] of c equals e[1] of c+x, etc.), as CG requires. */
 int aphgpu_set_system_expr(aphgpu_ctx* ctx, const double* expr8);
 
+/* Given-pressure cells: Proj::ApplyCellCond (src/solver/proj.ipp:326-338)
+ * on the current system (after aphgpu_assemble_projection or
+ * aphgpu_set_system_expr), e[0] += 1 and e[7] -= values[t] in cell
+ * cells[t] (x-fastest index), as aphros does for each CondCellVal of its
+ * cell-condition map.  Each cell at most once (else APHGPU_ERR_ARG).  The
+ * system then has an explicit diagonal and is no longer singular. */
+int aphgpu_apply_cell_cond(aphgpu_ctx* ctx, int64_t count, const int64_t* cells,
+                           const double* values);
+
 /* Copies the current system back as per-cell expressions (8 doubles per
  * cell, the layout of aphgpu_set_system_expr), e.g. to inspect the system
  * assembled by aphgpu_assemble_projection. */
@@ -190,8 +199,18 @@ int aphgpu_vof_init(aphgpu_ctx* ctx, const double* alpha, double clipth);
  * vof.ipp:212-327) in the order selected by the step count, each followed
  * by interface reconstruction; then FinishStep.  vflux: mixture face fluxes
  * (host, 3 face blocks) or NULL to use the resident corrected fluxes of
- * aphgpu_flux_correct().  Colour labelling is not part of this path. */
+ * aphgpu_flux_correct().  Colour labelling is not part of this path; the
+ * volume source, if any, is the one of aphgpu_vof_set_source. */
 int aphgpu_vof_step(aphgpu_ctx* ctx, const double* vflux, double dt);
+
+/* Sets the volume source of the following aphgpu_vof_step calls (host, one
+ * value per cell; NULL: none, the default): the init stage of
+ * Vof::MakeIteration (src/solver/vof.ipp:504-514) first sets
+ * u = u + dt * src * (1 - u) in every cell; the sweeps then start from that
+ * field, cells that became interfacial through the source carrying the
+ * plain flux v*u in the first sweep (they have no plane yet).  The
+ * reference reads the source from its owner (Vof's fcs argument). */
+int aphgpu_vof_set_source(aphgpu_ctx* ctx, const double* src);
 
 /* Copies the VOF state to the host; any pointer may be NULL.
  * normals: AoS 3 per cell, NaN outside the interface; plane: plane

@@ -106,6 +106,16 @@ def assemble_projection(n, h, dt, alpha, rho1, rho2, vflux, febp=None,
     return e, fka, fva
 
 
+def apply_cell_cond(expr8, cells, values):
+    """Proj::ApplyCellCond (solver/proj.ipp:326-338): for each given-pressure
+    cell c with value pc, e[0] += 1 and e[7] -= pc.  Returns a new array."""
+    e = np.array(expr8, dtype=np.float64).reshape(-1, 8)
+    for c, pc in zip(np.asarray(cells, dtype=np.int64), np.asarray(values, dtype=np.float64)):
+        e[c, 0] += 1
+        e[c, 7] -= pc
+    return e.ravel()
+
+
 def rel_tol(expr8, h, rtol=1e-10):
     """Absolute tolerance of the reference's CG norm sqrt(sum r^2/h^3) that
     corresponds to ||r||/||b|| = rtol with a zero guess (b = -e7)."""
@@ -205,14 +215,16 @@ class VofState:
         # field: 0 where u > 0, none (-1) elsewhere (vof.ipp:53-57)
         self.cl = np.where(self.u > 0, 0.0, -1.0)
 
-    def step(self, vflux, dt, nthreads=1):
+    def step(self, vflux, dt, nthreads=1, src=None):
+        """One MakeIteration; src: volume source per cell (None: zero)."""
         o = lib()
         if nthreads:
             os.environ.setdefault("OMP_NUM_THREADS", str(nthreads))
         vf, vfp = _faces(vflux, self.N)
-        o.orc_vof_step(self.n3c, self.hh, _p(self.u), vfp, _D(dt), _D(self.clipth),
-                       self.count, 1 if self.count == 0 else 0,
-                       self.mask.ctypes.data_as(_P), _p(self.nrm), _p(self.a))
+        sa = None if src is None else np.ascontiguousarray(src, dtype=np.float64)
+        o.orc_vof_step_src(self.n3c, self.hh, _p(self.u), vfp, _p(sa), _D(dt),
+                           _D(self.clipth), self.count, 1 if self.count == 0 else 0,
+                           self.mask.ctypes.data_as(_P), _p(self.nrm), _p(self.a))
         self.count += 1
 
     def recolor(self):

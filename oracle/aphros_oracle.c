@@ -683,8 +683,23 @@ void orc_vof_step(
     const int n[3], const double h[3], double* u, double* const ffv[3],
     double dt, double clipth, int count, int reconstruct_first, uint8_t* mask,
     double* nrm, double* a) {
+  orc_vof_step_src(n, h, u, ffv, NULL, dt, clipth, count, reconstruct_first,
+                   mask, nrm, a);
+}
+
+void orc_vof_step_src(
+    const int n[3], const double h[3], double* u, double* const ffv[3],
+    const double* src, double dt, double clipth, int count,
+    int reconstruct_first, uint8_t* mask, double* nrm, double* a) {
   const int64_t nc = (int64_t)n[0] * n[1] * n[2];
   if (reconstruct_first) orc_vof_reconstruct(n, h, u, mask, nrm, a);
+  if (src) {
+    /* vof.ipp:510-513: uc = um + dt * fcs * (1 - um) */
+    for (int64_t c = 0; c < nc; ++c) {
+      const double um = u[c];
+      u[c] = um + dt * src[c] * (1 - um);
+    }
+  }
   double* u0 = (double*)malloc(sizeof(double) * nc);
   memcpy(u0, u, sizeof(double) * nc);
   int dd[3];

@@ -151,6 +151,18 @@ void orc_vof_step(
     double dt, double clipth, int count, int reconstruct_first, uint8_t* mask,
     double* nrm, double* a);
 
+/* orc_vof_step with a volume source src (per cell, NULL: none): the init
+ * stage of Vof::MakeIteration (vof.ipp:504-514) first sets
+ * u = u + dt * src * (1 - u) in every cell and takes fcuu from that field;
+ * the first sweep then uses the planes reconstructed before the source
+ * (cells that became interfacial through the source have none and carry
+ * the plain flux v*u, as cells with an undefined normal do at
+ * vof.ipp:233-255). */
+void orc_vof_step_src(
+    const int n[3], const double h[3], double* u, double* const ffv[3],
+    const double* src, double dt, double clipth, int count,
+    int reconstruct_first, uint8_t* mask, double* nrm, double* a);
+
 /* ---------------- Curvature (height functions) ---------------- */
 
 /* UHeight::Good(uu) (util/height.h:69-124) on a column of `si` values. */

@@ -21,7 +21,8 @@
 //     test/advection/main.cpp:242-256.  Writes out.u, out.n (3N AoS),
 //     out.a, out.k, out.cl (Vof::GetColor, the connected-component colours
 //     of the default union-find recolouring; after the last step) and
-//     out.sumu (text, per step).
+//     out.sumu (text, per step).  With REF_VOF_SRC=path set, the volume
+//     source field of the Vof (raw, N values) is read from that file.
 //   overlap in out         rows (x y z hx hy hz cx cy cz r) -> GetSphereOverlap
 //   reconst in out         rows (n0 n1 n2 u a h0 h1 h2 q dt d) ->
 //                          GetLineA(n,u,h) GetLineU(n,a,h) GetLineFlux(...)
@@ -373,6 +374,13 @@ void RunVof(M& m, Vars& var) {
       t.ffv[f] = FaceInput(m, f, g.vflux);
     }
     t.fcsrc.Reinit(m, 0.);
+    if (const char* srcpath = std::getenv("REF_VOF_SRC")) {
+      // volume source of Vof::MakeIteration's init stage (vof.ipp:510-513)
+      const std::vector<double> src = ReadRaw(srcpath, NCells());
+      for (auto c : m.AllCells()) {
+        t.fcsrc[c] = src[GIdx(m.GetIndexCells().GetMIdx(c))];
+      }
+    }
     VofPar<M> par; // defaults: weymouth, clipth 1e-10, dim 3 (solver/vof.h:13-53)
     (void)var;
     const FieldCell<Scal> fccl(m, 0);

@@ -22,6 +22,10 @@ Fixtures:
                    host threads), its residual and iteration count.
   vof32.npz        3 VOF steps + Heights curvature on 32^3 (sphere r=0.2,
                    Taylor-Green flux at CFL 0.5): aphros's results.
+  vofsrc.npz       3 VOF steps on 32^3 (sphere r=0.2, Taylor-Green flux at
+                   CFL 0.5) with a volume source (Vof's fcs, vof.ipp:510-513)
+                   that vanishes within two cells of the block boundary:
+                   aphros's results (u, normals, plane constants, curvature).
   reconst.txt      random planes: GetLineA, GetLineU, GetLineFlux.
   height.txt       UHeight::Good on the reference's unit-test columns
                    (test/util/main.cpp) and on random 13-cell columns.
@@ -161,6 +165,35 @@ def vof32(tmp):
     np.savez_compressed(os.path.join(OUT, "vof32.npz"), n=n, h=h, dt=dt, steps=3,
                         u_ref=r("u"), n_ref=r("n"), a_ref=r("a"), k_ref=r("k"),
                         alpha_sum=float(case.alpha.sum()))
+
+
+def vof_source(n, seed=11):
+    """Volume source of the vofsrc fixture: half-integer multiples of 0.5 in
+    [-6, 6], zero within two cells of the boundary (there the reference's
+    first sweep would read halo values from before the source)."""
+    rng = np.random.default_rng(seed)
+    s = np.clip(np.round(rng.normal(size=(n, n, n)) * 4) / 2, -6, 6)
+    inner = np.zeros((n, n, n), bool)
+    inner[2:n - 2, 2:n - 2, 2:n - 2] = True
+    return np.where(inner, s, 0.0).ravel()
+
+
+def vofsrc(tmp):
+    case = workload.config("c1", n=32)
+    n, h = case.n, case.h
+    dt = case.cfl_dt(0.5)
+    src = vof_source(n)
+    case.alpha.tofile(os.path.join(tmp, "a.bin"))
+    case.flux.tofile(os.path.join(tmp, "f.bin"))
+    src.tofile(os.path.join(tmp, "s.bin"))
+    os.environ["REF_VOF_SRC"] = os.path.join(tmp, "s.bin")
+    try:
+        run(["vof", str(n), str(n), repr(h), repr(dt), "3", "a.bin", "f.bin", "vs"], tmp)
+    finally:
+        del os.environ["REF_VOF_SRC"]
+    r = lambda q: np.fromfile(os.path.join(tmp, "vs." + q))
+    np.savez_compressed(os.path.join(OUT, "vofsrc.npz"), n=n, h=h, dt=dt, steps=3,
+                        src=src, u_ref=r("u"), n_ref=r("n"), a_ref=r("a"), k_ref=r("k"))
 
 
 def reconst(tmp, rows=300):
@@ -381,7 +414,7 @@ def main():
     if not os.path.exists(HARNESS):
         sys.exit("build the reference harness first: python -m aphros_gb300.build")
     makers = [("advection3d", lambda t: advection3d(args.ref, t)), ("proj16", proj16),
-              ("proj64", proj64), ("vof32", vof32), ("reconst", reconst),
+              ("proj64", proj64), ("vof32", vof32), ("vofsrc", vofsrc), ("reconst", reconst),
               ("height", lambda t: height(args.ref, t)), ("overlap", overlap),
               ("dumps", dumps), ("colors", colors), ("bcg", bcg), ("fluid", fluid)]
     only = set(filter(None, args.only.split(",")))

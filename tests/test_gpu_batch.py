@@ -212,3 +212,42 @@ def test_ragged_domains_in_one_batch():
         a, b = _demean(ctx.get_solution()), _demean(ref[q])
         assert np.linalg.norm(a - b) / np.linalg.norm(b) < 1e-7, q
     batch.close()
+
+
+def _c4_selection():
+    """Eight domains of the 512-domain C4 draw: for every edge in
+    {32, 48, 64, 96} the one with the lowest and the one with the highest
+    density ratio (ratios drawn log-uniformly in [10, 1000])."""
+    cases = workload.batch_cases(512)
+    out = []
+    for n in (32, 48, 64, 96):
+        same = [c for c in cases if c.n == n]
+        ratio = lambda c: c.rho1 / c.rho2
+        out.append(min(same, key=ratio))
+        out.append(max(same, key=ratio))
+    return out
+
+
+def test_batch_c4_domains_within_1e9_of_oracle_cg():
+    """Each of eight C4 domains solved in one batch to ||r||/||b|| = 1e-10
+    has its pressure within 1e-9 (relative L2, mean removed) of the oracle's
+    CG (the algorithm of aphros's SolverConjugate) solved to 1e-13."""
+    import os
+
+    import oracle
+    cases = _c4_selection()
+    ratios = [c.rho1 / c.rho2 for c in cases]
+    assert min(ratios) < 15 and max(ratios) > 700
+    ctxs = _contexts(cases, diffusion=False)
+    batch = _lib.Batch(ctxs)
+    infos = batch.solve(_conf())
+    for q, (c, ctx, info) in enumerate(zip(cases, ctxs, infos)):
+        assert info.converged, q
+        e = ctx.get_system_expr()
+        tol = oracle.rel_tol(e, c.h, 1e-13)
+        xo, io = oracle.cg_solve(c.n, c.h, e, tol, nthreads=os.cpu_count() or 1)
+        assert io.residual < tol, q
+        a, b = _demean(ctx.get_solution()), _demean(xo)
+        err = np.linalg.norm(a - b) / np.linalg.norm(b)
+        assert err <= 1e-9, (q, c.n, ratios[q], err)
+    batch.close()

@@ -86,9 +86,9 @@ def test_oracle_tight_solution_equals_aphros_c1_64(c1_64):
     case, fx = c1_64
     e, _, _ = oracle.assemble_projection(case.n, case.h, case.dt, case.alpha, case.rho1,
                                          case.rho2, case.flux)
-    xo, info = oracle.cg_solve(case.n, case.h, e, oracle.rel_tol(e, case.h, 1e-13),
-                               nthreads=THREADS)
-    assert info.converged
+    tol = oracle.rel_tol(e, case.h, 1e-13)
+    xo, info = oracle.cg_solve(case.n, case.h, e, tol, nthreads=THREADS)
+    assert info.residual < tol
     assert rel_l2(xo, fx["p_ref"]) <= 1e-11
 
 
@@ -111,9 +111,9 @@ def test_c3_field_128_within_bar_of_oracle_cg():
     case = workload.config("c3", n=128)
     e, _, _ = oracle.assemble_projection(case.n, case.h, case.dt, case.alpha, case.rho1,
                                          case.rho2, case.flux)
-    xo, info = oracle.cg_solve(case.n, case.h, e, oracle.rel_tol(e, case.h, 1e-13),
-                               nthreads=THREADS)
-    assert info.converged
+    tol = oracle.rel_tol(e, case.h, 1e-13)
+    xo, info = oracle.cg_solve(case.n, case.h, e, tol, nthreads=THREADS)
+    assert info.residual < tol
     ctx = _context(case)
     errs = _solve_all(ctx, case, xo, (_lib.SOLVER_MGPCG, _lib.SOLVER_MIXED))
     ctx.close()

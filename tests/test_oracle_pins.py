@@ -309,3 +309,18 @@ def test_oracle_fluid_step_equals_reference():
                 key = "%s%d_%d" % (name, q, s)
                 assert np.array_equal(v[:8], fx[key + "_head"]), key
                 assert hashlib.sha256(v.tobytes()).hexdigest() == str(fx[key]), key
+
+
+def test_oracle_vof_source_equals_reference():
+    """orc_vof_step_src (the volume source of Vof::MakeIteration,
+    vof.ipp:504-514) equals aphros bit for bit after three steps."""
+    fx = np.load(golden("vofsrc.npz"))
+    n = int(fx["n"])
+    case = workload.config("c1", n=n)
+    st = oracle.VofState(n, case.h, case.alpha)
+    for _ in range(int(fx["steps"])):
+        st.step(case.flux, float(fx["dt"]), src=fx["src"])
+    assert np.array_equal(st.u, fx["u_ref"])
+    assert np.array_equal(st.nrm, fx["n_ref"], equal_nan=True)
+    assert np.array_equal(st.a, fx["a_ref"], equal_nan=True)
+    assert np.array_equal(st.curvature(), fx["k_ref"], equal_nan=True)
