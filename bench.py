@@ -2,8 +2,9 @@
 
 Headline metric: Poisson solves/s at ||r||/||b|| = 1e-10 on the 512^3
 mixed-precision configuration (64 gas bubbles, density ratio 1000), with the
-plain FP64 multigrid solver on the same system beside it, and p50/p99 of the
-per-solve latency.
+plain FP64 multigrid solver on the same system beside it, p50/p99 of the
+per-solve latency, and every pressure's relative L2 distance to a tight FP64
+solution (MG-PCG to ||r||/||b|| = 1e-13; the bar is 1e-9).
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
                     [--workload c3|c2|c1]
@@ -15,12 +16,18 @@ library's stream); `e2e` goes through the C ABI drop-in with host buffers:
 the 8-coefficient Expr system (64 B/cell) copied from pinned host memory,
 the solve, and the pressure copied back, every step.
 
+The same line carries the other configurations (one GPU): the literal C3
+cycle (V, 2+2 sweeps) and the W-cycle beside the headline; `c2_pipeline`
+(256^3, 100 steps of solve + PLIC advection + curvature); `c4_batch` (512
+uneven domains in one batched solve); `c5_serve` (2000 resident simulations,
+Poisson arrivals at 50-2000 steps/s under a 150 GB budget).
+
 N > 1 runs independent replicas (one per GPU, no collective on the data
 path): every rank solves its own copy; value = all ranks' solves / max time.
 
---impl reference times the reference algorithm's CPU implementation on the
-host cores (the C restatement of aphros's SolverConjugate in oracle/, since
-the reference tree is not available where this runs) on bounded samples.
+--impl reference times the reference's CPU solve on the host cores: aphros's
+own SolverConjugate compiled from its sources (oracle/ref) where they are
+staged, else the C restatement of it in oracle/, on bounded samples.
 """
 import argparse
 import ctypes
@@ -190,29 +197,23 @@ def pinned(count):
     return torch.empty(count, dtype=torch.float64, pin_memory=True)
 
 
-def cpu_baseline(case, expr8_np, threads, budget_s=15.0, cg_iters_full=None):
-    """Times the oracle's CG (aphros's SolverConjugate algorithm) on the host
-    cores for a bounded number of iterations; solves/s extrapolated with the
-    iteration count of a full CG solve (`cg_iters_full`)."""
-    import oracle
-    n = case.n
-    # one iteration first to size the sample
-    t1 = oracle.cg_time_iters(n, expr8_np, 1, threads)
-    iters = max(2, min(50, int(budget_s / max(t1, 1e-6))))
-    t = oracle.cg_time_iters(n, expr8_np, iters, threads)
-    per_iter = t / iters
-    out = {"per_iter_s": per_iter, "iters_sampled": iters}
-    if cg_iters_full:
-        out["value"] = 1.0 / (per_iter * cg_iters_full)
-        out["cg_iters_full"] = cg_iters_full
-    return out
-
-
-def cg_iterations_estimate(case_name, n_full, threads):
-    """Iterations aphros's CG needs on this bubble field at ||r||/||b||=1e-10,
-    measured with the CPU oracle CG on the same bubbles at n_full/8 (at
-    least 32^3) and scaled by the grid ratio (CG iterations grow linearly
-    with the grid edge on this operator)."""
+def cg_iterations_full(case_name, n_full, threads):
+    """Iterations aphros's CG needs at ||r||/||b|| = 1e-10 on this bubble
+    field at n_full^3: the fit iters = a * n^b of the counts the oracle CG
+    (the algorithm of SolverConjugate) measured at 64^3, 128^3 and 256^3
+    (oracle/data/cg_iterations.json, made by make_cg_iterations.py there).
+    Without that file: measured at n_full/8 and scaled by the grid ratio."""
+    p = os.path.join(ROOT, "oracle", "data", "cg_iterations.json")
+    if case_name == "c3":
+        try:
+            with open(p) as f:
+                d = json.load(f)
+            a, b = d["fit"]["a"], d["fit"]["b"]
+            rows = ", ".join("%d^3: %d" % (r["n"], r["iters"]) for r in d["rows"])
+            return int(round(a * n_full ** b)), ("fit %.3g * n^%.3f of the oracle CG's counts "
+                                                 "(%s)" % (a, b, rows))
+        except (OSError, KeyError, ValueError):
+            pass
     import oracle
     from aphros_gb300 import workload
     ns = max(32, n_full // 8)
@@ -221,7 +222,96 @@ def cg_iterations_estimate(case_name, n_full, threads):
                                           cs.flux)
     _, info = oracle.cg_solve(ns, cs.h, es, oracle.rel_tol(es, cs.h, 1e-10),
                               nthreads=threads)
-    return int(round(info.iter * n_full / ns)), int(info.iter), ns
+    return (int(round(info.iter * n_full / ns)),
+            "oracle CG at %d^3 (%d iterations) scaled by the grid ratio" % (ns, info.iter))
+
+
+def cpu_model():
+    """CPU model of the host, from /proc/cpuinfo (or the platform string)."""
+    try:
+        with open("/proc/cpuinfo") as f:
+            txt = f.read()
+        for key in ("model name", "Model Name", "CPU part"):
+            for line in txt.splitlines():
+                if line.lower().startswith(key.lower()):
+                    val = line.split(":", 1)[1].strip()
+                    if key == "CPU part":
+                        imp = [ln.split(":", 1)[1].strip() for ln in txt.splitlines()
+                               if ln.lower().startswith("cpu implementer")]
+                        return "arm implementer %s part %s" % (imp[0] if imp else "?", val)
+                    return val
+    except OSError:
+        pass
+    import platform
+    return platform.processor() or platform.machine()
+
+
+REF_HARNESS = os.path.join(ROOT, "oracle", "_ref", "ref_harness")
+
+
+def reference_cg_seconds(case, iters, threads, blocks=32):
+    """aphros's own SolverConjugate (compiled from the reference sources by
+    oracle/ref/Makefile into ref_harness) on the workload's projection
+    system, assembled by aphros's Proj code from the same volume fraction
+    and fluxes: exactly `iters` CG iterations on `threads` OpenMP threads,
+    blocks of blocks^3 cells.  Returns (seconds per iteration, iterations,
+    harness wall seconds) or None when the harness is not built."""
+    import tempfile
+    if not os.access(REF_HARNESS, os.X_OK):
+        return None
+    with tempfile.TemporaryDirectory() as tmp:
+        case.alpha.tofile(os.path.join(tmp, "a.bin"))
+        case.flux.tofile(os.path.join(tmp, "f.bin"))
+        env = dict(os.environ, OMP_NUM_THREADS=str(threads))
+        bs = min(blocks, case.n)
+        t0 = time.perf_counter()
+        r = subprocess.run([REF_HARNESS, "cgtime", str(case.n), str(bs), repr(case.dt),
+                            repr(case.rho1), repr(case.rho2), str(iters), "a.bin", "f.bin",
+                            "cg"], cwd=tmp, env=env, stdout=subprocess.PIPE,
+                           stderr=subprocess.STDOUT, text=True)
+        wall = time.perf_counter() - t0
+        if r.returncode != 0:
+            print("reference harness failed: %s" % r.stdout[-500:], file=sys.stderr)
+            return None
+        with open(os.path.join(tmp, "cg.time")) as f:
+            sec, it = f.read().split()[:2]
+    it = int(it)
+    return float(sec) / max(it, 1), it, wall
+
+
+def cpu_baseline(case, case_name, threads, budget_s=15.0, expr8_np=None):
+    """The reference's CPU CG on the host cores, on a bounded sample: aphros's
+    own SolverConjugate through ref_harness when built ("reference"), else
+    the oracle's C restatement ("port").  Solves/s from the time per
+    iteration and the iteration count of a full solve."""
+    iters_full, how = cg_iterations_full(case_name, case.n, threads)
+    # a sample of about budget_s of CG iterations (rate of the port first)
+    out = None
+    ref = reference_cg_seconds(case, max(2, int(budget_s / 1.0)), threads)
+    if ref is not None:
+        per_iter, it, wall = ref
+        out = {"kind": "reference", "per_iter_s": per_iter, "iters_sampled": it,
+               "sample": "%d iterations of aphros's own SolverConjugate (compiled from its "
+                         "sources, blocks of 32^3, %d OpenMP threads) on the %d^3 system "
+                         "assembled by aphros's Proj code (%.3f s/iteration; %.0f s with "
+                         "the assembly); full solve = %d iterations (%s)"
+                         % (it, threads, case.n, per_iter, wall, iters_full, how)}
+    else:
+        import oracle
+        if expr8_np is None:
+            expr8_np, _, _ = oracle.assemble_projection(case.n, case.h, case.dt, case.alpha,
+                                                        case.rho1, case.rho2, case.flux)
+        t1 = oracle.cg_time_iters(case.n, expr8_np, 1, threads)
+        iters = max(2, min(50, int(budget_s / max(t1, 1e-6))))
+        per_iter = oracle.cg_time_iters(case.n, expr8_np, iters, threads) / iters
+        out = {"kind": "port", "per_iter_s": per_iter, "iters_sampled": iters,
+               "sample": "%d CG iterations of the C restatement of aphros SolverConjugate on "
+                         "the %d^3 system (%.3f s/iter, %d threads); full solve = %d "
+                         "iterations (%s)" % (iters, case.n, per_iter, threads, iters_full,
+                                              how)}
+    out.update({"value": 1.0 / (out["per_iter_s"] * iters_full), "unit": UNIT,
+                "cores": threads, "cpu": cpu_model(), "cg_iters_full": iters_full})
+    return out
 
 
 # algorithmic bytes per cell (compulsory traffic, each array element read or
@@ -302,17 +392,38 @@ def measure_vof(ctx, case, peak, peak_kind, steps, cpu=True):
 
 
 # ---------------------------------------------------------------------------
-# The configuration's V-cycle: one red-black sweep before and after the
-# coarse correction on the finest level, and twice as many on each coarser
-# level (at most 16), the shape that is fastest at 512^3 (finest-level
-# sweeps dominate the cost; coarse ones are cheap and improve the coarse
-# correction).  Library defaults otherwise.
+# The headline V-cycle: one red-black sweep before and after the coarse
+# correction on the finest level, and twice as many on each coarser level
+# (at most 16), the shape that is fastest at 512^3 (finest-level sweeps
+# dominate the cost; coarse ones are cheap and improve the coarse
+# correction).  Library defaults otherwise.  The configuration's literal
+# cycle (2+2 sweeps on every level) is measured beside it.
 HEADLINE_MG = {"mg_pre": 1, "mg_post": 1}
+# The headline mixed solve stops at ||r||/||b|| <= 5e-11: stopped at 1e-10
+# its pressure was 1.5e-9 (relative L2) from the tight FP64 solution at
+# 512^3, above the 1e-9 bar; at 5e-11 it is 1.5e-10 for one more outer
+# iteration.  The FP64 comparator stops at 1e-10 (its pressure is within
+# the bar there).
+HEADLINE_STOP = 5e-11
+PRESSURE_BAR = 1e-9
+# algorithmic bytes of one FP32 red-black half sweep per cell: half of a
+# full sweep's x r/w 8 + b 4 + couplings 12 = 24 (FP64 48 halved)
+HALF_SWEEP_BYTES = 12.0
 
 
 def set_headline_cycle(ctx, _lib):
     ctx.set_option(_lib.OPT_CYCLE, 1)
     ctx.set_option(_lib.OPT_SWEEP_GROWTH, 3)
+
+
+def set_literal_cycle(ctx, _lib):
+    ctx.set_option(_lib.OPT_CYCLE, 1)
+    ctx.set_option(_lib.OPT_SWEEP_GROWTH, 1)
+
+
+def set_default_cycle(ctx, _lib):
+    ctx.set_option(_lib.OPT_CYCLE, 0)
+    ctx.set_option(_lib.OPT_SWEEP_GROWTH, 0)
 
 
 # arms
@@ -332,13 +443,9 @@ def run_ours(args):
     N = case.N
     ctx = _lib.Context(case.n, case.h, device)
     ctx.assemble_projection(case.alpha, case.rho1, case.rho2, case.flux, case.dt)
-    # the configuration's V-cycles; the W-cycle (library default at this
-    # size) is measured beside them
-    set_headline_cycle(ctx, _lib)
     _, bnorm = ctx.residual_norms()
-    tol = 1e-10 * bnorm / math.sqrt(case.h ** 3)
-    conf_mixed = _lib.default_conf(solver=_lib.SOLVER_MIXED, tol=tol, maxiter=100, **HEADLINE_MG)
-    conf_fp64 = _lib.default_conf(solver=_lib.SOLVER_MGPCG, tol=tol, maxiter=1000, **HEADLINE_MG)
+    abs_tol = lambda rt: rt * bnorm / math.sqrt(case.h ** 3)
+    tol = abs_tol(1e-10)
 
     def run_steps(conf, k, collect):
         times, launches, infos = [], 0, []
@@ -354,6 +461,19 @@ def run_ours(args):
         total_ms = ctx.elapsed(0, 1)
         return total_ms, times, launches, infos
 
+    # the tight FP64 reference of the pressure bar: MG-PCG (W-cycle) to
+    # ||r||/||b|| = 1e-13, untimed
+    set_default_cycle(ctx, _lib)
+    ctx.set_option(_lib.OPT_CYCLE, 2)
+    ctx.solve_resident(_lib.default_conf(solver=_lib.SOLVER_MGPCG, tol=abs_tol(1e-13),
+                                         maxiter=1000), zero_guess=True)
+    rn_t, bn_t = ctx.residual_norms()
+    p_tight = ctx.get_solution()
+    set_headline_cycle(ctx, _lib)
+
+    conf_mixed = _lib.default_conf(solver=_lib.SOLVER_MIXED, tol=abs_tol(HEADLINE_STOP),
+                                   maxiter=100, **HEADLINE_MG)
+    conf_fp64 = _lib.default_conf(solver=_lib.SOLVER_MGPCG, tol=tol, maxiter=1000, **HEADLINE_MG)
     # warm-up (builds both hierarchies)
     for conf in (conf_mixed, conf_fp64):
         run_steps(conf, args.warmup, False)
@@ -376,38 +496,54 @@ def run_ours(args):
     units64, tmax64 = aggregate_over_ranks(args.steps, t_fp64 / 1000.0)
     value = units / tmax
     fp64_value = units64 / tmax64
+    err_mixed = rel_l2(p_mixed, p_tight)
+    err_fp64 = rel_l2(p_fp64, p_tight)
+    # the same mixed solve stopped at exactly 1e-10 (why the headline stops
+    # at HEADLINE_STOP)
+    conf_mixed_10 = _lib.default_conf(solver=_lib.SOLVER_MIXED, tol=tol, maxiter=100,
+                                      **HEADLINE_MG)
+    t10, _, _, inf10 = run_steps(conf_mixed_10, 2, True)
+    at_1e10 = {"ms_per_step": t10 / 2, "pressure_rel_err_vs_tight_fp64":
+               rel_l2(ctx.get_solution(), p_tight), "outer": inf10[-1].iter,
+               "inner": inf10[-1].inner_iter}
 
-    # the same solves with W-cycles below the finest level
-    w_cycle = None
-    if not args.no_w_cycle:
-        # library defaults: W below the finest level, 2+2 sweeps on every level
-        ctx.set_option(_lib.OPT_CYCLE, 0)
-        ctx.set_option(_lib.OPT_SWEEP_GROWTH, 0)
-        conf_mixed_w = _lib.default_conf(solver=_lib.SOLVER_MIXED, tol=tol, maxiter=100)
-        conf_fp64_w = _lib.default_conf(solver=_lib.SOLVER_MGPCG, tol=tol, maxiter=1000)
-        kw = max(1, min(args.steps, 5))
-        run_steps(conf_mixed_w, 1, False)
-        run_steps(conf_fp64_w, 1, False)
-        tw, stw, _, infw = run_steps(conf_mixed_w, kw, True)
-        rnw, bnw = ctx.residual_norms()
-        pw = ctx.get_solution()
-        tw64, _, _, infw64 = run_steps(conf_fp64_w, kw, True)
+    def variant(setter, mg, k):
+        setter(ctx, _lib)
+        cm = _lib.default_conf(solver=_lib.SOLVER_MIXED, tol=tol, maxiter=100, **mg)
+        cf = _lib.default_conf(solver=_lib.SOLVER_MGPCG, tol=tol, maxiter=1000, **mg)
+        run_steps(cm, 1, False)
+        run_steps(cf, 1, False)
+        tm, _, _, im = run_steps(cm, k, True)
+        rnm, bnm = ctx.residual_norms()
+        pm = ctx.get_solution()
+        tf, _, _, iff = run_steps(cf, k, True)
+        pf = ctx.get_solution()
+        um, tmm = aggregate_over_ranks(k, tm / 1000.0)
+        uf, tmf = aggregate_over_ranks(k, tf / 1000.0)
         set_headline_cycle(ctx, _lib)
-        uw, tmw = aggregate_over_ranks(kw, tw / 1000.0)
-        uw64, tmw64 = aggregate_over_ranks(kw, tw64 / 1000.0)
-        w_cycle = {"value": uw / tmw, "unit": UNIT, "ms_per_step": float(tw / kw),
-                   "iters": {"outer": infw[-1].iter, "inner_fp32_pcg": infw[-1].inner_iter},
-                   "rel_residual": rnw / bnw, "pressure_rel_err_vs_fp64_v": rel_l2(pw, p_fp64),
-                   "fp64": {"value": uw64 / tmw64, "ms_per_step": float(tw64 / kw),
-                            "iters": infw64[-1].iter},
-                   "mixed_over_fp64": (uw / tmw) / (uw64 / tmw64)}
+        em, ef = rel_l2(pm, p_tight), rel_l2(pf, p_tight)
+        return {"value": um / tmm, "unit": UNIT, "ms_per_step": float(tm / k),
+                "iters": {"outer": im[-1].iter, "inner_fp32_pcg": im[-1].inner_iter},
+                "rel_residual": rnm / bnm, "pressure_rel_err_vs_tight_fp64": em,
+                "fp64": {"value": uf / tmf, "ms_per_step": float(tf / k),
+                         "iters": iff[-1].iter, "pressure_rel_err_vs_tight_fp64": ef},
+                "mixed_over_fp64": (um / tmm) / (uf / tmf),
+                "within_bar": bool(em <= PRESSURE_BAR and ef <= PRESSURE_BAR)}
+
+    kv = max(1, min(args.steps, 3))
+    # the configuration's literal cycle: V, 2+2 red-black sweeps on every level
+    literal = variant(set_literal_cycle, {"mg_pre": 2, "mg_post": 2}, kv)
+    # library defaults: W below the finest level, 2+2 sweeps
+    w_cycle = None if args.no_w_cycle else variant(set_default_cycle, {}, kv)
 
     # live roofline of the dominant kernel of the mixed solve
     peak, peak_kind = measured_peak_gbs()
-    kms, kbytes = ctx.time_kernel(_lib.K_SMOOTH32, reps=20)
+    kms, _ = ctx.time_kernel(_lib.K_SMOOTH32, reps=20)
+    kbytes = HALF_SWEEP_BYTES * N
     achieved = kbytes / (kms * 1e-3) / 1e9
+    traffic = ncu_traffic("KSmooth<float>", N)
     kernel_table = {}
-    for kid in (_lib.K_SMOOTH32, _lib.K_APPLY32, _lib.K_RESTRICT32,
+    for kid in (_lib.K_SMOOTH32, _lib.K_SWEEP32, _lib.K_APPLY32, _lib.K_RESTRICT32,
                 _lib.K_APPLY64, _lib.K_SMOOTH64):
         try:
             ms_k, b_k = ctx.time_kernel(kid, reps=10)
@@ -441,22 +577,27 @@ def run_ours(args):
                "d2h_bytes_per_step": 8 * N, "steps": e2e_steps,
                "path": "aphgpu_set_system_expr + aphgpu_solve (linear::Solver drop-in), "
                        "pinned host buffers"}
+    ctx.close()
 
     cpu = None
     if rank == 0 and not args.no_cpu:
         threads = os.cpu_count() or 1
-        iters_full, iters_small, n_small = cg_iterations_estimate(args.workload, case.n, threads)
-        expr_np = np.empty(8 * N)
-        ctx._check(ctx._L.aphgpu_get_system_expr(ctx.handle, _lib.ptr(expr_np)))
-        cb = cpu_baseline(case, expr_np, threads, budget_s=args.cpu_budget,
-                          cg_iters_full=iters_full)
-        cpu = {"value": cb.get("value"), "unit": UNIT, "cores": threads, "kind": "port",
-               "sample": "%d CG iterations of the C restatement of aphros SolverConjugate "
-                         "on the %d^3 system (%.3f s/iter, %d threads); full solve = %d "
-                         "iterations, from the same CG on the same bubble field at "
-                         "%d^3 (%d iterations) scaled by the grid ratio"
-                         % (cb["iters_sampled"], case.n, cb["per_iter_s"], threads,
-                            iters_full, n_small, iters_small, )}
+        cpu = cpu_baseline(case, args.workload, threads, budget_s=args.cpu_budget)
+
+    # the other configurations, on one GPU only
+    subs = {}
+    if world == 1 and args.workload == "c3":
+        if not args.no_pipeline:
+            subs["c2_pipeline"] = measure_pipeline(args)
+        if not args.no_batch:
+            sub = argparse.Namespace(**vars(args))
+            sub.steps, sub.warmup = max(2, min(args.steps, 5)), 2
+            subs["c4_batch"] = run_batch(sub)
+        if not args.no_serve:
+            sub = argparse.Namespace(**vars(args))
+            sub.sims, sub.requests = args.serve_sims, args.serve_requests
+            sub.rates = args.serve_rates
+            subs["c5_serve"] = run_serve(sub)
 
     if rank != 0:
         return None
@@ -474,25 +615,36 @@ def run_ours(args):
                    "l2": "inputs larger than L2 (1 GB per FP64 field), no flush",
                    "multigrid": "V-cycle, red-black Gauss-Seidel 1+1 on the finest level "
                                 "and 2^l+2^l (at most 16) on level l below it, coarse "
-                                "couplings 60 % series + 40 % half-Galerkin; w_cycle: "
-                                "library defaults (W below the finest level, 2+2 sweeps)",
+                                "couplings 60 % series + 40 % half-Galerkin; literal_c3_cycle: "
+                                "V, 2+2 on every level; w_cycle: library defaults (W below "
+                                "the finest level, 2+2 sweeps)",
+                   "stop": "mixed: ||r||/||b|| <= %g (pressure bar, see at_1e-10); FP64: "
+                           "<= 1e-10" % HEADLINE_STOP,
                    "parallelism": "replicas" if world > 1 else "single GPU"},
         "p50_ms": float(np.percentile(lat, 50)), "p99_ms": float(np.percentile(lat, 99)),
         "fp64": {"value": fp64_value, "unit": UNIT,
                  "ms_per_step": float(t_fp64 / args.steps),
                  "p50_ms": float(np.percentile(st_fp64, 50)),
                  "p99_ms": float(np.percentile(st_fp64, 99)),
-                 "iters": inf_fp64[-1].iter if inf_fp64 else None},
+                 "iters": inf_fp64[-1].iter if inf_fp64 else None,
+                 "pressure_rel_err_vs_tight_fp64": err_fp64},
         "mixed_over_fp64": value / fp64_value,
+        "pressure_rel_err_vs_tight_fp64": err_mixed,
+        "pressure_rel_err_vs_fp64_solve": rel_l2(p_mixed, p_fp64),
+        "tight_fp64_rel_residual": rn_t / bn_t,
+        "within_1e-9": bool(err_mixed <= PRESSURE_BAR and err_fp64 <= PRESSURE_BAR),
+        "at_1e-10": at_1e10,
+        "literal_c3_cycle": literal,
         "w_cycle": w_cycle,
         "iters": {"outer": inf_mixed[-1].iter, "inner_fp32_pcg": inf_mixed[-1].inner_iter},
         "rel_residual": rel_res_mixed,
-        "pressure_rel_err_vs_fp64": rel_l2(p_mixed, p_fp64),
         "cells_per_s": value * N,
-        "roofline": {"bound": "hbm", "kernel": "KSmooth<float> (red-black half sweep, finest level)",
+        "roofline": {"bound": "hbm",
+                     "kernel": "KSmooth<float> (red-black half sweep, finest level)",
                      "achieved": achieved, "peak": peak, "unit": "GB/s",
                      "frac": achieved / peak, "peak_kind": peak_kind,
-                     "traffic": ncu_traffic("KSmooth<float>", N)},
+                     "algorithmic_bytes": kbytes, "traffic": traffic,
+                     "traffic_over_algorithmic": (traffic / kbytes) if traffic else None},
         "kernels": kernel_table,
         "vof": vof,
         "gpu_launches": int(l_mixed),
@@ -500,11 +652,65 @@ def run_ours(args):
         "cpu_baseline": cpu,
         "clocks": sampler.summary(),
     }
+    line.update(subs)
     return line
 
 
+def measure_pipeline(args, steps=100):
+    """C2: 256^3, 16 bubbles, density ratio 1000; `steps` time steps of the
+    projection (assembly from the resident volume fraction and the predicted
+    fluxes, mixed solve to 1e-10 warm-started from the resident pressure,
+    flux correction) + PLIC advection + height curvature, everything
+    resident on the device; against the same steps with the FP64 MG-PCG."""
+    import torch
+    from aphros_gb300 import _lib, workload
+    case = workload.config("c2")
+    dt = case.cfl_dt(0.5)
+    flux = pinned(3 * case.N).numpy()
+    flux[:] = case.flux
+    out = {"workload": "C2: 256^3 periodic cube, 16 gas spheres r in [0.03,0.08], density "
+                       "ratio 1000, Taylor-Green + N(0,0.01) predicted fluxes, %d steps of "
+                       "solve (rel. residual 1e-10, warm start) + PLIC advection (CFL 0.5) "
+                       "+ height curvature" % steps}
+    for name, solver in (("mixed", _lib.SOLVER_MIXED), ("fp64", _lib.SOLVER_MGPCG)):
+        ctx = _lib.Context(case.n, case.h, 0)
+        ctx.vof_init(case.alpha)
+        conf = _lib.default_conf(solver=solver, tol=0.0, rtol=1e-10, maxiter=1000)
+        dev = {"solve": 0.0, "vof": 0.0, "curvature": 0.0}
+        iters, vol0 = [], None
+        torch.cuda.synchronize()
+        w0 = time.perf_counter()
+        for s in range(steps):
+            ctx._check(ctx._L.aphgpu_assemble_projection(ctx.handle, None, case.rho1, case.rho2,
+                                                         _lib.ptr(flux), None, case.dt, 1))
+            info = ctx.solve_resident(conf, zero_guess=(s == 0))
+            dev["solve"] += ctx.last_timing()[0]
+            iters.append(info.iter if solver == _lib.SOLVER_MGPCG else info.inner_iter)
+            ctx.flux_correct(out=False)
+            ctx.vof_step(None, dt)
+            dev["vof"] += ctx.last_timing()[0]
+            ctx.curvature(out=False)
+            dev["curvature"] += ctx.last_timing()[0]
+            if s == 0:
+                vol0 = float(ctx.vof_get()[0].sum())
+        torch.cuda.synchronize()
+        wall = time.perf_counter() - w0
+        vol1 = float(ctx.vof_get()[0].sum())
+        out[name] = {"steps_per_s": steps / wall, "wall_ms_per_step": 1e3 * wall / steps,
+                     "device_ms_per_step": {k: v / steps for k, v in dev.items()},
+                     "iters_mean": float(np.mean(iters)), "iters_first": iters[0],
+                     "volume_drift_rel": abs(vol1 - vol0) / vol0}
+        ctx.close()
+    out["mixed_over_fp64"] = out["mixed"]["steps_per_s"] / out["fp64"]["steps_per_s"]
+    return out
+
+
 def run_reference(args):
-    """aphros's CG algorithm (oracle restatement) on the host cores."""
+    """The reference's CPU solve on the host cores: aphros's own
+    SolverConjugate compiled from its sources (ref_harness), else the
+    oracle's C restatement.  Each step is one CG iteration of the workload's
+    system; solves/s = 1 / (seconds per iteration x iterations of a full
+    solve)."""
     rank, world, _ = dist_env()
     if rank != 0:
         return None
@@ -513,82 +719,105 @@ def run_reference(args):
     case = workload.config(args.workload)
     n, h = case.n, case.h
     threads = os.cpu_count() or 1
-    e, _, _ = oracle.assemble_projection(n, h, case.dt, case.alpha, case.rho1,
-                                         case.rho2, case.flux)
-    # iterations of a full solve: measured on the CPU at n/8 and scaled
-    iters_full, iters_small, ns = cg_iterations_estimate(args.workload, n, threads)
-    per = []
-    for _ in range(args.warmup):
-        oracle.cg_time_iters(n, e, 1, threads)
-    sample_iters = 3
-    for _ in range(args.steps):
-        t = oracle.cg_time_iters(n, e, sample_iters, threads)
-        per.append(t / sample_iters)
-    per_iter = float(np.median(per))
+    iters_full, how = cg_iterations_full(args.workload, n, threads)
+    ref = reference_cg_seconds(case, args.warmup + args.steps, threads)
+    if ref is not None:
+        per_iter, it, wall = ref
+        kind = "reference"
+        sample = ("each step one iteration of aphros's own SolverConjugate (compiled from "
+                  "its sources, blocks of 32^3, %d OpenMP threads) on the %d^3 system "
+                  "assembled by aphros's Proj code; %d iterations in one run (%.3f s each, "
+                  "%.0f s with the assembly); full solve = %d iterations (%s)"
+                  % (threads, n, it, per_iter, wall, iters_full, how))
+    else:
+        e, _, _ = oracle.assemble_projection(n, h, case.dt, case.alpha, case.rho1,
+                                             case.rho2, case.flux)
+        for _ in range(args.warmup):
+            oracle.cg_time_iters(n, e, 1, threads)
+        per = [oracle.cg_time_iters(n, e, 1, threads) for _ in range(args.steps)]
+        per_iter = float(np.median(per))
+        kind = "port"
+        sample = ("each step one CG iteration at %d^3 (C restatement of aphros "
+                  "SolverConjugate, %d threads); full solve = %d iterations (%s)"
+                  % (n, threads, iters_full, how))
     value = 1.0 / (per_iter * iters_full)
     return {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world,
-        "steps": args.steps, "warmup": args.warmup, "ms_per_step": per_iter * 1e3 * sample_iters,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": per_iter * 1e3,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
         "dtype": "f64", "data": "synthetic (seeded bubble field, Taylor-Green + noise)",
         "config": {"workload": WORKLOADS[args.workload], "cells": case.N},
         "impl": "reference",
-        "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port",
-                         "sample": "each step %d CG iterations at %d^3 (C restatement of "
-                                   "aphros SolverConjugate, %d threads); full solve %d "
-                                   "iterations (same CG at %d^3: %d, scaled by the grid ratio)"
-                                   % (sample_iters, n, threads, iters_full, ns, iters_small)},
+        "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": kind,
+                         "cpu": cpu_model(), "cg_iters_full": iters_full, "sample": sample},
         "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0,
                 "d2h_bytes_per_step": 0},
     }
 
 
 def run_serve(args):
-    """Served stream: Poisson-arrival step requests for resident simulations
-    of edge 32-128 (log-uniform, multiples of 16, 1-8 bubbles, density ratio
-    1000) on a continuous-batching server, against the same requests run one
-    by one with the plain FP64 solver."""
+    """Served stream (C5): Poisson-arrival step requests for resident
+    simulations of edge 32-128 (log-uniform, multiples of 16, 1-8 bubbles,
+    density ratio 1000) on a continuous-batching server under an HBM budget,
+    saturated and at each mean rate of `rates`; against the same requests
+    run one at a time with the plain FP64 solver."""
     import random
 
     from aphros_gb300 import _lib, build, serve, workload
     build.build()
+    t_setup = time.perf_counter()
     cases = workload.served_cases(args.sims)
     dts = [0.5 * c.cfl_dt(0.5) for c in cases]
     rng = random.Random(5)
-    order = [rng.randrange(len(cases)) for _ in range(args.requests)]
 
-    def drive(slots, conf, rate):
-        with serve.Server(budget_bytes=args.budget_gb * 1e9, slots=slots, conf=conf) as srv:
-            sims = [srv.add(c, sigma=0.05) for c in cases]
-            # warm-up: one step of every simulation (admission, hierarchy)
-            for t in [srv.submit(sims[i], cases[i].flux, dts[i]) for i in range(len(cases))]:
-                srv.wait(t)
-            tickets = []
-            t0 = time.perf_counter()
-            clock = 0.0
-            for i in order:
-                if rate > 0:
-                    clock += rng.expovariate(rate)
-                    delay = t0 + clock - time.perf_counter()
-                    if delay > 0:
-                        time.sleep(delay)
-                tickets.append(srv.submit(sims[i], cases[i].flux, dts[i]))
-            res = [srv.wait(t) for t in tickets]
-            t1 = time.perf_counter()
-            st = srv.stats()
+    def requests(k):
+        return [rng.randrange(len(cases)) for _ in range(k)]
+
+    def drive(srv, sims, order, rate):
+        tickets = []
+        t0 = time.perf_counter()
+        clock = 0.0
+        for i in order:
+            if rate > 0:
+                clock += rng.expovariate(rate)
+                delay = t0 + clock - time.perf_counter()
+                if delay > 0:
+                    time.sleep(delay)
+            tickets.append(srv.submit(sims[i], cases[i].flux, dts[i]))
+        res = [srv.wait(t) for t in tickets]
+        t1 = time.perf_counter()
         lat = np.array([r.latency_ms for r in res])
         ok = all(r.status == _lib.OK and r.converged for r in res)
-        return {"steps_per_s": len(res) / (t1 - t0), "p50_ms": float(np.percentile(lat, 50)),
-                "p99_ms": float(np.percentile(lat, 99)), "all_converged": ok,
-                "evictions": int(st.evictions), "resident_gb": st.resident_bytes / 1e9}
+        return {"requests": len(res), "steps_per_s": len(res) / (t1 - t0),
+                "p50_ms": float(np.percentile(lat, 50)), "p99_ms": float(np.percentile(lat, 99)),
+                "all_converged": ok}
+
+    def server(slots, conf):
+        srv = serve.Server(budget_bytes=args.budget_gb * 1e9, slots=slots, conf=conf)
+        sims = [srv.add(c, sigma=0.05) for c in cases]
+        return srv, sims
 
     mixed = _lib.default_conf(solver=_lib.SOLVER_MIXED, rtol=1e-10)
     plain = _lib.default_conf(solver=_lib.SOLVER_MGPCG, rtol=1e-10)
-    one_by_one = drive(1, plain, 0.0)
-    saturated = drive(args.slots, mixed, 0.0)
+    srv, sims = server(args.slots, mixed)
+    # warm-up: one step of every simulation (admission, hierarchy, evictions)
+    for t in [srv.submit(sims[i], cases[i].flux, dts[i]) for i in range(len(cases))]:
+        srv.wait(t)
+    setup_s = time.perf_counter() - t_setup
+    saturated = drive(srv, sims, requests(args.requests), 0.0)
     rates = {}
     for rate in args.rates:
-        rates[str(rate)] = drive(args.slots, mixed, rate)
+        rates[str(int(rate) if rate == int(rate) else rate)] = drive(
+            srv, sims, requests(args.requests), rate)
+    st = srv.stats()
+    srv.close()
+    # the plain FP64 solver, one request at a time, on a sample of requests
+    srv1, sims1 = server(1, plain)
+    order1 = requests(max(16, args.requests // 4))
+    for i in sorted(set(order1)):
+        srv1.wait(srv1.submit(sims1[i], cases[i].flux, dts[i]))
+    one_by_one = drive(srv1, sims1, order1, 0.0)
+    srv1.close()
     cells = [c.N for c in cases]
     return {
         "metric": "served steps/s and p50/p99 step latency (projection + PLIC advection + "
@@ -597,12 +826,14 @@ def run_serve(args):
         "higher_is_better": True,
         "config": {"workload": "served stream, %d resident simulations of edge 32-128 "
                                "(log-uniform, multiples of 16), 1-8 bubbles, density ratio "
-                               "1000, %d requests, %d slots, %g GB budget"
+                               "1000, %d requests per rate, %d slots, %g GB budget"
                                % (len(cases), args.requests, args.slots, args.budget_gb),
-                   "cells_mean": float(np.mean(cells))},
+                   "cells_total": int(sum(cells)), "cells_mean": float(np.mean(cells))},
         "served_saturated": saturated, "served_at_rate": rates,
         "one_by_one_plain_fp64": one_by_one,
         "speedup_vs_one_by_one": saturated["steps_per_s"] / one_by_one["steps_per_s"],
+        "evictions": int(st.evictions), "admissions": int(st.admissions),
+        "resident_gb": st.resident_bytes / 1e9, "setup_s": setup_s,
     }
 
 
@@ -806,11 +1037,22 @@ def main():
                          "after `warmup` solves, no other work and no output line")
     ap.add_argument("--serve", action="store_true",
                     help="served-stream benchmark instead of the solve benchmark")
-    ap.add_argument("--sims", type=int, default=64)
+    ap.add_argument("--sims", type=int, default=2000)
     ap.add_argument("--requests", type=int, default=256)
     ap.add_argument("--slots", type=int, default=8)
     ap.add_argument("--budget-gb", type=float, default=150.0)
-    ap.add_argument("--rates", type=float, nargs="*", default=[50.0, 200.0])
+    ap.add_argument("--rates", type=float, nargs="*",
+                    default=[50.0, 200.0, 500.0, 1000.0, 2000.0])
+    ap.add_argument("--no-pipeline", action="store_true",
+                    help="skip the C2 100-step pipeline sub-result")
+    ap.add_argument("--no-batch", action="store_true",
+                    help="skip the C4 batched sub-result")
+    ap.add_argument("--no-serve", action="store_true",
+                    help="skip the C5 served sub-result")
+    ap.add_argument("--serve-sims", type=int, default=2000)
+    ap.add_argument("--serve-requests", type=int, default=256)
+    ap.add_argument("--serve-rates", type=float, nargs="*",
+                    default=[50.0, 200.0, 500.0, 1000.0, 2000.0])
     ap.add_argument("--batch", action="store_true",
                     help="batched-domains benchmark instead of the solve benchmark")
     ap.add_argument("--domains", type=int, default=512)

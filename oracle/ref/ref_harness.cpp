@@ -15,6 +15,12 @@
 //     solve with linear::SolverConjugate ("conjugate" module), fluxes by
 //     UEmbed::Eval (proj.ipp:399-403).
 //     Writes out.expr (8N), out.p (N), out.flux (3N), out.info (text).
+//   cgtime n bs dt rho1 rho2 iters alpha.bin vflux.bin out
+//     the system of `proj`, then linear::SolverConjugate for exactly
+//     `iters` iterations (tolerance 0, miniter = maxiter = iters) on all
+//     OpenMP threads; writes out.time (text: wall-clock seconds from the
+//     end of the assembly to the end of the solve, and the iterations).
+//     Nothing else is written (the timing mode of the CPU baseline).
 //   vof   n bs h dt steps u.bin vflux.bin out
 //     Vof (scheme weymouth) StartStep/MakeIteration/FinishStep/PostStep and
 //     curvature::Heights::CalcCurvature per step, as in
@@ -45,6 +51,8 @@
 //   raw   n type in.f64 out.raw
 //     dump::Raw::WriteBlocks of one block covering the mesh (the
 //     sequential writer, dump/raw.ipp:73-158), values converted to type.
+#include <omp.h>
+
 #include <cmath>
 #include <cstdio>
 #include <cstdlib>
@@ -102,6 +110,8 @@ void WriteRaw(const std::string& path, const std::vector<double>& v) {
 }
 
 struct Global {
+  bool time_only = false;  // cgtime mode: no field outputs
+  double t_solve0 = 0, t_solve1 = 0;
   int n = 0; // unused when nx,ny,nz set
   int nn[3] = {0, 0, 0};
   Scal dt = 0, rho1 = 1, rho2 = 1;
@@ -198,6 +208,7 @@ void RunProj(M& m, Vars& var) {
     const Scal mean = t.sum7 / t.cnt;
     for (auto c : m.Cells()) {
       t.fcs[c].back() -= mean;
+      if (g.time_only) continue;
       const size_t i = GIdx(m.GetIndexCells().GetMIdx(c));
       for (size_t q = 0; q < 8; ++q) {
         g.out_expr[8 * i + q] = t.fcs[c][q];
@@ -208,10 +219,22 @@ void RunProj(M& m, Vars& var) {
     fassert(factory, "conjugate solver not found");
     t.solver = factory->Make(var, "symm", m);
   }
+  if (sem("clock0")) {
+    if (m.IsRoot()) g.t_solve0 = omp_get_wtime();
+  }
   if (sem.Nested("solve")) {
     t.info = t.solver->Solve(t.fcs, nullptr, t.fcp, m);
   }
-  if (sem("fluxes")) {
+  if (sem("clock1")) {
+    if (m.IsRoot()) g.t_solve1 = omp_get_wtime();
+  }
+  if (g.time_only && sem("info")) {
+    if (m.IsRoot()) {
+      g.residual = t.info.residual;
+      g.iter = t.info.iter;
+    }
+  }
+  if (!g.time_only && sem("fluxes")) {
     for (auto c : m.Cells()) {
       g.out_p[GIdx(m.GetIndexCells().GetMIdx(c))] = t.fcp[c];
     }
@@ -491,6 +514,27 @@ int Main(int argc, const char** argv) {
     int r = RunMpiBasicString<M>(mpi, RunProj, conf);
     return r;
   }
+  if (mode == "cgtime") {
+    if (argc != 11) return 1;
+    const MIdx nsz = ParseSize(argv[2]);
+    for (int d = 0; d < 3; ++d) g.nn[d] = nsz[d];
+    const MIdx bs = ParseSize(argv[3]);
+    g.dt = std::atof(argv[4]);
+    g.rho1 = std::atof(argv[5]);
+    g.rho2 = std::atof(argv[6]);
+    const std::string iters = argv[7];
+    g.alpha = ReadRaw(argv[8], NCells());
+    g.vflux = ReadRaw(argv[9], 3 * NCells());
+    g.out = argv[10];
+    g.time_only = true;
+    std::string conf = MeshConf(nsz, bs);
+    conf += "\nset double hypre_symm_tol 0";
+    conf += "\nset int hypre_symm_maxiter " + iters;
+    conf += "\nset int hypre_symm_miniter " + iters;
+    conf += "\nset int linsolver_symm_maxnorm 0";
+    MpiWrapper mpi(&argc, &argv);
+    return RunMpiBasicString<M>(mpi, RunProj, conf);
+  }
   if (mode == "fluid") {
     if (argc != 15) return 1;
     const MIdx nsz = ParseSize(argv[2]);
@@ -652,6 +696,10 @@ int main(int argc, const char** argv) {
     std::ofstream fo(g.out + ".info");
     fo.precision(17);
     fo << g.residual << " " << g.iter << "\n";
+  } else if (mode == "cgtime") {
+    std::ofstream fo(g.out + ".time");
+    fo.precision(17);
+    fo << (g.t_solve1 - g.t_solve0) << " " << g.iter << " " << g.residual << "\n";
   } else if (mode == "bcg") {
     WriteRaw(g.out + ".ffu", g.out_flux);
   } else if (mode == "fluid") {

@@ -428,7 +428,7 @@ def test_cell_conditions():
     assert np.array_equal(e, ref)
     tol = oracle.rel_tol(ref, h, 1e-12)
     xo, io = oracle.cg_solve(n, h, ref, tol, nthreads=os.cpu_count() or 1)
-    assert io.converged
+    assert io.residual < tol
     for solver in (_lib.SOLVER_CG, _lib.SOLVER_MGPCG, _lib.SOLVER_MIXED):
         x, info = ctx.solve(_lib.default_conf(solver=solver, tol=tol, maxiter=100000))
         assert info.converged, solver
