@@ -36,24 +36,26 @@ class GpuHeights final : public curvature::Estimator<M_> {
       const Multi<FieldCell<Scal>*>& fck, const Plic& plic, M& m,
       const M&) override {
     auto sem = m.GetSem("gpu-curvature");
+    const MIdx gs = m.GetGlobalSize();
+    const size_t n = size_t(gs.prod());
     if (sem()) {
+      // the lead prepares its buffers before any block writes into them (the
+      // blocks of a rank run each stage concurrently)
       if (m.IsLead()) {
-        shared_obj_ = std::make_unique<Shared>();
+        if (!shared_obj_) shared_obj_ = std::make_unique<Shared>();
         shared_ = shared_obj_.get();
+        shared_->ctx = resident_ ? resident_() : nullptr;
+        shared_->kappa.resize(n);
+        if (!shared_->ctx) shared_->u.resize(n);
       }
       m.BcastFromLead(&shared_);
     }
-    const MIdx gs = m.GetGlobalSize();
-    const size_t n = size_t(gs.prod());
     auto flat = [&gs](MIdx w) {  // x fastest, as aphgpu expects
       return size_t(w[0]) + size_t(gs[0]) * (size_t(w[1]) + size_t(gs[1]) * w[2]);
     };
     if (sem("gather")) {
       Shared& s = *shared_;
-      s.ctx = resident_ ? resident_() : nullptr;
-      if (m.IsLead()) s.kappa.resize(n);
       if (!s.ctx) {
-        if (m.IsLead()) s.u.resize(n);
         const FieldCell<Scal>& fcu = *plic.vfcu[0];
         for (auto c : m.Cells()) s.u[flat(MIdx(m.GetIndexCells().GetMIdx(c)))] = fcu[c];
       }

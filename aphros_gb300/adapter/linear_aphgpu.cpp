@@ -39,21 +39,23 @@ class SolverGpu : public Solver<M> {
       FieldCell<Scal>& fc_sol, M& m) override {
     auto sem = m.GetSem(__func__);
     auto& ms = m.GetShared();
+    const MIdx gs = ms.GetGlobalSize();
     if (sem()) {
+      // the lead sizes its buffers before any block writes into them (the
+      // blocks of a rank run each stage concurrently)
+      if (m.IsLead()) {
+        const size_t n = size_t(gs.prod());
+        shared_->expr.resize(8 * n);
+        shared_->x0.resize(n);
+        shared_->x.resize(n);
+      }
       m.BcastFromLead(&shared_);  // every block sees the lead's buffers
     }
     Shared& s = *shared_;  // valid after the first stage
-    const MIdx gs = ms.GetGlobalSize();
     auto flat = [&gs](MIdx w) {  // x fastest, as aphgpu expects
       return size_t(w[0]) + size_t(gs[0]) * (size_t(w[1]) + size_t(gs[1]) * w[2]);
     };
     if (sem("gather")) {
-      if (m.IsLead()) {
-        const size_t n = size_t(gs.prod());
-        s.expr.resize(8 * n);
-        s.x0.resize(n);
-        s.x.resize(n);
-      }
       // blocks of one rank share memory: each writes its own cells
       for (auto c : m.CellsM()) {
         const size_t i = flat(MIdx(c));

@@ -68,16 +68,20 @@ class GpuVof final : public AdvectionSolver<M_> {
     auto sem = this->m.GetSem("iter");
     auto& m = this->m;
     if (sem()) {
+      // the lead sizes its buffers before any block writes into them (the
+      // blocks of a rank run each stage concurrently)
+      if (m.IsLead()) {
+        const size_t n = size_t(m.GetGlobalSize().prod());
+        shared_->flux.resize(3 * n);
+        shared_->src.resize(n);
+        shared_->has_src = this->fcs_ != nullptr;
+      }
       m.BcastFromLead(&shared_);
     }
     if (sem("gather")) {
       Shared& s = *shared_;
       const MIdx gs = m.GetGlobalSize();
       const size_t n = size_t(gs.prod());
-      if (m.IsLead()) {
-        s.flux.resize(3 * n);
-        s.src.resize(n);
-      }
       const auto& ff = this->fev_->GetFieldFace();
       const auto& indexf = m.GetIndexFaces();
       for (auto f : m.Faces()) {
@@ -87,7 +91,6 @@ class GpuVof final : public AdvectionSolver<M_> {
         if (w[d] == gs[d]) continue;  // the periodic image of face w[d] = 0
         s.flux[d * n + Flat(gs, w)] = ff[f];
       }
-      s.has_src = this->fcs_ != nullptr;
       if (this->fcs_) {
         for (auto c : m.Cells()) s.src[Flat(gs, MIdx(m.GetIndexCells().GetMIdx(c)))] =
             (*this->fcs_)[c];
@@ -158,18 +161,18 @@ class GpuVof final : public AdvectionSolver<M_> {
     auto sem = this->m.GetSem("upload");
     auto& m = this->m;
     if (sem()) {
+      if (m.IsLead()) {
+        const size_t n = size_t(m.GetGlobalSize().prod());
+        shared_->u.resize(n);
+        shared_->n.resize(3 * n);
+        shared_->a.resize(n);
+        shared_->mask.resize(n);
+      }
       m.BcastFromLead(&shared_);
     }
     if (sem("gather")) {
       Shared& s = *shared_;
       const MIdx gs = m.GetGlobalSize();
-      const size_t n = size_t(gs.prod());
-      if (m.IsLead()) {
-        s.u.resize(n);
-        s.n.resize(3 * n);
-        s.a.resize(n);
-        s.mask.resize(n);
-      }
       for (auto c : m.Cells()) s.u[Flat(gs, MIdx(m.GetIndexCells().GetMIdx(c)))] = fcu[c];
     }
     if (sem("init") && m.IsLead()) {

@@ -218,6 +218,11 @@ int aphgpu_create(aphgpu_ctx** out, int nx, int ny, int nz, double h, int device
   if ((rc = Alloc(ctx, &ctx->scal, 1))) return fail(rc);
   if ((rc = Alloc(ctx, &ctx->scal2, 1))) return fail(rc);
   if ((rc = Alloc(ctx, &ctx->flags, 4))) return fail(rc);
+  // flags[3]: set by a pipelined sweep whose bounded wait gave up
+  if (cudaMemset(ctx->flags, 0, 4 * sizeof(unsigned int)) != cudaSuccess) {
+    cudaGetLastError();
+    return fail(APHGPU_ERR_CUDA);
+  }
   if ((rc = Alloc(ctx, &ctx->hist, 2 * (int64_t)kHistCap))) return fail(rc);
   ctx->red.max_blocks = (int)std::max<int64_t>(TileCount(ctx->d), 4096);
   if ((rc = Alloc(ctx, &ctx->red.part, (int64_t)kMaxRedVals * ctx->red.max_blocks)))
@@ -408,6 +413,18 @@ int aphgpu_solve_resident(aphgpu_ctx* ctx, const aphgpu_conf* conf, int zero_gue
   }
   ctx->x_zero = false;
   t.Stop();
+  if (rc == APHGPU_OK && ctx->fused_mode != 0) {
+    // a pipelined sweep that gave up a wait leaves its flag (the solve has
+    // synchronized the stream already)
+    unsigned int f = 0;
+    APH_CUDA(ctx, cudaMemcpyAsync(&f, ctx->flags + 3, sizeof(f), cudaMemcpyDeviceToHost,
+                                  ctx->stream));
+    APH_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    if (f) {
+      APH_CUDA(ctx, cudaMemsetAsync(ctx->flags + 3, 0, sizeof(f), ctx->stream));
+      return SetError(ctx, APHGPU_ERR_TIMEOUT, "a fused sweep's copy did not complete");
+    }
+  }
   return rc;
 }
 
@@ -616,7 +633,11 @@ int aphgpu_set_option(aphgpu_ctx* ctx, int option, int value) {
   if (!Valid(ctx)) return APHGPU_ERR_ARG;
   switch (option) {
     case APHGPU_OPT_GRAPHS: ctx->use_graphs = value != 0; return APHGPU_OK;
-    case APHGPU_OPT_FUSED_SWEEPS: ctx->use_fused = value != 0; return APHGPU_OK;
+    case APHGPU_OPT_FUSED_SWEEPS:
+      if (value < 0 || value > 3) return SetError(ctx, APHGPU_ERR_ARG, "fused sweeps %d", value);
+      if (value != ctx->fused_mode) ctx->mg.built32 = false;  // scratch of the levels
+      ctx->fused_mode = value;
+      return APHGPU_OK;
     case APHGPU_OPT_CYCLE:
       if (value < 0 || value > 2) return SetError(ctx, APHGPU_ERR_ARG, "cycle must be 0, 1 or 2");
       ctx->mg_gamma = value;

@@ -64,6 +64,7 @@ struct BDom {
   RedBuf red;
   const double* cinv;
   int cn;
+  int csing;  // singular coarsest operator: remove the mean of its b
   int flags;  // inner solver flags (bit 0 projection, bit 1 flexible beta)
 };
 
@@ -448,8 +449,8 @@ __device__ void CtaProlong(const BLevel& F, const BLevel& C) {
   }
 }
 
-// coarsest level: x = B^{-1} (b - mean b) with the dense inverse (see
-// KCoarsestDense)
+// coarsest level: x = B^{-1} (b - mean b) with the dense inverse, the mean
+// removed only for a singular operator (see KCoarsestDense)
 __device__ void CtaDense(const BDom& D) {
   const BLevel& C = D.lv[D.nlev - 1];
   const int n = D.cn;
@@ -468,7 +469,7 @@ __device__ void CtaDense(const BDom& D) {
   if (tid == 0) {
     double s = 0;
     for (int w = 0; w < (int)(blockDim.x >> 5); ++w) s += red[w];
-    red[0] = s / n;
+    red[0] = D.csing ? s / n : 0.0;
   }
   __syncthreads();
   const double mean = red[0];
@@ -1031,6 +1032,7 @@ int BuildTables(aphgpu_batch* B, const aphgpu_conf* conf) {
     D.red = c->red;
     D.cinv = c->mg.cinv32;
     D.cn = c->mg.cn32;
+    D.csing = c->mg.csing32;
     // the constant-mode projection holds only for the singular operator
     D.flags = c->diag_explicit ? (conf->inner_flags & ~1) : conf->inner_flags;
     B->nlev_max = std::max(B->nlev_max, nl);
@@ -1496,6 +1498,7 @@ int CoarseOneSetup(aphgpu_ctx* ctx) {
   }
   D.cinv = mg.cinv32;
   D.cn = mg.cn32;
+  D.csing = mg.csing32;
   // the staged levels must fit the shared memory of one CTA
   int64_t staged = 0;
   for (int l = lc; l < L; ++l) staged += kStagedFloats * lv[l].d.cells();

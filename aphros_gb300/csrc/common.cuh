@@ -232,6 +232,10 @@ struct Multigrid {
   double* cinv64 = nullptr;
   double* cinv32 = nullptr;
   int cn64 = 0, cn32 = 0;
+  // the coarsest operator is singular (row sums zero: periodic
+  // flux-difference systems): its dense inverse is that of A + c 11^T and
+  // the coarsest solves remove the mean of the right-hand side
+  int csing64 = 1, csing32 = 1;
   // one-CTA cycle of the smallest FP32 levels: device description of the
   // levels and the first level it covers (-1: not used)
   void* cdom = nullptr;
@@ -343,7 +347,12 @@ struct aphgpu_ctx {
   } graphs[4];
   int64_t mg_epoch = 0;        // bumped whenever a hierarchy is (re)allocated
   bool use_graphs = true;
-  bool use_fused = false;  // fused out-of-place red-black sweeps (FP32 levels)
+  // fused out-of-place red-black sweeps on the FP32 levels: 0 off (two
+  // in-place half sweeps), 1 the pipelined kernel (bulk copies into shared
+  // memory) on levels of at least kPipeMinCells cells (default), 2 the
+  // pipelined kernel on every level it supports, 3 the synchronous fused
+  // kernel on every level it supports
+  int fused_mode = 1;
   bool use_half = false;   // FP16 couplings for the finest-level smoother
   int mg_gamma = 0;        // cycles of each level below the finest (1 V, 2 W, 0 auto)
   int mg_series_pct = 60;  // weight (%) of the series couplings in the coarse operators

@@ -33,6 +33,7 @@
 
 #include "common.cuh"
 #include "stencil.cuh"
+#include "sweep.cuh"
 #include "vec.cuh"
 
 namespace aphgpu {
@@ -473,8 +474,57 @@ __global__ void __launch_bounds__(256, 3) KSweepRB4(Op<float> A, const float* __
                min(kb + kz, A.d.nz), sF);
 }
 
-// levels the fused sweep handles
+// levels the synchronous fused sweep handles
 inline bool FusedOk(const Dims& d) { return VecOk(d); }
+
+// The pipelined fused sweep (sweep.cuh): levels of at least kPipeMinCells
+// cells by default; every level with nx % 4 == 0 and nx >= 16 in mode 2.
+constexpr int64_t kPipeMinCells = int64_t(1) << 21;
+inline bool PipeDims(const Dims& d) { return (d.nx % 4) == 0 && d.nx >= 16; }
+inline bool PipeEligible(const aphgpu_ctx* ctx, const Dims& d) {
+  if (!PipeDims(d)) return false;
+  return ctx->fused_mode == 2 || (ctx->fused_mode == 1 && d.cells() >= kPipeMinCells);
+}
+// Tiles of the pipelined sweep: columns of at most kPipeCols (balanced),
+// bands of at most kPipeRows rows (balanced), and z segments so that the
+// items fill the SMs in one wave (at least 8 planes a segment).
+inline PipeTiling PipeTiles(const Dims& d, int sms) {
+  PipeTiling T;
+  T.xtiles = (d.nx + kPipeCols - 1) / kPipeCols;
+  T.w = 4 * ((d.nx / 4 + T.xtiles - 1) / T.xtiles);
+  T.bands = (d.ny + kPipeRows - 1) / kPipeRows;
+  T.rows = (d.ny + T.bands - 1) / T.bands;
+  T.bands = (d.ny + T.rows - 1) / T.rows;
+  const int tiles = T.xtiles * T.bands;
+  T.zsegs = std::max(1, std::min(d.nz / 8, sms / std::max(tiles, 1)));
+  return T;
+}
+inline int SmCount(aphgpu_ctx* ctx) {
+  int sms = 0;
+  if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, ctx->device) != cudaSuccess ||
+      sms < 1) {
+    cudaGetLastError();
+    sms = 152;
+  }
+  return sms;
+}
+// one pipelined sweep in -> out (first colour c0)
+inline int LaunchPipe(aphgpu_ctx* ctx, const Op<float>& A, const float* b, const float* in,
+                      float* out, int c0, int zero_init, const SolveScalars* s,
+                      cudaStream_t st) {
+  static bool attr_set[64] = {};
+  const int dev = ctx->device;
+  if (dev >= 0 && dev < 64 && !attr_set[dev]) {
+    APH_CUDA(ctx, cudaFuncSetAttribute(KSweepPipe, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                       kPipeSmemBytes));
+    attr_set[dev] = true;
+  }
+  const PipeTiling T = PipeTiles(A.d, SmCount(ctx));
+  const int items = T.xtiles * T.bands * T.zsegs;
+  KSweepPipe<<<items, kPipeThreads, kPipeSmemBytes, st>>>(A, b, in, out, c0, zero_init, s, T,
+                                                          (int*)ctx->flags + 3);
+  return APHGPU_OK;
+}
 inline dim3 SweepGrid(const Dims& d) {
   const int nq = d.nx / 4;
   const int kz = VecZ(d);
@@ -510,6 +560,25 @@ __global__ void KProlong4(Dims d, float* x, Dims dc, const float* __restrict__ x
   const int kb = blockIdx.z * kz;
   Prolong4Body(d, x, dc, xc, blockIdx.x * 32 + threadIdx.x, blockIdx.y * 8 + threadIdx.y, kb,
                min(kb + kz, d.nz));
+}
+
+// x_out = x + x_coarse(parent), the out-of-place KProlong4 (same addition)
+__global__ void KProlong4To(Dims d, const float* __restrict__ x, float* xo, Dims dc,
+                            const float* __restrict__ xc, const SolveScalars* s, int kz) {
+  if (s && s->done) return;
+  const int q = blockIdx.x * 32 + threadIdx.x, j = blockIdx.y * 8 + threadIdx.y;
+  const int kb = blockIdx.z * kz, ke = min(kb + kz, d.nz);
+  if (q >= d.nx / 4 || j >= d.ny) return;
+  for (int k = kb; k < ke; ++k) {
+    const int64_t c = d.idx(4 * q, j, k);
+    const float2 e = *reinterpret_cast<const float2*>(xc + dc.idx(2 * q, j >> 1, k >> 1));
+    float4 v = *reinterpret_cast<const float4*>(x + c);
+    v.x += e.x;
+    v.y += e.x;
+    v.z += e.y;
+    v.w += e.y;
+    *reinterpret_cast<float4*>(xo + c) = v;
+  }
 }
 
 // x += alpha p, r -= alpha (ap - mean(ap)), reductions and stopping test of
@@ -741,8 +810,11 @@ __device__ double CoarseFace(const Op<T>& A, int q, int I, int J, int K, double 
 
 // Coarse operator of constant prolongation and summed restriction, pass 1:
 // the three minus-face couplings of each coarse cell (CoarseFace) and, in
-// `diag`, half the summed diagonal shifts of its 8 children (shift =
-// diagonal + sum of the couplings; zero for flux-difference systems).
+// `diag`, the summed diagonal shifts of its 8 children (shift = diagonal +
+// sum of the couplings; zero for flux-difference systems).  The shifts
+// (mass terms of diffusion systems, given-pressure cells) take their
+// Galerkin value, the sum: constant prolongation represents them exactly,
+// unlike the couplings, whose Galerkin value is halved (CoarseFace).
 template <class T, class TC>
 __global__ void KCoarsenFaces(Op<T> A, Dims dc, TC* w0, TC* w1, TC* w2, TC* diag,
                               double series) {
@@ -767,11 +839,11 @@ __global__ void KCoarsenFaces(Op<T> A, Dims dc, TC* w0, TC* w1, TC* w2, TC* diag
     w0[C] = (TC)CoarseFace(A, 0, I, J, K, series);
     w1[C] = (TC)CoarseFace(A, 1, I, J, K, series);
     w2[C] = (TC)CoarseFace(A, 2, I, J, K, series);
-    diag[C] = (TC)(0.5 * shift);
+    diag[C] = (TC)shift;
   }
 }
 
-// Pass 2: diagonal = half shift (from pass 1) minus the sum of the six
+// Pass 2: diagonal = shift (from pass 1) minus the sum of the six
 // stored coarse couplings (so the row sums of the stored operator are the
 // shifts: the constant null space stays exact), and its inverse.
 template <class TC>
@@ -809,7 +881,7 @@ __global__ void KConvert(int64_t n, const TS* __restrict__ a, TD* out, double sc
 template <class TC>
 __global__ void __launch_bounds__(1024) KCoarsestCG(
     Op<TC> A, const TC* __restrict__ bc, TC* xc, double* r, double* p,
-    double* ap, double* x, const SolveScalars* s) {
+    double* ap, double* x, const SolveScalars* s, int singular) {
   if (s && s->done) return;
   const Dims& d = A.d;
   const int n = (int)d.cells();
@@ -832,7 +904,7 @@ __global__ void __launch_bounds__(1024) KCoarsestCG(
   };
   double sb = 0;
   for (int c = tid; c < n; c += blockDim.x) sb += (double)bc[c];
-  const double mean = bsum(sb) / n;
+  const double mean = singular ? bsum(sb) / n : 0.0;
   double rr = 0;
   for (int c = tid; c < n; c += blockDim.x) {
     const double v = (double)bc[c] - mean;
@@ -885,11 +957,12 @@ __global__ void __launch_bounds__(1024) KCoarsestCG(
 
 // Coarsest level, direct: x = B^{-1} (b - mean(b)) with the precomputed
 // dense inverse of B = A + 11^T c (c > 0), which equals the solution of the
-// periodic (singular) A x = b - mean(b) with zero mean.  FP64 throughout.
+// periodic (singular) A x = b - mean(b) with zero mean; for a non-singular
+// A (diagonal shifts) B = A and x = A^{-1} b.  FP64 throughout.
 template <class TC>
 __global__ void __launch_bounds__(1024) KCoarsestDense(int n, const double* __restrict__ binv,
                                                        const TC* __restrict__ bc, TC* xc,
-                                                       const SolveScalars* s) {
+                                                       const SolveScalars* s, int singular) {
   if (s && s->done) return;
   __shared__ double sb[kDenseMax];
   __shared__ double red[32];
@@ -906,7 +979,7 @@ __global__ void __launch_bounds__(1024) KCoarsestDense(int n, const double* __re
   if (tid == 0) {
     double t = 0;
     for (int w = 0; w < (int)(blockDim.x >> 5); ++w) t += red[w];
-    red[0] = t / n;
+    red[0] = singular ? t / n : 0.0;
   }
   __syncthreads();
   const double mean = red[0];
@@ -1136,7 +1209,8 @@ int EnsureCoarsestScratch(aphgpu_ctx* ctx, int64_t n) {
 // Dense inverse of the coarsest operator B = A + 11^T c, c = mean(diag)/n,
 // by Cholesky on the host (n <= kDenseMax cells; built once per system).
 template <class T>
-int BuildCoarsestInverse(aphgpu_ctx* ctx, const Level<T>& L, double** dinv, int* dn) {
+int BuildCoarsestInverse(aphgpu_ctx* ctx, const Level<T>& L, double** dinv, int* dn,
+                         int* singular) {
   const Dims d = L.d;
   const int n = (int)d.cells();
   if (n > kDenseMax) {
@@ -1153,7 +1227,7 @@ int BuildCoarsestInverse(aphgpu_ctx* ctx, const Level<T>& L, double** dinv, int*
   APH_CUDA(ctx, cudaStreamSynchronize(st));
   std::vector<double> B((size_t)n * n, 0.0);
   auto at = [&](int r, int c) -> double& { return B[(size_t)r * n + c]; };
-  double dsum = 0;
+  double dsum = 0, ssum = 0;  // diagonals, row sums (the shifts)
   for (int k = 0; k < d.nz; ++k)
     for (int j = 0; j < d.ny; ++j)
       for (int i = 0; i < d.nx; ++i) {
@@ -1167,16 +1241,21 @@ int BuildCoarsestInverse(aphgpu_ctx* ctx, const Level<T>& L, double** dinv, int*
         const double e[6] = {(double)w0[c], (double)w0[xp], (double)w1[c],
                              (double)w1[yp], (double)w2[c], (double)w2[zp]};
         const int nb[6] = {xm, xp, ym, yp, zm, zp};
-        double diag = 0;
+        double diag = 0, rowsum = 0;
         for (int q = 0; q < 6; ++q) {
           at(c, nb[q]) += e[q];
           diag -= e[q];
+          rowsum += e[q];
         }
         if (L.has_diag) diag = (double)dg[c];
         at(c, c) += diag;
         dsum += diag;
+        ssum += diag + rowsum;
       }
-  const double cshift = dsum / n / n;
+  // singular (periodic flux-difference operator: the row sums vanish up to
+  // the rounding of the coarse operators): invert A + c 11^T instead
+  *singular = std::fabs(ssum) <= 1e-5 * std::fabs(dsum) ? 1 : 0;
+  const double cshift = *singular ? dsum / n / n : 0.0;
   for (auto& v : B) v += cshift;
   // Cholesky B = L L^T, then B^{-1} column by column
   std::vector<double> Lm((size_t)n * n, 0.0);
@@ -1287,7 +1366,8 @@ int BuildHierarchy<double>(aphgpu_ctx* ctx, std::vector<Level<double>>& lv,
     APH_LAUNCHED(ctx);
   }
   APH_TRY(EnsureCoarsestScratch(ctx, lv.back().d.cells()));
-  APH_TRY(BuildCoarsestInverse(ctx, lv.back(), &ctx->mg.cinv64, &ctx->mg.cn64));
+  APH_TRY(BuildCoarsestInverse(ctx, lv.back(), &ctx->mg.cinv64, &ctx->mg.cn64,
+                               &ctx->mg.csing64));
   return APHGPU_OK;
 }
 
@@ -1306,7 +1386,8 @@ int BuildHierarchy<float>(aphgpu_ctx* ctx, std::vector<Level<float>>& lv,
       lv[l].d = dims[l];
       APH_TRY(AllocLevel(ctx, lv[l], true, l > 0));
       // scratch of the out-of-place fused sweeps (when enabled)
-      if (ctx->use_fused && FusedOk(dims[l])) APH_TRY(Alloc(ctx, &lv[l].r, dims[l].cells()));
+      if (PipeEligible(ctx, dims[l]) || (ctx->fused_mode == 3 && FusedOk(dims[l])))
+        APH_TRY(Alloc(ctx, &lv[l].r, dims[l].cells()));
       lv[l].has_diag = true;
     }
   }
@@ -1347,7 +1428,8 @@ int BuildHierarchy<float>(aphgpu_ctx* ctx, std::vector<Level<float>>& lv,
     APH_LAUNCHED(ctx);
   }
   APH_TRY(EnsureCoarsestScratch(ctx, lv.back().d.cells()));
-  APH_TRY(BuildCoarsestInverse(ctx, lv.back(), &ctx->mg.cinv32, &ctx->mg.cn32));
+  APH_TRY(BuildCoarsestInverse(ctx, lv.back(), &ctx->mg.cinv32, &ctx->mg.cn32,
+                               &ctx->mg.csing32));
   return CoarseOneSetup(ctx);
 }
 
@@ -1375,30 +1457,47 @@ void LaunchSmooth<float>(aphgpu_ctx* ctx, const Level<float>& f, const Op<float>
   }
 }
 // n red-black sweeps on level f (first colour c0; zero_first: the first
-// sweep starts from a zero guess) with the fused out-of-place kernel,
+// sweep starts from a zero guess) with a fused out-of-place kernel,
 // alternating between f.x and the level's scratch f.r so that the result
-// ends in f.x.  Returns kNotFused (nothing launched) where the level or the
-// context does not allow it, else APHGPU_OK or the launch error.
+// ends in f.x; in_r: the current values are in f.r (the prolongation wrote
+// them there), not in f.x.  Returns kNotFused (nothing launched) where the
+// level or the context does not allow it, else APHGPU_OK or the launch
+// error.
 constexpr int kNotFused = -1;
 template <class T>
-int FusedSweeps(aphgpu_ctx*, Level<T>&, const Op<T>&, int, int, bool, const SolveScalars*) {
+bool PipeUse(const aphgpu_ctx*, const Level<T>&, const Op<T>&) {
+  return false;
+}
+template <>
+bool PipeUse<float>(const aphgpu_ctx* ctx, const Level<float>& f, const Op<float>& A) {
+  return f.r && !A.diag && PipeEligible(ctx, f.d);
+}
+template <class T>
+int FusedSweeps(aphgpu_ctx*, Level<T>&, const Op<T>&, int, int, bool, const SolveScalars*,
+                bool) {
   return kNotFused;
 }
 template <>
 int FusedSweeps<float>(aphgpu_ctx* ctx, Level<float>& f, const Op<float>& A, int n, int c0,
-                       bool zero_first, const SolveScalars* s) {
-  if (!ctx->use_fused || n < 1 || !f.r || !FusedOk(f.d)) return kNotFused;
+                       bool zero_first, const SolveScalars* s, bool in_r) {
+  const bool pipe = PipeUse<float>(ctx, f, A);
+  const bool sync = !pipe && ctx->fused_mode == 3 && f.r && FusedOk(f.d);
+  if (n < 1 || !(pipe || sync)) return kNotFused;
   const dim3 g = SweepGrid(f.d);
   const int kz = VecZ(f.d);
-  float* in = f.x;
+  float* in = in_r ? f.r : f.x;
   // outputs: the last sweep writes f.x; a zero-guess first sweep reads
-  // nothing, so it may write f.x too
+  // nothing, so it may write its input buffer too
   for (int k = 0; k < n; ++k) {
     const bool last_to_x = ((n - 1 - k) % 2) == 0;
     float* out = last_to_x ? f.x : f.r;
-    if (out == in && !(k == 0 && zero_first)) out = f.r;  // never in place
-    KSweepRB4<<<g, TileBlock(), 0, ctx->stream>>>(A, f.b, in, out, c0, (k == 0 && zero_first),
-                                                  s, kz);
+    if (out == in && !(k == 0 && zero_first)) out = (in == f.x) ? f.r : f.x;
+    const int zero = (k == 0 && zero_first) ? 1 : 0;
+    if (pipe) {
+      APH_TRY(LaunchPipe(ctx, A, f.b, in, out, c0, zero, s, ctx->stream));
+    } else {
+      KSweepRB4<<<g, TileBlock(), 0, ctx->stream>>>(A, f.b, in, out, c0, zero, s, kz);
+    }
     APH_LAUNCHED(ctx);
     in = out;
   }
@@ -1412,6 +1511,14 @@ template <class T>
 void LaunchProlong(aphgpu_ctx* ctx, const Level<T>& f, const Level<T>& c,
                    const SolveScalars* s) {
   KProlong<T, T><<<TileGrid(f.d), TileBlock(), 0, ctx->stream>>>(f.d, f.x, c.d, c.x, s);
+}
+// f.r = f.x + the coarse correction (vectorized levels only): the
+// prolongation of KProlong4 written out of place, for an odd number of
+// fused post-sweeps that then end in f.x without a copy
+void LaunchProlongToR(aphgpu_ctx* ctx, const Level<float>& f, const Level<float>& c,
+                      const SolveScalars* s) {
+  KProlong4To<<<VecGrid(f.d), TileBlock(), 0, ctx->stream>>>(f.d, f.x, f.r, c.d, c.x, s,
+                                                             VecZ(f.d));
 }
 template <>
 void LaunchProlong<float>(aphgpu_ctx* ctx, const Level<float>& f, const Level<float>& c,
@@ -1569,10 +1676,13 @@ int CycleLevel(aphgpu_ctx* ctx, std::vector<Level<T>>& lv, int l, bool first, in
     const bool is64 = sizeof(T) == 8;
     const int dn = is64 ? mg.cn64 : mg.cn32;
     const double* dinv = is64 ? mg.cinv64 : mg.cinv32;
+    const int sing = is64 ? mg.csing64 : mg.csing32;
     if (dn == (int)c.d.cells() && dinv) {
-      KCoarsestDense<T><<<1, dn < 1024 ? ((dn + 31) / 32) * 32 : 1024, 0, st>>>(dn, dinv, c.b, c.x, s);
+      KCoarsestDense<T><<<1, dn < 1024 ? ((dn + 31) / 32) * 32 : 1024, 0, st>>>(dn, dinv, c.b,
+                                                                             c.x, s, sing);
     } else {
-      KCoarsestCG<T><<<1, 1024, 0, st>>>(A, c.b, c.x, mg.cr, mg.cp, mg.cap, mg.cx, s);
+      KCoarsestCG<T><<<1, 1024, 0, st>>>(A, c.b, c.x, mg.cr, mg.cp, mg.cap, mg.cx, s,
+                                         ctx->diag_explicit ? 0 : 1);
     }
     APH_LAUNCHED(ctx);
     return APHGPU_OK;
@@ -1580,7 +1690,7 @@ int CycleLevel(aphgpu_ctx* ctx, std::vector<Level<T>>& lv, int l, bool first, in
   Level<T>& f = lv[l];
   const Op<T> A = MakeOp(f);
   const int np = LevelSweeps(ctx, pre, l), nq = LevelSweeps(ctx, post, l);
-  const int fused = np > 0 ? FusedSweeps<T>(ctx, f, A, np, 0, first, s) : kNotFused;
+  const int fused = np > 0 ? FusedSweeps<T>(ctx, f, A, np, 0, first, s, false) : kNotFused;
   if (fused != kNotFused) APH_TRY(fused);
   for (int sw = 0; fused == kNotFused && sw < np; ++sw) {
     LaunchSmooth<T>(ctx, f, A, 0, first && sw == 0, s);
@@ -1598,9 +1708,16 @@ int CycleLevel(aphgpu_ctx* ctx, std::vector<Level<T>>& lv, int l, bool first, in
   APH_LAUNCHED(ctx);
   const int gamma = l == 0 ? 1 : CycleGamma(ctx);
   for (int g = 0; g < gamma; ++g) APH_TRY(CycleLevel<T>(ctx, lv, l + 1, g == 0, pre, post, s));
-  LaunchProlong<T>(ctx, f, lv[l + 1], s);
+  // an odd number of pipelined post-sweeps starts from f.r, written by the
+  // prolongation, and ends in f.x without a copy
+  bool in_r = false;
+  if constexpr (std::is_same<T, float>::value) {
+    in_r = nq % 2 == 1 && PipeUse<float>(ctx, f, A);
+    if (in_r) LaunchProlongToR(ctx, f, lv[l + 1], s);
+  }
+  if (!in_r) LaunchProlong<T>(ctx, f, lv[l + 1], s);
   APH_LAUNCHED(ctx);
-  const int fused2 = nq > 0 ? FusedSweeps<T>(ctx, f, A, nq, 1, false, s) : kNotFused;
+  const int fused2 = nq > 0 ? FusedSweeps<T>(ctx, f, A, nq, 1, false, s, in_r) : kNotFused;
   if (fused2 != kNotFused) APH_TRY(fused2);
   for (int sw = 0; fused2 == kNotFused && sw < nq; ++sw) {
     LaunchSmooth<T>(ctx, f, A, 1, 0, s);
@@ -1679,7 +1796,7 @@ int Pcg(aphgpu_ctx* ctx, const Op<T>& A, Precond precond, T* x, T* r, T* p,
     key = Mix(key, (uint64_t)(conf->mg_pre * 1000 + conf->mg_post));
     key = Mix(key, (uint64_t)check_every);
     key = Mix(key, (uint64_t)sizeof(T));
-    key = Mix(key, (uint64_t)(ctx->use_fused ? 1 : 0));
+    key = Mix(key, (uint64_t)ctx->fused_mode);
     key = Mix(key, (uint64_t)CycleGamma(ctx));
     key = Mix(key, (uint64_t)SweepGrowth(ctx));
     key = Mix(key, (uint64_t)(ctx->use_cta_coarse ? 1 + ctx->mg.clc : 0));
@@ -2092,9 +2209,13 @@ int TimeSolverKernel(aphgpu_ctx* ctx, int kernel, int reps, double* ms,
       float* xo = f.r;
       const dim3 g = SweepGrid(d);
       const int kz = VecZ(d);
-      launch = [=]() {
-        KSweepRB4<<<g, TileBlock(), 0, st>>>(A, bb, x, xo, 0, 0, nullptr, kz);
-      };
+      if (PipeUse<float>(ctx, f, A)) {
+        launch = [=]() { LaunchPipe(ctx, A, bb, x, xo, 0, 0, nullptr, st); };
+      } else {
+        launch = [=]() {
+          KSweepRB4<<<g, TileBlock(), 0, st>>>(A, bb, x, xo, 0, 0, nullptr, kz);
+        };
+      }
       // couplings 12, b 4, x read 4, x written 4 (once each per full sweep)
       b = N * 24;
       break;

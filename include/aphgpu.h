@@ -382,12 +382,18 @@ int aphgpu_batch_last_ms(const aphgpu_batch* batch, double* ms, int64_t* launche
  * exist to measure and check the variants):
  *   APHGPU_OPT_GRAPHS        1 (default): replay batches of PCG iterations
  *                            from CUDA graphs; 0: launch every kernel
- *   APHGPU_OPT_FUSED_SWEEPS  1: FP32 multigrid levels of at least 8 cells in
- *                            x (a multiple of 4) smooth with fused
- *                            out-of-place red-black sweeps (half the DRAM
- *                            traffic, but latency-bound and slower on GB300;
- *                            set before the first solve); 0 (default): two
- *                            in-place half sweeps per sweep
+ *   APHGPU_OPT_FUSED_SWEEPS  fused out-of-place red-black sweeps (both
+ *                            colours in one pass: half the DRAM traffic of
+ *                            two half sweeps) on the FP32 levels: 1
+ *                            (default) the pipelined kernel, fed by bulk
+ *                            copies into shared memory, on levels of at
+ *                            least 2^21 cells with nx a multiple of 4 and
+ *                            no stored diagonal; 2 the pipelined kernel on
+ *                            every such level whatever its size; 3 the
+ *                            synchronous fused kernel (latency-bound) on
+ *                            every level with nx a multiple of 4, nx >= 8;
+ *                            0 two in-place half sweeps everywhere.  Other
+ *                            levels take the half sweeps
  *   APHGPU_OPT_HALF_COUPLINGS 1: the smoother and the restriction of the
  *                            finest FP32 level read an FP16 copy of the
  *                            couplings scaled by a power of two (the PCG

@@ -231,11 +231,14 @@ def test_full_size_property_256():
 
 
 @pytest.mark.parametrize("solver", [_lib.SOLVER_MIXED, _lib.SOLVER_MGPCG32])
-@pytest.mark.parametrize("shape", [(64, 64, 64), (96, 48, 40), (40, 24, 32)])
+@pytest.mark.parametrize("shape", [(64, 64, 64), (96, 48, 40), (40, 24, 32), (128, 128, 128)])
 def test_fused_sweeps_bit_identical(solver, shape):
-    """The fused out-of-place red-black sweep computes every value with the
-    operations of the two in-place half sweeps: whole solves agree bit for
-    bit with and without it (and with and without CUDA graphs)."""
+    """The fused out-of-place red-black sweeps -- the pipelined kernel fed
+    by bulk copies (mode 2: on every level with nx % 4 == 0 and nx >= 16;
+    mode 1, the default: on levels of at least 2^21 cells) and the
+    synchronous kernel (mode 3) -- compute every value with the operations
+    of the two in-place half sweeps (mode 0): whole solves agree bit for bit
+    (with and without CUDA graphs)."""
     nx, ny, nz = shape
     h = 1.0 / nx
     c, r = workload.place_spheres(11, 3, 0.1, 0.2, gap=0.02)
@@ -252,7 +255,7 @@ def test_fused_sweeps_bit_identical(solver, shape):
     _, bn = ctx.residual_norms()
     conf = _lib.default_conf(solver=solver, tol=1e-10 * bn / math.sqrt(h ** 3), maxiter=200)
     out = {}
-    for fused in (1, 0):
+    for fused in (2, 1, 3, 0):
         for graphs in (1, 0):
             ctx.set_option(_lib.OPT_FUSED_SWEEPS, fused)
             ctx.set_option(_lib.OPT_GRAPHS, graphs)
