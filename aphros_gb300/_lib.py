@@ -105,6 +105,14 @@ def lib():
     L.aphgpu_vof_init.argtypes = [_P, _P, _D]
     L.aphgpu_vof_step.argtypes = [_P, _P, _D]
     L.aphgpu_vof_get.argtypes = [_P, _P, _P, _P, _P]
+    L.aphgpu_fluid_init.argtypes = [_P, _P, _D, _D, _D, _D, _P]
+    L.aphgpu_fluid_init.restype = _I
+    L.aphgpu_fluid_step.argtypes = [_P, _D, ctypes.POINTER(Conf), ctypes.POINTER(Info)]
+    L.aphgpu_fluid_step.restype = _I
+    L.aphgpu_fluid_get.argtypes = [_P, _P, _P, _P]
+    L.aphgpu_fluid_get.restype = _I
+    L.aphgpu_bcg_faces.argtypes = [_P, _P, _P, _P, _D, _P]
+    L.aphgpu_bcg_faces.restype = _I
     L.aphgpu_vof_set_source.argtypes = [_P, _P]
     L.aphgpu_vof_set_source.restype = _I
     L.aphgpu_apply_cell_cond.argtypes = [_P, ctypes.c_int64, _P, _P]
@@ -300,6 +308,32 @@ class Context:
     def vof_step(self, vflux, dt):
         v = None if vflux is None else self._f64(vflux, 3 * self.N)
         self._check(self._L.aphgpu_vof_step(self._p, ptr(v), dt))
+
+    # ---- projection fluid step ----
+    def fluid_init(self, alpha, rho1, rho2, mu1, mu2, vel):
+        a = None if alpha is None else self._f64(alpha, self.N)
+        v = self._f64(vel, 3 * self.N)
+        self._check(self._L.aphgpu_fluid_init(self._p, ptr(a), rho1, rho2, mu1, mu2, ptr(v)))
+
+    def fluid_step(self, dt, conf):
+        info = Info()
+        self._check(self._L.aphgpu_fluid_step(self._p, dt, ctypes.byref(conf),
+                                              ctypes.byref(info)))
+        return info
+
+    def fluid_get(self):
+        vel = np.empty(3 * self.N)
+        p = np.empty(self.N)
+        flux = np.empty(3 * self.N)
+        self._check(self._L.aphgpu_fluid_get(self._p, ptr(vel), ptr(p), ptr(flux)))
+        return vel, p, flux
+
+    def bcg_faces(self, u, vflux, src, dt):
+        out = np.empty(3 * self.N)
+        self._check(self._L.aphgpu_bcg_faces(self._p, ptr(self._f64(u, self.N)),
+                                             ptr(self._f64(vflux, 3 * self.N)),
+                                             ptr(self._f64(src, self.N)), dt, ptr(out)))
+        return out
 
     def vof_set_source(self, src):
         """Volume source of the following VOF steps (None: none)."""

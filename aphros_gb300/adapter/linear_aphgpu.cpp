@@ -51,11 +51,12 @@ class SolverGpu : public Solver<M> {
       }
       m.BcastFromLead(&shared_);  // every block sees the lead's buffers
     }
-    Shared& s = *shared_;  // valid after the first stage
+    // shared_ is valid on every block after the first stage (broadcast)
     auto flat = [&gs](MIdx w) {  // x fastest, as aphgpu expects
       return size_t(w[0]) + size_t(gs[0]) * (size_t(w[1]) + size_t(gs[1]) * w[2]);
     };
     if (sem("gather")) {
+      Shared& s = *shared_;
       // blocks of one rank share memory: each writes its own cells
       for (auto c : m.CellsM()) {
         const size_t i = flat(MIdx(c));
@@ -64,6 +65,7 @@ class SolverGpu : public Solver<M> {
       }
     }
     if (sem("solve") && m.IsLead()) {
+      Shared& s = *shared_;
       fassert(m.flags.is_periodic[0] && m.flags.is_periodic[1] &&
               m.flags.is_periodic[2], "gpu solver: periodic domains only");
       size_t ncells = 0;  // the rank must own the whole domain
@@ -106,10 +108,12 @@ class SolverGpu : public Solver<M> {
       s.info.iter = info.iter;
     }
     if (sem("scatter")) {
+      const Shared& s = *shared_;
       for (auto c : m.CellsM()) fc_sol[c] = s.x[flat(MIdx(c))];
       m.Comm(&fc_sol, M::CommStencil::direct_one);
     }
-    return s.info;
+    // the result of the last stage (the value of earlier stages is unused)
+    return shared_ ? shared_->info : Info{};
   }
 
  private:

@@ -41,6 +41,7 @@ CU_UNITS = {
     "batch.cu": [],
     "dump.cu": [],
     "label.cu": [],
+    "fluid.cu": ["-fmad=false"],
 }
 
 

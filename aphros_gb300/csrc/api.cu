@@ -217,9 +217,9 @@ int aphgpu_create(aphgpu_ctx** out, int nx, int ny, int nz, double h, int device
   if ((rc = Alloc(ctx, &ctx->x, N))) return fail(rc);
   if ((rc = Alloc(ctx, &ctx->scal, 1))) return fail(rc);
   if ((rc = Alloc(ctx, &ctx->scal2, 1))) return fail(rc);
-  if ((rc = Alloc(ctx, &ctx->flags, 4))) return fail(rc);
-  // flags[3]: set by a pipelined sweep whose bounded wait gave up
-  if (cudaMemset(ctx->flags, 0, 4 * sizeof(unsigned int)) != cudaSuccess) {
+  if ((rc = Alloc(ctx, &ctx->flags, 5))) return fail(rc);
+  // flags[4]: set by a pipelined sweep whose bounded wait gave up
+  if (cudaMemset(ctx->flags, 0, 5 * sizeof(unsigned int)) != cudaSuccess) {
     cudaGetLastError();
     return fail(APHGPU_ERR_CUDA);
   }
@@ -417,11 +417,11 @@ int aphgpu_solve_resident(aphgpu_ctx* ctx, const aphgpu_conf* conf, int zero_gue
     // a pipelined sweep that gave up a wait leaves its flag (the solve has
     // synchronized the stream already)
     unsigned int f = 0;
-    APH_CUDA(ctx, cudaMemcpyAsync(&f, ctx->flags + 3, sizeof(f), cudaMemcpyDeviceToHost,
+    APH_CUDA(ctx, cudaMemcpyAsync(&f, ctx->flags + 4, sizeof(f), cudaMemcpyDeviceToHost,
                                   ctx->stream));
     APH_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
     if (f) {
-      APH_CUDA(ctx, cudaMemsetAsync(ctx->flags + 3, 0, sizeof(f), ctx->stream));
+      APH_CUDA(ctx, cudaMemsetAsync(ctx->flags + 4, 0, sizeof(f), ctx->stream));
       return SetError(ctx, APHGPU_ERR_TIMEOUT, "a fused sweep's copy did not complete");
     }
   }
@@ -548,6 +548,88 @@ int aphgpu_vof_step(aphgpu_ctx* ctx, const double* vflux, double dt) {
   APH_TRY(VofStepDevice(ctx, d_vf, dt));
   t.Stop();
   return APHGPU_OK;
+}
+
+int aphgpu_fluid_init(aphgpu_ctx* ctx, const double* alpha, double rho1, double rho2,
+                      double mu1, double mu2, const double* vel) {
+  if (!Valid(ctx) || !vel) return APHGPU_ERR_ARG;
+  if (!alpha && !ctx->vof_ready)
+    return SetError(ctx, APHGPU_ERR_STATE, "alpha is NULL and no resident volume fraction");
+  APH_TRY(SetDevice(ctx));
+  APH_TRY(EnsureSolverVectors(ctx));
+  APH_TRY(EnsureVof(ctx));
+  const int64_t N = ctx->N;
+  auto& F = ctx->fluid;
+  if (!F.vel) {
+    for (double** p : {&F.vel, &F.vi, &F.flux, &F.ffv, &F.ffu, &F.acc, &F.guess})
+      APH_TRY(Alloc(ctx, p, 3 * N));
+    for (double** p : {&F.mu, &F.p, &F.ppred}) APH_TRY(Alloc(ctx, p, N));
+    APH_TRY(Alloc(ctx, &F.e8, 8 * N));
+  }
+  if (!ctx->alpha_proj) APH_TRY(Alloc(ctx, &ctx->alpha_proj, N));
+  if (alpha) {
+    APH_TRY(H2D(ctx, ctx->alpha_proj, alpha, sizeof(double) * N));
+  } else {
+    APH_CUDA(ctx, cudaMemcpyAsync(ctx->alpha_proj, ctx->u, sizeof(double) * N,
+                                  cudaMemcpyDeviceToDevice, ctx->stream));
+  }
+  F.follow_vof = alpha == nullptr;
+  APH_TRY(H2D(ctx, F.vel, vel, sizeof(double) * 3 * N));
+  APH_TRY(FluidInitDevice(ctx, rho1, rho2, mu1, mu2));
+  ctx->proj_rho[0] = rho1;
+  ctx->proj_rho[1] = rho2;
+  F.ready = true;
+  return aphgpu_sync(ctx);
+}
+
+int aphgpu_fluid_step(aphgpu_ctx* ctx, double dt, const aphgpu_conf* conf, aphgpu_info* info) {
+  if (!Valid(ctx) || !conf || !info || !(dt > 0)) return APHGPU_ERR_ARG;
+  if (!ctx->fluid.ready) return SetError(ctx, APHGPU_ERR_STATE, "fluid not initialised");
+  if (ctx->fluid.follow_vof && !ctx->vof_ready)
+    return SetError(ctx, APHGPU_ERR_STATE, "no resident volume fraction");
+  APH_TRY(SetDevice(ctx));
+  double* d_res = nullptr;
+  APH_TRY(FaceScratch(ctx, &d_res));
+  Timer t(ctx);
+  const int rc = FluidStepDevice(ctx, dt, conf, info, d_res);
+  t.Stop();
+  return rc;
+}
+
+int aphgpu_fluid_get(aphgpu_ctx* ctx, double* vel, double* p, double* flux) {
+  if (!Valid(ctx)) return APHGPU_ERR_ARG;
+  if (!ctx->fluid.ready) return SetError(ctx, APHGPU_ERR_STATE, "fluid not initialised");
+  APH_TRY(SetDevice(ctx));
+  const int64_t N = ctx->N;
+  if (vel) APH_TRY(D2H(ctx, vel, ctx->fluid.vel, sizeof(double) * 3 * N));
+  if (p) APH_TRY(D2H(ctx, p, ctx->fluid.p, sizeof(double) * N));
+  if (flux) APH_TRY(D2H(ctx, flux, ctx->fluid.flux, sizeof(double) * 3 * N));
+  return APHGPU_OK;
+}
+
+int aphgpu_bcg_faces(aphgpu_ctx* ctx, const double* u, const double* vflux, const double* src,
+                     double dt, double* out) {
+  if (!Valid(ctx) || !u || !vflux || !src || !out) return APHGPU_ERR_ARG;
+  APH_TRY(SetDevice(ctx));
+  const int64_t N = ctx->N;
+  // inputs and output staged in one temporary block of 8N doubles
+  double* d = nullptr;
+  APH_TRY(Alloc(ctx, &d, 8 * N));
+  int rc = H2D(ctx, d, u, sizeof(double) * N);
+  if (rc == APHGPU_OK) rc = H2D(ctx, d + N, vflux, sizeof(double) * 3 * N);
+  if (rc == APHGPU_OK) rc = H2D(ctx, d + 4 * N, src, sizeof(double) * N);
+  if (rc == APHGPU_OK) rc = BcgFacesDevice(ctx, d, d + N, d + 4 * N, dt, d + 5 * N);
+  if (rc == APHGPU_OK) rc = D2H(ctx, out, d + 5 * N, sizeof(double) * 3 * N);
+  cudaStreamSynchronize(ctx->stream);
+  for (size_t i = 0; i < ctx->allocs.size(); ++i) {
+    if (ctx->allocs[i] == d) {
+      cudaFree(d);
+      ctx->allocs.erase(ctx->allocs.begin() + i);
+      ctx->bytes -= (int64_t)sizeof(double) * 8 * N;
+      break;
+    }
+  }
+  return rc;
 }
 
 int aphgpu_vof_set_source(aphgpu_ctx* ctx, const double* src) {

@@ -295,7 +295,7 @@ struct aphgpu_ctx {
   double* hist = nullptr;      // device residual history, 2 x kHistCap
   std::vector<double> hist_outer, hist_inner;
   aphgpu::RedBuf red{nullptr, nullptr, 0};
-  unsigned int* flags = nullptr;  // 4 counters for validation kernels
+  unsigned int* flags = nullptr;  // 5 counters: validation kernels, FP16 range, sweep error
   aphgpu::Multigrid mg;
 
   // VOF state
@@ -312,6 +312,26 @@ struct aphgpu_ctx {
   // cell indices (int64), room for cc_cap cells
   double* cc_buf = nullptr;
   int64_t cc_cap = 0;
+  // projection fluid step (fluid.cu): time layer (velocity, fluxes),
+  // iteration layer, work arrays, cell viscosity, pressures
+  struct {
+    double* vel = nullptr;    // 3N, blocks per component
+    double* vi = nullptr;     // 3N
+    double* flux = nullptr;   // 3N face blocks
+    double* ffv = nullptr;    // 3N
+    double* ffu = nullptr;    // 3N
+    double* acc = nullptr;    // 3N AoS
+    double* guess = nullptr;  // 3N
+    double* mu = nullptr;
+    double* p = nullptr;
+    double* ppred = nullptr;
+    double* e8 = nullptr;     // 8N diffusion system
+    double rho1 = 1, rho2 = 1;
+    int steps = 0;
+    int unconverged = 0;
+    bool follow_vof = false;  // density from the resident volume fraction
+    bool ready = false;
+  } fluid;
   double* vof_src = nullptr;   // N, volume source of the VOF step
   bool has_vof_src = false;
   double clipth = 1e-10;
@@ -430,6 +450,12 @@ int SystemToExprDevice(aphgpu_ctx* ctx, double* d_e8);
 int FluxCorrect(aphgpu_ctx* ctx, double* d_out);
 int Acceleration(aphgpu_ctx* ctx, double* d_acc, const double* d_alpha,
                  double rho1, double rho2);
+// fluid.cu
+int FluidInitDevice(aphgpu_ctx* ctx, double rho1, double rho2, double mu1, double mu2);
+int FluidStepDevice(aphgpu_ctx* ctx, double dt, const aphgpu_conf* conf, aphgpu_info* info,
+                    double* d_res);
+int BcgFacesDevice(aphgpu_ctx* ctx, const double* u, const double* vflux, const double* src,
+                   double dt, double* out);
 // vof.cu
 int VofReconstruct(aphgpu_ctx* ctx);
 int ColorInit(aphgpu_ctx* ctx);

@@ -522,7 +522,7 @@ inline int LaunchPipe(aphgpu_ctx* ctx, const Op<float>& A, const float* b, const
   const PipeTiling T = PipeTiles(A.d, SmCount(ctx));
   const int items = T.xtiles * T.bands * T.zsegs;
   KSweepPipe<<<items, kPipeThreads, kPipeSmemBytes, st>>>(A, b, in, out, c0, zero_init, s, T,
-                                                          (int*)ctx->flags + 3);
+                                                          (int*)ctx->flags + 4);
   return APHGPU_OK;
 }
 inline dim3 SweepGrid(const Dims& d) {
@@ -811,13 +811,15 @@ __device__ double CoarseFace(const Op<T>& A, int q, int I, int J, int K, double 
 // Coarse operator of constant prolongation and summed restriction, pass 1:
 // the three minus-face couplings of each coarse cell (CoarseFace) and, in
 // `diag`, the summed diagonal shifts of its 8 children (shift = diagonal +
-// sum of the couplings; zero for flux-difference systems).  The shifts
-// (mass terms of diffusion systems, given-pressure cells) take their
-// Galerkin value, the sum: constant prolongation represents them exactly,
-// unlike the couplings, whose Galerkin value is halved (CoarseFace).
+// sum of the couplings).  The shifts (mass terms of diffusion systems,
+// given-pressure cells) take their Galerkin value, the sum: constant
+// prolongation represents them exactly, unlike the couplings, whose
+// Galerkin value is halved (CoarseFace).  Singular (flux-difference)
+// systems have no shifts: with_shift = 0 keeps them exactly zero, so that
+// the rounding of the coarse operators does not accumulate into them.
 template <class T, class TC>
 __global__ void KCoarsenFaces(Op<T> A, Dims dc, TC* w0, TC* w1, TC* w2, TC* diag,
-                              double series) {
+                              double series, int with_shift) {
   const int I = blockIdx.x * kTileX + threadIdx.x;
   const int J = blockIdx.y * kTileY + threadIdx.y;
   const int kb = blockIdx.z * kTileZ;
@@ -839,7 +841,7 @@ __global__ void KCoarsenFaces(Op<T> A, Dims dc, TC* w0, TC* w1, TC* w2, TC* diag
     w0[C] = (TC)CoarseFace(A, 0, I, J, K, series);
     w1[C] = (TC)CoarseFace(A, 1, I, J, K, series);
     w2[C] = (TC)CoarseFace(A, 2, I, J, K, series);
-    diag[C] = (TC)shift;
+    diag[C] = with_shift ? (TC)shift : (TC)0;
   }
 }
 
@@ -861,9 +863,10 @@ __global__ void KCoarsenDiag(Op<TC> C, TC* diag, TC* invdiag) {
 
 // Coarse level `lc` from the fine operator A (both passes).
 template <class T, class TC>
-void CoarsenOp(cudaStream_t st, const Op<T>& A, Level<TC>& lc, double series) {
+void CoarsenOp(cudaStream_t st, const Op<T>& A, Level<TC>& lc, double series, int with_shift) {
   KCoarsenFaces<T, TC><<<TileGrid(lc.d), TileBlock(), 0, st>>>(A, lc.d, lc.w[0], lc.w[1],
-                                                                lc.w[2], lc.diag, series);
+                                                                lc.w[2], lc.diag, series,
+                                                                with_shift);
   const Op<TC> C{lc.d, lc.w[0], lc.w[1], lc.w[2], nullptr};
   KCoarsenDiag<TC><<<TileGrid(lc.d), TileBlock(), 0, st>>>(C, lc.diag, lc.invdiag);
 }
@@ -1210,7 +1213,7 @@ int EnsureCoarsestScratch(aphgpu_ctx* ctx, int64_t n) {
 // by Cholesky on the host (n <= kDenseMax cells; built once per system).
 template <class T>
 int BuildCoarsestInverse(aphgpu_ctx* ctx, const Level<T>& L, double** dinv, int* dn,
-                         int* singular) {
+                         int singular) {
   const Dims d = L.d;
   const int n = (int)d.cells();
   if (n > kDenseMax) {
@@ -1227,7 +1230,7 @@ int BuildCoarsestInverse(aphgpu_ctx* ctx, const Level<T>& L, double** dinv, int*
   APH_CUDA(ctx, cudaStreamSynchronize(st));
   std::vector<double> B((size_t)n * n, 0.0);
   auto at = [&](int r, int c) -> double& { return B[(size_t)r * n + c]; };
-  double dsum = 0, ssum = 0;  // diagonals, row sums (the shifts)
+  double dsum = 0;
   for (int k = 0; k < d.nz; ++k)
     for (int j = 0; j < d.ny; ++j)
       for (int i = 0; i < d.nx; ++i) {
@@ -1241,21 +1244,18 @@ int BuildCoarsestInverse(aphgpu_ctx* ctx, const Level<T>& L, double** dinv, int*
         const double e[6] = {(double)w0[c], (double)w0[xp], (double)w1[c],
                              (double)w1[yp], (double)w2[c], (double)w2[zp]};
         const int nb[6] = {xm, xp, ym, yp, zm, zp};
-        double diag = 0, rowsum = 0;
+        double diag = 0;
         for (int q = 0; q < 6; ++q) {
           at(c, nb[q]) += e[q];
           diag -= e[q];
-          rowsum += e[q];
         }
         if (L.has_diag) diag = (double)dg[c];
         at(c, c) += diag;
         dsum += diag;
-        ssum += diag + rowsum;
       }
-  // singular (periodic flux-difference operator: the row sums vanish up to
-  // the rounding of the coarse operators): invert A + c 11^T instead
-  *singular = std::fabs(ssum) <= 1e-5 * std::fabs(dsum) ? 1 : 0;
-  const double cshift = *singular ? dsum / n / n : 0.0;
+  // singular (periodic flux-difference operator, constant null space):
+  // invert A + c 11^T instead
+  const double cshift = singular ? dsum / n / n : 0.0;
   for (auto& v : B) v += cshift;
   // Cholesky B = L L^T, then B^{-1} column by column
   std::vector<double> Lm((size_t)n * n, 0.0);
@@ -1361,13 +1361,15 @@ int BuildHierarchy<double>(aphgpu_ctx* ctx, std::vector<Level<double>>& lv,
   f.invdiag = ctx->invdiag;
   for (size_t l = 1; l < lv.size(); ++l) {
     const Op<double> A = MakeOp(lv[l - 1]);
-    CoarsenOp<double, double>(ctx->stream, A, lv[l], CoarseSeries(ctx));
+    CoarsenOp<double, double>(ctx->stream, A, lv[l], CoarseSeries(ctx),
+                              ctx->diag_explicit ? 1 : 0);
     ctx->launches += 1;  // two kernels
     APH_LAUNCHED(ctx);
   }
   APH_TRY(EnsureCoarsestScratch(ctx, lv.back().d.cells()));
+  ctx->mg.csing64 = ctx->diag_explicit ? 0 : 1;
   APH_TRY(BuildCoarsestInverse(ctx, lv.back(), &ctx->mg.cinv64, &ctx->mg.cn64,
-                               &ctx->mg.csing64));
+                               ctx->mg.csing64));
   return APHGPU_OK;
 }
 
@@ -1419,17 +1421,20 @@ int BuildHierarchy<float>(aphgpu_ctx* ctx, std::vector<Level<float>>& lv,
     // coarse operators from the FP64 fine operator at level 1, FP32 below
     if (l == 1) {
       const Op<double> A = FineOp(ctx);
-      CoarsenOp<double, float>(ctx->stream, A, lv[l], CoarseSeries(ctx));
+      CoarsenOp<double, float>(ctx->stream, A, lv[l], CoarseSeries(ctx),
+                              ctx->diag_explicit ? 1 : 0);
     } else {
       const Op<float> A = MakeOp(lv[l - 1]);
-      CoarsenOp<float, float>(ctx->stream, A, lv[l], CoarseSeries(ctx));
+      CoarsenOp<float, float>(ctx->stream, A, lv[l], CoarseSeries(ctx),
+                              ctx->diag_explicit ? 1 : 0);
     }
     ctx->launches += 1;  // two kernels
     APH_LAUNCHED(ctx);
   }
   APH_TRY(EnsureCoarsestScratch(ctx, lv.back().d.cells()));
+  ctx->mg.csing32 = ctx->diag_explicit ? 0 : 1;
   APH_TRY(BuildCoarsestInverse(ctx, lv.back(), &ctx->mg.cinv32, &ctx->mg.cn32,
-                               &ctx->mg.csing32));
+                               ctx->mg.csing32));
   return CoarseOneSetup(ctx);
 }
 

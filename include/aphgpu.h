@@ -236,6 +236,46 @@ int aphgpu_surface_tension(aphgpu_ctx* ctx, double sigma, double* febp);
  * (on != 0) when their febp argument is NULL. */
 int aphgpu_set_force_resident(aphgpu_ctx* ctx, int on);
 
+/* ---- projection fluid step ---- */
+
+/* Sets up the projection fluid solver of aphros, Proj
+ * (src/solver/proj.ipp) with the default ProjPar (BCG advection, implicit
+ * diffusion, one iteration per step), periodic, without forces or
+ * sources: density and dynamic viscosity are the mixtures rho1 (1 - a) +
+ * rho2 a and mu1 (1 - a) + mu2 a of the gas volume fraction a (alpha, or
+ * NULL for the resident VOF volume fraction, then re-read at every step);
+ * vel: the cell velocity, 3 blocks of N (x, y, z components); the face
+ * fluxes of the time layer are those of vel (Proj's constructor,
+ * proj.ipp:96-101); pressures start at zero. */
+int aphgpu_fluid_init(aphgpu_ctx* ctx, const double* alpha, double rho1, double rho2,
+                      double mu1, double mu2, const double* vel);
+
+/* One time step of Proj (StartStep, MakeIteration, FinishStep,
+ * proj.ipp:309-322, 455-613): on the first step the initial pressure
+ * (proj.ipp:111-127), then the acceleration of the pressure, the BCG
+ * predicted face fluxes and their projection with dt/2 (proj.ipp:484-499),
+ * the BCG advection of the velocity (proj.ipp:128-190), implicit
+ * diffusion of each component (proj.ipp:241-307), the face fluxes of the
+ * velocity projected with dt, and the new acceleration (proj.ipp:524-575).
+ * Its five linear systems (four after the first step) are solved by
+ * conf's solver (miniter 0, as Proj's solver is configured), each from
+ * its guess (the pressure of the previous solve, the advected velocity).
+ * The corrected fluxes become the resident advection fluxes of
+ * aphgpu_vof_step(ctx, NULL, dt).  info->iter: total solver iterations;
+ * info->converged: every solve converged. */
+int aphgpu_fluid_step(aphgpu_ctx* ctx, double dt, const aphgpu_conf* conf, aphgpu_info* info);
+
+/* Copies the fluid state to the host; any pointer may be NULL.  vel: 3
+ * blocks of N; p: pressure; flux: the face fluxes, 3 face blocks. */
+int aphgpu_fluid_get(aphgpu_ctx* ctx, double* vel, double* p, double* flux);
+
+/* BCG face values of a cell field: UEmbed::InterpolateBcg
+ * (src/solver/approx_eb.ipp:753-821) on the periodic mesh of the context,
+ * the predictor of Proj; u: cell field, vflux: face volume fluxes (3 face
+ * blocks), src: cell source, dt; out: 3 face blocks. */
+int aphgpu_bcg_faces(aphgpu_ctx* ctx, const double* u, const double* vflux, const double* src,
+                     double dt, double* out);
+
 /* ---- timing of the last solve (CUDA events on the context stream) ---- */
 
 /* Milliseconds of the last solve, VOF step or curvature

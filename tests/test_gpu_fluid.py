@@ -1,0 +1,114 @@
+"""The projection fluid step on the device (aphgpu_fluid_*, Proj with the
+default ProjPar) against aphros and the oracle.
+
+* The BCG face predictor (UEmbed::InterpolateBcg, approx_eb.ipp:753-821)
+  equals aphros's own bit for bit (fixture bcg.npz, made by aphros's code).
+* Whole steps (initial pressure, BCG predictor and its projection, BCG
+  advection, implicit diffusion, projection, acceleration) against the
+  oracle's orc_fluid_step, which equals aphros's Proj bit for bit
+  (tests/test_oracle_pins.py).  Everything outside the linear solves
+  follows the reference's arithmetic; the solves (the CG of the reference
+  and the library's solvers) stop at the same tolerance in a different
+  order of sums, so the fields agree to the solver tolerance: at the
+  fixture's tolerance and, ten thousand times closer, at a tight one.
+"""
+import os
+import sys
+
+import numpy as np
+import pytest
+
+import oracle
+from aphros_gb300 import _lib, workload
+from conftest import golden
+
+pytestmark = pytest.mark.gpu
+
+sys.path.insert(0, os.path.dirname(golden("fluid.npz")))
+from make_golden import FLUID, fluid_cases, taylor_green_cells  # noqa: E402
+
+
+def test_bcg_faces_equal_aphros():
+    fx = np.load(golden("bcg.npz"))
+    for q in range(2):
+        n3 = tuple(int(v) for v in fx["n%d" % q])
+        ctx = _lib.Context(n3, float(fx["h%d" % q]))
+        out = ctx.bcg_faces(fx["u%d" % q], fx["vflux%d" % q], fx["src%d" % q],
+                            float(fx["dt%d" % q]))
+        assert np.array_equal(out, fx["ffu%d" % q]), q
+        ctx.close()
+
+
+def _rel(a, b):
+    return float(np.max(np.abs(a - b)) / max(np.max(np.abs(b)), 1e-300))
+
+
+def _rel_demean(a, b):
+    a = a - a.mean()
+    b = b - b.mean()
+    return float(np.linalg.norm(a - b) / max(np.linalg.norm(b), 1e-300))
+
+
+def _run(q, tol, solver, steps):
+    n, centres, radii = fluid_cases()[q]
+    case = workload.Case(n, centres, radii, seed=1)
+    a = case.alpha
+    rho = FLUID["rho1"] * (1 - a) + FLUID["rho2"] * a
+    mu = FLUID["mu1"] * (1 - a) + FLUID["mu2"] * a
+    vel0 = taylor_green_cells(n)
+    st = oracle.FluidState(n, 1.0 / n, vel0, rho, mu, tol=tol)
+    ctx = _lib.Context(n, 1.0 / n)
+    ctx.fluid_init(a, FLUID["rho1"], FLUID["rho2"], FLUID["mu1"], FLUID["mu2"], vel0)
+    conf = _lib.default_conf(solver=solver, tol=tol, maxiter=100000)
+    out = []
+    for s in range(1, max(steps) + 1):
+        st.step(FLUID["dt"], nthreads=os.cpu_count() or 1)
+        info = ctx.fluid_step(FLUID["dt"], conf)
+        assert info.converged, (q, s)
+        if s in steps:
+            vel, p, flux = ctx.fluid_get()
+            out.append((s, _rel(vel, st.vel), _rel_demean(p, st.p), _rel(flux, st.flux)))
+    ctx.close()
+    return out
+
+
+@pytest.mark.parametrize("q", [0, 1])
+def test_fluid_step_matches_oracle_at_fixture_tolerance(q):
+    """The fixture's tolerance (1e-8): the plain FP64 CG on the device
+    against the oracle's CG, after 1 and 4 steps."""
+    for s, dv, dp, df in _run(q, FLUID["tol"], _lib.SOLVER_CG, (1, 4)):
+        print("case %d step %d: vel %.2e p %.2e flux %.2e" % (q, s, dv, dp, df))
+        assert dv <= 1e-7 and df <= 1e-7, (s, dv, df)
+        assert dp <= 1e-6, (s, dp)
+
+
+@pytest.mark.parametrize("solver", [_lib.SOLVER_CG, _lib.SOLVER_MGPCG, _lib.SOLVER_MIXED])
+def test_fluid_step_matches_oracle_tight(solver):
+    """At a tolerance 1e4 times tighter both sides reach the same discrete
+    fields: the device step differs from the reference's only through the
+    solver tolerance."""
+    for s, dv, dp, df in _run(1, FLUID["tol"] * 1e-4, solver, (1, 4)):
+        print("solver %d step %d: vel %.2e p %.2e flux %.2e" % (solver, s, dv, dp, df))
+        assert dv <= 1e-10 and df <= 1e-10, (s, dv, df)
+        assert dp <= 1e-9, (s, dp)
+
+
+def test_fluid_drives_the_vof_step():
+    """With the resident volume fraction (alpha NULL) the step's corrected
+    fluxes advect it (aphgpu_vof_step with NULL fluxes), conserving its
+    volume to round-off, and the next step reads the advected fraction."""
+    n = 16
+    case = workload.config("c1", n=n)
+    ctx = _lib.Context(n, case.h)
+    ctx.vof_init(case.alpha)
+    ctx.fluid_init(None, FLUID["rho1"], FLUID["rho2"], FLUID["mu1"], FLUID["mu2"],
+                   taylor_green_cells(n))
+    conf = _lib.default_conf(solver=_lib.SOLVER_MIXED, tol=1e-10, maxiter=1000)
+    v0 = ctx.vof_get()[0].sum()
+    for _ in range(3):
+        assert ctx.fluid_step(FLUID["dt"], conf).converged
+        ctx.vof_step(None, FLUID["dt"])
+    u = ctx.vof_get()[0]
+    assert abs(u.sum() - v0) <= 1e-10 * v0
+    assert not np.array_equal(u, case.alpha)
+    ctx.close()
