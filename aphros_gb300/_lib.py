@@ -35,7 +35,7 @@ K_SWEEP32 = 10
 KERNEL_NAMES = {0: "KSmooth<float>", 1: "KSmooth<double>", 2: "KPcgApply<double>",
                 3: "KPcgApply<float>", 4: "KResidualRestrict<float>",
                 5: "KSweepFlux", 6: "KSweepUpdate", 7: "KReconstruct",
-                8: "KHeights", 9: "KCurvature", 10: "KSweepRB4"}
+                8: "KHeights", 9: "KCurvature", 10: "KSweepPipe"}
 
 SOLVER_CG = 0
 SOLVER_MGPCG = 1

@@ -3,6 +3,9 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <mutex>
+#include <utility>
+#include <vector>
 #include <cmath>
 #include <cstdarg>
 #include <cstdio>
@@ -33,13 +36,119 @@ int CheckCuda(aphgpu_ctx* ctx, cudaError_t e, const char* what) {
                   "%s: %s", what, cudaGetErrorString(e));
 }
 
+namespace {
+
+std::mutex g_pool_mu;
+cudaMemPool_t g_pools[64] = {};
+bool g_pool_failed[64] = {};
+
+// the device's pool, created on first use; nullptr if pools are unsupported
+cudaMemPool_t DevicePool(int device) {
+  if (device < 0 || device >= 64) return nullptr;
+  std::lock_guard<std::mutex> lock(g_pool_mu);
+  if (g_pools[device] || g_pool_failed[device]) return g_pools[device];
+  cudaMemPoolProps props = {};
+  props.allocType = cudaMemAllocationTypePinned;
+  props.location.type = cudaMemLocationTypeDevice;
+  props.location.id = device;
+  cudaMemPool_t pool = nullptr;
+  if (cudaMemPoolCreate(&pool, &props) != cudaSuccess) {
+    cudaGetLastError();
+    g_pool_failed[device] = true;
+    return nullptr;
+  }
+  uint64_t keep = UINT64_MAX;  // freed memory stays in the pool
+  cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &keep);
+  g_pools[device] = pool;
+  return pool;
+}
+
+// pinned host buffers returned by destroyed contexts, at most kPinnedKeep
+// bytes in all
+constexpr size_t kPinnedKeep = size_t(8) << 30;
+std::mutex g_pin_mu;
+std::vector<std::pair<void*, size_t>> g_pinned;
+size_t g_pinned_bytes = 0;
+
+}  // namespace
+
+int DeviceAlloc(aphgpu_ctx* ctx, void** p, size_t bytes) {
+  cudaMemPool_t pool = DevicePool(ctx->device);
+  cudaError_t e = pool ? cudaMallocFromPoolAsync(p, bytes, pool, ctx->stream)
+                       : cudaMalloc(p, bytes);
+  if (e != cudaSuccess && pool) {
+    // memory kept by the pool but free: release it and try once more
+    cudaGetLastError();
+    cudaMemPoolTrimTo(pool, 0);
+    e = cudaMallocFromPoolAsync(p, bytes, pool, ctx->stream);
+  }
+  if (e != cudaSuccess) {
+    cudaGetLastError();
+    return SetError(ctx, APHGPU_ERR_NOMEM, "device allocation of %zu bytes failed: %s", bytes,
+                    cudaGetErrorString(e));
+  }
+  return APHGPU_OK;
+}
+
+void DeviceFree(aphgpu_ctx* ctx, void* p) {
+  if (!p) return;
+  if (DevicePool(ctx->device))
+    cudaFreeAsync(p, ctx->stream);
+  else
+    cudaFree(p);
+}
+
+void* PinnedTake(size_t bytes, size_t* got) {
+  {
+    std::lock_guard<std::mutex> lock(g_pin_mu);
+    // the smallest kept buffer that is large enough (and not much larger)
+    size_t best = g_pinned.size();
+    for (size_t i = 0; i < g_pinned.size(); ++i) {
+      const size_t sz = g_pinned[i].second;
+      if (sz >= bytes && sz <= 4 * bytes + 4096 &&
+          (best == g_pinned.size() || sz < g_pinned[best].second))
+        best = i;
+    }
+    if (best < g_pinned.size()) {
+      void* p = g_pinned[best].first;
+      *got = g_pinned[best].second;
+      g_pinned_bytes -= *got;
+      g_pinned.erase(g_pinned.begin() + best);
+      return p;
+    }
+  }
+  void* p = nullptr;
+  if (cudaMallocHost(&p, bytes) != cudaSuccess) {
+    cudaGetLastError();
+    return nullptr;
+  }
+  *got = bytes;
+  return p;
+}
+
+void PinnedGive(void* p, size_t bytes) {
+  if (!p) return;
+  {
+    std::lock_guard<std::mutex> lock(g_pin_mu);
+    if (g_pinned_bytes + bytes <= kPinnedKeep) {
+      g_pinned.emplace_back(p, bytes);
+      g_pinned_bytes += bytes;
+      return;
+    }
+  }
+  cudaFreeHost(p);
+}
+
 int Staging(aphgpu_ctx* ctx, size_t bytes, void** out) {
   if (ctx->pinned_bytes < bytes) {
-    if (ctx->pinned) cudaFreeHost(ctx->pinned);
+    PinnedGive(ctx->pinned, ctx->pinned_bytes);
     ctx->pinned = nullptr;
     ctx->pinned_bytes = 0;
-    APH_CUDA(ctx, cudaMallocHost(&ctx->pinned, bytes));
-    ctx->pinned_bytes = bytes;
+    size_t got = 0;
+    void* p = PinnedTake(bytes, &got);
+    if (!p) return SetError(ctx, APHGPU_ERR_NOMEM, "pinned host allocation of %zu bytes", bytes);
+    ctx->pinned = p;
+    ctx->pinned_bytes = got;
   }
   *out = ctx->pinned;
   return APHGPU_OK;
@@ -219,7 +328,7 @@ int aphgpu_create(aphgpu_ctx** out, int nx, int ny, int nz, double h, int device
   if ((rc = Alloc(ctx, &ctx->scal2, 1))) return fail(rc);
   if ((rc = Alloc(ctx, &ctx->flags, 5))) return fail(rc);
   // flags[4]: set by a pipelined sweep whose bounded wait gave up
-  if (cudaMemset(ctx->flags, 0, 5 * sizeof(unsigned int)) != cudaSuccess) {
+  if (cudaMemsetAsync(ctx->flags, 0, 5 * sizeof(unsigned int), ctx->stream) != cudaSuccess) {
     cudaGetLastError();
     return fail(APHGPU_ERR_CUDA);
   }
@@ -228,9 +337,10 @@ int aphgpu_create(aphgpu_ctx** out, int nx, int ny, int nz, double h, int device
   if ((rc = Alloc(ctx, &ctx->red.part, (int64_t)kMaxRedVals * ctx->red.max_blocks)))
     return fail(rc);
   if ((rc = Alloc(ctx, &ctx->red.ticket, 1))) return fail(rc);
-  if (cudaMallocHost(&ctx->hscal, sizeof(SolveScalars)) != cudaSuccess) {
-    cudaGetLastError();
-    return fail(APHGPU_ERR_NOMEM);
+  {
+    size_t got = 0;
+    ctx->hscal = (SolveScalars*)PinnedTake(sizeof(SolveScalars), &got);
+    if (!ctx->hscal) return fail(APHGPU_ERR_NOMEM);
   }
   cudaMemsetAsync(ctx->red.ticket, 0, sizeof(unsigned), ctx->stream);
   cudaMemsetAsync(ctx->x, 0, sizeof(double) * N, ctx->stream);
@@ -248,10 +358,12 @@ void aphgpu_destroy(aphgpu_ctx* ctx) {
   if (ctx->stream) cudaStreamSynchronize(ctx->stream);
   for (auto& g : ctx->graphs)
     if (g.exec) cudaGraphExecDestroy(g.exec);
-  for (void* p : ctx->allocs) cudaFree(p);
+  for (void* p : ctx->allocs) DeviceFree(ctx, p);
   ctx->allocs.clear();
-  if (ctx->hscal) cudaFreeHost(ctx->hscal);
-  if (ctx->pinned) cudaFreeHost(ctx->pinned);
+  if (ctx->stream) cudaStreamSynchronize(ctx->stream);
+  // pinned buffers are kept for the next contexts
+  PinnedGive(ctx->hscal, sizeof(SolveScalars));
+  PinnedGive(ctx->pinned, ctx->pinned_bytes);
   if (ctx->ev0) cudaEventDestroy(ctx->ev0);
   if (ctx->ev1) cudaEventDestroy(ctx->ev1);
   for (int q = 0; q < 8; ++q)
@@ -305,7 +417,7 @@ int aphgpu_apply_cell_cond(aphgpu_ctx* ctx, int64_t count, const int64_t* cells,
       for (size_t i = 0; i < ctx->allocs.size(); ++i) {
         if (ctx->allocs[i] == ctx->cc_buf) {
           APH_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
-          cudaFree(ctx->cc_buf);
+          DeviceFree(ctx, ctx->cc_buf);
           ctx->allocs.erase(ctx->allocs.begin() + i);
           ctx->bytes -= (int64_t)sizeof(double) * 2 * ctx->cc_cap;
           break;
@@ -336,7 +448,7 @@ int aphgpu_get_system_expr(aphgpu_ctx* ctx, double* expr8) {
   cudaStreamSynchronize(ctx->stream);
   for (size_t i = 0; i < ctx->allocs.size(); ++i) {
     if (ctx->allocs[i] == d_e8) {
-      cudaFree(d_e8);
+      DeviceFree(ctx, d_e8);
       ctx->allocs.erase(ctx->allocs.begin() + i);
       ctx->bytes -= (int64_t)sizeof(double) * 8 * ctx->N;
       break;
@@ -491,7 +603,7 @@ int aphgpu_acceleration(aphgpu_ctx* ctx, double* acc) {
   cudaStreamSynchronize(ctx->stream);
   for (size_t i = 0; i < ctx->allocs.size(); ++i) {
     if (ctx->allocs[i] == d_acc) {
-      cudaFree(d_acc);
+      DeviceFree(ctx, d_acc);
       ctx->allocs.erase(ctx->allocs.begin() + i);
       ctx->bytes -= (int64_t)sizeof(double) * 3 * ctx->N;
       break;
@@ -623,7 +735,7 @@ int aphgpu_bcg_faces(aphgpu_ctx* ctx, const double* u, const double* vflux, cons
   cudaStreamSynchronize(ctx->stream);
   for (size_t i = 0; i < ctx->allocs.size(); ++i) {
     if (ctx->allocs[i] == d) {
-      cudaFree(d);
+      DeviceFree(ctx, d);
       ctx->allocs.erase(ctx->allocs.begin() + i);
       ctx->bytes -= (int64_t)sizeof(double) * 8 * N;
       break;

@@ -368,11 +368,11 @@ struct aphgpu_ctx {
   int64_t mg_epoch = 0;        // bumped whenever a hierarchy is (re)allocated
   bool use_graphs = true;
   // fused out-of-place red-black sweeps on the FP32 levels: 0 off (two
-  // in-place half sweeps), 1 the pipelined kernel (bulk copies into shared
-  // memory) on levels of at least kPipeMinCells cells (default), 2 the
+  // in-place half sweeps, default), 1 the pipelined kernel (bulk copies
+  // into shared memory) on levels of at least kPipeMinCells cells, 2 the
   // pipelined kernel on every level it supports, 3 the synchronous fused
   // kernel on every level it supports
-  int fused_mode = 1;
+  int fused_mode = 0;
   bool use_half = false;   // FP16 couplings for the finest-level smoother
   int mg_gamma = 0;        // cycles of each level below the finest (1 V, 2 W, 0 auto)
   int mg_series_pct = 60;  // weight (%) of the series couplings in the coarse operators
@@ -393,16 +393,22 @@ namespace aphgpu {
 
 int SetError(aphgpu_ctx* ctx, int code, const char* fmt, ...);
 int CheckCuda(aphgpu_ctx* ctx, cudaError_t e, const char* what);
+// Device memory of the contexts comes from one stream-ordered pool per
+// device that keeps freed memory for reuse: destroying a context (an
+// eviction of the serving loop) does not synchronize the device, and the
+// next context reuses the memory without asking the driver.
+int DeviceAlloc(aphgpu_ctx* ctx, void** p, size_t bytes);
+void DeviceFree(aphgpu_ctx* ctx, void* p);
+// Pinned host buffers, recycled across contexts.
+void* PinnedTake(size_t bytes, size_t* got);
+void PinnedGive(void* p, size_t bytes);
+
 template <class T>
 int Alloc(aphgpu_ctx* ctx, T** p, int64_t count) {
   void* q = nullptr;
   const size_t bytes = sizeof(T) * (size_t)(count > 0 ? count : 1);
-  const cudaError_t e = cudaMalloc(&q, bytes);
-  if (e != cudaSuccess) {
-    cudaGetLastError();
-    return SetError(ctx, APHGPU_ERR_NOMEM, "cudaMalloc of %zu bytes failed: %s",
-                    bytes, cudaGetErrorString(e));
-  }
+  const int rc = DeviceAlloc(ctx, &q, bytes);
+  if (rc != APHGPU_OK) return rc;
   ctx->allocs.push_back(q);
   ctx->bytes += (int64_t)bytes;
   *p = (T*)q;

@@ -425,14 +425,15 @@ int aphgpu_batch_last_ms(const aphgpu_batch* batch, double* ms, int64_t* launche
  *   APHGPU_OPT_FUSED_SWEEPS  fused out-of-place red-black sweeps (both
  *                            colours in one pass: half the DRAM traffic of
  *                            two half sweeps) on the FP32 levels: 1
- *                            (default) the pipelined kernel, fed by bulk
+ *                            the pipelined kernel, fed by bulk
  *                            copies into shared memory, on levels of at
  *                            least 2^21 cells with nx a multiple of 4 and
  *                            no stored diagonal; 2 the pipelined kernel on
  *                            every such level whatever its size; 3 the
  *                            synchronous fused kernel (latency-bound) on
  *                            every level with nx a multiple of 4, nx >= 8;
- *                            0 two in-place half sweeps everywhere.  Other
+ *                            0 (default) two in-place half sweeps
+ *                            everywhere.  Other
  *                            levels take the half sweeps
  *   APHGPU_OPT_HALF_COUPLINGS 1: the smoother and the restriction of the
  *                            finest FP32 level read an FP16 copy of the
