@@ -827,6 +827,10 @@ int aphgpu_set_option(aphgpu_ctx* ctx, int option, int value) {
   if (!Valid(ctx)) return APHGPU_ERR_ARG;
   switch (option) {
     case APHGPU_OPT_GRAPHS: ctx->use_graphs = value != 0; return APHGPU_OK;
+    case APHGPU_OPT_PIPE_COPIES:
+      if (value < 0 || value > 1) return SetError(ctx, APHGPU_ERR_ARG, "pipe copies %d", value);
+      ctx->pipe_copies = value;
+      return APHGPU_OK;
     case APHGPU_OPT_FUSED_SWEEPS:
       if (value < 0 || value > 3) return SetError(ctx, APHGPU_ERR_ARG, "fused sweeps %d", value);
       if (value != ctx->fused_mode) ctx->mg.built32 = false;  // scratch of the levels

@@ -373,6 +373,9 @@ struct aphgpu_ctx {
   // pipelined kernel on every level it supports, 3 the synchronous fused
   // kernel on every level it supports
   int fused_mode = 0;
+  // staging of the pipelined sweep: 0 bulk copies (TMA) on mbarriers, 1
+  // per-thread 16-byte cp.async copies
+  int pipe_copies = 0;
   bool use_half = false;   // FP16 couplings for the finest-level smoother
   int mg_gamma = 0;        // cycles of each level below the finest (1 V, 2 W, 0 auto)
   int mg_series_pct = 60;  // weight (%) of the series couplings in the coarse operators

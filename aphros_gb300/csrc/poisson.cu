@@ -517,12 +517,20 @@ inline int LaunchPipe(aphgpu_ctx* ctx, const Op<float>& A, const float* b, const
   if (dev >= 0 && dev < 64 && !attr_set[dev]) {
     APH_CUDA(ctx, cudaFuncSetAttribute(KSweepPipe, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                        kPipeSmemBytes));
+    APH_CUDA(ctx, cudaFuncSetAttribute(KSweepPipeAsync,
+                                       cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                       kPipeSmemBytes));
     attr_set[dev] = true;
   }
   const PipeTiling T = PipeTiles(A.d, SmCount(ctx));
   const int items = T.xtiles * T.bands * T.zsegs;
-  KSweepPipe<<<items, kPipeThreads, kPipeSmemBytes, st>>>(A, b, in, out, c0, zero_init, s, T,
-                                                          (int*)ctx->flags + 4);
+  if (ctx->pipe_copies == 1) {
+    KSweepPipeAsync<<<items, kPipeThreads, kPipeSmemBytes, st>>>(A, b, in, out, c0, zero_init,
+                                                                 s, T);
+  } else {
+    KSweepPipe<<<items, kPipeThreads, kPipeSmemBytes, st>>>(A, b, in, out, c0, zero_init, s, T,
+                                                            (int*)ctx->flags + 4);
+  }
   return APHGPU_OK;
 }
 inline dim3 SweepGrid(const Dims& d) {
@@ -1802,6 +1810,7 @@ int Pcg(aphgpu_ctx* ctx, const Op<T>& A, Precond precond, T* x, T* r, T* p,
     key = Mix(key, (uint64_t)check_every);
     key = Mix(key, (uint64_t)sizeof(T));
     key = Mix(key, (uint64_t)ctx->fused_mode);
+    key = Mix(key, (uint64_t)ctx->pipe_copies);
     key = Mix(key, (uint64_t)CycleGamma(ctx));
     key = Mix(key, (uint64_t)SweepGrowth(ctx));
     key = Mix(key, (uint64_t)(ctx->use_cta_coarse ? 1 + ctx->mg.clc : 0));

@@ -452,4 +452,153 @@ __global__ void __launch_bounds__(kPipeThreads, 1)
   }
 }
 
+// ---------------------------------------------------------------------------
+// The same sweep with the rows staged by per-thread asynchronous copies
+// (cp.async, 16 bytes each) instead of bulk copies: every thread of the
+// CTA copies its share of the batch's 16-byte chunks (a row segment
+// [i0-4, i0+w+4) is (w+8)/4 chunks; the periodic wrap in x is per chunk,
+// since nx and i0 are multiples of 4) and commits them as one group; a
+// batch is complete once every thread has waited for its group
+// (cp.async.wait_group) and the block has passed a barrier.  No mbarrier
+// and no bounded wait is involved: each thread waits only for its own
+// copies.
+// ---------------------------------------------------------------------------
+
+__device__ __forceinline__ void CpAsync16(void* dst, const void* src) {
+  asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(SmemAddr(dst)), "l"(src)
+               : "memory");
+}
+__device__ __forceinline__ void CpAsyncCommit() {
+  asm volatile("cp.async.commit_group;" ::: "memory");
+}
+template <int kPending>
+__device__ __forceinline__ void CpAsyncWait() {
+  asm volatile("cp.async.wait_group %0;" ::"n"(kPending) : "memory");
+}
+
+// Issues a batch by all threads of the CTA, then commits one group.
+__device__ __forceinline__ void IssueBatchAsync(const Op<float>& A, const float* __restrict__ b,
+                                                const float* __restrict__ xin,
+                                                const PipeSmem& S, int base, int i0, int w,
+                                                int j0, int rows, const PipeBatch& B) {
+  const Dims d = A.d;
+  const int nxr = rows + 4, nc0 = rows + 2, nc1 = rows + 3, nw = rows + 2;
+  const int ncoef = B.pc_on ? nc0 + nc1 + nc0 : 0;
+  const int total = B.nxp * nxr + ncoef + B.nwp * nw;  // rows
+  const int cpr = (w + 8) / 4;                           // chunks per row
+  const int64_t plane = (int64_t)d.nx * d.ny;
+  for (int q = threadIdx.x; q < total * cpr; q += blockDim.x) {
+    int t = q / cpr;
+    const int ch = q - t * cpr;
+    const float* src;
+    float* dst;
+    int r, p;
+    if (t < B.nxp * nxr) {
+      p = B.px[t / nxr];
+      r = t % nxr - 2;
+      src = xin;
+      dst = S.xs + ((size_t)PosMod(p - base, kPipeXs) * kPipeXRows + (r + 2)) * kPipeStride;
+    } else if (t - B.nxp * nxr < ncoef) {
+      t -= B.nxp * nxr;
+      p = B.pc;
+      float* slot = S.cs + (size_t)PosMod(p - base, kPipeCs) * kPipeCRows * kPipeStride;
+      if (t < nc0) {
+        r = t - 1;
+        src = A.w0;
+        dst = slot + (size_t)(r + 1) * kPipeStride;
+      } else if (t < nc0 + nc1) {
+        r = t - nc0 - 1;
+        src = A.w1;
+        dst = slot + (size_t)(kPipeW0Rows + r + 1) * kPipeStride;
+      } else {
+        r = t - nc0 - nc1 - 1;
+        src = b;
+        dst = slot + (size_t)(kPipeW0Rows + kPipeW1Rows + r + 1) * kPipeStride;
+      }
+    } else {
+      t -= B.nxp * nxr + ncoef;
+      p = B.pw[t / nw];
+      r = t % nw - 1;
+      src = A.w2;
+      dst = S.ws + ((size_t)PosMod(p - base, kPipeWs) * kPipeW2Rows + (r + 1)) * kPipeStride;
+    }
+    const int jw = PosMod(j0 + r, d.ny);
+    const int pz = PosMod(p, d.nz);
+    const int col = PosMod(i0 - 4 + 4 * ch, d.nx);
+    CpAsync16(dst + 4 * ch, src + pz * plane + (int64_t)jw * d.nx + col);
+  }
+  CpAsyncCommit();
+}
+
+// KSweepPipe with cp.async staging (same tiling, rings and arithmetic).
+__global__ void __launch_bounds__(kPipeThreads, 1)
+    KSweepPipeAsync(Op<float> A, const float* __restrict__ b, const float* __restrict__ xin,
+                    float* xout, int c0, int zero_init, const SolveScalars* s, PipeTiling T) {
+  if (s && s->done) return;
+  extern __shared__ __align__(128) float smem[];
+  const Dims d = A.d;
+  PipeSmem S;
+  S.xs = smem;
+  S.cs = S.xs + (size_t)kPipeXs * kPipeXRows * kPipeStride;
+  S.ws = S.cs + (size_t)kPipeCs * kPipeCRows * kPipeStride;
+  S.fs = S.ws + (size_t)kPipeWs * kPipeW2Rows * kPipeStride;
+  S.bars = nullptr;
+  const int item = blockIdx.x;
+  const int xt = item % T.xtiles;
+  const int band = (item / T.xtiles) % T.bands;
+  const int zs = item / (T.xtiles * T.bands);
+  const int i0 = xt * T.w;
+  const int w = min(T.w, d.nx - i0);
+  const int j0 = band * T.rows;
+  const int rows = min(T.rows, d.ny - j0);
+  const int kb = (int)((int64_t)d.nz * zs / T.zsegs);
+  const int ke = (int)((int64_t)d.nz * (zs + 1) / T.zsegs);
+  const int warp = threadIdx.x >> 5;
+  const int base = kb - 2;
+  const int t0 = kb - 1;
+  auto batch = [&](int t) {
+    PipeBatch B;
+    B.nxp = 0;
+    if (!zero_init) {
+      B.px[B.nxp++] = t + 1;
+      if (t == t0) {
+        B.px[B.nxp++] = t - 1;
+        B.px[B.nxp++] = t;
+      }
+    }
+    B.pc = t;
+    B.pc_on = 1;
+    B.nwp = 0;
+    B.pw[B.nwp++] = t + 1;
+    if (t == t0) B.pw[B.nwp++] = t;
+    return B;
+  };
+  // prologue: B(t0), B(t0+1), B(t0+2); a batch past ke is an empty group
+  for (int t = t0; t <= t0 + 2; ++t) {
+    if (t <= ke)
+      IssueBatchAsync(A, b, xin, S, base, i0, w, j0, rows, batch(t));
+    else
+      CpAsyncCommit();
+  }
+  CpAsyncWait<2>();
+  __syncthreads();
+  for (int t = t0; t <= ke; ++t) {
+    // F(t): warps 0 .. rows+1 take rows -1 .. rows
+    if (warp < rows + 2) PipeFirst(S, base, c0, zero_init, i0, w, j0, warp - 1, t, d.ny, d.nz);
+    __syncthreads();
+    if (t - 1 >= kb && warp < rows) PipeSecond(S, base, c0, i0, w, j0, warp, t - 1, d, xout);
+    // the slots of plane t-1 (coefficients, w2) and t-2 (x) are free once
+    // every thread is past S(t-1): then B(t+3) may overwrite them
+    __syncthreads();
+    if (t + 3 <= ke)
+      IssueBatchAsync(A, b, xin, S, base, i0, w, j0, rows, batch(t + 3));
+    else
+      CpAsyncCommit();
+    // B(t+1) complete (B(t+2), B(t+3) may stay in flight)
+    CpAsyncWait<2>();
+    __syncthreads();
+  }
+  CpAsyncWait<0>();
+}
+
 }  // namespace aphgpu

@@ -255,14 +255,16 @@ def test_fused_sweeps_bit_identical(solver, shape):
     _, bn = ctx.residual_norms()
     conf = _lib.default_conf(solver=solver, tol=1e-10 * bn / math.sqrt(h ** 3), maxiter=200)
     out = {}
-    for fused in (2, 1, 3, 0):
+    # (fused mode, staging of the pipelined kernel: 0 bulk copies, 1 cp.async)
+    for fused, copies in ((2, 0), (2, 1), (1, 0), (1, 1), (3, 0), (0, 0)):
         for graphs in (1, 0):
             ctx.set_option(_lib.OPT_FUSED_SWEEPS, fused)
+            ctx.set_option(_lib.OPT_PIPE_COPIES, copies)
             ctx.set_option(_lib.OPT_GRAPHS, graphs)
             x, info = ctx.solve(conf)
             assert info.converged
-            out[(fused, graphs)] = (x, info.iter, info.inner_iter)
-    ref = out[(0, 0)]
+            out[(fused, copies, graphs)] = (x, info.iter, info.inner_iter)
+    ref = out[(0, 0, 0)]
     for key, val in out.items():
         assert np.array_equal(val[0], ref[0]), key
         assert val[1:] == ref[1:], key
@@ -429,13 +431,21 @@ def test_cell_conditions():
     e = ctx.get_system_expr()
     ref = oracle.apply_cell_cond(e0, cells, values)
     assert np.array_equal(e, ref)
+    # the unit penalty beside couplings of 1e-4 .. 1e-1 makes the system
+    # badly conditioned: the plain CG needs tens of thousands of iterations
+    # and two solutions at ||r||/||b|| = 1e-12 differ by ~3e-9, so the
+    # solutions are checked by their true residual (recomputed by the
+    # oracle in FP64) and against the oracle's CG within 1e-7
     tol = oracle.rel_tol(ref, h, 1e-12)
     xo, io = oracle.cg_solve(n, h, ref, tol, nthreads=os.cpu_count() or 1)
     assert io.residual < tol
-    for solver in (_lib.SOLVER_CG, _lib.SOLVER_MGPCG, _lib.SOLVER_MIXED):
-        x, info = ctx.solve(_lib.default_conf(solver=solver, tol=tol, maxiter=100000))
+    for solver in (_lib.SOLVER_MGPCG, _lib.SOLVER_MIXED, _lib.SOLVER_CG):
+        x, info = ctx.solve(_lib.default_conf(solver=solver, tol=tol, maxiter=200000))
         assert info.converged, solver
-        assert np.linalg.norm(x - xo) / np.linalg.norm(xo) <= 1e-9, solver
+        # true residual within 10x the tolerance (the recursive residual of
+        # the solvers drifts from the true one on this system)
+        assert math.sqrt(oracle.residual(n, ref, x)[1]) <= 10 * tol * math.sqrt(h ** 3), solver
+        assert np.linalg.norm(x - xo) / np.linalg.norm(xo) <= 1e-7, solver
     # a cell given twice, a cell outside the domain
     with pytest.raises(_lib.AphgpuError):
         ctx.apply_cell_cond([3, 3], [1.0, 1.0])
