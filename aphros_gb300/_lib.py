@@ -26,7 +26,6 @@ OPT_CYCLE = 3
 OPT_COARSE_SERIES = 4
 OPT_SWEEP_GROWTH = 5
 OPT_CTA_COARSE = 6
-OPT_PIPE_COPIES = 7
 FIELD_PRESSURE, FIELD_RHS, FIELD_VF, FIELD_CURVATURE = 0, 1, 2, 3
 DUMP_UINT16, DUMP_FLOAT32, DUMP_FLOAT64 = 0, 1, 2
 

@@ -327,7 +327,6 @@ int aphgpu_create(aphgpu_ctx** out, int nx, int ny, int nz, double h, int device
   if ((rc = Alloc(ctx, &ctx->scal, 1))) return fail(rc);
   if ((rc = Alloc(ctx, &ctx->scal2, 1))) return fail(rc);
   if ((rc = Alloc(ctx, &ctx->flags, 5))) return fail(rc);
-  // flags[4]: set by a pipelined sweep whose bounded wait gave up
   if (cudaMemsetAsync(ctx->flags, 0, 5 * sizeof(unsigned int), ctx->stream) != cudaSuccess) {
     cudaGetLastError();
     return fail(APHGPU_ERR_CUDA);
@@ -525,18 +524,6 @@ int aphgpu_solve_resident(aphgpu_ctx* ctx, const aphgpu_conf* conf, int zero_gue
   }
   ctx->x_zero = false;
   t.Stop();
-  if (rc == APHGPU_OK && ctx->fused_mode != 0) {
-    // a pipelined sweep that gave up a wait leaves its flag (the solve has
-    // synchronized the stream already)
-    unsigned int f = 0;
-    APH_CUDA(ctx, cudaMemcpyAsync(&f, ctx->flags + 4, sizeof(f), cudaMemcpyDeviceToHost,
-                                  ctx->stream));
-    APH_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
-    if (f) {
-      APH_CUDA(ctx, cudaMemsetAsync(ctx->flags + 4, 0, sizeof(f), ctx->stream));
-      return SetError(ctx, APHGPU_ERR_TIMEOUT, "a fused sweep's copy did not complete");
-    }
-  }
   return rc;
 }
 
@@ -827,10 +814,6 @@ int aphgpu_set_option(aphgpu_ctx* ctx, int option, int value) {
   if (!Valid(ctx)) return APHGPU_ERR_ARG;
   switch (option) {
     case APHGPU_OPT_GRAPHS: ctx->use_graphs = value != 0; return APHGPU_OK;
-    case APHGPU_OPT_PIPE_COPIES:
-      if (value < 0 || value > 1) return SetError(ctx, APHGPU_ERR_ARG, "pipe copies %d", value);
-      ctx->pipe_copies = value;
-      return APHGPU_OK;
     case APHGPU_OPT_FUSED_SWEEPS:
       if (value < 0 || value > 3) return SetError(ctx, APHGPU_ERR_ARG, "fused sweeps %d", value);
       if (value != ctx->fused_mode) ctx->mg.built32 = false;  // scratch of the levels

@@ -982,7 +982,7 @@ int BuildTables(aphgpu_batch* B, const aphgpu_conf* conf) {
     key = BMix(key, (uint64_t)(uintptr_t)c);
     key = BMix(key, (uint64_t)c->mg_epoch);
     key = BMix(key, (uint64_t)(uintptr_t)c->mg.l32[0].w[0]);
-    key = BMix(key, (uint64_t)(c->diag_explicit ? 1 : 0));
+    key = BMix(key, (uint64_t)(c->singular ? 1 : 0));
   }
   key = BMix(key, (uint64_t)B->kz);
   key = BMix(key, (uint64_t)B->coarse_cells);
@@ -1034,7 +1034,7 @@ int BuildTables(aphgpu_batch* B, const aphgpu_conf* conf) {
     D.cn = c->mg.cn32;
     D.csing = c->mg.csing32;
     // the constant-mode projection holds only for the singular operator
-    D.flags = c->diag_explicit ? (conf->inner_flags & ~1) : conf->inner_flags;
+    D.flags = c->singular ? conf->inner_flags : (conf->inner_flags & ~1);
     B->nlev_max = std::max(B->nlev_max, nl);
   }
   if (!B->d_doms) B_CUDA(B, cudaMalloc(&B->d_doms, sizeof(BDom) * B->ndom));

@@ -261,6 +261,9 @@ struct aphgpu_ctx {
   double* w[3] = {nullptr, nullptr, nullptr};
   double* diag = nullptr;      // NULL: diagonal = -(e1+...+e6) in order
   bool diag_explicit = false;
+  // every row sum vanishes (periodic flux-difference system: the constant
+  // null space); false with diagonal shifts (diffusion, given pressures)
+  bool singular = true;
   bool diag_valid = false;  // `diag` holds the FP64 diagonal (explicit or computed)
   bool x_zero = false;      // x was zeroed for the solve being run
   double* invdiag = nullptr;   // 1/diagonal (multigrid smoother)
@@ -295,7 +298,7 @@ struct aphgpu_ctx {
   double* hist = nullptr;      // device residual history, 2 x kHistCap
   std::vector<double> hist_outer, hist_inner;
   aphgpu::RedBuf red{nullptr, nullptr, 0};
-  unsigned int* flags = nullptr;  // 5 counters: validation kernels, FP16 range, sweep error
+  unsigned int* flags = nullptr;  // 5 counters: validation kernels, FP16 range
   aphgpu::Multigrid mg;
 
   // VOF state
@@ -368,14 +371,11 @@ struct aphgpu_ctx {
   int64_t mg_epoch = 0;        // bumped whenever a hierarchy is (re)allocated
   bool use_graphs = true;
   // fused out-of-place red-black sweeps on the FP32 levels: 0 off (two
-  // in-place half sweeps, default), 1 the pipelined kernel (bulk copies
-  // into shared memory) on levels of at least kPipeMinCells cells, 2 the
+  // in-place half sweeps, default), 1 the pipelined kernel (asynchronous
+  // copies into shared memory) on levels of at least kPipeMinCells cells, 2 the
   // pipelined kernel on every level it supports, 3 the synchronous fused
   // kernel on every level it supports
   int fused_mode = 0;
-  // staging of the pipelined sweep: 0 bulk copies (TMA) on mbarriers, 1
-  // per-thread 16-byte cp.async copies
-  int pipe_copies = 0;
   bool use_half = false;   // FP16 couplings for the finest-level smoother
   int mg_gamma = 0;        // cycles of each level below the finest (1 V, 2 W, 0 auto)
   int mg_series_pct = 60;  // weight (%) of the series couplings in the coarse operators

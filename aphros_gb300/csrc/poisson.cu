@@ -67,11 +67,13 @@ __device__ __forceinline__ double S(double a, double b) { return __dsub_rn(a, b)
 // System set-up
 // ---------------------------------------------------------------------------
 
-// flags[0]: asymmetric cells, flags[1]: cells whose e0 != -(sum of e_q)
+// flags[0]: asymmetric cells, flags[1]: cells whose e0 != -(sum of e_q),
+// flags[2]: cells whose row sum e0 + sum of e_q is more than rounding
+// (a diagonal shift: the system is not singular)
 __global__ void KExprToSystem(Dims d, const double* __restrict__ e8,
                               double* w0, double* w1, double* w2, double* diag,
                               double* b, unsigned int* flags) {
-  unsigned int asym = 0, nonpure = 0;
+  unsigned int asym = 0, nonpure = 0, shifted = 0;
   TILE_LOOP_BEGIN(d)
   const double* e = e8 + 8 * c;
   w0[c] = e[1];
@@ -83,12 +85,17 @@ __global__ void KExprToSystem(Dims d, const double* __restrict__ e8,
   if (e[2] != e8[8 * d.idx(ip, j, k) + 1]) ++asym;
   if (e[4] != e8[8 * d.idx(i, jp, k) + 3]) ++asym;
   if (e[6] != e8[8 * d.idx(i, j, kp) + 5]) ++asym;
-  double s = 0;
-  for (int q = 1; q <= 6; ++q) s += e[q];
+  double s = 0, mag = fabs(e[0]);
+  for (int q = 1; q <= 6; ++q) {
+    s += e[q];
+    mag += fabs(e[q]);
+  }
   if (e[0] != -s) ++nonpure;
+  if (!(fabs(e[0] + s) <= 1e-10 * mag)) ++shifted;
   TILE_LOOP_END
   if (asym) atomicAdd(&flags[0], asym);
   if (nonpure) atomicAdd(&flags[1], nonpure);
+  if (shifted) atomicAdd(&flags[2], shifted);
 }
 
 // Face coefficients and predicted fluxes (proj.ipp:343-360, 556-562):
@@ -487,8 +494,9 @@ inline bool PipeEligible(const aphgpu_ctx* ctx, const Dims& d) {
 }
 // Tiles of the pipelined sweep: columns of at most kPipeCols (balanced),
 // bands of at most kPipeRows rows (balanced), and z segments so that the
-// items fill the SMs in one wave (at least 8 planes a segment).
-inline PipeTiling PipeTiles(const Dims& d, int sms) {
+// items fill the `slots` resident CTAs in one wave (at least 8 planes a
+// segment).
+inline PipeTiling PipeTiles(const Dims& d, int slots) {
   PipeTiling T;
   T.xtiles = (d.nx + kPipeCols - 1) / kPipeCols;
   T.w = 4 * ((d.nx / 4 + T.xtiles - 1) / T.xtiles);
@@ -496,7 +504,7 @@ inline PipeTiling PipeTiles(const Dims& d, int sms) {
   T.rows = (d.ny + T.bands - 1) / T.bands;
   T.bands = (d.ny + T.rows - 1) / T.rows;
   const int tiles = T.xtiles * T.bands;
-  T.zsegs = std::max(1, std::min(d.nz / 8, sms / std::max(tiles, 1)));
+  T.zsegs = std::max(1, std::min(d.nz / 8, slots / std::max(tiles, 1)));
   return T;
 }
 inline int SmCount(aphgpu_ctx* ctx) {
@@ -517,20 +525,11 @@ inline int LaunchPipe(aphgpu_ctx* ctx, const Op<float>& A, const float* b, const
   if (dev >= 0 && dev < 64 && !attr_set[dev]) {
     APH_CUDA(ctx, cudaFuncSetAttribute(KSweepPipe, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                        kPipeSmemBytes));
-    APH_CUDA(ctx, cudaFuncSetAttribute(KSweepPipeAsync,
-                                       cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                       kPipeSmemBytes));
     attr_set[dev] = true;
   }
-  const PipeTiling T = PipeTiles(A.d, SmCount(ctx));
+  const PipeTiling T = PipeTiles(A.d, 2 * SmCount(ctx));
   const int items = T.xtiles * T.bands * T.zsegs;
-  if (ctx->pipe_copies == 1) {
-    KSweepPipeAsync<<<items, kPipeThreads, kPipeSmemBytes, st>>>(A, b, in, out, c0, zero_init,
-                                                                 s, T);
-  } else {
-    KSweepPipe<<<items, kPipeThreads, kPipeSmemBytes, st>>>(A, b, in, out, c0, zero_init, s, T,
-                                                            (int*)ctx->flags + 4);
-  }
+  KSweepPipe<<<items, kPipeThreads, kPipeSmemBytes, st>>>(A, b, in, out, c0, zero_init, s, T);
   return APHGPU_OK;
 }
 inline dim3 SweepGrid(const Dims& d) {
@@ -1370,12 +1369,12 @@ int BuildHierarchy<double>(aphgpu_ctx* ctx, std::vector<Level<double>>& lv,
   for (size_t l = 1; l < lv.size(); ++l) {
     const Op<double> A = MakeOp(lv[l - 1]);
     CoarsenOp<double, double>(ctx->stream, A, lv[l], CoarseSeries(ctx),
-                              ctx->diag_explicit ? 1 : 0);
+                              ctx->singular ? 0 : 1);
     ctx->launches += 1;  // two kernels
     APH_LAUNCHED(ctx);
   }
   APH_TRY(EnsureCoarsestScratch(ctx, lv.back().d.cells()));
-  ctx->mg.csing64 = ctx->diag_explicit ? 0 : 1;
+  ctx->mg.csing64 = ctx->singular ? 1 : 0;
   APH_TRY(BuildCoarsestInverse(ctx, lv.back(), &ctx->mg.cinv64, &ctx->mg.cn64,
                                ctx->mg.csing64));
   return APHGPU_OK;
@@ -1412,7 +1411,7 @@ int BuildHierarchy<float>(aphgpu_ctx* ctx, std::vector<Level<float>>& lv,
     APH_LAUNCHED(ctx);
   }
   if (!lv[0].diag) APH_TRY(Alloc(ctx, &lv[0].diag, N));
-  if (ctx->diag_explicit) {
+  if (!ctx->singular) {
     KConvert<double, float><<<fb, kFlatThreads, 0, ctx->stream>>>(N, ctx->diag, lv[0].diag, 1.0);
     APH_LAUNCHED(ctx);
     const Op<float> A{lv[0].d, lv[0].w[0], lv[0].w[1], lv[0].w[2], lv[0].diag};
@@ -1423,24 +1422,24 @@ int BuildHierarchy<float>(aphgpu_ctx* ctx, std::vector<Level<float>>& lv,
     KInvDiag<float><<<TileGrid(ctx->d), TileBlock(), 0, ctx->stream>>>(A, lv[0].invdiag);
     APH_LAUNCHED(ctx);
   }
-  lv[0].has_diag = ctx->diag_explicit;
+  lv[0].has_diag = !ctx->singular;
   APH_TRY(BuildHalfCouplings(ctx, lv[0]));
   for (size_t l = 1; l < lv.size(); ++l) {
     // coarse operators from the FP64 fine operator at level 1, FP32 below
     if (l == 1) {
       const Op<double> A = FineOp(ctx);
       CoarsenOp<double, float>(ctx->stream, A, lv[l], CoarseSeries(ctx),
-                              ctx->diag_explicit ? 1 : 0);
+                              ctx->singular ? 0 : 1);
     } else {
       const Op<float> A = MakeOp(lv[l - 1]);
       CoarsenOp<float, float>(ctx->stream, A, lv[l], CoarseSeries(ctx),
-                              ctx->diag_explicit ? 1 : 0);
+                              ctx->singular ? 0 : 1);
     }
     ctx->launches += 1;  // two kernels
     APH_LAUNCHED(ctx);
   }
   APH_TRY(EnsureCoarsestScratch(ctx, lv.back().d.cells()));
-  ctx->mg.csing32 = ctx->diag_explicit ? 0 : 1;
+  ctx->mg.csing32 = ctx->singular ? 1 : 0;
   APH_TRY(BuildCoarsestInverse(ctx, lv.back(), &ctx->mg.cinv32, &ctx->mg.cn32,
                                ctx->mg.csing32));
   return CoarseOneSetup(ctx);
@@ -1695,7 +1694,7 @@ int CycleLevel(aphgpu_ctx* ctx, std::vector<Level<T>>& lv, int l, bool first, in
                                                                              c.x, s, sing);
     } else {
       KCoarsestCG<T><<<1, 1024, 0, st>>>(A, c.b, c.x, mg.cr, mg.cp, mg.cap, mg.cx, s,
-                                         ctx->diag_explicit ? 0 : 1);
+                                         ctx->singular ? 1 : 0);
     }
     APH_LAUNCHED(ctx);
     return APHGPU_OK;
@@ -1810,7 +1809,6 @@ int Pcg(aphgpu_ctx* ctx, const Op<T>& A, Precond precond, T* x, T* r, T* p,
     key = Mix(key, (uint64_t)check_every);
     key = Mix(key, (uint64_t)sizeof(T));
     key = Mix(key, (uint64_t)ctx->fused_mode);
-    key = Mix(key, (uint64_t)ctx->pipe_copies);
     key = Mix(key, (uint64_t)CycleGamma(ctx));
     key = Mix(key, (uint64_t)SweepGrowth(ctx));
     key = Mix(key, (uint64_t)(ctx->use_cta_coarse ? 1 + ctx->mg.clc : 0));
@@ -1888,11 +1886,11 @@ int SetSystemExprDevice(aphgpu_ctx* ctx, const double* d_expr8) {
   APH_TRY(EnsureSolverVectors(ctx));
   if (!ctx->diag) APH_TRY(Alloc(ctx, &ctx->diag, ctx->N));
   unsigned int* flags = ctx->flags;
-  APH_CUDA(ctx, cudaMemsetAsync(flags, 0, 2 * sizeof(unsigned), ctx->stream));
+  APH_CUDA(ctx, cudaMemsetAsync(flags, 0, 3 * sizeof(unsigned), ctx->stream));
   KExprToSystem<<<TileGrid(ctx->d), TileBlock(), 0, ctx->stream>>>(
       ctx->d, d_expr8, ctx->w[0], ctx->w[1], ctx->w[2], ctx->diag, ctx->b, flags);
   APH_LAUNCHED(ctx);
-  unsigned int hf[2] = {0, 0};
+  unsigned int hf[3] = {0, 0, 0};
   APH_CUDA(ctx, cudaMemcpyAsync(hf, flags, sizeof(hf), cudaMemcpyDeviceToHost, ctx->stream));
   APH_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
   if (hf[0]) {
@@ -1901,6 +1899,9 @@ int SetSystemExprDevice(aphgpu_ctx* ctx, const double* d_expr8) {
                     "system is not symmetric in %u couplings", hf[0]);
   }
   ctx->diag_explicit = hf[1] != 0;
+  // singular: every row sum vanishes up to rounding (a flux-difference
+  // system, e.g. aphros's projection system summed in its own order)
+  ctx->singular = hf[2] == 0;
   // diag holds e0: the explicit diagonal, or (flux-difference systems)
   // the value Diag computes from the couplings
   ctx->diag_valid = true;
@@ -1936,6 +1937,7 @@ int ApplyCellCondDevice(aphgpu_ctx* ctx, int64_t count, const int64_t* d_cells,
   // not singular any more, and the FP32 and coarse levels take the stored
   // diagonal
   ctx->diag_explicit = true;
+  if (count > 0) ctx->singular = false;
   ctx->mg.built64 = ctx->mg.built32 = false;
   KInvDiag<double><<<TileGrid(ctx->d), TileBlock(), 0, ctx->stream>>>(FineOp(ctx), ctx->invdiag);
   APH_LAUNCHED(ctx);
@@ -1960,6 +1962,7 @@ int AssembleProjectionDevice(aphgpu_ctx* ctx, const double* d_alpha,
     APH_LAUNCHED(ctx);
   }
   ctx->diag_explicit = false;
+  ctx->singular = true;
   ctx->diag_valid = false;
   if (!ctx->diag) APH_TRY(Alloc(ctx, &ctx->diag, ctx->N));
   KFillDiag<<<TileGrid(ctx->d), TileBlock(), 0, ctx->stream>>>(FineOp(ctx), ctx->diag);
@@ -2161,7 +2164,7 @@ int SolveMixed(aphgpu_ctx* ctx, const aphgpu_conf* conf, aphgpu_info* info) {
     // the constant-mode projection is only valid for the singular
     // flux-difference operator (constant null space), not for systems with
     // an explicit diagonal shift
-    const int flags = ctx->diag_explicit ? (conf->inner_flags & ~1) : conf->inner_flags;
+    const int flags = ctx->singular ? conf->inner_flags : (conf->inner_flags & ~1);
     APH_TRY(InitScalars(ctx, s2, &ic, 1.0, ctx->hist + kHistCap, flags));
     APH_TRY(Pcg<float>(ctx, A32, precond, ctx->x32, ctx->r32, ctx->p32, ctx->ap32,
                        ctx->z32, (conf->inner_flags & 2) ? ctx->zold32 : (float*)nullptr,

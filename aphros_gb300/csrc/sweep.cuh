@@ -1,5 +1,5 @@
-// Fused red-black Gauss-Seidel sweep, out of place, fed by asynchronous bulk
-// copies (TMA) into shared memory.
+// Fused red-black Gauss-Seidel sweep, out of place, with the planes staged
+// in shared memory by asynchronous copies.
 //
 // One sweep updates the first colour c0 of every cell from the old values
 // x_in of the other colour, then the second colour from the new first-colour
@@ -8,31 +8,30 @@
 // b (FP32), and x_out is written once: 24 bytes per cell.
 //
 // Work item: a tile of w <= 128 columns (x) by rows <= kPipeRows rows (y),
-// marching over the planes [kb, ke) (z).  One CTA of 512 threads per SM; the
-// host sizes the tiles so that all items run in one wave, so neighbouring
-// tiles stream the same planes at the same time and the halo rows one tile
-// reads again come from L2.
+// marching over the planes [kb, ke) (z).  Two CTAs of 256 threads per SM
+// (104 KB of shared memory each); the host sizes the tiles so that all
+// items run in one wave, so neighbouring tiles stream the same planes at
+// the same time and the halo rows a tile reads again come from L2.
 //
 // Pipeline (time step t = kb-1 .. ke): F(t), the first colour of plane t on
 // the tile's rows -1..rows and columns -1..w (halo recomputed, never
-// exchanged), into a ring of three planes in shared memory; then S(t-1), the
-// second colour of plane t-1, written with the first colour of that plane
-// to x_out.  The data F(t) needs beyond earlier steps -- x_in of plane t+1,
-// w0 w1 b of plane t, w2 of plane t+1 -- arrive as batch B(t): one row
-// segment per array row, copied by cp.async.bulk from global to shared
-// memory with completion on an mbarrier.  Batch B(t+2) is issued at the
-// start of step t, so two planes of loads are in flight while a plane is
-// computed.  Row segments span columns [i0-4, i0+w+4) (16-byte aligned);
-// the periodic wrap in x splits a segment into two or three copies, the
-// wrap in y and z only changes which row is copied.
+// exchanged), into a ring of three planes; then S(t-1), the second colour
+// of plane t-1, written with the first colour of that plane to x_out.  The
+// data F(t) needs beyond earlier steps -- x_in of plane t+1, w0 w1 b of
+// plane t, w2 of plane t+1 -- form batch B(t): for each array row the
+// segment of columns [i0-4, i0+w+4), copied in 16-byte chunks by cp.async
+// (the periodic wrap in x is per chunk, since nx and i0 are multiples of 4;
+// the wraps in y and z only change which row is read).  Every thread copies
+// its share of a batch and commits it as one group; B(t+2) is issued after
+// S(t-1), so two planes of copies are in flight while a plane is computed,
+// and a batch is complete once every thread has waited for its group
+// (cp.async.wait_group) and the block has passed a barrier.  Each thread
+// waits only for copies it issued itself.
 //
 // Every value is computed by the same operations, in the same order, as in
 // the two in-place half sweeps (Smooth4Body), so results are bit-identical.
 // Requires: nx % 4 == 0, nx >= 16, no stored diagonal (the diagonal is
 // minus the sum of the couplings, as for the projection operator).
-//
-// Waits are bounded: a batch that does not complete within the limit sets
-// *err, the CTA waits (bounded again) for the copies it issued and returns.
 #pragma once
 
 #include <cstdint>
@@ -43,10 +42,11 @@
 namespace aphgpu {
 
 constexpr int kPipeCols = 128;                // columns of a tile at most
-constexpr int kPipeRows = 14;                 // rows of a tile at most
+constexpr int kPipeRows = 7;                  // rows of a tile at most
 constexpr int kPipeStride = kPipeCols + 8;    // floats per staged row
-constexpr int kPipeThreads = 512;
-constexpr int kPipeXs = 5, kPipeCs = 4, kPipeWs = 5, kPipeBars = 3;  // ring sizes
+constexpr int kPipeThreads = 256;
+constexpr int kPipeWarps = kPipeThreads / 32;
+constexpr int kPipeXs = 4, kPipeCs = 3, kPipeWs = 4;  // ring sizes (planes)
 constexpr int kPipeXRows = kPipeRows + 4;     // x_in rows -2 .. rows+1
 constexpr int kPipeW0Rows = kPipeRows + 2;    // w0 rows -1 .. rows
 constexpr int kPipeW1Rows = kPipeRows + 3;    // w1 rows -1 .. rows+1
@@ -57,10 +57,8 @@ constexpr int kPipeFRows = kPipeRows + 2;     // first colour rows -1 .. rows
 constexpr int kPipeSmemFloats =
     kPipeStride * (kPipeXs * kPipeXRows + kPipeCs * kPipeCRows + kPipeWs * kPipeW2Rows +
                    3 * kPipeFRows);
-constexpr int kPipeSmemBytes = kPipeSmemFloats * 4 + kPipeBars * 8;
-// iterations of mbarrier.try_wait (each may suspend the thread for a while)
-// before a batch is given up
-constexpr int kPipeWaitLimit = 1 << 22;
+constexpr int kPipeSmemBytes = kPipeSmemFloats * 4;
+static_assert(2 * (kPipeSmemBytes + 1024) <= 228 * 1024, "two CTAs per SM");
 
 struct PipeTiling {
   int w;       // columns of a tile (multiple of 4, <= kPipeCols)
@@ -72,67 +70,11 @@ __device__ __forceinline__ uint32_t SmemAddr(const void* p) {
   return (uint32_t)__cvta_generic_to_shared(p);
 }
 
-__device__ __forceinline__ void MbarInit(uint64_t* bar, int count) {
-  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(SmemAddr(bar)), "r"(count));
-}
-
-__device__ __forceinline__ void MbarExpectTx(uint64_t* bar, uint32_t bytes) {
-  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(SmemAddr(bar)),
-               "r"(bytes)
-               : "memory");
-}
-
-// true once the phase of `parity` has completed; false after the limit
-__device__ __forceinline__ bool MbarWait(uint64_t* bar, uint32_t parity) {
-  const uint32_t a = SmemAddr(bar);
-  for (int it = 0; it < kPipeWaitLimit; ++it) {
-    uint32_t done = 0;
-    asm volatile(
-        "{\n\t.reg .pred p;\n\t"
-        "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
-        "selp.u32 %0, 1, 0, p;\n\t}"
-        : "=r"(done)
-        : "r"(a), "r"(parity)
-        : "memory");
-    if (done) return true;
-  }
-  return false;
-}
-
-// 1-D bulk copy global -> shared, completion counted on `bar` (bytes: a
-// multiple of 16, both addresses 16-byte aligned)
-__device__ __forceinline__ void BulkG2S(void* dst, const void* src, uint32_t bytes,
-                                        uint64_t* bar) {
-  asm volatile(
-      "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];"
-      ::"r"(SmemAddr(dst)), "l"(src), "r"(bytes), "r"(SmemAddr(bar))
-      : "memory");
-}
-
-// Copies the periodic column range [i0-4, i0+w+4) of one row (row: the
-// row's first element in global memory) to dst (the staged row, local
-// column 0 = global column i0-4); one, two or three bulk copies.
-__device__ __forceinline__ void CopyRowSegment(float* dst, const float* row, int nx, int i0,
-                                               int w, uint64_t* bar) {
-  int s = i0 - 4;
-  int left = w + 8;
-  int off = 0;
-  if (s < 0) s += nx;
-  while (left > 0) {
-    const int n = min(left, nx - s);
-    BulkG2S(dst + off, row + s, 4u * (uint32_t)n, bar);
-    off += n;
-    left -= n;
-    s = 0;
-  }
-}
-
 struct PipeSmem {
   float* xs;   // [kPipeXs][kPipeXRows][stride]
   float* cs;   // [kPipeCs][kPipeCRows][stride]: w0, w1, b
   float* ws;   // [kPipeWs][kPipeW2Rows][stride]
   float* fs;   // [3][kPipeFRows][stride]
-  uint64_t* bars;
 };
 
 __device__ __forceinline__ int PosMod(int a, int m) {
@@ -147,62 +89,6 @@ struct PipeBatch {
   int pc, pc_on;
   int pw[2], nwp;
 };
-
-// Issues a batch (by the 32 lanes of the calling warp) into the ring slots
-// of its planes, completion on `bar`; lane 0 first registers the total
-// bytes.
-__device__ __forceinline__ void IssueBatch(const Op<float>& A, const float* __restrict__ b,
-                                           const float* __restrict__ xin, const PipeSmem& S,
-                                           int base, int i0, int w, int j0, int rows,
-                                           const PipeBatch& B, uint64_t* bar) {
-  const Dims d = A.d;
-  const int lane = threadIdx.x & 31;
-  const int nxr = rows + 4, nc0 = rows + 2, nc1 = rows + 3, nw = rows + 2;
-  const int ncoef = B.pc_on ? nc0 + nc1 + nc0 : 0;
-  const int total = B.nxp * nxr + ncoef + B.nwp * nw;
-  const uint32_t rowb = 4u * (uint32_t)(w + 8);
-  if (lane == 0) MbarExpectTx(bar, rowb * (uint32_t)total);
-  __syncwarp();
-  const int64_t plane = (int64_t)d.nx * d.ny;
-  for (int q = lane; q < total; q += 32) {
-    int t = q;
-    const float* src;
-    float* dst;
-    int r, p;
-    if (t < B.nxp * nxr) {
-      p = B.px[t / nxr];
-      r = t % nxr - 2;
-      src = xin;
-      dst = S.xs + ((size_t)PosMod(p - base, kPipeXs) * kPipeXRows + (r + 2)) * kPipeStride;
-    } else if (t - B.nxp * nxr < ncoef) {
-      t -= B.nxp * nxr;
-      p = B.pc;
-      float* slot = S.cs + (size_t)PosMod(p - base, kPipeCs) * kPipeCRows * kPipeStride;
-      if (t < nc0) {
-        r = t - 1;
-        src = A.w0;
-        dst = slot + (size_t)(r + 1) * kPipeStride;
-      } else if (t < nc0 + nc1) {
-        r = t - nc0 - 1;
-        src = A.w1;
-        dst = slot + (size_t)(kPipeW0Rows + r + 1) * kPipeStride;
-      } else {
-        r = t - nc0 - nc1 - 1;
-        src = b;
-        dst = slot + (size_t)(kPipeW0Rows + kPipeW1Rows + r + 1) * kPipeStride;
-      }
-    } else {
-      t -= B.nxp * nxr + ncoef;
-      p = B.pw[t / nw];
-      r = t % nw - 1;
-      src = A.w2;
-      dst = S.ws + ((size_t)PosMod(p - base, kPipeWs) * kPipeW2Rows + (r + 1)) * kPipeStride;
-    }
-    const int jw = PosMod(j0 + r, d.ny);
-    const int pz = PosMod(p, d.nz);
-    CopyRowSegment(dst, src + pz * plane + (int64_t)jw * d.nx, d.nx, i0, w, bar);
-  }
-}
 
 __device__ __forceinline__ float4 LdS4(const float* p) {
   return *reinterpret_cast<const float4*>(p);
@@ -357,113 +243,6 @@ __device__ __forceinline__ void PipeSecond(const PipeSmem& S, int base, int c0, 
   *reinterpret_cast<float4*>(xout + d.idx(i0 + 4 * g, j, pz)) = out;
 }
 
-// One fused sweep of one work item (grid: one CTA of kPipeThreads per item,
-// dynamic shared memory kPipeSmemBytes).  Item index: blockIdx.x =
-// (zseg * bands + band) * xtiles + xtile.
-__global__ void __launch_bounds__(kPipeThreads, 1)
-    KSweepPipe(Op<float> A, const float* __restrict__ b, const float* __restrict__ xin,
-               float* xout, int c0, int zero_init, const SolveScalars* s, PipeTiling T,
-               int* err) {
-  if (s && s->done) return;
-  extern __shared__ __align__(128) float smem[];
-  const Dims d = A.d;
-  PipeSmem S;
-  S.xs = smem;
-  S.cs = S.xs + (size_t)kPipeXs * kPipeXRows * kPipeStride;
-  S.ws = S.cs + (size_t)kPipeCs * kPipeCRows * kPipeStride;
-  S.fs = S.ws + (size_t)kPipeWs * kPipeW2Rows * kPipeStride;
-  S.bars = reinterpret_cast<uint64_t*>(S.fs + (size_t)3 * kPipeFRows * kPipeStride);
-  const int item = blockIdx.x;
-  const int xt = item % T.xtiles;
-  const int band = (item / T.xtiles) % T.bands;
-  const int zs = item / (T.xtiles * T.bands);
-  const int i0 = xt * T.w;
-  const int w = min(T.w, d.nx - i0);
-  const int j0 = band * T.rows;
-  const int rows = min(T.rows, d.ny - j0);
-  const int kb = (int)((int64_t)d.nz * zs / T.zsegs);
-  const int ke = (int)((int64_t)d.nz * (zs + 1) / T.zsegs);
-  const int warp = threadIdx.x >> 5;
-  if (threadIdx.x == 0) {
-    for (int q = 0; q < kPipeBars; ++q) MbarInit(S.bars + q, 1);
-    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
-  }
-  __syncthreads();
-  const int base = kb - 2;  // ring position 0: plane kb-2
-  const int t0 = kb - 1;    // first time step
-  auto bar_of = [&](int t) { return S.bars + PosMod(t - t0, kPipeBars); };
-  auto parity_of = [&](int t) { return (uint32_t)(((t - t0) / kPipeBars) & 1); };
-  // batch B(t) for t > t0: x_in of plane t+1, coefficients of plane t, w2
-  // of plane t+1; B(t0) also carries x_in of planes t0-1, t0 and w2 of t0
-  auto batch = [&](int t) {
-    PipeBatch B;
-    B.nxp = 0;
-    if (!zero_init) {
-      B.px[B.nxp++] = t + 1;
-      if (t == t0) {
-        B.px[B.nxp++] = t - 1;
-        B.px[B.nxp++] = t;
-      }
-    }
-    B.pc = t;
-    B.pc_on = 1;
-    B.nwp = 0;
-    B.pw[B.nwp++] = t + 1;
-    if (t == t0) B.pw[B.nwp++] = t;
-    return B;
-  };
-  if (warp == 0) {
-    for (int t = t0; t <= min(t0 + 2, ke); ++t)
-      IssueBatch(A, b, xin, S, base, i0, w, j0, rows, batch(t), bar_of(t));
-  }
-  bool ok = MbarWait(bar_of(t0), parity_of(t0));
-  int failed = __syncthreads_or(!ok);
-  int t_issued = min(t0 + 2, ke);  // last batch issued
-  int t_wait = t0;                 // batch of the last wait
-  for (int t = t0; t <= ke && !failed; ++t) {
-    // B(t+2) into the slots of plane t-2, free since the end of step t-1
-    if (warp == 0 && t + 2 <= ke && t > t0) {
-      asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-      IssueBatch(A, b, xin, S, base, i0, w, j0, rows, batch(t + 2), bar_of(t + 2));
-    }
-    if (t + 2 <= ke) t_issued = t + 2;
-    // F(t): warps 0 .. rows+1 take rows -1 .. rows
-    if (warp < rows + 2) PipeFirst(S, base, c0, zero_init, i0, w, j0, warp - 1, t, d.ny, d.nz);
-    __syncthreads();
-    // S(t-1)
-    if (t - 1 >= kb && warp < rows) PipeSecond(S, base, c0, i0, w, j0, warp, t - 1, d, xout);
-    // data of the next step
-    ok = true;
-    if (t + 1 <= ke) {
-      t_wait = t + 1;
-      ok = MbarWait(bar_of(t + 1), parity_of(t + 1));
-    }
-    failed = __syncthreads_or(!ok);
-  }
-  if (failed) {
-    if (threadIdx.x == 0) {
-      atomicExch(err, 1);
-      // the batches issued but not seen complete (from the one whose wait
-      // gave up): wait (bounded) for their copies before the shared memory
-      // goes away
-      for (int t = t_wait; t <= t_issued; ++t) MbarWait(bar_of(t), parity_of(t));
-    }
-    __syncthreads();
-  }
-}
-
-// ---------------------------------------------------------------------------
-// The same sweep with the rows staged by per-thread asynchronous copies
-// (cp.async, 16 bytes each) instead of bulk copies: every thread of the
-// CTA copies its share of the batch's 16-byte chunks (a row segment
-// [i0-4, i0+w+4) is (w+8)/4 chunks; the periodic wrap in x is per chunk,
-// since nx and i0 are multiples of 4) and commits them as one group; a
-// batch is complete once every thread has waited for its group
-// (cp.async.wait_group) and the block has passed a barrier.  No mbarrier
-// and no bounded wait is involved: each thread waits only for its own
-// copies.
-// ---------------------------------------------------------------------------
-
 __device__ __forceinline__ void CpAsync16(void* dst, const void* src) {
   asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(SmemAddr(dst)), "l"(src)
                : "memory");
@@ -530,10 +309,93 @@ __device__ __forceinline__ void IssueBatchAsync(const Op<float>& A, const float*
   CpAsyncCommit();
 }
 
-// KSweepPipe with cp.async staging (same tiling, rings and arithmetic).
-__global__ void __launch_bounds__(kPipeThreads, 1)
-    KSweepPipeAsync(Op<float> A, const float* __restrict__ b, const float* __restrict__ xin,
-                    float* xout, int c0, int zero_init, const SolveScalars* s, PipeTiling T) {
+// Chunks of a steady-state batch B(t) (x_in of plane t+1, w0 w1 b of plane
+// t, w2 of plane t+1) owned by one thread: at most kPipeOwn chunks, each
+// described once per work item by its array, its offset inside a plane of
+// that array and its offset inside the ring slot; a step then only adds
+// the planes' offsets.
+constexpr int kPipeOwn = 8;
+static_assert((5 * kPipeRows + 13) * ((kPipeCols + 8) / 4) <= kPipeOwn * kPipeThreads,
+              "a steady batch has more chunks than the threads own");
+struct PipeChunks {
+  int n;
+  int kind[kPipeOwn];     // 0 x, 1 w0, 2 w1, 3 b, 4 w2
+  int goff[kPipeOwn];     // row * nx + column (wrapped) inside the plane
+  int soff[kPipeOwn];     // offset inside the ring slot (floats)
+};
+
+__device__ __forceinline__ void PipeChunksInit(const Dims& d, int i0, int w, int j0, int rows,
+                                               int zero_init, PipeChunks& C) {
+  const int nxr = rows + 4, nc0 = rows + 2, nc1 = rows + 3, nw = rows + 2;
+  const int nxp = zero_init ? 0 : 1;
+  const int total = nxp * nxr + nc0 + nc1 + nc0 + nw;
+  const int cpr = (w + 8) / 4;
+  C.n = 0;
+  for (int q = threadIdx.x; q < total * cpr && C.n < kPipeOwn; q += blockDim.x) {
+    int t = q / cpr;
+    const int ch = q - t * cpr;
+    int kind, r, srow;
+    if (t < nxp * nxr) {
+      kind = 0;
+      r = t - 2;
+      srow = r + 2;
+    } else if ((t -= nxp * nxr) < nc0) {
+      kind = 1;
+      r = t - 1;
+      srow = r + 1;
+    } else if ((t -= nc0) < nc1) {
+      kind = 2;
+      r = t - 1;
+      srow = kPipeW0Rows + r + 1;
+    } else if ((t -= nc1) < nc0) {
+      kind = 3;
+      r = t - 1;
+      srow = kPipeW0Rows + kPipeW1Rows + r + 1;
+    } else {
+      t -= nc0;
+      kind = 4;
+      r = t - 1;
+      srow = r + 1;
+    }
+    const int jw = PosMod(j0 + r, d.ny);
+    const int col = PosMod(i0 - 4 + 4 * ch, d.nx);
+    C.kind[C.n] = kind;
+    C.goff[C.n] = jw * d.nx + col;
+    C.soff[C.n] = srow * kPipeStride + 4 * ch;
+    ++C.n;
+  }
+}
+
+// Steady-state batch B(t) from the thread's precomputed chunks.
+__device__ __forceinline__ void IssueSteadyAsync(const Op<float>& A, const float* __restrict__ b,
+                                                 const float* __restrict__ xin,
+                                                 const PipeSmem& S, int base, int t,
+                                                 const PipeChunks& C) {
+  const Dims d = A.d;
+  const int64_t plane = (int64_t)d.nx * d.ny;
+  const int64_t px = (int64_t)PosMod(t + 1, d.nz) * plane;  // x, w2
+  const int64_t pc = (int64_t)PosMod(t, d.nz) * plane;      // w0, w1, b
+  float* xs = S.xs + (size_t)PosMod(t + 1 - base, kPipeXs) * kPipeXRows * kPipeStride;
+  float* cs = S.cs + (size_t)PosMod(t - base, kPipeCs) * kPipeCRows * kPipeStride;
+  float* ws = S.ws + (size_t)PosMod(t + 1 - base, kPipeWs) * kPipeW2Rows * kPipeStride;
+#pragma unroll
+  for (int q = 0; q < kPipeOwn; ++q) {
+    if (q >= C.n) break;
+    const int k = C.kind[q];
+    const float* src = k == 0 ? xin + px : k == 1 ? A.w0 + pc : k == 2 ? A.w1 + pc
+                     : k == 3 ? b + pc : A.w2 + px;
+    float* dst = k == 0 ? xs : k == 4 ? ws : cs;
+    CpAsync16(dst + C.soff[q], src + C.goff[q]);
+  }
+  CpAsyncCommit();
+}
+
+// One fused sweep of one work item (grid: one CTA of kPipeThreads per item,
+// dynamic shared memory kPipeSmemBytes).  Item index: blockIdx.x =
+// (zseg * bands + band) * xtiles + xtile.
+__global__ void __launch_bounds__(kPipeThreads, 2)
+    KSweepPipe(Op<float> A, const float* __restrict__ b, const float* __restrict__ xin,
+               float* xout, int c0, int zero_init, const SolveScalars* s, PipeTiling T) {
   if (s && s->done) return;
   extern __shared__ __align__(128) float smem[];
   const Dims d = A.d;
@@ -542,7 +404,6 @@ __global__ void __launch_bounds__(kPipeThreads, 1)
   S.cs = S.xs + (size_t)kPipeXs * kPipeXRows * kPipeStride;
   S.ws = S.cs + (size_t)kPipeCs * kPipeCRows * kPipeStride;
   S.fs = S.ws + (size_t)kPipeWs * kPipeW2Rows * kPipeStride;
-  S.bars = nullptr;
   const int item = blockIdx.x;
   const int xt = item % T.xtiles;
   const int band = (item / T.xtiles) % T.bands;
@@ -554,48 +415,45 @@ __global__ void __launch_bounds__(kPipeThreads, 1)
   const int kb = (int)((int64_t)d.nz * zs / T.zsegs);
   const int ke = (int)((int64_t)d.nz * (zs + 1) / T.zsegs);
   const int warp = threadIdx.x >> 5;
-  const int base = kb - 2;
-  const int t0 = kb - 1;
-  auto batch = [&](int t) {
-    PipeBatch B;
-    B.nxp = 0;
-    if (!zero_init) {
-      B.px[B.nxp++] = t + 1;
-      if (t == t0) {
-        B.px[B.nxp++] = t - 1;
-        B.px[B.nxp++] = t;
-      }
-    }
-    B.pc = t;
-    B.pc_on = 1;
-    B.nwp = 0;
-    B.pw[B.nwp++] = t + 1;
-    if (t == t0) B.pw[B.nwp++] = t;
-    return B;
-  };
-  // prologue: B(t0), B(t0+1), B(t0+2); a batch past ke is an empty group
-  for (int t = t0; t <= t0 + 2; ++t) {
-    if (t <= ke)
-      IssueBatchAsync(A, b, xin, S, base, i0, w, j0, rows, batch(t));
-    else
-      CpAsyncCommit();
+  const int base = kb - 2;  // ring position 0: plane kb-2
+  const int t0 = kb - 1;    // first time step
+  // batch B(t0): x_in of planes t0-1 .. t0+1, coefficients of t0, w2 of
+  // t0 and t0+1; later batches come from the precomputed chunks
+  PipeBatch B0;
+  B0.nxp = 0;
+  if (!zero_init) {
+    B0.px[B0.nxp++] = t0 + 1;
+    B0.px[B0.nxp++] = t0 - 1;
+    B0.px[B0.nxp++] = t0;
   }
-  CpAsyncWait<2>();
+  B0.pc = t0;
+  B0.pc_on = 1;
+  B0.nwp = 0;
+  B0.pw[B0.nwp++] = t0 + 1;
+  B0.pw[B0.nwp++] = t0;
+  PipeChunks C;
+  PipeChunksInit(d, i0, w, j0, rows, zero_init, C);
+  IssueBatchAsync(A, b, xin, S, base, i0, w, j0, rows, B0);
+  if (t0 + 1 <= ke)
+    IssueSteadyAsync(A, b, xin, S, base, t0 + 1, C);
+  else
+    CpAsyncCommit();
+  CpAsyncWait<1>();  // B(t0)
   __syncthreads();
   for (int t = t0; t <= ke; ++t) {
-    // F(t): warps 0 .. rows+1 take rows -1 .. rows
-    if (warp < rows + 2) PipeFirst(S, base, c0, zero_init, i0, w, j0, warp - 1, t, d.ny, d.nz);
+    // F(t): rows -1 .. rows over the warps
+    for (int r = warp - 1; r <= rows; r += kPipeWarps)
+      PipeFirst(S, base, c0, zero_init, i0, w, j0, r, t, d.ny, d.nz);
     __syncthreads();
     if (t - 1 >= kb && warp < rows) PipeSecond(S, base, c0, i0, w, j0, warp, t - 1, d, xout);
-    // the slots of plane t-1 (coefficients, w2) and t-2 (x) are free once
-    // every thread is past S(t-1): then B(t+3) may overwrite them
+    // the slots of x_in plane t-1 and of the coefficients and w2 of plane
+    // t-1 are free once every thread is past S(t-1): B(t+2) goes there
     __syncthreads();
-    if (t + 3 <= ke)
-      IssueBatchAsync(A, b, xin, S, base, i0, w, j0, rows, batch(t + 3));
+    if (t + 2 <= ke)
+      IssueSteadyAsync(A, b, xin, S, base, t + 2, C);
     else
       CpAsyncCommit();
-    // B(t+1) complete (B(t+2), B(t+3) may stay in flight)
-    CpAsyncWait<2>();
+    CpAsyncWait<1>();  // B(t+1) complete, B(t+2) may stay in flight
     __syncthreads();
   }
   CpAsyncWait<0>();

@@ -425,7 +425,7 @@ int aphgpu_batch_last_ms(const aphgpu_batch* batch, double* ms, int64_t* launche
  *   APHGPU_OPT_FUSED_SWEEPS  fused out-of-place red-black sweeps (both
  *                            colours in one pass: half the DRAM traffic of
  *                            two half sweeps) on the FP32 levels: 1
- *                            the pipelined kernel, fed by bulk
+ *                            the pipelined kernel, fed by asynchronous
  *                            copies into shared memory, on levels of at
  *                            least 2^21 cells with nx a multiple of 4 and
  *                            no stored diagonal; 2 the pipelined kernel on
@@ -435,10 +435,6 @@ int aphgpu_batch_last_ms(const aphgpu_batch* batch, double* ms, int64_t* launche
  *                            0 (default) two in-place half sweeps
  *                            everywhere.  Other
  *                            levels take the half sweeps
- *   APHGPU_OPT_PIPE_COPIES   staging of the pipelined fused sweep: 0
- *                            (default) bulk copies (cp.async.bulk) counted
- *                            on mbarriers, 1 per-thread 16-byte cp.async
- *                            copies; the results are the same
  *   APHGPU_OPT_HALF_COUPLINGS 1: the smoother and the restriction of the
  *                            finest FP32 level read an FP16 copy of the
  *                            couplings scaled by a power of two (the PCG
@@ -476,8 +472,7 @@ enum {
   APHGPU_OPT_CYCLE = 3,
   APHGPU_OPT_COARSE_SERIES = 4,
   APHGPU_OPT_SWEEP_GROWTH = 5,
-  APHGPU_OPT_CTA_COARSE = 6,
-  APHGPU_OPT_PIPE_COPIES = 7
+  APHGPU_OPT_CTA_COARSE = 6
 };
 int aphgpu_set_option(aphgpu_ctx* ctx, int option, int value);
 
