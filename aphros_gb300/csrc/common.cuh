@@ -264,6 +264,9 @@ struct aphgpu_ctx {
   // every row sum vanishes (periodic flux-difference system: the constant
   // null space); false with diagonal shifts (diffusion, given pressures)
   bool singular = true;
+  // the stored system is the negation of the one set (negative definite
+  // input): readbacks negate it again
+  bool negated = false;
   bool diag_valid = false;  // `diag` holds the FP64 diagonal (explicit or computed)
   bool x_zero = false;      // x was zeroed for the solve being run
   double* invdiag = nullptr;   // 1/diagonal (multigrid smoother)

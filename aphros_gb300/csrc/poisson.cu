@@ -69,11 +69,12 @@ __device__ __forceinline__ double S(double a, double b) { return __dsub_rn(a, b)
 
 // flags[0]: asymmetric cells, flags[1]: cells whose e0 != -(sum of e_q),
 // flags[2]: cells whose row sum e0 + sum of e_q is more than rounding
-// (a diagonal shift: the system is not singular)
+// (a diagonal shift: the system is not singular), flags[3]: cells with a
+// negative diagonal
 __global__ void KExprToSystem(Dims d, const double* __restrict__ e8,
                               double* w0, double* w1, double* w2, double* diag,
                               double* b, unsigned int* flags) {
-  unsigned int asym = 0, nonpure = 0, shifted = 0;
+  unsigned int asym = 0, nonpure = 0, shifted = 0, negative = 0;
   TILE_LOOP_BEGIN(d)
   const double* e = e8 + 8 * c;
   w0[c] = e[1];
@@ -92,10 +93,28 @@ __global__ void KExprToSystem(Dims d, const double* __restrict__ e8,
   }
   if (e[0] != -s) ++nonpure;
   if (!(fabs(e[0] + s) <= 1e-10 * mag)) ++shifted;
+  if (e[0] < 0) ++negative;
   TILE_LOOP_END
   if (asym) atomicAdd(&flags[0], asym);
   if (nonpure) atomicAdd(&flags[1], nonpure);
   if (shifted) atomicAdd(&flags[2], shifted);
+  if (negative) atomicAdd(&flags[3], negative);
+}
+
+// The system negated in place (couplings, diagonal, right-hand side): a
+// negative definite system (aphros's own assembly without Proj's sign, as
+// in its linear-solver test) becomes the positive definite one with the
+// same solution and the same residual norms.
+__global__ void KNegateSystem(int64_t n, double* w0, double* w1, double* w2, double* diag,
+                              double* b) {
+  for (int64_t c = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; c < n;
+       c += (int64_t)gridDim.x * blockDim.x) {
+    w0[c] = -w0[c];
+    w1[c] = -w1[c];
+    w2[c] = -w2[c];
+    diag[c] = -diag[c];
+    b[c] = -b[c];
+  }
 }
 
 // Face coefficients and predicted fluxes (proj.ipp:343-360, 556-562):
@@ -168,20 +187,20 @@ __global__ void KRemoveMean(int64_t n, double* b, const double* sum) {
 // Expr of every cell from the compact storage (inverse of KExprToSystem):
 // e0 as GetFluxSum accumulates it when no explicit diagonal is stored.
 __global__ void KSystemToExpr(Op<double> Aop, const double* __restrict__ b,
-                              double* e8) {
+                              double* e8, double sign) {
   TILE_LOOP_BEGIN(Aop.d)
   double e[6];
   Couplings(Aop, i, j, k, c, e);
   double* o = e8 + 8 * c;
   if (Aop.diag) {
-    o[0] = Aop.diag[c];
+    o[0] = sign * Aop.diag[c];
   } else {
     double s = 0;
     for (int q = 0; q < 6; ++q) s = A(s, -e[q]);
-    o[0] = s;
+    o[0] = sign * s;
   }
-  for (int q = 0; q < 6; ++q) o[1 + q] = e[q];
-  o[7] = -b[c];
+  for (int q = 0; q < 6; ++q) o[1 + q] = sign * e[q];
+  o[7] = -sign * b[c];
   TILE_LOOP_END
 }
 
@@ -1886,11 +1905,11 @@ int SetSystemExprDevice(aphgpu_ctx* ctx, const double* d_expr8) {
   APH_TRY(EnsureSolverVectors(ctx));
   if (!ctx->diag) APH_TRY(Alloc(ctx, &ctx->diag, ctx->N));
   unsigned int* flags = ctx->flags;
-  APH_CUDA(ctx, cudaMemsetAsync(flags, 0, 3 * sizeof(unsigned), ctx->stream));
+  APH_CUDA(ctx, cudaMemsetAsync(flags, 0, 4 * sizeof(unsigned), ctx->stream));
   KExprToSystem<<<TileGrid(ctx->d), TileBlock(), 0, ctx->stream>>>(
       ctx->d, d_expr8, ctx->w[0], ctx->w[1], ctx->w[2], ctx->diag, ctx->b, flags);
   APH_LAUNCHED(ctx);
-  unsigned int hf[3] = {0, 0, 0};
+  unsigned int hf[4] = {0, 0, 0, 0};
   APH_CUDA(ctx, cudaMemcpyAsync(hf, flags, sizeof(hf), cudaMemcpyDeviceToHost, ctx->stream));
   APH_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
   if (hf[0]) {
@@ -1902,6 +1921,15 @@ int SetSystemExprDevice(aphgpu_ctx* ctx, const double* d_expr8) {
   // singular: every row sum vanishes up to rounding (a flux-difference
   // system, e.g. aphros's projection system summed in its own order)
   ctx->singular = hf[2] == 0;
+  // negative definite (every diagonal negative): solved as the negated,
+  // positive definite system (the multigrid's smoothers and coarsest
+  // solve assume positive diagonals); same solution, same residual norms
+  ctx->negated = hf[3] == (unsigned)ctx->N;
+  if (ctx->negated) {
+    KNegateSystem<<<FlatBlocks(ctx->N), kFlatThreads, 0, ctx->stream>>>(
+        ctx->N, ctx->w[0], ctx->w[1], ctx->w[2], ctx->diag, ctx->b);
+    APH_LAUNCHED(ctx);
+  }
   // diag holds e0: the explicit diagonal, or (flux-difference systems)
   // the value Diag computes from the couplings
   ctx->diag_valid = true;
@@ -1914,23 +1942,25 @@ int SetSystemExprDevice(aphgpu_ctx* ctx, const double* d_expr8) {
 }
 
 // Proj::ApplyCellCond (proj.ipp:326-338) for given-pressure cells:
-// e[0] += 1 and e[7] -= pc, i.e. diag += 1 and b += pc (b = -e[7]); each
-// listed cell at most once.
+// e[0] += 1 and e[7] -= pc, i.e. diag += 1 and b += pc (b = -e[7]), both
+// times sign (-1 when the stored system is the negation of the one set);
+// each listed cell at most once.
 __global__ void KCellCond(int64_t count, const int64_t* __restrict__ cells,
-                          const double* __restrict__ values, double* diag, double* b) {
+                          const double* __restrict__ values, double* diag, double* b,
+                          double sign) {
   for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < count;
        t += (int64_t)gridDim.x * blockDim.x) {
     const int64_t c = cells[t];
-    diag[c] += 1.;
-    b[c] += values[t];
+    diag[c] += sign;
+    b[c] += sign * values[t];
   }
 }
 
 int ApplyCellCondDevice(aphgpu_ctx* ctx, int64_t count, const int64_t* d_cells,
                         const double* d_values) {
   if (count > 0) {
-    KCellCond<<<FlatBlocks(count), kFlatThreads, 0, ctx->stream>>>(count, d_cells, d_values,
-                                                                   ctx->diag, ctx->b);
+    KCellCond<<<FlatBlocks(count), kFlatThreads, 0, ctx->stream>>>(
+        count, d_cells, d_values, ctx->diag, ctx->b, ctx->negated ? -1.0 : 1.0);
     APH_LAUNCHED(ctx);
   }
   // the diagonal is no longer minus the sum of the couplings: the system is
@@ -1963,6 +1993,7 @@ int AssembleProjectionDevice(aphgpu_ctx* ctx, const double* d_alpha,
   }
   ctx->diag_explicit = false;
   ctx->singular = true;
+  ctx->negated = false;
   ctx->diag_valid = false;
   if (!ctx->diag) APH_TRY(Alloc(ctx, &ctx->diag, ctx->N));
   KFillDiag<<<TileGrid(ctx->d), TileBlock(), 0, ctx->stream>>>(FineOp(ctx), ctx->diag);
@@ -2308,7 +2339,8 @@ int TimeSolverKernel(aphgpu_ctx* ctx, int kernel, int reps, double* ms,
 }
 
 int SystemToExprDevice(aphgpu_ctx* ctx, double* d_e8) {
-  KSystemToExpr<<<TileGrid(ctx->d), TileBlock(), 0, ctx->stream>>>(FineOp(ctx), ctx->b, d_e8);
+  KSystemToExpr<<<TileGrid(ctx->d), TileBlock(), 0, ctx->stream>>>(
+      FineOp(ctx), ctx->b, d_e8, ctx->negated ? -1.0 : 1.0);
   APH_LAUNCHED(ctx);
   return APHGPU_OK;
 }

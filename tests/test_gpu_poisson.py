@@ -187,6 +187,30 @@ def test_diffusion_type_system(solver):
     assert np.linalg.norm(x - xo) / np.linalg.norm(xo) < 1e-9
 
 
+@pytest.mark.parametrize("solver", [_lib.SOLVER_CG, _lib.SOLVER_MGPCG, _lib.SOLVER_MIXED])
+@pytest.mark.parametrize("shift", [0.0, 0.5])
+def test_negative_definite_system(solver, shift):
+    """aphros's own Laplacian has a negative diagonal and positive couplings
+    (its linear-solver test assembles it so): the system is stored negated,
+    which leaves the solution and the residual norms unchanged, and reads
+    back as it was set."""
+    n, h = 16, 1 / 16
+    e = _diffusion_system(n, shift=shift).reshape(-1, 8)
+    if shift == 0:  # singular: a consistent right-hand side
+        e[:, 7] -= e[:, 7].mean()
+    e = e.ravel()
+    tol = oracle.rel_tol(e, h, 1e-11)
+    xo, _ = oracle.cg_solve(n, h, e, tol)
+    ctx = _lib.Context(n, h)
+    ctx.set_system_expr(-e)
+    assert np.array_equal(ctx.get_system_expr(), -e)
+    x, info = ctx.solve(_lib.default_conf(solver=solver, tol=tol, maxiter=5000))
+    assert info.converged
+    if shift == 0:  # singular: the solution up to a constant
+        x = x - x.mean() + xo.mean()
+    assert np.linalg.norm(x - xo) / np.linalg.norm(xo) < 1e-9
+
+
 @pytest.mark.parametrize("n", [24, 48])
 def test_c1_sizes_and_warm_start(n):
     """Non-power-of-two grids coarsen to small odd levels; a warm start from
