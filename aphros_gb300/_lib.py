@@ -34,7 +34,7 @@ K_VOF_FLUX, K_VOF_UPDATE, K_RECONSTRUCT, K_HEIGHTS, K_CURVATURE = 5, 6, 7, 8, 9
 K_SWEEP32 = 10
 KERNEL_NAMES = {0: "KSmooth<float>", 1: "KSmooth<double>", 2: "KPcgApply<double>",
                 3: "KPcgApply<float>", 4: "KResidualRestrict<float>",
-                5: "KSweepFlux", 6: "KSweepUpdate", 7: "KReconstruct",
+                5: "KSweepFluxList", 6: "KSweepFused", 7: "KReconstruct",
                 8: "KHeights", 9: "KCurvature", 10: "KSweepPipe"}
 
 SOLVER_CG = 0

@@ -250,6 +250,7 @@ int EnsureVof(aphgpu_ctx* ctx) {
   if (N >= INT32_MAX)
     return SetError(ctx, APHGPU_ERR_UNSUPPORTED, "VOF needs fewer than 2^31 cells");
   APH_TRY(Alloc(ctx, &ctx->u, N));
+  APH_TRY(Alloc(ctx, &ctx->u_alt, N));
   APH_TRY(Alloc(ctx, &ctx->u0, N));
   APH_TRY(Alloc(ctx, &ctx->nrm, 3 * N));
   APH_TRY(Alloc(ctx, &ctx->pa, N));
@@ -815,7 +816,7 @@ int aphgpu_set_option(aphgpu_ctx* ctx, int option, int value) {
   switch (option) {
     case APHGPU_OPT_GRAPHS: ctx->use_graphs = value != 0; return APHGPU_OK;
     case APHGPU_OPT_FUSED_SWEEPS:
-      if (value < 0 || value > 3) return SetError(ctx, APHGPU_ERR_ARG, "fused sweeps %d", value);
+      if (value < 0 || value > 4) return SetError(ctx, APHGPU_ERR_ARG, "fused sweeps %d", value);
       if (value != ctx->fused_mode) ctx->mg.built32 = false;  // scratch of the levels
       ctx->fused_mode = value;
       return APHGPU_OK;

@@ -306,6 +306,8 @@ struct aphgpu_ctx {
 
   // VOF state
   double* u = nullptr;
+  double* u_alt = nullptr;     // N, written by each directional update, then
+                               // exchanged with u
   double* u0 = nullptr;
   double* nrm = nullptr;       // 3N AoS
   double* pa = nullptr;        // plane constant

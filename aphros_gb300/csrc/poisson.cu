@@ -504,26 +504,43 @@ __global__ void __launch_bounds__(256, 3) KSweepRB4(Op<float> A, const float* __
 inline bool FusedOk(const Dims& d) { return VecOk(d); }
 
 // The pipelined fused sweep (sweep.cuh): levels of at least kPipeMinCells
-// cells by default; every level with nx % 4 == 0 and nx >= 16 in mode 2.
+// cells in mode 1; every level with nx % 4 == 0, nx >= 16 and nz >= 8 in
+// mode 2.
 constexpr int64_t kPipeMinCells = int64_t(1) << 21;
-inline bool PipeDims(const Dims& d) { return (d.nx % 4) == 0 && d.nx >= 16; }
+inline bool PipeDims(const Dims& d) {
+  return (d.nx % 4) == 0 && d.nx >= 16 && d.ny >= 2 && d.nz >= 8;
+}
 inline bool PipeEligible(const aphgpu_ctx* ctx, const Dims& d) {
   if (!PipeDims(d)) return false;
-  return ctx->fused_mode == 2 || (ctx->fused_mode == 1 && d.cells() >= kPipeMinCells);
+  return ctx->fused_mode == 2 ||
+         ((ctx->fused_mode == 1 || ctx->fused_mode == 4) && d.cells() >= kPipeMinCells);
 }
 // Tiles of the pipelined sweep: columns of at most kPipeCols (balanced),
-// bands of at most kPipeRows rows (balanced), and z segments so that the
-// items fill the `slots` resident CTAs in one wave (at least 8 planes a
-// segment).
-inline PipeTiling PipeTiles(const Dims& d, int slots) {
+// bands of at most `maxrows` rows (balanced), and z segments (at least 8
+// planes each) so that the items fill the `slots` resident CTAs in as few
+// waves as possible, the last one as full as possible.
+inline PipeTiling PipeTiles(const Dims& d, int slots, int maxrows) {
   PipeTiling T;
   T.xtiles = (d.nx + kPipeCols - 1) / kPipeCols;
   T.w = 4 * ((d.nx / 4 + T.xtiles - 1) / T.xtiles);
-  T.bands = (d.ny + kPipeRows - 1) / kPipeRows;
+  T.bands = (d.ny + maxrows - 1) / maxrows;
   T.rows = (d.ny + T.bands - 1) / T.bands;
   T.bands = (d.ny + T.rows - 1) / T.rows;
   const int tiles = T.xtiles * T.bands;
-  T.zsegs = std::max(1, std::min(d.nz / 8, slots / std::max(tiles, 1)));
+  T.zsegs = 1;
+  double best = 0;
+  for (int z = 1; z <= std::max(1, d.nz / 8); ++z) {
+    const int64_t items = (int64_t)tiles * z;
+    const int64_t waves = (items + slots - 1) / slots;
+    // fill of the waves, with a small cost per segment (each restarts the
+    // pipeline: about 3 extra planes of copies per segment)
+    const double fill = (double)items / (double)(waves * slots);
+    const double seg = (double)(d.nz / z) / (double)(d.nz / z + 3);
+    if (fill * seg > best * 1.0001) {
+      best = fill * seg;
+      T.zsegs = z;
+    }
+  }
   return T;
 }
 inline int SmCount(aphgpu_ctx* ctx) {
@@ -535,21 +552,36 @@ inline int SmCount(aphgpu_ctx* ctx) {
   }
   return sms;
 }
-// one pipelined sweep in -> out (first colour c0)
-inline int LaunchPipe(aphgpu_ctx* ctx, const Op<float>& A, const float* b, const float* in,
-                      float* out, int c0, int zero_init, const SolveScalars* s,
-                      cudaStream_t st) {
+// one pipelined sweep in -> out (first colour c0) with the kernel shape P
+template <class P>
+inline int LaunchPipeShape(aphgpu_ctx* ctx, const Op<float>& A, const float* b,
+                           const float* in, float* out, int c0, int zero_init,
+                           const SolveScalars* s, cudaStream_t st) {
   static bool attr_set[64] = {};
   const int dev = ctx->device;
   if (dev >= 0 && dev < 64 && !attr_set[dev]) {
-    APH_CUDA(ctx, cudaFuncSetAttribute(KSweepPipe, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                       kPipeSmemBytes));
+    APH_CUDA(ctx, cudaFuncSetAttribute(KSweepPipe<P, 0>,
+                                       cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                       P::kSmemBytes));
+    APH_CUDA(ctx, cudaFuncSetAttribute(KSweepPipe<P, 1>,
+                                       cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                       P::kSmemBytes));
     attr_set[dev] = true;
   }
-  const PipeTiling T = PipeTiles(A.d, 2 * SmCount(ctx));
+  const PipeTiling T = PipeTiles(A.d, P::kCtasPerSm * SmCount(ctx), P::kRows);
   const int items = T.xtiles * T.bands * T.zsegs;
-  KSweepPipe<<<items, kPipeThreads, kPipeSmemBytes, st>>>(A, b, in, out, c0, zero_init, s, T);
+  if (zero_init)
+    KSweepPipe<P, 1><<<items, P::kThreads, P::kSmemBytes, st>>>(A, b, in, out, c0, s, T);
+  else
+    KSweepPipe<P, 0><<<items, P::kThreads, P::kSmemBytes, st>>>(A, b, in, out, c0, s, T);
   return APHGPU_OK;
+}
+inline int LaunchPipe(aphgpu_ctx* ctx, const Op<float>& A, const float* b, const float* in,
+                      float* out, int c0, int zero_init, const SolveScalars* s,
+                      cudaStream_t st) {
+  if (ctx->fused_mode == 4)
+    return LaunchPipeShape<PipeShort>(ctx, A, b, in, out, c0, zero_init, s, st);
+  return LaunchPipeShape<PipeTall>(ctx, A, b, in, out, c0, zero_init, s, st);
 }
 inline dim3 SweepGrid(const Dims& d) {
   const int nq = d.nx / 4;

@@ -42,7 +42,7 @@ using Clock = std::chrono::steady_clock;
 
 // device bytes per cell of a resident simulation (FP64 system, solver and
 // VOF state, FP32 hierarchy), used before its first step measures it
-constexpr double kBytesPerCellEstimate = 440.0;
+constexpr double kBytesPerCellEstimate = 448.0;
 
 struct Sim {
   int id = 0;

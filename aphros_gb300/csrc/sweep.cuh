@@ -7,31 +7,39 @@
 // every array is read once from HBM: x_in, the three couplings w0 w1 w2 and
 // b (FP32), and x_out is written once: 24 bytes per cell.
 //
-// Work item: a tile of w <= 128 columns (x) by rows <= kPipeRows rows (y),
-// marching over the planes [kb, ke) (z).  Two CTAs of 256 threads per SM
-// (104 KB of shared memory each); the host sizes the tiles so that all
-// items run in one wave, so neighbouring tiles stream the same planes at
-// the same time and the halo rows a tile reads again come from L2.
+// Work item: a tile of w <= 128 columns (x, one float4 per lane) by rows <=
+// kPipeRows rows (y), marching over the planes [kb, ke) (z).  One CTA of
+// kPipeRows + 2 warps per SM (the staged rings take 213 KB of shared
+// memory); the host sizes the tiles so that all items run in one wave, so
+// neighbouring tiles stream the same planes at the same time and the halo
+// rows a tile reads again come from L2.
 //
-// Pipeline (time step t = kb-1 .. ke): F(t), the first colour of plane t on
-// the tile's rows -1..rows and columns -1..w (halo recomputed, never
-// exchanged), into a ring of three planes; then S(t-1), the second colour
-// of plane t-1, written with the first colour of that plane to x_out.  The
-// data F(t) needs beyond earlier steps -- x_in of plane t+1, w0 w1 b of
-// plane t, w2 of plane t+1 -- form batch B(t): for each array row the
-// segment of columns [i0-4, i0+w+4), copied in 16-byte chunks by cp.async
-// (the periodic wrap in x is per chunk, since nx and i0 are multiples of 4;
-// the wraps in y and z only change which row is read).  Every thread copies
-// its share of a batch and commits it as one group; B(t+2) is issued after
-// S(t-1), so two planes of copies are in flight while a plane is computed,
-// and a batch is complete once every thread has waited for its group
-// (cp.async.wait_group) and the block has passed a barrier.  Each thread
-// waits only for copies it issued itself.
+// Time step t (kb-1 .. ke):
+//   F(t)  warp v updates the first colour of row v-1 (rows -1 .. rows) of
+//         plane t, in place in the staged x_in plane: the first-colour
+//         positions are written, the second-colour ones keep x_in, which is
+//         what the later first-colour updates of planes t+-1 read there;
+//   wait for batch B(t+1), barrier;
+//   S(t-1) warps 0 .. rows-1 update the second colour of plane t-1 from the
+//         first-colour values of planes t-2, t-1, t and write both colours
+//         of the row to x_out; the two remaining warps update the first
+//         colour of the halo columns -1 and w of plane t (read by S(t));
+//   issue B(t+2) and an L2 prefetch of the planes two steps further.
+// Batch B(t): x_in of plane t+1, w0 w1 b of plane t, w2 of plane t+1, each
+// array row as the segment of columns [i0-4, i0+w+4) in 16-byte chunks
+// copied by cp.async (the periodic wrap in x is per chunk, since nx and i0
+// are multiples of 4; the wraps in y and z only change the row read).  The
+// rings hold six x and w2 planes and four coefficient planes: a slot is
+// refilled two steps after its last reader passed a barrier, so one barrier
+// per step orders every read before the copy that overwrites it.  Each
+// thread copies the same chunks of every plane (their offsets are computed
+// once per item) and waits only for its own copies.
 //
 // Every value is computed by the same operations, in the same order, as in
 // the two in-place half sweeps (Smooth4Body), so results are bit-identical.
-// Requires: nx % 4 == 0, nx >= 16, no stored diagonal (the diagonal is
-// minus the sum of the couplings, as for the projection operator).
+// Requires: nx % 4 == 0, nx >= 16, ny >= 2, nz >= 8, no stored diagonal
+// (the diagonal is minus the sum of the couplings, as for the projection
+// operator).
 #pragma once
 
 #include <cstdint>
@@ -41,24 +49,46 @@
 
 namespace aphgpu {
 
-constexpr int kPipeCols = 128;                // columns of a tile at most
-constexpr int kPipeRows = 7;                  // rows of a tile at most
-constexpr int kPipeStride = kPipeCols + 8;    // floats per staged row
-constexpr int kPipeThreads = 256;
-constexpr int kPipeWarps = kPipeThreads / 32;
-constexpr int kPipeXs = 4, kPipeCs = 3, kPipeWs = 4;  // ring sizes (planes)
-constexpr int kPipeXRows = kPipeRows + 4;     // x_in rows -2 .. rows+1
-constexpr int kPipeW0Rows = kPipeRows + 2;    // w0 rows -1 .. rows
-constexpr int kPipeW1Rows = kPipeRows + 3;    // w1 rows -1 .. rows+1
-constexpr int kPipeBRows = kPipeRows + 2;     // b rows -1 .. rows
-constexpr int kPipeCRows = kPipeW0Rows + kPipeW1Rows + kPipeBRows;
-constexpr int kPipeW2Rows = kPipeRows + 2;    // w2 rows -1 .. rows
-constexpr int kPipeFRows = kPipeRows + 2;     // first colour rows -1 .. rows
-constexpr int kPipeSmemFloats =
-    kPipeStride * (kPipeXs * kPipeXRows + kPipeCs * kPipeCRows + kPipeWs * kPipeW2Rows +
-                   3 * kPipeFRows);
-constexpr int kPipeSmemBytes = kPipeSmemFloats * 4;
-static_assert(2 * (kPipeSmemBytes + 1024) <= 228 * 1024, "two CTAs per SM");
+constexpr int kPipeCols = 128;               // columns of a tile at most
+constexpr int kPipeStride = kPipeCols + 8;   // floats per staged row
+constexpr int kPipeAhead = 2;                // batches issued ahead
+constexpr int kPipeXs = kPipeAhead + 4;      // x_in and w2 rings (planes)
+constexpr int kPipeCs = 4;                   // w0 w1 b ring (planes)
+constexpr int kPipePrefetch = 2;             // L2 prefetch: steps beyond the copies
+static_assert(kPipeCs >= kPipeAhead + 2 && (kPipeCs & (kPipeCs - 1)) == 0,
+              "coefficient ring: refilled two steps after its last read, power of two");
+static_assert(kPipeXs >= kPipeAhead + 4, "x ring: refilled two steps after its last read");
+
+// Shape of the kernel for bands of at most R rows: R + 2 warps (one per
+// first-colour row), the staged rings, and the CTAs resident per SM.
+template <int R>
+struct PipeShape {
+  static constexpr int kRows = R;
+  static constexpr int kWarps = R + 2;
+  static constexpr int kThreads = 32 * kWarps;
+  static constexpr int kXRows = R + 4;    // x_in rows -2 .. rows+1
+  static constexpr int kW0Rows = R + 2;   // w0 rows -1 .. rows
+  static constexpr int kW1Rows = R + 3;   // w1 rows -1 .. rows+1
+  static constexpr int kBRows = R + 2;    // b rows -1 .. rows
+  static constexpr int kCRows = kW0Rows + kW1Rows + kBRows;
+  static constexpr int kW2Rows = R + 2;   // w2 rows -1 .. rows
+  static constexpr int kXSlot = kXRows * kPipeStride;  // floats
+  static constexpr int kCSlot = kCRows * kPipeStride;
+  static constexpr int kWSlot = kW2Rows * kPipeStride;
+  static constexpr int kSmemBytes =
+      4 * (kPipeXs * kXSlot + kPipeCs * kCSlot + kPipeXs * kWSlot);
+  // CTAs per SM: 228 KB of shared memory per SM, 1 KB reserved per CTA
+  static constexpr int kCtasPerSm = 233472 / (kSmemBytes + 1024) >= 2 ? 2 : 1;
+  static_assert(kSmemBytes <= 227 * 1024, "shared memory of one CTA");
+  static_assert(kXRows * (kPipeStride / 4) <= 2 * kThreads, "two chunks per thread and array");
+  static_assert(2 * (R + 2) <= 64, "halo cells of a plane for the two spare warps");
+  static_assert(5 * R + 13 <= kThreads, "one prefetched row per thread");
+};
+// the two shapes built: 14-row bands, one CTA of 16 warps per SM; 6-row
+// bands, two CTAs of 8 warps per SM
+using PipeTall = PipeShape<14>;
+using PipeShort = PipeShape<6>;
+static_assert(PipeTall::kCtasPerSm == 1 && PipeShort::kCtasPerSm == 2, "residency");
 
 struct PipeTiling {
   int w;       // columns of a tile (multiple of 4, <= kPipeCols)
@@ -70,182 +100,17 @@ __device__ __forceinline__ uint32_t SmemAddr(const void* p) {
   return (uint32_t)__cvta_generic_to_shared(p);
 }
 
-struct PipeSmem {
-  float* xs;   // [kPipeXs][kPipeXRows][stride]
-  float* cs;   // [kPipeCs][kPipeCRows][stride]: w0, w1, b
-  float* ws;   // [kPipeWs][kPipeW2Rows][stride]
-  float* fs;   // [3][kPipeFRows][stride]
-};
-
 __device__ __forceinline__ int PosMod(int a, int m) {
   const int r = a % m;
   return r < 0 ? r + m : r;
 }
 
-// Rows of one batch: x_in planes px[0..nxp), the coefficient rows (w0, w1,
-// b) of plane pc (pc_on), w2 planes pw[0..nwp).
-struct PipeBatch {
-  int px[3], nxp;
-  int pc, pc_on;
-  int pw[2], nwp;
-};
-
 __device__ __forceinline__ float4 LdS4(const float* p) {
   return *reinterpret_cast<const float4*>(p);
 }
 
-// First colour of row r (-1..rows) of plane p into its F slot: float4
-// groups of the w columns, and (lanes 0 and 1) the halo columns -1 and w.
-__device__ __forceinline__ void PipeFirst(const PipeSmem& S, int base, int c0, int zero_init,
-                                          int i0, int w, int j0, int r, int p, int nyd,
-                                          int nzd) {
-  const int lane = threadIdx.x & 31;
-  const float* X0 = S.xs + (size_t)PosMod(p - 1 - base, kPipeXs) * kPipeXRows * kPipeStride;
-  const float* X1 = S.xs + (size_t)PosMod(p - base, kPipeXs) * kPipeXRows * kPipeStride;
-  const float* X2 = S.xs + (size_t)PosMod(p + 1 - base, kPipeXs) * kPipeXRows * kPipeStride;
-  const float* C = S.cs + (size_t)PosMod(p - base, kPipeCs) * kPipeCRows * kPipeStride;
-  const float* W0 = C + (size_t)(r + 1) * kPipeStride;
-  const float* W1 = C + (size_t)(kPipeW0Rows + r + 1) * kPipeStride;
-  const float* W1n = W1 + kPipeStride;
-  const float* B = C + (size_t)(kPipeW0Rows + kPipeW1Rows + r + 1) * kPipeStride;
-  const float* Z1 =
-      S.ws + ((size_t)PosMod(p - base, kPipeWs) * kPipeW2Rows + (r + 1)) * kPipeStride;
-  const float* Z2 =
-      S.ws + ((size_t)PosMod(p + 1 - base, kPipeWs) * kPipeW2Rows + (r + 1)) * kPipeStride;
-  const float* Xc = X1 + (size_t)(r + 2) * kPipeStride;
-  const float* Xm = Xc - kPipeStride;
-  const float* Xp = Xc + kPipeStride;
-  const float* Xz0 = X0 + (size_t)(r + 2) * kPipeStride;
-  const float* Xz2 = X2 + (size_t)(r + 2) * kPipeStride;
-  float* Fo = S.fs + ((size_t)PosMod(p - base, 3) * kPipeFRows + (r + 1)) * kPipeStride;
-  // colour parity of the wrapped indices (i0 is a multiple of 4)
-  const int j = PosMod(j0 + r, nyd);
-  const int pz = PosMod(p, nzd);
-  const int g = lane;
-  if (4 * g < w) {
-    const int l = 4 * g + 4;
-    const float4 w0v = LdS4(W0 + l), w1v = LdS4(W1 + l), w1nv = LdS4(W1n + l);
-    const float4 z1v = LdS4(Z1 + l), z2v = LdS4(Z2 + l), bv = LdS4(B + l);
-    const float wr = W0[l + 4];
-    float4 xc = make_float4(0, 0, 0, 0), xjm = xc, xjp = xc, xz0 = xc, xz2 = xc;
-    float xl = 0.f, xr = 0.f;
-    if (!zero_init) {
-      xc = LdS4(Xc + l);
-      xjm = LdS4(Xm + l);
-      xjp = LdS4(Xp + l);
-      xz0 = LdS4(Xz0 + l);
-      xz2 = LdS4(Xz2 + l);
-      xl = Xc[l - 1];
-      xr = Xc[l + 4];
-    }
-    float4 out = make_float4(0, 0, 0, 0);
-    const int e0 = (c0 + j + pz) & 1;
-#pragma unroll
-    for (int e = 0; e < 4; ++e) {
-      if ((e & 1) != e0) continue;
-      const float cxm = El(w0v, e);
-      const float cxp = e == 3 ? wr : El(w0v, e + 1);
-      const float cym = El(w1v, e), cyp = El(w1nv, e);
-      const float czm = El(z1v, e), czp = El(z2v, e);
-      const float dg = -(((((cxm + cxp) + cym) + cyp) + czm) + czp);
-      float acc = El(bv, e);
-      if (!zero_init) {
-        const float vxm = e == 0 ? xl : El(xc, e - 1);
-        const float vxp = e == 3 ? xr : El(xc, e + 1);
-        acc -= cxm * vxm;
-        acc -= cxp * vxp;
-        acc -= cym * El(xjm, e);
-        acc -= cyp * El(xjp, e);
-        acc -= czm * El(xz0, e);
-        acc -= czp * El(xz2, e);
-      }
-      SetEl(out, e, acc / dg);
-    }
-    *reinterpret_cast<float4*>(Fo + l) = out;
-  }
-  // halo columns: lane 0 column -1, lane 1 column w (the parity of i0 - 1
-  // and i0 + w equals that of their wrapped columns: nx is even)
-  if (lane < 2) {
-    const int col = lane == 0 ? -1 : w;
-    const int l = col + 4;
-    if (((col + j + pz) & 1) == c0) {
-      const float cxm = W0[l], cxp = W0[l + 1];
-      const float cym = W1[l], cyp = W1n[l];
-      const float czm = Z1[l], czp = Z2[l];
-      const float dg = -(((((cxm + cxp) + cym) + cyp) + czm) + czp);
-      float acc = B[l];
-      if (!zero_init) {
-        acc -= cxm * Xc[l - 1];
-        acc -= cxp * Xc[l + 1];
-        acc -= cym * Xm[l];
-        acc -= cyp * Xp[l];
-        acc -= czm * Xz0[l];
-        acc -= czp * Xz2[l];
-      }
-      Fo[l] = acc / dg;
-    }
-  }
-}
-
-// Second colour of row r (0..rows-1) of plane m from the first colour of
-// planes m-1, m, m+1; both colours of the row's w columns to x_out.
-__device__ __forceinline__ void PipeSecond(const PipeSmem& S, int base, int c0, int i0, int w,
-                                           int j0, int r, int m, const Dims& d, float* xout) {
-  const int lane = threadIdx.x & 31;
-  const int g = lane;
-  if (4 * g >= w) return;
-  const int l = 4 * g + 4;
-  const float* C = S.cs + (size_t)PosMod(m - base, kPipeCs) * kPipeCRows * kPipeStride;
-  const float* W0 = C + (size_t)(r + 1) * kPipeStride;
-  const float* W1 = C + (size_t)(kPipeW0Rows + r + 1) * kPipeStride;
-  const float* W1n = W1 + kPipeStride;
-  const float* B = C + (size_t)(kPipeW0Rows + kPipeW1Rows + r + 1) * kPipeStride;
-  const float* Z1 =
-      S.ws + ((size_t)PosMod(m - base, kPipeWs) * kPipeW2Rows + (r + 1)) * kPipeStride;
-  const float* Z2 =
-      S.ws + ((size_t)PosMod(m + 1 - base, kPipeWs) * kPipeW2Rows + (r + 1)) * kPipeStride;
-  const float* Fm =
-      S.fs + ((size_t)PosMod(m - 1 - base, 3) * kPipeFRows + (r + 1)) * kPipeStride;
-  const float* F0 = S.fs + ((size_t)PosMod(m - base, 3) * kPipeFRows + (r + 1)) * kPipeStride;
-  const float* Fp =
-      S.fs + ((size_t)PosMod(m + 1 - base, 3) * kPipeFRows + (r + 1)) * kPipeStride;
-  const float4 w0v = LdS4(W0 + l), w1v = LdS4(W1 + l), w1nv = LdS4(W1n + l);
-  const float4 z1v = LdS4(Z1 + l), z2v = LdS4(Z2 + l), bv = LdS4(B + l);
-  const float wr = W0[l + 4];
-  const float4 f0 = LdS4(F0 + l);
-  const float4 fym = LdS4(F0 - kPipeStride + l), fyp = LdS4(F0 + kPipeStride + l);
-  const float4 fzm = LdS4(Fm + l), fzp = LdS4(Fp + l);
-  const float fl = F0[l - 1], fr = F0[l + 4];
-  const int j = j0 + r;
-  const int pz = PosMod(m, d.nz);
-  const int e0 = (c0 + j + pz) & 1;  // first-colour positions
-  float4 out;
-#pragma unroll
-  for (int e = 0; e < 4; ++e) {
-    if ((e & 1) == e0) {
-      SetEl(out, e, El(f0, e));
-      continue;
-    }
-    const float cxm = El(w0v, e);
-    const float cxp = e == 3 ? wr : El(w0v, e + 1);
-    const float cym = El(w1v, e), cyp = El(w1nv, e);
-    const float czm = El(z1v, e), czp = El(z2v, e);
-    const float dg = -(((((cxm + cxp) + cym) + cyp) + czm) + czp);
-    float acc = El(bv, e);
-    acc -= cxm * (e == 0 ? fl : El(f0, e - 1));
-    acc -= cxp * (e == 3 ? fr : El(f0, e + 1));
-    acc -= cym * El(fym, e);
-    acc -= cyp * El(fyp, e);
-    acc -= czm * El(fzm, e);
-    acc -= czp * El(fzp, e);
-    SetEl(out, e, acc / dg);
-  }
-  *reinterpret_cast<float4*>(xout + d.idx(i0 + 4 * g, j, pz)) = out;
-}
-
-__device__ __forceinline__ void CpAsync16(void* dst, const void* src) {
-  asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(SmemAddr(dst)), "l"(src)
-               : "memory");
+__device__ __forceinline__ void CpAsync16(uint32_t dst, const void* src) {
+  asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(dst), "l"(src) : "memory");
 }
 __device__ __forceinline__ void CpAsyncCommit() {
   asm volatile("cp.async.commit_group;" ::: "memory");
@@ -254,156 +119,174 @@ template <int kPending>
 __device__ __forceinline__ void CpAsyncWait() {
   asm volatile("cp.async.wait_group %0;" ::"n"(kPending) : "memory");
 }
-
-// Issues a batch by all threads of the CTA, then commits one group.
-__device__ __forceinline__ void IssueBatchAsync(const Op<float>& A, const float* __restrict__ b,
-                                                const float* __restrict__ xin,
-                                                const PipeSmem& S, int base, int i0, int w,
-                                                int j0, int rows, const PipeBatch& B) {
-  const Dims d = A.d;
-  const int nxr = rows + 4, nc0 = rows + 2, nc1 = rows + 3, nw = rows + 2;
-  const int ncoef = B.pc_on ? nc0 + nc1 + nc0 : 0;
-  const int total = B.nxp * nxr + ncoef + B.nwp * nw;  // rows
-  const int cpr = (w + 8) / 4;                           // chunks per row
-  const int64_t plane = (int64_t)d.nx * d.ny;
-  for (int q = threadIdx.x; q < total * cpr; q += blockDim.x) {
-    int t = q / cpr;
-    const int ch = q - t * cpr;
-    const float* src;
-    float* dst;
-    int r, p;
-    if (t < B.nxp * nxr) {
-      p = B.px[t / nxr];
-      r = t % nxr - 2;
-      src = xin;
-      dst = S.xs + ((size_t)PosMod(p - base, kPipeXs) * kPipeXRows + (r + 2)) * kPipeStride;
-    } else if (t - B.nxp * nxr < ncoef) {
-      t -= B.nxp * nxr;
-      p = B.pc;
-      float* slot = S.cs + (size_t)PosMod(p - base, kPipeCs) * kPipeCRows * kPipeStride;
-      if (t < nc0) {
-        r = t - 1;
-        src = A.w0;
-        dst = slot + (size_t)(r + 1) * kPipeStride;
-      } else if (t < nc0 + nc1) {
-        r = t - nc0 - 1;
-        src = A.w1;
-        dst = slot + (size_t)(kPipeW0Rows + r + 1) * kPipeStride;
-      } else {
-        r = t - nc0 - nc1 - 1;
-        src = b;
-        dst = slot + (size_t)(kPipeW0Rows + kPipeW1Rows + r + 1) * kPipeStride;
-      }
-    } else {
-      t -= B.nxp * nxr + ncoef;
-      p = B.pw[t / nw];
-      r = t % nw - 1;
-      src = A.w2;
-      dst = S.ws + ((size_t)PosMod(p - base, kPipeWs) * kPipeW2Rows + (r + 1)) * kPipeStride;
-    }
-    const int jw = PosMod(j0 + r, d.ny);
-    const int pz = PosMod(p, d.nz);
-    const int col = PosMod(i0 - 4 + 4 * ch, d.nx);
-    CpAsync16(dst + 4 * ch, src + pz * plane + (int64_t)jw * d.nx + col);
-  }
-  CpAsyncCommit();
+// L2 prefetch of a contiguous range (16-byte aligned, size a multiple of 16)
+__device__ __forceinline__ void PrefetchBulkL2(const void* src, uint32_t bytes) {
+  asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;" ::"l"(src), "r"(bytes) : "memory");
 }
 
-// Chunks of a steady-state batch B(t) (x_in of plane t+1, w0 w1 b of plane
-// t, w2 of plane t+1) owned by one thread: at most kPipeOwn chunks, each
-// described once per work item by its array, its offset inside a plane of
-// that array and its offset inside the ring slot; a step then only adds
-// the planes' offsets.
-constexpr int kPipeOwn = 8;
-static_assert((5 * kPipeRows + 13) * ((kPipeCols + 8) / 4) <= kPipeOwn * kPipeThreads,
-              "a steady batch has more chunks than the threads own");
+// The chunks of one staged array that a thread copies: the array's rows
+// r = 0 .. nrows-1 (array row j0 + r + roff, wrapped) land in slot rows
+// srow0 + r; chunk q = threadIdx.x + i * kThreads (i = 0, 1) is column
+// chunk q % cpr of row q / cpr.  g: offset inside a plane (floats); s:
+// offset inside the slot (bytes), -1 if the thread has no such chunk.
 struct PipeChunks {
-  int n;
-  int kind[kPipeOwn];     // 0 x, 1 w0, 2 w1, 3 b, 4 w2
-  int goff[kPipeOwn];     // row * nx + column (wrapped) inside the plane
-  int soff[kPipeOwn];     // offset inside the ring slot (floats)
+  int g[2];
+  int s[2];
 };
 
-__device__ __forceinline__ void PipeChunksInit(const Dims& d, int i0, int w, int j0, int rows,
-                                               int zero_init, PipeChunks& C) {
-  const int nxr = rows + 4, nc0 = rows + 2, nc1 = rows + 3, nw = rows + 2;
-  const int nxp = zero_init ? 0 : 1;
-  const int total = nxp * nxr + nc0 + nc1 + nc0 + nw;
-  const int cpr = (w + 8) / 4;
-  C.n = 0;
-  for (int q = threadIdx.x; q < total * cpr && C.n < kPipeOwn; q += blockDim.x) {
-    int t = q / cpr;
-    const int ch = q - t * cpr;
-    int kind, r, srow;
-    if (t < nxp * nxr) {
-      kind = 0;
-      r = t - 2;
-      srow = r + 2;
-    } else if ((t -= nxp * nxr) < nc0) {
-      kind = 1;
-      r = t - 1;
-      srow = r + 1;
-    } else if ((t -= nc0) < nc1) {
-      kind = 2;
-      r = t - 1;
-      srow = kPipeW0Rows + r + 1;
-    } else if ((t -= nc1) < nc0) {
-      kind = 3;
-      r = t - 1;
-      srow = kPipeW0Rows + kPipeW1Rows + r + 1;
-    } else {
-      t -= nc0;
-      kind = 4;
-      r = t - 1;
-      srow = r + 1;
-    }
-    const int jw = PosMod(j0 + r, d.ny);
-    const int col = PosMod(i0 - 4 + 4 * ch, d.nx);
-    C.kind[C.n] = kind;
-    C.goff[C.n] = jw * d.nx + col;
-    C.soff[C.n] = srow * kPipeStride + 4 * ch;
-    ++C.n;
-  }
-}
-
-// Steady-state batch B(t) from the thread's precomputed chunks.
-__device__ __forceinline__ void IssueSteadyAsync(const Op<float>& A, const float* __restrict__ b,
-                                                 const float* __restrict__ xin,
-                                                 const PipeSmem& S, int base, int t,
-                                                 const PipeChunks& C) {
-  const Dims d = A.d;
-  const int64_t plane = (int64_t)d.nx * d.ny;
-  const int64_t px = (int64_t)PosMod(t + 1, d.nz) * plane;  // x, w2
-  const int64_t pc = (int64_t)PosMod(t, d.nz) * plane;      // w0, w1, b
-  float* xs = S.xs + (size_t)PosMod(t + 1 - base, kPipeXs) * kPipeXRows * kPipeStride;
-  float* cs = S.cs + (size_t)PosMod(t - base, kPipeCs) * kPipeCRows * kPipeStride;
-  float* ws = S.ws + (size_t)PosMod(t + 1 - base, kPipeWs) * kPipeW2Rows * kPipeStride;
+template <int kThreads>
+__device__ __forceinline__ PipeChunks PipeChunksOf(const Dims& d, int i0, int w, int j0,
+                                                   int nrows, int roff, int srow0) {
+  PipeChunks c;
+  const int cpr = (w + 8) >> 2;
 #pragma unroll
-  for (int q = 0; q < kPipeOwn; ++q) {
-    if (q >= C.n) break;
-    const int k = C.kind[q];
-    const float* src = k == 0 ? xin + px : k == 1 ? A.w0 + pc : k == 2 ? A.w1 + pc
-                     : k == 3 ? b + pc : A.w2 + px;
-    float* dst = k == 0 ? xs : k == 4 ? ws : cs;
-    CpAsync16(dst + C.soff[q], src + C.goff[q]);
+  for (int i = 0; i < 2; ++i) {
+    const int q = threadIdx.x + i * kThreads;
+    c.g[i] = 0;
+    c.s[i] = -1;
+    if (q < nrows * cpr) {
+      const int r = q / cpr, ch = q - r * cpr;
+      const int jw = PosMod(j0 + r + roff, d.ny);
+      const int col = PosMod(i0 - 4 + 4 * ch, d.nx);
+      c.g[i] = jw * d.nx + col;
+      c.s[i] = 4 * ((srow0 + r) * kPipeStride + 4 * ch);
+    }
   }
-  CpAsyncCommit();
+  return c;
 }
 
-// One fused sweep of one work item (grid: one CTA of kPipeThreads per item,
-// dynamic shared memory kPipeSmemBytes).  Item index: blockIdx.x =
-// (zseg * bands + band) * xtiles + xtile.
-__global__ void __launch_bounds__(kPipeThreads, 2)
+__device__ __forceinline__ void PipeCopy(uint32_t slot, const float* plane, const PipeChunks& c) {
+#pragma unroll
+  for (int i = 0; i < 2; ++i)
+    if (c.s[i] >= 0) CpAsync16(slot + (uint32_t)c.s[i], plane + c.g[i]);
+}
+
+// First colour of the float4 group at slot column l of one row (elements E0
+// and E0+2 carry the first colour), written in place into the row's staged
+// x_in.  xc, xm, xp: x_in rows r, r-1, r+1 of plane t; xz0, xz2: row r of
+// planes t-1, t+1; w0, w1, w1n (row r+1), bb: the coefficient rows; z1, z2:
+// w2 row r of planes t, t+1.
+template <int E0, int ZI>
+__device__ __forceinline__ void PipeFirst(float* xc, const float* xm, const float* xp,
+                                          const float* xz0, const float* xz2, const float* w0,
+                                          const float* w1, const float* w1n, const float* bb,
+                                          const float* z1, const float* z2, int l) {
+  const float4 w0v = LdS4(w0 + l), w1v = LdS4(w1 + l), w1nv = LdS4(w1n + l);
+  const float4 z1v = LdS4(z1 + l), z2v = LdS4(z2 + l), bv = LdS4(bb + l);
+  const float wr = E0 == 1 ? w0[l + 4] : 0.f;
+  float4 c = make_float4(0, 0, 0, 0), jm = c, jp = c, zm = c, zp = c;
+  float xs = 0.f;  // the x neighbour outside the group
+  if (!ZI) {
+    c = LdS4(xc + l);
+    jm = LdS4(xm + l);
+    jp = LdS4(xp + l);
+    zm = LdS4(xz0 + l);
+    zp = LdS4(xz2 + l);
+    xs = E0 == 0 ? xc[l - 1] : xc[l + 4];
+  }
+#pragma unroll
+  for (int h = 0; h < 2; ++h) {
+    const int e = E0 + 2 * h;
+    const float cxm = El(w0v, e);
+    const float cxp = e == 3 ? wr : El(w0v, e + 1);
+    const float cym = El(w1v, e), cyp = El(w1nv, e);
+    const float czm = El(z1v, e), czp = El(z2v, e);
+    const float dg = -(((((cxm + cxp) + cym) + cyp) + czm) + czp);
+    float acc = El(bv, e);
+    if (!ZI) {
+      const float vxm = e == 0 ? xs : El(c, e - 1);
+      const float vxp = e == 3 ? xs : El(c, e + 1);
+      acc -= cxm * vxm;
+      acc -= cxp * vxp;
+      acc -= cym * El(jm, e);
+      acc -= cyp * El(jp, e);
+      acc -= czm * El(zm, e);
+      acc -= czp * El(zp, e);
+    }
+    xc[l + e] = acc / dg;
+  }
+}
+
+// First colour of the single cell at slot column l (a halo column), same
+// arguments as PipeFirst.
+template <int ZI>
+__device__ __forceinline__ void PipeFirstCell(float* xc, const float* xm, const float* xp,
+                                              const float* xz0, const float* xz2,
+                                              const float* w0, const float* w1,
+                                              const float* w1n, const float* bb,
+                                              const float* z1, const float* z2, int l) {
+  const float cxm = w0[l], cxp = w0[l + 1];
+  const float cym = w1[l], cyp = w1n[l];
+  const float czm = z1[l], czp = z2[l];
+  const float dg = -(((((cxm + cxp) + cym) + cyp) + czm) + czp);
+  float acc = bb[l];
+  if (!ZI) {
+    acc -= cxm * xc[l - 1];
+    acc -= cxp * xc[l + 1];
+    acc -= cym * xm[l];
+    acc -= cyp * xp[l];
+    acc -= czm * xz0[l];
+    acc -= czp * xz2[l];
+  }
+  xc[l] = acc / dg;
+}
+
+// Second colour of the group at slot column l of one row (elements 1-E0 and
+// 3-E0, E0 the first colour's parity) from the first-colour values staged
+// in the x_in slots: f0, fym, fyp rows r, r-1, r+1 of plane m; fzm, fzp row
+// r of planes m-1, m+1; coefficient rows as in PipeFirst (z1, z2: w2 of
+// planes m, m+1).  Both colours of the group go to out.
+template <int E0>
+__device__ __forceinline__ void PipeSecond(const float* f0, const float* fym, const float* fyp,
+                                           const float* fzm, const float* fzp,
+                                           const float* w0, const float* w1, const float* w1n,
+                                           const float* bb, const float* z1, const float* z2,
+                                           int l, float* out) {
+  const float4 w0v = LdS4(w0 + l), w1v = LdS4(w1 + l), w1nv = LdS4(w1n + l);
+  const float4 z1v = LdS4(z1 + l), z2v = LdS4(z2 + l), bv = LdS4(bb + l);
+  const float wr = E0 == 0 ? w0[l + 4] : 0.f;
+  const float4 fv = LdS4(f0 + l);
+  const float4 jm = LdS4(fym + l), jp = LdS4(fyp + l), zm = LdS4(fzm + l), zp = LdS4(fzp + l);
+  const float fs = E0 == 0 ? f0[l + 4] : f0[l - 1];
+  float4 o = fv;
+#pragma unroll
+  for (int h = 0; h < 2; ++h) {
+    const int e = 1 - E0 + 2 * h;
+    const float cxm = El(w0v, e);
+    const float cxp = e == 3 ? wr : El(w0v, e + 1);
+    const float cym = El(w1v, e), cyp = El(w1nv, e);
+    const float czm = El(z1v, e), czp = El(z2v, e);
+    const float dg = -(((((cxm + cxp) + cym) + cyp) + czm) + czp);
+    float acc = El(bv, e);
+    acc -= cxm * (e == 0 ? fs : El(fv, e - 1));
+    acc -= cxp * (e == 3 ? fs : El(fv, e + 1));
+    acc -= cym * El(jm, e);
+    acc -= cyp * El(jp, e);
+    acc -= czm * El(zm, e);
+    acc -= czp * El(zp, e);
+    SetEl(o, e, acc / dg);
+  }
+  St4(out, o);
+}
+
+// One fused sweep of one work item (grid: one CTA of P::kThreads per item,
+// dynamic shared memory P::kSmemBytes).  Item index: blockIdx.x = (zseg *
+// bands + band) * xtiles + xtile.  ZI: x_in is taken as zero (not read).
+template <class P, int ZI>
+__global__ void __launch_bounds__(P::kThreads, P::kCtasPerSm)
     KSweepPipe(Op<float> A, const float* __restrict__ b, const float* __restrict__ xin,
-               float* xout, int c0, int zero_init, const SolveScalars* s, PipeTiling T) {
+               float* __restrict__ xout, int c0, const SolveScalars* s, PipeTiling T) {
+  constexpr int kPipeRows = P::kRows;
+  constexpr int kPipeThreads = P::kThreads;
+  constexpr int kPipeXSlot = P::kXSlot, kPipeCSlot = P::kCSlot, kPipeWSlot = P::kWSlot;
+  constexpr int kPipeW0Rows = P::kW0Rows, kPipeW1Rows = P::kW1Rows;
   if (s && s->done) return;
   extern __shared__ __align__(128) float smem[];
+  float* const XS = smem;
+  float* const CS = XS + kPipeXs * kPipeXSlot;
+  float* const WS = CS + kPipeCs * kPipeCSlot;
+  const uint32_t xs_addr = SmemAddr(XS), cs_addr = SmemAddr(CS), ws_addr = SmemAddr(WS);
   const Dims d = A.d;
-  PipeSmem S;
-  S.xs = smem;
-  S.cs = S.xs + (size_t)kPipeXs * kPipeXRows * kPipeStride;
-  S.ws = S.cs + (size_t)kPipeCs * kPipeCRows * kPipeStride;
-  S.fs = S.ws + (size_t)kPipeWs * kPipeW2Rows * kPipeStride;
   const int item = blockIdx.x;
   const int xt = item % T.xtiles;
   const int band = (item / T.xtiles) % T.bands;
@@ -414,47 +297,177 @@ __global__ void __launch_bounds__(kPipeThreads, 2)
   const int rows = min(T.rows, d.ny - j0);
   const int kb = (int)((int64_t)d.nz * zs / T.zsegs);
   const int ke = (int)((int64_t)d.nz * (zs + 1) / T.zsegs);
-  const int warp = threadIdx.x >> 5;
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int64_t plane = (int64_t)d.nx * d.ny;
   const int base = kb - 2;  // ring position 0: plane kb-2
   const int t0 = kb - 1;    // first time step
-  // batch B(t0): x_in of planes t0-1 .. t0+1, coefficients of t0, w2 of
-  // t0 and t0+1; later batches come from the precomputed chunks
-  PipeBatch B0;
-  B0.nxp = 0;
-  if (!zero_init) {
-    B0.px[B0.nxp++] = t0 + 1;
-    B0.px[B0.nxp++] = t0 - 1;
-    B0.px[B0.nxp++] = t0;
+
+  // the thread's chunks of every array
+  const PipeChunks cx = PipeChunksOf<kPipeThreads>(d, i0, w, j0, ZI ? 0 : rows + 4, -2, 0);
+  const PipeChunks c0w = PipeChunksOf<kPipeThreads>(d, i0, w, j0, rows + 2, -1, 0);
+  const PipeChunks c1w = PipeChunksOf<kPipeThreads>(d, i0, w, j0, rows + 3, -1, kPipeW0Rows);
+  const PipeChunks cbb = PipeChunksOf<kPipeThreads>(d, i0, w, j0, rows + 2, -1, kPipeW0Rows + kPipeW1Rows);
+  const PipeChunks c2w = PipeChunksOf<kPipeThreads>(d, i0, w, j0, rows + 2, -1, 0);
+  // the thread's L2 prefetch: one array row of a future batch (in-range
+  // columns only; the 16-byte wrapped ends are left to the copies)
+  const float* pf_src = nullptr;
+  uint32_t pf_bytes = 0;
+  int pf_coef = 0;
+  {
+    const int nr[5] = {ZI ? 0 : rows + 4, rows + 2, rows + 3, rows + 2, rows + 2};
+    const float* arr[5] = {xin, A.w0, A.w1, b, A.w2};
+    int q = threadIdx.x;
+#pragma unroll
+    for (int a = 0; a < 5; ++a) {
+      if (q >= 0 && q < nr[a]) {
+        const int jw = PosMod(j0 + q + (a == 0 ? -2 : -1), d.ny);
+        const int lo = max(i0 - 4, 0), hi = min(i0 + w + 4, d.nx);
+        pf_src = arr[a] + (int64_t)jw * d.nx + lo;
+        pf_bytes = 4u * (uint32_t)(hi - lo);
+        pf_coef = a >= 1 && a <= 3;
+      }
+      q -= nr[a];
+    }
   }
-  B0.pc = t0;
-  B0.pc_on = 1;
-  B0.nwp = 0;
-  B0.pw[B0.nwp++] = t0 + 1;
-  B0.pw[B0.nwp++] = t0;
-  PipeChunks C;
-  PipeChunksInit(d, i0, w, j0, rows, zero_init, C);
-  IssueBatchAsync(A, b, xin, S, base, i0, w, j0, rows, B0);
-  if (t0 + 1 <= ke)
-    IssueSteadyAsync(A, b, xin, S, base, t0 + 1, C);
-  else
+  // row of this warp's first-colour update (F) and second-colour update (S)
+  const int rf = warp - 1, rs = warp;
+  const int jf = PosMod(j0 + rf, d.ny), js = PosMod(j0 + rs, d.ny);
+  // halo cell of the two spare warps: row rh, column -1 or w
+  const int hh = (warp - kPipeRows) * 32 + lane;
+  const int rh = (hh >> 1) - 1;
+  const int colh = (hh & 1) ? w : -1;
+  const int jh = PosMod(j0 + rh, d.ny);
+  const bool f_on = rf <= rows && 4 * lane < w;
+  const bool s_on = rs < rows && 4 * lane < w;
+  const bool h_on = warp >= kPipeRows && rh <= rows;
+  const int l = 4 * lane + 4;  // slot column of the lane's group
+
+  // prologue: B(t0) (x_in of planes t0-1 .. t0+1, coefficients of t0, w2
+  // of t0 and t0+1) and B(t0+1) .. B(t0+kPipeAhead-1)
+  {
+    const int pz = PosMod(t0, d.nz);
+    const int pzm = PosMod(t0 - 1, d.nz), pzp = PosMod(t0 + 1, d.nz);
+    if (!ZI) {
+      PipeCopy(xs_addr + 4u * 0 * kPipeXSlot, xin + pzm * plane, cx);
+      PipeCopy(xs_addr + 4u * 1 * kPipeXSlot, xin + pz * plane, cx);
+      PipeCopy(xs_addr + 4u * 2 * kPipeXSlot, xin + pzp * plane, cx);
+    }
+    const uint32_t cslot = cs_addr + 4u * ((t0 - base) & (kPipeCs - 1)) * kPipeCSlot;
+    PipeCopy(cslot, A.w0 + pz * plane, c0w);
+    PipeCopy(cslot, A.w1 + pz * plane, c1w);
+    PipeCopy(cslot, b + pz * plane, cbb);
+    PipeCopy(ws_addr + 4u * 1 * kPipeWSlot, A.w2 + pz * plane, c2w);
+    PipeCopy(ws_addr + 4u * 2 * kPipeWSlot, A.w2 + pzp * plane, c2w);
     CpAsyncCommit();
-  CpAsyncWait<1>();  // B(t0)
-  __syncthreads();
-  for (int t = t0; t <= ke; ++t) {
-    // F(t): rows -1 .. rows over the warps
-    for (int r = warp - 1; r <= rows; r += kPipeWarps)
-      PipeFirst(S, base, c0, zero_init, i0, w, j0, r, t, d.ny, d.nz);
-    __syncthreads();
-    if (t - 1 >= kb && warp < rows) PipeSecond(S, base, c0, i0, w, j0, warp, t - 1, d, xout);
-    // the slots of x_in plane t-1 and of the coefficients and w2 of plane
-    // t-1 are free once every thread is past S(t-1): B(t+2) goes there
-    __syncthreads();
-    if (t + 2 <= ke)
-      IssueSteadyAsync(A, b, xin, S, base, t + 2, C);
-    else
+#pragma unroll
+    for (int k = 1; k < kPipeAhead; ++k) {
+      const int t = t0 + k;
+      if (t <= ke) {
+        const int64_t pc = (int64_t)PosMod(t, d.nz) * plane;
+        const int64_t px = (int64_t)PosMod(t + 1, d.nz) * plane;
+        const uint32_t xsl = 4u * ((t + 1 - base) % kPipeXs);
+        if (!ZI) PipeCopy(xs_addr + xsl * kPipeXSlot, xin + px, cx);
+        const uint32_t cslot2 = cs_addr + 4u * ((t - base) & (kPipeCs - 1)) * kPipeCSlot;
+        PipeCopy(cslot2, A.w0 + pc, c0w);
+        PipeCopy(cslot2, A.w1 + pc, c1w);
+        PipeCopy(cslot2, b + pc, cbb);
+        PipeCopy(ws_addr + xsl * kPipeWSlot, A.w2 + px, c2w);
+      }
       CpAsyncCommit();
-    CpAsyncWait<1>();  // B(t+1) complete, B(t+2) may stay in flight
+    }
+    CpAsyncWait<kPipeAhead - 1>();
     __syncthreads();
+  }
+
+  int ph = t0 - base;         // (t - base) mod kPipeXs
+  int pz = PosMod(t0, d.nz);  // t mod nz
+  for (int t = t0; t <= ke; ++t) {
+    auto xslot = [&](int k) {  // x_in / w2 ring slot of plane t + k (-2 <= k <= 3)
+      const int v = ph + k;
+      return v < 0 ? v + kPipeXs : (v >= kPipeXs ? v - kPipeXs : v);
+    };
+    const int cs0 = (t - base) & (kPipeCs - 1);
+    float* const X0 = XS + xslot(0) * kPipeXSlot;
+    float* const Xm1 = XS + xslot(-1) * kPipeXSlot;
+    float* const Xp1 = XS + xslot(1) * kPipeXSlot;
+    const float* const C0 = CS + cs0 * kPipeCSlot;
+    const float* const W20 = WS + xslot(0) * kPipeWSlot;
+    const float* const W2p = WS + xslot(1) * kPipeWSlot;
+    // F(t)
+    if (f_on) {
+      float* xc = X0 + (rf + 2) * kPipeStride;
+      const float* w0 = C0 + (rf + 1) * kPipeStride;
+      const float* w1 = C0 + (kPipeW0Rows + rf + 1) * kPipeStride;
+      const float* bb = C0 + (kPipeW0Rows + kPipeW1Rows + rf + 1) * kPipeStride;
+      const float* xz0 = Xm1 + (rf + 2) * kPipeStride;
+      const float* xz2 = Xp1 + (rf + 2) * kPipeStride;
+      const float* z1 = W20 + (rf + 1) * kPipeStride;
+      const float* z2 = W2p + (rf + 1) * kPipeStride;
+      if ((c0 + jf + pz) & 1)
+        PipeFirst<1, ZI>(xc, xc - kPipeStride, xc + kPipeStride, xz0, xz2, w0, w1,
+                         w1 + kPipeStride, bb, z1, z2, l);
+      else
+        PipeFirst<0, ZI>(xc, xc - kPipeStride, xc + kPipeStride, xz0, xz2, w0, w1,
+                         w1 + kPipeStride, bb, z1, z2, l);
+    }
+    CpAsyncWait<kPipeAhead - 2>();  // B(t+1)
+    __syncthreads();
+    // S(t-1)
+    if (t - 1 >= kb && s_on) {
+      const int m = t - 1;
+      const int pzm = pz == 0 ? d.nz - 1 : pz - 1;
+      const float* Fm = XS + xslot(-2) * kPipeXSlot;
+      const float* C1 = CS + ((m - base) & (kPipeCs - 1)) * kPipeCSlot;
+      const float* f0 = Xm1 + (rs + 2) * kPipeStride;
+      const float* w0 = C1 + (rs + 1) * kPipeStride;
+      const float* w1 = C1 + (kPipeW0Rows + rs + 1) * kPipeStride;
+      const float* bb = C1 + (kPipeW0Rows + kPipeW1Rows + rs + 1) * kPipeStride;
+      const float* z1 = WS + xslot(-1) * kPipeWSlot + (rs + 1) * kPipeStride;
+      const float* z2 = W20 + (rs + 1) * kPipeStride;
+      float* out = xout + pzm * plane + (int64_t)js * d.nx + i0 + 4 * lane;
+      if ((c0 + js + pzm) & 1)
+        PipeSecond<1>(f0, f0 - kPipeStride, f0 + kPipeStride, Fm + (rs + 2) * kPipeStride,
+                      X0 + (rs + 2) * kPipeStride, w0, w1, w1 + kPipeStride, bb, z1, z2, l,
+                      out);
+      else
+        PipeSecond<0>(f0, f0 - kPipeStride, f0 + kPipeStride, Fm + (rs + 2) * kPipeStride,
+                      X0 + (rs + 2) * kPipeStride, w0, w1, w1 + kPipeStride, bb, z1, z2, l,
+                      out);
+    }
+    // first colour of the halo columns of plane t (read by S(t))
+    if (h_on && t >= kb && t < ke && ((colh + jh + pz + c0) & 1) == 0) {
+      const int lh = colh + 4;
+      float* xc = X0 + (rh + 2) * kPipeStride;
+      const float* w1 = C0 + (kPipeW0Rows + rh + 1) * kPipeStride;
+      PipeFirstCell<ZI>(xc, xc - kPipeStride, xc + kPipeStride, Xm1 + (rh + 2) * kPipeStride,
+                        Xp1 + (rh + 2) * kPipeStride, C0 + (rh + 1) * kPipeStride, w1,
+                        w1 + kPipeStride,
+                        C0 + (kPipeW0Rows + kPipeW1Rows + rh + 1) * kPipeStride,
+                        W20 + (rh + 1) * kPipeStride, W2p + (rh + 1) * kPipeStride, lh);
+    }
+    // B(t+kPipeAhead): x_in and w2 of plane t+kPipeAhead+1, coefficients of
+    // t+kPipeAhead (their slots were last read before this step's barrier)
+    if (t + kPipeAhead <= ke) {
+      const int kc = kPipeAhead, kx = kPipeAhead + 1;
+      const int pc = pz + kc >= d.nz ? pz + kc - d.nz : pz + kc;
+      const int px = pz + kx >= d.nz ? pz + kx - d.nz : pz + kx;
+      const uint32_t xsl = (uint32_t)xslot(kx - kPipeXs);
+      if (!ZI) PipeCopy(xs_addr + 4u * xsl * kPipeXSlot, xin + px * plane, cx);
+      const uint32_t cslot = cs_addr + 4u * ((t + kc - base) & (kPipeCs - 1)) * kPipeCSlot;
+      PipeCopy(cslot, A.w0 + pc * plane, c0w);
+      PipeCopy(cslot, A.w1 + pc * plane, c1w);
+      PipeCopy(cslot, b + pc * plane, cbb);
+      PipeCopy(ws_addr + 4u * xsl * kPipeWSlot, A.w2 + px * plane, c2w);
+    }
+    CpAsyncCommit();
+    // L2 prefetch of the rows of B(t+kPipeAhead+kPipePrefetch)
+    if (pf_bytes && t + kPipeAhead + kPipePrefetch <= ke) {
+      const int k = kPipeAhead + kPipePrefetch + (pf_coef ? 0 : 1);
+      const int pp = pz + k >= d.nz ? pz + k - d.nz : pz + k;
+      PrefetchBulkL2(pf_src + pp * plane, pf_bytes);
+    }
+    ph = ph + 1 == kPipeXs ? 0 : ph + 1;
+    pz = pz + 1 == d.nz ? 0 : pz + 1;
   }
   CpAsyncWait<0>();
 }

@@ -379,32 +379,14 @@ __global__ void KReconstructList(Dims d, double hx, double hy, double hz,
   }
 }
 
-// Fluxes of Vof::Sweep (vof.ipp:228-256) through the faces of direction dir
-// whose upwind cell is not interfacial: v * u(upwind) (the face flux v / 1.
-// of the reference is v); faces with an interfacial upwind cell are written
-// by KSweepFluxList.
-__global__ void KSweepFlux(Dims d, int dir, const double* __restrict__ u,
-                           const double* __restrict__ vflux, double* ffvu) {
-  VOF_CELL_LOOP(d)
-  const int64_t cm = dir == 0 ? d.idx(wrapm(i - 1, d.nx), j, k)
-                   : dir == 1 ? d.idx(i, wrapm(j - 1, d.ny), k)
-                              : d.idx(i, j, wrapm(k - 1, d.nz));
-  // both candidate upwind values are loaded with the flux (one round trip
-  // to memory instead of two dependent ones)
-  const double v = vflux[c];
-  const double um = u[cm], uc = u[c];
-  const long long vb = Bits(v);
-  const double uu = PositiveBits(vb) ? um : uc;
-  const long long ub = Bits(uu);
-  if (InterfaceBits(ub)) continue;
-  // finite v: v * (+0) is the zero with the sign of v, v * 1 is v
+// v * uu for a face whose upwind value uu is not interfacial; for finite v,
+// v * (+0) is the zero with the sign of v and v * 1 is v (no FP64 multiply)
+__device__ __forceinline__ double BulkFlux(double v, double uu) {
+  const long long vb = Bits(v), ub = Bits(uu);
   const bool fin = ExpBits(vb) != 0x7FF;
-  double f;
-  if (fin && ub == 0) f = copysign(0.0, v);
-  else if (fin && ub == kOneBits) f = v;
-  else f = v * uu;
-  ffvu[c] = f;
-  }
+  if (fin && ub == 0) return copysign(0.0, v);
+  if (fin && ub == kOneBits) return v;
+  return v * uu;
 }
 
 // Flux of a face with interfacial upwind cell (normal n, plane constant a,
@@ -450,65 +432,92 @@ __global__ void KSweepFluxList(Dims d, int dir, double hx, double hy, double hz,
 // arithmetic makes them unnecessary, with bit-identical results: a zero
 // numerator gives a zero of the same sign; fcuu = 0 makes fcuu * ds a zero
 // with the sign of ds (finite); fcuu = 1 with equal numerators makes
-// ds - dl = +0.  That covers every cell away from the interface.  Cells
-// interfacial after the update are appended to the list.
-__global__ void KSweepUpdate(Dims d, int dir, double vol, double* u,
-                             const double* __restrict__ vflux,
-                             const double* __restrict__ ffvu,
-                             const uint8_t* __restrict__ fcuu, double dt,
-                             double clipth, int emax, int full_ok, int* list,
-                             int* count) {
+// ds - dl = +0.  That covers every cell away from the interface.
+// UpdateCell: one cell (fc = fcuu, uc = u, face fluxes v0 v1 and fluid
+// fluxes f0 f1 of its lower and upper face); returns true for a bulk cell
+// (u unchanged, w not set), else the new value in w.
+__device__ __forceinline__ bool UpdateCell(int fc, double uc, double v0, double v1, double f0,
+                                           double f1, double vol, double big, double dt,
+                                           double clipth, int emax, int full_ok, double& w) {
+  const long long ub = Bits(uc);
+  const long long a0 = Bits(v0), a1 = Bits(v1), b0 = Bits(f0), b1 = Bits(f1);
+  // magnitudes below 2^(emax-1023): every difference times dt / vol below
+  // is finite
+  const bool fin =
+      ExpBits(a0) < emax && ExpBits(a1) < emax && ExpBits(b0) < emax && ExpBits(b1) < emax;
+  // bulk cells, no FP64 instruction: empty (u = +0, fcuu = 0, zero fluid
+  // fluxes: u + (0*ds - dl) is +0 and stays +0 when clipped) and full (u =
+  // 1, fcuu = 1, fluid fluxes equal to the face fluxes: ds - dl = +0, u
+  // stays 1 for clipth <= 1); u is unchanged
+  const bool bulk = fin && ((ub == 0 && fc == 0 && ((b0 | b1) << 1) == 0) ||
+                            (full_ok && ub == kOneBits && fc == 1 && a0 == b0 && a1 == b1));
+  if (bulk) return true;
+  const double dsn = (v1 - v0) * dt;
+  const double dln = (f1 - f0) * dt;
+  const double dl = dln == 0 ? dln : dln / vol;
+  double t;
+  if (fc == 0 && fabs(dsn) <= big) {
+    t = copysign(0.0, dsn) - dl;
+  } else if (fc == 1 && fabs(dsn) <= big && Bits(dsn) == Bits(dln)) {
+    t = 0.0;
+  } else {
+    t = (double)fc * (dsn / vol) - dl;
+  }
+  w = uc;
+  w += t;
+  if (!(w >= clipth)) {
+    w = 0;
+  } else if (!(w <= 1 - clipth)) {
+    w = 1;
+  }
+  return false;
+}
+
+// Fluid fluxes and update of one direction of Vof::Sweep (vof.ipp:228-256,
+// 287-326) in one pass, out of place.  The flux of a face whose upwind cell
+// is not interfacial is v * u(upwind) of the old volume fraction uin
+// (BulkFlux: the face flux v / 1. of the reference is v); the faces with an
+// interfacial upwind cell are read from ffvu, written before by
+// KSweepFluxList.  Every cell of uout is written (bulk cells with their old
+// value); cells interfacial after the update are appended to the list.
+// Per cell: uin and vflux read once (the neighbours' values come from
+// cache), fcuu read, uout written.
+__global__ void KSweepFused(Dims d, int dir, double vol, const double* __restrict__ uin,
+                            double* __restrict__ uout, const double* __restrict__ vflux,
+                            const double* __restrict__ ffvu,
+                            const uint8_t* __restrict__ fcuu, double dt, double clipth,
+                            int emax, int full_ok, int* list, int* count) {
   const int i = blockIdx.x * kTileX + threadIdx.x;
   const int j = blockIdx.y * kTileY + threadIdx.y;
   const int kb = blockIdx.z * kTileZ;
   const int ke = min(kb + kTileZ, d.nz);
   const bool in = i < d.nx && j < d.ny;
-  const double big = vol * 1e300;  // |num| below this: num / vol is finite
+  const double big = vol * 1e300;
   for (int k = kb; k < ke; ++k) {
     int64_t c = 0;
     bool want = false;
     if (in) {
       c = d.idx(i, j, k);
+      const int64_t cm = dir == 0 ? d.idx(wrapm(i - 1, d.nx), j, k)
+                       : dir == 1 ? d.idx(i, wrapm(j - 1, d.ny), k)
+                                  : d.idx(i, j, wrapm(k - 1, d.nz));
       const int64_t fp = dir == 0 ? d.idx(wrapp(i + 1, d.nx), j, k)
                        : dir == 1 ? d.idx(i, wrapp(j + 1, d.ny), k)
                                   : d.idx(i, j, wrapp(k + 1, d.nz));
-      const int fc = fcuu[c];
-      const double v0 = vflux[c], v1 = vflux[fp], f0 = ffvu[c], f1 = ffvu[fp];
-      const long long ub = Bits(u[c]);
-      const long long a0 = Bits(v0), a1 = Bits(v1), b0 = Bits(f0), b1 = Bits(f1);
-      // magnitudes below 2^(emax-1023): every difference times dt / vol
-      // below is finite
-      const bool fin =
-          ExpBits(a0) < emax && ExpBits(a1) < emax && ExpBits(b0) < emax && ExpBits(b1) < emax;
-      // bulk cells, no FP64 instruction: empty (u = +0, fcuu = 0, zero
-      // fluid fluxes: u + (0*ds - dl) is +0 and stays +0 when clipped) and
-      // full (u = 1, fcuu = 1, fluid fluxes equal to the face fluxes:
-      // ds - dl = +0, u stays 1 for clipth <= 1); u is unchanged
-      const bool bulk =
-          fin && ((ub == 0 && fc == 0 && ((b0 | b1) << 1) == 0) ||
-                  (full_ok && ub == kOneBits && fc == 1 && a0 == b0 && a1 == b1));
-      if (!bulk) {
-        const double dsn = (v1 - v0) * dt;
-        const double dln = (f1 - f0) * dt;
-        const double dl = dln == 0 ? dln : dln / vol;
-        double t;
-        if (fc == 0 && fabs(dsn) <= big) {
-          t = copysign(0.0, dsn) - dl;
-        } else if (fc == 1 && fabs(dsn) <= big && Bits(dsn) == Bits(dln)) {
-          t = 0.0;
-        } else {
-          t = (double)fc * (dsn / vol) - dl;
-        }
-        double w = __longlong_as_double(ub);
-        w += t;
-        if (!(w >= clipth)) {
-          w = 0;
-        } else if (!(w <= 1 - clipth)) {
-          w = 1;
-        }
-        u[c] = w;
+      const double v0 = vflux[c], v1 = vflux[fp];
+      const double um = uin[cm], uc = uin[c], up = uin[fp];
+      // upwind values of the lower face (c) and the upper face (fp)
+      const double u0 = PositiveBits(Bits(v0)) ? um : uc;
+      const double u1 = PositiveBits(Bits(v1)) ? uc : up;
+      const double f0 = InterfaceBits(Bits(u0)) ? ffvu[c] : BulkFlux(v0, u0);
+      const double f1 = InterfaceBits(Bits(u1)) ? ffvu[fp] : BulkFlux(v1, u1);
+      double w;
+      if (UpdateCell(fcuu[c], uc, v0, v1, f0, f1, vol, big, dt, clipth, emax, full_ok, w)) {
+        w = uc;
+      } else {
         want = InterfaceBits(Bits(w));
       }
+      uout[c] = w;
     }
     ListAppend(want, (int)c, list, count);
   }
@@ -714,11 +723,10 @@ int ReconstructListed(aphgpu_ctx* ctx, const VofScratch& sc) {
   return APHGPU_OK;
 }
 
-int SweepFlux(aphgpu_ctx* ctx, const VofScratch& sc, int dir, const double* vf, double dt) {
+// fluid fluxes of the faces of direction dir with an interfacial upwind cell
+int SweepFluxList(aphgpu_ctx* ctx, const VofScratch& sc, int dir, const double* vf,
+                  double dt) {
   const double h = ctx->h;
-  KSweepFlux<<<TileGrid(ctx->d), TileBlock(), 0, ctx->stream>>>(ctx->d, dir, ctx->u, vf,
-                                                                 ctx->ffvu);
-  APH_LAUNCHED(ctx);
   KSweepFluxList<<<ListGrid(ctx), 256, 0, ctx->stream>>>(ctx->d, dir, h, h, h, ctx->u, vf,
                                                           ctx->nrm, ctx->pa, dt, ctx->ffvu,
                                                           sc.list, sc.count);
@@ -726,7 +734,10 @@ int SweepFlux(aphgpu_ctx* ctx, const VofScratch& sc, int dir, const double* vf, 
   return APHGPU_OK;
 }
 
-int SweepUpdate(aphgpu_ctx* ctx, const VofScratch& sc, int dir, const double* vf, double dt) {
+// the fused flux + update of direction dir from ctx->u into ctx->u_alt,
+// then (swap) the two buffers exchanged: ctx->u is the new volume fraction
+int SweepUpdate(aphgpu_ctx* ctx, const VofScratch& sc, int dir, const double* vf, double dt,
+                bool swap) {
   const double h = ctx->h;
   APH_CUDA(ctx, cudaMemsetAsync(sc.count, 0, sizeof(int), ctx->stream));
   const double vol = (h * h) * h;
@@ -742,10 +753,11 @@ int SweepUpdate(aphgpu_ctx* ctx, const VofScratch& sc, int dir, const double* vf
     if (adt > 1) e = std::min(e, std::floor(2021.0 - std::log2(adt)));
     emax = (int)std::max(0.0, e);
   }
-  KSweepUpdate<<<TileGrid(ctx->d), TileBlock(), 0, ctx->stream>>>(
-      ctx->d, dir, vol, ctx->u, vf, ctx->ffvu, sc.fcuu, dt, ctx->clipth, emax,
+  KSweepFused<<<TileGrid(ctx->d), TileBlock(), 0, ctx->stream>>>(
+      ctx->d, dir, vol, ctx->u, ctx->u_alt, vf, ctx->ffvu, sc.fcuu, dt, ctx->clipth, emax,
       ctx->clipth <= 1 ? 1 : 0, sc.list, sc.count);
   APH_LAUNCHED(ctx);
+  if (swap) std::swap(ctx->u, ctx->u_alt);
   return APHGPU_OK;
 }
 
@@ -776,8 +788,8 @@ int VofStepDevice(aphgpu_ctx* ctx, const double* d_vflux, double dt) {
   for (int id = 0; id < 3; ++id) {
     const int dir = dd[id];
     const double* vf = d_vflux + (int64_t)dir * N;
-    APH_TRY(SweepFlux(ctx, sc, dir, vf, dt));
-    APH_TRY(SweepUpdate(ctx, sc, dir, vf, dt));
+    APH_TRY(SweepFluxList(ctx, sc, dir, vf, dt));
+    APH_TRY(SweepUpdate(ctx, sc, dir, vf, dt, true));
     APH_TRY(ReconstructListed(ctx, sc));
   }
   ctx->vof_count += 1;
@@ -810,23 +822,23 @@ int TimeVofKernel(aphgpu_ctx* ctx, int kernel, int reps, double* ms, double* byt
   APH_CUDA(ctx, cudaStreamSynchronize(st));
   double b = 0;
   switch (kernel) {
-    // bulk faces: u (upwind), flux, ffvu; interfacial cells: index, normal,
-    // plane constant, u, two faces each way
-    case APHGPU_K_VOF_FLUX: b = N * (8 + 8 + 8) + nif * (4.0 + 24 + 8 + 8 + 32); break;
-    // u r/w, flux, ffvu, fcuu, list entries
-    case APHGPU_K_VOF_UPDATE: b = N * (8 + 8 + 8 + 8 + 1) + nif * 4.0; break;
+    // interfacial cells: index, normal, plane constant, u, two faces each way
+    case APHGPU_K_VOF_FLUX: b = nif * (4.0 + 24 + 8 + 8 + 32); break;
+    // u read and written, flux, fcuu, list entries
+    case APHGPU_K_VOF_UPDATE: b = N * (8 + 8 + 8 + 1) + nif * 4.0; break;
     // listed cells: index, u, normal and plane constant written
     case APHGPU_K_RECONSTRUCT: b = nif * (4.0 + 8 + 24 + 8); break;
     case APHGPU_K_HEIGHTS: b = N * 8; break;
     case APHGPU_K_CURVATURE: b = N * (8 + 8); break;  // u, kappa
     default: return SetError(ctx, APHGPU_ERR_ARG, "unknown kernel %d", kernel);
   }
-  // flux and update of the x direction with the last step's time step: the
-  // update advances u again (state left modified)
+  // flux and update of the x direction with the last step's time step (the
+  // update writes the scratch copy of u: the state is left as it was, the
+  // interface list as the update leaves it)
   auto launch = [&]() -> int {
     switch (kernel) {
-      case APHGPU_K_VOF_FLUX: return SweepFlux(ctx, sc, 0, d_vflux, dt);
-      case APHGPU_K_VOF_UPDATE: return SweepUpdate(ctx, sc, 0, d_vflux, dt);
+      case APHGPU_K_VOF_FLUX: return SweepFluxList(ctx, sc, 0, d_vflux, dt);
+      case APHGPU_K_VOF_UPDATE: return SweepUpdate(ctx, sc, 0, d_vflux, dt, false);
       case APHGPU_K_RECONSTRUCT: return ReconstructListed(ctx, sc);
       case APHGPU_K_HEIGHTS:
         KHeights<<<TileGrid(d), TileBlock(), 0, st>>>(d, h, h, h, ctx->u, ctx->hgt);

@@ -999,6 +999,8 @@ def run_profile(args):
     _, bnorm = ctx.residual_norms()
     tol = 1e-10 * bnorm / math.sqrt(case.h ** 3)
     solver = _lib.SOLVER_MGPCG if args.profile == "fp64" else _lib.SOLVER_MIXED
+    if args.sweeps is not None:
+        ctx.set_option(_lib.OPT_FUSED_SWEEPS, args.sweeps)
     if args.cycle == 1:
         # the configuration's V-cycle (as in the headline, whose mixed solve
         # stops at HEADLINE_STOP)
@@ -1010,7 +1012,8 @@ def run_profile(args):
         conf = _lib.default_conf(solver=solver, tol=tol)
     if args.profile == "vof":
         # one solve, the corrected fluxes, then `warmup` + `steps` PLIC steps
-        # with the height curvature after each
+        # with the height curvature and the recolouring after each (as the
+        # VOF measurement of the benchmark line)
         ctx.solve_resident(conf, zero_guess=True)
         ctx.flux_correct(out=False)
         ctx.vof_init(case.alpha)
@@ -1018,6 +1021,7 @@ def run_profile(args):
         for _ in range(args.warmup + args.steps):
             ctx.vof_step(None, dt)
             ctx.curvature(out=False)
+            ctx.vof_recolor()
         print("profile vof: %d steps of %d^3" % (args.warmup + args.steps, case.n))
         return
     for _ in range(args.warmup + args.steps):
@@ -1046,6 +1050,8 @@ def main():
     ap.add_argument("--profile", choices=["mixed", "fp64", "batch", "vof"], default=None,
                     help="profiling run: assemble, then `steps` solves of one solver "
                          "after `warmup` solves, no other work and no output line")
+    ap.add_argument("--sweeps", type=int, choices=[0, 1, 2, 3, 4], default=None,
+                    help="--profile: red-black sweep variant (APHGPU_OPT_FUSED_SWEEPS)")
     ap.add_argument("--serve", action="store_true",
                     help="served-stream benchmark instead of the solve benchmark")
     ap.add_argument("--sims", type=int, default=2000)

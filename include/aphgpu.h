@@ -427,13 +427,15 @@ int aphgpu_batch_last_ms(const aphgpu_batch* batch, double* ms, int64_t* launche
  *                            two half sweeps) on the FP32 levels: 1
  *                            the pipelined kernel, fed by asynchronous
  *                            copies into shared memory, on levels of at
- *                            least 2^21 cells with nx a multiple of 4 and
- *                            no stored diagonal; 2 the pipelined kernel on
+ *                            least 2^21 cells with nx a multiple of 4,
+ *                            nx >= 16, nz >= 8 and no stored diagonal; 2
+ *                            the pipelined kernel on
  *                            every such level whatever its size; 3 the
  *                            synchronous fused kernel (latency-bound) on
  *                            every level with nx a multiple of 4, nx >= 8;
- *                            0 (default) two in-place half sweeps
- *                            everywhere.  Other
+ *                            4 as 1 with bands of 6 rows (two CTAs per
+ *                            SM instead of one); 0 (default) two
+ *                            in-place half sweeps everywhere.  Other
  *                            levels take the half sweeps
  *   APHGPU_OPT_HALF_COUPLINGS 1: the smoother and the restriction of the
  *                            finest FP32 level read an FP16 copy of the
@@ -486,8 +488,10 @@ enum {
   APHGPU_K_APPLY64 = 2,    /* FP64 y = A p with the p.y reduction */
   APHGPU_K_APPLY32 = 3,    /* FP32 y = A p with the p.y reduction */
   APHGPU_K_RESTRICT32 = 4, /* FP32 residual + restriction, finest level */
-  APHGPU_K_VOF_FLUX = 5,   /* VOF fluid fluxes of one direction */
-  APHGPU_K_VOF_UPDATE = 6, /* VOF update of one direction */
+  APHGPU_K_VOF_FLUX = 5,   /* VOF fluid fluxes of one direction through the
+                              faces with an interfacial upwind cell */
+  APHGPU_K_VOF_UPDATE = 6, /* VOF fluxes of the other faces and update of one
+                              direction (one fused pass) */
   APHGPU_K_RECONSTRUCT = 7,/* interface normals and plane constants */
   APHGPU_K_HEIGHTS = 8,    /* height functions */
   APHGPU_K_CURVATURE = 9,  /* curvature from heights */

@@ -258,8 +258,8 @@ def test_full_size_property_256():
 @pytest.mark.parametrize("shape", [(64, 64, 64), (96, 48, 40), (40, 24, 32), (128, 128, 128)])
 def test_fused_sweeps_bit_identical(solver, shape):
     """The fused out-of-place red-black sweeps -- the pipelined kernel fed
-    by bulk copies (mode 2: on every level with nx % 4 == 0 and nx >= 16;
-    mode 1, the default: on levels of at least 2^21 cells) and the
+    by asynchronous copies (mode 2: on every level with nx % 4 == 0, nx >=
+    16 and nz >= 8; mode 1: on such levels of at least 2^21 cells) and the
     synchronous kernel (mode 3) -- compute every value with the operations
     of the two in-place half sweeps (mode 0): whole solves agree bit for bit
     (with and without CUDA graphs)."""
@@ -279,7 +279,7 @@ def test_fused_sweeps_bit_identical(solver, shape):
     _, bn = ctx.residual_norms()
     conf = _lib.default_conf(solver=solver, tol=1e-10 * bn / math.sqrt(h ** 3), maxiter=200)
     out = {}
-    for fused in (2, 1, 3, 0):
+    for fused in (2, 1, 4, 3, 0):
         for graphs in (1, 0):
             ctx.set_option(_lib.OPT_FUSED_SWEEPS, fused)
             ctx.set_option(_lib.OPT_GRAPHS, graphs)
