@@ -308,6 +308,8 @@ struct aphgpu_ctx {
   double* u = nullptr;
   double* u_alt = nullptr;     // N, written by each directional update, then
                                // exchanged with u
+  bool vof_list_valid = false; // the scratch list holds the interfacial
+                               // cells of u
   double* u0 = nullptr;
   double* nrm = nullptr;       // 3N AoS
   double* pa = nullptr;        // plane constant

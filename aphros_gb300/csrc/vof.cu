@@ -493,33 +493,54 @@ __global__ void KSweepFused(Dims d, int dir, double vol, const double* __restric
   const int ke = min(kb + kTileZ, d.nz);
   const bool in = i < d.nx && j < d.ny;
   const double big = vol * 1e300;
+  // the loads of plane k+1 are issued before plane k is computed: two
+  // planes of loads in flight per thread
+  struct Plane {
+    double v0, v1, um, uc, up;
+    int fc;
+  };
+  auto load = [&](int k, Plane& q) {
+    const int64_t c = d.idx(i, j, k);
+    const int64_t cm = dir == 0 ? d.idx(wrapm(i - 1, d.nx), j, k)
+                     : dir == 1 ? d.idx(i, wrapm(j - 1, d.ny), k)
+                                : d.idx(i, j, wrapm(k - 1, d.nz));
+    const int64_t fp = dir == 0 ? d.idx(wrapp(i + 1, d.nx), j, k)
+                     : dir == 1 ? d.idx(i, wrapp(j + 1, d.ny), k)
+                                : d.idx(i, j, wrapp(k + 1, d.nz));
+    q.v0 = vflux[c];
+    q.v1 = vflux[fp];
+    q.um = uin[cm];
+    q.uc = uin[c];
+    q.up = uin[fp];
+    q.fc = fcuu[c];
+  };
+  Plane cur{}, nxt{};
+  if (in && kb < ke) load(kb, cur);
   for (int k = kb; k < ke; ++k) {
+    if (in && k + 1 < ke) load(k + 1, nxt);
     int64_t c = 0;
     bool want = false;
     if (in) {
       c = d.idx(i, j, k);
-      const int64_t cm = dir == 0 ? d.idx(wrapm(i - 1, d.nx), j, k)
-                       : dir == 1 ? d.idx(i, wrapm(j - 1, d.ny), k)
-                                  : d.idx(i, j, wrapm(k - 1, d.nz));
       const int64_t fp = dir == 0 ? d.idx(wrapp(i + 1, d.nx), j, k)
                        : dir == 1 ? d.idx(i, wrapp(j + 1, d.ny), k)
                                   : d.idx(i, j, wrapp(k + 1, d.nz));
-      const double v0 = vflux[c], v1 = vflux[fp];
-      const double um = uin[cm], uc = uin[c], up = uin[fp];
       // upwind values of the lower face (c) and the upper face (fp)
-      const double u0 = PositiveBits(Bits(v0)) ? um : uc;
-      const double u1 = PositiveBits(Bits(v1)) ? uc : up;
-      const double f0 = InterfaceBits(Bits(u0)) ? ffvu[c] : BulkFlux(v0, u0);
-      const double f1 = InterfaceBits(Bits(u1)) ? ffvu[fp] : BulkFlux(v1, u1);
+      const double u0 = PositiveBits(Bits(cur.v0)) ? cur.um : cur.uc;
+      const double u1 = PositiveBits(Bits(cur.v1)) ? cur.uc : cur.up;
+      const double f0 = InterfaceBits(Bits(u0)) ? ffvu[c] : BulkFlux(cur.v0, u0);
+      const double f1 = InterfaceBits(Bits(u1)) ? ffvu[fp] : BulkFlux(cur.v1, u1);
       double w;
-      if (UpdateCell(fcuu[c], uc, v0, v1, f0, f1, vol, big, dt, clipth, emax, full_ok, w)) {
-        w = uc;
+      if (UpdateCell(cur.fc, cur.uc, cur.v0, cur.v1, f0, f1, vol, big, dt, clipth, emax,
+                     full_ok, w)) {
+        w = cur.uc;
       } else {
         want = InterfaceBits(Bits(w));
       }
       uout[c] = w;
     }
     ListAppend(want, (int)c, list, count);
+    cur = nxt;
   }
 }
 
@@ -544,111 +565,159 @@ __device__ double HeightGood(const double uu[13]) {
   return nan("");
 }
 
-// CalcDiff2/CalcDiff4/CalcHeight (curv.ipp:100-254) fused per interfacial
-// cell: the column is rebuilt exactly as CalcHeight does from the
-// two-step differences du2(q) = u(q+2) - u(q-2) and four-step differences
-// du4(q) = du2(q+2) - du2(q-2).
-__global__ void KHeights(Dims d, double hx, double hy, double hz,
-                         const double* __restrict__ u, double* hgt) {
-  const double h[3] = {hx, hy, hz};
-  VOF_CELL_LOOP(d)
-  if (!IsInterface(u[c])) continue;
-  const int w[3] = {i, j, k};
-  const int nd[3] = {d.nx, d.ny, d.nz};
-#pragma unroll 1
-  for (int dd = 0; dd < 3; ++dd) {
-    double uc[13];  // u at offsets -6..6 along dd
+// Index q wrapped into [0, n) (periodic); one correction covers offsets
+// smaller than n, the remainder the rest.
+__device__ __forceinline__ int WrapAny(int q, int n) {
+  if (q < 0) {
+    q += n;
+    if (q < 0) q = (q % n + n) % n;
+  } else if (q >= n) {
+    q -= n;
+    if (q >= n) q %= n;
+  }
+  return q;
+}
+
+// Linear index of cell (i, j, k) shifted by o along axis A (periodic).
+template <int A>
+__device__ __forceinline__ int64_t ShiftIdx(const Dims& d, int i, int j, int k, int o) {
+  if (A == 0) return d.idx(WrapAny(i + o, d.nx), j, k);
+  if (A == 1) return d.idx(i, WrapAny(j + o, d.ny), k);
+  return d.idx(i, j, WrapAny(k + o, d.nz));
+}
+
+// Height of an interfacial cell along axis A: CalcDiff2/CalcDiff4/
+// CalcHeight (curv.ipp:100-254) fused; the 13-cell column is rebuilt
+// exactly as CalcHeight does from the two-step differences du2(q) = u(q+2)
+// - u(q-2) and the four-step differences du4(q) = du2(q+2) - du2(q-2).
+template <int A>
+__device__ __forceinline__ double HeightAlong(const Dims& d, double hA, int i, int j, int k,
+                                              const double* __restrict__ u) {
+  double uc[13];  // u at offsets -6..6 along A
 #pragma unroll
-    for (int s = -6; s <= 6; ++s) {
-      int q[3] = {i, j, k};
-      q[dd] = ((w[dd] + s) % nd[dd] + nd[dd]) % nd[dd];
-      uc[s + 6] = u[d.idx(q[0], q[1], q[2])];
-    }
+  for (int s = -6; s <= 6; ++s) uc[s + 6] = u[ShiftIdx<A>(d, i, j, k, s)];
 #define U(s) uc[(s) + 6]
 #define DU2(s) ((0 + -1 * U((s)-2)) + 1 * U((s) + 2))
 #define DU4(s) ((0 + -1 * DU2((s)-2)) + 1 * DU2((s) + 2))
-    double uu[13];
-    uu[6] = U(0);
-    uu[5] = U(-1);
-    uu[7] = U(1);
-    uu[4] = U(-2);
-    uu[8] = U(2);
-    uu[3] = uu[7] - DU2(-1);
-    uu[9] = uu[5] + DU2(1);
-    uu[2] = uu[6] - DU2(-2);
-    uu[10] = uu[6] + DU2(2);
-    uu[1] = uu[9] - DU4(-1);
-    uu[11] = uu[3] + DU4(1);
-    uu[0] = uu[8] - DU4(-2);
-    uu[12] = uu[4] + DU4(2);
+  double uu[13];
+  uu[6] = U(0);
+  uu[5] = U(-1);
+  uu[7] = U(1);
+  uu[4] = U(-2);
+  uu[8] = U(2);
+  uu[3] = uu[7] - DU2(-1);
+  uu[9] = uu[5] + DU2(1);
+  uu[2] = uu[6] - DU2(-2);
+  uu[10] = uu[6] + DU2(2);
+  uu[1] = uu[9] - DU4(-1);
+  uu[11] = uu[3] + DU4(1);
+  uu[0] = uu[8] - DU4(-2);
+  uu[12] = uu[4] + DU4(2);
 #undef DU4
 #undef DU2
 #undef U
-    const double off = HeightGood(uu);
-    const double center = (0. + h[dd] * 0.5) + (double)w[dd] * h[dd];
-    hgt[3 * c + dd] = center + off * h[dd];
-  }
+  const double off = HeightGood(uu);
+  const int wA = A == 0 ? i : A == 1 ? j : k;
+  const double center = (0. + hA * 0.5) + (double)wA * hA;
+  return center + off * hA;
+}
+
+// Heights of the listed interfacial cells (the heights of the other cells
+// are never read: the curvature reads the heights of interfacial cells).
+__global__ void KHeightsList(Dims d, double hx, double hy, double hz,
+                             const double* __restrict__ u, double* hgt,
+                             const int* __restrict__ list, const int* count) {
+  const int n = *count;
+  for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < n; t += gridDim.x * blockDim.x) {
+    const int64_t c = list[t];
+    int i, j, k;
+    CellIJK(d, c, i, j, k);
+    hgt[3 * c] = HeightAlong<0>(d, hx, i, j, k, u);
+    hgt[3 * c + 1] = HeightAlong<1>(d, hy, i, j, k, u);
+    hgt[3 * c + 2] = HeightAlong<2>(d, hz, i, j, k, u);
   }
 }
 
-// CalcCurvHeight (curv.ipp:261-356); NaN outside the interface
-__global__ void KCurvature(Dims d, double hx, double hy, double hz,
-                           const double* __restrict__ u,
-                           const double* __restrict__ nrm,
-                           const double* __restrict__ hgt, double* kappa) {
-  const double h[3] = {hx, hy, hz};
-  VOF_CELL_LOOP(d)
-  if (!IsInterface(u[c])) {
-    kappa[c] = nan("");
-    continue;
+// Height of column (sx, sy) of the 3x3 stencil around (i, j, k) in the
+// plane across axis dn (dx = dn+1, dy = dn+2 mod 3): the height of the
+// first interfacial cell among the shifts 0, 1, -1, 2, -2 along dn, NaN if
+// none (CalcCurvHeight, curv.ipp:261-356).
+__device__ __forceinline__ double ColumnHeight(const Dims& d, int i, int j, int k, int dn,
+                                               int sx, int sy,
+                                               const double* __restrict__ u,
+                                               const double* __restrict__ hgt) {
+  const int dx = dn == 2 ? 0 : dn + 1, dy = dn == 0 ? 2 : dn - 1;
+  const int bi = i + (dx == 0 ? sx : 0) + (dy == 0 ? sy : 0);
+  const int bj = j + (dx == 1 ? sx : 0) + (dy == 1 ? sy : 0);
+  const int bk = k + (dx == 2 ? sx : 0) + (dy == 2 ? sy : 0);
+  const int shifts[5] = {0, 1, -1, 2, -2};
+#pragma unroll
+  for (int t = 0; t < 5; ++t) {
+    const int o = shifts[t];
+    const int64_t cn = d.idx(WrapAny(bi + (dn == 0 ? o : 0), d.nx),
+                             WrapAny(bj + (dn == 1 ? o : 0), d.ny),
+                             WrapAny(bk + (dn == 2 ? o : 0), d.nz));
+    if (IsInterface(u[cn])) return hgt[3 * cn + dn];
   }
-  const double n[3] = {nrm[3 * c], nrm[3 * c + 1], nrm[3 * c + 2]};
-  const double an[3] = {fabs(n[0]), fabs(n[1]), fabs(n[2])};
-  int dn = 0;
-  if (an[1] > an[dn]) dn = 1;
-  if (an[2] > an[dn]) dn = 2;
-  const int dx = (dn + 1) % 3, dy = (dn + 2) % 3;
-  const double lx = h[dx], ly = h[dy];
-  const int nd[3] = {d.nx, d.ny, d.nz};
-  const int w[3] = {i, j, k};
-  double hv[3][3];
-  for (int sy = -1; sy <= 1; ++sy)
-    for (int sx = -1; sx <= 1; ++sx) {
-      int b[3] = {w[0], w[1], w[2]};
-      b[dx] += sx;
-      b[dy] += sy;
-      double r = nan("");
-      const int shifts[5] = {0, 1, -1, 2, -2};
-      for (int t = 0; t < 5; ++t) {
-        int q[3] = {b[0], b[1], b[2]};
-        q[dn] += shifts[t];
-        for (int e = 0; e < 3; ++e) q[e] = ((q[e] % nd[e]) + nd[e]) % nd[e];
-        const int64_t cn = d.idx(q[0], q[1], q[2]);
-        if (IsInterface(u[cn])) {
-          r = hgt[3 * cn + dn];
-          break;
-        }
-      }
-      hv[sy + 1][sx + 1] = r;
+  return nan("");
+}
+
+// CalcCurvHeight (curv.ipp:261-356) on the listed interfacial cells (kappa
+// of the other cells is set to NaN by KFillNan before).
+__global__ void KCurvatureList(Dims d, double hx, double hy, double hz,
+                               const double* __restrict__ u,
+                               const double* __restrict__ nrm,
+                               const double* __restrict__ hgt, double* kappa,
+                               const int* __restrict__ list, const int* count) {
+  const int n = *count;
+  for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < n; t += gridDim.x * blockDim.x) {
+    const int64_t c = list[t];
+    int i, j, k;
+    CellIJK(d, c, i, j, k);
+    const double n0 = nrm[3 * c], n1 = nrm[3 * c + 1], n2 = nrm[3 * c + 2];
+    const double a0 = fabs(n0), a1 = fabs(n1), a2 = fabs(n2);
+    int dn = 0;
+    double amax = a0;
+    if (a1 > amax) {
+      dn = 1;
+      amax = a1;
     }
-  const double hcc = hv[1][1], hmc = hv[1][0], hpc = hv[1][2];
-  const double hcm = hv[0][1], hcp = hv[2][1];
-  const double hmm = hv[0][0], hmp = hv[2][0], hpm = hv[0][2], hpp = hv[2][2];
-  const double hxd = (hpc - hmc) / (2 * lx);
-  const double hyd = (hcp - hcm) / (2 * ly);
-  const double fl = 0.2;
-  const double hxx = ((hpm - 2 * hcm + hmm) * fl + (hpc - 2 * hcc + hmc) +
-                      (hpp - 2 * hcp + hmp) * fl) /
-                     ((1 + 2 * fl) * lx * lx);
-  const double hyy = ((hmp - 2 * hmc + hmm) * fl + (hcp - 2 * hcc + hcm) +
-                      (hpp - 2 * hpc + hpm) * fl) /
-                     ((1 + 2 * fl) * ly * ly);
-  const double hxy = ((hpp - hmp) - (hpm - hmm)) / (4 * lx * ly);
-  double kk = (2 * hxd * hyd * hxy - (sqr(hyd) + 1) * hxx - (sqr(hxd) + 1) * hyy) /
-              pow(sqr(hxd) + sqr(hyd) + 1, 3. / 2.);
-  if (n[dn] < 0) kk *= -1;
-  kappa[c] = kk;
+    if (a2 > amax) dn = 2;
+    const int dx = dn == 2 ? 0 : dn + 1, dy = dn == 0 ? 2 : dn - 1;
+    const double lx = dx == 0 ? hx : dx == 1 ? hy : hz;
+    const double ly = dy == 0 ? hx : dy == 1 ? hy : hz;
+    const double hcc = ColumnHeight(d, i, j, k, dn, 0, 0, u, hgt);
+    const double hmc = ColumnHeight(d, i, j, k, dn, -1, 0, u, hgt);
+    const double hpc = ColumnHeight(d, i, j, k, dn, 1, 0, u, hgt);
+    const double hcm = ColumnHeight(d, i, j, k, dn, 0, -1, u, hgt);
+    const double hcp = ColumnHeight(d, i, j, k, dn, 0, 1, u, hgt);
+    const double hmm = ColumnHeight(d, i, j, k, dn, -1, -1, u, hgt);
+    const double hmp = ColumnHeight(d, i, j, k, dn, -1, 1, u, hgt);
+    const double hpm = ColumnHeight(d, i, j, k, dn, 1, -1, u, hgt);
+    const double hpp = ColumnHeight(d, i, j, k, dn, 1, 1, u, hgt);
+    const double hxd = (hpc - hmc) / (2 * lx);
+    const double hyd = (hcp - hcm) / (2 * ly);
+    const double fl = 0.2;
+    const double hxx = ((hpm - 2 * hcm + hmm) * fl + (hpc - 2 * hcc + hmc) +
+                        (hpp - 2 * hcp + hmp) * fl) /
+                       ((1 + 2 * fl) * lx * lx);
+    const double hyy = ((hmp - 2 * hmc + hmm) * fl + (hcp - 2 * hcc + hcm) +
+                        (hpp - 2 * hpc + hpm) * fl) /
+                       ((1 + 2 * fl) * ly * ly);
+    const double hxy = ((hpp - hmp) - (hpm - hmm)) / (4 * lx * ly);
+    double kk = (2 * hxd * hyd * hxy - (sqr(hyd) + 1) * hxx - (sqr(hxd) + 1) * hyy) /
+                pow(sqr(hxd) + sqr(hyd) + 1, 3. / 2.);
+    const double ndn = dn == 0 ? n0 : dn == 1 ? n1 : n2;
+    if (ndn < 0) kk *= -1;
+    kappa[c] = kk;
   }
+}
+
+__global__ void KFillNan(int64_t n, double* v) {
+  const double nanv = __longlong_as_double(0x7FF8000000000000LL);
+  for (int64_t c = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; c < n;
+       c += (int64_t)gridDim.x * blockDim.x)
+    v[c] = nanv;
 }
 
 // AppendSurfaceTension (util/hydro.ipp:1289-1310) into zeroed face blocks
@@ -766,12 +835,14 @@ int SweepUpdate(aphgpu_ctx* ctx, const VofScratch& sc, int dir, const double* vf
 int VofReconstruct(aphgpu_ctx* ctx) {
   const VofScratch sc = Scratch(ctx);
   APH_TRY(ListInterface(ctx, sc, false));
+  ctx->vof_list_valid = true;
   return ReconstructListed(ctx, sc);
 }
 
 int VofStepDevice(aphgpu_ctx* ctx, const double* d_vflux, double dt) {
   const int64_t N = ctx->N;
   const VofScratch sc = Scratch(ctx);
+  ctx->vof_list_valid = false;
   if (ctx->has_vof_src) {
     APH_CUDA(ctx, cudaMemsetAsync(sc.count, 0, sizeof(int), ctx->stream));
     KSourceList<<<TileGrid(ctx->d), TileBlock(), 0, ctx->stream>>>(
@@ -794,29 +865,52 @@ int VofStepDevice(aphgpu_ctx* ctx, const double* d_vflux, double dt) {
   }
   ctx->vof_count += 1;
   ctx->vof_dt = dt;
+  // the last update listed the interfacial cells of the new u
+  ctx->vof_list_valid = true;
   return APHGPU_OK;
 }
 
-int CurvatureDevice(aphgpu_ctx* ctx) {
+namespace {
+int HeightsListed(aphgpu_ctx* ctx, const VofScratch& sc) {
   const double h = ctx->h;
-  KHeights<<<TileGrid(ctx->d), TileBlock(), 0, ctx->stream>>>(ctx->d, h, h, h,
-                                                               ctx->u, ctx->hgt);
-  APH_LAUNCHED(ctx);
-  KCurvature<<<TileGrid(ctx->d), TileBlock(), 0, ctx->stream>>>(
-      ctx->d, h, h, h, ctx->u, ctx->nrm, ctx->hgt, ctx->kappa);
+  KHeightsList<<<ListGrid(ctx), 256, 0, ctx->stream>>>(ctx->d, h, h, h, ctx->u, ctx->hgt,
+                                                        sc.list, sc.count);
   APH_LAUNCHED(ctx);
   return APHGPU_OK;
+}
+int CurvatureListed(aphgpu_ctx* ctx, const VofScratch& sc) {
+  const double h = ctx->h;
+  KFillNan<<<FlatBlocks(ctx->N), kFlatThreads, 0, ctx->stream>>>(ctx->N, ctx->kappa);
+  APH_LAUNCHED(ctx);
+  KCurvatureList<<<ListGrid(ctx), 256, 0, ctx->stream>>>(
+      ctx->d, h, h, h, ctx->u, ctx->nrm, ctx->hgt, ctx->kappa, sc.list, sc.count);
+  APH_LAUNCHED(ctx);
+  return APHGPU_OK;
+}
+}  // namespace
+
+// Heights and curvature of the interfacial cells, from the interface list
+// of the current volume fraction (rebuilt when the last VOF call did not
+// leave it).
+int CurvatureDevice(aphgpu_ctx* ctx) {
+  const VofScratch sc = Scratch(ctx);
+  if (!ctx->vof_list_valid) {
+    APH_TRY(ListInterface(ctx, sc, false));
+    ctx->vof_list_valid = true;
+  }
+  APH_TRY(HeightsListed(ctx, sc));
+  return CurvatureListed(ctx, sc);
 }
 
 int TimeVofKernel(aphgpu_ctx* ctx, int kernel, int reps, double* ms, double* bytes,
                   const double* d_vflux, double dt) {
-  const double h = ctx->h;
-  const Dims d = ctx->d;
   const double N = (double)ctx->N;
   cudaStream_t st = ctx->stream;
   const VofScratch sc = Scratch(ctx);
-  // the interface list and fcuu of the current volume fraction
+  // the interface list and fcuu of the current volume fraction (the
+  // timed update leaves the list of its scratch output)
   APH_TRY(ListInterface(ctx, sc, true));
+  ctx->vof_list_valid = kernel != APHGPU_K_VOF_UPDATE;
   int nif = 0;
   APH_CUDA(ctx, cudaMemcpyAsync(&nif, sc.count, sizeof(int), cudaMemcpyDeviceToHost, st));
   APH_CUDA(ctx, cudaStreamSynchronize(st));
@@ -828,8 +922,11 @@ int TimeVofKernel(aphgpu_ctx* ctx, int kernel, int reps, double* ms, double* byt
     case APHGPU_K_VOF_UPDATE: b = N * (8 + 8 + 8 + 1) + nif * 4.0; break;
     // listed cells: index, u, normal and plane constant written
     case APHGPU_K_RECONSTRUCT: b = nif * (4.0 + 8 + 24 + 8); break;
-    case APHGPU_K_HEIGHTS: b = N * 8; break;
-    case APHGPU_K_CURVATURE: b = N * (8 + 8); break;  // u, kappa
+    // listed cells: index, 39 u values (mostly cached), 3 heights written
+    case APHGPU_K_HEIGHTS: b = nif * (4.0 + 8 + 24); break;
+    // NaN fill of kappa; listed cells: index, normal, u and heights of the
+    // columns, kappa
+    case APHGPU_K_CURVATURE: b = N * 8 + nif * (4.0 + 24 + 8 + 9 * 8 + 8); break;
     default: return SetError(ctx, APHGPU_ERR_ARG, "unknown kernel %d", kernel);
   }
   // flux and update of the x direction with the last step's time step (the
@@ -840,13 +937,8 @@ int TimeVofKernel(aphgpu_ctx* ctx, int kernel, int reps, double* ms, double* byt
       case APHGPU_K_VOF_FLUX: return SweepFluxList(ctx, sc, 0, d_vflux, dt);
       case APHGPU_K_VOF_UPDATE: return SweepUpdate(ctx, sc, 0, d_vflux, dt, false);
       case APHGPU_K_RECONSTRUCT: return ReconstructListed(ctx, sc);
-      case APHGPU_K_HEIGHTS:
-        KHeights<<<TileGrid(d), TileBlock(), 0, st>>>(d, h, h, h, ctx->u, ctx->hgt);
-        break;
-      case APHGPU_K_CURVATURE:
-        KCurvature<<<TileGrid(d), TileBlock(), 0, st>>>(d, h, h, h, ctx->u, ctx->nrm,
-                                                        ctx->hgt, ctx->kappa);
-        break;
+      case APHGPU_K_HEIGHTS: return HeightsListed(ctx, sc);
+      case APHGPU_K_CURVATURE: return CurvatureListed(ctx, sc);
     }
     APH_LAUNCHED(ctx);
     return APHGPU_OK;
