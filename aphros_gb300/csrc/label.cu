@@ -34,6 +34,8 @@ namespace {
 constexpr int kLabelThreads = 256;
 constexpr int kMaxComponents = 1 << 21;
 constexpr unsigned long long kNoFirst = ~0ull;
+constexpr int kPropBatch = 8;  // cells of a line loaded ahead by the propagation
+constexpr long long kNoColorBits = 0xBFF0000000000000LL;  // -1.0, no colour
 
 __device__ __forceinline__ int Wrap(int i, int n) { return i < 0 ? i + n : (i >= n ? i - n : i); }
 
@@ -211,26 +213,52 @@ __global__ void KLabelPropagate(Dims d, int dir, const double* __restrict__ u, d
     }
     const int64_t last = base + (int64_t)(m - 1) * stride;
     double cl0 = pre[last], u0 = u[last];  // halo copy before cell 0
-    for (int w = 0; w <= m; ++w) {
-      const int64_t c1 = base + (int64_t)w * stride;
-      double cl1, u1;
-      if (w < m) {
-        cl1 = cl[c1];
-        u1 = u[c1];
-      } else {
-        cl1 = pre[base];  // halo copy after the last cell
-        u1 = u[base];
+    // the cells are loaded kPropBatch at a time ahead of the faces that
+    // read them (a cell changes only at its own faces, replayed by this
+    // thread after the load, and the running values carry the changes)
+    for (int w0 = 0; w0 <= m; w0 += kPropBatch) {
+      double clb[kPropBatch], ub[kPropBatch];
+#pragma unroll
+      for (int q = 0; q < kPropBatch; ++q) {
+        const int w = w0 + q;
+        clb[q] = -1.0;
+        ub[q] = 0.0;
+        if (w < m) {
+          const int64_t c1 = base + (int64_t)w * stride;
+          clb[q] = cl[c1];
+          ub[q] = u[c1];
+        } else if (w == m) {
+          clb[q] = pre[base];  // halo copy after the last cell
+          ub[q] = u[base];
+        }
       }
-      if (cl0 == -1.0 && u0 > 0 && u1 > u0 && cl1 != -1.0) {
+#pragma unroll
+      for (int q = 0; q < kPropBatch; ++q) {
+        const int w = w0 + q;
+        if (w > m) break;
+        const int64_t c1 = base + (int64_t)w * stride;
+        double cl1 = clb[q];
+        const double u1 = ub[q];
+        // the comparisons on the bit patterns (integer instructions; FP64
+        // issues at 2 per clock per SM here): in each rule one operand of
+        // u0 > u1 / u1 > u0 is positive, and for a positive double and any
+        // other non-NaN double the signed 64-bit order of the bits is the
+        // numeric order; -1 (no colour) has one bit pattern
+        const long long b0 = __double_as_longlong(u0), b1 = __double_as_longlong(u1);
+        bool none0 = __double_as_longlong(cl0) == kNoColorBits;
+        const bool none1 = __double_as_longlong(cl1) == kNoColorBits;
+        if (none0 && b0 > 0 && b1 > b0 && !none1) {
+          cl0 = cl1;
+          none0 = false;
+          if (w > 0) cl[c1 - stride] = cl0;
+        }
+        if (none1 && b1 > 0 && b0 > b1 && !none0) {
+          cl1 = cl0;
+          if (w < m) cl[c1] = cl1;
+        }
         cl0 = cl1;
-        if (w > 0) cl[c1 - stride] = cl0;
+        u0 = u1;
       }
-      if (cl1 == -1.0 && u1 > 0 && u0 > u1 && cl0 != -1.0) {
-        cl1 = cl0;
-        if (w < m) cl[c1] = cl1;
-      }
-      cl0 = cl1;
-      u0 = u1;
     }
   }
 }

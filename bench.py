@@ -314,13 +314,27 @@ def cpu_baseline(case, case_name, threads, budget_s=15.0, expr8_np=None):
     return out
 
 
-# algorithmic bytes per cell (compulsory traffic, each array element read or
-# written once): one PLIC step = three directional sweeps, each with its
-# re-reconstruction (volume fraction r/w 16, normals 24, plane constant 8,
-# face flux 8, fluid flux 8, reconstruction 41), and the height curvature
-# (second and fourth differences 80, heights 80, curvature with its inputs 40)
+# algorithmic bytes per cell of the dense formulation (each array element
+# read or written once): one PLIC step = three directional sweeps, each
+# with its re-reconstruction (volume fraction r/w 16, normals 24, plane
+# constant 8, face flux 8, fluid flux 8, reconstruction 41), and the height
+# curvature (second and fourth differences 80, heights 80, curvature with
+# its inputs 40)
 VOF_STEP_BYTES = 315
 CURVATURE_BYTES = 200
+# the device path touches normals, plane constants, fluid fluxes and
+# heights of interfacial cells only: its compulsory traffic per step is the
+# interface listing (u read, fcuu written: 9 B/cell), three fused
+# directional passes (u read and written, face flux, fcuu: 25 B/cell each)
+# and, per interfacial cell, about 112 B per direction (flux through its
+# faces: normal, plane constant, u, two face fluxes and fluid fluxes;
+# re-reconstruction: u, normal and plane constant written); the curvature
+# writes kappa for every cell (8 B/cell) and reads/writes about 88 B per
+# interfacial cell (u, normal, three heights written and read, kappa)
+VOF_DEVICE_BYTES_CELL = 9 + 3 * 25
+VOF_DEVICE_BYTES_IF = 3 * 112
+CURV_DEVICE_BYTES_CELL = 8
+CURV_DEVICE_BYTES_IF = 88
 
 
 def measure_vof(ctx, case, peak, peak_kind, steps, cpu=True):
@@ -354,16 +368,33 @@ def measure_vof(ctx, case, peak, peak_kind, steps, cpu=True):
                                           "GB/s": round(b_k / (ms_k * 1e-3) / 1e9, 1)}
     adv_ms, curv_ms = float(np.median(adv)), float(np.median(curv))
     ach_a = VOF_STEP_BYTES * N / (adv_ms * 1e-3) / 1e9
-    ach_k = CURVATURE_BYTES * N / (curv_ms * 1e-3) / 1e9
+    # interfacial cells of the last step (u alone read back)
+    u = np.empty(N)
+    ctx._check(ctx._L.aphgpu_vof_get(ctx._p, _lib.ptr(u), None, None, None))
+    nif = int(np.count_nonzero((u > 0) & (u < 1)))
+    del u
+    dev_a = VOF_DEVICE_BYTES_CELL * N + VOF_DEVICE_BYTES_IF * nif
+    dev_k = CURV_DEVICE_BYTES_CELL * N + CURV_DEVICE_BYTES_IF * nif
+    ach_da = dev_a / (adv_ms * 1e-3) / 1e9
+    ach_dk = dev_k / (curv_ms * 1e-3) / 1e9
     out = {"dt_cfl": 0.5, "steps": steps,
            "advection_ms_per_step": adv_ms, "curvature_ms": curv_ms,
            "recolor_ms": float(np.median(recol)),
            "cell_steps_per_s": N / ((adv_ms + curv_ms) * 1e-3),
+           "interfacial_cells": nif,
            "roofline": {"bound": "hbm", "unit": "GB/s", "peak": peak, "peak_kind": peak_kind,
                         "advection": {"bytes_per_cell": VOF_STEP_BYTES, "achieved": ach_a,
-                                      "frac": ach_a / peak},
-                        "curvature": {"bytes_per_cell": CURVATURE_BYTES, "achieved": ach_k,
-                                      "frac": ach_k / peak}},
+                                      "frac": ach_a / peak,
+                                      "device_bytes_per_cell": dev_a / N,
+                                      "device_achieved": ach_da,
+                                      "device_frac": ach_da / peak},
+                        "curvature": {"bytes_per_cell": dev_k / N, "achieved": ach_dk,
+                                      "frac": ach_dk / peak,
+                                      "dense_bytes_per_cell": CURVATURE_BYTES,
+                                      "note": "bytes of the interface-list algorithm: kappa "
+                                              "of every cell, heights and inputs of "
+                                              "interfacial cells; the dense formulation's "
+                                              "200 B/cell are not moved"}},
            "kernels": kernels}
     if cpu:
         import oracle
