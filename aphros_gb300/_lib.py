@@ -62,6 +62,16 @@ class Info(ctypes.Structure):
                 ("converged", _I)]
 
 
+class PartConf(ctypes.Structure):
+    """aphgpu_part_conf: parameters of the particle-string curvature."""
+    _fields_ = [("np", ctypes.c_int), ("ns", ctypes.c_int), ("leq", ctypes.c_double),
+                ("relax", ctypes.c_double), ("tol", ctypes.c_double),
+                ("itermax", ctypes.c_int), ("segcirc", ctypes.c_double), ("dn", ctypes.c_int)]
+
+
+CURV_HEIGHTS, CURV_PARTICLES, CURV_HYBRID = 0, 1, 2
+
+
 class AphgpuError(RuntimeError):
     def __init__(self, code, msg):
         super().__init__("aphgpu error %d: %s" % (code, msg))
@@ -118,6 +128,10 @@ def lib():
     L.aphgpu_apply_cell_cond.argtypes = [_P, ctypes.c_int64, _P, _P]
     L.aphgpu_apply_cell_cond.restype = _I
     L.aphgpu_curvature.argtypes = [_P, _P, _P]
+    L.aphgpu_part_conf_default.argtypes = [ctypes.POINTER(PartConf)]
+    L.aphgpu_part_conf_default.restype = None
+    L.aphgpu_curvature_estimator.argtypes = [_P, _I, ctypes.POINTER(PartConf), _P]
+    L.aphgpu_curvature_estimator.restype = _I
     L.aphgpu_surface_tension.argtypes = [_P, _D, _P]
     L.aphgpu_set_force_resident.argtypes = [_P, _I]
     L.aphgpu_last_timing.argtypes = [_P, _PD, ctypes.POINTER(ctypes.c_int64)]
@@ -163,6 +177,13 @@ def lib():
         getattr(L, name).restype = _I
     _lib = L
     return L
+
+
+def part_conf_default():
+    """The reference's part_* defaults (aphgpu_part_conf_default)."""
+    c = PartConf()
+    lib().aphgpu_part_conf_default(ctypes.byref(c))
+    return c
 
 
 def ptr(a):
@@ -355,6 +376,15 @@ class Context:
         m = np.empty(self.N, dtype=np.uint8)
         self._check(self._L.aphgpu_vof_get(self._p, ptr(u), ptr(nrm), ptr(a), ptr(m)))
         return u, nrm, a, m
+
+    def curvature_estimator(self, estimator, conf=None, out=True):
+        """Curvature by the estimator (CURV_HEIGHTS, CURV_PARTICLES,
+        CURV_HYBRID) with the particle parameters conf (None: defaults);
+        out=False leaves it on the device (returns None)."""
+        k = np.empty(self.N) if out else None
+        pc = None if conf is None else ctypes.byref(conf)
+        self._check(self._L.aphgpu_curvature_estimator(self._p, estimator, pc, ptr(k)))
+        return k
 
     def curvature(self, heights=False, out=True):
         """Height-function curvature of the resident volume fraction; out=False

@@ -42,6 +42,7 @@ CU_UNITS = {
     "dump.cu": [],
     "label.cu": [],
     "fluid.cu": ["-fmad=false"],
+    "partstr.cu": ["-fmad=false"],
 }
 
 
@@ -96,11 +97,11 @@ def build_gen():
 def build_oracle():
     out = os.path.join(ORACLE, "_build")
     os.makedirs(out, exist_ok=True)
-    src = os.path.join(ORACLE, "aphros_oracle.c")
+    srcs = [os.path.join(ORACLE, "aphros_oracle.c"), os.path.join(ORACLE, "partstr_oracle.c")]
     lib = os.path.join(out, "liboracle.so")
-    if _newer(lib, [src, os.path.join(ORACLE, "aphros_oracle.h")]):
+    if _newer(lib, srcs + [os.path.join(ORACLE, "aphros_oracle.h")]):
         _run(["gcc", "-O2", "-fPIC", "-shared", "-fopenmp", "-ffp-contract=off",
-              "-o", lib, src, "-lm"])
+              "-o", lib] + srcs + ["-lm"])
     return lib
 
 

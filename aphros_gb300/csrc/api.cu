@@ -795,6 +795,39 @@ int aphgpu_curvature(aphgpu_ctx* ctx, double* kappa, double* heights) {
   return APHGPU_OK;
 }
 
+void aphgpu_part_conf_default(aphgpu_part_conf* conf) {
+  if (!conf) return;
+  conf->np = 7;
+  conf->ns = 3;
+  conf->leq = 4;
+  conf->relax = 0.5;
+  conf->tol = 1e-5;
+  conf->itermax = 20;
+  conf->segcirc = 0;
+  conf->dn = 0;
+}
+
+int aphgpu_curvature_estimator(aphgpu_ctx* ctx, int estimator, const aphgpu_part_conf* conf,
+                               double* kappa) {
+  if (!Valid(ctx)) return APHGPU_ERR_ARG;
+  if (!ctx->vof_ready) return SetError(ctx, APHGPU_ERR_STATE, "vof not initialised");
+  if (estimator < APHGPU_CURV_HEIGHTS || estimator > APHGPU_CURV_HYBRID)
+    return SetError(ctx, APHGPU_ERR_ARG, "unknown curvature estimator %d", estimator);
+  APH_TRY(SetDevice(ctx));
+  aphgpu_part_conf pc;
+  aphgpu_part_conf_default(&pc);
+  if (conf) pc = *conf;
+  Timer t(ctx);
+  if (estimator == APHGPU_CURV_HEIGHTS) {
+    APH_TRY(CurvatureDevice(ctx));
+  } else {
+    APH_TRY(CurvatureParticlesDevice(ctx, pc, estimator == APHGPU_CURV_HYBRID));
+  }
+  t.Stop();
+  if (kappa) APH_TRY(D2H(ctx, kappa, ctx->kappa, sizeof(double) * ctx->N));
+  return APHGPU_OK;
+}
+
 int aphgpu_surface_tension(aphgpu_ctx* ctx, double sigma, double* febp) {
   if (!Valid(ctx)) return APHGPU_ERR_ARG;
   if (!ctx->vof_ready) return SetError(ctx, APHGPU_ERR_STATE, "vof not initialised");

@@ -310,6 +310,8 @@ struct aphgpu_ctx {
                                // exchanged with u
   bool vof_list_valid = false; // the scratch list holds the interfacial
                                // cells of u
+  double* kpart = nullptr;     // curvature of each particle string
+  int64_t kpart_cap = 0;
   double* u0 = nullptr;
   double* nrm = nullptr;       // 3N AoS
   double* pa = nullptr;        // plane constant
@@ -478,6 +480,13 @@ int ColorInit(aphgpu_ctx* ctx);
 int Recolor(aphgpu_ctx* ctx);
 int VofStepDevice(aphgpu_ctx* ctx, const double* d_vflux, double dt);
 int CurvatureDevice(aphgpu_ctx* ctx);
+// the interface list (cells with 0 < u < 1) of the current u, rebuilt if
+// the last VOF call did not leave it: device pointers to the cell indices
+// and their count
+int InterfaceListDevice(aphgpu_ctx* ctx, const int** list, const int** count);
+int KFillNanDevice(aphgpu_ctx* ctx, double* v, int64_t n);
+// partstr.cu
+int CurvatureParticlesDevice(aphgpu_ctx* ctx, const aphgpu_part_conf& conf, bool hybrid);
 int SurfaceTensionDevice(aphgpu_ctx* ctx, double sigma, double* d_febp);
 int TimeVofKernel(aphgpu_ctx* ctx, int kernel, int reps, double* ms, double* bytes,
                   const double* d_vflux, double dt);

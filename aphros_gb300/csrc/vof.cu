@@ -889,6 +889,23 @@ int CurvatureListed(aphgpu_ctx* ctx, const VofScratch& sc) {
 }
 }  // namespace
 
+int InterfaceListDevice(aphgpu_ctx* ctx, const int** list, const int** count) {
+  const VofScratch sc = Scratch(ctx);
+  if (!ctx->vof_list_valid) {
+    APH_TRY(ListInterface(ctx, sc, false));
+    ctx->vof_list_valid = true;
+  }
+  *list = sc.list;
+  *count = sc.count;
+  return APHGPU_OK;
+}
+
+int KFillNanDevice(aphgpu_ctx* ctx, double* v, int64_t n) {
+  KFillNan<<<FlatBlocks(n), kFlatThreads, 0, ctx->stream>>>(n, v);
+  APH_LAUNCHED(ctx);
+  return APHGPU_OK;
+}
+
 // Heights and curvature of the interfacial cells, from the interface list
 // of the current volume fraction (rebuilt when the last VOF call did not
 // leave it).

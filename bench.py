@@ -366,6 +366,15 @@ def measure_vof(ctx, case, peak, peak_kind, steps, cpu=True):
         ms_k, b_k = ctx.time_kernel(kid, reps=5)
         kernels[_lib.KERNEL_NAMES[kid]] = {"ms": round(ms_k, 4),
                                           "GB/s": round(b_k / (ms_k * 1e-3) / 1e9, 1)}
+    # the particle-string and hybrid estimators on the last state (the
+    # reference's default estimator is particles)
+    part, hyb = [], []
+    for _ in range(3):
+        ctx.curvature_estimator(_lib.CURV_PARTICLES, out=False)
+        part.append(ctx.last_timing()[0])
+        ctx.curvature_estimator(_lib.CURV_HYBRID, out=False)
+        hyb.append(ctx.last_timing()[0])
+    ctx.curvature(out=False)
     adv_ms, curv_ms = float(np.median(adv)), float(np.median(curv))
     ach_a = VOF_STEP_BYTES * N / (adv_ms * 1e-3) / 1e9
     # interfacial cells of the last step (u alone read back)
@@ -382,6 +391,8 @@ def measure_vof(ctx, case, peak, peak_kind, steps, cpu=True):
            "recolor_ms": float(np.median(recol)),
            "cell_steps_per_s": N / ((adv_ms + curv_ms) * 1e-3),
            "interfacial_cells": nif,
+           "curvature_particles_ms": float(np.median(part)),
+           "curvature_hybrid_ms": float(np.median(hyb)),
            "roofline": {"bound": "hbm", "unit": "GB/s", "peak": peak, "peak_kind": peak_kind,
                         "advection": {"bytes_per_cell": VOF_STEP_BYTES, "achieved": ach_a,
                                       "frac": ach_a / peak,
@@ -413,6 +424,19 @@ def measure_vof(ctx, case, peak, peak_kind, steps, cpu=True):
             st.step(f, dts, nthreads=threads)
             st.curvature()
         per = (time.perf_counter() - t0) / reps
+        # the particle estimator of the reference, restated (the oracle),
+        # on the same sample state with all host threads
+        t0 = time.perf_counter()
+        kp = oracle.curv_particles(ns, cs.h, st.u, st.nrm, st.a, nthreads=threads)
+        part_s = time.perf_counter() - t0
+        nifs = int(np.count_nonzero(~np.isnan(kp)))
+        out["cpu_particles"] = {"interfacial_cells_per_s": nifs / part_s, "cores": threads,
+                                "kind": "port",
+                                "sample": "curvature::Particles (part_* defaults) restated "
+                                          "in C, %d interfacial cells of the %d^3 sample "
+                                          "state, %.3f s" % (nifs, ns, part_s)}
+        out["gpu_particles_interfacial_cells_per_s"] = nif / (out["curvature_particles_ms"]
+                                                              * 1e-3)
         out["cpu_baseline"] = {"value": ns ** 3 / per, "unit": "cell-steps/s", "cores": threads,
                                "kind": "port",
                                "sample": "%d steps of the C restatement of aphros Vof "
@@ -1053,6 +1077,10 @@ def run_profile(args):
             ctx.vof_step(None, dt)
             ctx.curvature(out=False)
             ctx.vof_recolor()
+        if args.estimator != "heights":
+            # one call of the particle-string (or hybrid) estimator at the end
+            est = _lib.CURV_PARTICLES if args.estimator == "particles" else _lib.CURV_HYBRID
+            ctx.curvature_estimator(est, out=False)
         print("profile vof: %d steps of %d^3" % (args.warmup + args.steps, case.n))
         return
     for _ in range(args.warmup + args.steps):
@@ -1083,6 +1111,9 @@ def main():
                          "after `warmup` solves, no other work and no output line")
     ap.add_argument("--sweeps", type=int, choices=[0, 1, 2, 3, 4], default=None,
                     help="--profile: red-black sweep variant (APHGPU_OPT_FUSED_SWEEPS)")
+    ap.add_argument("--estimator", choices=["heights", "particles", "hybrid"],
+                    default="heights",
+                    help="--profile vof: one call of this curvature estimator after the steps")
     ap.add_argument("--serve", action="store_true",
                     help="served-stream benchmark instead of the solve benchmark")
     ap.add_argument("--sims", type=int, default=2000)

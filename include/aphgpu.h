@@ -225,6 +225,43 @@ int aphgpu_vof_get(aphgpu_ctx* ctx, double* alpha, double* normals,
  * (results stay resident for aphgpu_surface_tension). */
 int aphgpu_curvature(aphgpu_ctx* ctx, double* kappa, double* heights);
 
+/* Parameters of the particle-string curvature: PartStr::Par and
+ * PartStrMeshM::Par (src/solver/partstr.h:38-45, partstrmeshm.h:26-36),
+ * the part_* variables of the reference's configuration. */
+typedef struct {
+  int np;          /* particles per string, odd, 3..15 (part_np) */
+  int ns;          /* strings (section planes) per cell (part_ns) */
+  double leq;      /* string length in cells (part_h) */
+  double relax;    /* relaxation factor (part_relax) */
+  double tol;      /* tolerance on the correction (part_tol) */
+  int itermax;     /* iterations at most (part_itermax) */
+  double segcirc;  /* shift to a circular segment (part_segcirc) */
+  int dn;          /* 1: normal displacement of the whole string (part_dn) */
+} aphgpu_part_conf;
+
+/* The defaults of deploy/scripts/sim_base.conf: np 7, ns 3, leq 4, relax
+ * 0.5, tol 1e-5, itermax 20, segcirc 0, dn 0. */
+void aphgpu_part_conf_default(aphgpu_part_conf* conf);
+
+enum {
+  APHGPU_CURV_HEIGHTS = 0,   /* curvature::Heights (aphgpu_curvature) */
+  APHGPU_CURV_PARTICLES = 1, /* curvature::Particles */
+  APHGPU_CURV_HYBRID = 2     /* curvature::Hybrid: heights, particles where
+                                the heights give none */
+};
+
+/* Curvature of the current VOF state by the estimator that
+ * curvature::MakeEstimator (src/solver/curv.ipp:604-622) selects by name:
+ * Particles (curv.ipp:29-54 with partstrmeshm.ipp:266-395 and
+ * partstr.h:57-646) seeds ns strings in every interfacial cell, one layer,
+ * no colours (the single-field Vof gives the estimator none, vof.ipp:746-
+ * 749), periodic, no contact angles.  conf: NULL for the defaults.  kappa:
+ * host output (NaN where no estimate), or NULL to keep it resident (for
+ * aphgpu_surface_tension).  Equal to the reference up to the last bits of
+ * the device's cos and sin. */
+int aphgpu_curvature_estimator(aphgpu_ctx* ctx, int estimator, const aphgpu_part_conf* conf,
+                               double* kappa);
+
 /* Surface-tension face force sigma*kappa*grad(alpha) of
  * AppendSurfaceTension (src/util/hydro.ipp:1289-1310) from the resident
  * volume fraction and curvature.  febp: 3 face blocks (host) or NULL to keep

@@ -227,6 +227,12 @@ class VofState:
                            self.mask.ctypes.data_as(_P), _p(self.nrm), _p(self.a))
         self.count += 1
 
+    def reconstruct(self):
+        """Vof::ReconstPlanes of the current field (mask, normals, plane
+        constants), as the state after StartStep at t=0."""
+        lib().orc_vof_reconstruct(self.n3c, self.hh, _p(self.u), self.mask.ctypes.data_as(_P),
+                                  _p(self.nrm), _p(self.a))
+
     def recolor(self):
         """Connected-component colours of the current field (the resetcolor,
         union-find recolor and propagate stages of Vof::MakeIteration)."""
@@ -241,6 +247,41 @@ class VofState:
         hg = np.empty(3 * self.N)
         o.orc_heights_curvature(self.n3c, self.hh, _p(self.u), _p(self.nrm), _p(k), _p(hg))
         return (k, hg) if heights else k
+
+
+class PartPar(ctypes.Structure):
+    """Parameters of the particle-string curvature (OrcPartPar)."""
+    _fields_ = [("np", ctypes.c_int), ("ns", ctypes.c_int), ("leq", ctypes.c_double),
+                ("relax", ctypes.c_double), ("tol", ctypes.c_double),
+                ("itermax", ctypes.c_int), ("segcirc", ctypes.c_double), ("dn", ctypes.c_int)]
+
+
+def part_default():
+    """The part_* defaults of the reference's sim_base.conf."""
+    p = PartPar()
+    lib().orc_part_default(ctypes.byref(p))
+    return p
+
+
+def curv_particles(n, h, u, nrm, a, cl=None, par=None, nthreads=0):
+    """curvature::Particles of the PLIC state (u, normals AoS, plane
+    constants) with colours cl (None: no colours); NaN where no string is
+    seeded (orc_curv_particles)."""
+    n3c, n3 = _n3(n)
+    N = n3[0] * n3[1] * n3[2]
+    u = np.ascontiguousarray(u, dtype=np.float64)
+    nrm = np.ascontiguousarray(nrm, dtype=np.float64)
+    a = np.ascontiguousarray(a, dtype=np.float64)
+    cl = None if cl is None else np.ascontiguousarray(cl, dtype=np.float64)
+    par = part_default() if par is None else par
+    out = np.empty(N)
+    o = lib()
+    o.orc_curv_particles.restype = ctypes.c_int
+    rc = o.orc_curv_particles(n3c, _D(h), _p(u), _p(nrm), _p(a), _p(cl), ctypes.byref(par),
+                              _p(out), ctypes.c_int(nthreads))
+    if rc != 0:
+        raise ValueError("particle parameters out of range")
+    return out
 
 
 def recolor(n, u, cl_prev):

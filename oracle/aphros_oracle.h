@@ -178,6 +178,32 @@ void orc_heights_curvature(
     const int n[3], const double h[3], const double* u, const double* nrm,
     double* kappa, double* hgt);
 
+/* Parameters of the particle-string curvature (PartStr::Par and
+ * PartStrMeshM::Par, src/solver/partstr.h:38-45, partstrmeshm.h:26-36):
+ * particles per string (odd), strings per cell, string length in cells,
+ * relaxation, tolerance, iterations at most, circular-segment factor,
+ * normal displacement. */
+typedef struct {
+  int np, ns;
+  double leq, relax, tol;
+  int itermax;
+  double segcirc;
+  int dn;
+} OrcPartPar;
+
+/* The defaults of deploy/scripts/sim_base.conf (part_*). */
+void orc_part_default(OrcPartPar* p);
+
+/* curvature::Particles (src/solver/curv.ipp:29-54, partstrmeshm.ipp:266-395)
+ * for one layer of a periodic domain of cubic cells h: strings seeded in the
+ * interfacial cells (0 < u < 1) with a colour (cl NULL: no colours), lines
+ * from the PLIC polygons (nrm AoS, pa) of the interfacial cells of the same
+ * colour in the 5x5x5 stencil.  kappa: NaN where no string is seeded.
+ * Returns 0, or -1 for parameters out of range. */
+int orc_curv_particles(const int n[3], double h, const double* u, const double* nrm,
+                       const double* pa, const double* cl, const OrcPartPar* p,
+                       double* kappa, int nthreads);
+
 /* Connected-component colours after a VOF step on one periodic block
  * (Vof::MakeIteration resetcolor + union-find recolor + propagate,
  * src/solver/vof.ipp:546-578): cl_prev the colours before, cl the result

@@ -29,6 +29,9 @@
 //     of the default union-find recolouring; after the last step) and
 //     out.sumu (text, per step).  With REF_VOF_SRC=path set, the volume
 //     source field of the Vof (raw, N values) is read from that file.
+//     REF_CURV=particles or hybrid replaces the estimator of out.k by
+//     curvature::Particles or curvature::Hybrid (part_* defaults of
+//     deploy/scripts/sim_base.conf).
 //   overlap in out         rows (x y z hx hy hz cx cy cz r) -> GetSphereOverlap
 //   reconst in out         rows (n0 n1 n2 u a h0 h1 h2 q dt d) ->
 //                          GetLineA(n,u,h) GetLineU(n,a,h) GetLineFlux(...)
@@ -413,7 +416,29 @@ void RunVof(M& m, Vars& var) {
     t.layers = GRange<size_t>(1);
     t.fck.resize(t.layers);
     t.fck.InitAll(FieldCell<Scal>(m, GetNan<Scal>()));
-    t.curv = std::make_unique<curvature::Heights<M>>();
+    // REF_CURV=particles or hybrid selects the particle-string estimator
+    // (curv.ipp:604-622) with the part_* defaults of sim_base.conf
+    const char* est = std::getenv("REF_CURV");
+    const std::string name = est ? est : "heights";
+    if (name == "particles" || name == "hybrid") {
+      typename PartStrMeshM<M>::Par pp;
+      pp.ps.leq = 4;
+      pp.ps.relax = 0.5;
+      pp.ps.npmax = 7;
+      pp.ps.segcirc = 0;
+      pp.ps.dn = false;
+      pp.ns = 3;
+      pp.tol = 1e-5;
+      pp.itermax = 20;
+      pp.dim = 3;
+      if (name == "particles") {
+        t.curv = std::make_unique<curvature::Particles<M>>(m, pp, t.layers);
+      } else {
+        t.curv = std::make_unique<curvature::Hybrid<M>>(m, pp, t.layers);
+      }
+    } else {
+      t.curv = std::make_unique<curvature::Heights<M>>();
+    }
   }
   sem.LoopBegin();
   if (sem("empty")) {

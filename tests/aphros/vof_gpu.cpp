@@ -1,7 +1,8 @@
 // aphros's block framework stepping the reference-side VOF and curvature
-// adapters (GpuVof, GpuHeights) the way test/advection/main.cpp steps Vof
+// adapters (GpuVof, GpuCurvature) the way test/advection/main.cpp steps Vof
 // and curvature::Heights (StartStep, MakeIteration, FinishStep, PostStep,
-// CalcCurvature per step), on raw inputs.  Test infrastructure: its output
+// CalcCurvature per step), on raw inputs; APHGPU_CURV=particles or hybrid
+// selects the particle-string estimators.  Test infrastructure: its output
 // is compared with oracle/_ref/ref_harness's `vof` mode (aphros's own Vof
 // and Heights) on the same inputs and block layout.
 //
@@ -66,7 +67,7 @@ void Run(M& m, Vars&) {
     MapEmbed<BCondAdvection<Scal>> bc;  // empty: periodic
     std::unique_ptr<GpuVof<M>> as;
     Multi<FieldCell<Scal>> fck;
-    std::unique_ptr<GpuHeights<M>> curv;
+    std::unique_ptr<GpuCurvature<M>> curv;
     int step = 0;
   } * ctx(sem);
   auto& t = *ctx;
@@ -83,7 +84,14 @@ void Run(M& m, Vars&) {
     t.fcsrc.Reinit(m, 0.);
     t.as.reset(new GpuVof<M>(m, t.fcu, t.bc, &t.ffv, &t.fcsrc, 0., g.dt, 1e-10));
     GpuVof<M>* as = t.as.get();
-    t.curv.reset(new GpuHeights<M>([as]() { return as->GetContext(); }));
+    // APHGPU_CURV=particles or hybrid selects the particle estimators (the
+    // reference run takes REF_CURV with the same name)
+    int est = APHGPU_CURV_HEIGHTS;
+    if (const char* e = std::getenv("APHGPU_CURV")) {
+      if (std::string(e) == "particles") est = APHGPU_CURV_PARTICLES;
+      if (std::string(e) == "hybrid") est = APHGPU_CURV_HYBRID;
+    }
+    t.curv.reset(new GpuCurvature<M>([as]() { return as->GetContext(); }, est));
     t.fck.resize(GRange<size_t>(1));
     t.fck.InitAll(FieldCell<Scal>(m, GetNan<Scal>()));
   }

@@ -43,6 +43,12 @@ Fixtures:
   bcg.npz          UEmbed::InterpolateBcg face values on periodic 12x10x8
                    and 8^3 meshes (random cell field, face fluxes and
                    source).
+  partcurv.npz     curvature::Particles and curvature::Hybrid (part_*
+                   defaults of sim_base.conf) after 3 VOF steps on one 32^3
+                   block (C1 sphere, Taylor-Green flux at CFL 0.5) and after
+                   2 steps on one 48^3 block of 16 bubbles (C2 draw): the
+                   PLIC state (u, normals, plane constants) and both
+                   curvature fields.
   dumps.npz        dump::Xmf::WriteXmf texts of dump::Raw::WriteWithXmf
                    metadata for several meshes and element types, and
                    dump::Raw::WriteBlocks output of a 3x4x5 array converted
@@ -194,6 +200,28 @@ def vofsrc(tmp):
     r = lambda q: np.fromfile(os.path.join(tmp, "vs." + q))
     np.savez_compressed(os.path.join(OUT, "vofsrc.npz"), n=n, h=h, dt=dt, steps=3,
                         src=src, u_ref=r("u"), n_ref=r("n"), a_ref=r("a"), k_ref=r("k"))
+
+
+def partcurv(tmp):
+    out = {}
+    for q, (cname, n, steps) in enumerate((("c1", 32, 3), ("c2", 48, 2))):
+        case = workload.config(cname, n=n)
+        dt = case.cfl_dt(0.5)
+        case.alpha.tofile(os.path.join(tmp, "a.bin"))
+        case.flux.tofile(os.path.join(tmp, "f.bin"))
+        for est in ("particles", "hybrid"):
+            os.environ["REF_CURV"] = est
+            try:
+                run(["vof", str(n), str(n), repr(case.h), repr(dt), str(steps), "a.bin",
+                     "f.bin", "pc"], tmp)
+            finally:
+                del os.environ["REF_CURV"]
+            r = lambda s_: np.fromfile(os.path.join(tmp, "pc." + s_))
+            out["k_%s%d" % (est, q)] = r("k")
+        out.update({"n%d" % q: n, "h%d" % q: case.h, "dt%d" % q: dt, "steps%d" % q: steps,
+                    "case%d" % q: cname, "u%d" % q: r("u"), "nrm%d" % q: r("n"),
+                    "a%d" % q: r("a")})
+    np.savez_compressed(os.path.join(OUT, "partcurv.npz"), **out)
 
 
 def reconst(tmp, rows=300):
@@ -416,7 +444,8 @@ def main():
     makers = [("advection3d", lambda t: advection3d(args.ref, t)), ("proj16", proj16),
               ("proj64", proj64), ("vof32", vof32), ("vofsrc", vofsrc), ("reconst", reconst),
               ("height", lambda t: height(args.ref, t)), ("overlap", overlap),
-              ("dumps", dumps), ("colors", colors), ("bcg", bcg), ("fluid", fluid)]
+              ("dumps", dumps), ("colors", colors), ("bcg", bcg), ("fluid", fluid),
+              ("partcurv", partcurv)]
     only = set(filter(None, args.only.split(",")))
     with tempfile.TemporaryDirectory() as tmp:
         for name, make in makers:

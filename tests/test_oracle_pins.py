@@ -324,3 +324,58 @@ def test_oracle_vof_source_equals_reference():
     assert np.array_equal(st.nrm, fx["n_ref"], equal_nan=True)
     assert np.array_equal(st.a, fx["a_ref"], equal_nan=True)
     assert np.array_equal(st.curvature(), fx["k_ref"], equal_nan=True)
+
+
+def _oracle_heights(n, h, u, nrm):
+    st = oracle.VofState(n, h, u)
+    st.nrm[:] = nrm
+    return st.curvature()
+
+
+@pytest.mark.parametrize("q", [0, 1])
+def test_oracle_particle_curvature_equals_reference(q):
+    """curvature::Particles and curvature::Hybrid with the part_* defaults
+    (partcurv.npz: aphros's own estimators after VOF steps on one block,
+    ref_harness REF_CURV): the oracle equals them bit for bit on the same
+    PLIC state."""
+    fx = np.load(golden("partcurv.npz"))
+    n, h = int(fx["n%d" % q]), float(fx["h%d" % q])
+    u, nrm, a = fx["u%d" % q], fx["nrm%d" % q], fx["a%d" % q]
+    kp = oracle.curv_particles(n, h, u, nrm, a, nthreads=os.cpu_count() or 1)
+    ref = fx["k_particles%d" % q]
+    assert np.array_equal(np.isnan(kp), np.isnan(ref))
+    m = ~np.isnan(ref)
+    assert m.sum() > 500
+    assert np.array_equal(kp[m], ref[m])
+    kh = _oracle_heights(n, h, u, nrm)
+    hyb = np.where(np.isnan(kh), kp, kh)
+    ref = fx["k_hybrid%d" % q]
+    assert np.array_equal(np.isnan(hyb), np.isnan(ref))
+    m = ~np.isnan(ref)
+    assert np.array_equal(hyb[m], ref[m])
+    # the heights leave cells undefined that the particles fill
+    assert (np.isnan(kh) & m).sum() > 10
+
+
+def test_oracle_particle_curvature_sphere_and_parameters():
+    """A sphere of radius 0.25 on 32^3: every interfacial cell gets a
+    curvature, the mean is within 5 % of 2/R; parameters out of range are
+    refused; fewer particles and strings change the estimate."""
+    from aphros_gb300 import workload
+    n = 32
+    case = workload.Case(n, [(0.5, 0.5, 0.5)], [0.25], seed=1)
+    st = oracle.VofState(n, case.h, case.alpha)
+    st.reconstruct()
+    k = oracle.curv_particles(n, case.h, st.u, st.nrm, st.a)
+    ifc = (st.u > 0) & (st.u < 1)
+    assert np.array_equal(~np.isnan(k), ifc)
+    assert abs(np.mean(k[ifc]) - 8.0) < 0.4
+    p = oracle.part_default()
+    p.np = 6
+    with pytest.raises(ValueError):
+        oracle.curv_particles(n, case.h, st.u, st.nrm, st.a, par=p)
+    p = oracle.part_default()
+    p.np, p.ns = 5, 2
+    k2 = oracle.curv_particles(n, case.h, st.u, st.nrm, st.a, par=p)
+    assert np.array_equal(np.isnan(k2), np.isnan(k))
+    assert not np.array_equal(k2[ifc], k[ifc])
