@@ -77,20 +77,36 @@ def test_batch_and_served_shapes():
 
 
 def _replica_worker(rank, world, port, q):
+    import time
+
     import torch.distributed as dist
     os.environ["MASTER_ADDR"] = "127.0.0.1"
     os.environ["MASTER_PORT"] = str(port)
     dist.init_process_group("gloo", rank=rank, world_size=world)
     import bench
+    import oracle
     units, secs = bench.replica_share(rank, world, 10)
     agg = bench.aggregate_over_ranks(units, 1.0 + rank)
-    q.put((rank, units, agg))
+    # each rank solves its own share of independent systems (the replicas'
+    # work, here by the oracle CG on the host): no data crosses ranks, and
+    # the job's value is all ranks' solves over the slowest rank's time
+    t0 = time.perf_counter()
+    solved = 0
+    for u in range(units):
+        case = workload.config("c1", n=12)
+        e, _, _ = oracle.assemble_projection(12, case.h, case.dt, case.alpha, case.rho1,
+                                             case.rho2, case.flux)
+        _, info = oracle.cg_solve(12, case.h, e, oracle.rel_tol(e, case.h, 1e-10))
+        solved += int(info.residual < oracle.rel_tol(e, case.h, 1e-10))
+    work = bench.aggregate_over_ranks(solved, time.perf_counter() - t0)
+    q.put((rank, units, agg, work[0]))
     dist.destroy_process_group()
 
 
 def test_replicas_over_gloo():
-    """N>1 runs independent replicas: each rank gets its share of units and
-    the job value is total units / max time over ranks."""
+    """N>1 runs independent replicas: each rank gets its share of units,
+    solves them without exchanging data, and the job value is total units /
+    max time over ranks."""
     import multiprocessing as mp
     import socket
     s = socket.socket()
@@ -110,6 +126,8 @@ def test_replicas_over_gloo():
     total_units, max_time = res[0][2]
     assert total_units == 10 and max_time == 2.0
     assert res[1][2] == res[0][2]
+    # every unit of every rank was solved, and both ranks see the job total
+    assert res[0][3] == 10 and res[1][3] == 10
 
 
 def test_reference_arm_prints_the_contract_line():
