@@ -525,6 +525,7 @@ int aphgpu_solve_resident(aphgpu_ctx* ctx, const aphgpu_conf* conf, int zero_gue
   }
   ctx->x_zero = false;
   t.Stop();
+  if (rc == APHGPU_OK) rc = CheckWave(ctx);
   return rc;
 }
 
@@ -849,7 +850,7 @@ int aphgpu_set_option(aphgpu_ctx* ctx, int option, int value) {
   switch (option) {
     case APHGPU_OPT_GRAPHS: ctx->use_graphs = value != 0; return APHGPU_OK;
     case APHGPU_OPT_FUSED_SWEEPS:
-      if (value < 0 || value > 4) return SetError(ctx, APHGPU_ERR_ARG, "fused sweeps %d", value);
+      if (value < 0 || value > 6) return SetError(ctx, APHGPU_ERR_ARG, "fused sweeps %d", value);
       if (value != ctx->fused_mode) ctx->mg.built32 = false;  // scratch of the levels
       ctx->fused_mode = value;
       return APHGPU_OK;

@@ -312,6 +312,10 @@ struct aphgpu_ctx {
                                // cells of u
   double* kpart = nullptr;     // curvature of each particle string
   int64_t kpart_cap = 0;
+  // the wavefront sweep: progress counters (one per tile) and, after them,
+  // the flag of a wait that gave up; set when a solve launched it
+  int* wave_buf = nullptr;
+  bool wave_used = false;
   double* u0 = nullptr;
   double* nrm = nullptr;       // 3N AoS
   double* pa = nullptr;        // plane constant
@@ -491,5 +495,7 @@ int SurfaceTensionDevice(aphgpu_ctx* ctx, double sigma, double* d_febp);
 int TimeVofKernel(aphgpu_ctx* ctx, int kernel, int reps, double* ms, double* bytes,
                   const double* d_vflux, double dt);
 int TimeSolverKernel(aphgpu_ctx* ctx, int kernel, int reps, double* ms, double* bytes);
+// the error flag of the wavefront sweeps launched since the last check
+int CheckWave(aphgpu_ctx* ctx);
 
 }  // namespace aphgpu

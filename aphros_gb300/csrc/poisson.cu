@@ -510,6 +510,25 @@ constexpr int64_t kPipeMinCells = int64_t(1) << 21;
 inline bool PipeDims(const Dims& d) {
   return (d.nx % 4) == 0 && d.nx >= 16 && d.ny >= 2 && d.nz >= 8;
 }
+// The wavefront sweep (sweep.cuh): option value 5 on levels of at least
+// kPipeMinCells cells, 6 on every level, where nx % 4 == 0, nz >= 4 and the
+// tiles of 128 columns by bands of at most kWaveRows rows fit the SMs (one
+// CTA per SM).
+constexpr int kWaveMaxTiles = 4096;
+inline WaveTiling WaveTiles(const Dims& d, int sms) {
+  WaveTiling T;
+  T.w = 128;
+  T.xtiles = (d.nx + 127) / 128;
+  const int bands_max = std::max(1, sms / T.xtiles);
+  T.rows = (d.ny + bands_max - 1) / bands_max;
+  T.bands = (d.ny + T.rows - 1) / T.rows;
+  return T;
+}
+inline bool WaveDims(const Dims& d, int sms) {
+  if (!((d.nx % 4) == 0 && d.nx >= 8 && d.nz >= 4)) return false;
+  const WaveTiling T = WaveTiles(d, sms);
+  return T.rows <= kWaveRows && T.xtiles * T.bands <= std::min(sms, kWaveMaxTiles);
+}
 inline bool PipeEligible(const aphgpu_ctx* ctx, const Dims& d) {
   if (!PipeDims(d)) return false;
   return ctx->fused_mode == 2 ||
@@ -551,6 +570,46 @@ inline int SmCount(aphgpu_ctx* ctx) {
     sms = 152;
   }
   return sms;
+}
+// one wavefront sweep in place (first colour c0; zero_init: the first
+// colour starts from zero), cooperative launch
+inline int LaunchWave(aphgpu_ctx* ctx, const Op<float>& A, const float* b, float* x, int c0,
+                      int zero_init, const SolveScalars* s, cudaStream_t st) {
+  const int sms = SmCount(ctx);
+  const WaveTiling T = WaveTiles(A.d, sms);
+  const int tiles = T.xtiles * T.bands;
+  if (!ctx->wave_buf) APH_TRY(Alloc(ctx, &ctx->wave_buf, kWaveMaxTiles + 1));
+  if (!ctx->wave_used) {
+    APH_CUDA(ctx, cudaMemsetAsync(ctx->wave_buf + kWaveMaxTiles, 0, sizeof(int), st));
+    ctx->wave_used = true;
+  }
+  APH_CUDA(ctx, cudaMemsetAsync(ctx->wave_buf, 0xff, sizeof(int) * tiles, st));
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3(tiles);
+  cfg.blockDim = dim3(kWaveThreads);
+  cfg.dynamicSmemBytes = 0;
+  cfg.stream = st;
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeCooperative;
+  attr[0].val.cooperative = 1;
+  cfg.attrs = attr;
+  cfg.numAttrs = 1;
+  int* err = ctx->wave_buf + kWaveMaxTiles;
+  if (zero_init)
+    APH_CUDA(ctx, cudaLaunchKernelEx(&cfg, KSweepWave<1>, A, b, x, c0, s, T, ctx->wave_buf, err));
+  else
+    APH_CUDA(ctx, cudaLaunchKernelEx(&cfg, KSweepWave<0>, A, b, x, c0, s, T, ctx->wave_buf, err));
+  return APHGPU_OK;
+}
+// the flag of a wavefront wait that gave up (after the solve's last sync)
+int CheckWaveFlag(aphgpu_ctx* ctx) {
+  if (!ctx->wave_used) return APHGPU_OK;
+  int e = 0;
+  APH_CUDA(ctx, cudaMemcpy(&e, ctx->wave_buf + kWaveMaxTiles, sizeof(int),
+                           cudaMemcpyDeviceToHost));
+  ctx->wave_used = false;
+  if (e) return SetError(ctx, APHGPU_ERR_TIMEOUT, "wavefront sweep: a tile waited too long");
+  return APHGPU_OK;
 }
 // one pipelined sweep in -> out (first colour c0) with the kernel shape P
 template <class P>
@@ -1531,6 +1590,11 @@ template <class T>
 bool PipeUse(const aphgpu_ctx*, const Level<T>&, const Op<T>&) {
   return false;
 }
+inline bool WaveUse(aphgpu_ctx* ctx, const Level<float>& f) {
+  if (ctx->fused_mode != 5 && ctx->fused_mode != 6) return false;
+  if (ctx->fused_mode == 5 && f.d.cells() < kPipeMinCells) return false;
+  return WaveDims(f.d, SmCount(ctx));
+}
 template <>
 bool PipeUse<float>(const aphgpu_ctx* ctx, const Level<float>& f, const Op<float>& A) {
   return f.r && !A.diag && PipeEligible(ctx, f.d);
@@ -1543,6 +1607,14 @@ int FusedSweeps(aphgpu_ctx*, Level<T>&, const Op<T>&, int, int, bool, const Solv
 template <>
 int FusedSweeps<float>(aphgpu_ctx* ctx, Level<float>& f, const Op<float>& A, int n, int c0,
                        bool zero_first, const SolveScalars* s, bool in_r) {
+  if (WaveUse(ctx, f) && !in_r && n >= 1) {
+    // in place: the result is in f.x after each sweep
+    for (int k = 0; k < n; ++k)
+      APH_TRY(LaunchWave(ctx, A, f.b, f.x, c0, (k == 0 && zero_first) ? 1 : 0, s,
+                         ctx->stream));
+    ctx->launches += n;
+    return APHGPU_OK;
+  }
   const bool pipe = PipeUse<float>(ctx, f, A);
   const bool sync = !pipe && ctx->fused_mode == 3 && f.r && FusedOk(f.d);
   if (n < 1 || !(pipe || sync)) return kNotFused;
@@ -2280,7 +2352,8 @@ int TimeSolverKernel(aphgpu_ctx* ctx, int kernel, int reps, double* ms,
       break;
     }
     case APHGPU_K_SWEEP32: {
-      if (!mg.built32 || !ctx->r32 || !mg.l32[0].r)
+      const bool wave = mg.built32 && ctx->r32 && WaveUse(ctx, mg.l32[0]);
+      if (!mg.built32 || !ctx->r32 || !(mg.l32[0].r || wave))
         return SetError(ctx, APHGPU_ERR_STATE, "run a mixed solve first (fused level)");
       Level<float>& f = mg.l32[0];
       const Op<float> A = MakeOp(f);
@@ -2289,7 +2362,11 @@ int TimeSolverKernel(aphgpu_ctx* ctx, int kernel, int reps, double* ms,
       float* xo = f.r;
       const dim3 g = SweepGrid(d);
       const int kz = VecZ(d);
-      if (PipeUse<float>(ctx, f, A)) {
+      if (wave) {
+        // in place on the solver's scratch vector
+        float* xw = ctx->z32;
+        launch = [=]() { LaunchWave(ctx, A, bb, xw, 0, 0, nullptr, st); };
+      } else if (PipeUse<float>(ctx, f, A)) {
         launch = [=]() { LaunchPipe(ctx, A, bb, x, xo, 0, 0, nullptr, st); };
       } else {
         launch = [=]() {
@@ -2367,7 +2444,7 @@ int TimeSolverKernel(aphgpu_ctx* ctx, int kernel, int reps, double* ms,
   APH_CUDA(ctx, cudaEventElapsedTime(&t, ctx->ev0, ctx->ev1));
   *ms = (double)t / reps;
   *bytes = b;
-  return APHGPU_OK;
+  return CheckWave(ctx);
 }
 
 int SystemToExprDevice(aphgpu_ctx* ctx, double* d_e8) {
@@ -2406,5 +2483,7 @@ int Acceleration(aphgpu_ctx* ctx, double* d_acc, const double* d_alpha,
   APH_LAUNCHED(ctx);
   return APHGPU_OK;
 }
+
+int CheckWave(aphgpu_ctx* ctx) { return CheckWaveFlag(ctx); }
 
 }  // namespace aphgpu

@@ -473,3 +473,208 @@ __global__ void __launch_bounds__(P::kThreads, P::kCtasPerSm)
 }
 
 }  // namespace aphgpu
+
+namespace aphgpu {
+
+// ---------------------------------------------------------------------------
+// Wavefront red-black sweep, in place, one launch per full sweep.
+//
+// A CTA owns a tile of w <= 128 columns (one float4 per lane) by rows <=
+// kWaveRows rows and walks the planes: at step s it updates the first
+// colour c0 of plane s (the half sweep's operations, KSmooth4 / Smooth4Body,
+// for that plane), publishes "first colour done up to plane s" in its
+// progress counter, waits until the four neighbouring tiles have published
+// at least s - kWaveLag, and updates the second colour of plane s -
+// kWaveLag.  The second colour of plane 0 goes last (it reads the first
+// colour of plane nz-1, and the first colour of plane nz-1 reads its old
+// values).  Every value is read and written as in the two half sweeps: a
+// first-colour update reads old second-colour values (a tile's own second
+// colour of plane z changes only at step z + kWaveLag; a neighbour's only
+// after this tile published z), a second-colour update reads final
+// first-colour values (own planes up to s, the neighbours' after the wait),
+// so whole solves are bit-identical to the half sweeps.  The neighbours
+// lag each other by at most kWaveLag steps, so a plane's data is still in
+// L2 when the second colour re-reads it: HBM traffic is one read of x, b,
+// the couplings and one write of x per full sweep (24 B/cell).
+//
+// The CTAs wait on one another: the launch is cooperative (all CTAs
+// resident), every wait is bounded, and a wait that gives up sets err[0]
+// and goes on (the sweep's result is then wrong, and the solve reports
+// APHGPU_ERR_TIMEOUT).  The minimum-progress tile never waits (its
+// neighbours are at least at its own step), so the waits end.
+constexpr int kWaveRows = 14;
+constexpr int kWaveLag = 2;
+constexpr int kWaveThreads = 32 * kWaveRows;
+
+struct WaveTiling {
+  int w;       // columns of a tile (multiple of 4, <= 128)
+  int rows;    // rows of a band (<= kWaveRows)
+  int xtiles, bands;
+};
+
+// The rolling z window of one front (first or second colour) of a thread:
+// x of planes k-1 and k of its float4 and w2 of plane k.
+struct WaveFront {
+  float4 xz0, xz1, wz1;
+};
+
+// One plane k of one colour at the thread's float4 (column group q, row j),
+// in place: the body of Smooth4Body for one plane.  Loads x of plane k+1
+// into the window and rolls it.  Every lane of the warp calls it (XHalo).
+template <int ZI>
+__device__ __forceinline__ void WavePlane(const Op<float>& A, const float* __restrict__ b,
+                                          float* x, int color, int q, int j, bool act, int k,
+                                          WaveFront& F) {
+  const Dims d = A.d;
+  const int nq = d.nx >> 2;
+  const int i0 = 4 * q;
+  const int jm = wrapm(j - 1, d.ny), jp = wrapp(j + 1, d.ny);
+  const int kp = wrapp(k + 1, d.nz);
+  const int64_t c = d.idx(i0, j, k);
+  float4 w0v = make_float4(0, 0, 0, 0), w1v = w0v, w1n = w0v, bv = w0v, xjm = w0v, xjp = w0v;
+  float4 xz2 = w0v, wz2 = w0v;
+  if (act) {
+    wz2 = Ld4(A.w2 + d.idx(i0, j, kp));
+    w0v = Ld4(A.w0 + c);
+    w1v = Ld4(A.w1 + c);
+    w1n = Ld4(A.w1 + d.idx(i0, jp, k));
+    bv = Ld4(b + c);
+    if (!ZI) {
+      xz2 = Ld4(x + d.idx(i0, j, kp));
+      xjm = Ld4(x + d.idx(i0, jm, k));
+      xjp = Ld4(x + d.idx(i0, jp, k));
+    }
+  }
+  float xl, xr, wl, wr;
+  XHalo(x + d.idx(0, act ? j : 0, k), F.xz1, q, nq, act && !ZI, xl, xr);
+  XHalo(A.w0 + d.idx(0, act ? j : 0, k), w0v, q, nq, act, wl, wr);
+  (void)wl;
+  if (act) {
+    float4 out = F.xz1;
+    const int e0 = (color + j + k) & 1;
+#pragma unroll
+    for (int e = 0; e < 4; ++e) {
+      if ((e & 1) != e0) continue;
+      const float cxm = El(w0v, e);
+      const float cxp = e == 3 ? wr : El(w0v, e + 1);
+      const float cym = El(w1v, e), cyp = El(w1n, e);
+      const float czm = El(F.wz1, e), czp = El(wz2, e);
+      const float dg = A.diag ? A.diag[c + e] : -(((((cxm + cxp) + cym) + cyp) + czm) + czp);
+      float acc = El(bv, e);
+      if (!ZI) {
+        const float vxm = e == 0 ? xl : El(F.xz1, e - 1);
+        const float vxp = e == 3 ? xr : El(F.xz1, e + 1);
+        acc -= cxm * vxm;
+        acc -= cxp * vxp;
+        acc -= cym * El(xjm, e);
+        acc -= cyp * El(xjp, e);
+        acc -= czm * El(F.xz0, e);
+        acc -= czp * El(xz2, e);
+      }
+      SetEl(out, e, acc / dg);
+    }
+    St4(x + c, out);
+  }
+  F.xz0 = F.xz1;
+  F.xz1 = xz2;
+  F.wz1 = wz2;
+}
+
+// the window of a front about to update plane k
+template <int ZI>
+__device__ __forceinline__ void WaveInit(const Op<float>& A, const float* x, int q, int j,
+                                         bool act, int k, WaveFront& F) {
+  const Dims d = A.d;
+  const int i0 = 4 * q;
+  F.xz0 = F.xz1 = F.wz1 = make_float4(0, 0, 0, 0);
+  if (!act) return;
+  F.wz1 = Ld4(A.w2 + d.idx(i0, j, k));
+  if (!ZI) {
+    F.xz0 = Ld4(x + d.idx(i0, j, wrapm(k - 1, d.nz)));
+    F.xz1 = Ld4(x + d.idx(i0, j, k));
+  }
+}
+
+// thread 0 of the CTA: waits (bounded, about 0.3 s) until the four
+// neighbouring tiles have published at least z; err[0] = 1 when a wait
+// gives up, after which no tile of the grid waits any more
+__device__ __forceinline__ void WaveWait(const volatile int* prog, const int* nb, int z,
+                                         int* err) {
+  const volatile int* verr = err;
+  for (int q = 0; q < 4; ++q) {
+    int64_t it = 0;
+    while (prog[nb[q]] < z && *verr == 0) {
+      if (++it > (int64_t(1) << 22)) {
+        atomicExch(err, 1);
+        break;
+      }
+      __nanosleep(64);
+    }
+  }
+  __threadfence();
+}
+
+// One full sweep (first colour c0; ZI: the first colour starts from zero).
+// Grid: one CTA of kWaveThreads per tile (xtiles * bands), cooperative;
+// prog: one counter per tile, -1 before the launch.
+template <int ZI>
+__global__ void __launch_bounds__(kWaveThreads, 1)
+    KSweepWave(Op<float> A, const float* __restrict__ b, float* x, int c0,
+               const SolveScalars* s, WaveTiling T, int* prog, int* err) {
+  if (s && s->done) return;
+  const Dims d = A.d;
+  const int tile = blockIdx.x;
+  const int xt = tile % T.xtiles, band = tile / T.xtiles;
+  const int lane = threadIdx.x & 31, wp = threadIdx.x >> 5;
+  const int q = xt * (T.w >> 2) + lane;
+  const int j0 = band * T.rows;
+  const int rows = min(T.rows, d.ny - j0);
+  const int j = j0 + min(wp, rows - 1);
+  const bool act = wp < rows && 4 * lane < min(T.w, d.nx - xt * T.w);
+  __shared__ int nb[4];
+  if (threadIdx.x == 0) {
+    nb[0] = band * T.xtiles + (xt == 0 ? T.xtiles - 1 : xt - 1);
+    nb[1] = band * T.xtiles + (xt == T.xtiles - 1 ? 0 : xt + 1);
+    nb[2] = (band == 0 ? T.bands - 1 : band - 1) * T.xtiles + xt;
+    nb[3] = (band == T.bands - 1 ? 0 : band + 1) * T.xtiles + xt;
+  }
+  WaveFront f0, f1;
+  WaveInit<ZI>(A, x, q, j, act, 0, f0);
+  __syncthreads();
+  const int c1 = 1 - c0;
+  const int last = d.nz - 1 + kWaveLag;
+  for (int st = 0; st <= last; ++st) {
+    if (st < d.nz) {
+      // plane st+2 into L2 for the first colour's next steps
+      if (act && st + 2 < d.nz) {
+        const int64_t cn = d.idx(4 * q, j, st + 2);
+        PrefetchL2(A.w0 + cn);
+        PrefetchL2(A.w1 + cn);
+        PrefetchL2(A.w2 + cn);
+        PrefetchL2(b + cn);
+        PrefetchL2(x + cn);
+      }
+      WavePlane<ZI>(A, b, x, c0, q, j, act, st, f0);
+      __syncthreads();
+      if (threadIdx.x == 0) {
+        __threadfence();
+        *(volatile int*)(prog + tile) = st;
+      }
+    }
+    const int z = st - kWaveLag;
+    if (z >= 1 && z <= d.nz - 1) {
+      if (threadIdx.x == 0) WaveWait(prog, nb, z, err);
+      __syncthreads();
+      if (z == 1) WaveInit<0>(A, x, q, j, act, 1, f1);
+      WavePlane<0>(A, b, x, c1, q, j, act, z, f1);
+    }
+  }
+  // the second colour of plane 0, after every first colour of the
+  // neighbours (it reads the first colour of plane nz-1)
+  if (threadIdx.x == 0) WaveWait(prog, nb, d.nz - 1, err);
+  __syncthreads();
+  WaveInit<0>(A, x, q, j, act, 0, f1);
+  WavePlane<0>(A, b, x, c1, q, j, act, 0, f1);
+}
+
+}  // namespace aphgpu

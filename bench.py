@@ -1109,7 +1109,7 @@ def main():
     ap.add_argument("--profile", choices=["mixed", "fp64", "batch", "vof"], default=None,
                     help="profiling run: assemble, then `steps` solves of one solver "
                          "after `warmup` solves, no other work and no output line")
-    ap.add_argument("--sweeps", type=int, choices=[0, 1, 2, 3, 4], default=None,
+    ap.add_argument("--sweeps", type=int, choices=[0, 1, 2, 3, 4, 5, 6], default=None,
                     help="--profile: red-black sweep variant (APHGPU_OPT_FUSED_SWEEPS)")
     ap.add_argument("--estimator", choices=["heights", "particles", "hybrid"],
                     default="heights",

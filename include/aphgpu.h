@@ -471,7 +471,13 @@ int aphgpu_batch_last_ms(const aphgpu_batch* batch, double* ms, int64_t* launche
  *                            synchronous fused kernel (latency-bound) on
  *                            every level with nx a multiple of 4, nx >= 8;
  *                            4 as 1 with bands of 6 rows (two CTAs per
- *                            SM instead of one); 0 (default) two
+ *                            SM instead of one); 5 the in-place wavefront
+ *                            sweep (each CTA walks the planes of a tile,
+ *                            the second colour two planes behind the
+ *                            first, waiting for its neighbour tiles) on
+ *                            levels of at least 2^21 cells with nx a
+ *                            multiple of 4 and nz >= 4; 6 the wavefront
+ *                            sweep on every such level; 0 (default) two
  *                            in-place half sweeps everywhere.  Other
  *                            levels take the half sweeps
  *   APHGPU_OPT_HALF_COUPLINGS 1: the smoother and the restriction of the

@@ -279,7 +279,7 @@ def test_fused_sweeps_bit_identical(solver, shape):
     _, bn = ctx.residual_norms()
     conf = _lib.default_conf(solver=solver, tol=1e-10 * bn / math.sqrt(h ** 3), maxiter=200)
     out = {}
-    for fused in (2, 1, 4, 3, 0):
+    for fused in (2, 1, 4, 3, 6, 5, 0):
         for graphs in (1, 0):
             ctx.set_option(_lib.OPT_FUSED_SWEEPS, fused)
             ctx.set_option(_lib.OPT_GRAPHS, graphs)
