@@ -1,7 +1,7 @@
 """GPU parity of the PLIC VOF advection and height-function curvature
 against the oracle and aphros's own outputs.  Calls go through the C ABI.
 
-Tolerances: volume fractions within 1e-12 of aphros (spec bound; the
+Tolerances: volume fractions within 1e-12 of aphros (the required bound; the
 kernels follow the reference's arithmetic without FMA, so most cells agree
 bit for bit and the rest differ by libm last-bit effects in pow/acos/cos),
 the reference test's own 1e-11 against its golden file, curvature within
