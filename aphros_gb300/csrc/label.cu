@@ -70,9 +70,7 @@ __global__ void KLabelUnion(Dims d, int* par, int* err) {
   for (int64_t c = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; c < n;
        c += (int64_t)gridDim.x * blockDim.x) {
     if (vp[c] < 0) continue;
-    // fewer than 2^31 cells: the index splits in 32-bit arithmetic
-    const int c32 = (int)c, jk = c32 / d.nx;
-    const int i = c32 - jk * d.nx, j = jk % d.ny, k = jk / d.ny;
+    const int i = (int)(c % d.nx), j = (int)((c / d.nx) % d.ny), k = (int)(c / ((int64_t)d.nx * d.ny));
     for (int o = 0; o < 13; ++o) {
       // offsets with dz > 0, or dz == 0 and dy > 0, or dz == dy == 0, dx > 0
       const int q = o + 14;  // 14..26 in the 27-point numbering
@@ -133,39 +131,21 @@ __global__ void KLabelRoot(int64_t n, int* par) {
 // The first position, in the order of the cells with two halo layers
 // (x-fastest over [-2, n+2) per axis), of a gas cell of each component that
 // has a previous colour.  A cell's smallest position takes its left halo
-// copy where it has one (the last two cells of an axis).  The positions fit
-// 32 bits (fewer than 2^31 cells, each axis below 2^10 + 4 here), the lanes
-// of a warp that update the same component first take their minimum
-// together (one atomic per component and warp), and the cell index is split
-// with 32-bit arithmetic.
+// copy where it has one (the last two cells of an axis).
 __global__ void KLabelFirst(Dims d, const int* __restrict__ root, const int* __restrict__ slot,
                             const double* __restrict__ clprev, unsigned long long* first) {
-  const int n = (int)d.cells();
-  const unsigned ex = d.nx + 4, ey = d.ny + 4;
-  const int lane = threadIdx.x & 31;
-  const int stride = gridDim.x * blockDim.x;
-  // every lane of a warp runs the same iterations (warp-collective below)
-  for (int base = blockIdx.x * blockDim.x + (threadIdx.x & ~31); base < n; base += stride) {
-    const int c = base + lane;
-    int key = -1;
-    unsigned e = 0;
-    if (c < n) {
-      const int r = root[c];
-      if (r >= 0 && clprev[c] != -1.0) {
-        const int i = c % d.nx, jk = c / d.nx;
-        const int j = jk % d.ny, k = jk / d.ny;
-        const int xi = i >= d.nx - 2 ? i - d.nx + 2 : i + 2;
-        const int yj = j >= d.ny - 2 ? j - d.ny + 2 : j + 2;
-        const int zk = k >= d.nz - 2 ? k - d.nz + 2 : k + 2;
-        e = ((unsigned)zk * ey + (unsigned)yj) * ex + (unsigned)xi;
-        key = slot[r];
-      }
-    }
-    // most warps hold no coloured gas cell: the grouping only where one does
-    if (__ballot_sync(0xffffffffu, key >= 0) == 0) continue;
-    const unsigned group = __match_any_sync(0xffffffffu, key);
-    const unsigned m = __reduce_min_sync(group, e);
-    if (key >= 0 && lane == __ffs(group) - 1) atomicMin(&first[key], (unsigned long long)m);
+  const int64_t n = d.cells();
+  const unsigned long long ex = d.nx + 4, ey = d.ny + 4;
+  for (int64_t c = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; c < n;
+       c += (int64_t)gridDim.x * blockDim.x) {
+    const int r = root[c];
+    if (r < 0 || clprev[c] == -1.0) continue;
+    const int i = (int)(c % d.nx), j = (int)((c / d.nx) % d.ny), k = (int)(c / ((int64_t)d.nx * d.ny));
+    const int xi = i >= d.nx - 2 ? i - d.nx + 2 : i + 2;
+    const int yj = j >= d.ny - 2 ? j - d.ny + 2 : j + 2;
+    const int zk = k >= d.nz - 2 ? k - d.nz + 2 : k + 2;
+    const unsigned long long e = ((unsigned long long)zk * ey + yj) * ex + xi;
+    atomicMin(&first[slot[r]], e);
   }
 }
 
@@ -347,10 +327,6 @@ int Recolor(aphgpu_ctx* ctx) {
   std::vector<double> color(std::max(nc, 1));
   if (nc > 0) {
     APH_CUDA(ctx, cudaMemsetAsync(L.first, 0xff, sizeof(unsigned long long) * nc, st));
-    // the positions of KLabelFirst are 32-bit
-    if ((uint64_t)(d.nx + 4) * (d.ny + 4) * (d.nz + 4) >= (uint64_t(1) << 32))
-      return SetError(ctx, APHGPU_ERR_UNSUPPORTED,
-                      "recolor: the grid with two halo layers exceeds 2^32 cells");
     KLabelFirst<<<nb, kLabelThreads, 0, st>>>(d, L.par, L.slot, ctx->cl, L.first);
     APH_LAUNCHED(ctx);
     KLabelStable<<<Blocks(nc), kLabelThreads, 0, st>>>(d, nc, L.first, ctx->cl, L.stable);

@@ -7,9 +7,8 @@
 // estimator (curv.ipp:525-560: heights, then particles where the heights
 // give no curvature).
 //
-// One thread per interfacial cell, its strings in turn: for string s the
-// section plane at angle s*pi/ns through the cell's PLIC centre, the
-// segments where that plane
+// One thread per (interfacial cell, string): the section plane at angle
+// s*pi/ns through the cell's PLIC centre, the segments where that plane
 // cuts the PLIC polygons of the interfacial cells of the 5x5x5 stencil
 // (mesh order, x fastest; cell centres unwrapped, data wrapped), a string
 // of np particles relaxed by the interface force and the rotation and
@@ -446,19 +445,19 @@ struct PartArgs {
   aphgpu_part_conf p;
 };
 
-// the strings of one listed cell (thread t = position in the list): a
-// warp then waits for the sum of its cells' strings, whose spread is
-// smaller than that of single strings
+// one string of a listed cell: t = position in the list * ns + string
 __global__ void KPartStrings(PartArgs A, const double* __restrict__ u,
                              const double* __restrict__ nrm, const double* __restrict__ pa,
                              const double* __restrict__ kappa, int fill_only,
                              const int* __restrict__ list, const int* count, double* kpart) {
   const int ns = A.p.ns, np = A.p.np;
-  const int64_t total = *count;
+  const int64_t total = (int64_t)(*count) * ns;
   const Dims d = A.d;
   const double h = A.h, half = h * 0.5;
-  for (int64_t li = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; li < total;
-       li += (int64_t)gridDim.x * blockDim.x) {
+  for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < total;
+       t += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t li = t / ns;
+    const int s = (int)(t - li * ns);
     const int64_t c = list[li];
     if (fill_only && kappa[c] == kappa[c]) continue;  // defined by the heights
     const int i = (int)(c % d.nx);
@@ -466,57 +465,54 @@ __global__ void KPartStrings(PartArgs A, const double* __restrict__ u,
     const int k = (int)(c / ((int64_t)d.nx * d.ny));
     const double xc[3] = {(0. + half) + (double)i * h, (0. + half) + (double)j * h,
                           (0. + half) + (double)k * h};
+    const double an = (double)s * M_PI / (double)ns;
     const double nc[3] = {nrm[3 * c], nrm[3 * c + 1], nrm[3 * c + 2]};
-    for (int s = 0; s < ns; ++s) {
-      const double an = (double)s * M_PI / (double)ns;
-      Basis B;
-      PlaneBasis(xc, nc, pa[c], an, h, B);
-      double uz[3];
-      Cross3(B.ux, B.uy, uz);
-      Seg sg[kPsMaxSeg];
-      int nseg = 0;
-      for (int dz = -2; dz <= 2; ++dz)
-        for (int dy = -2; dy <= 2; ++dy)
-          for (int dx = -2; dx <= 2; ++dx) {
-            const int64_t cn =
-                d.idx(Wrap(i + dx, d.nx), Wrap(j + dy, d.ny), Wrap(k + dz, d.nz));
-            if (!Interfacial(u[cn])) continue;
-            const double xn[3] = {(0. + half) + (double)(i + dx) * h,
-                                  (0. + half) + (double)(j + dy) * h,
-                                  (0. + half) + (double)(k + dz) * h};
-            const double nn[3] = {nrm[3 * cn], nrm[3 * cn + 1], nrm[3 * cn + 2]};
-            V2 e[2];
-            if (AppendInterface(B, uz, xn, pa[cn], nn, h, e)) {
-              Seg& g = sg[nseg++];
-              g.x0 = e[0];
-              g.x1 = e[1];
-              g.l = Sub(e[1], e[0]);
-              g.ll = Dot(g.l, g.l);
-            }
+    Basis B;
+    PlaneBasis(xc, nc, pa[c], an, h, B);
+    double uz[3];
+    Cross3(B.ux, B.uy, uz);
+    Seg sg[kPsMaxSeg];
+    int nseg = 0;
+    for (int dz = -2; dz <= 2; ++dz)
+      for (int dy = -2; dy <= 2; ++dy)
+        for (int dx = -2; dx <= 2; ++dx) {
+          const int64_t cn = d.idx(Wrap(i + dx, d.nx), Wrap(j + dy, d.ny), Wrap(k + dz, d.nz));
+          if (!Interfacial(u[cn])) continue;
+          const double xn[3] = {(0. + half) + (double)(i + dx) * h,
+                                (0. + half) + (double)(j + dy) * h,
+                                (0. + half) + (double)(k + dz) * h};
+          const double nn[3] = {nrm[3 * cn], nrm[3 * cn + 1], nrm[3 * cn + 2]};
+          V2 e[2];
+          if (AppendInterface(B, uz, xn, pa[cn], nn, h, e)) {
+            Seg& g = sg[nseg++];
+            g.x0 = e[0];
+            g.x1 = e[1];
+            g.l = Sub(e[1], e[0]);
+            g.ll = Dot(g.l, g.l);
           }
-      // seed (PartStr::Add, partstr.h:82-92: centre 0, tangent (1, 0)) and
-      // iterate (Run0 with Iter, partstr.h:110-157)
-      V2 xx[kPsMaxNp], ff[kPsMaxNp];
-      const double leq = A.p.leq * h / (double)(np - 1);
-      for (int q = 0; q < np; ++q) {
-        const double sq = ((double)q - (np - 1) * 0.5) * leq;
-        xx[q] = Mk(0. + 1. * sq, 0. + 0. * sq);
-      }
-      for (int it = 0; it < A.p.itermax; ++it) {
-        InterfaceForce(xx, np, sg, nseg, A.p.segcirc, ff);
-        ApplyConstraints(xx, np, A.p.relax, A.p.dn, ff);
-        double r = 0.;
-        for (int q = 0; q < np; ++q) {
-          xx[q] = Add(xx[q], ff[q]);
-          const double ax = fabs(ff[q].x), ay = fabs(ff[q].y);
-          r = r < ax ? ax : r;
-          r = r < ay ? ay : r;
         }
-        r /= h * A.p.relax;
-        if (r < A.p.tol) break;
-      }
-      kpart[li * ns + s] = PartK(xx, np);
+    // seed (PartStr::Add, partstr.h:82-92: centre 0, tangent (1, 0)) and
+    // iterate (Run0 with Iter, partstr.h:110-157)
+    V2 xx[kPsMaxNp], ff[kPsMaxNp];
+    const double leq = A.p.leq * h / (double)(np - 1);
+    for (int q = 0; q < np; ++q) {
+      const double sq = ((double)q - (np - 1) * 0.5) * leq;
+      xx[q] = Mk(0. + 1. * sq, 0. + 0. * sq);
     }
+    for (int it = 0; it < A.p.itermax; ++it) {
+      InterfaceForce(xx, np, sg, nseg, A.p.segcirc, ff);
+      ApplyConstraints(xx, np, A.p.relax, A.p.dn, ff);
+      double r = 0.;
+      for (int q = 0; q < np; ++q) {
+        xx[q] = Add(xx[q], ff[q]);
+        const double ax = fabs(ff[q].x), ay = fabs(ff[q].y);
+        r = r < ax ? ax : r;
+        r = r < ay ? ay : r;
+      }
+      r /= h * A.p.relax;
+      if (r < A.p.tol) break;
+    }
+    kpart[t] = PartK(xx, np);
   }
 }
 
@@ -570,7 +566,7 @@ int CurvatureParticlesDevice(aphgpu_ctx* ctx, const aphgpu_part_conf& conf, bool
     ctx->kpart_cap = need;
   }
   PartArgs A{ctx->d, ctx->h, conf};
-  const int blocks = (int)std::min<int64_t>((nif + 127) / 128, 16 * 1024);
+  const int blocks = (int)std::min<int64_t>((need + 127) / 128, 16 * 1024);
   KPartStrings<<<blocks, 128, 0, ctx->stream>>>(A, ctx->u, ctx->nrm, ctx->pa, ctx->kappa,
                                                 hybrid ? 1 : 0, list, count, ctx->kpart);
   APH_LAUNCHED(ctx);

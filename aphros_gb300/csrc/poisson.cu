@@ -944,8 +944,9 @@ __global__ void KCoarsenFaces(Op<T> A, Dims dc, TC* w0, TC* w1, TC* w2, TC* diag
   if (I >= dc.nx || J >= dc.ny) return;
   const Dims& d = A.d;
   for (int K = kb; K < ke; ++K) {
+    // the children's summed row sums (diagonal shifts), for systems with one
     double shift = 0;
-    for (int q = 0; q < 8; ++q) {
+    for (int q = 0; with_shift && q < 8; ++q) {
       const int i = 2 * I + (q & 1), j = 2 * J + ((q >> 1) & 1), k = 2 * K + (q >> 2);
       const int64_t c = d.idx(i, j, k);
       T e[6];
