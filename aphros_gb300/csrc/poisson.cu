@@ -608,7 +608,11 @@ int CheckWaveFlag(aphgpu_ctx* ctx) {
   APH_CUDA(ctx, cudaMemcpy(&e, ctx->wave_buf + kWaveMaxTiles, sizeof(int),
                            cudaMemcpyDeviceToHost));
   ctx->wave_used = false;
-  if (e) return SetError(ctx, APHGPU_ERR_TIMEOUT, "wavefront sweep: a tile waited too long");
+  if (e) {
+    // cleared for the next solve, which sets it again only if it times out
+    APH_CUDA(ctx, cudaMemset(ctx->wave_buf + kWaveMaxTiles, 0, sizeof(int)));
+    return SetError(ctx, APHGPU_ERR_TIMEOUT, "wavefront sweep: a tile waited too long");
+  }
   return APHGPU_OK;
 }
 // one pipelined sweep in -> out (first colour c0) with the kernel shape P
