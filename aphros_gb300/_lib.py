@@ -26,6 +26,7 @@ OPT_CYCLE = 3
 OPT_COARSE_SERIES = 4
 OPT_SWEEP_GROWTH = 5
 OPT_CTA_COARSE = 6
+OPT_WAVE_PLANES = 7
 FIELD_PRESSURE, FIELD_RHS, FIELD_VF, FIELD_CURVATURE = 0, 1, 2, 3
 DUMP_UINT16, DUMP_FLOAT32, DUMP_FLOAT64 = 0, 1, 2
 
@@ -148,6 +149,7 @@ def lib():
     L.aphgpu_residual_history.restype = _I
     L.aphgpu_elapsed.argtypes = [_P, _I, _I, _PD]
     L.aphgpu_time_kernel.argtypes = [_P, _I, _I, _PD, _PD]
+    L.aphgpu_wave_wait_check.argtypes = [_P]
     L.aphgpu_batch_create.argtypes = [ctypes.POINTER(_P), _I, ctypes.POINTER(_P)]
     L.aphgpu_batch_destroy.argtypes = [_P]
     L.aphgpu_batch_destroy.restype = None

@@ -859,6 +859,11 @@ int aphgpu_set_option(aphgpu_ctx* ctx, int option, int value) {
       ctx->mg_gamma = value;
       return APHGPU_OK;
     case APHGPU_OPT_CTA_COARSE: ctx->use_cta_coarse = value != 0; return APHGPU_OK;
+    case APHGPU_OPT_WAVE_PLANES:
+      if (value < 0 || value > 4096)
+        return SetError(ctx, APHGPU_ERR_ARG, "wave planes must be 0..4096");
+      ctx->wave_planes = value;
+      return APHGPU_OK;
     case APHGPU_OPT_SWEEP_GROWTH:
       if (value < 0 || value > 3) return SetError(ctx, APHGPU_ERR_ARG, "sweep growth must be 0..3");
       ctx->mg_growth = value;
@@ -907,6 +912,12 @@ int aphgpu_time_kernel(aphgpu_ctx* ctx, int kernel, int reps, double* ms, double
     return TimeVofKernel(ctx, kernel, reps, ms, bytes, d_vf, ctx->vof_dt);
   }
   return TimeSolverKernel(ctx, kernel, reps, ms, bytes);
+}
+
+int aphgpu_wave_wait_check(aphgpu_ctx* ctx) {
+  if (!Valid(ctx)) return APHGPU_ERR_ARG;
+  APH_TRY(SetDevice(ctx));
+  return WaveWaitCheck(ctx);
 }
 
 int aphgpu_last_timing(const aphgpu_ctx* ctx, double* ms, int64_t* launches) {

@@ -389,6 +389,7 @@ struct aphgpu_ctx {
   // pipelined kernel on every level it supports, 3 the synchronous fused
   // kernel on every level it supports
   int fused_mode = 0;
+  int wave_planes = 0;  // planes per step of the wavefront sweep (0: sized to L2)
   bool use_half = false;   // FP16 couplings for the finest-level smoother
   int mg_gamma = 0;        // cycles of each level below the finest (1 V, 2 W, 0 auto)
   int mg_series_pct = 60;  // weight (%) of the series couplings in the coarse operators
@@ -497,5 +498,7 @@ int TimeVofKernel(aphgpu_ctx* ctx, int kernel, int reps, double* ms, double* byt
 int TimeSolverKernel(aphgpu_ctx* ctx, int kernel, int reps, double* ms, double* bytes);
 // the error flag of the wavefront sweeps launched since the last check
 int CheckWave(aphgpu_ctx* ctx);
+// the wavefront sweep's bounded wait on a counter nothing sets
+int WaveWaitCheck(aphgpu_ctx* ctx);
 
 }  // namespace aphgpu

@@ -23,6 +23,7 @@
 //   MIXED  FP64 defect correction: r = b - A x, the update and the outer
 //          norms in FP64; the correction equation solved by FP32 MG-PCG;
 //          the coarsest level solved in FP64.
+#include <atomic>
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -515,6 +516,20 @@ inline bool PipeDims(const Dims& d) {
 // tiles of 128 columns by bands of at most kWaveRows rows fit the SMs (one
 // CTA per SM).
 constexpr int kWaveMaxTiles = 4096;
+// Planes per step of the wavefront sweep: three chunks of the level (the
+// one prefetched, the one in its first colour, the one in its second) of x,
+// b and the three couplings (20 bytes per cell) within about half of the
+// 126 MB L2, and one chunk of a tile within 150 KB of L1 (a phase's items
+// reread their neighbours' rows from there).
+constexpr double kWaveL2Bytes = 60e6;
+constexpr double kWaveL1Bytes = 150e3;
+inline int WavePlanes(const aphgpu_ctx* ctx, const Dims& d, const WaveTiling& T) {
+  if (ctx->wave_planes > 0) return std::min(ctx->wave_planes, d.nz);
+  const double plane = 20.0 * (double)d.nx * (double)d.ny;
+  const double tile = 20.0 * (double)T.w * (double)T.rows;
+  const int k = (int)std::min(kWaveL2Bytes / (3.0 * plane), kWaveL1Bytes / tile);
+  return std::max(1, std::min(k, d.nz));
+}
 inline WaveTiling WaveTiles(const Dims& d, int sms) {
   WaveTiling T;
   T.w = 128;
@@ -595,10 +610,23 @@ inline int LaunchWave(aphgpu_ctx* ctx, const Op<float>& A, const float* b, float
   cfg.attrs = attr;
   cfg.numAttrs = 1;
   int* err = ctx->wave_buf + kWaveMaxTiles;
+  const int K = WavePlanes(ctx, A.d, T);
+  // all of the SM's shared storage as L1 (once per device; the attribute
+  // is a preference, so a failure only clears the error)
+  static std::atomic<uint64_t> carveout{0};
+  const uint64_t bit = uint64_t(1) << (ctx->device & 63);
+  if (!(carveout.load() & bit)) {
+    cudaFuncSetAttribute(KSweepWave<0>, cudaFuncAttributePreferredSharedMemoryCarveout, 0);
+    cudaFuncSetAttribute(KSweepWave<1>, cudaFuncAttributePreferredSharedMemoryCarveout, 0);
+    cudaGetLastError();
+    carveout.fetch_or(bit);
+  }
   if (zero_init)
-    APH_CUDA(ctx, cudaLaunchKernelEx(&cfg, KSweepWave<1>, A, b, x, c0, s, T, ctx->wave_buf, err));
+    APH_CUDA(ctx, cudaLaunchKernelEx(&cfg, KSweepWave<1>, A, b, x, c0, s, T, K, ctx->wave_buf,
+                                     err));
   else
-    APH_CUDA(ctx, cudaLaunchKernelEx(&cfg, KSweepWave<0>, A, b, x, c0, s, T, ctx->wave_buf, err));
+    APH_CUDA(ctx, cudaLaunchKernelEx(&cfg, KSweepWave<0>, A, b, x, c0, s, T, K, ctx->wave_buf,
+                                     err));
   return APHGPU_OK;
 }
 // the flag of a wavefront wait that gave up (after the solve's last sync)
@@ -1509,12 +1537,14 @@ int BuildHierarchy<float>(aphgpu_ctx* ctx, std::vector<Level<float>>& lv,
     for (size_t l = 0; l < dims.size(); ++l) {
       lv[l].d = dims[l];
       APH_TRY(AllocLevel(ctx, lv[l], true, l > 0));
-      // scratch of the out-of-place fused sweeps (when enabled)
-      if (PipeEligible(ctx, dims[l]) || (ctx->fused_mode == 3 && FusedOk(dims[l])))
-        APH_TRY(Alloc(ctx, &lv[l].r, dims[l].cells()));
       lv[l].has_diag = true;
     }
   }
+  // scratch of the out-of-place fused sweeps, also when the option was
+  // switched on after the levels were first allocated
+  for (size_t l = 0; l < dims.size(); ++l)
+    if (!lv[l].r && (PipeEligible(ctx, dims[l]) || (ctx->fused_mode == 3 && FusedOk(dims[l]))))
+      APH_TRY(Alloc(ctx, &lv[l].r, dims[l].cells()));
   // fine FP32 operator from the FP64 system: couplings rounded to FP32;
   // the diagonal is -(sum of the FP32 couplings) for flux-difference
   // systems (keeps the constant null space exact) or the rounded FP64
@@ -1937,6 +1967,7 @@ int Pcg(aphgpu_ctx* ctx, const Op<T>& A, Precond precond, T* x, T* r, T* p,
     key = Mix(key, (uint64_t)check_every);
     key = Mix(key, (uint64_t)sizeof(T));
     key = Mix(key, (uint64_t)ctx->fused_mode);
+    key = Mix(key, (uint64_t)ctx->wave_planes);
     key = Mix(key, (uint64_t)CycleGamma(ctx));
     key = Mix(key, (uint64_t)SweepGrowth(ctx));
     key = Mix(key, (uint64_t)(ctx->use_cta_coarse ? 1 + ctx->mg.clc : 0));
@@ -2490,5 +2521,16 @@ int Acceleration(aphgpu_ctx* ctx, double* d_acc, const double* d_alpha,
 }
 
 int CheckWave(aphgpu_ctx* ctx) { return CheckWaveFlag(ctx); }
+
+int WaveWaitCheck(aphgpu_ctx* ctx) {
+  if (!ctx->wave_buf) APH_TRY(Alloc(ctx, &ctx->wave_buf, kWaveMaxTiles + 1));
+  APH_CUDA(ctx, cudaMemsetAsync(ctx->wave_buf, 0xff, sizeof(int), ctx->stream));
+  APH_CUDA(ctx, cudaMemsetAsync(ctx->wave_buf + kWaveMaxTiles, 0, sizeof(int), ctx->stream));
+  ctx->wave_used = true;
+  KWaveWaitProbe<<<1, 32, 0, ctx->stream>>>(ctx->wave_buf, ctx->wave_buf + kWaveMaxTiles);
+  APH_LAUNCHED(ctx);
+  APH_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+  return CheckWaveFlag(ctx);
+}
 
 }  // namespace aphgpu

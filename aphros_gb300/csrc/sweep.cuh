@@ -479,158 +479,221 @@ namespace aphgpu {
 // ---------------------------------------------------------------------------
 // Wavefront red-black sweep, in place, one launch per full sweep.
 //
-// A CTA owns a tile of w <= 128 columns (one float4 per lane) by rows <=
-// kWaveRows rows and walks the planes: at step s it updates the first
-// colour c0 of plane s (the half sweep's operations, KSmooth4 / Smooth4Body,
-// for that plane), publishes "first colour done up to plane s" in its
-// progress counter, waits until the four neighbouring tiles have published
-// at least s - kWaveLag, and updates the second colour of plane s -
-// kWaveLag.  The second colour of plane 0 goes last (it reads the first
-// colour of plane nz-1, and the first colour of plane nz-1 reads its old
-// values).  Every value is read and written as in the two half sweeps: a
-// first-colour update reads old second-colour values (a tile's own second
-// colour of plane z changes only at step z + kWaveLag; a neighbour's only
-// after this tile published z), a second-colour update reads final
-// first-colour values (own planes up to s, the neighbours' after the wait),
-// so whole solves are bit-identical to the half sweeps.  The neighbours
-// lag each other by at most kWaveLag steps, so a plane's data is still in
-// L2 when the second colour re-reads it: HBM traffic is one read of x, b,
-// the couplings and one write of x per full sweep (24 B/cell).
+// A CTA owns a tile of w <= 128 columns (one float4 per lane) by `rows`
+// rows and walks the planes in chunks of K: at step s it updates the first
+// colour c0 of the chunk's planes [sK, sK+K) (the half sweep's operations,
+// KSmooth4 / Smooth4Body, cell for cell), publishes in its progress counter
+// the number of planes whose first colour is done, waits until the four
+// neighbouring tiles have published at least the end of chunk s-1, and
+// updates the second colour of the planes [(s-1)K - 1, sK - 1) (the first
+// of them 1).  After the last chunk the remaining planes up to nz-1 follow,
+// and the second colour of plane 0 goes last (it reads the first colour of
+// plane nz-1, and the first colour of plane nz-1 reads its old values).
+// Every value is read and written as in the two half sweeps: a first-colour
+// update reads old second-colour values (a tile's own second colour of plane
+// z changes only after its first colour of plane z+1; a neighbour's only
+// after this tile published z+1), a second-colour update reads final
+// first-colour values (own planes up to the chunk end, the neighbours' after
+// the wait), so whole solves are bit-identical to the half sweeps.  Within a
+// phase the (plane, row) items are independent and the 16 warps take them
+// two at a time, both items' loads issued before either update: a phase is
+// a few memory round trips however many planes it covers, and the
+// synchronisation (a fence, a release, four polls in parallel, an acquire)
+// is paid once per chunk.  The next chunk is prefetched into L2 at the start
+// of a step (prefetch.global.L2 of each lane's float4 of the five arrays),
+// and the host sizes K so that three chunks of the grid (prefetched, first
+// colour, second colour) fit in L2 and a tile's chunk in L1, where the
+// items of a phase find the rows their neighbours loaded: HBM traffic is
+// one read of x, b and the couplings and one write of x per full sweep
+// (24 B/cell).
 //
 // The CTAs wait on one another: the launch is cooperative (all CTAs
 // resident), every wait is bounded, and a wait that gives up sets err[0]
 // and goes on (the sweep's result is then wrong, and the solve reports
-// APHGPU_ERR_TIMEOUT).  The minimum-progress tile never waits (its
-// neighbours are at least at its own step), so the waits end.
-constexpr int kWaveRows = 14;
-constexpr int kWaveLag = 2;
-constexpr int kWaveThreads = 32 * kWaveRows;
+// APHGPU_ERR_TIMEOUT).  The tile at the smallest step never waits (every
+// neighbour has published at least the chunk before), so the waits end.
+constexpr int kWaveWarps = 16;
+constexpr int kWaveThreads = 32 * kWaveWarps;
+constexpr int kWaveRows = 64;
 
 struct WaveTiling {
   int w;       // columns of a tile (multiple of 4, <= 128)
-  int rows;    // rows of a band (<= kWaveRows)
+  int rows;    // rows of a band
   int xtiles, bands;
 };
 
-// The rolling z window of one front (first or second colour) of a thread:
-// x of planes k-1 and k of its float4 and w2 of plane k.
-struct WaveFront {
-  float4 xz0, xz1, wz1;
+// Operands of one (plane k, row j) item of a colour at a thread's float4,
+// loaded ahead of its update.  xl, xr, wr: the x and w0 values left and
+// right of the float4 where a shuffle cannot supply them (tile edge lanes
+// and the periodic wrap).
+struct WaveLoads {
+  float4 xc, xm, xp, xjm, xjp, wz, wzp, w0v, w1v, w1n, bv;
+  float xl, xr, wr;
 };
 
-// One plane k of one colour at the thread's float4 (column group q, row j),
-// in place: the body of Smooth4Body for one plane.  Loads x of plane k+1
-// into the window and rolls it.  Every lane of the warp calls it (XHalo).
-template <int ZI>
-__device__ __forceinline__ void WavePlane(const Op<float>& A, const float* __restrict__ b,
-                                          float* x, int color, int q, int j, bool act, int k,
-                                          WaveFront& F) {
-  const Dims d = A.d;
-  const int nq = d.nx >> 2;
-  const int i0 = 4 * q;
-  const int jm = wrapm(j - 1, d.ny), jp = wrapp(j + 1, d.ny);
-  const int kp = wrapp(k + 1, d.nz);
-  const int64_t c = d.idx(i0, j, k);
-  float4 w0v = make_float4(0, 0, 0, 0), w1v = w0v, w1n = w0v, bv = w0v, xjm = w0v, xjp = w0v;
-  float4 xz2 = w0v, wz2 = w0v;
-  if (act) {
-    wz2 = Ld4(A.w2 + d.idx(i0, j, kp));
-    w0v = Ld4(A.w0 + c);
-    w1v = Ld4(A.w1 + c);
-    w1n = Ld4(A.w1 + d.idx(i0, jp, k));
-    bv = Ld4(b + c);
-    if (!ZI) {
-      xz2 = Ld4(x + d.idx(i0, j, kp));
-      xjm = Ld4(x + d.idx(i0, jm, k));
-      xjp = Ld4(x + d.idx(i0, jp, k));
-    }
-  }
-  float xl, xr, wl, wr;
-  XHalo(x + d.idx(0, act ? j : 0, k), F.xz1, q, nq, act && !ZI, xl, xr);
-  XHalo(A.w0 + d.idx(0, act ? j : 0, k), w0v, q, nq, act, wl, wr);
-  (void)wl;
-  if (act) {
-    float4 out = F.xz1;
-    const int e0 = (color + j + k) & 1;
-#pragma unroll
-    for (int e = 0; e < 4; ++e) {
-      if ((e & 1) != e0) continue;
-      const float cxm = El(w0v, e);
-      const float cxp = e == 3 ? wr : El(w0v, e + 1);
-      const float cym = El(w1v, e), cyp = El(w1n, e);
-      const float czm = El(F.wz1, e), czp = El(wz2, e);
-      const float dg = A.diag ? A.diag[c + e] : -(((((cxm + cxp) + cym) + cyp) + czm) + czp);
-      float acc = El(bv, e);
-      if (!ZI) {
-        const float vxm = e == 0 ? xl : El(F.xz1, e - 1);
-        const float vxp = e == 3 ? xr : El(F.xz1, e + 1);
-        acc -= cxm * vxm;
-        acc -= cxp * vxp;
-        acc -= cym * El(xjm, e);
-        acc -= cyp * El(xjp, e);
-        acc -= czm * El(F.xz0, e);
-        acc -= czp * El(xz2, e);
-      }
-      SetEl(out, e, acc / dg);
-    }
-    St4(x + c, out);
-  }
-  F.xz0 = F.xz1;
-  F.xz1 = xz2;
-  F.wz1 = wz2;
+__device__ __forceinline__ float4 Ldcg4(const float* p) {
+  return __ldcg(reinterpret_cast<const float4*>(p));
 }
 
-// the window of a front about to update plane k
-template <int ZI>
-__device__ __forceinline__ void WaveInit(const Op<float>& A, const float* x, int q, int j,
-                                         bool act, int k, WaveFront& F) {
+// Loads through L1, which is coherent with this CTA's own stores: a
+// tile's own rows, and the neighbours' old second-colour values (which no
+// one writes before this tile publishes).  SC (second colour): the rows and
+// columns of the neighbouring tiles (first-colour values those tiles wrote
+// after this SM may have cached the line) are read through L2 only, after
+// the acquire of the wait.
+template <int ZI, int SC>
+__device__ __forceinline__ void WaveLoad(const Op<float>& A, const float* __restrict__ b,
+                                         const float* x, int q, int j, int k, bool act,
+                                         bool jfirst, bool jlast, WaveLoads& L) {
   const Dims d = A.d;
-  const int i0 = 4 * q;
-  F.xz0 = F.xz1 = F.wz1 = make_float4(0, 0, 0, 0);
+  const int nq = d.nx >> 2, i0 = 4 * q, sl = threadIdx.x & 31;
+  const float4 z4 = make_float4(0.f, 0.f, 0.f, 0.f);
+  L.xc = L.xm = L.xp = L.xjm = L.xjp = L.wz = L.wzp = L.w0v = L.w1v = L.w1n = L.bv = z4;
+  L.xl = L.xr = L.wr = 0.f;
   if (!act) return;
-  F.wz1 = Ld4(A.w2 + d.idx(i0, j, k));
+  const int jm = wrapm(j - 1, d.ny), jp = wrapp(j + 1, d.ny);
+  const int km = wrapm(k - 1, d.nz), kp = wrapp(k + 1, d.nz);
+  const int64_t c = d.idx(i0, j, k);
+  const int64_t row = d.idx(0, j, k);
+  const bool right = sl == 31 || q == nq - 1;
+  L.wz = Ld4(A.w2 + c);
+  L.wzp = Ld4(A.w2 + d.idx(i0, j, kp));
+  L.w0v = Ld4(A.w0 + c);
+  L.w1v = Ld4(A.w1 + c);
+  L.w1n = Ld4(A.w1 + d.idx(i0, jp, k));
+  L.bv = Ld4(b + c);
+  if (right) L.wr = A.w0[row + (q == nq - 1 ? 0 : 4 * q + 4)];
   if (!ZI) {
-    F.xz0 = Ld4(x + d.idx(i0, j, wrapm(k - 1, d.nz)));
-    F.xz1 = Ld4(x + d.idx(i0, j, k));
+    L.xc = Ld4(x + c);
+    L.xm = Ld4(x + d.idx(i0, j, km));
+    L.xp = Ld4(x + d.idx(i0, j, kp));
+    const float* pjm = x + d.idx(i0, jm, k);
+    const float* pjp = x + d.idx(i0, jp, k);
+    L.xjm = SC && jfirst ? Ldcg4(pjm) : Ld4(pjm);
+    L.xjp = SC && jlast ? Ldcg4(pjp) : Ld4(pjp);
+    if (sl == 0 || q == 0) L.xl = __ldcg(x + row + (q == 0 ? 4 * nq - 1 : 4 * q - 1));
+    if (right) L.xr = __ldcg(x + row + (q == nq - 1 ? 0 : 4 * q + 4));
   }
 }
 
-// thread 0 of the CTA: waits (bounded, about 0.3 s) until the four
-// neighbouring tiles have published at least z; err[0] = 1 when a wait
-// gives up, after which no tile of the grid waits any more
-__device__ __forceinline__ void WaveWait(const volatile int* prog, const int* nb, int z,
-                                         int* err) {
-  const volatile int* verr = err;
-  for (int q = 0; q < 4; ++q) {
-    int64_t it = 0;
-    while (prog[nb[q]] < z && *verr == 0) {
-      if (++it > (int64_t(1) << 22)) {
-        atomicExch(err, 1);
-        break;
-      }
-      __nanosleep(64);
+// The update of one item (every lane of the warp calls it: shuffles).
+template <int ZI>
+__device__ __forceinline__ void WaveUpdate(const Op<float>& A, float* x, int color, int q,
+                                           int j, int k, bool act, const WaveLoads& L) {
+  const Dims d = A.d;
+  const int nq = d.nx >> 2, sl = threadIdx.x & 31;
+  float xl = __shfl_up_sync(0xffffffffu, L.xc.w, 1);
+  float xr = __shfl_down_sync(0xffffffffu, L.xc.x, 1);
+  float wr = __shfl_down_sync(0xffffffffu, L.w0v.x, 1);
+  if (!act) return;
+  if (sl == 0 || q == 0) xl = L.xl;
+  if (sl == 31 || q == nq - 1) {
+    xr = L.xr;
+    wr = L.wr;
+  }
+  const int64_t c = d.idx(4 * q, j, k);
+  float4 out = L.xc;
+  const int e0 = (color + j + k) & 1;
+#pragma unroll
+  for (int e = 0; e < 4; ++e) {
+    if ((e & 1) != e0) continue;
+    const float cxm = El(L.w0v, e);
+    const float cxp = e == 3 ? wr : El(L.w0v, e + 1);
+    const float cym = El(L.w1v, e), cyp = El(L.w1n, e);
+    const float czm = El(L.wz, e), czp = El(L.wzp, e);
+    const float dg = A.diag ? A.diag[c + e] : -(((((cxm + cxp) + cym) + cyp) + czm) + czp);
+    float acc = El(L.bv, e);
+    if (!ZI) {
+      const float vxm = e == 0 ? xl : El(L.xc, e - 1);
+      const float vxp = e == 3 ? xr : El(L.xc, e + 1);
+      acc -= cxm * vxm;
+      acc -= cxp * vxp;
+      acc -= cym * El(L.xjm, e);
+      acc -= cyp * El(L.xjp, e);
+      acc -= czm * El(L.xm, e);
+      acc -= czp * El(L.xp, e);
     }
+    SetEl(out, e, acc / dg);
+  }
+  St4(x + c, out);
+}
+
+// One colour on the planes [p0, p1) of the tile (rows j0 .. j0+rows-1):
+// item i = (plane p0 + i / rows, row j0 + i % rows); warp v takes the items
+// v, v + 16, v + 32, ... two at a time.
+template <int ZI, int SC>
+__device__ __forceinline__ void WavePhase(const Op<float>& A, const float* __restrict__ b,
+                                          float* x, int color, int p0, int p1, int q,
+                                          bool colok, int j0, int rows) {
+  const int wp = threadIdx.x >> 5;
+  const int n = (p1 - p0) * rows;
+  for (int i = wp; i < n; i += 2 * kWaveWarps) {
+    const int i2 = i + kWaveWarps;
+    const bool two = i2 < n;  // uniform over the warp
+    const int k1 = p0 + i / rows, j1 = j0 + i % rows;
+    const int k2 = two ? p0 + i2 / rows : k1, j2 = two ? j0 + i2 % rows : j1;
+    WaveLoads L1, L2;
+    const int jl = j0 + rows - 1;
+    WaveLoad<ZI, SC>(A, b, x, q, j1, k1, colok, j1 == j0, j1 == jl, L1);
+    WaveLoad<ZI, SC>(A, b, x, q, j2, k2, colok && two, j2 == j0, j2 == jl, L2);
+    WaveUpdate<ZI>(A, x, color, q, j1, k1, colok, L1);
+    if (two) WaveUpdate<ZI>(A, x, color, q, j2, k2, colok, L2);
+  }
+}
+
+// the tile's rows of x, b and the couplings on the planes [p0, p1) into L2:
+// the items of a phase, each lane its float4 of the five arrays
+__device__ __forceinline__ void WavePrefetch(const Op<float>& A, const float* b,
+                                             const float* x, int p0, int p1, int q, bool colok,
+                                             int j0, int rows) {
+  const Dims d = A.d;
+  const int wp = threadIdx.x >> 5;
+  const int n = (p1 - p0) * rows;
+  if (!colok) return;
+  for (int i = wp; i < n; i += kWaveWarps) {
+    const int64_t c = d.idx(4 * q, j0 + i % rows, p0 + i / rows);
+    PrefetchL2(x + c);
+    PrefetchL2(b + c);
+    PrefetchL2(A.w0 + c);
+    PrefetchL2(A.w1 + c);
+    PrefetchL2(A.w2 + c);
+  }
+}
+
+// one thread per neighbour: waits (bounded, at least 0.3 s) until the
+// neighbouring tile t has published at least `need` planes; err[0] = 1 when
+// a wait gives up, after which no tile of the grid waits any more
+__device__ __forceinline__ void WaveWait(const volatile int* prog, int t, int need, int* err) {
+  const volatile int* verr = err;
+  int64_t it = 0;
+  while (prog[t] < need && *verr == 0) {
+    if (++it > (int64_t(1) << 22)) {
+      atomicExch(err, 1);
+      break;
+    }
+    __nanosleep(64);
   }
   __threadfence();
 }
 
 // One full sweep (first colour c0; ZI: the first colour starts from zero).
 // Grid: one CTA of kWaveThreads per tile (xtiles * bands), cooperative;
-// prog: one counter per tile, -1 before the launch.
+// K: planes per chunk; prog: one counter per tile, -1 before the launch.
 template <int ZI>
 __global__ void __launch_bounds__(kWaveThreads, 1)
     KSweepWave(Op<float> A, const float* __restrict__ b, float* x, int c0,
-               const SolveScalars* s, WaveTiling T, int* prog, int* err) {
+               const SolveScalars* s, WaveTiling T, int K, int* prog, int* err) {
   if (s && s->done) return;
   const Dims d = A.d;
   const int tile = blockIdx.x;
   const int xt = tile % T.xtiles, band = tile / T.xtiles;
-  const int lane = threadIdx.x & 31, wp = threadIdx.x >> 5;
+  const int lane = threadIdx.x & 31;
   const int q = xt * (T.w >> 2) + lane;
+  const int i0 = xt * T.w;
+  const int wcols = min(T.w, d.nx - i0);
+  const bool colok = 4 * lane < wcols;
   const int j0 = band * T.rows;
   const int rows = min(T.rows, d.ny - j0);
-  const int j = j0 + min(wp, rows - 1);
-  const bool act = wp < rows && 4 * lane < min(T.w, d.nx - xt * T.w);
   __shared__ int nb[4];
   if (threadIdx.x == 0) {
     nb[0] = band * T.xtiles + (xt == 0 ? T.xtiles - 1 : xt - 1);
@@ -638,43 +701,43 @@ __global__ void __launch_bounds__(kWaveThreads, 1)
     nb[2] = (band == 0 ? T.bands - 1 : band - 1) * T.xtiles + xt;
     nb[3] = (band == T.bands - 1 ? 0 : band + 1) * T.xtiles + xt;
   }
-  WaveFront f0, f1;
-  WaveInit<ZI>(A, x, q, j, act, 0, f0);
   __syncthreads();
   const int c1 = 1 - c0;
-  const int last = d.nz - 1 + kWaveLag;
-  for (int st = 0; st <= last; ++st) {
-    if (st < d.nz) {
-      // plane st+2 into L2 for the first colour's next steps
-      if (act && st + 2 < d.nz) {
-        const int64_t cn = d.idx(4 * q, j, st + 2);
-        PrefetchL2(A.w0 + cn);
-        PrefetchL2(A.w1 + cn);
-        PrefetchL2(A.w2 + cn);
-        PrefetchL2(b + cn);
-        PrefetchL2(x + cn);
-      }
-      WavePlane<ZI>(A, b, x, c0, q, j, act, st, f0);
+  const int nch = (d.nz + K - 1) / K;
+  WavePrefetch(A, b, x, 0, min(K, d.nz), q, colok, j0, rows);
+  int blo = 1;
+  for (int st = 0; st <= nch; ++st) {
+    if (st < nch) {
+      const int p0 = st * K, p1 = min(d.nz, p0 + K);
+      if (st + 1 < nch) WavePrefetch(A, b, x, p1, min(d.nz, p1 + K), q, colok, j0, rows);
+      WavePhase<ZI, 0>(A, b, x, c0, p0, p1, q, colok, j0, rows);
       __syncthreads();
       if (threadIdx.x == 0) {
         __threadfence();
-        *(volatile int*)(prog + tile) = st;
+        *(volatile int*)(prog + tile) = p1;
       }
     }
-    const int z = st - kWaveLag;
-    if (z >= 1 && z <= d.nz - 1) {
-      if (threadIdx.x == 0) WaveWait(prog, nb, z, err);
+    // planes whose second colour can go: up to the end of chunk st-1 minus
+    // one (every plane after the last chunk)
+    const int done = st < nch ? min(d.nz, st * K) : d.nz;
+    const int bhi = st < nch ? done - 1 : d.nz;
+    if (bhi > blo) {
+      if (threadIdx.x < 4) WaveWait(prog, nb[threadIdx.x], done, err);
       __syncthreads();
-      if (z == 1) WaveInit<0>(A, x, q, j, act, 1, f1);
-      WavePlane<0>(A, b, x, c1, q, j, act, z, f1);
+      WavePhase<0, 1>(A, b, x, c1, blo, bhi, q, colok, j0, rows);
+      blo = bhi;
     }
   }
-  // the second colour of plane 0, after every first colour of the
-  // neighbours (it reads the first colour of plane nz-1)
-  if (threadIdx.x == 0) WaveWait(prog, nb, d.nz - 1, err);
+  // the second colour of plane 0 (every neighbour has published nz above)
   __syncthreads();
-  WaveInit<0>(A, x, q, j, act, 0, f1);
-  WavePlane<0>(A, b, x, c1, q, j, act, 0, f1);
+  WavePhase<0, 1>(A, b, x, c1, 0, 1, q, colok, j0, rows);
+}
+
+// The sweep's wait run once on a progress counter that nothing sets
+// (prog[0] = -1 before the launch): it gives up after its bound and sets
+// err[0], the path a sweep takes when a neighbouring tile never publishes.
+__global__ void KWaveWaitProbe(const int* prog, int* err) {
+  if (threadIdx.x == 0) WaveWait(prog, 0, 1, err);
 }
 
 }  // namespace aphgpu

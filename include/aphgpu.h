@@ -472,9 +472,10 @@ int aphgpu_batch_last_ms(const aphgpu_batch* batch, double* ms, int64_t* launche
  *                            every level with nx a multiple of 4, nx >= 8;
  *                            4 as 1 with bands of 6 rows (two CTAs per
  *                            SM instead of one); 5 the in-place wavefront
- *                            sweep (each CTA walks the planes of a tile,
- *                            the second colour two planes behind the
- *                            first, waiting for its neighbour tiles) on
+ *                            sweep (each CTA walks the planes of a tile
+ *                            in chunks, the second colour one chunk
+ *                            behind the first, waiting for its neighbour
+ *                            tiles; cooperative launch) on
  *                            levels of at least 2^21 cells with nx a
  *                            multiple of 4 and nz >= 4; 6 the wavefront
  *                            sweep on every such level; 0 (default) two
@@ -509,7 +510,11 @@ int aphgpu_batch_last_ms(const aphgpu_batch* batch, double* ms, int64_t* launche
  *                            shared memory (the batch's per-domain coarse
  *                            cycle); 0 (default): one launch per pass on
  *                            every level (as fast at 512^3: the one-CTA
- *                            passes are bound by the CTA's own issue rate) */
+ *                            passes are bound by the CTA's own issue rate)
+ *   APHGPU_OPT_WAVE_PLANES   planes per step of the wavefront sweep
+ *                            (APHGPU_OPT_FUSED_SWEEPS 5 and 6); 0 (default):
+ *                            as many as let three steps' worth of a level's
+ *                            x, b and couplings fit in 60 MB of L2 */
 enum {
   APHGPU_OPT_GRAPHS = 0,
   APHGPU_OPT_FUSED_SWEEPS = 1,
@@ -517,7 +522,8 @@ enum {
   APHGPU_OPT_CYCLE = 3,
   APHGPU_OPT_COARSE_SERIES = 4,
   APHGPU_OPT_SWEEP_GROWTH = 5,
-  APHGPU_OPT_CTA_COARSE = 6
+  APHGPU_OPT_CTA_COARSE = 6,
+  APHGPU_OPT_WAVE_PLANES = 7
 };
 int aphgpu_set_option(aphgpu_ctx* ctx, int option, int value);
 
@@ -550,6 +556,15 @@ enum {
  * leave it modified. */
 int aphgpu_time_kernel(aphgpu_ctx* ctx, int kernel, int reps, double* ms,
                        double* bytes);
+
+/* Failure path of the wavefront sweep (APHGPU_OPT_FUSED_SWEEPS 5 and 6),
+ * whose tiles wait on their neighbours' progress: runs its bounded wait
+ * once (one warp) on a progress counter that nothing sets.  The wait gives
+ * up after its bound (2^22 polls: one to a few seconds) and reports; the
+ * call returns
+ * APHGPU_ERR_TIMEOUT, as a solve does when a wait of its sweeps gave up,
+ * and the context stays usable (the flag is cleared once reported). */
+int aphgpu_wave_wait_check(aphgpu_ctx* ctx);
 
 /* ---- connected-component colours of the volume fraction ---- */
 

@@ -261,8 +261,10 @@ def test_fused_sweeps_bit_identical(solver, shape):
     by asynchronous copies (mode 2: on every level with nx % 4 == 0, nx >=
     16 and nz >= 8; mode 1: on such levels of at least 2^21 cells) and the
     synchronous kernel (mode 3) -- compute every value with the operations
-    of the two in-place half sweeps (mode 0): whole solves agree bit for bit
-    (with and without CUDA graphs)."""
+    of the two in-place half sweeps (mode 0), and so does the in-place
+    wavefront sweep (modes 5 and 6) with any number of planes per step
+    (whole chunks, a ragged last chunk, one chunk for the whole level):
+    whole solves agree bit for bit (with and without CUDA graphs)."""
     nx, ny, nz = shape
     h = 1.0 / nx
     c, r = workload.place_spheres(11, 3, 0.1, 0.2, gap=0.02)
@@ -286,6 +288,14 @@ def test_fused_sweeps_bit_identical(solver, shape):
             x, info = ctx.solve(conf)
             assert info.converged
             out[(fused, graphs)] = (x, info.iter, info.inner_iter)
+    for planes in (1, 3, 5, 64):
+        ctx.set_option(_lib.OPT_FUSED_SWEEPS, 6)
+        ctx.set_option(_lib.OPT_GRAPHS, 1)
+        ctx.set_option(_lib.OPT_WAVE_PLANES, planes)
+        x, info = ctx.solve(conf)
+        assert info.converged
+        out[("wave", planes)] = (x, info.iter, info.inner_iter)
+    ctx.set_option(_lib.OPT_WAVE_PLANES, 0)
     ref = out[(0, 0)]
     for key, val in out.items():
         assert np.array_equal(val[0], ref[0]), key
@@ -473,3 +483,30 @@ def test_cell_conditions():
         ctx.apply_cell_cond([3, 3], [1.0, 1.0])
     with pytest.raises(_lib.AphgpuError):
         ctx.apply_cell_cond([n ** 3], [1.0])
+
+
+def test_wavefront_wait_gives_up_and_reports():
+    """The wavefront sweep's bounded wait, run on a progress counter that
+    nothing sets, gives up and reports APHGPU_ERR_TIMEOUT (no fault, no
+    hang); the context stays usable, and a following wavefront solve (whose
+    waits all end) returns the half sweeps' result."""
+    import time
+    n = 32
+    c, r = workload.place_spheres(3, 2, 0.1, 0.2, gap=0.02)
+    case = workload.Case(n, c, r, rho1=1.0, rho2=1e-3, seed=4)
+    ctx = _lib.Context(n, case.h)
+    ctx.assemble_projection(case.alpha, case.rho1, case.rho2, case.flux, case.dt)
+    _, bn = ctx.residual_norms()
+    conf = _lib.default_conf(solver=_lib.SOLVER_MIXED, tol=1e-10 * bn / math.sqrt(case.h ** 3))
+    x0, _ = ctx.solve(conf)
+    t0 = time.perf_counter()
+    rc = ctx._L.aphgpu_wave_wait_check(ctx.handle)
+    waited = time.perf_counter() - t0
+    print("bounded wait gave up after %.2f s" % waited)
+    assert rc == _lib.ERR_TIMEOUT
+    assert waited < 30
+    ctx.set_option(_lib.OPT_FUSED_SWEEPS, 6)
+    x6, info = ctx.solve(conf)
+    assert info.converged
+    assert np.array_equal(x6, x0)
+    ctx.close()
