@@ -63,23 +63,33 @@ __device__ __forceinline__ void Sort3(double v[3]) {
   if (v[1] < v[0]) { t = v[0]; v[0] = v[1]; v[1] = t; }
 }
 
-// reconst.h:140-168
+// reconst.h:140-168.  Each branch forms its numerator and denominator and
+// the one division follows the branches, so the lanes of a warp in
+// different cases share it (each lane's operations are the reference's).
 __device__ double LineU0(const double n[3], double a) {
   const double nx = n[0], ny = n[1], nz = n[2];
   const double f = a + 0.5 * (nx + ny + nz);
   if (f <= 0) return 0;
-  if (nx >= f) return cube(f) / (6 * nx * ny * nz);
-  if (ny >= f) return (3 * sqr(f) - 3 * f * nx + sqr(nx)) / (6 * ny * nz);
-  if (nz >= f) {
+  double num, den;
+  if (nx >= f) {
+    num = cube(f);
+    den = 6 * nx * ny * nz;
+  } else if (ny >= f) {
+    num = 3 * sqr(f) - 3 * f * nx + sqr(nx);
+    den = 6 * ny * nz;
+  } else if (nz >= f) {
     if (nx + ny >= f) {
-      return (3 * sqr(f) - 3 * f * nx + sqr(nx) -
-              smin(1., (f - ny) / nx) * sqr(f - ny)) /
-             (6 * ny * nz);
+      num = 3 * sqr(f) - 3 * f * nx + sqr(nx) - smin(1., (f - ny) / nx) * sqr(f - ny);
+      den = 6 * ny * nz;
+    } else {
+      num = 2 * f - nx - ny;
+      den = 2 * nz;
     }
-    return (2 * f - nx - ny) / (2 * nz);
+  } else {
+    num = cube(f) - cube(f - nx) - cube(f - ny) - cube(f - nz);
+    den = 6 * nx * ny * nz;
   }
-  return (cube(f) - cube(f - nx) - cube(f - ny) - cube(f - nz)) /
-         (6 * nx * ny * nz);
+  return num / den;
 }
 
 // reconst.h:183-203, n already multiplied by h
@@ -97,32 +107,45 @@ __device__ __forceinline__ double LineU(const double n[3], double a, const doubl
   return LineU1(nh, a);
 }
 
-// reconst.h:218-250
+// reconst.h:218-250.  The branches pick the case and, for the three cubic
+// cases, the cubic's coefficients; SolveCubic then runs at one call site,
+// so the lanes of a warp in different cubic cases share one evaluation (the
+// operations of each lane are those of the reference's branch: a = 1 or 2
+// as a value gives the same products as the constant).
 __device__ double LineA0(const double n[3], double u) {
   const double nx = n[0], ny = n[1], nz = n[2];
-  double f;
+  double f = 0;
+  double ca = 1., cb = 0, cc = 0, cd = 0;
+  bool cubic = false;
   if (6. * ny * nz * u < sqr(nx)) {
     f = pow(6. * nx * ny * nz * u, 1. / 3.);
   } else if (6. * ny * nz * u < 3. * sqr(ny) - 3 * nx * ny + sqr(nx)) {
     f = 0.5 * nx + sqrt(2. * ny * nz * u - sqr(nx) / 12.);
   } else if (nz > nx + ny) {
     if (2. * nz * u < nx + ny) {
-      f = SolveCubic(1., -3. * (nx + ny), 3. * (sqr(nx) + sqr(ny)),
-                     -(cube(nx) + cube(ny)) + 6. * nx * ny * nz * u, 1);
+      cubic = true;
+      cb = -3. * (nx + ny);
+      cc = 3. * (sqr(nx) + sqr(ny));
+      cd = -(cube(nx) + cube(ny)) + 6. * nx * ny * nz * u;
     } else {
       f = nz * u + 0.5 * (nx + ny);
     }
   } else {
+    cubic = true;
     if (6. * nx * ny * nz * u < -cube(nz) + 3. * sqr(nz) * (nx + ny) -
                                     3. * nz * (sqr(nx) + sqr(ny)) + cube(nx) +
                                     cube(ny)) {
-      f = SolveCubic(1., -3. * (nx + ny), 3. * (sqr(nx) + sqr(ny)),
-                     -(cube(nx) + cube(ny)) + 6. * nx * ny * nz * u, 1);
+      cb = -3. * (nx + ny);
+      cc = 3. * (sqr(nx) + sqr(ny));
+      cd = -(cube(nx) + cube(ny)) + 6. * nx * ny * nz * u;
     } else {
-      f = SolveCubic(2., -3. * (nx + ny + nz), 3. * (sqr(nx) + sqr(ny) + sqr(nz)),
-                     -(cube(nx) + cube(ny) + cube(nz)) + 6. * nx * ny * nz * u, 1);
+      ca = 2.;
+      cb = -3. * (nx + ny + nz);
+      cc = 3. * (sqr(nx) + sqr(ny) + sqr(nz));
+      cd = -(cube(nx) + cube(ny) + cube(nz)) + 6. * nx * ny * nz * u;
     }
   }
+  if (cubic) f = SolveCubic(ca, cb, cc, cd, 1);
   return f - 0.5 * (nx + ny + nz);
 }
 
@@ -420,8 +443,13 @@ __global__ void KSweepFluxList(Dims d, int dir, double hx, double hy, double hz,
     const double nv[3] = {nrm[3 * c], nrm[3 * c + 1], nrm[3 * c + 2]};
     const double a = pa[c], uu = u[c];
     const double vl = vflux[c], vu = vflux[fp];
-    if (!(vl > 0)) ffvu[c] = InterfaceFlux(nv, a, uu, h, vl, dt, dir);
-    if (vu > 0) ffvu[fp] = InterfaceFlux(nv, a, uu, h, vu, dt, dir);
+    // the lower face where its flux is not positive, the upper face where
+    // its flux is positive; one call site for the first of them (most
+    // cells have one), a second only for the cells that have both
+    const bool lower = !(vl > 0), upper = vu > 0;
+    if (lower || upper)
+      ffvu[lower ? c : fp] = InterfaceFlux(nv, a, uu, h, lower ? vl : vu, dt, dir);
+    if (lower && upper) ffvu[fp] = InterfaceFlux(nv, a, uu, h, vu, dt, dir);
   }
 }
 
@@ -432,13 +460,17 @@ __global__ void KSweepFluxList(Dims d, int dir, double hx, double hy, double hz,
 // arithmetic makes them unnecessary, with bit-identical results: a zero
 // numerator gives a zero of the same sign; fcuu = 0 makes fcuu * ds a zero
 // with the sign of ds (finite); fcuu = 1 with equal numerators makes
-// ds - dl = +0.  That covers every cell away from the interface.
+// ds - dl = +0.  That covers every cell away from the interface.  Where
+// the cell volume is a power of two (ivol = 1 / vol, else 0), x * ivol is
+// the correctly rounded x / vol itself (both round the same exact value),
+// so the remaining divisions become multiplications.
 // UpdateCell: one cell (fc = fcuu, uc = u, face fluxes v0 v1 and fluid
 // fluxes f0 f1 of its lower and upper face); returns true for a bulk cell
 // (u unchanged, w not set), else the new value in w.
 __device__ __forceinline__ bool UpdateCell(int fc, double uc, double v0, double v1, double f0,
-                                           double f1, double vol, double big, double dt,
-                                           double clipth, int emax, int full_ok, double& w) {
+                                           double f1, double vol, double ivol, double big,
+                                           double dt, double clipth, int emax, int full_ok,
+                                           double& w) {
   const long long ub = Bits(uc);
   const long long a0 = Bits(v0), a1 = Bits(v1), b0 = Bits(f0), b1 = Bits(f1);
   // magnitudes below 2^(emax-1023): every difference times dt / vol below
@@ -454,14 +486,14 @@ __device__ __forceinline__ bool UpdateCell(int fc, double uc, double v0, double 
   if (bulk) return true;
   const double dsn = (v1 - v0) * dt;
   const double dln = (f1 - f0) * dt;
-  const double dl = dln == 0 ? dln : dln / vol;
+  const double dl = dln == 0 ? dln : ivol != 0 ? dln * ivol : dln / vol;
   double t;
   if (fc == 0 && fabs(dsn) <= big) {
     t = copysign(0.0, dsn) - dl;
   } else if (fc == 1 && fabs(dsn) <= big && Bits(dsn) == Bits(dln)) {
     t = 0.0;
   } else {
-    t = (double)fc * (dsn / vol) - dl;
+    t = (double)fc * (ivol != 0 ? dsn * ivol : dsn / vol) - dl;
   }
   w = uc;
   w += t;
@@ -473,6 +505,27 @@ __device__ __forceinline__ bool UpdateCell(int fc, double uc, double v0, double 
   return false;
 }
 
+// One cell of the fused pass: the fluid fluxes of its lower face (index c)
+// and upper face (index fp) from the face fluxes v0 v1 and the old values
+// um uc up (lower neighbour, cell, upper neighbour), then the update; returns
+// the new value in w and whether the cell is interfacial after it.
+__device__ __forceinline__ bool FusedCell(int64_t c, int64_t fp, double v0, double v1,
+                                          double um, double uc, double up, int fc,
+                                          const double* __restrict__ ffvu, double vol,
+                                          double ivol, double big, double dt, double clipth,
+                                          int emax, int full_ok, double& w) {
+  // upwind values of the lower face (c) and the upper face (fp)
+  const double u0 = PositiveBits(Bits(v0)) ? um : uc;
+  const double u1 = PositiveBits(Bits(v1)) ? uc : up;
+  const double f0 = InterfaceBits(Bits(u0)) ? ffvu[c] : BulkFlux(v0, u0);
+  const double f1 = InterfaceBits(Bits(u1)) ? ffvu[fp] : BulkFlux(v1, u1);
+  if (UpdateCell(fc, uc, v0, v1, f0, f1, vol, ivol, big, dt, clipth, emax, full_ok, w)) {
+    w = uc;
+    return false;
+  }
+  return InterfaceBits(Bits(w));
+}
+
 // Fluid fluxes and update of one direction of Vof::Sweep (vof.ipp:228-256,
 // 287-326) in one pass, out of place.  The flux of a face whose upwind cell
 // is not interfacial is v * u(upwind) of the old volume fraction uin
@@ -481,8 +534,13 @@ __device__ __forceinline__ bool UpdateCell(int fc, double uc, double v0, double 
 // KSweepFluxList.  Every cell of uout is written (bulk cells with their old
 // value); cells interfacial after the update are appended to the list.
 // Per cell: uin and vflux read once (the neighbours' values come from
-// cache), fcuu read, uout written.
-__global__ void KSweepFused(Dims d, int dir, double vol, const double* __restrict__ uin,
+// cache), fcuu read, uout written.  DIR is the sweep direction; a thread
+// walks the planes of a column with its lower and upper neighbours at fixed
+// offsets (periodic wrap at the ends of the column's row, column or plane
+// range), so a plane costs additions, not index products.
+template <int DIR>
+__global__ void __launch_bounds__(256, 5)
+    KSweepFused(Dims d, double vol, double ivol, const double* __restrict__ uin,
                             double* __restrict__ uout, const double* __restrict__ vflux,
                             const double* __restrict__ ffvu,
                             const uint8_t* __restrict__ fcuu, double dt, double clipth,
@@ -493,54 +551,56 @@ __global__ void KSweepFused(Dims d, int dir, double vol, const double* __restric
   const int ke = min(kb + kTileZ, d.nz);
   const bool in = i < d.nx && j < d.ny;
   const double big = vol * 1e300;
+  const int64_t nxy = (int64_t)d.nx * d.ny;
+  // offsets of the lower (dm) and upper (dp) neighbour; for DIR 2 they
+  // change at the first and last plane only
+  int64_t dm, dp;
+  if (DIR == 0) {
+    dm = i == 0 ? d.nx - 1 : -1;
+    dp = i == d.nx - 1 ? -(int64_t)(d.nx - 1) : 1;
+  } else if (DIR == 1) {
+    dm = j == 0 ? (int64_t)(d.ny - 1) * d.nx : -(int64_t)d.nx;
+    dp = j == d.ny - 1 ? -(int64_t)(d.ny - 1) * d.nx : (int64_t)d.nx;
+  } else {
+    dm = -nxy;
+    dp = nxy;
+  }
+  auto offm = [&](int k) -> int64_t {
+    return DIR == 2 && k == 0 ? (int64_t)(d.nz - 1) * nxy : dm;
+  };
+  auto offp = [&](int k) -> int64_t {
+    return DIR == 2 && k == d.nz - 1 ? -(int64_t)(d.nz - 1) * nxy : dp;
+  };
   // the loads of plane k+1 are issued before plane k is computed: two
   // planes of loads in flight per thread
   struct Plane {
     double v0, v1, um, uc, up;
     int fc;
   };
-  auto load = [&](int k, Plane& q) {
-    const int64_t c = d.idx(i, j, k);
-    const int64_t cm = dir == 0 ? d.idx(wrapm(i - 1, d.nx), j, k)
-                     : dir == 1 ? d.idx(i, wrapm(j - 1, d.ny), k)
-                                : d.idx(i, j, wrapm(k - 1, d.nz));
-    const int64_t fp = dir == 0 ? d.idx(wrapp(i + 1, d.nx), j, k)
-                     : dir == 1 ? d.idx(i, wrapp(j + 1, d.ny), k)
-                                : d.idx(i, j, wrapp(k + 1, d.nz));
+  auto load = [&](int64_t c, int k, Plane& q) {
+    const int64_t fp = c + offp(k);
     q.v0 = vflux[c];
     q.v1 = vflux[fp];
-    q.um = uin[cm];
+    q.um = uin[c + offm(k)];
     q.uc = uin[c];
     q.up = uin[fp];
     q.fc = fcuu[c];
   };
+  int64_t c = in ? d.idx(i, j, kb) : 0;
   Plane cur{}, nxt{};
-  if (in && kb < ke) load(kb, cur);
+  if (in && kb < ke) load(c, kb, cur);
   for (int k = kb; k < ke; ++k) {
-    if (in && k + 1 < ke) load(k + 1, nxt);
-    int64_t c = 0;
+    if (in && k + 1 < ke) load(c + nxy, k + 1, nxt);
     bool want = false;
     if (in) {
-      c = d.idx(i, j, k);
-      const int64_t fp = dir == 0 ? d.idx(wrapp(i + 1, d.nx), j, k)
-                       : dir == 1 ? d.idx(i, wrapp(j + 1, d.ny), k)
-                                  : d.idx(i, j, wrapp(k + 1, d.nz));
-      // upwind values of the lower face (c) and the upper face (fp)
-      const double u0 = PositiveBits(Bits(cur.v0)) ? cur.um : cur.uc;
-      const double u1 = PositiveBits(Bits(cur.v1)) ? cur.uc : cur.up;
-      const double f0 = InterfaceBits(Bits(u0)) ? ffvu[c] : BulkFlux(cur.v0, u0);
-      const double f1 = InterfaceBits(Bits(u1)) ? ffvu[fp] : BulkFlux(cur.v1, u1);
       double w;
-      if (UpdateCell(cur.fc, cur.uc, cur.v0, cur.v1, f0, f1, vol, big, dt, clipth, emax,
-                     full_ok, w)) {
-        w = cur.uc;
-      } else {
-        want = InterfaceBits(Bits(w));
-      }
+      want = FusedCell(c, c + offp(k), cur.v0, cur.v1, cur.um, cur.uc, cur.up, cur.fc, ffvu,
+                       vol, ivol, big, dt, clipth, emax, full_ok, w);
       uout[c] = w;
     }
     ListAppend(want, (int)c, list, count);
     cur = nxt;
+    c += nxy;
   }
 }
 
@@ -822,8 +882,15 @@ int SweepUpdate(aphgpu_ctx* ctx, const VofScratch& sc, int dir, const double* vf
     if (adt > 1) e = std::min(e, std::floor(2021.0 - std::log2(adt)));
     emax = (int)std::max(0.0, e);
   }
-  KSweepFused<<<TileGrid(ctx->d), TileBlock(), 0, ctx->stream>>>(
-      ctx->d, dir, vol, ctx->u, ctx->u_alt, vf, ctx->ffvu, sc.fcuu, dt, ctx->clipth, emax,
+  // 1 / vol where vol is a power of two (and so is its reciprocal), else 0
+  int ve = 0;
+  const double vm = std::frexp(vol, &ve);
+  const double ivol = (vm == 0.5 && std::isnormal(vol) && std::isnormal(std::ldexp(1.0, 1 - ve)))
+                          ? std::ldexp(1.0, 1 - ve)
+                          : 0.0;
+  auto kern = dir == 0 ? KSweepFused<0> : dir == 1 ? KSweepFused<1> : KSweepFused<2>;
+  kern<<<TileGrid(ctx->d), TileBlock(), 0, ctx->stream>>>(
+      ctx->d, vol, ivol, ctx->u, ctx->u_alt, vf, ctx->ffvu, sc.fcuu, dt, ctx->clipth, emax,
       ctx->clipth <= 1 ? 1 : 0, sc.list, sc.count);
   APH_LAUNCHED(ctx);
   if (swap) std::swap(ctx->u, ctx->u_alt);
