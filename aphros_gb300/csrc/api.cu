@@ -251,7 +251,7 @@ int EnsureVof(aphgpu_ctx* ctx) {
     return SetError(ctx, APHGPU_ERR_UNSUPPORTED, "VOF needs fewer than 2^31 cells");
   APH_TRY(Alloc(ctx, &ctx->u, N));
   APH_TRY(Alloc(ctx, &ctx->u_alt, N));
-  APH_TRY(Alloc(ctx, &ctx->u0, N));
+  APH_TRY(Alloc(ctx, &ctx->u0, N + 8));  // the VOF scratch (two fcuu slots, the list)
   APH_TRY(Alloc(ctx, &ctx->nrm, 3 * N));
   APH_TRY(Alloc(ctx, &ctx->pa, N));
   APH_TRY(Alloc(ctx, &ctx->ffvu, N));

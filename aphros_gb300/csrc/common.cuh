@@ -352,6 +352,8 @@ struct aphgpu_ctx {
   bool has_vof_src = false;
   double clipth = 1e-10;
   int vof_count = 0;
+  int fcuu_sel = 0;         // which of the two fcuu slots of the VOF scratch is current
+  bool fcuu_ready = false;  // the current slot holds fcuu of u (left by the last step)
   double vof_dt = 0;  // time step of the last VOF step (kernel timing)
   bool vof_ready = false;
 

@@ -534,7 +534,8 @@ __device__ __forceinline__ bool FusedCell(int64_t c, int64_t fp, double v0, doub
 // KSweepFluxList.  Every cell of uout is written (bulk cells with their old
 // value); cells interfacial after the update are appended to the list.
 // Per cell: uin and vflux read once (the neighbours' values come from
-// cache), fcuu read, uout written.  DIR is the sweep direction; a thread
+// cache), fcuu read, uout written (and, on the step's last sweep, the next
+// step's fcuu byte).  DIR is the sweep direction; a thread
 // walks the planes of a column with its lower and upper neighbours at fixed
 // offsets (periodic wrap at the ends of the column's row, column or plane
 // range), so a plane costs additions, not index products.
@@ -544,7 +545,8 @@ __global__ void __launch_bounds__(256, 5)
                             double* __restrict__ uout, const double* __restrict__ vflux,
                             const double* __restrict__ ffvu,
                             const uint8_t* __restrict__ fcuu, double dt, double clipth,
-                            int emax, int full_ok, int* list, int* count) {
+                            int emax, int full_ok, int* list, int* count,
+                            uint8_t* __restrict__ fcuu_out) {
   const int i = blockIdx.x * kTileX + threadIdx.x;
   const int j = blockIdx.y * kTileY + threadIdx.y;
   const int kb = blockIdx.z * kTileZ;
@@ -597,6 +599,12 @@ __global__ void __launch_bounds__(256, 5)
       want = FusedCell(c, c + offp(k), cur.v0, cur.v1, cur.um, cur.uc, cur.up, cur.fc, ffvu,
                        vol, ivol, big, dt, clipth, emax, full_ok, w);
       uout[c] = w;
+      if (fcuu_out) {
+        // the next step's fcuu = u < 0.5 ? 0 : 1 of the new value, as
+        // KListInterface sets it
+        const long long wb = Bits(w);
+        fcuu_out[c] = (!NanBits(wb) && wb < kHalfBits) ? 0 : 1;
+      }
     }
     ListAppend(want, (int)c, list, count);
     cur = nxt;
@@ -808,19 +816,28 @@ __global__ void KSurfaceTension(Dims d, double h, double sigma,
 
 namespace {
 
-// Scratch of a VOF step inside the context's u0 array (8 bytes per cell):
-// fcuu (1 byte per cell), then the interface list (4 bytes per cell, room
-// for every cell) and its length.
+// Scratch of a VOF step inside the context's u0 array: fcuu (1 byte per
+// cell) in two slots, the interface list (4 bytes per cell, room for every
+// cell) and its length.
 struct VofScratch {
-  uint8_t* fcuu;
+  uint8_t* fcuu;       // fcuu of the current volume fraction
+  uint8_t* fcuu_next;  // fcuu of the next step's, written by its last sweep
   int* list;
   int* count;
 };
 
+// Two fcuu slots (ctx->fcuu_sel picks the current one), the list and its
+// count, in the u0 array of N + 8 doubles: 16-byte aligned pieces of N, 4 N,
+// 16 and N bytes.
 VofScratch Scratch(aphgpu_ctx* ctx) {
   char* base = (char*)ctx->u0;
-  const size_t off = ((size_t)ctx->N + 15) & ~(size_t)15;
-  return VofScratch{(uint8_t*)base, (int*)(base + off), (int*)(base + off + 4 * ctx->N)};
+  const size_t n = (size_t)ctx->N;
+  const size_t off = (n + 15) & ~(size_t)15;
+  uint8_t* a = (uint8_t*)base;
+  uint8_t* b = (uint8_t*)(base + off + 4 * n + 16);
+  uint8_t* cur = ctx->fcuu_sel ? b : a;
+  uint8_t* nxt = ctx->fcuu_sel ? a : b;
+  return VofScratch{cur, nxt, (int*)(base + off), (int*)(base + off + 4 * n)};
 }
 
 // grid of the list kernels: 4 CTAs of 256 threads per SM, looping over the
@@ -866,7 +883,7 @@ int SweepFluxList(aphgpu_ctx* ctx, const VofScratch& sc, int dir, const double* 
 // the fused flux + update of direction dir from ctx->u into ctx->u_alt,
 // then (swap) the two buffers exchanged: ctx->u is the new volume fraction
 int SweepUpdate(aphgpu_ctx* ctx, const VofScratch& sc, int dir, const double* vf, double dt,
-                bool swap) {
+                bool swap, uint8_t* fcuu_out = nullptr) {
   const double h = ctx->h;
   APH_CUDA(ctx, cudaMemsetAsync(sc.count, 0, sizeof(int), ctx->stream));
   const double vol = (h * h) * h;
@@ -891,7 +908,7 @@ int SweepUpdate(aphgpu_ctx* ctx, const VofScratch& sc, int dir, const double* vf
   auto kern = dir == 0 ? KSweepFused<0> : dir == 1 ? KSweepFused<1> : KSweepFused<2>;
   kern<<<TileGrid(ctx->d), TileBlock(), 0, ctx->stream>>>(
       ctx->d, vol, ivol, ctx->u, ctx->u_alt, vf, ctx->ffvu, sc.fcuu, dt, ctx->clipth, emax,
-      ctx->clipth <= 1 ? 1 : 0, sc.list, sc.count);
+      ctx->clipth <= 1 ? 1 : 0, sc.list, sc.count, fcuu_out);
   APH_LAUNCHED(ctx);
   if (swap) std::swap(ctx->u, ctx->u_alt);
   return APHGPU_OK;
@@ -901,6 +918,7 @@ int SweepUpdate(aphgpu_ctx* ctx, const VofScratch& sc, int dir, const double* vf
 
 int VofReconstruct(aphgpu_ctx* ctx) {
   const VofScratch sc = Scratch(ctx);
+  ctx->fcuu_ready = false;  // u was set from outside the steps
   APH_TRY(ListInterface(ctx, sc, false));
   ctx->vof_list_valid = true;
   return ReconstructListed(ctx, sc);
@@ -909,15 +927,20 @@ int VofReconstruct(aphgpu_ctx* ctx) {
 int VofStepDevice(aphgpu_ctx* ctx, const double* d_vflux, double dt) {
   const int64_t N = ctx->N;
   const VofScratch sc = Scratch(ctx);
-  ctx->vof_list_valid = false;
   if (ctx->has_vof_src) {
+    ctx->vof_list_valid = false;
     APH_CUDA(ctx, cudaMemsetAsync(sc.count, 0, sizeof(int), ctx->stream));
     KSourceList<<<TileGrid(ctx->d), TileBlock(), 0, ctx->stream>>>(
         ctx->d, dt, ctx->vof_src, ctx->u, sc.fcuu, ctx->nrm, sc.list, sc.count);
     APH_LAUNCHED(ctx);
-  } else {
+  } else if (!(ctx->fcuu_ready && ctx->vof_list_valid)) {
+    // else the previous step's last sweep left both the list of the
+    // interfacial cells and fcuu of the current volume fraction
+    ctx->vof_list_valid = false;
     APH_TRY(ListInterface(ctx, sc, true));
   }
+  ctx->vof_list_valid = false;
+  ctx->fcuu_ready = false;
   int dd[3];
   const int cnt = ctx->vof_count % 3;  // vof.ipp:428-435
   if (cnt == 0) { dd[0] = 0; dd[1] = 1; dd[2] = 2; }
@@ -927,13 +950,16 @@ int VofStepDevice(aphgpu_ctx* ctx, const double* d_vflux, double dt) {
     const int dir = dd[id];
     const double* vf = d_vflux + (int64_t)dir * N;
     APH_TRY(SweepFluxList(ctx, sc, dir, vf, dt));
-    APH_TRY(SweepUpdate(ctx, sc, dir, vf, dt, true));
+    APH_TRY(SweepUpdate(ctx, sc, dir, vf, dt, true, id == 2 ? sc.fcuu_next : nullptr));
     APH_TRY(ReconstructListed(ctx, sc));
   }
   ctx->vof_count += 1;
   ctx->vof_dt = dt;
-  // the last update listed the interfacial cells of the new u
+  // the last update listed the interfacial cells of the new u and wrote its
+  // fcuu into the other slot
   ctx->vof_list_valid = true;
+  ctx->fcuu_sel ^= 1;
+  ctx->fcuu_ready = true;
   return APHGPU_OK;
 }
 
@@ -995,6 +1021,7 @@ int TimeVofKernel(aphgpu_ctx* ctx, int kernel, int reps, double* ms, double* byt
   // timed update leaves the list of its scratch output)
   APH_TRY(ListInterface(ctx, sc, true));
   ctx->vof_list_valid = kernel != APHGPU_K_VOF_UPDATE;
+  ctx->fcuu_ready = false;
   int nif = 0;
   APH_CUDA(ctx, cudaMemcpyAsync(&nif, sc.count, sizeof(int), cudaMemcpyDeviceToHost, st));
   APH_CUDA(ctx, cudaStreamSynchronize(st));
