@@ -98,8 +98,10 @@ __device__ double LineU1(const double n0[3], double a) {
   Sort3(n);
   const double s = ((0 + n[0]) + n[1]) + n[2];
   a = smax(-0.5 * s, smin(0.5 * s, a));
-  if (a < 0) return LineU0(n, a);
-  return 1 - LineU0(n, -a);
+  // one call site for both signs (the lanes of a warp share it)
+  const bool neg = a < 0;
+  const double r = LineU0(n, neg ? a : -a);
+  return neg ? r : 1 - r;
 }
 
 __device__ __forceinline__ double LineU(const double n[3], double a, const double h[3]) {
@@ -154,8 +156,10 @@ __device__ double LineA(const double n0[3], double u, const double h[3]) {
   double n[3] = {fabs(n0[0] * h[0]), fabs(n0[1] * h[1]), fabs(n0[2] * h[2])};
   Sort3(n);
   u = smax(0., smin(1., u));
-  if (u <= 0.5) return LineA0(n, u);
-  return -LineA0(n, 1 - u);
+  // one call site for both halves (the lanes of a warp share it)
+  const bool lo = u <= 0.5;
+  const double r = LineA0(n, lo ? u : 1 - u);
+  return lo ? r : -r;
 }
 
 // reconst.h:290-324 and 371-379

@@ -325,15 +325,16 @@ def cpu_baseline(case, case_name, threads, budget_s=15.0, expr8_np=None):
 VOF_STEP_BYTES = 315
 CURVATURE_BYTES = 200
 # the device path touches normals, plane constants, fluid fluxes and
-# heights of interfacial cells only: its compulsory traffic per step is the
-# interface listing (u read, fcuu written: 9 B/cell), three fused
-# directional passes (u read and written, face flux, fcuu: 25 B/cell each)
-# and, per interfacial cell, about 112 B per direction (flux through its
+# heights of interfacial cells only: its compulsory traffic per step is
+# three fused directional passes (u read and written, face flux, fcuu:
+# 25 B/cell each; the last one also writes the next step's fcuu, 1 B/cell,
+# so a step that follows a step needs no interface listing) and, per
+# interfacial cell, about 112 B per direction (flux through its
 # faces: normal, plane constant, u, two face fluxes and fluid fluxes;
 # re-reconstruction: u, normal and plane constant written); the curvature
 # writes kappa for every cell (8 B/cell) and reads/writes about 88 B per
 # interfacial cell (u, normal, three heights written and read, kappa)
-VOF_DEVICE_BYTES_CELL = 9 + 3 * 25
+VOF_DEVICE_BYTES_CELL = 3 * 25 + 1
 VOF_DEVICE_BYTES_IF = 3 * 112
 CURV_DEVICE_BYTES_CELL = 8
 CURV_DEVICE_BYTES_IF = 88
