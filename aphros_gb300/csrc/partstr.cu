@@ -471,26 +471,36 @@ __global__ void KPartStrings(PartArgs A, const double* __restrict__ u,
     PlaneBasis(xc, nc, pa[c], an, h, B);
     double uz[3];
     Cross3(B.ux, B.uy, uz);
+    // the interfacial cells of the 5x5x5 stencil in stencil order (dz, dy,
+    // dx), listed first so that the polygon cuts below run once per listed
+    // cell of each lane, not once per stencil cell some lane of the warp
+    // needs
+    unsigned char cand[kPsMaxSeg];
+    int ncand = 0;
+    for (int q = 0; q < 125; ++q) {
+      const int dx = q % 5 - 2, dy = (q / 5) % 5 - 2, dz = q / 25 - 2;
+      const int64_t cn = d.idx(Wrap(i + dx, d.nx), Wrap(j + dy, d.ny), Wrap(k + dz, d.nz));
+      if (Interfacial(u[cn])) cand[ncand++] = (unsigned char)q;
+    }
     Seg sg[kPsMaxSeg];
     int nseg = 0;
-    for (int dz = -2; dz <= 2; ++dz)
-      for (int dy = -2; dy <= 2; ++dy)
-        for (int dx = -2; dx <= 2; ++dx) {
-          const int64_t cn = d.idx(Wrap(i + dx, d.nx), Wrap(j + dy, d.ny), Wrap(k + dz, d.nz));
-          if (!Interfacial(u[cn])) continue;
-          const double xn[3] = {(0. + half) + (double)(i + dx) * h,
-                                (0. + half) + (double)(j + dy) * h,
-                                (0. + half) + (double)(k + dz) * h};
-          const double nn[3] = {nrm[3 * cn], nrm[3 * cn + 1], nrm[3 * cn + 2]};
-          V2 e[2];
-          if (AppendInterface(B, uz, xn, pa[cn], nn, h, e)) {
-            Seg& g = sg[nseg++];
-            g.x0 = e[0];
-            g.x1 = e[1];
-            g.l = Sub(e[1], e[0]);
-            g.ll = Dot(g.l, g.l);
-          }
-        }
+    for (int m = 0; m < ncand; ++m) {
+      const int q = cand[m];
+      const int dx = q % 5 - 2, dy = (q / 5) % 5 - 2, dz = q / 25 - 2;
+      const int64_t cn = d.idx(Wrap(i + dx, d.nx), Wrap(j + dy, d.ny), Wrap(k + dz, d.nz));
+      const double xn[3] = {(0. + half) + (double)(i + dx) * h,
+                            (0. + half) + (double)(j + dy) * h,
+                            (0. + half) + (double)(k + dz) * h};
+      const double nn[3] = {nrm[3 * cn], nrm[3 * cn + 1], nrm[3 * cn + 2]};
+      V2 e[2];
+      if (AppendInterface(B, uz, xn, pa[cn], nn, h, e)) {
+        Seg& g = sg[nseg++];
+        g.x0 = e[0];
+        g.x1 = e[1];
+        g.l = Sub(e[1], e[0]);
+        g.ll = Dot(g.l, g.l);
+      }
+    }
     // seed (PartStr::Add, partstr.h:82-92: centre 0, tangent (1, 0)) and
     // iterate (Run0 with Iter, partstr.h:110-157)
     V2 xx[kPsMaxNp], ff[kPsMaxNp];
