@@ -362,14 +362,15 @@ struct aphgpu_ctx {
   // connected-component colours of the volume fraction (label.cu; -1 none)
   double* cl = nullptr;
   struct {
-    int* par = nullptr;     // union-find parent, then root (-1: not gas)
+    int* par = nullptr;     // union-find parent, then root (gas cells only)
+    int* gas = nullptr;     // the gas cells (u > 0.5), listed
     int* slot = nullptr;    // component slot of each root
     int* croot = nullptr;   // root of each slot
     unsigned long long* first = nullptr;  // first halo-order position per slot
     double* stable = nullptr;  // previous colour at that position
     double* color = nullptr;   // new colour per slot
     double* pre = nullptr;     // colours before the propagation pass
-    int* ctl = nullptr;        // component count, error flag
+    int* ctl = nullptr;        // component count, error flag, gas cell count
     unsigned char* flag = nullptr;  // lines the propagation pass visits
   } lab;
   // host staging (pinned)

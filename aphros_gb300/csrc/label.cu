@@ -3,8 +3,9 @@
 // Vof::MakeIteration (src/solver/vof.ipp:546-578) with
 // UVof::Imp::RecolorUnionFind (src/util/vof.ipp:982-1150), same results.
 //
-//   components  gas cells (u > 0.5), 26-connected across the periodic
-//               boundaries, by a lock-free union-find: a root is only ever
+//   components  gas cells (u > 0.5), listed by one pass over the field and
+//               then walked from the list alone, 26-connected across the
+//               periodic boundaries, by a lock-free union-find: a root is only ever
 //               hooked under a smaller root (atomicCAS), so each
 //               component's root is its first cell in x-fastest order, the
 //               cell whose unique initial colour the reference keeps;
@@ -56,27 +57,52 @@ __device__ __forceinline__ int Find(volatile int* par, int x, int64_t cap) {
   return x;
 }
 
-__global__ void KLabelInit(int64_t n, const double* __restrict__ u, int* par) {
-  for (int64_t c = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; c < n;
-       c += (int64_t)gridDim.x * blockDim.x)
-    par[c] = u[c] > 0.5 ? (int)c : -1;
+__device__ __forceinline__ bool Gas(double u) { return u > 0.5; }
+
+// warp-aggregated append of c to the list when `want` (every lane of the
+// warp calls it)
+__device__ __forceinline__ void Append(bool want, int c, int* list, int* count) {
+  const unsigned m = __ballot_sync(0xffffffffu, want);
+  if (!m) return;
+  const int lane = threadIdx.x & 31;
+  const int leader = __ffs(m) - 1;
+  int base = 0;
+  if (lane == leader) base = atomicAdd(count, __popc(m));
+  base = __shfl_sync(0xffffffffu, base, leader);
+  if (want) list[base + __popc(m & ((1u << lane) - 1u))] = c;
 }
 
-// Union of every gas cell with its gas neighbours in the 13 offsets of one
-// half of the 3x3x3 stencil (the other half is the same pairs reversed).
-__global__ void KLabelUnion(Dims d, int* par, int* err) {
+// the gas cells: par[c] = c and c listed (par of the other cells is never
+// read: gas is tested on u).  The loop bound is uniform over each warp.
+__global__ void KLabelInit(int64_t n, const double* __restrict__ u, int* par, int* list,
+                           int* count) {
+  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  for (int64_t c0 = blockIdx.x * (int64_t)blockDim.x + (threadIdx.x & ~31); c0 < n;
+       c0 += stride) {
+    const int64_t c = c0 + (threadIdx.x & 31);
+    const bool g = c < n && Gas(u[c]);
+    if (g) par[c] = (int)c;
+    Append(g, (int)c, list, count);
+  }
+}
+
+// Union of every listed gas cell with its gas neighbours in the 13 offsets
+// of one half of the 3x3x3 stencil (the other half is the same pairs
+// reversed).
+__global__ void KLabelUnion(Dims d, const double* __restrict__ u, int* par,
+                            const int* __restrict__ gas, const int* gcount, int* err) {
   const int64_t n = d.cells();
+  const int ng = *gcount;
   volatile int* vp = par;
-  for (int64_t c = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; c < n;
-       c += (int64_t)gridDim.x * blockDim.x) {
-    if (vp[c] < 0) continue;
+  for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < ng; t += gridDim.x * blockDim.x) {
+    const int64_t c = gas[t];
     const int i = (int)(c % d.nx), j = (int)((c / d.nx) % d.ny), k = (int)(c / ((int64_t)d.nx * d.ny));
     for (int o = 0; o < 13; ++o) {
       // offsets with dz > 0, or dz == 0 and dy > 0, or dz == dy == 0, dx > 0
       const int q = o + 14;  // 14..26 in the 27-point numbering
       const int dx = q % 3 - 1, dy = (q / 3) % 3 - 1, dz = q / 9 - 1;
       const int64_t cn = d.idx(Wrap(i + dx, d.nx), Wrap(j + dy, d.ny), Wrap(k + dz, d.nz));
-      if (cn == c || vp[cn] < 0) continue;
+      if (cn == c || !Gas(u[cn])) continue;
       int a = (int)c, b = (int)cn;
       bool done = false;
       for (int it = 0; it < (1 << 20) && !done; ++it) {
@@ -86,9 +112,9 @@ __global__ void KLabelUnion(Dims d, int* par, int* err) {
           done = true;
         } else {
           if (a < b) {
-            const int t = a;
+            const int t2 = a;
             a = b;
-            b = t;
+            b = t2;
           }
           // hook the larger root under the smaller, if still a root
           if (atomicCAS(&par[a], a, b) == a) done = true;
@@ -99,19 +125,20 @@ __global__ void KLabelUnion(Dims d, int* par, int* err) {
   }
 }
 
-// Roots of all gas cells; each root gets a component slot.
-__global__ void KLabelFlatten(int64_t n, int* par, int* slot, int* ncomp, int* croot, int cap,
+// Roots of the listed gas cells; each root gets a component slot.
+__global__ void KLabelFlatten(int64_t n, int* par, const int* __restrict__ gas,
+                              const int* gcount, int* slot, int* ncomp, int* croot, int cap,
                               int* err) {
   volatile int* vp = par;
-  for (int64_t c = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; c < n;
-       c += (int64_t)gridDim.x * blockDim.x) {
-    if (vp[c] < 0) continue;
-    const int r = Find(vp, (int)c, n);
-    if (r == (int)c) {
+  const int ng = *gcount;
+  for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < ng; t += gridDim.x * blockDim.x) {
+    const int c = gas[t];
+    const int r = Find(vp, c, n);
+    if (r == c) {
       const int s = atomicAdd(ncomp, 1);
       if (s < cap) {
         slot[c] = s;
-        croot[s] = (int)c;
+        croot[s] = c;
       } else {
         atomicExch(err, 2);
       }
@@ -119,12 +146,12 @@ __global__ void KLabelFlatten(int64_t n, int* par, int* slot, int* ncomp, int* c
   }
 }
 
-__global__ void KLabelRoot(int64_t n, int* par) {
+__global__ void KLabelRoot(int64_t n, int* par, const int* __restrict__ gas, const int* gcount) {
   volatile int* vp = par;
-  for (int64_t c = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; c < n;
-       c += (int64_t)gridDim.x * blockDim.x) {
-    if (vp[c] < 0) continue;
-    par[c] = Find(vp, (int)c, n);
+  const int ng = *gcount;
+  for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < ng; t += gridDim.x * blockDim.x) {
+    const int c = gas[t];
+    par[c] = Find(vp, c, n);
   }
 }
 
@@ -133,19 +160,52 @@ __global__ void KLabelRoot(int64_t n, int* par) {
 // has a previous colour.  A cell's smallest position takes its left halo
 // copy where it has one (the last two cells of an axis).
 __global__ void KLabelFirst(Dims d, const int* __restrict__ root, const int* __restrict__ slot,
+                            const int* __restrict__ gas, const int* gcount,
                             const double* __restrict__ clprev, unsigned long long* first) {
-  const int64_t n = d.cells();
   const unsigned long long ex = d.nx + 4, ey = d.ny + 4;
-  for (int64_t c = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; c < n;
-       c += (int64_t)gridDim.x * blockDim.x) {
-    const int r = root[c];
-    if (r < 0 || clprev[c] == -1.0) continue;
-    const int i = (int)(c % d.nx), j = (int)((c / d.nx) % d.ny), k = (int)(c / ((int64_t)d.nx * d.ny));
-    const int xi = i >= d.nx - 2 ? i - d.nx + 2 : i + 2;
-    const int yj = j >= d.ny - 2 ? j - d.ny + 2 : j + 2;
-    const int zk = k >= d.nz - 2 ? k - d.nz + 2 : k + 2;
-    const unsigned long long e = ((unsigned long long)zk * ey + yj) * ex + xi;
-    atomicMin(&first[slot[r]], e);
+  const int ng = *gcount;
+  const int lane = threadIdx.x & 31;
+  const int stride = gridDim.x * blockDim.x;
+  // the loop bound is uniform over each warp; the listed cells of a warp
+  // are consecutive gas cells, mostly of one component: their minimum is
+  // formed in the warp and written by one atomic
+  for (int t0 = blockIdx.x * blockDim.x + (threadIdx.x & ~31); t0 < ng; t0 += stride) {
+    const int t = t0 + lane;
+    unsigned long long e = kNoFirst;
+    int s = -1;
+    if (t < ng) {
+      const int64_t c = gas[t];
+      if (clprev[c] != -1.0) {
+        const int i = (int)(c % d.nx), j = (int)((c / d.nx) % d.ny),
+                  k = (int)(c / ((int64_t)d.nx * d.ny));
+        const int xi = i >= d.nx - 2 ? i - d.nx + 2 : i + 2;
+        const int yj = j >= d.ny - 2 ? j - d.ny + 2 : j + 2;
+        const int zk = k >= d.nz - 2 ? k - d.nz + 2 : k + 2;
+        e = ((unsigned long long)zk * ey + yj) * ex + xi;
+        s = slot[root[c]];
+      }
+    }
+    const unsigned want = __ballot_sync(0xffffffffu, s >= 0);
+    if (!want) continue;
+    // lanes without a candidate take the first candidate's slot and a
+    // neutral position, so that one component in the warp matches all
+    const int s0 = __shfl_sync(0xffffffffu, s, __ffs(want) - 1);
+    const int sv = s >= 0 ? s : s0;
+    int all = 0;
+    __match_all_sync(0xffffffffu, sv, &all);
+    // the stored minimum only decreases: an atomic that could not lower it
+    // is skipped (a read through L2 first), so most of a component's cells
+    // issue none
+    if (all) {
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) {
+        const unsigned long long v = __shfl_xor_sync(0xffffffffu, e, o);
+        e = v < e ? v : e;
+      }
+      if (lane == 0 && e < __ldcg(&first[s0])) atomicMin(&first[s0], e);
+    } else if (s >= 0 && e < __ldcg(&first[s])) {
+      atomicMin(&first[s], e);
+    }
   }
 }
 
@@ -166,26 +226,53 @@ __global__ void KLabelStable(Dims d, int nc, const unsigned long long* __restric
   }
 }
 
-// New colours (and their copy from before the propagation pass).  Cells
-// the propagation may colour (none, u > 0) flag their line of each
-// direction; a line without such a cell cannot change and is skipped.
+// New colours, and their copy from before the propagation pass on the
+// cells at the ends of the lines (the only ones it reads there).  Cells the
+// propagation may colour (none, u > 0) flag their line of each direction; a
+// line without such a cell cannot change and is skipped.  A CTA walks rows
+// (y, z) of the grid (row = y + ny z), two cells of a row per thread with
+// 16-byte loads and stores (nx even; else one cell per thread).
+__device__ __forceinline__ double ApplyCell(int64_t c, double uc, const int* __restrict__ root,
+                                            const int* __restrict__ slot,
+                                            const double* __restrict__ color) {
+  return Gas(uc) ? color[slot[root[c]]] : -1.0;
+}
 __global__ void KLabelApply(Dims d, const int* __restrict__ root, const int* __restrict__ slot,
                             const double* __restrict__ color, const double* __restrict__ u,
                             double* cl, double* pre, unsigned char* flag) {
-  const int64_t n = d.cells();
   unsigned char* f1 = flag + (int64_t)d.ny * d.nz;
   unsigned char* f2 = f1 + (int64_t)d.nx * d.nz;
-  for (int64_t c = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; c < n;
-       c += (int64_t)gridDim.x * blockDim.x) {
-    const int r = root[c];
-    const double v = r < 0 ? -1.0 : color[slot[r]];
-    cl[c] = v;
-    pre[c] = v;
-    if (v == -1.0 && u[c] > 0) {
-      const int64_t x = c % d.nx, y = (c / d.nx) % d.ny, z = c / ((int64_t)d.nx * d.ny);
-      flag[c / d.nx] = 1;
-      f1[x + z * d.nx] = 1;
-      f2[x + y * d.nx] = 1;
+  const int per = (d.nx % 2 == 0) ? 2 : 1;
+  const int nrows = d.ny * d.nz;
+  for (int row = blockIdx.x; row < nrows; row += gridDim.x) {
+    const int y = row % d.ny, z = row / d.ny;
+    const int64_t base = (int64_t)row * d.nx;
+    const bool edge_yz = y == 0 || y == d.ny - 1 || z == 0 || z == d.nz - 1;
+    for (int x0 = per * (blockIdx.y * blockDim.x + threadIdx.x); x0 < d.nx;
+         x0 += per * gridDim.y * blockDim.x) {
+      const int64_t c = base + x0;
+      double u2[2], v2[2];
+      if (per == 2) {
+        const double2 uu = *reinterpret_cast<const double2*>(u + c);
+        u2[0] = uu.x;
+        u2[1] = uu.y;
+        v2[0] = ApplyCell(c, u2[0], root, slot, color);
+        v2[1] = ApplyCell(c + 1, u2[1], root, slot, color);
+        *reinterpret_cast<double2*>(cl + c) = make_double2(v2[0], v2[1]);
+      } else {
+        u2[0] = u[c];
+        v2[0] = ApplyCell(c, u2[0], root, slot, color);
+        cl[c] = v2[0];
+      }
+      for (int e = 0; e < per; ++e) {
+        const int x = x0 + e;
+        if (edge_yz || x == 0 || x == d.nx - 1) pre[c + e] = v2[e];
+        if (v2[e] == -1.0 && u2[e] > 0) {
+          flag[row] = 1;
+          f1[x + (int64_t)z * d.nx] = 1;
+          f2[x + (int64_t)y * d.nx] = 1;
+        }
+      }
     }
   }
 }
@@ -296,6 +383,7 @@ int Recolor(aphgpu_ctx* ctx) {
   auto& L = ctx->lab;
   if (!L.par) {
     APH_TRY(Alloc(ctx, &L.par, N));
+    APH_TRY(Alloc(ctx, &L.gas, N));
     APH_TRY(Alloc(ctx, &L.slot, N));
     APH_TRY(Alloc(ctx, &L.croot, kMaxComponents));
     APH_TRY(Alloc(ctx, &L.first, kMaxComponents));
@@ -307,14 +395,23 @@ int Recolor(aphgpu_ctx* ctx) {
   }
   const int nb = Blocks(N);
   APH_CUDA(ctx, cudaMemsetAsync(L.ctl, 0, 4 * sizeof(int), st));
-  KLabelInit<<<nb, kLabelThreads, 0, st>>>(N, ctx->u, L.par);
+  int* gcount = L.ctl + 2;
+  KLabelInit<<<nb, kLabelThreads, 0, st>>>(N, ctx->u, L.par, L.gas, gcount);
   APH_LAUNCHED(ctx);
-  KLabelUnion<<<nb, kLabelThreads, 0, st>>>(d, L.par, L.ctl + 1);
+  // the list passes: a grid of 8 CTAs per SM looping over the gas cells
+  int sms = 0;
+  if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, ctx->device) != cudaSuccess ||
+      sms < 1) {
+    cudaGetLastError();
+    sms = 152;
+  }
+  const int lb = 8 * sms;
+  KLabelUnion<<<lb, kLabelThreads, 0, st>>>(d, ctx->u, L.par, L.gas, gcount, L.ctl + 1);
   APH_LAUNCHED(ctx);
-  KLabelFlatten<<<nb, kLabelThreads, 0, st>>>(N, L.par, L.slot, L.ctl, L.croot, kMaxComponents,
-                                              L.ctl + 1);
+  KLabelFlatten<<<lb, kLabelThreads, 0, st>>>(N, L.par, L.gas, gcount, L.slot, L.ctl, L.croot,
+                                              kMaxComponents, L.ctl + 1);
   APH_LAUNCHED(ctx);
-  KLabelRoot<<<nb, kLabelThreads, 0, st>>>(N, L.par);
+  KLabelRoot<<<lb, kLabelThreads, 0, st>>>(N, L.par, L.gas, gcount);
   APH_LAUNCHED(ctx);
   int hc[2] = {0, 0};
   APH_CUDA(ctx, cudaMemcpyAsync(hc, L.ctl, sizeof(hc), cudaMemcpyDeviceToHost, st));
@@ -327,7 +424,7 @@ int Recolor(aphgpu_ctx* ctx) {
   std::vector<double> color(std::max(nc, 1));
   if (nc > 0) {
     APH_CUDA(ctx, cudaMemsetAsync(L.first, 0xff, sizeof(unsigned long long) * nc, st));
-    KLabelFirst<<<nb, kLabelThreads, 0, st>>>(d, L.par, L.slot, ctx->cl, L.first);
+    KLabelFirst<<<lb, kLabelThreads, 0, st>>>(d, L.par, L.slot, L.gas, gcount, ctx->cl, L.first);
     APH_LAUNCHED(ctx);
     KLabelStable<<<Blocks(nc), kLabelThreads, 0, st>>>(d, nc, L.first, ctx->cl, L.stable);
     APH_LAUNCHED(ctx);
@@ -359,8 +456,13 @@ int Recolor(aphgpu_ctx* ctx) {
                                   cudaMemcpyHostToDevice, st));
   }
   APH_CUDA(ctx, cudaMemsetAsync(L.flag, 0, (size_t)LineFlags(d), st));
-  KLabelApply<<<nb, kLabelThreads, 0, st>>>(d, L.par, L.slot, L.color, ctx->u, ctx->cl, L.pre,
-                                            L.flag);
+  {
+    // CTAs of 256 threads, each over rows of up to 512 cells (more CTAs
+    // per row along y for longer rows), 16 per SM
+    const int rows = d.ny * d.nz;
+    const dim3 g((unsigned)std::min(rows, 16 * sms), (unsigned)((d.nx + 511) / 512));
+    KLabelApply<<<g, 256, 0, st>>>(d, L.par, L.slot, L.color, ctx->u, ctx->cl, L.pre, L.flag);
+  }
   APH_LAUNCHED(ctx);
   const unsigned char* fl = L.flag;
   for (int dir = 0; dir < 3; ++dir) {
