@@ -221,6 +221,7 @@ struct Multigrid {
   std::vector<Level<double>> l64;  // level 0 aliases the fine system
   std::vector<Level<float>> l32;
   bool built64 = false, built32 = false;
+  int cmax64 = 0, cmax32 = 0;  // the coarse_max each hierarchy was built with
   // coarsest-level CG scratch (FP64)
   double* cr = nullptr;
   double* cp = nullptr;
@@ -397,7 +398,7 @@ struct aphgpu_ctx {
   int mg_gamma = 0;        // cycles of each level below the finest (1 V, 2 W, 0 auto)
   int mg_series_pct = 60;  // weight (%) of the series couplings in the coarse operators
   int mg_growth = 0;       // sweeps below the finest level (1 same, 2 linear, 3 doubling, 0 auto)
-  bool use_cta_coarse = false;  // smallest FP32 levels cycled by one CTA
+  bool use_cta_coarse = true;  // smallest FP32 levels cycled by one CTA
 
   // timing
   cudaEvent_t ev0 = nullptr, ev1 = nullptr;

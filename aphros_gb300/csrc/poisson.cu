@@ -2194,18 +2194,20 @@ int EnsureMixedVectors(aphgpu_ctx* ctx) {
 
 int EnsureMixedHierarchy(aphgpu_ctx* ctx, const aphgpu_conf* conf) {
   APH_TRY(EnsureMixedVectors(ctx));
-  if (!ctx->mg.built32) {
+  if (!ctx->mg.built32 || ctx->mg.cmax32 != conf->mg_coarse_max) {
     APH_TRY(BuildHierarchy<float>(ctx, ctx->mg.l32, conf->mg_coarse_max));
     ctx->mg.built32 = true;
+    ctx->mg.cmax32 = conf->mg_coarse_max;
   }
   return APHGPU_OK;
 }
 
 int SolveMGPCG(aphgpu_ctx* ctx, const aphgpu_conf* conf, aphgpu_info* info) {
   auto& mg = ctx->mg;
-  if (!mg.built64) {
+  if (!mg.built64 || mg.cmax64 != conf->mg_coarse_max) {
     APH_TRY(BuildHierarchy<double>(ctx, mg.l64, conf->mg_coarse_max));
     mg.built64 = true;
+    mg.cmax64 = conf->mg_coarse_max;
   }
   const Op<double> A = FineOp(ctx);
   cudaStream_t st = ctx->stream;
@@ -2237,9 +2239,10 @@ int SolveMGPCG(aphgpu_ctx* ctx, const aphgpu_conf* conf, aphgpu_info* info) {
 int SolveMGPCG32(aphgpu_ctx* ctx, const aphgpu_conf* conf, aphgpu_info* info) {
   auto& mg = ctx->mg;
   APH_TRY(EnsureMixedVectors(ctx));
-  if (!mg.built32) {
+  if (!mg.built32 || mg.cmax32 != conf->mg_coarse_max) {
     APH_TRY(BuildHierarchy<float>(ctx, mg.l32, conf->mg_coarse_max));
     mg.built32 = true;
+    mg.cmax32 = conf->mg_coarse_max;
   }
   const Op<double> A = FineOp(ctx);
   cudaStream_t st = ctx->stream;
@@ -2287,9 +2290,10 @@ int SolveMixed(aphgpu_ctx* ctx, const aphgpu_conf* conf, aphgpu_info* info) {
   auto& mg = ctx->mg;
   const int64_t N = ctx->N;
   APH_TRY(EnsureMixedVectors(ctx));
-  if (!mg.built32) {
+  if (!mg.built32 || mg.cmax32 != conf->mg_coarse_max) {
     APH_TRY(BuildHierarchy<float>(ctx, mg.l32, conf->mg_coarse_max));
     mg.built32 = true;
+    mg.cmax32 = conf->mg_coarse_max;
   }
   const Op<double> A = FineOp(ctx);
   const Op<float> A32 = MakeOp(mg.l32[0]);
