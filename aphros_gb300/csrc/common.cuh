@@ -371,8 +371,8 @@ struct aphgpu_ctx {
     double* stable = nullptr;  // previous colour at that position
     double* color = nullptr;   // new colour per slot
     double* pre = nullptr;     // colours before the propagation pass
-    int* ctl = nullptr;        // component count, error flag, gas cell count
-    unsigned char* flag = nullptr;  // lines the propagation pass visits
+    int* ctl = nullptr;        // component count, error flag, gas and candidate counts
+    unsigned char* flag = nullptr;  // the propagation's candidate cells (1 byte each)
   } lab;
   // host staging (pinned)
   void* pinned = nullptr;

@@ -17,8 +17,10 @@
 //   propagate   cells without colour with 0 < u take the colour of a face
 //               neighbour with larger u, faces in the mesh's order.  Faces of
 //               one direction that share no cell lie on different lines
-//               along that direction, so one thread replays one line in
-//               order; halo cells hold the colours from before the pass.
+//               along that direction, and within a line only the runs of
+//               such cells (with the faces on both sides) can change, so
+//               one thread replays one run in order; halo cells hold the
+//               colours from before the pass.
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -35,7 +37,6 @@ namespace {
 constexpr int kLabelThreads = 256;
 constexpr int kMaxComponents = 1 << 21;
 constexpr unsigned long long kNoFirst = ~0ull;
-constexpr int kPropBatch = 8;  // cells of a line loaded ahead by the propagation
 constexpr long long kNoColorBits = 0xBFF0000000000000LL;  // -1.0, no colour
 
 __device__ __forceinline__ int Wrap(int i, int n) { return i < 0 ? i + n : (i >= n ? i - n : i); }
@@ -227,21 +228,32 @@ __global__ void KLabelStable(Dims d, int nc, const unsigned long long* __restric
 }
 
 // New colours, and their copy from before the propagation pass on the
-// cells at the ends of the lines (the only ones it reads there).  Cells the
-// propagation may colour (none, u > 0) flag their line of each direction; a
-// line without such a cell cannot change and is skipped.  A CTA walks rows
-// (y, z) of the grid (row = y + ny z), two cells of a row per thread with
-// 16-byte loads and stores (nx even; else one cell per thread).
+// cells at the ends of the lines (the only ones it reads there).  The cells
+// the propagation may colour (no colour, u > 0: the candidates) are marked
+// in `cand` and listed.  A CTA walks rows (y, z) of the grid (row = y + ny
+// z), two cells of a row per thread with 16-byte loads and stores (nx
+// even; else one cell per thread).
 __device__ __forceinline__ double ApplyCell(int64_t c, double uc, const int* __restrict__ root,
                                             const int* __restrict__ slot,
                                             const double* __restrict__ color) {
   return Gas(uc) ? color[slot[root[c]]] : -1.0;
 }
+// Append over the active lanes of a warp
+__device__ __forceinline__ void AppendActive(bool want, int c, int* list, int* count) {
+  const unsigned act = __activemask();
+  const unsigned m = __ballot_sync(act, want);
+  if (!m) return;
+  const int lane = threadIdx.x & 31;
+  const int leader = __ffs(m) - 1;
+  int base = 0;
+  if (lane == leader) base = atomicAdd(count, __popc(m));
+  base = __shfl_sync(act, base, leader);
+  if (want) list[base + __popc(m & ((1u << lane) - 1u))] = c;
+}
 __global__ void KLabelApply(Dims d, const int* __restrict__ root, const int* __restrict__ slot,
                             const double* __restrict__ color, const double* __restrict__ u,
-                            double* cl, double* pre, unsigned char* flag) {
-  unsigned char* f1 = flag + (int64_t)d.ny * d.nz;
-  unsigned char* f2 = f1 + (int64_t)d.nx * d.nz;
+                            double* cl, double* pre, unsigned char* cand, int* clist,
+                            int* ccount) {
   const int per = (d.nx % 2 == 0) ? 2 : 1;
   const int nrows = d.ny * d.nz;
   for (int row = blockIdx.x; row < nrows; row += gridDim.x) {
@@ -267,11 +279,9 @@ __global__ void KLabelApply(Dims d, const int* __restrict__ root, const int* __r
       for (int e = 0; e < per; ++e) {
         const int x = x0 + e;
         if (edge_yz || x == 0 || x == d.nx - 1) pre[c + e] = v2[e];
-        if (v2[e] == -1.0 && u2[e] > 0) {
-          flag[row] = 1;
-          f1[x + (int64_t)z * d.nx] = 1;
-          f2[x + (int64_t)y * d.nx] = 1;
-        }
+        const bool cd = v2[e] == -1.0 && u2[e] > 0;
+        cand[c + e] = cd ? 1 : 0;
+        AppendActive(cd, (int)(c + e), clist, ccount);
       }
     }
   }
@@ -280,72 +290,71 @@ __global__ void KLabelApply(Dims d, const int* __restrict__ root, const int* __r
 // The faces of direction `dir` of one line, in order: face w lies between
 // the line's cells w-1 and w; at w = 0 and w = m the outer cell is the
 // halo copy of the line's other end, with the colour from before the pass.
+// A face changes a colour only where one of its cells is a candidate (no
+// colour, u > 0), and a cell that is not one never changes (its colour is
+// set, or u <= 0), so the faces of a line split into independent runs: each
+// maximal run of consecutive candidates with the faces on both sides of it.
+// A thread replays the run that starts at a listed candidate whose previous
+// cell along `dir` is not one (or at the line's first cell, whose previous
+// cell is the halo copy), in face order, exactly as the whole line's replay
+// would.
 __global__ void KLabelPropagate(Dims d, int dir, const double* __restrict__ u, double* cl,
                                 const double* __restrict__ pre,
-                                const unsigned char* __restrict__ flag) {
+                                const unsigned char* __restrict__ cand,
+                                const int* __restrict__ clist, const int* ccount) {
   const int m = dir == 0 ? d.nx : dir == 1 ? d.ny : d.nz;
   const int64_t stride = dir == 0 ? 1 : dir == 1 ? (int64_t)d.nx : (int64_t)d.nx * d.ny;
-  const int64_t nlines = d.cells() / m;
-  for (int64_t l = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; l < nlines;
-       l += (int64_t)gridDim.x * blockDim.x) {
-    if (!flag[l]) continue;
-    int64_t base;
-    if (dir == 0) {
-      base = l * d.nx;
-    } else if (dir == 1) {
-      const int64_t x = l % d.nx, z = l / d.nx;
-      base = x + z * (int64_t)d.nx * d.ny;
-    } else {
-      base = l;
-    }
+  const int n = *ccount;
+  for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < n; t += gridDim.x * blockDim.x) {
+    const int64_t c = clist[t];
+    const int64_t x = c % d.nx, y = (c / d.nx) % d.ny, z = c / ((int64_t)d.nx * d.ny);
+    const int w0 = (int)(dir == 0 ? x : dir == 1 ? y : z);
+    const int64_t base = c - (int64_t)w0 * stride;  // the line's first cell
+    if (w0 > 0 && cand[c - stride]) continue;  // not the start of its run
     const int64_t last = base + (int64_t)(m - 1) * stride;
-    double cl0 = pre[last], u0 = u[last];  // halo copy before cell 0
-    // the cells are loaded kPropBatch at a time ahead of the faces that
-    // read them (a cell changes only at its own faces, replayed by this
-    // thread after the load, and the running values carry the changes)
-    for (int w0 = 0; w0 <= m; w0 += kPropBatch) {
-      double clb[kPropBatch], ub[kPropBatch];
-#pragma unroll
-      for (int q = 0; q < kPropBatch; ++q) {
-        const int w = w0 + q;
-        clb[q] = -1.0;
-        ub[q] = 0.0;
-        if (w < m) {
-          const int64_t c1 = base + (int64_t)w * stride;
-          clb[q] = cl[c1];
-          ub[q] = u[c1];
-        } else if (w == m) {
-          clb[q] = pre[base];  // halo copy after the last cell
-          ub[q] = u[base];
-        }
+    double cl0, u0;
+    if (w0 == 0) {
+      cl0 = pre[last];  // halo copy before cell 0
+      u0 = u[last];
+    } else {
+      cl0 = cl[c - stride];
+      u0 = u[c - stride];
+    }
+    // faces w0 .. (the run's last cell) + 1
+    for (int w = w0; w <= m; ++w) {
+      const int64_t c1 = base + (int64_t)w * stride;
+      double cl1;
+      double u1;
+      bool in_run;
+      if (w < m) {
+        cl1 = cl[c1];
+        u1 = u[c1];
+        in_run = cand[c1] != 0;
+      } else {
+        cl1 = pre[base];  // halo copy after the last cell
+        u1 = u[base];
+        in_run = false;
       }
-#pragma unroll
-      for (int q = 0; q < kPropBatch; ++q) {
-        const int w = w0 + q;
-        if (w > m) break;
-        const int64_t c1 = base + (int64_t)w * stride;
-        double cl1 = clb[q];
-        const double u1 = ub[q];
-        // the comparisons on the bit patterns (integer instructions; FP64
-        // issues at 2 per clock per SM here): in each rule one operand of
-        // u0 > u1 / u1 > u0 is positive, and for a positive double and any
-        // other non-NaN double the signed 64-bit order of the bits is the
-        // numeric order; -1 (no colour) has one bit pattern
-        const long long b0 = __double_as_longlong(u0), b1 = __double_as_longlong(u1);
-        bool none0 = __double_as_longlong(cl0) == kNoColorBits;
-        const bool none1 = __double_as_longlong(cl1) == kNoColorBits;
-        if (none0 && b0 > 0 && b1 > b0 && !none1) {
-          cl0 = cl1;
-          none0 = false;
-          if (w > 0) cl[c1 - stride] = cl0;
-        }
-        if (none1 && b1 > 0 && b0 > b1 && !none0) {
-          cl1 = cl0;
-          if (w < m) cl[c1] = cl1;
-        }
+      // the comparisons on the bit patterns (integer instructions): in each
+      // rule one operand of u0 > u1 / u1 > u0 is positive, and for a
+      // positive double and any other non-NaN double the signed 64-bit
+      // order of the bits is the numeric order; -1 (no colour) has one bit
+      // pattern
+      const long long b0 = __double_as_longlong(u0), b1 = __double_as_longlong(u1);
+      bool none0 = __double_as_longlong(cl0) == kNoColorBits;
+      const bool none1 = __double_as_longlong(cl1) == kNoColorBits;
+      if (none0 && b0 > 0 && b1 > b0 && !none1) {
         cl0 = cl1;
-        u0 = u1;
+        none0 = false;
+        if (w > 0) cl[c1 - stride] = cl0;
       }
+      if (none1 && b1 > 0 && b0 > b1 && !none0) {
+        cl1 = cl0;
+        if (w < m) cl[c1] = cl1;
+      }
+      cl0 = cl1;
+      u0 = u1;
+      if (!in_run) break;  // the face after the run's last cell is done
     }
   }
 }
@@ -357,12 +366,6 @@ __global__ void KColorInit(int64_t n, const double* __restrict__ u, double* cl) 
 }
 
 int Blocks(int64_t n) { return FlatBlocks(n); }
-
-// Line flags of the three directions: ny*nz x-lines, nx*nz y-lines, nx*ny
-// z-lines.
-int64_t LineFlags(const Dims& d) {
-  return (int64_t)d.ny * d.nz + (int64_t)d.nx * d.nz + (int64_t)d.nx * d.ny;
-}
 
 }  // namespace
 
@@ -391,7 +394,7 @@ int Recolor(aphgpu_ctx* ctx) {
     APH_TRY(Alloc(ctx, &L.color, kMaxComponents));
     APH_TRY(Alloc(ctx, &L.pre, N));
     APH_TRY(Alloc(ctx, &L.ctl, 4));
-    APH_TRY(Alloc(ctx, &L.flag, LineFlags(d)));
+    APH_TRY(Alloc(ctx, &L.flag, N));
   }
   const int nb = Blocks(N);
   APH_CUDA(ctx, cudaMemsetAsync(L.ctl, 0, 4 * sizeof(int), st));
@@ -455,22 +458,22 @@ int Recolor(aphgpu_ctx* ctx) {
     APH_CUDA(ctx, cudaMemcpyAsync(L.color, color.data(), sizeof(double) * nc,
                                   cudaMemcpyHostToDevice, st));
   }
-  APH_CUDA(ctx, cudaMemsetAsync(L.flag, 0, (size_t)LineFlags(d), st));
+  // the candidates of the propagation, listed in the gas list's storage
+  // (the union-find passes are done with it) and counted in ctl[3]
+  int* ccount = L.ctl + 3;
   {
     // CTAs of 256 threads, each over rows of up to 512 cells (more CTAs
     // per row along y for longer rows), 16 per SM
     const int rows = d.ny * d.nz;
     const dim3 g((unsigned)std::min(rows, 16 * sms), (unsigned)((d.nx + 511) / 512));
-    KLabelApply<<<g, 256, 0, st>>>(d, L.par, L.slot, L.color, ctx->u, ctx->cl, L.pre, L.flag);
+    KLabelApply<<<g, 256, 0, st>>>(d, L.par, L.slot, L.color, ctx->u, ctx->cl, L.pre, L.flag,
+                                   L.gas, ccount);
   }
   APH_LAUNCHED(ctx);
-  const unsigned char* fl = L.flag;
   for (int dir = 0; dir < 3; ++dir) {
-    const int m = dir == 0 ? d.nx : dir == 1 ? d.ny : d.nz;
-    const int64_t nlines = N / m;
-    KLabelPropagate<<<Blocks(nlines), kLabelThreads, 0, st>>>(d, dir, ctx->u, ctx->cl, L.pre, fl);
+    KLabelPropagate<<<lb, kLabelThreads, 0, st>>>(d, dir, ctx->u, ctx->cl, L.pre, L.flag, L.gas,
+                                                  ccount);
     APH_LAUNCHED(ctx);
-    fl += nlines;
   }
   // the host vector of colours stays alive until the copy has completed
   APH_CUDA(ctx, cudaStreamSynchronize(st));

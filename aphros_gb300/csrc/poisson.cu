@@ -1145,12 +1145,19 @@ __global__ void __launch_bounds__(1024) KCoarsestDense(int n, const double* __re
 }
 
 // r = b - A x (FP64) with reductions r.r, max|r|, b.b; stopping test
+// BB: also sum b.b (for aphgpu_residual_norms; the solves do not read it).
+// The kernel is bound by FP64 issue on this GPU, so the running max|r| is
+// taken on the bit patterns of |r| (integer instructions; for non-negative
+// doubles the integer order is the numeric order, NaN skipped as fmax
+// does) and the stored -u is u with its sign bit flipped: the same values.
+template <bool BB>
 __global__ void KResidual64(Op<double> A, const double* __restrict__ b,
                             const double* __restrict__ x, double* r,
                             SolveScalars* s, RedBuf rb, int count_iter,
                             int zero_guess = 0) {
   double v[3] = {0, 0, 0};
   const int op[3] = {0, 1, 0};
+  long long amax = 0;  // bits of the largest |r| so far (+0)
   TILE_LOOP_BEGIN(A.d)
   // r = -(x*e0 + e7 + sum x_nb e_q) as linear.ipp:47-53, e7 = -b; with a
   // zero x, r = b (as KCgInit's zero guess: no stencil, no FP64 product)
@@ -1170,12 +1177,15 @@ __global__ void KResidual64(Op<double> A, const double* __restrict__ b,
     u += x[d.idx(i, j, wrapm(k - 1, d.nz))] * e[4];
     u += x[d.idx(i, j, wrapp(k + 1, d.nz))] * e[5];
   }
-  const double rv = -u;
+  const long long ub = __double_as_longlong(u);
+  const double rv = __longlong_as_double(ub ^ (long long)0x8000000000000000ULL);
   if (r) r[c] = rv;
   v[0] += rv * rv;
-  v[1] = fmax(v[1], fabs(rv));
-  v[2] += b[c] * b[c];
+  const long long ab = ub & 0x7FFFFFFFFFFFFFFFLL;
+  if (ab <= 0x7FF0000000000000LL && ab > amax) amax = ab;
+  if (BB) v[2] += b[c] * b[c];
   TILE_LOOP_END
+  v[1] = __longlong_as_double(amax);
   __shared__ double out[3];
   if (GridReduce<3>(v, op, rb, out)) {
     if (threadIdx.x == 0 && threadIdx.y == 0) {
@@ -2213,8 +2223,8 @@ int SolveMGPCG(aphgpu_ctx* ctx, const aphgpu_conf* conf, aphgpu_info* info) {
   cudaStream_t st = ctx->stream;
   APH_TRY(InitScalars(ctx, ctx->scal, conf, 1.0, ctx->hist));
   // r = b - A x0 (x holds the initial guess)
-  KResidual64<<<TileGrid(ctx->d), TileBlock(), 0, st>>>(A, ctx->b, ctx->x, ctx->r,
-                                                        ctx->scal, ctx->red, 0);
+  KResidual64<false><<<TileGrid(ctx->d), TileBlock(), 0, st>>>(A, ctx->b, ctx->x, ctx->r,
+                                                               ctx->scal, ctx->red, 0);
   APH_LAUNCHED(ctx);
   auto& lv = mg.l64;
   SolveScalars* s = ctx->scal;
@@ -2249,8 +2259,8 @@ int SolveMGPCG32(aphgpu_ctx* ctx, const aphgpu_conf* conf, aphgpu_info* info) {
   const int64_t N = ctx->N;
   const int fb = FlatBlocks(N);
   APH_TRY(InitScalars(ctx, ctx->scal, conf, 1.0, ctx->hist));
-  KResidual64<<<TileGrid(ctx->d), TileBlock(), 0, st>>>(A, ctx->b, ctx->x, ctx->r,
-                                                        ctx->scal, ctx->red, 0);
+  KResidual64<false><<<TileGrid(ctx->d), TileBlock(), 0, st>>>(A, ctx->b, ctx->x, ctx->r,
+                                                               ctx->scal, ctx->red, 0);
   APH_LAUNCHED(ctx);
   auto& lv = mg.l32;
   SolveScalars* s = ctx->scal;
@@ -2315,7 +2325,7 @@ int SolveMixed(aphgpu_ctx* ctx, const aphgpu_conf* conf, aphgpu_info* info) {
   for (;;) {
     // outer residual in FP64 and the stopping test (r = b for the zero
     // initial guess)
-    KResidual64<<<TileGrid(ctx->d), TileBlock(), 0, st>>>(
+    KResidual64<false><<<TileGrid(ctx->d), TileBlock(), 0, st>>>(
         A, ctx->b, ctx->x, ctx->r, ctx->scal, ctx->red, 1, outer == 0 && ctx->x_zero ? 1 : 0);
     APH_LAUNCHED(ctx);
     APH_TRY(ReadScalars(ctx, ctx->scal, &hs));
@@ -2498,7 +2508,7 @@ int ResidualNorms(aphgpu_ctx* ctx, double* rnorm, double* bnorm) {
   aphgpu_conf c;
   aphgpu_conf_default(&c);
   APH_TRY(InitScalars(ctx, ctx->scal2, &c, 1.0));
-  KResidual64<<<TileGrid(ctx->d), TileBlock(), 0, ctx->stream>>>(
+  KResidual64<true><<<TileGrid(ctx->d), TileBlock(), 0, ctx->stream>>>(
       FineOp(ctx), ctx->b, ctx->x, nullptr, ctx->scal2, ctx->red, 0);
   APH_LAUNCHED(ctx);
   SolveScalars hs;
