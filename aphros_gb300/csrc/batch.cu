@@ -1471,7 +1471,7 @@ namespace aphgpu {
 // staged in at most this much dynamic shared memory (the kernel's static
 // shared memory, the coarsest right-hand side and the copy of the level
 // description, stays within the 227 KB of a CTA).
-constexpr int64_t kCoarseOneCells = 4096;
+constexpr int64_t kCoarseOneCells = 512;
 constexpr size_t kCoarseOneSmem = 200 * 1024;
 
 int CoarseOneSetup(aphgpu_ctx* ctx) {

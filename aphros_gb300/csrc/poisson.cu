@@ -1518,6 +1518,11 @@ int BuildHierarchy<double>(aphgpu_ctx* ctx, std::vector<Level<double>>& lv,
   f.w[2] = ctx->w[2];
   f.diag = ctx->diag;
   f.has_diag = ctx->diag_valid;
+  // the FP64 inverse diagonal, used by this hierarchy's smoother only: made
+  // here, with the hierarchy, after every change of the system (the mixed
+  // solver's FP32 levels have their own)
+  KInvDiag<double><<<TileGrid(ctx->d), TileBlock(), 0, ctx->stream>>>(FineOp(ctx), ctx->invdiag);
+  APH_LAUNCHED(ctx);
   f.invdiag = ctx->invdiag;
   for (size_t l = 1; l < lv.size(); ++l) {
     const Op<double> A = MakeOp(lv[l - 1]);
@@ -2086,8 +2091,6 @@ int SetSystemExprDevice(aphgpu_ctx* ctx, const double* d_expr8) {
   ctx->has_system = true;
   ctx->has_proj = false;
   ctx->mg.built64 = ctx->mg.built32 = false;
-  KInvDiag<double><<<TileGrid(ctx->d), TileBlock(), 0, ctx->stream>>>(FineOp(ctx), ctx->invdiag);
-  APH_LAUNCHED(ctx);
   return APHGPU_OK;
 }
 
@@ -2119,8 +2122,6 @@ int ApplyCellCondDevice(aphgpu_ctx* ctx, int64_t count, const int64_t* d_cells,
   ctx->diag_explicit = true;
   if (count > 0) ctx->singular = false;
   ctx->mg.built64 = ctx->mg.built32 = false;
-  KInvDiag<double><<<TileGrid(ctx->d), TileBlock(), 0, ctx->stream>>>(FineOp(ctx), ctx->invdiag);
-  APH_LAUNCHED(ctx);
   return APHGPU_OK;
 }
 
@@ -2152,8 +2153,6 @@ int AssembleProjectionDevice(aphgpu_ctx* ctx, const double* d_alpha,
   ctx->has_system = true;
   ctx->has_proj = true;
   ctx->mg.built64 = ctx->mg.built32 = false;
-  KInvDiag<double><<<TileGrid(ctx->d), TileBlock(), 0, ctx->stream>>>(FineOp(ctx), ctx->invdiag);
-  APH_LAUNCHED(ctx);
   return APHGPU_OK;
 }
 
@@ -2456,11 +2455,9 @@ int TimeSolverKernel(aphgpu_ctx* ctx, int kernel, int reps, double* ms,
         return SetError(ctx, APHGPU_ERR_STATE, "run a mixed solve first");
       const Op<float> A = MakeOp(mg.l32[0]);
       SolveScalars* s = ctx->scal2;
-      RedBuf rb = ctx->red;
       const float* p = ctx->p32;
       float* ap = ctx->ap32;
       APH_CUDA(ctx, cudaMemsetAsync(s, 0, sizeof(SolveScalars), st));
-      (void)rb;
       launch = [=]() { LaunchApply<float>(ctx, A, p, ap, s); };
       b = N * (4 + 12 + 4);
       break;

@@ -452,10 +452,10 @@ def measure_vof(ctx, case, peak, peak_kind, steps, cpu=True):
 # ---------------------------------------------------------------------------
 # The headline solve runs the library defaults: a W-cycle below the finest
 # level from 256^3 cells up, 2 pre- and 2 post-smoothing red-black sweeps
-# on every level (the levels of at most 16^3 cells cycled by one CTA per
+# on every level (the levels of at most 8^3 cells cycled by one CTA per
 # visit), inner FP32 PCG to 3e-4, stopped at ||r||/||b|| <= 1e-10.
 # Measured at 512^3 it is the fastest configuration whose pressure is
-# within the 1e-9 bar of a tight FP64 solution (7.5e-10) at that stop.  The
+# within the 1e-9 bar of a tight FP64 solution (5.7e-10) at that stop.  The
 # configuration's literal cycle (V, 2+2 sweeps on every level) and the
 # fastest V-cycle (one sweep before and after on the finest level, 2^l on
 # level l below it, inner PCG to 1e-3, which keeps its pressure within the
@@ -696,7 +696,7 @@ def run_ours(args):
                    "l2": "inputs larger than L2 (1 GB per FP64 field), no flush",
                    "multigrid": "library defaults: W-cycle below the finest level, "
                                 "red-black Gauss-Seidel 2+2 on every level (levels of at "
-                                "most 16^3 cells cycled by one CTA per visit), coarse "
+                                "most 8^3 cells cycled by one CTA per visit), coarse "
                                 "couplings 60 % series + 40 % half-Galerkin, inner FP32 PCG "
                                 "to 3e-4; "
                                 "literal_c3_cycle: V, 2+2 on every level; v_cycle: V, 1+1 on "

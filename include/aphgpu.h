@@ -504,12 +504,12 @@ int aphgpu_batch_last_ms(const aphgpu_batch* batch, double* ms, int64_t* launche
  *                            count, 2 count * (l + 1), 3 count * 2^l (at
  *                            most 16), 0 (default) 2 for V-cycles from
  *                            256^3 cells up and 1 otherwise
- *   APHGPU_OPT_CTA_COARSE    1 (default): the FP32 levels of at most 4096
- *                            cells (16^3) below the finest are cycled by
+ *   APHGPU_OPT_CTA_COARSE    1 (default): the FP32 levels of at most 512
+ *                            cells (8^3) below the finest are cycled by
  *                            one CTA per visit of their parent level,
  *                            staged in shared memory (the batch's
  *                            per-domain coarse cycle; a W-cycle at 512^3
- *                            launches 4 k kernels per solve instead of
+ *                            launches 8 k kernels per solve instead of
  *                            16 k); 0: one launch per pass on every level
  *   APHGPU_OPT_WAVE_PLANES   planes per step of the wavefront sweep
  *                            (APHGPU_OPT_FUSED_SWEEPS 5 and 6); 0 (default):
