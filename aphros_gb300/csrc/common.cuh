@@ -313,6 +313,10 @@ struct aphgpu_ctx {
                                // cells of u
   double* kpart = nullptr;     // curvature of each particle string
   int64_t kpart_cap = 0;
+  double* ppoly = nullptr;     // PLIC polygon of each listed cell (particle strings)
+  int* ppk = nullptr;          // its vertex count
+  int64_t ppoly_cap = 0;
+  int* ppos = nullptr;         // list position of each listed cell (N entries)
   // the wavefront sweep: progress counters (one per tile) and, after them,
   // the flag of a wait that gave up; set when a solve launched it
   int* wave_buf = nullptr;

@@ -168,8 +168,8 @@ struct Basis {
 };
 
 // PartStrMeshM::Imp::GetPlaneBasis, dim 3 (partstrmeshm.ipp:166-195)
-__device__ void PlaneBasis(const double* xc, const double* n, double a, double an, double h,
-                           Basis& B) {
+__device__ void PlaneBasis(const double* xc, const double* n, int k, const double (*xx)[3],
+                           double an, Basis& B) {
   const double na[3] = {fabs(n[0]), fabs(n[1]), fabs(n[2])};
   int d = 0;
   if (na[1] < na[d]) d = 1;
@@ -187,8 +187,6 @@ __device__ void PlaneBasis(const double* xc, const double* n, double a, double a
   for (int i = 0; i < 3; ++i) t[i] = t0[i] * ca + t1[i] * sa;
   nn = Norm3(t);
   for (int i = 0; i < 3; ++i) t[i] /= nn;
-  double xx[6][3];
-  const int k = CutPoly2(n, a, h, xx);
   double c[3] = {0, 0, 0};
   for (int q = 0; q < k; ++q)
     for (int i = 0; i < 3; ++i) c[i] += xx[q][i];
@@ -208,12 +206,13 @@ __device__ __forceinline__ V2 PlaneCoords(const double* x, const Basis& B) {
 
 // AppendInterface, dim 3 (partstrmeshm.ipp:222-257) with
 // Reconst::GetInterPoly (reconst.h:748-765)
-__device__ bool AppendInterface(const Basis& B, const double* uz, const double* xc, double a,
-                                const double* n, double h, V2* seg) {
+// (the cell's polygon xx0, k vertices relative to its centre, made once per
+// call by KPartPolys)
+__device__ bool AppendInterface(const Basis& B, const double* uz, const double* xc, int k,
+                                const double (*xx0)[3], const double* n, V2* seg) {
   double xx[6][3];
-  const int k = CutPoly2(n, a, h, xx);
   for (int q = 0; q < k; ++q)
-    for (int i = 0; i < 3; ++i) xx[q][i] += xc[i];
+    for (int i = 0; i < 3; ++i) xx[q][i] = xx0[q][i] + xc[i];
   double e[2][3];
   int j = 0;
   for (int i = 0; i < k && j < 2; ++i) {
@@ -445,11 +444,32 @@ struct PartArgs {
   aphgpu_part_conf p;
 };
 
+// The PLIC polygon of each listed cell (GetCutPoly2, relative to the cell's
+// centre) and the cell's position in the list: each polygon is cut once
+// per call instead of once per string of every cell whose stencil holds it.
+__global__ void KPartPolys(PartArgs A, const double* __restrict__ nrm,
+                           const double* __restrict__ pa, const int* __restrict__ list,
+                           const int* count, double* poly, int* pk, int* pos) {
+  const int n = *count;
+  for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < n; t += gridDim.x * blockDim.x) {
+    const int64_t c = list[t];
+    const double nc[3] = {nrm[3 * c], nrm[3 * c + 1], nrm[3 * c + 2]};
+    double xx[6][3];
+    const int k = CutPoly2(nc, pa[c], A.h, xx);
+    for (int q = 0; q < 6; ++q)
+      for (int i = 0; i < 3; ++i) poly[(int64_t)t * 18 + 3 * q + i] = q < k ? xx[q][i] : 0.;
+    pk[t] = k;
+    pos[c] = t;
+  }
+}
+
 // one string of a listed cell: t = position in the list * ns + string
 __global__ void KPartStrings(PartArgs A, const double* __restrict__ u,
-                             const double* __restrict__ nrm, const double* __restrict__ pa,
+                             const double* __restrict__ nrm,
                              const double* __restrict__ kappa, int fill_only,
-                             const int* __restrict__ list, const int* count, double* kpart) {
+                             const int* __restrict__ list, const int* count,
+                             const double* __restrict__ poly, const int* __restrict__ pk,
+                             const int* __restrict__ pos, double* kpart) {
   const int ns = A.p.ns, np = A.p.np;
   const int64_t total = (int64_t)(*count) * ns;
   const Dims d = A.d;
@@ -468,7 +488,7 @@ __global__ void KPartStrings(PartArgs A, const double* __restrict__ u,
     const double an = (double)s * M_PI / (double)ns;
     const double nc[3] = {nrm[3 * c], nrm[3 * c + 1], nrm[3 * c + 2]};
     Basis B;
-    PlaneBasis(xc, nc, pa[c], an, h, B);
+    PlaneBasis(xc, nc, pk[li], reinterpret_cast<const double(*)[3]>(poly + li * 18), an, B);
     double uz[3];
     Cross3(B.ux, B.uy, uz);
     // the interfacial cells of the 5x5x5 stencil in stencil order (dz, dy,
@@ -492,8 +512,10 @@ __global__ void KPartStrings(PartArgs A, const double* __restrict__ u,
                             (0. + half) + (double)(j + dy) * h,
                             (0. + half) + (double)(k + dz) * h};
       const double nn[3] = {nrm[3 * cn], nrm[3 * cn + 1], nrm[3 * cn + 2]};
+      const int tn = pos[cn];
       V2 e[2];
-      if (AppendInterface(B, uz, xn, pa[cn], nn, h, e)) {
+      if (AppendInterface(B, uz, xn, pk[tn],
+                          reinterpret_cast<const double(*)[3]>(poly + (int64_t)tn * 18), nn, e)) {
         Seg& g = sg[nseg++];
         g.x0 = e[0];
         g.x1 = e[1];
@@ -575,10 +597,33 @@ int CurvatureParticlesDevice(aphgpu_ctx* ctx, const aphgpu_part_conf& conf, bool
     APH_TRY(Alloc(ctx, &ctx->kpart, need));
     ctx->kpart_cap = need;
   }
+  // the polygons of the listed cells (18 doubles each), their vertex
+  // counts, and the list position of each listed cell (N entries)
+  if (nif > ctx->ppoly_cap) {
+    for (void* q : {(void*)ctx->ppoly, (void*)ctx->ppk}) {
+      if (!q) continue;
+      for (size_t i = 0; i < ctx->allocs.size(); ++i)
+        if (ctx->allocs[i] == q) {
+          DeviceFree(ctx, q);
+          ctx->allocs.erase(ctx->allocs.begin() + i);
+          break;
+        }
+    }
+    ctx->ppoly = nullptr;
+    ctx->ppk = nullptr;
+    APH_TRY(Alloc(ctx, &ctx->ppoly, (int64_t)nif * 18));
+    APH_TRY(Alloc(ctx, &ctx->ppk, nif));
+    ctx->ppoly_cap = nif;
+  }
+  if (!ctx->ppos) APH_TRY(Alloc(ctx, &ctx->ppos, ctx->N));
   PartArgs A{ctx->d, ctx->h, conf};
+  KPartPolys<<<FlatBlocks(nif), kFlatThreads, 0, ctx->stream>>>(A, ctx->nrm, ctx->pa, list, count,
+                                                              ctx->ppoly, ctx->ppk, ctx->ppos);
+  APH_LAUNCHED(ctx);
   const int blocks = (int)std::min<int64_t>((need + 127) / 128, 16 * 1024);
-  KPartStrings<<<blocks, 128, 0, ctx->stream>>>(A, ctx->u, ctx->nrm, ctx->pa, ctx->kappa,
-                                                hybrid ? 1 : 0, list, count, ctx->kpart);
+  KPartStrings<<<blocks, 128, 0, ctx->stream>>>(A, ctx->u, ctx->nrm, ctx->kappa,
+                                                hybrid ? 1 : 0, list, count, ctx->ppoly,
+                                                ctx->ppk, ctx->ppos, ctx->kpart);
   APH_LAUNCHED(ctx);
   KPartAverage<<<FlatBlocks(nif), kFlatThreads, 0, ctx->stream>>>(
       conf.ns, list, count, ctx->kpart, hybrid ? 1 : 0, ctx->kappa);
