@@ -73,16 +73,26 @@ __device__ __forceinline__ void Append(bool want, int c, int* list, int* count) 
   if (want) list[base + __popc(m & ((1u << lane) - 1u))] = c;
 }
 
-// the gas cells: par[c] = c and c listed (par of the other cells is never
-// read: gas is tested on u).  The loop bound is uniform over each warp.
-__global__ void KLabelInit(int64_t n, const double* __restrict__ u, int* par, int* list,
-                           int* count) {
+// the gas cells, listed, each with an initial parent: the gas cell before
+// it along z, else along y, else along x (no wrap: a smaller index, in the
+// same component), else itself, as ECL-CC initialises its parents with a
+// smaller neighbour, so the unions start from trees already joined (par of the other cells is never read: gas is tested on u).  The
+// loop bound is uniform over each warp.
+__global__ void KLabelInit(int64_t n, int nx, int ny, const double* __restrict__ u, int* par,
+                           int* list, int* count) {
   const int64_t stride = (int64_t)gridDim.x * blockDim.x;
   for (int64_t c0 = blockIdx.x * (int64_t)blockDim.x + (threadIdx.x & ~31); c0 < n;
        c0 += stride) {
     const int64_t c = c0 + (threadIdx.x & 31);
     const bool g = c < n && Gas(u[c]);
-    if (g) par[c] = (int)c;
+    if (g) {
+      const int64_t nxy = (int64_t)nx * ny;
+      int p = (int)c;
+      if (c % nx != 0 && Gas(u[c - 1])) p = (int)(c - 1);
+      if ((c / nx) % ny != 0 && Gas(u[c - nx])) p = (int)(c - nx);
+      if (c >= nxy && Gas(u[c - nxy])) p = (int)(c - nxy);
+      par[c] = p;
+    }
     Append(g, (int)c, list, count);
   }
 }
@@ -399,7 +409,7 @@ int Recolor(aphgpu_ctx* ctx) {
   const int nb = Blocks(N);
   APH_CUDA(ctx, cudaMemsetAsync(L.ctl, 0, 4 * sizeof(int), st));
   int* gcount = L.ctl + 2;
-  KLabelInit<<<nb, kLabelThreads, 0, st>>>(N, ctx->u, L.par, L.gas, gcount);
+  KLabelInit<<<nb, kLabelThreads, 0, st>>>(N, d.nx, d.ny, ctx->u, L.par, L.gas, gcount);
   APH_LAUNCHED(ctx);
   // the list passes: a grid of 8 CTAs per SM looping over the gas cells
   int sms = 0;
