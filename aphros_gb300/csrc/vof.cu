@@ -518,6 +518,21 @@ __device__ __forceinline__ bool FusedCell(int64_t c, int64_t fp, double v0, doub
                                           const double* __restrict__ ffvu, double vol,
                                           double ivol, double big, double dt, double clipth,
                                           int emax, int full_ok, double& w) {
+  // the cells of a pure region first: with the cell and both neighbours
+  // exactly +0 and fcuu 0 (or exactly 1 and fcuu 1) and face fluxes of
+  // magnitude below 2^(emax-1023), the fluid fluxes are the zeros (the face
+  // fluxes) of BulkFlux and UpdateCell takes its bulk branch: u is unchanged
+  // and the cell is not interfacial (fcuu is the step's first value, so it
+  // is tested, not implied by u)
+  {
+    const long long bm = Bits(um), bc = Bits(uc), bp = Bits(up);
+    const bool fin = ExpBits(Bits(v0)) < emax && ExpBits(Bits(v1)) < emax;
+    if (fin && ((fc == 0 && (bm | bc | bp) == 0) ||
+                (full_ok && fc == 1 && bm == kOneBits && bc == kOneBits && bp == kOneBits))) {
+      w = uc;
+      return false;
+    }
+  }
   // upwind values of the lower face (c) and the upper face (fp)
   const double u0 = PositiveBits(Bits(v0)) ? um : uc;
   const double u1 = PositiveBits(Bits(v1)) ? uc : up;
