@@ -859,6 +859,7 @@ int aphgpu_set_option(aphgpu_ctx* ctx, int option, int value) {
       ctx->mg_gamma = value;
       return APHGPU_OK;
     case APHGPU_OPT_CTA_COARSE: ctx->use_cta_coarse = value != 0; return APHGPU_OK;
+    case APHGPU_OPT_COLOR_SPLIT: ctx->use_split = value != 0; return APHGPU_OK;
     case APHGPU_OPT_WAVE_PLANES:
       if (value < 0 || value > 4096)
         return SetError(ctx, APHGPU_ERR_ARG, "wave planes must be 0..4096");

@@ -214,6 +214,9 @@ struct Level {
   // the smoother and the restriction of the finest FP32 level when set
   uint16_t* wh[3];
   float hscale;
+  // x, b (and the inner PCG's vectors on the finest level) in the
+  // colour-split order of split.cuh (the mixed solver's finest level)
+  bool split;
 };
 
 struct Multigrid {
@@ -398,6 +401,7 @@ struct aphgpu_ctx {
   // kernel on every level it supports
   int fused_mode = 0;
   int wave_planes = 0;  // planes per step of the wavefront sweep (0: sized to L2)
+  bool use_split = true;  // colour-split finest level in the mixed solver
   bool use_half = false;   // FP16 couplings for the finest-level smoother
   int mg_gamma = 0;        // cycles of each level below the finest (1 V, 2 W, 0 auto)
   int mg_series_pct = 60;  // weight (%) of the series couplings in the coarse operators

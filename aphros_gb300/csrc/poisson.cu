@@ -34,6 +34,7 @@
 
 #include "common.cuh"
 #include "stencil.cuh"
+#include "split.cuh"
 #include "sweep.cuh"
 #include "vec.cuh"
 
@@ -474,6 +475,19 @@ inline dim3 VecGrid(const Dims& d) {
   return dim3((nq + 31) / 32, (d.ny + 7) / 8, (d.nz + kz - 1) / kz);
 }
 inline bool VecOk(const Dims& d) { return (d.nx % 4) == 0 && d.nx >= 8; }
+// the colour-split kernels (split.cuh): 4 positions of each half per
+// thread, 32 x 8 threads per CTA, z planes per thread as VecZ
+inline int SplitZ(const Dims& d) {
+  const int nq = d.nx / 8;
+  const int64_t xy = (int64_t)((nq + 31) / 32) * ((d.ny + 7) / 8);
+  int kz = 16;
+  while (kz > 1 && xy * ((d.nz + kz - 1) / kz) < 4 * 152) kz /= 2;
+  return kz;
+}
+inline dim3 SplitGrid(const Dims& d) {
+  const int kz = SplitZ(d);
+  return dim3((d.nx / 8 + 31) / 32, (d.ny + 7) / 8, (d.nz + kz - 1) / kz);
+}
 
 // One red-black half sweep (FP32, vectorized); see KSmooth for the update.
 // The diagonal is recomputed from the six couplings (read anyway) unless the
@@ -1615,7 +1629,10 @@ void LaunchSmooth(aphgpu_ctx* ctx, const Level<T>& f, const Op<T>& A, int color,
 template <>
 void LaunchSmooth<float>(aphgpu_ctx* ctx, const Level<float>& f, const Op<float>& A,
                          int color, int zero_init, const SolveScalars* s) {
-  if (VecOk(f.d) && f.wh[0] && f.hscale > 0.f) {
+  if (f.split) {
+    KSmoothSplit<<<SplitGrid(f.d), TileBlock(), 0, ctx->stream>>>(A, f.b, f.x, color, zero_init,
+                                                                  s, SplitZ(f.d));
+  } else if (VecOk(f.d) && f.wh[0] && f.hscale > 0.f) {
     const Op<__half> H{f.d, (const __half*)f.wh[0], (const __half*)f.wh[1],
                        (const __half*)f.wh[2], nullptr};
     KSmooth4<__half><<<VecGrid(f.d), TileBlock(), 0, ctx->stream>>>(
@@ -1708,7 +1725,10 @@ void LaunchProlongToR(aphgpu_ctx* ctx, const Level<float>& f, const Level<float>
 template <>
 void LaunchProlong<float>(aphgpu_ctx* ctx, const Level<float>& f, const Level<float>& c,
                           const SolveScalars* s) {
-  if (VecOk(f.d)) {
+  if (f.split) {
+    KProlongSplit<<<SplitGrid(f.d), TileBlock(), 0, ctx->stream>>>(f.d, f.x, c.d, c.x, s,
+                                                                   SplitZ(f.d));
+  } else if (VecOk(f.d)) {
     KProlong4<<<VecGrid(f.d), TileBlock(), 0, ctx->stream>>>(f.d, f.x, c.d, c.x, s, VecZ(f.d));
   } else {
     KProlong<float, float><<<TileGrid(f.d), TileBlock(), 0, ctx->stream>>>(f.d, f.x, c.d,
@@ -1724,7 +1744,14 @@ void LaunchRestrict(aphgpu_ctx* ctx, const Level<T>& f, const Level<T>& c, const
 template <>
 void LaunchRestrict<float>(aphgpu_ctx* ctx, const Level<float>& f, const Level<float>& c,
                            const Op<float>& A, const SolveScalars* s) {
-  if (VecOk(f.d)) {
+  if (f.split) {
+    const Dims& dc = c.d;
+    int kz = 8;
+    const int64_t xy = (int64_t)((f.d.nx / 8 + 31) / 32) * ((dc.ny + 7) / 8);
+    while (kz > 1 && xy * ((dc.nz + kz - 1) / kz) < 4 * 152) kz /= 2;
+    const dim3 g((f.d.nx / 8 + 31) / 32, (dc.ny + 7) / 8, (dc.nz + kz - 1) / kz);
+    KResidualRestrictSplit<<<g, TileBlock(), 0, ctx->stream>>>(A, f.b, f.x, dc, c.b, s, kz);
+  } else if (VecOk(f.d)) {
     const int64_t xy = (int64_t)((f.d.nx / 4 + 31) / 32) * ((c.d.ny + 7) / 8);
     int kz = 8;
     while (kz > 1 && xy * ((c.d.nz + kz - 1) / kz) < 4 * 152) kz /= 2;
@@ -1750,7 +1777,11 @@ void LaunchApply(aphgpu_ctx* ctx, const Op<T>& A, const T* p, T* ap, SolveScalar
 template <>
 void LaunchApply<float>(aphgpu_ctx* ctx, const Op<float>& A, const float* p, float* ap,
                         SolveScalars* s) {
-  if (VecOk(A.d)) {
+  const auto& l32 = ctx->mg.l32;
+  if (!l32.empty() && l32[0].split && A.w0 == l32[0].w[0]) {
+    KPcgApplySplit<<<SplitGrid(A.d), TileBlock(), 0, ctx->stream>>>(A, p, ap, s, ctx->red,
+                                                                    SplitZ(A.d));
+  } else if (VecOk(A.d)) {
     KPcgApply4<<<VecGrid(A.d), TileBlock(), 0, ctx->stream>>>(A, p, ap, s, ctx->red, VecZ(A.d));
   } else {
     KPcgApply<float><<<TileGrid(A.d), TileBlock(), 0, ctx->stream>>>(A, p, ap, s, ctx->red);
@@ -1986,6 +2017,7 @@ int Pcg(aphgpu_ctx* ctx, const Op<T>& A, Precond precond, T* x, T* r, T* p,
     key = Mix(key, (uint64_t)CycleGamma(ctx));
     key = Mix(key, (uint64_t)SweepGrowth(ctx));
     key = Mix(key, (uint64_t)(ctx->use_cta_coarse ? 1 + ctx->mg.clc : 0));
+    key = Mix(key, (uint64_t)(!ctx->mg.l32.empty() && ctx->mg.l32[0].split));
     // the FP16 coupling scale is a kernel argument: part of the key
     float hs = ctx->mg.l32.empty() ? 0.f : ctx->mg.l32[0].hscale;
     uint32_t hb;
@@ -2262,6 +2294,7 @@ int SolveMGPCG32(aphgpu_ctx* ctx, const aphgpu_conf* conf, aphgpu_info* info) {
                                                                ctx->scal, ctx->red, 0);
   APH_LAUNCHED(ctx);
   auto& lv = mg.l32;
+  lv[0].split = false;
   SolveScalars* s = ctx->scal;
   auto precond = [&](double* r, double* z) -> int {
     KConvert<double, float><<<fb, kFlatThreads, 0, st>>>(N, r, ctx->r32, 1.0);
@@ -2315,6 +2348,15 @@ int SolveMixed(aphgpu_ctx* ctx, const aphgpu_conf* conf, aphgpu_info* info) {
   int outer = 0, inner_total = 0;
   aphgpu_conf ic = *conf;
   auto& lv = mg.l32;
+  // the finest FP32 level in the colour-split order (split.cuh) when the
+  // plain red-black smoother runs on it (no fused sweeps, no FP16
+  // couplings) and the grid allows it
+  const Dims d0 = lv[0].d;
+  lv[0].split = ctx->use_split && ctx->fused_mode == 0 && !(lv[0].wh[0] && lv[0].hscale > 0.f) &&
+                d0.nx % 8 == 0 && d0.nx >= 16 && d0.ny % 2 == 0 && d0.nz % 2 == 0 &&
+                lv.size() >= 2;
+  const bool split = lv[0].split;
+  const int rb = (int)std::min<int64_t>((int64_t)d0.ny * d0.nz, 32 * SmCount(ctx));
   SolveScalars* s2 = ctx->scal2;
   auto precond = [&](float* r, float* z) -> int {
     lv[0].b = r;
@@ -2335,7 +2377,10 @@ int SolveMixed(aphgpu_ctx* ctx, const aphgpu_conf* conf, aphgpu_info* info) {
     }
     if (outer > conf->maxiter) break;
     // inner FP32 MG-PCG on A e = r / max|r|
-    KScaleResidual<<<fb, kFlatThreads, 0, st>>>(N, ctx->r, ctx->r32, ctx->scal);
+    if (split)
+      KScaleResidualSplit<<<rb, 256, 0, st>>>(d0, ctx->r, ctx->r32, ctx->scal);
+    else
+      KScaleResidual<<<fb, kFlatThreads, 0, st>>>(N, ctx->r, ctx->r32, ctx->scal);
     APH_LAUNCHED(ctx);
     KZeroF<<<fb, kFlatThreads, 0, st>>>(N, ctx->x32);
     APH_LAUNCHED(ctx);
@@ -2360,7 +2405,10 @@ int SolveMixed(aphgpu_ctx* ctx, const aphgpu_conf* conf, aphgpu_info* info) {
     APH_TRY(SaveHistory(ctx, ctx->hist + kHistCap, is.iter, h));
     for (double v : h) ctx->hist_inner.push_back(v / r0);
     ctx->hist_inner.push_back(-1.0);  // separator between inner solves
-    KAddCorrection<<<fb, kFlatThreads, 0, st>>>(N, ctx->x, ctx->x32, ctx->scal);
+    if (split)
+      KAddCorrectionSplit<<<rb, 256, 0, st>>>(d0, ctx->x, ctx->x32, ctx->scal);
+    else
+      KAddCorrection<<<fb, kFlatThreads, 0, st>>>(N, ctx->x, ctx->x32, ctx->scal);
     APH_LAUNCHED(ctx);
     ++outer;
     const int it = outer;
@@ -2396,8 +2444,9 @@ int TimeSolverKernel(aphgpu_ctx* ctx, int kernel, int reps, double* ms,
       fl.x = x;
       launch = [=]() { LaunchSmooth<float>(ctx, fl, A, 0, 0, nullptr); };
       // x read 4 + couplings 12 (6 as FP16) + half of (b 4, invdiag 4,
-      // x write 4)
-      b = N * (4 + (f.hscale > 0.f ? 6 : 12) + 0.5 * 12);
+      // x write 4); colour-split: the other colour's x, the own b and x
+      // (2 each) + couplings 12
+      b = f.split ? N * 18.0 : N * (4 + (f.hscale > 0.f ? 6 : 12) + 0.5 * 12);
       break;
     }
     case APHGPU_K_SWEEP32: {

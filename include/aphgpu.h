@@ -514,7 +514,19 @@ int aphgpu_batch_last_ms(const aphgpu_batch* batch, double* ms, int64_t* launche
  *   APHGPU_OPT_WAVE_PLANES   planes per step of the wavefront sweep
  *                            (APHGPU_OPT_FUSED_SWEEPS 5 and 6); 0 (default):
  *                            as many as let three steps' worth of a level's
- *                            x, b and couplings fit in 60 MB of L2 */
+ *                            x, b and couplings fit in 60 MB of L2
+ *   APHGPU_OPT_COLOR_SPLIT   1 (default): the mixed solver keeps its finest
+ *                            FP32 level (the right-hand side, the iterate
+ *                            and the inner CG vectors) with each row's two
+ *                            red-black colours in separate halves, so that
+ *                            a half sweep reads and writes only the cells
+ *                            it needs (18 instead of 24 bytes per cell);
+ *                            taken when nx is a multiple of 8, ny and nz
+ *                            are even, APHGPU_OPT_FUSED_SWEEPS is 0 and
+ *                            APHGPU_OPT_HALF_COUPLINGS is off.  Same
+ *                            smoothing, restriction and prolongation
+ *                            values; the inner CG's FP32 dot products sum
+ *                            in another order.  0: natural order */
 enum {
   APHGPU_OPT_GRAPHS = 0,
   APHGPU_OPT_FUSED_SWEEPS = 1,
@@ -523,7 +535,8 @@ enum {
   APHGPU_OPT_COARSE_SERIES = 4,
   APHGPU_OPT_SWEEP_GROWTH = 5,
   APHGPU_OPT_CTA_COARSE = 6,
-  APHGPU_OPT_WAVE_PLANES = 7
+  APHGPU_OPT_WAVE_PLANES = 7,
+  APHGPU_OPT_COLOR_SPLIT = 8
 };
 int aphgpu_set_option(aphgpu_ctx* ctx, int option, int value);
 

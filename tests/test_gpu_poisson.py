@@ -271,8 +271,9 @@ def test_fused_sweeps_bit_identical(solver, shape):
     case = workload.Case(nx, c, r, rho1=1.0, rho2=1e-3, seed=12)
     ctx = _lib.Context(shape, h)
     # the fused sweep reads the FP32 couplings: compare against the FP32
-    # half sweeps
+    # half sweeps in the natural order
     ctx.set_option(_lib.OPT_HALF_COUPLINGS, 0)
+    ctx.set_option(_lib.OPT_COLOR_SPLIT, 0)
     N = nx * ny * nz
     alpha = workload.alpha_spheres(nx, c, r)[:N] if nx == ny == nz else np.zeros(N)
     flux = workload.tg_flux(max(shape), seed=5)
@@ -420,6 +421,55 @@ def test_cta_coarse_cycle(cycle, shape):
             assert abs(its - ref[1]) <= 2, (solver, key, its, ref[1])
         # graphs do not change the results
         assert np.array_equal(out[(1, 1)][0], out[(1, 0)][0])
+
+
+@pytest.mark.parametrize("cycle", [1, 2])
+@pytest.mark.parametrize("shape", [(128, 128, 128), (96, 48, 40), (16, 10, 6), (36, 24, 20)])
+def test_color_split_finest_level(cycle, shape):
+    """The mixed solver's finest FP32 level in the colour-split order
+    (APHGPU_OPT_COLOR_SPLIT; shapes with nx % 8 == 0 and even ny, nz, and
+    one, 36 x 24 x 20, that keeps the natural order) smooths, restricts and
+    prolongs with the natural kernels' values; only the inner CG's FP32 dot
+    products sum in another order.  The solves reach the tolerance with the
+    same pressure and (rounding aside) the same iteration counts, with and
+    without CUDA graphs; the split level's apply, restriction and half
+    sweep agree with the natural ones through the whole solve."""
+    nx, ny, nz = shape
+    h = 1.0 / nx
+    c, r = workload.place_spheres(31, 5, 0.08, 0.18, gap=0.02)
+    N = nx * ny * nz
+    alpha = workload.alpha_spheres(nx, c, r)[:N] if nx == ny == nz else np.zeros(N)
+    flux = workload.tg_flux(max(shape), seed=9)
+    flux = np.concatenate([flux[d * max(shape) ** 3:d * max(shape) ** 3 + N] for d in range(3)])
+    ctx = _lib.Context(shape, h)
+    ctx.set_option(_lib.OPT_HALF_COUPLINGS, 0)
+    ctx.assemble_projection(alpha, 1.0, 1e-3, flux, 1e-3)
+    ctx.set_option(_lib.OPT_CYCLE, cycle)
+    _, bn = ctx.residual_norms()
+    tol = 1e-10 * bn / math.sqrt(h ** 3)
+    ctx.set_option(_lib.OPT_COLOR_SPLIT, 1)
+    ctx.set_option(_lib.OPT_FUSED_SWEEPS, 0)
+    ctx.set_option(_lib.OPT_GRAPHS, 0)
+    ctx.solve(_lib.default_conf(solver=_lib.SOLVER_MGPCG, tol=1e-3 * tol, maxiter=300))
+    xt = ctx.get_solution()
+    out = {}
+    for split in (0, 1):
+        for graphs in (1, 0):
+            ctx.set_option(_lib.OPT_COLOR_SPLIT, split)
+            ctx.set_option(_lib.OPT_GRAPHS, graphs)
+            x, info = ctx.solve(_lib.default_conf(solver=_lib.SOLVER_MIXED, tol=tol, maxiter=100))
+            rn, bn2 = ctx.residual_norms()
+            assert info.converged and rn / bn2 <= 1.01e-10, (split, graphs)
+            assert rel_l2(x, xt) <= 1e-9, (split, graphs)
+            out[(split, graphs)] = (x, info.iter, info.inner_iter)
+    ref = out[(0, 0)]
+    for key, (x, it, inner) in out.items():
+        assert rel_l2(x, ref[0]) < 1e-9, key
+        assert it == ref[1] and abs(inner - ref[2]) <= 2, (key, it, inner, ref[1:])
+    # graphs do not change the split path's results
+    assert np.array_equal(out[(1, 1)][0], out[(1, 0)][0])
+    assert out[(1, 1)][1:] == out[(1, 0)][1:]
+    ctx.set_option(_lib.OPT_COLOR_SPLIT, 1)
 
 
 @pytest.mark.parametrize("shape", [(30, 18, 22), (18, 18, 18), (26, 12, 14)])
