@@ -548,6 +548,8 @@ def test_wavefront_wait_gives_up_and_reports():
     ctx.assemble_projection(case.alpha, case.rho1, case.rho2, case.flux, case.dt)
     _, bn = ctx.residual_norms()
     conf = _lib.default_conf(solver=_lib.SOLVER_MIXED, tol=1e-10 * bn / math.sqrt(case.h ** 3))
+    # the half sweeps in the natural order, which the wavefront reproduces
+    ctx.set_option(_lib.OPT_COLOR_SPLIT, 0)
     x0, _ = ctx.solve(conf)
     t0 = time.perf_counter()
     rc = ctx._L.aphgpu_wave_wait_check(ctx.handle)
