@@ -860,6 +860,10 @@ int aphgpu_set_option(aphgpu_ctx* ctx, int option, int value) {
       return APHGPU_OK;
     case APHGPU_OPT_CTA_COARSE: ctx->use_cta_coarse = value != 0; return APHGPU_OK;
     case APHGPU_OPT_COLOR_SPLIT: ctx->use_split = value != 0; return APHGPU_OK;
+    case APHGPU_OPT_DF_RESIDUAL:
+      if (value < 0 || value > 2) return SetError(ctx, APHGPU_ERR_ARG, "df residual must be 0..2");
+      ctx->use_df = value;
+      return APHGPU_OK;
     case APHGPU_OPT_WAVE_PLANES:
       if (value < 0 || value > 4096)
         return SetError(ctx, APHGPU_ERR_ARG, "wave planes must be 0..4096");

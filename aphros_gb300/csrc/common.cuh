@@ -245,6 +245,11 @@ struct Multigrid {
   void* cdom = nullptr;
   int clc = -1;
   int csmem = 0;  // dynamic shared memory of that cycle (bytes)
+  // FP32 low parts of the fine couplings (w - (double)l32[0].w), for the
+  // mixed solver's double-float residual update; made at its first use
+  // after each build of the FP32 hierarchy
+  float* wlo[3] = {nullptr, nullptr, nullptr};
+  bool wlo_ready = false;
 };
 constexpr int kDenseMax = 1024;
 
@@ -402,6 +407,7 @@ struct aphgpu_ctx {
   int fused_mode = 0;
   int wave_planes = 0;  // planes per step of the wavefront sweep (0: sized to L2)
   bool use_split = true;  // colour-split finest level in the mixed solver
+  int use_df = 2;  // double-float outer residual update: 0 off, 1 on, 2 from 2^21 cells
   bool use_half = false;   // FP16 couplings for the finest-level smoother
   int mg_gamma = 0;        // cycles of each level below the finest (1 V, 2 W, 0 auto)
   int mg_series_pct = 60;  // weight (%) of the series couplings in the coarse operators

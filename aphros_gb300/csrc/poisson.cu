@@ -34,6 +34,7 @@
 
 #include "common.cuh"
 #include "stencil.cuh"
+#include "dfloat.cuh"
 #include "split.cuh"
 #include "sweep.cuh"
 #include "vec.cuh"
@@ -1597,6 +1598,7 @@ int BuildHierarchy<float>(aphgpu_ctx* ctx, std::vector<Level<float>>& lv,
     APH_LAUNCHED(ctx);
   }
   lv[0].has_diag = !ctx->singular;
+  ctx->mg.wlo_ready = false;
   APH_TRY(BuildHalfCouplings(ctx, lv[0]));
   for (size_t l = 1; l < lv.size(); ++l) {
     // coarse operators from the FP64 fine operator at level 1, FP32 below
@@ -2357,6 +2359,20 @@ int SolveMixed(aphgpu_ctx* ctx, const aphgpu_conf* conf, aphgpu_info* info) {
                 lv.size() >= 2;
   const bool split = lv[0].split;
   const int rb = (int)std::min<int64_t>((int64_t)d0.ny * d0.nz, 32 * SmCount(ctx));
+  // after the first outer iteration the residual is updated (r -= s A e)
+  // in double-float arithmetic (dfloat.cuh) for flux-difference systems
+  const bool df = ctx->singular &&
+                  (ctx->use_df == 1 || (ctx->use_df == 2 && N >= ((int64_t)1 << 21)));
+  if (df && !mg.wlo_ready) {
+    for (int q = 0; q < 3; ++q) {
+      if (!mg.wlo[q]) APH_TRY(Alloc(ctx, &mg.wlo[q], N));
+      KCouplingLo<<<fb, kFlatThreads, 0, st>>>(N, ctx->w[q], lv[0].w[q], mg.wlo[q]);
+      APH_LAUNCHED(ctx);
+    }
+    mg.wlo_ready = true;
+  }
+  const PairCouplings W{{lv[0].w[0], lv[0].w[1], lv[0].w[2]}, {mg.wlo[0], mg.wlo[1], mg.wlo[2]}};
+  unsigned long long* rp = reinterpret_cast<unsigned long long*>(ctx->r);
   SolveScalars* s2 = ctx->scal2;
   auto precond = [&](float* r, float* z) -> int {
     lv[0].b = r;
@@ -2366,9 +2382,13 @@ int SolveMixed(aphgpu_ctx* ctx, const aphgpu_conf* conf, aphgpu_info* info) {
   for (;;) {
     // outer residual in FP64 and the stopping test (r = b for the zero
     // initial guess)
-    KResidual64<false><<<TileGrid(ctx->d), TileBlock(), 0, st>>>(
-        A, ctx->b, ctx->x, ctx->r, ctx->scal, ctx->red, 1, outer == 0 && ctx->x_zero ? 1 : 0);
-    APH_LAUNCHED(ctx);
+    // (from the second iteration on, the double-float update at the end of
+    // the previous one has computed it)
+    if (outer == 0 || !df) {
+      KResidual64<false><<<TileGrid(ctx->d), TileBlock(), 0, st>>>(
+          A, ctx->b, ctx->x, ctx->r, ctx->scal, ctx->red, 1, outer == 0 && ctx->x_zero ? 1 : 0);
+      APH_LAUNCHED(ctx);
+    }
     APH_TRY(ReadScalars(ctx, ctx->scal, &hs));
     ctx->hist_outer.push_back(hs.residual);
     if (hs.done || (outer >= conf->miniter && hs.residual < conf->tol)) {
@@ -2377,8 +2397,13 @@ int SolveMixed(aphgpu_ctx* ctx, const aphgpu_conf* conf, aphgpu_info* info) {
     }
     if (outer > conf->maxiter) break;
     // inner FP32 MG-PCG on A e = r / max|r|
-    if (split)
+    const bool pairs = df && outer > 0;
+    if (split && pairs)
+      KScaleResidualDFSplit<<<rb, 256, 0, st>>>(d0, rp, ctx->r32, ctx->scal);
+    else if (split)
       KScaleResidualSplit<<<rb, 256, 0, st>>>(d0, ctx->r, ctx->r32, ctx->scal);
+    else if (pairs)
+      KScaleResidualDF<<<fb, kFlatThreads, 0, st>>>(N, rp, ctx->r32, ctx->scal);
     else
       KScaleResidual<<<fb, kFlatThreads, 0, st>>>(N, ctx->r, ctx->r32, ctx->scal);
     APH_LAUNCHED(ctx);
@@ -2405,15 +2430,27 @@ int SolveMixed(aphgpu_ctx* ctx, const aphgpu_conf* conf, aphgpu_info* info) {
     APH_TRY(SaveHistory(ctx, ctx->hist + kHistCap, is.iter, h));
     for (double v : h) ctx->hist_inner.push_back(v / r0);
     ctx->hist_inner.push_back(-1.0);  // separator between inner solves
-    if (split)
-      KAddCorrectionSplit<<<rb, 256, 0, st>>>(d0, ctx->x, ctx->x32, ctx->scal);
-    else
-      KAddCorrection<<<fb, kFlatThreads, 0, st>>>(N, ctx->x, ctx->x32, ctx->scal);
-    APH_LAUNCHED(ctx);
     ++outer;
     const int it = outer;
     APH_CUDA(ctx, cudaMemcpyAsync(&ctx->scal->iter, &it, sizeof(int),
                                   cudaMemcpyHostToDevice, st));
+    if (df) {
+      // x += s e and the next residual with its stopping test
+      const dim3 tg = TileGrid(ctx->d), tb = TileBlock();
+      if (outer == 1 && split)
+        KCorrectDF<true, true><<<tg, tb, 0, st>>>(d0, W, ctx->x32, ctx->x, rp, ctx->scal, ctx->red);
+      else if (outer == 1)
+        KCorrectDF<true, false><<<tg, tb, 0, st>>>(d0, W, ctx->x32, ctx->x, rp, ctx->scal, ctx->red);
+      else if (split)
+        KCorrectDF<false, true><<<tg, tb, 0, st>>>(d0, W, ctx->x32, ctx->x, rp, ctx->scal, ctx->red);
+      else
+        KCorrectDF<false, false><<<tg, tb, 0, st>>>(d0, W, ctx->x32, ctx->x, rp, ctx->scal, ctx->red);
+    } else if (split) {
+      KAddCorrectionSplit<<<rb, 256, 0, st>>>(d0, ctx->x, ctx->x32, ctx->scal);
+    } else {
+      KAddCorrection<<<fb, kFlatThreads, 0, st>>>(N, ctx->x, ctx->x32, ctx->scal);
+    }
+    APH_LAUNCHED(ctx);
     APH_CUDA(ctx, cudaStreamSynchronize(st));
   }
   info->residual = hs.residual;

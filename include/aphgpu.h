@@ -526,7 +526,20 @@ int aphgpu_batch_last_ms(const aphgpu_batch* batch, double* ms, int64_t* launche
  *                            APHGPU_OPT_HALF_COUPLINGS is off.  Same
  *                            smoothing, restriction and prolongation
  *                            values; the inner CG's FP32 dot products sum
- *                            in another order.  0: natural order */
+ *                            in another order.  0: natural order
+ *   APHGPU_OPT_DF_RESIDUAL   1: for flux-difference systems (every
+ *                            diagonal minus the sum of its row's
+ *                            couplings) the mixed solver updates its outer
+ *                            residual after each inner solve as
+ *                            r -= s A e in double-float arithmetic (pairs
+ *                            of floats, 48 significant bits) on the FP32
+ *                            pipe, with the correction x += s e in FP64;
+ *                            the first residual is computed in FP64.  It
+ *                            holds the couplings' FP32 low parts (12
+ *                            bytes per cell).  2 (default): so from 2^21
+ *                            cells up, where the FP64 residual's time
+ *                            matters; 0: every outer residual b - A x in
+ *                            FP64 */
 enum {
   APHGPU_OPT_GRAPHS = 0,
   APHGPU_OPT_FUSED_SWEEPS = 1,
@@ -536,7 +549,8 @@ enum {
   APHGPU_OPT_SWEEP_GROWTH = 5,
   APHGPU_OPT_CTA_COARSE = 6,
   APHGPU_OPT_WAVE_PLANES = 7,
-  APHGPU_OPT_COLOR_SPLIT = 8
+  APHGPU_OPT_COLOR_SPLIT = 8,
+  APHGPU_OPT_DF_RESIDUAL = 9
 };
 int aphgpu_set_option(aphgpu_ctx* ctx, int option, int value);
 

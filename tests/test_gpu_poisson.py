@@ -472,6 +472,55 @@ def test_color_split_finest_level(cycle, shape):
     ctx.set_option(_lib.OPT_COLOR_SPLIT, 1)
 
 
+@pytest.mark.parametrize("shape", [(128, 128, 128), (96, 48, 40), (36, 24, 20), (30, 18, 22)])
+def test_double_float_residual_update(shape):
+    """The mixed solver's outer residual updated as r -= s A e in
+    double-float arithmetic (APHGPU_OPT_DF_RESIDUAL, flux-difference
+    systems; with the colour-split finest level and without it) reaches the
+    1e-10 stop with the FP64 residual b - A x recomputed afterwards within
+    1% of the solver's own, the same outer iteration count as the FP64
+    residual, and the pressure of the tight FP64 solution within the 1e-9
+    bar.  The inner counts may differ by a few: by the last outer
+    iteration the residual is about 1e-6 of the first, and both its FP64
+    and its updated values carry rounding of order 1e-16 |A| |x|, near FP32
+    precision relative to it, so the last inner solves start from right-hand
+    sides that differ in their last bits (128^3: 3 + 14 + 13 inner
+    iterations against 3 + 14 + 10)."""
+    nx, ny, nz = shape
+    h = 1.0 / nx
+    c, r = workload.place_spheres(41, 5, 0.08, 0.18, gap=0.02)
+    N = nx * ny * nz
+    alpha = workload.alpha_spheres(nx, c, r)[:N] if nx == ny == nz else np.zeros(N)
+    flux = workload.tg_flux(max(shape), seed=13)
+    flux = np.concatenate([flux[d * max(shape) ** 3:d * max(shape) ** 3 + N] for d in range(3)])
+    ctx = _lib.Context(shape, h)
+    ctx.assemble_projection(alpha, 1.0, 1e-3, flux, 1e-3)
+    _, bn = ctx.residual_norms()
+    tol = 1e-10 * bn / math.sqrt(h ** 3)
+    ctx.solve(_lib.default_conf(solver=_lib.SOLVER_MGPCG, tol=1e-3 * tol, maxiter=300))
+    xt = ctx.get_solution()
+    out = {}
+    for split in (1, 0):
+        for dfr in (1, 0):
+            ctx.set_option(_lib.OPT_COLOR_SPLIT, split)
+            ctx.set_option(_lib.OPT_DF_RESIDUAL, dfr)
+            x, info = ctx.solve(_lib.default_conf(solver=_lib.SOLVER_MIXED, tol=tol, maxiter=100))
+            rn, bn2 = ctx.residual_norms()
+            assert info.converged and rn / bn2 <= 1.01e-10, (split, dfr, rn / bn2)
+            # the solver's residual (updated) against b - A x in FP64
+            true_res = rn / math.sqrt(h ** 3)
+            assert abs(info.residual - true_res) <= 1e-2 * true_res, (split, dfr, info.residual,
+                                                                    true_res)
+            assert rel_l2(x, xt) <= 1e-9, (split, dfr)
+            out[(split, dfr)] = (x, info.iter, info.inner_iter)
+    for split in (1, 0):
+        a, b = out[(split, 1)], out[(split, 0)]
+        assert rel_l2(a[0], b[0]) < 1e-9, split
+        assert a[1] == b[1] and abs(a[2] - b[2]) <= max(3, 0.2 * b[2]), (split, a[1:], b[1:])
+    ctx.set_option(_lib.OPT_COLOR_SPLIT, 1)
+    ctx.set_option(_lib.OPT_DF_RESIDUAL, 2)
+
+
 @pytest.mark.parametrize("shape", [(30, 18, 22), (18, 18, 18), (26, 12, 14)])
 def test_ragged_grids_scalar_paths(shape):
     """Grids whose x size is not a multiple of 4 take the scalar kernels
