@@ -94,45 +94,69 @@ __global__ void KCouplingLo(int64_t n, const double* __restrict__ w, const float
     lo[c] = __double2float_rn(w[c] - (double)hi[c]);
 }
 
+// A normal float widened to FP64 by rearranging its bits (IEEE 754 binary32
+// to binary64: exponent rebiased by 1023 - 127, significand shifted by 29),
+// exact, with integer instructions; zero, subnormals, infinities and NaN
+// by the conversion instruction.
+__device__ __forceinline__ double WidenFloat(float f) {
+  const unsigned u = __float_as_uint(f);
+  const unsigned ex = (u >> 23) & 0xffu;
+  if (ex == 0u || ex == 0xffu) return (double)f;
+  const unsigned hi = (u & 0x80000000u) | ((ex + 896u) << 20) | ((u & 0x7fffffu) >> 3);
+  return __hiloint2double((int)hi, (int)(u << 29));
+}
+
 // x += s e (FP64, as the plain defect correction) and r -= s A e (df64),
 // with the norms of the new r and the stopping test of KResidual64
 // (count_iter); FIRST: r read as FP64 (the residual of the initial guess).
+// A CTA walks a contiguous chunk of rows (y neighbours then come from L1),
+// its threads the cells of a row; the grid is a few CTAs per SM, so the
+// grid reduction is paid once per several hundred cells of a thread.
 template <bool FIRST, bool SPLIT>
-__global__ void KCorrectDF(Dims d, PairCouplings W, const float* __restrict__ e, double* x,
-                           unsigned long long* rp, SolveScalars* s, RedBuf rb) {
+__global__ void __launch_bounds__(256) KCorrectDF(Dims d, PairCouplings W,
+                                                  const float* __restrict__ e, double* x,
+                                                  unsigned long long* rp, SolveScalars* s,
+                                                  RedBuf rb) {
   const double scale = s->tmp[1];
   const DF sc = SplitDouble(scale);
   DF rr = {0.f, 0.f};
   unsigned amax = 0;  // bits of the largest |r| so far (+0)
-  TILE_LOOP_BEGIN(d)
-  const int im = wrapm(i - 1, d.nx), ip = wrapp(i + 1, d.nx);
-  const int jm = wrapm(j - 1, d.ny), jp = wrapp(j + 1, d.ny);
-  const int km = wrapm(k - 1, d.nz), kp = wrapp(k + 1, d.nz);
-  const float ec = e[LevelIdx<SPLIT>(d, i, j, k)];
-  const float en[6] = {e[LevelIdx<SPLIT>(d, im, j, k)], e[LevelIdx<SPLIT>(d, ip, j, k)],
-                       e[LevelIdx<SPLIT>(d, i, jm, k)], e[LevelIdx<SPLIT>(d, i, jp, k)],
-                       e[LevelIdx<SPLIT>(d, i, j, km)], e[LevelIdx<SPLIT>(d, i, j, kp)]};
-  const int64_t cw[6] = {c, d.idx(ip, j, k), c, d.idx(i, jp, k), c, d.idx(i, j, kp)};
-  DF ae = {0.f, 0.f};
+  const int rows = d.ny * d.nz;
+  const int per = (rows + gridDim.x - 1) / gridDim.x;
+  const int rb0 = blockIdx.x * per, rb1 = min(rb0 + per, rows);
+  for (int row = rb0; row < rb1; ++row) {
+    const int j = row % d.ny, k = row / d.ny;
+    const int jm = wrapm(j - 1, d.ny), jp = wrapp(j + 1, d.ny);
+    const int km = wrapm(k - 1, d.nz), kp = wrapp(k + 1, d.nz);
+    for (int i = threadIdx.x; i < d.nx; i += blockDim.x) {
+      const int64_t c = (int64_t)row * d.nx + i;
+      const int im = wrapm(i - 1, d.nx), ip = wrapp(i + 1, d.nx);
+      const float ec = e[LevelIdx<SPLIT>(d, i, j, k)];
+      const float en[6] = {e[LevelIdx<SPLIT>(d, im, j, k)], e[LevelIdx<SPLIT>(d, ip, j, k)],
+                           e[LevelIdx<SPLIT>(d, i, jm, k)], e[LevelIdx<SPLIT>(d, i, jp, k)],
+                           e[LevelIdx<SPLIT>(d, i, j, km)], e[LevelIdx<SPLIT>(d, i, j, kp)]};
+      const int64_t cw[6] = {c, d.idx(ip, j, k), c, d.idx(i, jp, k), c, d.idx(i, j, kp)};
+      DF ae = {0.f, 0.f};
 #pragma unroll
-  for (int q = 0; q < 6; ++q) {
-    const DF w = {W.h[q >> 1][cw[q]], W.l[q >> 1][cw[q]]};
-    ae = DfAdd(ae, DfMul(w, TwoSum(en[q], -ec)));
+      for (int q = 0; q < 6; ++q) {
+        const DF w = {W.h[q >> 1][cw[q]], W.l[q >> 1][cw[q]]};
+        ae = DfAdd(ae, DfMul(w, TwoSum(en[q], -ec)));
+      }
+      const unsigned long long rv = rp[c];
+      const DF r0 = FIRST ? SplitDouble(__longlong_as_double((long long)rv)) : UnpackDF(rv);
+      const DF r1 = DfAdd(r0, DfNeg(DfMul(sc, ae)));
+      rp[c] = PackDF(r1);
+      x[c] += scale * WidenFloat(ec);
+      rr = DfAdd(rr, DfMul(r1, r1));
+      const unsigned ab = __float_as_uint(r1.h) & 0x7fffffffu;
+      if (ab <= 0x7f800000u && ab > amax) amax = ab;
+    }
   }
-  const unsigned long long rv = rp[c];
-  const DF r0 = FIRST ? SplitDouble(__longlong_as_double((long long)rv)) : UnpackDF(rv);
-  const DF r1 = DfAdd(r0, DfNeg(DfMul(sc, ae)));
-  rp[c] = PackDF(r1);
-  x[c] += scale * (double)ec;
-  rr = DfAdd(rr, DfMul(r1, r1));
-  const unsigned ab = __float_as_uint(r1.h) & 0x7fffffffu;
-  if (ab <= 0x7f800000u && ab > amax) amax = ab;
-  TILE_LOOP_END
   double v[3] = {(double)rr.h + (double)rr.l, (double)__uint_as_float(amax), 0.0};
   const int op[3] = {0, 1, 0};
   __shared__ double out[3];
   if (GridReduce<3>(v, op, rb, out)) {
-    if (threadIdx.x == 0 && threadIdx.y == 0) {
+    if (threadIdx.x == 0) {
       s->rr = out[0];
       s->maxr = out[1];
       const double res = s->maxnorm ? out[1] / s->cellvol : sqrt(out[0] / s->cellvol);

@@ -2436,7 +2436,8 @@ int SolveMixed(aphgpu_ctx* ctx, const aphgpu_conf* conf, aphgpu_info* info) {
                                   cudaMemcpyHostToDevice, st));
     if (df) {
       // x += s e and the next residual with its stopping test
-      const dim3 tg = TileGrid(ctx->d), tb = TileBlock();
+      const dim3 tg((unsigned)std::min<int64_t>((int64_t)d0.ny * d0.nz, 4 * SmCount(ctx))),
+          tb(256);
       if (outer == 1 && split)
         KCorrectDF<true, true><<<tg, tb, 0, st>>>(d0, W, ctx->x32, ctx->x, rp, ctx->scal, ctx->red);
       else if (outer == 1)
