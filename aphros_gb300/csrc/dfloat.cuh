@@ -109,9 +109,11 @@ __device__ __forceinline__ double WidenFloat(float f) {
 // x += s e (FP64, as the plain defect correction) and r -= s A e (df64),
 // with the norms of the new r and the stopping test of KResidual64
 // (count_iter); FIRST: r read as FP64 (the residual of the initial guess).
-// A CTA walks a contiguous chunk of rows (y neighbours then come from L1),
-// its threads the cells of a row; the grid is a few CTAs per SM, so the
-// grid reduction is paid once per several hundred cells of a thread.
+// CTAs walk the rows grid-stride (the rows in flight at one time are
+// consecutive, so their y and z neighbour rows are read by other CTAs at
+// about the same time and come from L2), threads the cells of a row (two
+// per iteration, their loads issued together); the grid is a few CTAs per
+// SM, so the grid reduction is paid once per several hundred cells.
 template <bool FIRST, bool SPLIT>
 __global__ void __launch_bounds__(256) KCorrectDF(Dims d, PairCouplings W,
                                                   const float* __restrict__ e, double* x,
@@ -122,12 +124,11 @@ __global__ void __launch_bounds__(256) KCorrectDF(Dims d, PairCouplings W,
   DF rr = {0.f, 0.f};
   unsigned amax = 0;  // bits of the largest |r| so far (+0)
   const int rows = d.ny * d.nz;
-  const int per = (rows + gridDim.x - 1) / gridDim.x;
-  const int rb0 = blockIdx.x * per, rb1 = min(rb0 + per, rows);
-  for (int row = rb0; row < rb1; ++row) {
+  for (int row = blockIdx.x; row < rows; row += gridDim.x) {
     const int j = row % d.ny, k = row / d.ny;
     const int jm = wrapm(j - 1, d.ny), jp = wrapp(j + 1, d.ny);
     const int km = wrapm(k - 1, d.nz), kp = wrapp(k + 1, d.nz);
+#pragma unroll 2
     for (int i = threadIdx.x; i < d.nx; i += blockDim.x) {
       const int64_t c = (int64_t)row * d.nx + i;
       const int im = wrapm(i - 1, d.nx), ip = wrapp(i + 1, d.nx);

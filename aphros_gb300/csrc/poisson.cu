@@ -2436,16 +2436,23 @@ int SolveMixed(aphgpu_ctx* ctx, const aphgpu_conf* conf, aphgpu_info* info) {
                                   cudaMemcpyHostToDevice, st));
     if (df) {
       // x += s e and the next residual with its stopping test
-      const dim3 tg((unsigned)std::min<int64_t>((int64_t)d0.ny * d0.nz, 4 * SmCount(ctx))),
-          tb(256);
+      // one CTA per resident slot (the rows are shared out grid-stride)
+      auto launch = [&](auto kernel) {
+        int per_sm = 0;
+        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, 256, 0) != cudaSuccess)
+          per_sm = 1;
+        const int64_t grid = std::min<int64_t>((int64_t)d0.ny * d0.nz,
+                                               (int64_t)std::max(per_sm, 1) * SmCount(ctx));
+        kernel<<<(unsigned)grid, 256, 0, st>>>(d0, W, ctx->x32, ctx->x, rp, ctx->scal, ctx->red);
+      };
       if (outer == 1 && split)
-        KCorrectDF<true, true><<<tg, tb, 0, st>>>(d0, W, ctx->x32, ctx->x, rp, ctx->scal, ctx->red);
+        launch(KCorrectDF<true, true>);
       else if (outer == 1)
-        KCorrectDF<true, false><<<tg, tb, 0, st>>>(d0, W, ctx->x32, ctx->x, rp, ctx->scal, ctx->red);
+        launch(KCorrectDF<true, false>);
       else if (split)
-        KCorrectDF<false, true><<<tg, tb, 0, st>>>(d0, W, ctx->x32, ctx->x, rp, ctx->scal, ctx->red);
+        launch(KCorrectDF<false, true>);
       else
-        KCorrectDF<false, false><<<tg, tb, 0, st>>>(d0, W, ctx->x32, ctx->x, rp, ctx->scal, ctx->red);
+        launch(KCorrectDF<false, false>);
     } else if (split) {
       KAddCorrectionSplit<<<rb, 256, 0, st>>>(d0, ctx->x, ctx->x32, ctx->scal);
     } else {
