@@ -29,6 +29,7 @@ OPT_CTA_COARSE = 6
 OPT_WAVE_PLANES = 7
 OPT_COLOR_SPLIT = 8
 OPT_DF_RESIDUAL = 9
+OPT_W_MIN_CELLS = 10
 FIELD_PRESSURE, FIELD_RHS, FIELD_VF, FIELD_CURVATURE = 0, 1, 2, 3
 DUMP_UINT16, DUMP_FLOAT32, DUMP_FLOAT64 = 0, 1, 2
 

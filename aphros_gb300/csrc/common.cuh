@@ -410,6 +410,7 @@ struct aphgpu_ctx {
   int use_df = 2;  // double-float outer residual update: 0 off, 1 on, 2 from 2^21 cells
   bool use_half = false;   // FP16 couplings for the finest-level smoother
   int mg_gamma = 0;        // cycles of each level below the finest (1 V, 2 W, 0 auto)
+  int64_t mg_wmin = 4096; // W-cycles: levels of at most so many cells visit their child once
   int mg_series_pct = 60;  // weight (%) of the series couplings in the coarse operators
   int mg_growth = 0;       // sweeps below the finest level (1 same, 2 linear, 3 doubling, 0 auto)
   bool use_cta_coarse = true;  // smallest FP32 levels cycled by one CTA

@@ -1924,7 +1924,9 @@ int CycleLevel(aphgpu_ctx* ctx, std::vector<Level<T>>& lv, int l, bool first, in
   }
   LaunchRestrict<T>(ctx, f, lv[l + 1], A, s);
   APH_LAUNCHED(ctx);
-  const int gamma = l == 0 ? 1 : CycleGamma(ctx);
+  // (a W-cycle's small levels visit theirs once: below 16^3 cells the
+  // extra visits cost launches and one-CTA cycles, and buy no iterations)
+  const int gamma = (l == 0 || f.d.cells() <= ctx->mg_wmin) ? 1 : CycleGamma(ctx);
   for (int g = 0; g < gamma; ++g) APH_TRY(CycleLevel<T>(ctx, lv, l + 1, g == 0, pre, post, s));
   // an odd number of pipelined post-sweeps starts from f.r, written by the
   // prolongation, and ends in f.x without a copy
@@ -2018,6 +2020,7 @@ int Pcg(aphgpu_ctx* ctx, const Op<T>& A, Precond precond, T* x, T* r, T* p,
     key = Mix(key, (uint64_t)ctx->wave_planes);
     key = Mix(key, (uint64_t)CycleGamma(ctx));
     key = Mix(key, (uint64_t)SweepGrowth(ctx));
+    key = Mix(key, (uint64_t)ctx->mg_wmin);
     key = Mix(key, (uint64_t)(ctx->use_cta_coarse ? 1 + ctx->mg.clc : 0));
     key = Mix(key, (uint64_t)(!ctx->mg.l32.empty() && ctx->mg.l32[0].split));
     // the FP16 coupling scale is a kernel argument: part of the key

@@ -523,6 +523,36 @@ def test_double_float_residual_update(shape):
     ctx.set_option(_lib.OPT_DF_RESIDUAL, 2)
 
 
+@pytest.mark.parametrize("solver", [_lib.SOLVER_MIXED, _lib.SOLVER_MGPCG])
+def test_w_cycle_floor(solver):
+    """W-cycles whose small levels visit the level below once
+    (APHGPU_OPT_W_MIN_CELLS: none, 16^3 = the default, 32^3) reach the
+    1e-10 stop with the pressure of the tight FP64 solution within the
+    1e-9 bar, with CUDA graphs (the floor is part of the graph's key)."""
+    n = 128
+    h = 1.0 / n
+    c, r = workload.place_spheres(51, 5, 0.08, 0.18, gap=0.02)
+    ctx = _lib.Context(n, h)
+    ctx.assemble_projection(workload.alpha_spheres(n, c, r), 1.0, 1e-3,
+                            workload.tg_flux(n, seed=17), 1e-3)
+    _, bn = ctx.residual_norms()
+    tol = 1e-10 * bn / math.sqrt(h ** 3)
+    ctx.solve(_lib.default_conf(solver=_lib.SOLVER_MGPCG, tol=1e-3 * tol, maxiter=300))
+    xt = ctx.get_solution()
+    ctx.set_option(_lib.OPT_CYCLE, 2)
+    its = {}
+    for wmin in (0, 4096, 32768, 4096):
+        ctx.set_option(_lib.OPT_W_MIN_CELLS, wmin)
+        x, info = ctx.solve(_lib.default_conf(solver=solver, tol=tol, maxiter=300))
+        rn, bn2 = ctx.residual_norms()
+        assert info.converged and rn / bn2 <= 1.01e-10, wmin
+        assert rel_l2(x, xt) <= 1e-9, wmin
+        key = (wmin, info.iter, info.inner_iter)
+        its.setdefault(wmin, key)
+        assert its[wmin] == key  # the same graph key rebuilt gives the same solve
+    ctx.set_option(_lib.OPT_CYCLE, 0)
+
+
 @pytest.mark.parametrize("shape", [(30, 18, 22), (18, 18, 18), (26, 12, 14)])
 def test_ragged_grids_scalar_paths(shape):
     """Grids whose x size is not a multiple of 4 take the scalar kernels
