@@ -407,7 +407,7 @@ struct aphgpu_ctx {
   int fused_mode = 0;
   int wave_planes = 0;  // planes per step of the wavefront sweep (0: sized to L2)
   bool use_split = true;  // colour-split finest level in the mixed solver
-  int use_df = 2;  // double-float outer residual update: 0 off, 1 on, 2 from 2^21 cells
+  int use_df = 2;  // double-float outer residual update: 0 off, 1 on, 2 from 2^22 cells
   bool use_half = false;   // FP16 couplings for the finest-level smoother
   int mg_gamma = 0;        // cycles of each level below the finest (1 V, 2 W, 0 auto)
   int64_t mg_wmin = 4096; // W-cycles: levels of at most so many cells visit their child once

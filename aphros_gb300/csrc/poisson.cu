@@ -2365,7 +2365,7 @@ int SolveMixed(aphgpu_ctx* ctx, const aphgpu_conf* conf, aphgpu_info* info) {
   // after the first outer iteration the residual is updated (r -= s A e)
   // in double-float arithmetic (dfloat.cuh) for flux-difference systems
   const bool df = ctx->singular &&
-                  (ctx->use_df == 1 || (ctx->use_df == 2 && N >= ((int64_t)1 << 21)));
+                  (ctx->use_df == 1 || (ctx->use_df == 2 && N >= ((int64_t)1 << 22)));
   if (df && !mg.wlo_ready) {
     for (int q = 0; q < 3; ++q) {
       if (!mg.wlo[q]) APH_TRY(Alloc(ctx, &mg.wlo[q], N));

@@ -451,14 +451,14 @@ def measure_vof(ctx, case, peak, peak_kind, steps, cpu=True):
 
 # ---------------------------------------------------------------------------
 # The headline solve runs the library defaults: a W-cycle below the finest
-# level from 256^3 cells up, 2 pre- and 2 post-smoothing red-black sweeps
+# level from 256^3 cells up (its levels of at most 16^3 cells visiting the
+# level below once), 2 pre- and 2 post-smoothing red-black sweeps
 # on every level (the levels of at most 8^3 cells cycled by one CTA per
 # visit, the finest FP32 level in the colour-split order), inner FP32 PCG
 # to 3e-4, the outer residual after the first updated in double-float
 # arithmetic, stopped at ||r||/||b|| <= 1e-10.  Measured at 512^3 it is the
 # fastest configuration whose pressure is within the 1e-9 bar of a tight
-# FP64 solution (8.5e-10; 5.7e-10 with the natural order and the FP64
-# residual, whose stops fall at slightly smaller residuals) at that stop.  The
+# FP64 solution (4.9e-10) at that stop.  The
 # configuration's literal cycle (V, 2+2 sweeps on every level) and the
 # fastest V-cycle (one sweep before and after on the finest level, 2^l on
 # level l below it, inner PCG to 1e-3, which keeps its pressure within the

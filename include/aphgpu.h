@@ -536,9 +536,10 @@ int aphgpu_batch_last_ms(const aphgpu_batch* batch, double* ms, int64_t* launche
  *                            pipe, with the correction x += s e in FP64;
  *                            the first residual is computed in FP64.  It
  *                            holds the couplings' FP32 low parts (12
- *                            bytes per cell).  2 (default): so from 2^21
- *                            cells up, where the FP64 residual's time
- *                            matters; 0: every outer residual b - A x in
+ *                            bytes per cell, made again after each new
+ *                            system).  2 (default): so from 2^22 cells up,
+ *                            where the FP64 residual's time outweighs
+ *                            that; 0: every outer residual b - A x in
  *                            FP64
  *   APHGPU_OPT_W_MIN_CELLS   with W-cycles: a level of at most this many
  *                            cells visits the level below it once (a V
