@@ -859,7 +859,10 @@ int aphgpu_set_option(aphgpu_ctx* ctx, int option, int value) {
       ctx->mg_gamma = value;
       return APHGPU_OK;
     case APHGPU_OPT_CTA_COARSE: ctx->use_cta_coarse = value != 0; return APHGPU_OK;
-    case APHGPU_OPT_COLOR_SPLIT: ctx->use_split = value != 0; return APHGPU_OK;
+    case APHGPU_OPT_COLOR_SPLIT:
+      if (value < 0 || value > 2) return SetError(ctx, APHGPU_ERR_ARG, "colour split must be 0..2");
+      ctx->use_split = value;
+      return APHGPU_OK;
     case APHGPU_OPT_W_MIN_CELLS:
       if (value < 0) return SetError(ctx, APHGPU_ERR_ARG, "W-cycle floor must be >= 0");
       ctx->mg_wmin = value;

@@ -406,7 +406,7 @@ struct aphgpu_ctx {
   // kernel on every level it supports
   int fused_mode = 0;
   int wave_planes = 0;  // planes per step of the wavefront sweep (0: sized to L2)
-  bool use_split = true;  // colour-split finest level in the mixed solver
+  int use_split = 2;  // colour-split finest level (mixed solver): 0 off, 1 on, 2 from 2^22 cells
   int use_df = 2;  // double-float outer residual update: 0 off, 1 on, 2 from 2^22 cells
   bool use_half = false;   // FP16 couplings for the finest-level smoother
   int mg_gamma = 0;        // cycles of each level below the finest (1 V, 2 W, 0 auto)

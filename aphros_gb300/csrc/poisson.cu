@@ -2357,7 +2357,8 @@ int SolveMixed(aphgpu_ctx* ctx, const aphgpu_conf* conf, aphgpu_info* info) {
   // plain red-black smoother runs on it (no fused sweeps, no FP16
   // couplings) and the grid allows it
   const Dims d0 = lv[0].d;
-  lv[0].split = ctx->use_split && ctx->fused_mode == 0 && !(lv[0].wh[0] && lv[0].hscale > 0.f) &&
+  lv[0].split = (ctx->use_split == 1 || (ctx->use_split == 2 && N >= ((int64_t)1 << 22))) &&
+                ctx->fused_mode == 0 && !(lv[0].wh[0] && lv[0].hscale > 0.f) &&
                 d0.nx % 8 == 0 && d0.nx >= 16 && d0.ny % 2 == 0 && d0.nz % 2 == 0 &&
                 lv.size() >= 2;
   const bool split = lv[0].split;

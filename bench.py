@@ -478,11 +478,12 @@ HALF_SWEEP_BYTES = 12.0
 
 def color_split_used(shape):
     """Whether the mixed solver keeps its finest FP32 level in the
-    colour-split order (the library default, taken when nx % 8 == 0 and ny,
-    nz are even): the half sweep then moves 18 of the 24 bytes per cell of
-    the natural order's."""
+    colour-split order (the library default, taken from 2^22 cells up when
+    nx % 8 == 0 and ny, nz are even): the half sweep then moves 18 of the 24
+    bytes per cell of the natural order's."""
     nx, ny, nz = (shape,) * 3 if isinstance(shape, int) else shape
-    return nx % 8 == 0 and nx >= 16 and ny % 2 == 0 and nz % 2 == 0
+    return (nx % 8 == 0 and nx >= 16 and ny % 2 == 0 and nz % 2 == 0 and
+            nx * ny * nz >= 1 << 22)
 
 
 def set_v_cycle(ctx, _lib):

@@ -515,7 +515,7 @@ int aphgpu_batch_last_ms(const aphgpu_batch* batch, double* ms, int64_t* launche
  *                            (APHGPU_OPT_FUSED_SWEEPS 5 and 6); 0 (default):
  *                            as many as let three steps' worth of a level's
  *                            x, b and couplings fit in 60 MB of L2
- *   APHGPU_OPT_COLOR_SPLIT   1 (default): the mixed solver keeps its finest
+ *   APHGPU_OPT_COLOR_SPLIT   1: the mixed solver keeps its finest
  *                            FP32 level (the right-hand side, the iterate
  *                            and the inner CG vectors) with each row's two
  *                            red-black colours in separate halves, so that
@@ -526,7 +526,11 @@ int aphgpu_batch_last_ms(const aphgpu_batch* batch, double* ms, int64_t* launche
  *                            APHGPU_OPT_HALF_COUPLINGS is off.  Same
  *                            smoothing, restriction and prolongation
  *                            values; the inner CG's FP32 dot products sum
- *                            in another order.  0: natural order
+ *                            in another order.  2 (default): so from
+ *                            2^22 cells up (on smaller grids the split
+ *                            kernels' 8 cells per thread leave too few
+ *                            threads: the served 32^3-128^3 simulations
+ *                            ran 10 % slower); 0: natural order
  *   APHGPU_OPT_DF_RESIDUAL   1: for flux-difference systems (every
  *                            diagonal minus the sum of its row's
  *                            couplings) the mixed solver updates its outer

@@ -471,7 +471,7 @@ def test_color_split_finest_level(cycle, shape):
     # graphs do not change the split path's results
     assert np.array_equal(out[(1, 1)][0], out[(1, 0)][0])
     assert out[(1, 1)][1:] == out[(1, 0)][1:]
-    ctx.set_option(_lib.OPT_COLOR_SPLIT, 1)
+    ctx.set_option(_lib.OPT_COLOR_SPLIT, 2)
 
 
 @pytest.mark.parametrize("shape", [(128, 128, 128), (96, 48, 40), (36, 24, 20), (30, 18, 22)])
@@ -519,7 +519,7 @@ def test_double_float_residual_update(shape):
         a, b = out[(split, 1)], out[(split, 0)]
         assert rel_l2(a[0], b[0]) < 1e-9, split
         assert a[1] == b[1] and abs(a[2] - b[2]) <= max(3, 0.2 * b[2]), (split, a[1:], b[1:])
-    ctx.set_option(_lib.OPT_COLOR_SPLIT, 1)
+    ctx.set_option(_lib.OPT_COLOR_SPLIT, 2)
     ctx.set_option(_lib.OPT_DF_RESIDUAL, 2)
 
 
